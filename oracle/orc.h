@@ -1,0 +1,89 @@
+/*
+ * Oracle: CPU restatement of the QPMS mode-problem hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product library (qpms_gb300/) links,
+ * loads or calls this code; only the tests, the smoke check and the CPU
+ * baseline leg of bench.py do, and there only as the checker.
+ *
+ * Every function restates one function of the reference (kostyfisik/qpms) and
+ * cites the reference file:line it follows.  The reference's third-party
+ * numerics (GSL special functions, AMOS complex Bessel, GSL 3j) are replaced
+ * by self-written equivalents from the mathematics; each is pinned in the
+ * CPU tests against mpmath / sympy, and the Gaunt coefficients against the
+ * reference's own gaunt.c compiled from its sources (oracle/_ref).
+ *
+ * Prefix: orc_.  Complex numbers are C99 `double complex`, which has the
+ * same layout as the reference's `complex double` and numpy complex128.
+ */
+#ifndef QPMS_ORACLE_H
+#define QPMS_ORACLE_H
+#include <complex.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- special functions (orc_specfunc.c) ---- */
+
+/* Wigner 3j symbol with integer arguments (replaces gsl_sf_coupling_3j with
+ * doubled arguments, translations.c:375-376).  Racah formula in long double. */
+double orc_wigner3j(int j1, int j2, int j3, int m1, int m2, int m3);
+
+/* Gaunt coefficients a_q(m,n,mu,nu), q = 0..qmax, of the product expansion
+ * P_n^m P_nu^mu = sum_q a_q P_{n+nu-2q}^{m+mu} (replaces gaunt_xu, gaunt.c:396).
+ * Returns qmax = gaunt_q_max(m,n,mu,nu) (gaunt.h:6-8). */
+int orc_gaunt(int m, int n, int mu, int nu, double *aq);
+int orc_gaunt_q_max(int m, int n, int mu, int nu);
+
+/* Unnormalised associated Legendre P_l^m(x), 0<=m<=l<=L, in GSL layout
+ * l(l+1)/2+m, with Condon-Shortley factor csphase^m (replaces
+ * gsl_sf_legendre_array_e(GSL_SF_LEGENDRE_NONE, ...), translations.c:651-653). */
+void orc_legendre_array(int L, double x, double csphase, double *out);
+
+/* Spherical Bessel functions z_l(x), l = 0..lmax, of kind J
+ * (1 = j, 2 = y, 3 = h+, 4 = h-).  Follows qpms_sph_bessel_fill
+ * (bessel.c:86-147, :52-83): real x and complex x branches. */
+int orc_sph_bessel_fill(int J, int lmax, double complex x, double complex *res);
+
+/* ---- translation operator (orc_trans.c) ---- */
+
+typedef struct orc_trans_calculator {
+  int normalisation;            /* qpms_normalisation_t bits */
+  int lMax;
+  int nelem;                    /* lMax (lMax + 2) */
+  double complex **A_multipliers; /* nelem^2 + 1 pointers into one block */
+  double complex **B_multipliers;
+} orc_trans_calculator;
+
+/* translations.c:439-508 */
+orc_trans_calculator *orc_trans_calculator_init(int lMax, int normalisation);
+void orc_trans_calculator_free(orc_trans_calculator *c);
+/* Total number of A / B multipliers (ragged table sizes). */
+size_t orc_trans_calculator_nA(const orc_trans_calculator *c);
+size_t orc_trans_calculator_nB(const orc_trans_calculator *c);
+
+/* translations.c:610-698, 1124-1132 (the _ext form, kd = (r, theta, phi)). */
+int orc_trans_calculator_get_AB_arrays_ext(const orc_trans_calculator *c,
+    double complex *Adest, double complex *Bdest,
+    size_t deststride, size_t srcstride,
+    double complex kdlj_r, double kdlj_theta, double kdlj_phi,
+    int r_ge_d, int J);
+
+/* Batched loop over n vectors (the numpy loop of translations_python.c:24-132,
+ * extended to complex kr): A,B at [i][nelem][nelem]. */
+int orc_trans_AB_batch(const orc_trans_calculator *c, size_t n,
+    const double complex *kr, const double *theta, const double *phi,
+    int J, double complex *A, double complex *B);
+
+/* Closed-form single coefficients (translations.c:135-286), used by the
+ * single-vs-array property test (tests/single_translations_vs_calc.c). */
+double complex orc_trans_single_A(int norm, int m, int n, int mu, int nu,
+    double complex kr, double theta, double phi, int r_ge_d, int J);
+double complex orc_trans_single_B(int norm, int m, int n, int mu, int nu,
+    double complex kr, double theta, double phi, int r_ge_d, int J);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

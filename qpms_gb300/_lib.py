@@ -1,0 +1,65 @@
+"""Loader of the in-tree libqpms_gb300.so (the CUDA implementation).
+
+There is no CPU fallback: if the library is missing or cannot be loaded, every
+entry point raises.  ``build()`` compiles it in place (nvcc, sm_103a).
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libqpms_gb300.so")
+
+_lib = None
+
+
+class QpmsGpuError(RuntimeError):
+    pass
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise QpmsGpuError("libqpms_gb300.so is not built (run qpms_gb300.build.build())")
+        _lib = C.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def last_error():
+    return lib().qpms_gpu_last_error().decode(errors="replace")
+
+
+def check(rc, what):
+    if rc != 0:
+        raise QpmsGpuError("%s failed (code %d): %s" % (what, rc, last_error()))
+
+
+def _declare(L):
+    vp, sz, ci, cd = C.c_void_p, C.c_size_t, C.c_int, C.c_double
+    L.qpms_gpu_last_error.restype = C.c_char_p
+    L.qpms_gpu_last_error.argtypes = []
+    L.qpms_gpu_kernel_launch_count.restype = C.c_ulonglong
+    L.qpms_gpu_kernel_launch_count.argtypes = []
+    L.qpms_trans_calculator_init.restype = vp
+    L.qpms_trans_calculator_init.argtypes = [ci, ci]
+    L.qpms_trans_calculator_free.restype = None
+    L.qpms_trans_calculator_free.argtypes = [vp]
+    L.qpms_gpu_trans_calculator_n_multipliers.restype = sz
+    L.qpms_gpu_trans_calculator_n_multipliers.argtypes = [vp, ci]
+    L.qpms_gpu_trans_AB_arrays_batch.restype = ci
+    L.qpms_gpu_trans_AB_arrays_batch.argtypes = [vp, sz, vp, vp, vp, vp, ci, vp, vp, vp]
+    L.qpms_gpu_trans_AB_arrays_batch_host.restype = ci
+    L.qpms_gpu_trans_AB_arrays_batch_host.argtypes = [vp, sz, vp, vp, vp, vp, ci, vp, vp]
+    L.qpms_gpu_trans_multipliers_export.restype = ci
+    L.qpms_gpu_trans_multipliers_export.argtypes = [ci, ci, vp, vp, vp, vp]
+    L.qpms_gpu_measure_fp64_peak.restype = ci
+    L.qpms_gpu_measure_fp64_peak.argtypes = [vp]
+    # complex by value is passed as two doubles (same registers on x86-64 and aarch64)
+    L.qpms_trans_calculator_get_AB_arrays_ext.restype = ci
+    L.qpms_trans_calculator_get_AB_arrays_ext.argtypes = [vp, vp, vp, sz, sz, cd, cd, cd, cd, ci, ci]
+    try:
+        from . import _lib_more
+        _lib_more.declare(L)
+    except ImportError:
+        pass
