@@ -16,6 +16,7 @@
 
 #include <stddef.h>
 #include <stdbool.h>
+#include <stdint.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -121,6 +122,167 @@ size_t qpms_gpu_trans_calculator_n_multipliers(const qpms_trans_calculator *c, i
  * *nA, *nB: capacity on input, table size on output; NULL outputs query sizes. */
 int qpms_gpu_trans_multipliers_export(qpms_l_t lMax, qpms_normalisation_t nt,
     qpms_complex_t *A_out, size_t *nA, qpms_complex_t *B_out, size_t *nB);
+
+
+/* ---------------- scattering systems (scatsystem.h of the reference) ----------------
+ * Struct layouts are field-for-field those of the reference (qpms_types.h,
+ * scatsystem.h, materials.h), so objects built by the reference's own
+ * constructors can be passed to the drop-in functions below.  Members the hot
+ * path never reads (symmetry orbits, irrep bases, generator tables) are kept as
+ * opaque pointers of the same size. */
+typedef struct cart3_t { double x, y, z; } cart3_t;                 /* qpms_types.h:186-189 */
+typedef unsigned long long qpms_uvswfi_t;                            /* qpms_types.h:81 */
+typedef int qpms_iri_t;                                              /* qpms_types.h:323 */
+typedef int32_t qpms_ss_tmi_t, qpms_ss_tmgi_t, qpms_ss_pi_t;         /* qpms_types.h:310-316 */
+
+typedef struct qpms_vswf_set_spec_t {                                /* qpms_types.h:290-308 */
+  size_t n;
+  qpms_uvswfi_t *ilist;
+  qpms_l_t lMax, lMax_M, lMax_N, lMax_L;
+  size_t capacity;
+  qpms_normalisation_t norm;
+} qpms_vswf_set_spec_t;
+
+typedef struct qpms_tmatrix_t {                                      /* qpms_types.h:338-351 */
+  const qpms_vswf_set_spec_t *spec;
+  qpms_complex_t *m;  /* row-major spec->n x spec->n */
+  bool owns_m;
+} qpms_tmatrix_t;
+
+typedef struct qpms_epsmu_t { qpms_complex_t eps, mu; } qpms_epsmu_t; /* qpms_types.h:422-425 */
+
+typedef struct qpms_epsmu_generator_t {                              /* materials.h:16-25 */
+  qpms_epsmu_t (*function)(qpms_complex_t omega, const void *params);
+  const void *params;
+} qpms_epsmu_generator_t;
+
+typedef struct qpms_particle_tid_t {                                 /* scatsystem.h:36-40 */
+  cart3_t pos;
+  qpms_ss_tmi_t tmatrix_id;
+} qpms_particle_tid_t;
+
+typedef struct qpms_scatsys_periodic_info_t {                        /* scatsystem.h:135-158 */
+  cart3_t lattice_basis[3];
+  cart3_t reciprocal_basis[3];
+  double unitcell_volume;
+  double eta;
+} qpms_scatsys_periodic_info_t;
+
+typedef struct qpms_scatsys_t {                                      /* scatsystem.h:169-227 */
+  int lattice_dimension;
+  qpms_epsmu_generator_t medium;
+  void *tmg;                    /* qpms_tmatrix_function_t * */
+  qpms_ss_tmgi_t tmg_count;
+  void *tm;                     /* qpms_ss_derived_tmatrix_t * */
+  qpms_ss_tmi_t tm_count;
+  qpms_ss_tmi_t tm_capacity;
+  qpms_particle_tid_t *p;
+  qpms_ss_pi_t p_count;
+  qpms_ss_pi_t p_capacity;
+  const void *sym;              /* const struct qpms_finite_group_t * */
+  qpms_ss_pi_t *p_sym_map;
+  qpms_ss_tmi_t *tm_sym_map;
+  int32_t orbit_type_count;     /* qpms_ss_oti_t */
+  void *orbit_types;
+  void *p_orbitinfo;
+  size_t fecv_size;
+  size_t *saecv_sizes;
+  size_t *fecv_pstarts;
+  size_t *saecv_ot_offsets;
+  size_t max_bspecn;
+  qpms_ss_pi_t *p_by_orbit;
+  char *otspace;
+  char *otspace_end;
+  double lenscale;
+  struct qpms_trans_calculator *c;
+  qpms_scatsys_periodic_info_t per;
+} qpms_scatsys_t;
+
+typedef struct qpms_scatsys_at_omega_t {                             /* scatsystem.h:239-249 */
+  const qpms_scatsys_t *ss;
+  qpms_tmatrix_t **tm;
+  qpms_complex_t omega;
+  qpms_epsmu_t medium;
+  qpms_complex_t wavenumber;
+} qpms_scatsys_at_omega_t;
+
+typedef struct qpms_scatsys_at_omega_k_t {                           /* scatsystem.h:488-492 */
+  const qpms_scatsys_at_omega_t *ssw;
+  double k[3];
+  double eta;
+} qpms_scatsys_at_omega_k_t;
+
+typedef struct qpms_ss_LU {                                          /* scatsystem.h:432-441 */
+  const qpms_scatsys_at_omega_t *ssw;
+  const qpms_scatsys_at_omega_k_t *sswk;
+  bool full;
+  qpms_iri_t iri;
+  qpms_complex_t *a;
+  int *ipiv;
+} qpms_ss_LU;
+
+/* -- constructors of this library (the reference builds systems through its
+ *    symmetry machinery, scatsystem.c:233-604, which is outside the hot path) -- */
+
+/* Finite system of spheres with constant permittivities (Mie T-matrices,
+ * tmatrices.c:580-606) in a constant medium; bspec from lMax (vswf.c:76-92).
+ * kind[i] in [0, nkinds) selects radius[kind] and eps_inside[kind]. */
+qpms_scatsys_t *qpms_gpu_scatsys_create_spheres(int np, const double *pos_xyz, const int *kind,
+    int nkinds, const double *radius, const qpms_complex_t *eps_inside,
+    qpms_complex_t eps_medium, qpms_l_t lMax);
+void qpms_gpu_scatsys_free(qpms_scatsys_t *ss);
+
+/* Evaluates the medium and the T-matrices at omega, like qpms_scatsys_at_omega
+ * (scatsystem.c:606-630). */
+qpms_scatsys_at_omega_t *qpms_gpu_scatsys_at_omega(const qpms_scatsys_t *ss, qpms_complex_t omega);
+void qpms_gpu_scatsys_at_omega_free(qpms_scatsys_at_omega_t *ssw);
+
+/* -- drop-in replacements of the reference's hot-path functions -- */
+
+/* Replaces qpms_scatsysw_build_modeproblem_matrix_full (scatsystem.h:368-372,
+ * scatsystem.c:1345-1350): M = I - T S on the GPU (finite systems: S(R<-R) = 0,
+ * the intended semantics of scatsystem.c:1283-1343).  target: host buffer of
+ * fecv_size^2 (NULL -> malloc, caller frees). Returns target, NULL on error. */
+qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_full(qpms_complex_t *target,
+    const qpms_scatsys_at_omega_t *ssw);
+
+/* Replaces qpms_scatsys_build_translation_matrix_e_full (scatsystem.h:357-363,
+ * scatsystem.c:1180-1217): S(R<-C) of kind J for R != C, zero diagonal blocks. */
+qpms_complex_t *qpms_scatsys_build_translation_matrix_e_full(qpms_complex_t *target,
+    const qpms_scatsys_t *ss, qpms_complex_t k, qpms_bessel_t J);
+
+/* Replace qpms_scatsysw_modeproblem_matrix_full_factorise / _build_..._LU /
+ * qpms_scatsys_scatter_solve / qpms_ss_LU_free (scatsystem.h:442-480,
+ * scatsystem.c:2202-2273): LU with partial pivoting (zgetrf semantics,
+ * row-major, 0-based ipiv) computed on the GPU; solve on the GPU. */
+qpms_ss_LU qpms_scatsysw_modeproblem_matrix_full_factorise(qpms_complex_t *mpmatrix_full,
+    int *target_piv, const qpms_scatsys_at_omega_t *ssw, const qpms_scatsys_at_omega_k_t *sswk);
+qpms_ss_LU qpms_scatsysw_build_modeproblem_matrix_full_LU(qpms_complex_t *target,
+    int *target_piv, const qpms_scatsys_at_omega_t *ssw);
+qpms_complex_t *qpms_scatsys_scatter_solve(qpms_complex_t *f, const qpms_complex_t *a_inc,
+    qpms_ss_LU lu);
+void qpms_ss_LU_free(qpms_ss_LU lu);
+
+/* Replaces qpms_scatsysw_apply_Tmatrices_full (scatsystem.h:621-630,
+ * scatsystem.c:1996-2011): target = T a per particle. */
+qpms_complex_t *qpms_scatsysw_apply_Tmatrices_full(qpms_complex_t *target_full,
+    const qpms_complex_t *inc_full, const qpms_scatsys_at_omega_t *ssw);
+
+/* Plane-wave incident vector (qpms_scatsys_incident_field_vector_full with
+ * qpms_incfield_planewave, scatsystem.c:1970-1983, vswf.c:480-530), real k. */
+int qpms_gpu_incident_planewave_full(qpms_complex_t *target_full, const qpms_scatsys_t *ss,
+    const double k_cart[3], const qpms_complex_t E_cart[3]);
+
+/* Batched plane-wave scattering over frequencies (the loop of
+ * misc/finiterectlat-scatter.py:70-111 on the full system): for each omega,
+ * assemble M = I - T S, a = plane wave, solve M f = T a, sigma_ext =
+ * -Re(a^H f)/k^2.  mode 0: plain FP64 (LU in complex128);  mode 1: LU in
+ * complex64 with FP64 iterative refinement to the FP64 residual.
+ * f_out (nw x fecv, host) may be NULL; resid_out[i] = ||M f - T a|| / ||T a||
+ * (FP64); iters_out[i] = refinement steps (0 in mode 0).  Synchronous. */
+int qpms_gpu_finite_planewave_scatter(const qpms_scatsys_t *ss, size_t nw,
+    const double *omegas, const double k_dir[3], const qpms_complex_t E_cart[3], int mode,
+    qpms_complex_t *f_out, double *sigma_ext, double *resid_out, int *iters_out);
 
 /* ---------------- diagnostics ---------------- */
 /* Thread-local message of the last failing call (empty string if none). */

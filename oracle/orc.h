@@ -83,6 +83,26 @@ double complex orc_trans_single_A(int norm, int m, int n, int mu, int nu,
 double complex orc_trans_single_B(int norm, int m, int n, int mu, int nu,
     double complex kr, double theta, double phi, int r_ge_d, int J);
 
+/* ---- finite scattering system (orc_scatsys.c) ---- */
+void orc_mie_coefficients(int lMax, double a, double complex k_i, double complex k_e,
+                          double complex mu_i, double complex mu_e, int J_ext, int J_scat,
+                          double complex *RV, double complex *RH);
+void orc_tmatrix_sphere_diag(int lMax, double radius, double complex omega, double complex eps_i,
+                             double complex eps_e, double complex *Tdiag);
+void orc_planewave_full(int lMax, int np, const double *pos, const double k_cart[3],
+                        const double complex E_cart[3], double complex *out);
+int orc_finite_modeproblem(const orc_trans_calculator *c, int np, const double *pos,
+                           const double complex *T, double complex k, double complex *M);
+int orc_finite_translation_matrix(const orc_trans_calculator *c, int np, const double *pos,
+                                  double complex k, int J, double complex *S_out);
+int orc_lu_factor(size_t n, double complex *a, int *ipiv);
+void orc_lu_solve(size_t n, const double complex *a, const int *ipiv, double complex *b, size_t nrhs);
+int orc_finite_sphere_scatter(const orc_trans_calculator *c, int np, const double *pos, double radius,
+                              double complex eps_i, double complex eps_e, double omega,
+                              const double k_dir[3], const double complex E_cart[3],
+                              double complex *f_out, double complex *a_out, double *sigma_ext,
+                              double complex *M_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -54,6 +54,7 @@ def _declare(L):
         f.argtypes = [C.c_int] * 5 + [C.c_double] * 4 + [C.c_int, C.c_int, vp]
     L.orc_num_threads.restype = C.c_int
     L.orc_num_threads.argtypes = []
+    _declare_scatsys(L)
 
 
 def num_threads():
@@ -154,3 +155,101 @@ def trans_single(which, norm, m, n, mu, nu, kr, theta, phi, r_ge_d, J):
     f(norm, m, n, mu, nu, kr.real, kr.imag, float(theta), float(phi), int(r_ge_d), int(J),
       out.ctypes.data)
     return out[0]
+
+
+def _declare_scatsys(L):
+    vp, ci, cd, sz = C.c_void_p, C.c_int, C.c_double, C.c_size_t
+    L.orc_tmatrix_sphere_diag_ri.restype = None
+    L.orc_tmatrix_sphere_diag_ri.argtypes = [ci, cd, cd, cd, cd, cd, cd, cd, vp]
+    L.orc_finite_modeproblem_ri.restype = ci
+    L.orc_finite_modeproblem_ri.argtypes = [vp, ci, vp, vp, cd, cd, vp]
+    L.orc_finite_translation_matrix_ri.restype = ci
+    L.orc_finite_translation_matrix_ri.argtypes = [vp, ci, vp, cd, cd, ci, vp]
+    L.orc_finite_sphere_scatter_ri.restype = ci
+    L.orc_finite_sphere_scatter_ri.argtypes = [vp, ci, vp, cd, cd, cd, cd, cd, cd, vp, vp, vp, vp, vp, vp]
+    L.orc_planewave_full.restype = None
+    L.orc_planewave_full.argtypes = [ci, ci, vp, vp, vp, vp]
+    L.orc_lu_factor.restype = ci
+    L.orc_lu_factor.argtypes = [sz, vp, vp]
+    L.orc_lu_solve.restype = None
+    L.orc_lu_solve.argtypes = [sz, vp, vp, vp, sz]
+
+
+C0 = 299792458.0
+
+
+def tmatrix_sphere_diag(lMax, radius, omega, eps_i, eps_e):
+    L = lib()
+    out = np.zeros(2 * lMax * (lMax + 2), dtype=np.complex128)
+    om, ei, ee = complex(omega), complex(eps_i), complex(eps_e)
+    L.orc_tmatrix_sphere_diag_ri(lMax, radius, om.real, om.imag, ei.real, ei.imag, ee.real, ee.imag,
+                                 out.ctypes.data)
+    return out
+
+
+def finite_modeproblem(calc, pos, T, k):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.complex128)
+    np_ = pos.shape[0]
+    N = np_ * 2 * calc.nelem
+    M = np.empty((N, N), dtype=np.complex128)
+    k = complex(k)
+    lib().orc_finite_modeproblem_ri(calc.ptr, np_, pos.ctypes.data, T.ctypes.data, k.real, k.imag,
+                                    M.ctypes.data)
+    return M
+
+
+def finite_translation_matrix(calc, pos, k, J):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    np_ = pos.shape[0]
+    N = np_ * 2 * calc.nelem
+    S = np.empty((N, N), dtype=np.complex128)
+    k = complex(k)
+    lib().orc_finite_translation_matrix_ri(calc.ptr, np_, pos.ctypes.data, k.real, k.imag, J, S.ctypes.data)
+    return S
+
+
+def planewave_full(lMax, pos, k_cart, E_cart):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    kc = np.ascontiguousarray(k_cart, dtype=np.float64)
+    Ec = np.ascontiguousarray(E_cart, dtype=np.complex128)
+    out = np.empty(pos.shape[0] * 2 * lMax * (lMax + 2), dtype=np.complex128)
+    lib().orc_planewave_full(lMax, pos.shape[0], pos.ctypes.data, kc.ctypes.data, Ec.ctypes.data,
+                             out.ctypes.data)
+    return out
+
+
+def finite_sphere_scatter(calc, pos, radius, eps_i, eps_e, omega, k_dir=(0, 0, 1), E_cart=(1, 0, 0),
+                          want_M=False):
+    """One frequency: returns (f, a_inc, sigma_ext[, M])."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    np_ = pos.shape[0]
+    N = np_ * 2 * calc.nelem
+    f = np.empty(N, dtype=np.complex128)
+    a = np.empty(N, dtype=np.complex128)
+    sig = np.zeros(1)
+    M = np.empty((N, N), dtype=np.complex128) if want_M else None
+    kd = np.ascontiguousarray(k_dir, dtype=np.float64)
+    Ec = np.ascontiguousarray(E_cart, dtype=np.complex128)
+    ei, ee = complex(eps_i), complex(eps_e)
+    info = lib().orc_finite_sphere_scatter_ri(calc.ptr, np_, pos.ctypes.data, radius, ei.real, ei.imag,
+                                              ee.real, ee.imag, float(omega), kd.ctypes.data, Ec.ctypes.data,
+                                              f.ctypes.data, a.ctypes.data, sig.ctypes.data,
+                                              M.ctypes.data if want_M else None)
+    if info:
+        raise ArithmeticError("singular mode-problem matrix (info=%d)" % info)
+    return (f, a, float(sig[0]), M) if want_M else (f, a, float(sig[0]))
+
+
+def lu_factor(M):
+    a = np.array(M, dtype=np.complex128, order="C", copy=True)
+    ipiv = np.zeros(a.shape[0], dtype=np.int32)
+    info = lib().orc_lu_factor(a.shape[0], a.ctypes.data, ipiv.ctypes.data)
+    return a, ipiv, info
+
+
+def lu_solve(a, ipiv, b):
+    b = np.array(b, dtype=np.complex128, order="C", copy=True)
+    nrhs = 1 if b.ndim == 1 else b.shape[1]
+    lib().orc_lu_solve(a.shape[0], a.ctypes.data, ipiv.ctypes.data, b.ctypes.data, nrhs)
+    return b

@@ -5,3 +5,4 @@ this package is a thin Python mirror of the reference's Cython interface over it
 """
 from ._lib import QpmsGpuError, lib, last_error  # noqa: F401
 from .translations import trans_calculator  # noqa: F401
+from .scatsystem import ScatteringSystem  # noqa: F401,E402

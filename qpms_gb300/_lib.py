@@ -58,8 +58,5 @@ def _declare(L):
     # complex by value is passed as two doubles (same registers on x86-64 and aarch64)
     L.qpms_trans_calculator_get_AB_arrays_ext.restype = ci
     L.qpms_trans_calculator_get_AB_arrays_ext.argtypes = [vp, vp, vp, sz, sz, cd, cd, cd, cd, ci, ci]
-    try:
-        from . import _lib_more
-        _lib_more.declare(L)
-    except ImportError:
-        pass
+    from . import scatsystem
+    scatsystem.declare(L)

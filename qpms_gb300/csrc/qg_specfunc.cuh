@@ -203,4 +203,35 @@ QG_HD void legendre_column(int L, int m, double x, double *out) {
   }
 }
 
+// Reciprocals 1/k, k = 1..kRecipMax, for division-free recurrences (FP64
+// division costs an order of magnitude more than an FMA on the FP64 pipe).
+constexpr int kRecipMax = 48;
+#if defined(__CUDACC__)
+static __constant__ double c_recip[kRecipMax + 1] = {
+    0.0, 1.0 / 1, 1.0 / 2, 1.0 / 3, 1.0 / 4, 1.0 / 5, 1.0 / 6, 1.0 / 7, 1.0 / 8, 1.0 / 9, 1.0 / 10,
+    1.0 / 11, 1.0 / 12, 1.0 / 13, 1.0 / 14, 1.0 / 15, 1.0 / 16, 1.0 / 17, 1.0 / 18, 1.0 / 19, 1.0 / 20,
+    1.0 / 21, 1.0 / 22, 1.0 / 23, 1.0 / 24, 1.0 / 25, 1.0 / 26, 1.0 / 27, 1.0 / 28, 1.0 / 29, 1.0 / 30,
+    1.0 / 31, 1.0 / 32, 1.0 / 33, 1.0 / 34, 1.0 / 35, 1.0 / 36, 1.0 / 37, 1.0 / 38, 1.0 / 39, 1.0 / 40,
+    1.0 / 41, 1.0 / 42, 1.0 / 43, 1.0 / 44, 1.0 / 45, 1.0 / 46, 1.0 / 47, 1.0 / 48};
+
+// legendre_column with the division by (l - m) replaced by a product with
+// the correctly rounded reciprocal (L <= kRecipMax).
+__device__ __forceinline__ void legendre_column_rt(int L, int m, double x, double *out) {
+  const double u = sqrt((1.0 - x) * (1.0 + x));
+  double pmm = 1.0;
+  for (int k = 1; k <= m; ++k) pmm *= -(2 * k - 1) * u;
+  out[m * (m + 1) / 2 + m] = pmm;
+  if (m + 1 > L) return;
+  double pm1 = x * (2 * m + 1) * pmm;
+  out[(m + 1) * (m + 2) / 2 + m] = pm1;
+  double a = pmm, b = pm1;
+  for (int l = m + 2; l <= L; ++l) {
+    double pl = ((2 * l - 1) * x * b - (l + m - 1) * a) * c_recip[l - m];
+    out[l * (l + 1) / 2 + m] = pl;
+    a = b;
+    b = pl;
+  }
+}
+#endif
+
 }  // namespace qg

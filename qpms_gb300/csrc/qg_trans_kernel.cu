@@ -125,19 +125,27 @@ __global__ void __launch_bounds__(kThreads) trans_ab_kernel(TransDevTables T, si
     __syncthreads();
     for (int t = tid; t < V * (L + 1); t += kThreads) {
       const int v = t / (L + 1), m = t - v * (L + 1);
-      legendre_column(L, m, info[v].ct, leg + v * NL);
+      legendre_column_rt(L, m, info[v].ct, leg + v * NL);
     }
     __syncthreads();
-    for (int t = tid; t < V * S; t += kThreads) {
-      const int v = t / S, s = t - v * S;
-      const int p = (int)sqrtf((float)s + 0.5f);
-      const int d = s - p * p - p;
-      const int ad = d < 0 ? -d : d;
-      qg_c ph = eph[v * (L + 1) + ad];
-      if (d < 0) ph.im = -ph.im;
-      qg_c val = cscale(cmul(zb[v * (L + 1) + p], ph), leg[v * NL + p * (p + 1) / 2 + ad]);
-      if (info[v].nan_out) val = cmk(__longlong_as_double(0x7ff8000000000000ULL), __longlong_as_double(0x7ff8000000000000ULL));
-      w[t] = val;
+    // w[p^2+p+d] and w[p^2+p-d] share P_p^{|d|} z_p; the phases are conjugate
+    constexpr int NPD = (L + 1) * (L + 2) / 2;  // (p, |d|) pairs
+    for (int t = tid; t < V * NPD; t += kThreads) {
+      const int v = t / NPD, i = t - v * NPD;
+      int p = (int)((sqrtf(8.0f * i + 1.0f) - 1.0f) * 0.5f);
+      if ((p + 1) * (p + 2) / 2 <= i) ++p;
+      if (p * (p + 1) / 2 > i) --p;
+      const int ad = i - p * (p + 1) / 2;
+      const qg_c u = cscale(zb[v * (L + 1) + p], leg[v * NL + i]);
+      const qg_c ph = eph[v * (L + 1) + ad];
+      qg_c wp = cmul(u, ph), wm = cmul(u, cconj(ph));
+      if (info[v].nan_out) {
+        const double nan = __longlong_as_double(0x7ff8000000000000ULL);
+        wp = wm = cmk(nan, nan);
+      }
+      qg_c *wv = w + v * S + p * p + p;
+      wv[ad] = wp;
+      if (ad) wv[-ad] = wm;
     }
     __syncthreads();
 
@@ -158,16 +166,17 @@ __global__ void __launch_bounds__(kThreads) trans_ab_kernel(TransDevTables T, si
           __syncthreads();
         }
         for (int k = tid; k < NE2; k += kThreads) {
+          // term counts are sorted, so the trip count is (nearly) warp-uniform
           const int c = cnt[k];
           double sr = 0.0, si = 0.0;
-#pragma unroll
-          for (int q = 0; q < TQ; ++q) {
-            if (q < c) {
-              const double a = __ldg(coef + q * NE2 + k);
-              const qg_c x = wv[__ldg(slot + q * NE2 + k)];
-              sr = fma(a, x.re, sr);
-              si = fma(a, x.im, si);
-            }
+          const double *cq = coef + k;
+          const uint16_t *sq = slot + k;
+#pragma unroll 2
+          for (int q = 0; q < c; ++q) {
+            const double a = __ldg(cq + q * NE2);
+            const qg_c x = wv[__ldg(sq + q * NE2)];
+            sr = fma(a, x.re, sr);
+            si = fma(a, x.im, si);
           }
           const qg_c r = which ? cmk(-si, sr) : cmk(sr, si);
           const int e = __ldg(T.perm + k);

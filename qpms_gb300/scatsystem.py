@@ -1,0 +1,179 @@
+"""Python mirror of the reference's scattering-system wrappers (qpms_c.pyx):
+``ScatteringSystem`` (:390-902), ``_ScatteringSystemAtOmega`` (:1000-1082) and
+``ScatteringMatrix`` (:1144-1195), over the C-ABI of libqpms_gb300.
+
+Systems are built from spheres with constant permittivities (the Mie T-matrix
+generator of the benchmark configurations); every heavy step runs on the GPU.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+QPMS_HANKEL_PLUS = 3
+
+
+class _LU(C.Structure):
+    _fields_ = [("ssw", C.c_void_p), ("sswk", C.c_void_p), ("full", C.c_bool), ("iri", C.c_int),
+                ("a", C.c_void_p), ("ipiv", C.c_void_p)]
+
+
+def declare(L):
+    vp, ci, cd, sz = C.c_void_p, C.c_int, C.c_double, C.c_size_t
+    L.qpms_gpu_scatsys_create_spheres.restype = vp
+    L.qpms_gpu_scatsys_create_spheres.argtypes = [ci, vp, vp, ci, vp, vp, cd, cd, ci]
+    L.qpms_gpu_scatsys_free.restype = None
+    L.qpms_gpu_scatsys_free.argtypes = [vp]
+    L.qpms_gpu_scatsys_at_omega.restype = vp
+    L.qpms_gpu_scatsys_at_omega.argtypes = [vp, cd, cd]
+    L.qpms_gpu_scatsys_at_omega_free.restype = None
+    L.qpms_gpu_scatsys_at_omega_free.argtypes = [vp]
+    L.qpms_scatsysw_build_modeproblem_matrix_full.restype = vp
+    L.qpms_scatsysw_build_modeproblem_matrix_full.argtypes = [vp, vp]
+    L.qpms_scatsys_build_translation_matrix_e_full.restype = vp
+    L.qpms_scatsys_build_translation_matrix_e_full.argtypes = [vp, vp, cd, cd, ci]
+    L.qpms_scatsysw_build_modeproblem_matrix_full_LU.restype = _LU
+    L.qpms_scatsysw_build_modeproblem_matrix_full_LU.argtypes = [vp, vp, vp]
+    L.qpms_scatsysw_modeproblem_matrix_full_factorise.restype = _LU
+    L.qpms_scatsysw_modeproblem_matrix_full_factorise.argtypes = [vp, vp, vp, vp]
+    L.qpms_scatsys_scatter_solve.restype = vp
+    L.qpms_scatsys_scatter_solve.argtypes = [vp, vp, _LU]
+    L.qpms_ss_LU_free.restype = None
+    L.qpms_ss_LU_free.argtypes = [_LU]
+    L.qpms_scatsysw_apply_Tmatrices_full.restype = vp
+    L.qpms_scatsysw_apply_Tmatrices_full.argtypes = [vp, vp, vp]
+    L.qpms_gpu_incident_planewave_full.restype = ci
+    L.qpms_gpu_incident_planewave_full.argtypes = [vp, vp, vp, vp]
+    L.qpms_gpu_finite_planewave_scatter.restype = ci
+    L.qpms_gpu_finite_planewave_scatter.argtypes = [vp, sz, vp, vp, vp, ci, vp, vp, vp, vp]
+
+
+class ScatteringSystem:
+    """Finite system of spheres; ``ss(omega)`` evaluates it at a frequency."""
+
+    def __init__(self, positions, radius, eps_inside, eps_medium, lMax, kinds=None):
+        self._L = _lib.lib()
+        pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        radius = np.atleast_1d(np.asarray(radius, dtype=np.float64))
+        eps_in = np.ascontiguousarray(np.atleast_1d(np.asarray(eps_inside, dtype=np.complex128)))
+        if kinds is None:
+            kinds = np.zeros(pos.shape[0], dtype=np.int32)
+        kinds = np.ascontiguousarray(kinds, dtype=np.int32)
+        em = complex(eps_medium)
+        self.positions = pos
+        self.lMax = int(lMax)
+        self.s = self._L.qpms_gpu_scatsys_create_spheres(pos.shape[0], pos.ctypes.data, kinds.ctypes.data,
+                                                         radius.size, radius.ctypes.data, eps_in.ctypes.data,
+                                                         em.real, em.imag, self.lMax)
+        if not self.s:
+            raise _lib.QpmsGpuError("qpms_gpu_scatsys_create_spheres: " + _lib.last_error())
+        self.fecv_size = pos.shape[0] * 2 * self.lMax * (self.lMax + 2)
+
+    def __del__(self):
+        s = getattr(self, "s", None)
+        if s:
+            self._L.qpms_gpu_scatsys_free(s)
+            self.s = None
+
+    def __call__(self, omega):
+        return _ScatteringSystemAtOmega(self, omega)
+
+    def planewave_full(self, k_cart, E_cart):
+        k = np.ascontiguousarray(k_cart, dtype=np.float64)
+        E = np.ascontiguousarray(E_cart, dtype=np.complex128)
+        out = np.empty(self.fecv_size, dtype=np.complex128)
+        _lib.check(self._L.qpms_gpu_incident_planewave_full(out.ctypes.data, self.s, k.ctypes.data, E.ctypes.data),
+                   "qpms_gpu_incident_planewave_full")
+        return out
+
+    def translation_matrix_full(self, wavenumber, J=QPMS_HANKEL_PLUS):
+        k = complex(wavenumber)
+        out = np.empty((self.fecv_size, self.fecv_size), dtype=np.complex128)
+        r = self._L.qpms_scatsys_build_translation_matrix_e_full(out.ctypes.data, self.s, k.real, k.imag, int(J))
+        if not r:
+            raise _lib.QpmsGpuError("translation matrix: " + _lib.last_error())
+        return out
+
+    def planewave_scatter_batch(self, omegas, k_dir=(0.0, 0.0, 1.0), E_cart=(1.0, 0.0, 0.0), mode=1,
+                                want_f=False):
+        """Batched loop of misc/finiterectlat-scatter.py over frequencies:
+        returns dict(sigma_ext, residual, iters[, f]).  mode 0: FP64 LU;
+        mode 1: complex64 LU + FP64 refinement."""
+        om = np.ascontiguousarray(omegas, dtype=np.float64)
+        kd = np.ascontiguousarray(k_dir, dtype=np.float64)
+        E = np.ascontiguousarray(E_cart, dtype=np.complex128)
+        nw = om.size
+        sig = np.empty(nw)
+        res = np.empty(nw)
+        it = np.empty(nw, dtype=np.int32)
+        f = np.empty((nw, self.fecv_size), dtype=np.complex128) if want_f else None
+        rc = self._L.qpms_gpu_finite_planewave_scatter(self.s, nw, om.ctypes.data, kd.ctypes.data, E.ctypes.data,
+                                                       int(mode), f.ctypes.data if want_f else None,
+                                                       sig.ctypes.data, res.ctypes.data, it.ctypes.data)
+        _lib.check(rc, "qpms_gpu_finite_planewave_scatter")
+        out = {"sigma_ext": sig, "residual": res, "iters": it}
+        if want_f:
+            out["f"] = f
+        return out
+
+
+class _ScatteringSystemAtOmega:
+    def __init__(self, ss, omega):
+        self.ss = ss
+        self._L = ss._L
+        om = complex(omega)
+        self.omega = om
+        self.ssw = self._L.qpms_gpu_scatsys_at_omega(ss.s, om.real, om.imag)
+        if not self.ssw:
+            raise _lib.QpmsGpuError("qpms_gpu_scatsys_at_omega: " + _lib.last_error())
+
+    def __del__(self):
+        w = getattr(self, "ssw", None)
+        if w:
+            self._L.qpms_gpu_scatsys_at_omega_free(w)
+            self.ssw = None
+
+    def modeproblem_matrix_full(self):
+        n = self.ss.fecv_size
+        out = np.empty((n, n), dtype=np.complex128)
+        if not self._L.qpms_scatsysw_build_modeproblem_matrix_full(out.ctypes.data, self.ssw):
+            raise _lib.QpmsGpuError("modeproblem_matrix_full: " + _lib.last_error())
+        return out
+
+    def apply_Tmatrices_full(self, a):
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        out = np.empty_like(a)
+        if not self._L.qpms_scatsysw_apply_Tmatrices_full(out.ctypes.data, a.ctypes.data, self.ssw):
+            raise _lib.QpmsGpuError("apply_Tmatrices_full: " + _lib.last_error())
+        return out
+
+    def scatter_solver(self):
+        return ScatteringMatrix(self)
+
+
+class ScatteringMatrix:
+    """LU-factorised (I - T S) (qpms_ss_LU); calling it solves for f."""
+
+    def __init__(self, ssw):
+        self.ssw = ssw
+        self._L = ssw._L
+        self.lu = self._L.qpms_scatsysw_build_modeproblem_matrix_full_LU(None, None, ssw.ssw)
+        if not self.lu.a:
+            raise _lib.QpmsGpuError("LU: " + _lib.last_error())
+
+    def __del__(self):
+        lu = getattr(self, "lu", None)
+        if lu is not None and lu.a:
+            self._L.qpms_ss_LU_free(lu)
+            self.lu = None
+
+    def __call__(self, a_inc):
+        n = self.ssw.ss.fecv_size
+        a = np.ascontiguousarray(a_inc, dtype=np.complex128)
+        if a.size != n:
+            raise ValueError("Length of a full coefficient vector has to be %d, not %d" % (n, a.size))
+        f = np.empty(n, dtype=np.complex128)
+        if not self._L.qpms_scatsys_scatter_solve(f.ctypes.data, a.ctypes.data, self.lu):
+            raise _lib.QpmsGpuError("scatter_solve: " + _lib.last_error())
+        return f

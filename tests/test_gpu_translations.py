@@ -2,9 +2,10 @@
 
 Tolerance (translation coefficients, 1e-11 relative): for every translation
 and each of A, B: ||G - O||_F <= 1e-11 ||O||_F, and element-wise
-|g - o| <= 1e-11 |o| for elements with |o| >= 1e-6 max|O| (smaller elements
-are sums whose terms are ~max|O| in size, so only the norm-wise bound is
-meaningful for them).
+|g - o| <= 1e-11 |o| + 1e-13 max|O|.  The absolute floor (1e-13 of the
+matrix's largest element) covers elements that are small only because their
+q-terms, each of order max|O|, cancel: their rounding error is set by the
+terms, not by the sum, in the reference (AMOS/GSL) as much as here.
 """
 import numpy as np
 import pytest
@@ -14,6 +15,7 @@ from qpms_gb300.workloads import translation_vectors
 pytestmark = pytest.mark.gpu
 
 RTOL = 1e-11
+ATOL_REL = 1e-13
 
 
 def _check(G, O, what):
@@ -22,10 +24,10 @@ def _check(G, O, what):
     fro = np.linalg.norm(G - O, axis=1) / np.linalg.norm(O, axis=1)
     assert np.all(np.isfinite(fro)), what
     assert fro.max() <= RTOL, (what, fro.max())
-    big = np.abs(O) >= 1e-6 * np.abs(O).max(axis=1, keepdims=True)
-    rel = np.abs(G - O)[big] / np.abs(O)[big]
-    assert rel.max() <= RTOL, (what, rel.max())
-    return fro.max(), rel.max()
+    bound = RTOL * np.abs(O) + ATOL_REL * np.abs(O).max(axis=1, keepdims=True)
+    excess = (np.abs(G - O) / bound).max()
+    assert excess <= 1.0, (what, excess)
+    return fro.max(), excess
 
 
 @pytest.fixture(scope="module")
