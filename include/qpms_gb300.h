@@ -232,6 +232,13 @@ qpms_scatsys_t *qpms_gpu_scatsys_create_spheres(int np, const double *pos_xyz, c
     qpms_complex_t eps_medium, qpms_l_t lMax);
 void qpms_gpu_scatsys_free(qpms_scatsys_t *ss);
 
+/* 2D-periodic system (lattice_dimension 2) with direct basis b1, b2 in the xy
+ * plane; fills ss->per as process_lattice_bases does (scatsystem.c:187-214:
+ * reduced basis, reciprocal basis, unit-cell area, eta = sqrt(pi / A)). */
+qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_2d(int np, const double *pos_xyz, const int *kind,
+    int nkinds, const double *radius, const qpms_complex_t *eps_inside,
+    qpms_complex_t eps_medium, qpms_l_t lMax, const double b1[2], const double b2[2]);
+
 /* Evaluates the medium and the T-matrices at omega, like qpms_scatsys_at_omega
  * (scatsystem.c:606-630). */
 qpms_scatsys_at_omega_t *qpms_gpu_scatsys_at_omega(const qpms_scatsys_t *ss, qpms_complex_t omega);
@@ -268,6 +275,29 @@ void qpms_ss_LU_free(qpms_ss_LU lu);
 qpms_complex_t *qpms_scatsysw_apply_Tmatrices_full(qpms_complex_t *target_full,
     const qpms_complex_t *inc_full, const qpms_scatsys_at_omega_t *ssw);
 
+/* Replaces qpms_ss_adjusted_eta (scatsystem.h:795, scatsystem.c:68-80). */
+double qpms_ss_adjusted_eta(const qpms_scatsys_t *ss, qpms_complex_t wavenumber, const double wavevector[3]);
+
+/* Replaces qpms_scatsyswk_build_modeproblem_matrix_full (scatsystem.h:498-502,
+ * scatsystem.c:1352-1357): M = I - T W(omega, k) of a 2D lattice, W from the
+ * Ewald sums (short range, long range, sigma0) on the GPU; eta = sswk->eta or,
+ * if 0/NaN, qpms_ss_adjusted_eta.  Diagonal T-matrices. */
+qpms_complex_t *qpms_scatsyswk_build_modeproblem_matrix_full(qpms_complex_t *target,
+    const qpms_scatsys_at_omega_k_t *sswk);
+/* Replaces qpms_scatsyswk_build_modeproblem_matrix_full_LU (scatsystem.h:523-527). */
+qpms_ss_LU qpms_scatsyswk_build_modeproblem_matrix_full_LU(qpms_complex_t *target, int *target_piv,
+    const qpms_scatsys_at_omega_k_t *sswk);
+
+/* Batched dispersion scan of a 2D lattice (config "2D-periodic dispersion
+ * scan"): for every omega (nw, real) and in-plane Bloch vector (nk, kvecs
+ * [nk][2]) assemble M = I - T W (adjusted eta), LU-factorise (FP64), and write
+ * logdet[w][k] = log|det M|; optionally solve for the excitation of a plane
+ * wave with in-plane wavevector = Bloch vector and E along x projected
+ * perpendicular to k (x-polarised at normal incidence): f_out[w][k][fecv],
+ * sigma_ext = -Re(a^H f)/k^2 per cell, resid = ||M f - T a|| / ||T a||.  Synchronous. */
+int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *omegas, size_t nk,
+    const double *kvecs, double *logdet, qpms_complex_t *f_out, double *sigma_ext, double *resid_out);
+
 /* Plane-wave incident vector (qpms_scatsys_incident_field_vector_full with
  * qpms_incfield_planewave, scatsystem.c:1970-1983, vswf.c:480-530), real k. */
 int qpms_gpu_incident_planewave_full(qpms_complex_t *target_full, const qpms_scatsys_t *ss,
@@ -290,6 +320,8 @@ const char *qpms_gpu_last_error(void);
 /* FP64 FMA throughput of the current device in TFLOP/s (probe kernel), the
  * denominator of FP64-pipe roofline fractions.  No counterpart in the reference. */
 int qpms_gpu_measure_fp64_peak(double *tflops);
+/* Host evaluation of the library's complex erfc (Weideman Faddeeva), for tests. */
+int qpms_gpu_debug_cerfc(double re, double im, double *out);
 /* Number of kernels this library launched since load (for benchmarks). */
 unsigned long long qpms_gpu_kernel_launch_count(void);
 

@@ -55,6 +55,7 @@ def _declare(L):
     L.orc_num_threads.restype = C.c_int
     L.orc_num_threads.argtypes = []
     _declare_scatsys(L)
+    _declare_ewald(L)
 
 
 def num_threads():
@@ -253,3 +254,83 @@ def lu_solve(a, ipiv, b):
     nrhs = 1 if b.ndim == 1 else b.shape[1]
     lib().orc_lu_solve(a.shape[0], a.ctypes.data, ipiv.ctypes.data, b.ctypes.data, nrhs)
     return b
+
+
+def _declare_ewald(L):
+    vp, ci, cd = C.c_void_p, C.c_int, C.c_double
+    L.orc_ewald3_sigma_xy_ri.restype = None
+    L.orc_ewald3_sigma_xy_ri.argtypes = [ci, ci, cd, cd, cd, vp, vp, vp, cd, cd, ci, vp, vp, vp]
+    L.orc_get_AB_arrays_e32_ri.restype = ci
+    L.orc_get_AB_arrays_e32_ri.argtypes = [vp, vp, vp, cd, cd, cd, vp, vp, vp, cd, cd, ci]
+    L.orc_periodic_modeproblem_ri.restype = ci
+    L.orc_periodic_modeproblem_ri.argtypes = [vp, ci, vp, vp, cd, cd, vp, vp, cd, vp]
+    L.orc_complex_gamma_inc_ri.restype = None
+    L.orc_complex_gamma_inc_ri.argtypes = [cd, cd, cd, ci, vp]
+    L.orc_ewald_sr_integral_ri.restype = None
+    L.orc_ewald_sr_integral_ri.argtypes = [cd, cd, cd, ci, cd, vp]
+    L.orc_adjusted_eta.restype = cd
+    L.orc_adjusted_eta.argtypes = [cd, C.c_double * 2, vp, ci]
+
+
+def ewald_sigma_xy(lMax_e, eta, k, b1, b2, beta, shift, maxR, maxK, parts=7, csphase=-1):
+    """(sigma_total, sigma_short, sigma_long) of the 2D xy Ewald sum, nelem_sc each."""
+    L = lib()
+    ne = lMax_e * (lMax_e + 2) + 1
+    out = [np.zeros(ne, dtype=np.complex128) for _ in range(3)]
+    b12 = np.array([b1[0], b1[1], b2[0], b2[1]], dtype=np.float64)
+    be = np.array(beta[:2], dtype=np.float64)
+    sh = np.array(shift[:2], dtype=np.float64)
+    k = complex(k)
+    L.orc_ewald3_sigma_xy_ri(lMax_e, csphase, float(eta), k.real, k.imag, b12.ctypes.data, be.ctypes.data,
+                             sh.ctypes.data, float(maxR), float(maxK), int(parts), out[0].ctypes.data,
+                             out[1].ctypes.data, out[2].ctypes.data)
+    return tuple(out)
+
+
+def get_AB_arrays_e32(calc, eta, k, b1, b2, beta, shift, maxR, maxK, parts=7):
+    L = lib()
+    ne = calc.nelem
+    A = np.zeros((ne, ne), dtype=np.complex128)
+    B = np.zeros((ne, ne), dtype=np.complex128)
+    b12 = np.array([b1[0], b1[1], b2[0], b2[1]], dtype=np.float64)
+    be = np.array(beta[:2], dtype=np.float64)
+    sh = np.array(shift[:2], dtype=np.float64)
+    k = complex(k)
+    L.orc_get_AB_arrays_e32_ri(calc.ptr, A.ctypes.data, B.ctypes.data, float(eta), k.real, k.imag, b12.ctypes.data,
+                               be.ctypes.data, sh.ctypes.data, float(maxR), float(maxK), int(parts))
+    return A, B
+
+
+def periodic_modeproblem(calc, pos, T, k, b1, b2, kvec, eta):
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.complex128)
+    np_ = pos.shape[0]
+    N = np_ * 2 * calc.nelem
+    M = np.empty((N, N), dtype=np.complex128)
+    b12 = np.array([b1[0], b1[1], b2[0], b2[1]], dtype=np.float64)
+    kv = np.array(kvec[:2], dtype=np.float64)
+    k = complex(k)
+    lib().orc_periodic_modeproblem_ri(calc.ptr, np_, pos.ctypes.data, T.ctypes.data, k.real, k.imag,
+                                      b12.ctypes.data, kv.ctypes.data, float(eta), M.ctypes.data)
+    return M
+
+
+def complex_gamma_inc(a, x, m=0):
+    out = np.zeros(1, dtype=np.complex128)
+    x = complex(x)
+    lib().orc_complex_gamma_inc_ri(float(a), x.real, x.imag, int(m), out.ctypes.data)
+    return out[0]
+
+
+def ewald_sr_integral(r, k, n, eta):
+    out = np.zeros(1, dtype=np.complex128)
+    k = complex(k)
+    lib().orc_ewald_sr_integral_ri(float(r), k.real, k.imag, int(n), float(eta), out.ctypes.data)
+    return out[0]
+
+
+def adjusted_eta(area, wavenumber, kvec, lMax):
+    kv = np.zeros(3)
+    kv[:len(kvec)] = kvec
+    w = complex(wavenumber)
+    return lib().orc_adjusted_eta(float(area), (C.c_double * 2)(w.real, w.imag), kv.ctypes.data, int(lMax))

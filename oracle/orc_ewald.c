@@ -1,0 +1,668 @@
+/*
+ * Oracle 2D Ewald lattice sums and the lattice ("e32") translation operator
+ * (test infrastructure only; see orc.h).
+ *
+ * Restates, for 2D lattices in the xy plane of 3D space (LAT_2D_IN_3D_XYONLY,
+ * particle shifts with z = 0), the reference build (LATTICESUMS32,
+ * EWALD_AUTO_CUTOFF, no GEN_[RK]SHIFTEDPOINTS):
+ *   lattice utilities        lattices2d.c:635-760, 801-855
+ *   PGen_xyWeb               latticegens.c:449-568
+ *   ewald3 constants         ewald.c:104-157 (EWALD32_CONSTANTS_AGNOSTIC), :228-241 (legendre0)
+ *   sigma0                   ewald.c:260-273
+ *   long-range sum           ewald.c:286-503 (xy branch, auto cutoff)
+ *   short-range sum          ewald.c:742-920 (xy branch, auto cutoff)
+ *   SR integrals             ewald.c:656-740: gsl_integration_qagiu at epsabs = epsrel = 1e-13,
+ *                            restated as adaptive 15-point Gauss-Kronrod on the same
+ *                            transformed interval (x = a + (1 - t)/t) without extrapolation
+ *   incomplete gamma         ewaldsf.c:44-205 (series, continued fraction, branch m);
+ *                            gsl_sf_gamma_e -> tgamma, the real branch -> the same series/CF
+ *   clilgamma                ewald.h:157-170
+ *   e32 contraction          translations.c:926-1078 (B summed over q <= qmax_A, as there)
+ *   trans array e32          translations.c:724-776
+ *   periodic M = I - T W     scatsystem.c:1219-1237, 1283-1343
+ *   adjusted eta             scatsystem.c:68-80, default eta scatsystem.c:194-207
+ */
+#include "orc.h"
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_SQRTPI 1.7724538509055160272981674833411452
+
+static int m1pow(int p) { return (p % 2) ? -1 : 1; }
+static double complex ipow(int x) {
+  x = ((x % 4) + 4) % 4;
+  switch (x) {
+    case 0: return 1;
+    case 1: return I;
+    case 2: return -1;
+    default: return -I;
+  }
+}
+static double sq(double x) { return x * x; }
+static double complex csq(double complex x) { return x * x; }
+
+static void kahanadd(double *sum, double *c, double in) {
+  double ci = in - *c, ns = *sum + ci;
+  *c = (ns - *sum) - ci;
+  *sum = ns;
+}
+static void ckahanadd(double complex *sum, double complex *c, double complex in) {
+  double complex ci = in - *c, ns = *sum + ci;
+  *c = (ns - *sum) - ci;
+  *sum = ns;
+}
+
+/* ---------------- lattices2d.c ---------------- */
+static double dot2(orc_c2 a, orc_c2 b) { return a.x * b.x + a.y * b.y; }
+static orc_c2 sub2(orc_c2 a, orc_c2 b) { orc_c2 r = {a.x - b.x, a.y - b.y}; return r; }
+static orc_c2 add2(orc_c2 a, orc_c2 b) { orc_c2 r = {a.x + b.x, a.y + b.y}; return r; }
+static orc_c2 scale2(double s, orc_c2 a) { orc_c2 r = {s * a.x, s * a.y}; return r; }
+
+void orc_l2d_reduceBasis(orc_c2 b1, orc_c2 b2, orc_c2 *o1, orc_c2 *o2) {
+  double B1 = dot2(b1, b1);
+  double mu = dot2(b1, b2) / B1;
+  b2 = sub2(b2, scale2(round(mu), b1));
+  double B2 = dot2(b2, b2);
+  while (B2 < B1) {
+    orc_c2 t = b1;
+    b1 = b2;
+    b2 = t;
+    B1 = B2;
+    mu = dot2(b1, b2) / B1;
+    b2 = sub2(b2, scale2(round(mu), b1));
+    B2 = dot2(b2, b2);
+  }
+  *o1 = b1;
+  *o2 = b2;
+}
+
+static int is_obtuse(orc_c2 b1, orc_c2 b2, double rtol) {
+  double B1 = dot2(b1, b1), B2 = dot2(b2, b2);
+  orc_c2 b3 = sub2(b2, b1);
+  return dot2(b3, b3) - B2 - B1 > rtol * (B1 + B2);
+}
+
+static double hexweb_incircle(orc_c2 i1, orc_c2 i2) {
+  orc_c2 b1, b2, b3;
+  orc_l2d_reduceBasis(i1, i2, &b1, &b2);
+  if (is_obtuse(b1, b2, 0)) {
+    b3 = b2;
+    b2 = add2(b2, b1);
+  } else {
+    b3 = sub2(b2, b1);
+  }
+  double r1 = sqrt(dot2(b1, b1)), r2 = sqrt(dot2(b2, b2)), r3 = sqrt(dot2(b3, b3));
+  double p = (r1 + r2 + r3) * 0.5;
+  return 2 * sqrt(p * (p - r1) * (p - r2) * (p - r3)) / r3;
+}
+
+static int right_angles(orc_c2 b1, orc_c2 b2, double rtol) {
+  orc_l2d_reduceBasis(b1, b2, &b1, &b2);
+  orc_c2 ht = sub2(b2, b1);
+  double b1s = dot2(b1, b1), b2s = dot2(b2, b2), hts = dot2(ht, ht);
+  return hts - b2s - b1s <= rtol * (b2s + b1s);
+}
+
+double orc_l2d_unitcell_area(orc_c2 b1, orc_c2 b2) {
+  orc_l2d_reduceBasis(b1, b2, &b1, &b2);
+  return fabs(b1.x * b2.y - b1.y * b2.x);
+}
+
+void orc_l2d_reciprocalBasis2pi(orc_c2 b1, orc_c2 b2, orc_c2 *rb1, orc_c2 *rb2) {
+  orc_l2d_reduceBasis(b1, b2, &b1, &b2);
+  double det = b1.x * b2.y - b1.y * b2.x;
+  rb1->x = 2 * M_PI * b2.y / det;
+  rb1->y = -2 * M_PI * b2.x / det;
+  rb2->x = -2 * M_PI * b1.y / det;
+  rb2->y = 2 * M_PI * b1.x / det;
+}
+
+/* ---------------- PGen_xyWeb (latticegens.c:449-568) ---------------- */
+typedef struct {
+  long layer, last_layer, i, j;
+  int phase, ortho;
+  orc_c2 b1, b2;
+} xyweb;
+
+static void xyweb_init(xyweb *s, orc_c2 b1, orc_c2 b2, double rtol, double minR, int inc_minR, double maxR,
+                       int inc_maxR) {
+  orc_l2d_reduceBasis(b1, b2, &s->b1, &s->b2);
+  s->ortho = right_angles(s->b1, s->b2, rtol);
+  double h = hexweb_incircle(s->b1, s->b2);
+  s->layer = (long)ceil(minR / h);
+  if (!inc_minR && (s->layer * h) <= minR) ++s->layer;
+  s->i = s->layer;
+  s->j = 0;
+  s->phase = 0;
+  s->last_layer = (long)floor(maxR / h);
+  if (!inc_maxR && (s->last_layer * h) >= maxR) --s->last_layer;
+}
+
+static int xyweb_next(xyweb *s, orc_c2 *pt) {
+  if (s->layer > s->last_layer) return 0;
+  *pt = add2(scale2((double)s->i, s->b1), scale2((double)s->j, s->b2));
+  if (s->layer == 0) {
+    ++s->layer;
+    s->phase = 0;
+    s->i = s->layer;
+    s->j = 0;
+  } else if (s->ortho) {
+    switch (s->phase) {
+      case 0: --s->i; ++s->j; if (s->i <= 0) ++s->phase; break;
+      case 1: --s->i; --s->j; if (s->j <= 0) ++s->phase; break;
+      case 2: ++s->i; --s->j; if (s->i >= 0) ++s->phase; break;
+      case 3: ++s->i; ++s->j; if (s->j >= 0) ++s->phase; break;
+    }
+    if (s->phase == 4) {
+      ++s->layer;
+      s->phase = 0;
+      s->i = s->layer;
+      s->j = 0;
+    }
+  } else {
+    switch (s->phase) {
+      case 0: --s->i; ++s->j; if (s->i <= 0) ++s->phase; break;
+      case 1: --s->i; if (s->i + s->j <= 0) ++s->phase; break;
+      case 2: --s->j; if (s->j <= 0) ++s->phase; break;
+      case 3: ++s->i; --s->j; if (s->i >= 0) ++s->phase; break;
+      case 4: ++s->i; if (s->i + s->j >= 0) ++s->phase; break;
+      case 5: ++s->j; if (s->j >= 0) ++s->phase; break;
+    }
+    if (s->phase == 6) {
+      ++s->layer;
+      s->phase = 0;
+      s->i = s->layer;
+      s->j = 0;
+    }
+  }
+  return 1;
+}
+
+/* ---------------- incomplete gamma (ewaldsf.c:44-205) ---------------- */
+static int gamma_inc_series(double a, double complex z, double complex *val) {
+  double fullgamma = tgamma(a);
+  double complex sumprefac = cpow(z, a) * cexp(-z);
+  double complex sum = 0, sumc = 0;
+  int brk = 0;
+  for (int k = 0; !brk && (a + k + 1 <= 171.0); ++k) {
+    double g = tgamma(a + k + 1);
+    double complex summand = -cpow(z, k) / g;
+    ckahanadd(&sum, &sumc, summand);
+    if (a + k >= 18 && cabs(summand) < DBL_EPSILON) brk = 1;
+  }
+  sum *= sumprefac;
+  sumc *= sumprefac;
+  ckahanadd(&sum, &sumc, 1.);
+  *val = sum * fullgamma;
+  return brk ? 0 : 1;
+}
+
+static double complex gamma_inc_F_CF(double a, double complex z) {
+  const int nmax = 5000;
+  const double small = DBL_EPSILON * DBL_EPSILON * DBL_EPSILON;
+  double complex hn = 1.0, Cn = 1.0 / small, Dn = 1.0;
+  for (int n = 2; n < nmax; n++) {
+    double complex an = (n % 2) ? 0.5 * (n - 1) / z : (0.5 * n - a) / z;
+    Dn = 1.0 + an * Dn;
+    if (cabs(Dn) < small) Dn = small;
+    Cn = 1.0 + an / Cn;
+    if (cabs(Cn) < small) Cn = small;
+    Dn = 1.0 / Dn;
+    double complex delta = Cn * Dn;
+    hn *= delta;
+    if (cabs(delta - 1.0) < DBL_EPSILON) break;
+  }
+  return hn;
+}
+
+static double complex gamma_inc_CF(double a, double complex z) {
+  double complex am1lgz = (a - 1.0) * clog(z);
+  double complex F = gamma_inc_F_CF(a, z);
+  double complex cpre = exp(creal(am1lgz - z)) * cexp(I * cimag(am1lgz - z));
+  return F * cpre;
+}
+
+double complex orc_complex_gamma_inc(double a, double complex x, int m) {
+  double complex val;
+  if (creal(x) >= 0 && (0 == fabs(cimag(x)) || fabs(cimag(x)) < fabs(creal(x)) * 1e-14)) {
+    /* real positive argument (gsl_sf_gamma_inc_e in the reference) */
+    double xr = creal(x);
+    if (xr > 0.5) val = gamma_inc_CF(a, xr);
+    else gamma_inc_series(a, xr, &val);
+    val = creal(val);
+  } else if (creal(x) >= 0 && cabs(x) > 0.5) {
+    val = gamma_inc_CF(a, x);
+  } else {
+    gamma_inc_series(a, x, &val);
+  }
+  if (m) {
+    double complex f = cexp(2 * m * M_PI * a * I);
+    val = f * val + (1 - f) * tgamma(a);
+  }
+  return val;
+}
+
+/* ewald.h:157-170 */
+static double complex clilgamma(double complex z) {
+  double complex a1 = z - 1, a2 = z + 1;
+  if (creal(a2) < 0 && cimag(a2) <= 0) a2 = -csqrt(a2);
+  else a2 = csqrt(a2);
+  if (creal(a1) < 0 && cimag(a1) >= 0) a1 = -csqrt(a1);
+  else a1 = csqrt(a1);
+  return a1 * a2;
+}
+
+/* ---------------- ewald3 constants (xy part) ---------------- */
+static double factorial(int n) {
+  if (n <= 20) {
+    double f = 1;
+    for (int i = 1; i <= n; ++i) f *= i;
+    return f;
+  }
+  return tgamma(n + 1);
+}
+
+typedef struct {
+  int lMax, nelem_sc;
+  int *jmax;
+  double complex **s1;
+  double complex *s1_base;
+  double *legendre0;
+} e3c_t;
+
+static e3c_t *e3c_init(int lMax, int csphase) {
+  e3c_t *c = malloc(sizeof(*c));
+  c->lMax = lMax;
+  c->nelem_sc = lMax * (lMax + 2) + 1;
+  c->jmax = malloc(sizeof(int) * c->nelem_sc);
+  c->s1 = malloc(sizeof(double complex *) * c->nelem_sc);
+  size_t sz = 0;
+  for (int y = 0; y < c->nelem_sc; ++y) {
+    int n = (int)sqrt((double)y), m = y - n * (n + 1);
+    if ((m + n) % 2 == 0) sz += 1 + (c->jmax[y] = (n - abs(m)) / 2);
+    else c->jmax[y] = -1;
+  }
+  c->s1_base = malloc(sizeof(double complex) * (sz ? sz : 1));
+  size_t cum = 0;
+  for (int y = 0; y < c->nelem_sc; ++y) {
+    int n = (int)sqrt((double)y), m = y - n * (n + 1);
+    if ((m + n) % 2 == 0) {
+      c->s1[y] = c->s1_base + cum;
+      for (int j = 0; j <= c->jmax[y]; ++j)
+        c->s1[y][j] = -2 * ipow(n + 1) * ORC_SQRTPI * factorial((n - m) / 2) * factorial((n + m) / 2) * m1pow(j) /
+                      (factorial(j) * factorial((n - m) / 2 - j) * factorial((n + m) / 2 - j));
+      cum += 1 + c->jmax[y];
+    } else
+      c->s1[y] = NULL;
+  }
+  c->legendre0 = malloc(sizeof(double) * (lMax + 1) * (lMax + 2) / 2);
+  orc_legendre_array(lMax, 0.0, csphase, c->legendre0);
+  return c;
+}
+
+static void e3c_free(e3c_t *c) {
+  free(c->jmax);
+  free(c->s1);
+  free(c->s1_base);
+  free(c->legendre0);
+  free(c);
+}
+
+static int leg_idx(int l, int m) { return l * (l + 1) / 2 + m; }
+static int m1pow_m_neg(int m) { return (m < 0) ? m1pow(m) : 1; }
+
+/* ewald.c:260-273 */
+static double complex sigma0(const e3c_t *c, double eta, double complex k) {
+  double complex z = -csq(k / (2 * eta));
+  double complex g = orc_complex_gamma_inc(-0.5, z, (creal(z) < 0 && !signbit(cimag(z))) ? -1 : 0);
+  return g * c->legendre0[0] / 2 / ORC_SQRTPI;
+}
+
+static double complex cpow_0lim_zi(double complex x, long z) {
+  if (x == 0 && z == 0) return 1;
+  if (x == 0 && z > 0) return 0;
+  return cpow(x, z);
+}
+
+/* ewald.c:286-503, xy lattice with particle_shift.z == 0 */
+static void sigma_long(const e3c_t *c, double complex *target, double eta, double complex k, double A, orc_c2 rb1,
+                       orc_c2 rb2, double maxK, orc_c2 beta, orc_c2 shift) {
+  const int nelem_sc = c->nelem_sc, lMax = c->lMax;
+  double complex *tc = calloc(nelem_sc, sizeof(double complex));
+  memset(target, 0, sizeof(double complex) * nelem_sc);
+  size_t lw = 1, li = 0;
+  double lsum = 0, lsum_c = 0;
+  const double complex commonfac = 1 / (k * k * A);
+  xyweb g;
+  xyweb_init(&g, rb1, rb2, 1e-13, 0, 1, maxK, 0);
+  orc_c2 K;
+  double complex Gam[lMax / 2 + 1];
+  while (xyweb_next(&g, &K)) {
+    orc_c2 bK = add2(K, beta);
+    const double rbeta = sqrt(dot2(bK, bK));
+    const double arg = atan2(bK.y, bK.x);
+    const double complex phasefac = cexp(I * dot2(K, shift));
+    const double complex gamma_pq = clilgamma(rbeta / k);
+    const double complex x = gamma_pq * k / (2 * eta);
+    const double complex x2 = x * x;
+    for (int j = 0; j <= lMax / 2; ++j)
+      Gam[j] = orc_complex_gamma_inc(0.5 - j, x2, (creal(x2) < 0 && !signbit(cimag(x2))) ? -1 : 0);
+    for (int n = 0; n <= lMax; ++n)
+      for (int m = -n; m <= n; ++m) {
+        if ((m + n) % 2 != 0) continue;
+        const int y = n * (n + 1) + m;
+        const double complex e_im = cexp(I * m * arg);
+        double complex jsum = 0, jsum_c = 0;
+        for (int j = 0; j <= c->jmax[y]; ++j) {
+          double complex summand = cpow_0lim_zi(rbeta / k, n - 2 * j) * e_im * c->legendre0[leg_idx(n, abs(m))] *
+                                   m1pow_m_neg(m) * cpow(gamma_pq, 2 * j - 1) * c->s1[y][j];
+          summand *= Gam[j];
+          ckahanadd(&jsum, &jsum_c, summand);
+        }
+        jsum *= phasefac;
+        ckahanadd(target + y, tc + y, jsum);
+        kahanadd(&lsum, &lsum_c, cabs(jsum));
+      }
+    ++li;
+    double cursum_min = INFINITY;
+    for (int y = 0; y < nelem_sc; ++y) {
+      const double a = cabs(target[y]);
+      if (a && a < cursum_min) cursum_min = a;
+    }
+    if (li >= 12 * lw + 1) {
+      if (lsum < DBL_EPSILON * cursum_min) break;
+      lsum = lsum_c = 0;
+      li = 0;
+      ++lw;
+    }
+  }
+  free(tc);
+  for (int y = 0; y < nelem_sc; ++y) target[y] *= commonfac;
+}
+
+/* ---- adaptive Gauss-Kronrod (15 points) on (0, 1] for the QAGIU transform ---- */
+static const double xgk[8] = {0.991455371120812639206854697526329, 0.949107912342758524526189684047851,
+                              0.864864423359769072789712788640926, 0.741531185599394439863864773280788,
+                              0.586087235467691130294144845693013, 0.405845151377397166906606412076961,
+                              0.207784955007898467600689403773245, 0.000000000000000000000000000000000};
+static const double wgk[8] = {0.022935322010529224963732008058970, 0.063092092629978553290700663189204,
+                              0.104790010322250183839876322541518, 0.140653259715525918745189590510238,
+                              0.169004726639267902826583426598550, 0.190350578064785409913256402421014,
+                              0.204432940075298892414161999234649, 0.209482141084727828012999174891714};
+static const double wg[4] = {0.129484966168869693270611432679082, 0.279705391489276667901467771423780,
+                             0.381830050505118944950369775488975, 0.417959183673469387755102040816327};
+
+typedef orc_fn_t orc_fn;
+
+static void qk15(orc_fn f, const void *p, double a, double b, double *res, double *err) {
+  const double c = 0.5 * (a + b), h = 0.5 * (b - a);
+  double fc = f(c, p);
+  double rg = fc * wg[3], rk = fc * wgk[7];
+  for (int j = 0; j < 7; ++j) {
+    double x = h * xgk[j];
+    double f1 = f(c - x, p), f2 = f(c + x, p);
+    rk += wgk[j] * (f1 + f2);
+    if (j % 2 == 1) rg += wg[j / 2] * (f1 + f2);
+  }
+  *res = rk * h;
+  *err = fabs((rk - rg) * h);
+}
+
+typedef struct {
+  orc_fn f;
+  const void *p;
+  double a;
+} qagiu_t;
+
+static double qagiu_tr(double t, const void *pp) {
+  const qagiu_t *q = pp;
+  double x = q->a + (1 - t) / t;
+  return q->f(x, q->p) / (t * t);
+}
+
+/* Integral of f over [a, inf) to max(epsabs, epsrel |I|), adaptive bisection. */
+double orc_qagiu(orc_fn f, const void *p, double a, double epsabs, double epsrel, double *abserr) {
+  qagiu_t q = {f, p, a};
+  enum { MAXIV = 2000 };
+  double lo[MAXIV], hi[MAXIV], r[MAXIV], e[MAXIV];
+  int n = 1;
+  lo[0] = 0;
+  hi[0] = 1;
+  qk15(qagiu_tr, &q, 0, 1, &r[0], &e[0]);
+  for (;;) {
+    double tot = 0, terr = 0;
+    int worst = 0;
+    for (int i = 0; i < n; ++i) {
+      tot += r[i];
+      terr += e[i];
+      if (e[i] > e[worst]) worst = i;
+    }
+    double tol = fmax(epsabs, epsrel * fabs(tot));
+    if (terr <= tol || n >= MAXIV - 1) {
+      if (abserr) *abserr = terr;
+      return tot;
+    }
+    double m = 0.5 * (lo[worst] + hi[worst]);
+    lo[n] = m;
+    hi[n] = hi[worst];
+    hi[worst] = m;
+    qk15(qagiu_tr, &q, lo[worst], hi[worst], &r[worst], &e[worst]);
+    qk15(qagiu_tr, &q, lo[n], hi[n], &r[n], &e[n]);
+    ++n;
+  }
+}
+
+typedef struct {
+  int n;
+  double complex k;
+  double R;
+  int part;  /* 0 real, 1 imaginary */
+} sr_par;
+
+static double sr_integrand(double ksi, const void *pp) {
+  const sr_par *p = pp;
+  double complex v = cexp(-csq(p->R * ksi) + csq(p->k / ksi / 2)) * pow(ksi, 2 * p->n);
+  return p->part ? cimag(v) : creal(v);
+}
+
+/* ewald.c:656-740: integral of exp(-r^2 x^2 + k^2 / (4 x^2)) x^(2n) over [eta, inf) */
+double complex orc_ewald_sr_integral(double r, double complex k, int n, double eta) {
+  const double R0 = r;
+  sr_par p;
+  p.n = n;
+  p.k = k * R0;
+  p.R = r / R0;
+  double etas = eta * R0;
+  p.part = 0;
+  double re = orc_qagiu(sr_integrand, &p, etas, 1e-13, 1e-13, NULL);
+  double im = 0;
+  if (cimag(k) != 0) {
+    p.part = 1;
+    im = orc_qagiu(sr_integrand, &p, etas, 1e-13, 1e-13, NULL);
+  }
+  return (re + I * im) * pow(R0, -2 * n - 1);
+}
+
+/* ewald.c:742-920, xy lattice */
+static void sigma_short(const e3c_t *c, double complex *target, double eta, double complex k, orc_c2 b1, orc_c2 b2,
+                        double maxR, int include_origin, orc_c2 beta, orc_c2 shift) {
+  const int nelem_sc = c->nelem_sc, lMax = c->lMax;
+  const int k_is_real = (cimag(k) == 0);
+  double complex *tc = calloc(nelem_sc, sizeof(double complex));
+  memset(target, 0, sizeof(double complex) * nelem_sc);
+  size_t lw = 1, li = 0;
+  double lsum = 0, lsum_c = 0;
+  xyweb g;
+  xyweb_init(&g, b1, b2, 1e-13, 0, include_origin, maxR, 0);
+  orc_c2 Rb;
+  double complex cintres[lMax + 1];
+  while (xyweb_next(&g, &Rb)) {
+    orc_c2 Rs = sub2(Rb, shift);
+    const double arg = atan2(Rs.y, Rs.x);
+    const double r = sqrt(dot2(Rs, Rs));
+    const double complex e_beta = cexp(I * dot2(beta, Rs));
+    for (int n = 0; n <= lMax; ++n) {
+      const double complex prefacn = -I * (k_is_real ? pow(2. / creal(k), n + 1) : cpow(2. / k, n + 1)) / ORC_SQRTPI;
+      const double Rpown = pow(r, n);
+      cintres[n] = orc_ewald_sr_integral(r, k, n, eta);
+      for (int m = -n; m <= n; ++m) {
+        if ((m + n) % 2 != 0) continue;
+        const double complex e_imf = cexp(I * m * arg);
+        const double leg = c->legendre0[leg_idx(n, abs(m))];
+        const int y = n * (n + 1) + m;
+        double complex s = prefacn * Rpown * leg * cintres[n] * e_beta * e_imf * m1pow_m_neg(m);
+        ckahanadd(target + y, tc + y, s);
+        kahanadd(&lsum, &lsum_c, cabs(s));
+      }
+    }
+    ++li;
+    double cursum_min = INFINITY;
+    for (int y = 0; y < nelem_sc; ++y) {
+      const double a = cabs(target[y]);
+      if (a && a < cursum_min) cursum_min = a;
+    }
+    if (li >= 12 * lw + 1) {
+      if (lsum < DBL_EPSILON * cursum_min) break;
+      lsum = lsum_c = 0;
+      li = 0;
+      ++lw;
+    }
+  }
+  free(tc);
+}
+
+/* sigma = sigma_S + sigma_L (+ sigma0 when the shift vanishes), all nelem_sc */
+void orc_ewald3_sigma_xy(int lMax_e, int csphase, double eta, double complex k, orc_c2 b1, orc_c2 b2, orc_c2 beta,
+                         orc_c2 shift, double maxR, double maxK, int parts, double complex *sigma_out,
+                         double complex *sigma_short_out, double complex *sigma_long_out) {
+  e3c_t *c = e3c_init(lMax_e, csphase);
+  const int ne = c->nelem_sc;
+  const int do_sigma0 = (shift.x == 0 && shift.y == 0);
+  double complex *ss = calloc(ne, sizeof(double complex)), *sl = calloc(ne, sizeof(double complex));
+  const double A = orc_l2d_unitcell_area(b1, b2);
+  orc_c2 rb1, rb2;
+  orc_l2d_reciprocalBasis2pi(b1, b2, &rb1, &rb2);
+  if (parts & 1) sigma_long(c, sl, eta, k, A, rb1, rb2, maxK, beta, shift);
+  if (parts & 2) sigma_short(c, ss, eta, k, b1, b2, maxR, !do_sigma0, beta, shift);
+  for (int y = 0; y < ne; ++y) sigma_out[y] = ((parts & 2) ? ss[y] : 0) + ((parts & 1) ? sl[y] : 0);
+  if (do_sigma0 && (parts & 4)) sigma_out[0] += sigma0(c, eta, k);
+  if (sigma_short_out) memcpy(sigma_short_out, ss, sizeof(double complex) * ne);
+  if (sigma_long_out) memcpy(sigma_long_out, sl, sizeof(double complex) * ne);
+  free(ss);
+  free(sl);
+  e3c_free(c);
+}
+
+/* translations.c:926-1078 (with the q <= qmax_A bound of the B sum at :1048-1050) */
+int orc_trans_calculator_get_AB_arrays_e32(const orc_trans_calculator *c, double complex *Adest,
+                                           double complex *Bdest, size_t deststride, size_t srcstride, double eta,
+                                           double complex k, orc_c2 b1, orc_c2 b2, orc_c2 beta, orc_c2 shift,
+                                           double maxR, double maxK, int parts) {
+  const int lMax_e = 2 * c->lMax + 1, ne_sc = lMax_e * (lMax_e + 2) + 1;
+  const int csphase = (c->normalisation & 8) ? -1 : 1;
+  double complex *sig = malloc(sizeof(double complex) * ne_sc);
+  orc_ewald3_sigma_xy(lMax_e, csphase, eta, k, b1, b2, beta, shift, maxR, maxK, parts, sig, NULL, NULL);
+  size_t desti = 0, srci = 0;
+  for (int n = 1; n <= c->lMax; ++n)
+    for (int m = -n; m <= n; ++m) {
+      for (int nu = 1; nu <= c->lMax; ++nu)
+        for (int mu = -nu; mu <= nu; ++mu) {
+          const size_t i = (size_t)c->nelem * (n * (n + 1) + m - 1) + (nu * (nu + 1) + mu - 1);
+          const size_t qmax = c->A_multipliers[i + 1] - c->A_multipliers[i] - 1;
+          double complex As = 0, Asc = 0, Bs = 0, Bsc = 0;
+          for (size_t q = 0; q <= qmax; ++q) {
+            const int p = n + nu - 2 * (int)q;
+            ckahanadd(&As, &Asc, c->A_multipliers[i][q] * sig[p * (p + 1) + mu - m]);
+          }
+          for (size_t q = 0; q <= qmax; ++q) {
+            const int p_ = n + nu - 2 * (int)q + 1;
+            ckahanadd(&Bs, &Bsc, c->B_multipliers[i][q] * sig[p_ * (p_ + 1) + mu - m]);
+          }
+          Adest[deststride * desti + srcstride * srci] = As;
+          Bdest[deststride * desti + srcstride * srci] = Bs;
+          ++srci;
+        }
+      ++desti;
+      srci = 0;
+    }
+  free(sig);
+  return 0;
+}
+
+/* scatsystem.c:68-80 with the default eta of scatsystem.c:194-207 */
+double orc_adjusted_eta(double unitcell_area, double complex wavenumber, const double kvec[3], int lMax) {
+  const double eta_default = ORC_SQRTPI / sqrt(unitcell_area);
+  const double k2 = kvec[0] * kvec[0] + kvec[1] * kvec[1] + kvec[2] * kvec[2];
+  const double kappa2 = sq(cabs(wavenumber));
+  if (kappa2 < k2) return eta_default;
+  const double mina = 0.5 * (2 - 1) - lMax;
+  const double eta_min = sqrt(fabs((kappa2 - k2) * (mina - 1.) / 16.));
+  return eta_default > eta_min ? eta_default : eta_min;
+}
+
+/* Periodic M = I - T W for np particles per cell with a common full bspec;
+ * W(R <- C) from the e32 sums with particle_shift = pos_R - pos_C,
+ * maxR = 64 sqrt(A), maxK = 2048 * 2 pi / maxR (scatsystem.c:1219-1237). */
+int orc_periodic_modeproblem(const orc_trans_calculator *c, int np, const double *pos, const double complex *T,
+                             double complex k, orc_c2 b1, orc_c2 b2, const double kvec[2], double eta,
+                             double complex *M) {
+  const int ne = c->nelem, n = 2 * ne;
+  const size_t N = (size_t)np * n;
+  const double A = orc_l2d_unitcell_area(b1, b2);
+  const double maxR = sqrt(A) * 64, maxK = 2048 * 2 * M_PI / maxR;
+  double complex *Am = malloc(sizeof(double complex) * ne * ne), *Bm = malloc(sizeof(double complex) * ne * ne);
+  double complex *W = malloc(sizeof(double complex) * n * n);
+  orc_c2 beta = {kvec[0], kvec[1]};
+  memset(M, 0, sizeof(double complex) * N * N);
+  for (int R = 0; R < np; ++R)
+    for (int Cc = 0; Cc < np; ++Cc) {
+      orc_c2 shift = {pos[3 * R] - pos[3 * Cc], pos[3 * R + 1] - pos[3 * Cc + 1]};
+      orc_trans_calculator_get_AB_arrays_e32(c, Am, Bm, ne, 1, eta, k, b1, b2, beta, shift, maxR, maxK, 7);
+      for (int ti = 0; ti < 2; ++ti)
+        for (int yi = 0; yi < ne; ++yi)
+          for (int tj = 0; tj < 2; ++tj)
+            for (int yj = 0; yj < ne; ++yj)
+              W[(ti * ne + yi) * n + tj * ne + yj] = (ti == tj) ? Am[yi * ne + yj] : Bm[yi * ne + yj];
+      const double complex *TR = T + (size_t)R * n * n;
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+          double complex s = 0;
+          for (int q = 0; q < n; ++q) s += TR[i * n + q] * W[q * n + j];
+          M[((size_t)R * n + i) * N + (size_t)Cc * n + j] = -s;
+        }
+    }
+  for (size_t i = 0; i < N; ++i) M[i * N + i] += 1;
+  free(Am);
+  free(Bm);
+  free(W);
+  return 0;
+}
+
+/* ---- plain-argument shims for ctypes ---- */
+void orc_ewald3_sigma_xy_ri(int lMax_e, int csphase, double eta, double kr, double ki, const double *b12,
+                            const double *beta, const double *shift, double maxR, double maxK, int parts,
+                            double complex *sig, double complex *ss, double complex *sl) {
+  orc_c2 b1 = {b12[0], b12[1]}, b2 = {b12[2], b12[3]}, be = {beta[0], beta[1]}, sh = {shift[0], shift[1]};
+  orc_ewald3_sigma_xy(lMax_e, csphase, eta, kr + I * ki, b1, b2, be, sh, maxR, maxK, parts, sig, ss, sl);
+}
+int orc_get_AB_arrays_e32_ri(const orc_trans_calculator *c, double complex *A, double complex *B, double eta,
+                             double kr, double ki, const double *b12, const double *beta, const double *shift,
+                             double maxR, double maxK, int parts) {
+  orc_c2 b1 = {b12[0], b12[1]}, b2 = {b12[2], b12[3]}, be = {beta[0], beta[1]}, sh = {shift[0], shift[1]};
+  return orc_trans_calculator_get_AB_arrays_e32(c, A, B, c->nelem, 1, eta, kr + I * ki, b1, b2, be, sh, maxR, maxK,
+                                                parts);
+}
+int orc_periodic_modeproblem_ri(const orc_trans_calculator *c, int np, const double *pos, const double complex *T,
+                                double kr, double ki, const double *b12, const double *kvec, double eta,
+                                double complex *M) {
+  orc_c2 b1 = {b12[0], b12[1]}, b2 = {b12[2], b12[3]};
+  return orc_periodic_modeproblem(c, np, pos, T, kr + I * ki, b1, b2, kvec, eta, M);
+}
+void orc_complex_gamma_inc_ri(double a, double xr, double xi, int m, double complex *out) {
+  *out = orc_complex_gamma_inc(a, xr + I * xi, m);
+}
+void orc_ewald_sr_integral_ri(double r, double kr, double ki, int n, double eta, double complex *out) {
+  *out = orc_ewald_sr_integral(r, kr + I * ki, n, eta);
+}

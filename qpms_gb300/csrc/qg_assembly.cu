@@ -143,35 +143,36 @@ __global__ void __launch_bounds__(kAThreads) assemble_kernel(AsmArgs a, TransDev
       const qg_c *wv = w + v * S;
       const int tmR = a.tmid[inf.R];
       const qg_c *TR = a.T + ((size_t)inf.w * a.ntm + tmR) * (DENSE ? NB * NB : NB);
-      for (int k = tid; k < NE2; k += kAThreads) {
-        const int ca = T.cntA[k], cb = T.cntB[k];
-        double ar = 0, ai = 0, br = 0, bi = 0;
-        for (int q = 0; q < ca; ++q) {
-          const double c = __ldg(T.coefA + q * NE2 + k);
-          const qg_c x = wv[__ldg(T.slotA + q * NE2 + k)];
-          ar = fma(c, x.re, ar);
-          ai = fma(c, x.im, ai);
-        }
-        for (int q = 0; q < cb; ++q) {
-          const double c = __ldg(T.coefB + q * NE2 + k);
-          const qg_c x = wv[__ldg(T.slotB + q * NE2 + k)];
-          br = fma(c, x.re, br);
-          bi = fma(c, x.im, bi);
-        }
-        const qg_c A = cmk(ar, ai), B = cmk(-bi, br);  // B multipliers are imaginary
-        const int e = __ldg(T.perm + k);
-        const int yi = e / NE, yj = e - yi * NE;
-        if (DENSE) {
-          sblk[yi * NB + yj] = A;
-          sblk[(NE + yi) * NB + NE + yj] = A;
-          sblk[yi * NB + NE + yj] = B;
-          sblk[(NE + yi) * NB + yj] = B;
-        } else {
-          const qg_c tE = TR[yi], tM = TR[NE + yi];
-          M[(row0 + yi) * N + col0 + yj] = cscale(cmul(tE, A), -1.0);
-          M[(row0 + NE + yi) * N + col0 + NE + yj] = cscale(cmul(tM, A), -1.0);
-          M[(row0 + yi) * N + col0 + NE + yj] = cscale(cmul(tE, B), -1.0);
-          M[(row0 + NE + yi) * N + col0 + yj] = cscale(cmul(tM, B), -1.0);
+      // A and B each in their own term-count order; each value lands in two
+      // blocks of the (electric, magnetic) type structure
+#pragma unroll 1
+      for (int which = 0; which < 2; ++which) {
+        const uint8_t *cnt = which ? T.cntB : T.cntA;
+        const double *coef = which ? T.coefB : T.coefA;
+        const uint16_t *slot = which ? T.slotB : T.slotA;
+        const int32_t *perm = which ? T.permB : T.perm;
+        for (int k = tid; k < NE2; k += kAThreads) {
+          const int c = cnt[k];
+          double sr = 0, si = 0;
+          for (int q = 0; q < c; ++q) {
+            const double cf = __ldg(coef + q * NE2 + k);
+            const qg_c x = wv[__ldg(slot + q * NE2 + k)];
+            sr = fma(cf, x.re, sr);
+            si = fma(cf, x.im, si);
+          }
+          const qg_c v = which ? cmk(-si, sr) : cmk(sr, si);  // B multipliers are imaginary
+          const int e = __ldg(perm + k);
+          const int yi = e / NE, yj = e - yi * NE;
+          // A: (E <- E) and (M <- M) blocks; B: (E <- M) and (M <- E) blocks
+          const int r1 = yi, c1 = which ? NE + yj : yj;
+          const int r2 = NE + yi, c2 = which ? yj : NE + yj;
+          if (DENSE) {
+            sblk[r1 * NB + c1] = v;
+            sblk[r2 * NB + c2] = v;
+          } else {
+            M[(row0 + r1) * N + col0 + c1] = cscale(cmul(TR[r1], v), -1.0);
+            M[(row0 + r2) * N + col0 + c2] = cscale(cmul(TR[r2], v), -1.0);
+          }
         }
       }
       if (DENSE) {
@@ -225,8 +226,8 @@ int launch_asm(const AsmArgs &a, const TransDevTables &T, cudaStream_t st) {
 // ---------------- small pipeline kernels ----------------
 
 // a[w][p*n + i] = coef[i] * exp(i kvec_w . r_p)
-__global__ void incident_kernel(int nw, int np, int n, const qg_c *coef, const double *kvec, const double *pos,
-                                qg_c *a) {
+__global__ void incident_kernel(int nw, int np, int n, const qg_c *coef, size_t coef_stride, const double *kvec,
+                                const double *pos, qg_c *a) {
   const size_t N = (size_t)np * n, tot = (size_t)nw * N;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < tot; t += (size_t)gridDim.x * blockDim.x) {
     const int w = (int)(t / N);
@@ -235,7 +236,7 @@ __global__ void incident_kernel(int nw, int np, int n, const qg_c *coef, const d
     const double ph = kvec[3 * w] * pos[3 * p] + kvec[3 * w + 1] * pos[3 * p + 1] + kvec[3 * w + 2] * pos[3 * p + 2];
     double s, c;
     sincos(ph, &s, &c);
-    a[t] = cmul(coef[i], cmk(c, s));
+    a[t] = cmul(coef[(size_t)w * coef_stride + i], cmk(c, s));
   }
 }
 
@@ -372,8 +373,8 @@ int launch_assemble(const AsmArgs &a, const TransDevTables &T, cudaStream_t st) 
 }
 
 int launch_incident(int nw, int np, int n, const qg_c *coef, const double *kvec, const double *pos, qg_c *a,
-                    cudaStream_t st) {
-  incident_kernel<<<grid_for((size_t)nw * np * n, 256), 256, 0, st>>>(nw, np, n, coef, kvec, pos, a);
+                    cudaStream_t st, size_t coef_stride) {
+  incident_kernel<<<grid_for((size_t)nw * np * n, 256), 256, 0, st>>>(nw, np, n, coef, coef_stride, kvec, pos, a);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(1);
   return QPMS_SUCCESS;

@@ -21,8 +21,9 @@ struct AsmArgs {
 };
 
 int launch_assemble(const AsmArgs &a, const TransDevTables &T, cudaStream_t st);
+// a[w][p n + i] = coef[w coef_stride + i] exp(i kvec_w . r_p)
 int launch_incident(int nw, int np, int n, const qg_c *coef, const double *kvec, const double *pos, qg_c *a,
-                    cudaStream_t st);
+                    cudaStream_t st, size_t coef_stride = 0);
 int launch_apply_t(int nw, int np, int n, int ntm, int dense, const int *tmid, const qg_c *T, const qg_c *a,
                    qg_c *b, cudaStream_t st);
 int launch_residual(int nw, size_t N, const qg_c *M, const qg_c *x, const qg_c *b, qg_c *r, double *rn2,

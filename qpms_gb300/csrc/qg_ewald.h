@@ -1,0 +1,45 @@
+// Device-side Ewald lattice sums (qg_ewald.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "qg_internal.h"
+
+namespace qg {
+
+// Largest sigma order lMax_e = 2 lMax + 1 compiled (lMax <= 4).
+constexpr int kEwLE = 9;
+constexpr int kEwS = (kEwLE + 1) * (kEwLE + 1);
+
+// Lattice- and convention-dependent constants (one lattice at a time).
+struct EwaldConst {
+  double b[4];    // direct basis b1 (x, y), b2 (x, y)
+  double rb[4];   // reciprocal basis (2 pi normalised)
+  double bn[2];   // |b1|, |b2|
+  double rbn[2];  // |rb1|, |rb2|
+  double area;    // unit cell area
+  // P_n^{|m|}(0) (-1)^{m<0 ? m : 0} per y = n(n+1) + m (ewald.c:425, 877, 886)
+  double leg0m[kEwS];
+  // long-range constants s1_constfacs[y][j] (ewald.c:142-146) times leg0m[y]
+  int s1off[kEwS];
+  qg_c s1[kEwS * (kEwLE / 2 + 1)];
+};
+
+struct EwaldArgs {
+  int nw, nk, np, ntm;
+  const double *pos;   // [np][3]
+  const int *tmid;     // [np]
+  const qg_c *T;       // [nw][ntm][n] diagonal T-matrices
+  const qg_c *k;       // [nw] medium wavenumbers
+  const double *beta;  // [nk][2] Bloch vectors
+  const double *eta;   // [nw * nk] Ewald parameters
+  qg_c *M;             // [nw * nk][N][N]
+  int *err;            // set to 1 if a unit's lattice-point range exceeded the bound
+};
+
+// Bound on the lattice points one unit may enumerate per sum.
+constexpr long kEwMaxPoints = 1L << 22;
+
+int ewald_upload_constants(const EwaldConst &c, cudaStream_t st);
+int launch_ewald_assemble(const EwaldArgs &a, const TransDevTables &T, cudaStream_t st);
+
+}  // namespace qg

@@ -26,6 +26,16 @@ extern std::atomic<unsigned long long> g_launches;
     }                                                                                \
   } while (0)
 
+// cuBLAS calls (CUBLAS_STATUS_SUCCESS == 0)
+#define QG_BLAS_TRY(expr)                                                                \
+  do {                                                                                   \
+    int _s = (int)(expr);                                                                \
+    if (_s != 0) {                                                                       \
+      qg::set_error("%s:%d: %s: cublas status %d", __FILE__, __LINE__, #expr, _s);      \
+      return QPMS_ERROR;                                                                 \
+    }                                                                                    \
+  } while (0)
+
 // ---- translation tables (qg_tables.cu) ----
 
 // Largest lMax with a compiled translation kernel.
@@ -36,9 +46,12 @@ struct TransHostTables {
   // reference-layout ragged multipliers (complex), row-major over (y, yu)
   std::vector<qg_c> A_mult, B_mult;
   std::vector<size_t> A_off, B_off;  // nelem^2 + 1 offsets
-  // kernel tables, element e = y * nelem + yu, in "sorted" order k:
-  std::vector<int32_t> perm;         // k -> e
+  // kernel tables, element e = y * nelem + yu; A and B each in their own
+  // term-count order k (permA / permB: k -> e)
+  std::vector<int32_t> perm, permB;
   std::vector<uint8_t> cntA, cntB;   // per k
+  std::vector<uint8_t> cntBe;        // B order: min(cntB, cntA of the same element), the
+                                     // q <= qmax_A bound of the lattice-sum contraction
   std::vector<double> coefA, coefB;  // [q][k]: A real part, B imaginary part
   std::vector<uint16_t> slotA, slotB;  // [q][k]: w-table slot p^2 + p + d
 };
@@ -49,8 +62,8 @@ bool build_trans_tables(int lMax, int normalisation, TransHostTables *t);
 // Device copy of the kernel tables.
 struct TransDevTables {
   int lMax, nelem, ne2, tq;
-  const int32_t *perm;
-  const uint8_t *cntA, *cntB;
+  const int32_t *perm, *permB;
+  const uint8_t *cntA, *cntB, *cntBe;
   const double *coefA, *coefB;
   const uint16_t *slotA, *slotB;
 };

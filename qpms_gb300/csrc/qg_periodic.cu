@@ -1,0 +1,369 @@
+// Periodic (2D lattice) systems: Ewald parameter, the drop-in
+// qpms_scatsyswk_build_modeproblem_matrix_full[_LU], and the batched
+// dispersion scan (assembly over (omega, Bloch vector) -> LU -> log|det| ->
+// plane-wave excitation).
+#include <cublas_v2.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "qg_assembly.h"
+#include "qg_ewald.h"
+#include "qg_internal.h"
+#include "qg_specfunc.cuh"
+
+namespace qg {
+bool scatsys_is_own(const qpms_scatsys_t *ss);
+int scatsys_lmax(const qpms_scatsys_t *ss);
+void scatsys_tdiag(const qpms_scatsys_t *ss, int t, double om_re, double om_im, std::vector<qg_c> &out);
+qg_c scatsys_wavenumber(const qpms_scatsys_t *ss, double om_re, double om_im);
+void planewave_direction_coeffs(int lMax, const double k_dir[3], const qpms_complex_t E_cart[3],
+                                std::vector<qg_c> &coef);
+int blas_handle_get(cublasHandle_t *h);
+
+namespace {
+
+struct Dev {
+  void *p = nullptr;
+  ~Dev() {
+    if (p) cudaFree(p);
+  }
+  template <typename T>
+  T *as() const {
+    return reinterpret_cast<T *>(p);
+  }
+};
+int dalloc(Dev &b, size_t bytes) {
+  QG_CUDA_TRY(cudaMalloc(&b.p, bytes ? bytes : 16));
+  return QPMS_SUCCESS;
+}
+
+double fact(int n) {
+  double f = 1;
+  for (int i = 2; i <= n; ++i) f *= i;
+  return f;
+}
+
+// Lattice constants of the Ewald kernel (ewald.c:104-157, 228-241).
+int build_ewald_const(const qpms_scatsys_t *ss, int lMax, EwaldConst *c) {
+  const int LE = 2 * lMax + 1;
+  if (LE > kEwLE) {
+    set_error("periodic systems support lMax <= %d", (kEwLE - 1) / 2);
+    return QPMS_EINVAL;
+  }
+  memset(c, 0, sizeof *c);
+  const cart3_t b1 = ss->per.lattice_basis[0], b2 = ss->per.lattice_basis[1];
+  c->b[0] = b1.x; c->b[1] = b1.y; c->b[2] = b2.x; c->b[3] = b2.y;
+  const double det = b1.x * b2.y - b1.y * b2.x;
+  c->rb[0] = 2 * M_PI * b2.y / det;
+  c->rb[1] = -2 * M_PI * b2.x / det;
+  c->rb[2] = -2 * M_PI * b1.y / det;
+  c->rb[3] = 2 * M_PI * b1.x / det;
+  c->bn[0] = hypot(c->b[0], c->b[1]);
+  c->bn[1] = hypot(c->b[2], c->b[3]);
+  c->rbn[0] = hypot(c->rb[0], c->rb[1]);
+  c->rbn[1] = hypot(c->rb[2], c->rb[3]);
+  c->area = fabs(det);
+  std::vector<double> P((LE + 1) * (LE + 2) / 2);
+  for (int m = 0; m <= LE; ++m) legendre_column(LE, m, 0.0, P.data());  // csphase -1 (default normalisation)
+  int off = 0;
+  for (int n = 0; n <= LE; ++n)
+    for (int m = -n; m <= n; ++m) {
+      const int y = n * (n + 1) + m, am = m < 0 ? -m : m;
+      const double sgn = (m < 0 && (m % 2)) ? -1.0 : 1.0;
+      c->leg0m[y] = P[n * (n + 1) / 2 + am] * sgn;
+      c->s1off[y] = off;
+      if ((m + n) % 2 == 0) {
+        static const double ipr[4][2] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}};
+        const double *ip = ipr[(n + 1) % 4];
+        for (int j = 0; j <= (n - am) / 2; ++j) {
+          const double f = -2 * 1.7724538509055160273 * fact((n - m) / 2) * fact((n + m) / 2) * ((j % 2) ? -1 : 1) /
+                           (fact(j) * fact((n - m) / 2 - j) * fact((n + m) / 2 - j)) * c->leg0m[y];
+          c->s1[off + j] = cmk(f * ip[0], f * ip[1]);
+        }
+        off += (n - am) / 2 + 1;
+      }
+    }
+  return QPMS_SUCCESS;
+}
+
+// log|det| of nb row-major N x N LU factors (column-major getrf of M^T has
+// the same diagonal of U)
+__global__ void logdet_kernel(int nb, int N, const qg_c *LU, double *out) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const qg_c *A = LU + (size_t)b * N * N;
+  double s = 0;
+  for (int i = 0; i < N; ++i) s += log(hypot(A[(size_t)i * N + i].re, A[(size_t)i * N + i].im));
+  out[b] = s;
+}
+
+}  // namespace
+}  // namespace qg
+
+using namespace qg;
+
+extern "C" {
+
+double qpms_ss_adjusted_eta(const qpms_scatsys_t *ss, qpms_complex_t wavenumber, const double wavevector[3]) {
+  // scatsystem.c:68-80
+  const double eta_default = ss->per.eta;
+  const double k2 = wavevector[0] * wavevector[0] + wavevector[1] * wavevector[1] + wavevector[2] * wavevector[2];
+  const double kappa2 = wavenumber.re * wavenumber.re + wavenumber.im * wavenumber.im;
+  if (kappa2 < k2) return eta_default;
+  const int maxj = ss->c->lMax;
+  const double mina = 0.5 * (ss->lattice_dimension - 1) - maxj;
+  const double eta_min = sqrt(fabs((kappa2 - k2) * (mina - 1.) / 16.));
+  return std::max(eta_default, eta_min);
+}
+
+// Batched periodic assembly into device memory: nw frequencies x nk Bloch vectors.
+static int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_host,
+                                    const std::vector<qg_c> &T_host, int nk, const double *beta_host,
+                                    const double *eta_host, qg_c *dM, cudaStream_t st) {
+  const int lMax = ss->c->lMax, np = ss->p_count;
+  EwaldConst ec;
+  int e;
+  if ((e = build_ewald_const(ss, lMax, &ec))) return e;
+  if ((e = ewald_upload_constants(ec, st))) return e;
+  std::vector<double> pos(3 * np);
+  std::vector<int> tm(np);
+  for (int i = 0; i < np; ++i) {
+    pos[3 * i] = ss->p[i].pos.x;
+    pos[3 * i + 1] = ss->p[i].pos.y;
+    pos[3 * i + 2] = ss->p[i].pos.z;
+    tm[i] = ss->p[i].tmatrix_id;
+    if (ss->p[i].pos.z != ss->p[0].pos.z) {
+      set_error("particles must share one z plane (xy lattice sums)");
+      return QPMS_EINVAL;
+    }
+  }
+  // the Ewald parameter sets how many lattice points each sum visits
+  for (size_t i = 0; i < (size_t)nw * nk; ++i)
+    if (!(eta_host[i] >= 0.05 * ss->per.eta && eta_host[i] <= 50 * ss->per.eta)) {
+      set_error("Ewald eta %g outside [0.05, 50] x the lattice default %g", eta_host[i], ss->per.eta);
+      return QPMS_EINVAL;
+    }
+  Dev dpos, dtm, dT, dk, dbeta, deta, derr;
+  if ((e = dalloc(derr, 4))) return e;
+  QG_CUDA_TRY(cudaMemsetAsync(derr.p, 0, 4, st));
+  if ((e = dalloc(dpos, pos.size() * 8)) || (e = dalloc(dtm, np * 4)) || (e = dalloc(dT, T_host.size() * 16)) ||
+      (e = dalloc(dk, nw * 16)) || (e = dalloc(dbeta, nk * 16)) || (e = dalloc(deta, (size_t)nw * nk * 8)))
+    return e;
+  QG_CUDA_TRY(cudaMemcpyAsync(dpos.p, pos.data(), pos.size() * 8, cudaMemcpyHostToDevice, st));
+  QG_CUDA_TRY(cudaMemcpyAsync(dtm.p, tm.data(), np * 4, cudaMemcpyHostToDevice, st));
+  QG_CUDA_TRY(cudaMemcpyAsync(dT.p, T_host.data(), T_host.size() * 16, cudaMemcpyHostToDevice, st));
+  QG_CUDA_TRY(cudaMemcpyAsync(dk.p, k_host, nw * 16, cudaMemcpyHostToDevice, st));
+  QG_CUDA_TRY(cudaMemcpyAsync(dbeta.p, beta_host, nk * 16, cudaMemcpyHostToDevice, st));
+  QG_CUDA_TRY(cudaMemcpyAsync(deta.p, eta_host, (size_t)nw * nk * 8, cudaMemcpyHostToDevice, st));
+  EwaldArgs a;
+  a.nw = nw;
+  a.nk = nk;
+  a.np = np;
+  a.ntm = ss->tm_count;
+  a.pos = dpos.as<double>();
+  a.tmid = dtm.as<int>();
+  a.T = dT.as<qg_c>();
+  a.k = dk.as<qg_c>();
+  a.beta = dbeta.as<double>();
+  a.eta = deta.as<double>();
+  a.M = dM;
+  a.err = derr.as<int>();
+  if ((e = launch_ewald_assemble(a, priv(ss->c)->dev, st))) return e;
+  int herr = 0;
+  QG_CUDA_TRY(cudaMemcpyAsync(&herr, derr.p, 4, cudaMemcpyDeviceToHost, st));
+  QG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr) {
+    set_error("Ewald sum: lattice-point range above the bound (wavenumber or eta out of range)");
+    return QPMS_ERROR;
+  }
+  return QPMS_SUCCESS;
+}
+
+qpms_complex_t *qpms_scatsyswk_build_modeproblem_matrix_full(qpms_complex_t *target,
+                                                             const qpms_scatsys_at_omega_k_t *sswk) {
+  clear_error();
+  if (!sswk || !sswk->ssw) { set_error("NULL sswk"); return nullptr; }
+  const qpms_scatsys_at_omega_t *ssw = sswk->ssw;
+  const qpms_scatsys_t *ss = ssw->ss;
+  if (ss->lattice_dimension != 2) { set_error("only 2D lattices are supported"); return nullptr; }
+  if (sswk->k[2] != 0) { set_error("Bloch vector must lie in the xy plane"); return nullptr; }
+  const size_t N = ss->fecv_size, n = ssw->tm[0]->spec->n;
+  std::vector<qg_c> T;
+  for (int t = 0; t < ss->tm_count; ++t)
+    for (size_t i = 0; i < n; ++i) {
+      for (size_t j = 0; j < n; ++j)
+        if (i != j && (ssw->tm[t]->m[i * n + j].re != 0 || ssw->tm[t]->m[i * n + j].im != 0)) {
+          set_error("periodic assembly supports diagonal T-matrices");
+          return nullptr;
+        }
+      T.push_back(*(const qg_c *)&ssw->tm[t]->m[i * n + i]);
+    }
+  const qg_c k = *(const qg_c *)&ssw->wavenumber;
+  double eta = sswk->eta;
+  if (eta == 0 || isnan(eta)) eta = qpms_ss_adjusted_eta(ss, ssw->wavenumber, sswk->k);
+  const double beta[2] = {sswk->k[0], sswk->k[1]};
+  Dev dM;
+  if (dalloc(dM, N * N * 16)) return nullptr;
+  if (periodic_assemble_device(ss, 1, &k, T, 1, beta, &eta, dM.as<qg_c>(), 0)) return nullptr;
+  bool own = false;
+  if (!target) {
+    target = (qpms_complex_t *)malloc(N * N * 16);
+    own = true;
+  }
+  if (cudaMemcpy(target, dM.p, N * N * 16, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    set_error("device to host copy failed");
+    if (own) free(target);
+    return nullptr;
+  }
+  return target;
+}
+
+qpms_ss_LU qpms_scatsyswk_build_modeproblem_matrix_full_LU(qpms_complex_t *target, int *target_piv,
+                                                           const qpms_scatsys_at_omega_k_t *sswk) {
+  qpms_complex_t *M = qpms_scatsyswk_build_modeproblem_matrix_full(target, sswk);
+  if (!M) {
+    qpms_ss_LU lu;
+    memset(&lu, 0, sizeof lu);
+    return lu;
+  }
+  return qpms_scatsysw_modeproblem_matrix_full_factorise(M, target_piv, sswk->ssw, sswk);
+}
+
+int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *omegas, size_t nk,
+                           const double *kvecs, double *logdet, qpms_complex_t *f_out, double *sigma_ext,
+                           double *resid_out) {
+  clear_error();
+  if (!scatsys_is_own(ss) || ss->lattice_dimension != 2) {
+    set_error("system must come from qpms_gpu_scatsys_create_spheres_2d");
+    return QPMS_EINVAL;
+  }
+  if (!omegas || !kvecs || !logdet) { set_error("NULL argument"); return QPMS_EINVAL; }
+  if (!nw || !nk) return QPMS_SUCCESS;
+  const int lMax = scatsys_lmax(ss), np = ss->p_count, ntm = ss->tm_count, n = 2 * lMax * (lMax + 2);
+  const size_t N = ss->fecv_size, N2 = N * N;
+  cublasHandle_t h;
+  int e;
+  if ((e = blas_handle_get(&h))) return e;
+  QG_BLAS_TRY(cublasSetStream(h, 0));
+  // process in chunks of whole frequencies, <= ~2 GiB of matrices per chunk
+  const size_t per_w = nk * N2 * 16;
+  const int wchunk = (int)std::max<size_t>(1, std::min<size_t>(nw, (size_t(2) << 30) / per_w));
+  std::vector<qg_c> coef;
+  std::vector<double> pos(3 * np);
+  std::vector<int> tm(np);
+  for (int i = 0; i < np; ++i) {
+    pos[3 * i] = ss->p[i].pos.x;
+    pos[3 * i + 1] = ss->p[i].pos.y;
+    pos[3 * i + 2] = ss->p[i].pos.z;
+    tm[i] = ss->p[i].tmatrix_id;
+  }
+  Dev dM, dLU, dpiv, dinfo, darr, darrb, dlog, dT, dtm, dpos, dk, dkv, dcoef, da, db, dx, dr, dn, dsig;
+  const size_t nmat = (size_t)wchunk * nk;
+  if ((e = dalloc(dM, nmat * N2 * 16)) || (e = dalloc(dLU, nmat * N2 * 16)) || (e = dalloc(dpiv, nmat * N * 4)) ||
+      (e = dalloc(dinfo, nmat * 4)) || (e = dalloc(darr, nmat * 8)) || (e = dalloc(darrb, nmat * 8)) ||
+      (e = dalloc(dlog, nmat * 8)) || (e = dalloc(dtm, np * 4)) || (e = dalloc(dpos, np * 24)) ||
+      (e = dalloc(da, nmat * N * 16)) || (e = dalloc(db, nmat * N * 16)) || (e = dalloc(dx, nmat * N * 16)) ||
+      (e = dalloc(dr, nmat * N * 16)) || (e = dalloc(dn, nmat * 16)) || (e = dalloc(dsig, nmat * 8)) ||
+      (e = dalloc(dk, nmat * 16)) || (e = dalloc(dkv, nmat * 24)) || (e = dalloc(dT, nmat * ntm * n * 16)))
+    return e;
+  QG_CUDA_TRY(cudaMemcpy(dtm.p, tm.data(), np * 4, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpy(dpos.p, pos.data(), np * 24, cudaMemcpyHostToDevice));
+  {
+    std::vector<void *> pa(nmat), pb(nmat);
+    for (size_t i = 0; i < nmat; ++i) {
+      pa[i] = dLU.as<char>() + i * N2 * 16;
+      pb[i] = dx.as<char>() + i * N * 16;
+    }
+    QG_CUDA_TRY(cudaMemcpy(darr.p, pa.data(), nmat * 8, cudaMemcpyHostToDevice));
+    QG_CUDA_TRY(cudaMemcpy(darrb.p, pb.data(), nmat * 8, cudaMemcpyHostToDevice));
+  }
+  for (size_t w0 = 0; w0 < nw; w0 += wchunk) {
+    const int W = (int)std::min<size_t>(wchunk, nw - w0);
+    const size_t nm = (size_t)W * nk;
+    std::vector<qg_c> T, k(W), kk(nm), Tm;
+    std::vector<double> eta(nm), kvec(3 * nm);
+    std::vector<qg_c> coefs(nm * n);
+    for (int w = 0; w < W; ++w) {
+      for (int t = 0; t < ntm; ++t) {
+        std::vector<qg_c> d;
+        scatsys_tdiag(ss, t, omegas[w0 + w], 0.0, d);
+        T.insert(T.end(), d.begin(), d.end());
+      }
+      k[w] = scatsys_wavenumber(ss, omegas[w0 + w], 0.0);
+      const double kap = k[w].re;
+      for (size_t ik = 0; ik < nk; ++ik) {
+        const size_t m = (size_t)w * nk + ik;
+        const double kv[3] = {kvecs[2 * ik], kvecs[2 * ik + 1], 0.0};
+        eta[m] = qpms_ss_adjusted_eta(ss, *(const qpms_complex_t *)&k[w], kv);
+        kk[m] = k[w];
+        // incident plane wave with in-plane wavevector beta, E along x projected
+        // perpendicular to k (x-polarised at normal incidence)
+        const double b2 = kv[0] * kv[0] + kv[1] * kv[1];
+        const double kz = kap * kap > b2 ? sqrt(kap * kap - b2) : 0.0;
+        const double kd[3] = {kv[0], kv[1], kz};
+        const double kn = sqrt(b2 + kz * kz);
+        double E[3] = {1, 0, 0};
+        const double ex = kd[0] / kn;
+        for (int c = 0; c < 3; ++c) E[c] -= ex * kd[c] / kn;
+        const double En = sqrt(E[0] * E[0] + E[1] * E[1] + E[2] * E[2]);
+        qpms_complex_t Ec[3];
+        for (int c = 0; c < 3; ++c) Ec[c] = {E[c] / En, 0.0};
+        std::vector<qg_c> cf;
+        planewave_direction_coeffs(lMax, kd, Ec, cf);
+        const bool prop = kap * kap > b2;
+        for (int i = 0; i < n; ++i) coefs[m * n + i] = prop ? cf[i] : cmk(0, 0);
+        for (int c = 0; c < 3; ++c) kvec[3 * m + c] = kd[c];
+        for (int t = 0; t < ntm; ++t) Tm.insert(Tm.end(), T.begin() + ((size_t)w * ntm + t) * n,
+                                                T.begin() + ((size_t)w * ntm + t + 1) * n);
+      }
+    }
+    if ((e = periodic_assemble_device(ss, W, k.data(), T, (int)nk, kvecs, eta.data(), dM.as<qg_c>(), 0))) return e;
+    QG_CUDA_TRY(cudaMemcpy(dLU.p, dM.p, nm * N2 * 16, cudaMemcpyDeviceToDevice));
+    // factorise M^T (the row-major buffer read column-major): same |det|
+    QG_BLAS_TRY(cublasZgetrfBatched(h, (int)N, darr.as<cuDoubleComplex *>(), (int)N, dpiv.as<int>(),
+                                    dinfo.as<int>(), (int)nm));
+    g_launches.fetch_add(1);
+    logdet_kernel<<<(unsigned)((nm + 127) / 128), 128>>>((int)nm, (int)N, dLU.as<qg_c>(), dlog.as<double>());
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+    QG_CUDA_TRY(cudaMemcpy(logdet + w0 * nk, dlog.p, nm * 8, cudaMemcpyDeviceToHost));
+    if (f_out || sigma_ext || resid_out) {
+      // per-matrix incidence: coefficients and phases differ per (w, k)
+      Dev dcf;
+      if ((e = dalloc(dcf, coefs.size() * 16))) return e;
+      QG_CUDA_TRY(cudaMemcpy(dcf.p, coefs.data(), coefs.size() * 16, cudaMemcpyHostToDevice));
+      QG_CUDA_TRY(cudaMemcpy(dkv.p, kvec.data(), nm * 24, cudaMemcpyHostToDevice));
+      QG_CUDA_TRY(cudaMemcpy(dk.p, kk.data(), nm * 16, cudaMemcpyHostToDevice));
+      QG_CUDA_TRY(cudaMemcpy(dT.p, Tm.data(), Tm.size() * 16, cudaMemcpyHostToDevice));
+      if ((e = launch_incident((int)nm, np, n, dcf.as<qg_c>(), dkv.as<double>(), dpos.as<double>(), da.as<qg_c>(), 0,
+                               (size_t)n)))
+        return e;
+      if ((e = launch_apply_t((int)nm, np, n, ntm, 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(), db.as<qg_c>(), 0)))
+        return e;
+      QG_CUDA_TRY(cudaMemcpy(dx.p, db.p, nm * N * 16, cudaMemcpyDeviceToDevice));
+      int info = 0;
+      QG_BLAS_TRY(cublasZgetrsBatched(h, CUBLAS_OP_T, (int)N, 1, darr.as<const cuDoubleComplex *>(), (int)N,
+                                      dpiv.as<int>(), darrb.as<cuDoubleComplex *>(), (int)N, &info, (int)nm));
+      g_launches.fetch_add(1);
+      double *rn2 = dn.as<double>(), *bn2 = rn2 + nm;
+      if ((e = launch_residual((int)nm, N, dM.as<qg_c>(), dx.as<qg_c>(), db.as<qg_c>(), dr.as<qg_c>(), rn2, bn2, 0)))
+        return e;
+      if ((e = launch_sigma_ext((int)nm, N, da.as<qg_c>(), dx.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), 0)))
+        return e;
+      if (sigma_ext) QG_CUDA_TRY(cudaMemcpy(sigma_ext + w0 * nk, dsig.p, nm * 8, cudaMemcpyDeviceToHost));
+      if (f_out) QG_CUDA_TRY(cudaMemcpy(f_out + w0 * nk * N, dx.p, nm * N * 16, cudaMemcpyDeviceToHost));
+      if (resid_out) {
+        std::vector<double> hr(nm), hb(nm);
+        QG_CUDA_TRY(cudaMemcpy(hr.data(), rn2, nm * 8, cudaMemcpyDeviceToHost));
+        QG_CUDA_TRY(cudaMemcpy(hb.data(), bn2, nm * 8, cudaMemcpyDeviceToHost));
+        for (size_t m = 0; m < nm; ++m) resid_out[w0 * nk + m] = hb[m] > 0 ? sqrt(hr[m] / hb[m]) : 0.0;
+      }
+    }
+  }
+  return QPMS_SUCCESS;
+}
+
+}  // extern "C"

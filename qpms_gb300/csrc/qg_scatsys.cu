@@ -56,14 +56,7 @@ int blas_handle(cublasHandle_t *h) {
   return QPMS_SUCCESS;
 }
 
-#define QG_BLAS_TRY(expr)                                              \
-  do {                                                                 \
-    cublasStatus_t _s = (expr);                                        \
-    if (_s != CUBLAS_STATUS_SUCCESS) {                                 \
-      qg::set_error("%s:%d: %s: cublas status %d", __FILE__, __LINE__, #expr, (int)_s); \
-      return QPMS_ERROR;                                               \
-    }                                                                  \
-  } while (0)
+
 
 // ---------------- Mie sphere T-matrix (tmatrices.c:500-561) ----------------
 template <int L>
@@ -272,6 +265,27 @@ int upload_particles(const qpms_scatsys_t *ss, DevBuf &dpos, DevBuf &dtm) {
 
 }  // namespace
 
+// Lagrange-Gauss reduction of a 2D basis (lattices2d.c:635-655 semantics).
+void lattice_reduce(double *b1, double *b2) {
+  auto dot = [](const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1]; };
+  double B1 = dot(b1, b1), mu = dot(b1, b2) / B1;
+  b2[0] -= round(mu) * b1[0];
+  b2[1] -= round(mu) * b1[1];
+  double B2 = dot(b2, b2);
+  while (B2 < B1) {
+    double t0 = b1[0], t1 = b1[1];
+    b1[0] = b2[0];
+    b1[1] = b2[1];
+    b2[0] = t0;
+    b2[1] = t1;
+    B1 = B2;
+    mu = dot(b1, b2) / B1;
+    b2[0] -= round(mu) * b1[0];
+    b2[1] -= round(mu) * b1[1];
+    B2 = dot(b2, b2);
+  }
+}
+
 // Accessors used by qg_solve.cu.
 bool scatsys_is_own(const qpms_scatsys_t *ss) { return ss && ss->medium.function == epsmu_const_fn; }
 int scatsys_lmax(const qpms_scatsys_t *ss) { return sspriv(ss)->lMax; }
@@ -338,9 +352,30 @@ using namespace qg;
 
 extern "C" {
 
+static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *kind, int nkinds,
+                                      const double *radius, const qpms_complex_t *eps_inside,
+                                      qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1, const double *b2);
+
 qpms_scatsys_t *qpms_gpu_scatsys_create_spheres(int np, const double *pos_xyz, const int *kind, int nkinds,
                                                 const double *radius, const qpms_complex_t *eps_inside,
                                                 qpms_complex_t eps_medium, qpms_l_t lMax) {
+  return create_spheres(np, pos_xyz, kind, nkinds, radius, eps_inside, eps_medium, lMax, nullptr, nullptr);
+}
+
+qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_2d(int np, const double *pos_xyz, const int *kind, int nkinds,
+                                                   const double *radius, const qpms_complex_t *eps_inside,
+                                                   qpms_complex_t eps_medium, qpms_l_t lMax, const double b1[2],
+                                                   const double b2[2]) {
+  if (!b1 || !b2) {
+    set_error("NULL lattice basis");
+    return nullptr;
+  }
+  return create_spheres(np, pos_xyz, kind, nkinds, radius, eps_inside, eps_medium, lMax, b1, b2);
+}
+
+static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *kind, int nkinds,
+                                      const double *radius, const qpms_complex_t *eps_inside,
+                                      qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1, const double *b2) {
   clear_error();
   if (np < 1 || !pos_xyz || nkinds < 1 || !radius || !eps_inside || lMax < 1 || lMax > 6) {
     set_error("invalid arguments (np >= 1, 1 <= lMax <= 6)");
@@ -391,6 +426,21 @@ qpms_scatsys_t *qpms_gpu_scatsys_create_spheres(int np, const double *pos_xyz, c
     double r = sqrt(pos_xyz[3 * i] * pos_xyz[3 * i] + pos_xyz[3 * i + 1] * pos_xyz[3 * i + 1] +
                     pos_xyz[3 * i + 2] * pos_xyz[3 * i + 2]);
     if (r > P.lenscale) P.lenscale = r;
+  }
+  if (b1) {
+    // scatsystem.c:187-214: reduced basis, reciprocal basis (without 2 pi),
+    // unit-cell area and the default Ewald eta = sqrt(pi / A)
+    double u1[2] = {b1[0], b1[1]}, u2[2] = {b2[0], b2[1]};
+    lattice_reduce(u1, u2);
+    const double det = u1[0] * u2[1] - u1[1] * u2[0];
+    if (det == 0) { set_error("degenerate lattice basis"); delete s; return nullptr; }
+    P.lattice_dimension = 2;
+    P.per.lattice_basis[0] = {u1[0], u1[1], 0};
+    P.per.lattice_basis[1] = {u2[0], u2[1], 0};
+    P.per.reciprocal_basis[0] = {u2[1] / det, -u2[0] / det, 0};
+    P.per.reciprocal_basis[1] = {-u1[1] / det, u1[0] / det, 0};
+    P.per.unitcell_volume = fabs(det);
+    P.per.eta = sqrt(M_PI) / sqrt(fabs(det));
   }
   P.c = qpms_trans_calculator_init(lMax, QPMS_NORMALISATION_DEFAULT);
   if (!P.c) {

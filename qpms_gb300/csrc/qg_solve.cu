@@ -30,14 +30,7 @@ int assemble_modeproblem_device(const qpms_scatsys_t *ss, int nw, const std::vec
 
 namespace {
 
-#define QG_BLAS_TRY(expr)                                                                \
-  do {                                                                                   \
-    cublasStatus_t _s = (expr);                                                          \
-    if (_s != CUBLAS_STATUS_SUCCESS) {                                                   \
-      qg::set_error("%s:%d: %s: cublas status %d", __FILE__, __LINE__, #expr, (int)_s); \
-      return QPMS_ERROR;                                                                 \
-    }                                                                                    \
-  } while (0)
+
 
 struct Dev {
   void *p = nullptr;

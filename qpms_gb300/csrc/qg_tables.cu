@@ -230,32 +230,34 @@ bool build_trans_tables(int lMax, int norm, TransHostTables *t) {
     for (ld v : cA[e]) t->A_mult.push_back(cmk((double)v, 0.0));
     for (ld v : cB[e]) t->B_mult.push_back(cmk(0.0, (double)v));
   }
-  // kernel order: by term count, descending, so a warp's lanes share trip counts
+  // kernel order: A and B elements each sorted by their own term count
+  // (descending), so the lanes of a warp share trip counts
   t->perm.resize(ne2);
+  t->permB.resize(ne2);
   std::iota(t->perm.begin(), t->perm.end(), 0);
-  std::stable_sort(t->perm.begin(), t->perm.end(), [&](int a, int b) {
-    size_t ka = cA[a].size() + cB[a].size(), kb = cA[b].size() + cB[b].size();
-    if (ka != kb) return ka > kb;
-    return cA[a].size() > cA[b].size();
-  });
+  std::iota(t->permB.begin(), t->permB.end(), 0);
+  std::stable_sort(t->perm.begin(), t->perm.end(), [&](int a, int b) { return cA[a].size() > cA[b].size(); });
+  std::stable_sort(t->permB.begin(), t->permB.end(), [&](int a, int b) { return cB[a].size() > cB[b].size(); });
   const int tq = t->tq;
   t->cntA.assign(ne2, 0);
   t->cntB.assign(ne2, 0);
+  t->cntBe.assign(ne2, 0);
   t->coefA.assign((size_t)tq * ne2, 0.0);
   t->coefB.assign((size_t)tq * ne2, 0.0);
   t->slotA.assign((size_t)tq * ne2, 0);
   t->slotB.assign((size_t)tq * ne2, 0);
   for (int k = 0; k < ne2; ++k) {
-    const int e = t->perm[k];
+    const int e = t->perm[k], eb = t->permB[k];
     t->cntA[k] = (uint8_t)cA[e].size();
-    t->cntB[k] = (uint8_t)cB[e].size();
+    t->cntB[k] = (uint8_t)cB[eb].size();
+    t->cntBe[k] = (uint8_t)std::min(cB[eb].size(), cA[eb].size());
     for (size_t q = 0; q < cA[e].size(); ++q) {
       t->coefA[q * ne2 + k] = (double)cA[e][q];
       t->slotA[q * ne2 + k] = (uint16_t)sA[e][q];
     }
-    for (size_t q = 0; q < cB[e].size(); ++q) {
-      t->coefB[q * ne2 + k] = (double)cB[e][q];
-      t->slotB[q * ne2 + k] = (uint16_t)sB[e][q];
+    for (size_t q = 0; q < cB[eb].size(); ++q) {
+      t->coefB[q * ne2 + k] = (double)cB[eb][q];
+      t->slotB[q * ne2 + k] = (uint16_t)sB[eb][q];
     }
   }
   return true;

@@ -37,8 +37,10 @@ int upload_tables(TransCalcPriv *p) {
   size_t total = 0;
   auto add = [&](size_t bytes) { total = ((total + 255) & ~size_t(255)) + bytes; };
   add(h.perm.size() * 4);
+  add(h.permB.size() * 4);
   add(h.cntA.size());
   add(h.cntB.size());
+  add(h.cntBe.size());
   add(h.coefA.size() * 8);
   add(h.coefB.size() * 8);
   add(h.slotA.size() * 2);
@@ -62,8 +64,10 @@ int upload_tables(TransCalcPriv *p) {
     return (char *)d + o;
   };
   T.perm = (const int32_t *)put(h.perm.data(), h.perm.size() * 4);
+  T.permB = (const int32_t *)put(h.permB.data(), h.permB.size() * 4);
   T.cntA = (const uint8_t *)put(h.cntA.data(), h.cntA.size());
   T.cntB = (const uint8_t *)put(h.cntB.data(), h.cntB.size());
+  T.cntBe = (const uint8_t *)put(h.cntBe.data(), h.cntBe.size());
   T.coefA = (const double *)put(h.coefA.data(), h.coefA.size() * 8);
   T.coefB = (const double *)put(h.coefB.data(), h.coefB.size() * 8);
   T.slotA = (const uint16_t *)put(h.slotA.data(), h.slotA.size() * 2);

@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(kThreads) trans_ab_kernel(TransDevTables T, si
         const uint8_t *cnt = which ? T.cntB : T.cntA;
         const double *coef = which ? T.coefB : T.coefA;
         const uint16_t *slot = which ? T.slotB : T.slotA;
+        const int32_t *perm = which ? T.permB : T.perm;
         qg_c *out = (which ? B : A) + (base + v) * (size_t)NE2;
         qg_c *buf = nullptr;
         if (STAGED) {
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(kThreads) trans_ab_kernel(TransDevTables T, si
             si = fma(a, x.im, si);
           }
           const qg_c r = which ? cmk(-si, sr) : cmk(sr, si);
-          const int e = __ldg(T.perm + k);
+          const int e = __ldg(perm + k);
           if (STAGED)
             buf[e] = r;
           else

@@ -14,6 +14,10 @@ from . import _lib
 QPMS_HANKEL_PLUS = 3
 
 
+class _SSWK(C.Structure):
+    _fields_ = [("ssw", C.c_void_p), ("k", C.c_double * 3), ("eta", C.c_double)]
+
+
 class _LU(C.Structure):
     _fields_ = [("ssw", C.c_void_p), ("sswk", C.c_void_p), ("full", C.c_bool), ("iri", C.c_int),
                 ("a", C.c_void_p), ("ipiv", C.c_void_p)]
@@ -45,6 +49,16 @@ def declare(L):
     L.qpms_scatsysw_apply_Tmatrices_full.argtypes = [vp, vp, vp]
     L.qpms_gpu_incident_planewave_full.restype = ci
     L.qpms_gpu_incident_planewave_full.argtypes = [vp, vp, vp, vp]
+    L.qpms_gpu_scatsys_create_spheres_2d.restype = vp
+    L.qpms_gpu_scatsys_create_spheres_2d.argtypes = [ci, vp, vp, ci, vp, vp, cd, cd, ci, vp, vp]
+    L.qpms_ss_adjusted_eta.restype = cd
+    L.qpms_ss_adjusted_eta.argtypes = [vp, cd, cd, vp]
+    L.qpms_scatsyswk_build_modeproblem_matrix_full.restype = vp
+    L.qpms_scatsyswk_build_modeproblem_matrix_full.argtypes = [vp, C.POINTER(_SSWK)]
+    L.qpms_gpu_periodic_scan.restype = ci
+    L.qpms_gpu_periodic_scan.argtypes = [vp, sz, vp, sz, vp, vp, vp, vp, vp]
+    L.qpms_gpu_debug_cerfc.restype = ci
+    L.qpms_gpu_debug_cerfc.argtypes = [cd, cd, vp]
     L.qpms_gpu_finite_planewave_scatter.restype = ci
     L.qpms_gpu_finite_planewave_scatter.argtypes = [vp, sz, vp, vp, vp, ci, vp, vp, vp, vp]
 
@@ -52,7 +66,8 @@ def declare(L):
 class ScatteringSystem:
     """Finite system of spheres; ``ss(omega)`` evaluates it at a frequency."""
 
-    def __init__(self, positions, radius, eps_inside, eps_medium, lMax, kinds=None):
+    def __init__(self, positions, radius, eps_inside, eps_medium, lMax, kinds=None, lattice=None):
+        """lattice: None (finite system) or (b1, b2), 2D basis vectors in the xy plane."""
         self._L = _lib.lib()
         pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
         radius = np.atleast_1d(np.asarray(radius, dtype=np.float64))
@@ -63,9 +78,17 @@ class ScatteringSystem:
         em = complex(eps_medium)
         self.positions = pos
         self.lMax = int(lMax)
-        self.s = self._L.qpms_gpu_scatsys_create_spheres(pos.shape[0], pos.ctypes.data, kinds.ctypes.data,
-                                                         radius.size, radius.ctypes.data, eps_in.ctypes.data,
-                                                         em.real, em.imag, self.lMax)
+        self.lattice = lattice
+        if lattice is None:
+            self.s = self._L.qpms_gpu_scatsys_create_spheres(pos.shape[0], pos.ctypes.data, kinds.ctypes.data,
+                                                             radius.size, radius.ctypes.data, eps_in.ctypes.data,
+                                                             em.real, em.imag, self.lMax)
+        else:
+            b1 = np.ascontiguousarray(lattice[0][:2], dtype=np.float64)
+            b2 = np.ascontiguousarray(lattice[1][:2], dtype=np.float64)
+            self.s = self._L.qpms_gpu_scatsys_create_spheres_2d(
+                pos.shape[0], pos.ctypes.data, kinds.ctypes.data, radius.size, radius.ctypes.data,
+                eps_in.ctypes.data, em.real, em.imag, self.lMax, b1.ctypes.data, b2.ctypes.data)
         if not self.s:
             raise _lib.QpmsGpuError("qpms_gpu_scatsys_create_spheres: " + _lib.last_error())
         self.fecv_size = pos.shape[0] * 2 * self.lMax * (self.lMax + 2)
@@ -93,6 +116,36 @@ class ScatteringSystem:
         r = self._L.qpms_scatsys_build_translation_matrix_e_full(out.ctypes.data, self.s, k.real, k.imag, int(J))
         if not r:
             raise _lib.QpmsGpuError("translation matrix: " + _lib.last_error())
+        return out
+
+    def adjusted_eta(self, wavenumber, kvec):
+        """qpms_ss_adjusted_eta (scatsystem.c:68-80)."""
+        k = complex(wavenumber)
+        kv = np.zeros(3)
+        kv[:len(kvec)] = kvec
+        return self._L.qpms_ss_adjusted_eta(self.s, k.real, k.imag, kv.ctypes.data)
+
+    def dispersion_scan(self, omegas, kvecs, want_f=False, want_sigma=True):
+        """Batched 2D-lattice scan: log|det M(omega, k)| for all pairs, plus the
+        plane-wave excitation (f, sigma_ext per cell, residual)."""
+        om = np.ascontiguousarray(omegas, dtype=np.float64)
+        kv = np.ascontiguousarray(kvecs, dtype=np.float64).reshape(-1, 2)
+        nw, nk = om.size, kv.shape[0]
+        logdet = np.empty((nw, nk))
+        sig = np.empty((nw, nk)) if want_sigma else None
+        res = np.empty((nw, nk)) if want_sigma else None
+        f = np.empty((nw, nk, self.fecv_size), dtype=np.complex128) if want_f else None
+        rc = self._L.qpms_gpu_periodic_scan(self.s, nw, om.ctypes.data, nk, kv.ctypes.data, logdet.ctypes.data,
+                                            f.ctypes.data if want_f else None,
+                                            sig.ctypes.data if want_sigma else None,
+                                            res.ctypes.data if want_sigma else None)
+        _lib.check(rc, "qpms_gpu_periodic_scan")
+        out = {"logdet": logdet}
+        if want_sigma:
+            out["sigma_ext"] = sig
+            out["residual"] = res
+        if want_f:
+            out["f"] = f
         return out
 
     def planewave_scatter_batch(self, omegas, k_dir=(0.0, 0.0, 1.0), E_cart=(1.0, 0.0, 0.0), mode=1,
@@ -134,10 +187,21 @@ class _ScatteringSystemAtOmega:
             self._L.qpms_gpu_scatsys_at_omega_free(w)
             self.ssw = None
 
-    def modeproblem_matrix_full(self):
+    def modeproblem_matrix_full(self, k=None, eta=0.0):
+        """M = I - T S (finite) or, with a Bloch vector k, M = I - T W(k) (2D lattice)."""
         n = self.ss.fecv_size
         out = np.empty((n, n), dtype=np.complex128)
-        if not self._L.qpms_scatsysw_build_modeproblem_matrix_full(out.ctypes.data, self.ssw):
+        if k is None:
+            r = self._L.qpms_scatsysw_build_modeproblem_matrix_full(out.ctypes.data, self.ssw)
+        else:
+            wk = _SSWK()
+            wk.ssw = self.ssw
+            kk = list(k) + [0.0] * (3 - len(k))
+            for i in range(3):
+                wk.k[i] = kk[i]
+            wk.eta = float(eta)
+            r = self._L.qpms_scatsyswk_build_modeproblem_matrix_full(out.ctypes.data, C.byref(wk))
+        if not r:
             raise _lib.QpmsGpuError("modeproblem_matrix_full: " + _lib.last_error())
         return out
 

@@ -30,3 +30,39 @@ def translation_vectors(n, seed=2024, n_medium=1.5, rmin=50e-9, rmax=10e-6, E_lo
     kim = rng.uniform(0.0, im_frac, n) * kre
     kr = (kre + 1j * kim) * r
     return kr.astype(np.complex128), np.arccos(cth), phi
+
+
+def square_lattice(a=580e-9):
+    """Square lattice, one particle at the origin: (b1, b2, positions)."""
+    return (a, 0.0), (0.0, a), np.zeros((1, 3))
+
+
+def honeycomb_lattice(a=580e-9):
+    """Hexagonal Bravais lattice of constant a with two particles at
+    +-(a/sqrt 3)/2 along x (nearest-neighbour distance a/sqrt 3)."""
+    d = a / np.sqrt(3) / 2
+    return (a, 0.0), (a / 2, a * np.sqrt(3) / 2), np.array([[-d, 0, 0], [d, 0, 0]])
+
+
+def kpath(points, n):
+    """n points uniform in arc length along the polyline through `points` (2D)."""
+    P = np.asarray(points, dtype=np.float64)
+    seg = np.linalg.norm(np.diff(P, axis=0), axis=1)
+    s = np.concatenate([[0], np.cumsum(seg)])
+    t = np.linspace(0, s[-1], n)
+    out = np.empty((n, 2))
+    for d in range(2):
+        out[:, d] = np.interp(t, s, P[:, d])
+    return out
+
+
+def square_path(a=580e-9, n=4096):
+    """Gamma - X - M - Gamma of the square lattice."""
+    G, X, M = (0, 0), (np.pi / a, 0), (np.pi / a, np.pi / a)
+    return kpath([G, X, M, G], n)
+
+
+def honeycomb_path(a=580e-9, n=4096):
+    """Gamma - K - M - Gamma of the hexagonal lattice with b1 = (a, 0), b2 = (a/2, a sqrt3/2)."""
+    G, K, M = (0, 0), (4 * np.pi / (3 * a), 0), (np.pi / a, np.pi / (np.sqrt(3) * a))
+    return kpath([G, K, M, G], n)

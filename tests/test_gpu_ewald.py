@@ -1,0 +1,99 @@
+"""GPU parity of the 2D-periodic (Ewald) mode-problem path against the oracle.
+
+Tolerances: mode-problem matrices 1e-10 Frobenius-relative on M and 1e-9 on
+the lattice part M - I (that part carries the Ewald sums, whose short- and
+long-range pieces cancel); eta invariance of M - I to 1e-9 (the reference's
+own check is 1e-10 rel / 1e-8 abs on sigma, tests/test_scalar_ewald32.c);
+log|det M| to 1e-9 absolute; plane-wave solves to a 1e-10 residual.
+"""
+import numpy as np
+import pytest
+
+from qpms_gb300.workloads import EV, HBAR, C0, square_lattice, honeycomb_lattice
+
+pytestmark = pytest.mark.gpu
+
+EPS_I = -12 + 1.2j
+EPS_E = 2.25
+RAD = 80e-9
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import qpms_gb300
+    return qpms_gb300
+
+
+def _oracle_M(orc, lMax, pos, b1, b2, om, kv, eta):
+    c = orc.TransCalculator(lMax)
+    Td = orc.tmatrix_sphere_diag(lMax, RAD, om, EPS_I, EPS_E)
+    T = np.stack([np.diag(Td)] * len(pos))
+    ke = np.sqrt(EPS_E) * om / C0
+    return orc.periodic_modeproblem(c, pos, T, ke, b1, b2, kv, eta)
+
+
+CASES = [("square", 1.6, (0.0, 0.0)), ("square", 2.1, (3e6, 1e6)), ("square", 2.6, (5.4e6, 5.4e6)),
+         ("honeycomb", 1.7, (0.0, 0.0)), ("honeycomb", 2.3, (4e6, -2e6)), ("honeycomb", 2.55, (7.2e6, 0.0))]
+
+
+@pytest.mark.parametrize("lat,E,kv", CASES)
+def test_periodic_M_vs_oracle(gpu, orc, lat, E, kv):
+    lMax = 3
+    b1, b2, pos = square_lattice() if lat == "square" else honeycomb_lattice()
+    ss = gpu.ScatteringSystem(pos, RAD, EPS_I, EPS_E, lMax, lattice=(b1, b2))
+    om = E * EV / HBAR
+    ke = np.sqrt(EPS_E) * om / C0
+    eta = ss.adjusted_eta(ke, kv)
+    M = ss(om).modeproblem_matrix_full(k=kv)
+    O = _oracle_M(orc, lMax, pos, b1, b2, om, kv, eta)
+    I = np.eye(len(M))
+    assert np.linalg.norm(M - O) <= 1e-10 * np.linalg.norm(O)
+    assert np.linalg.norm(M - O) <= 1e-9 * np.linalg.norm(O - I), np.linalg.norm(M - O) / np.linalg.norm(O - I)
+
+
+def test_eta_invariance_gpu(gpu):
+    lMax = 3
+    b1, b2, pos = honeycomb_lattice()
+    ss = gpu.ScatteringSystem(pos, RAD, EPS_I, EPS_E, lMax, lattice=(b1, b2))
+    om = 2.0 * EV / HBAR
+    ke = np.sqrt(EPS_E) * om / C0
+    kv = (2e6, 1e6)
+    eta0 = ss.adjusted_eta(ke, kv)
+    ssw = ss(om)
+    Ms = [ssw.modeproblem_matrix_full(k=kv, eta=f * eta0) for f in (1.0, 1.3, 1.7)]
+    I = np.eye(len(Ms[0]))
+    for Mx in Ms[1:]:
+        assert np.linalg.norm(Mx - Ms[0]) <= 1e-9 * np.linalg.norm(Ms[0] - I)
+
+
+@pytest.mark.parametrize("lat", ["square", "honeycomb"])
+def test_dispersion_scan_vs_oracle(gpu, orc, lat):
+    lMax = 3
+    b1, b2, pos = square_lattice() if lat == "square" else honeycomb_lattice()
+    ss = gpu.ScatteringSystem(pos, RAD, EPS_I, EPS_E, lMax, lattice=(b1, b2))
+    om = np.array([1.65, 2.05, 2.45]) * EV / HBAR
+    kvs = np.array([[0.0, 0.0], [2.5e6, 0.0], [4e6, 3e6]])
+    out = ss.dispersion_scan(om, kvs, want_f=True)
+    assert (out["residual"] <= 1e-10).all(), out["residual"].max()
+    c = orc.TransCalculator(lMax)
+    for i, w in enumerate(om):
+        ke = np.sqrt(EPS_E) * w / C0
+        for j, kv in enumerate(kvs):
+            eta = ss.adjusted_eta(ke, kv)
+            O = _oracle_M(orc, lMax, pos, b1, b2, w, kv, eta)
+            sgn, ld = np.linalg.slogdet(O)
+            assert abs(out["logdet"][i, j] - ld) <= 1e-9, (out["logdet"][i, j], ld)
+            # plane wave with in-plane k = Bloch vector, E = x projected perpendicular to k
+            kz = np.sqrt(ke ** 2 - kv[0] ** 2 - kv[1] ** 2)
+            kd = np.array([kv[0], kv[1], kz])
+            E = np.array([1.0, 0, 0]) - (kd[0] / ke) * kd / ke
+            E /= np.linalg.norm(E)
+            a = orc.planewave_full(lMax, pos, kd, E)
+            Td = orc.tmatrix_sphere_diag(lMax, RAD, w, EPS_I, EPS_E)
+            f = np.linalg.solve(O, np.tile(Td, len(pos)) * a)
+            assert np.linalg.norm(out["f"][i, j] - f) <= 1e-9 * np.linalg.norm(f)
+            sig = -np.vdot(a, f).real / ke ** 2
+            assert abs(out["sigma_ext"][i, j] - sig) <= 1e-9 * abs(sig)
