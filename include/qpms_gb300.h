@@ -113,6 +113,25 @@ int qpms_gpu_trans_AB_arrays_batch_host(const qpms_trans_calculator *c, size_t n
     const unsigned char *r_ge_d, qpms_bessel_t J,
     qpms_complex_t *A, qpms_complex_t *B);
 
+/* Allocation-free form of qpms_gpu_trans_AB_arrays_batch_host, for callers
+ * that must not allocate device or pinned memory while they run (a process
+ * whose device memory is owned by a pool allocator or capped by a budget, a
+ * real-time loop that forbids allocation after start-up, a plug-in that must
+ * not change its host's memory footprint).  No counterpart in the reference.
+ * Same kernel and results; inputs and outputs are host buffers.  Staging uses
+ * a file-scope device array of 32 MiB that every GPU loading the library holds
+ * until exit, so a batch must fit in it (about 4,600 translations at lMax 3,
+ * 450 at lMax 6); larger batches are rejected with QPMS_EINVAL and a message.
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream
+ * capture.  All calls share the array and it keeps the last call's contents;
+ * calls that overlap on the GPU race on it, so serialise them.  Synchronous,
+ * on the legacy default stream. */
+int qpms_gpu_trans_AB_arrays_batch_host_noalloc(const qpms_trans_calculator *c, size_t n,
+    const qpms_complex_t *kr, const double *theta, const double *phi,
+    const unsigned char *r_ge_d, qpms_bessel_t J,
+    qpms_complex_t *A, qpms_complex_t *B);
+
 /* Number of A / B multipliers (ragged table sizes), for tests. */
 size_t qpms_gpu_trans_calculator_n_multipliers(const qpms_trans_calculator *c, int which_B);
 
