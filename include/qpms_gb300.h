@@ -333,6 +333,106 @@ int qpms_gpu_finite_planewave_scatter(const qpms_scatsys_t *ss, size_t nw,
     const double *omegas, const double k_dir[3], const qpms_complex_t E_cart[3], int mode,
     qpms_complex_t *f_out, double *sigma_ext, double *resid_out, int *iters_out);
 
+/* Dense complex solve X = M^-1 B on DEVICE pointers (column-major, any N):
+ * random butterfly transform + blocked LU without pivoting;
+ * mode 0 complex128 (plain FP64), mode 1 complex64 factors with FP64
+ * iterative refinement (tensor-core GEMMs).  The solver of the Beyn contour
+ * nodes (the reference factorises with LAPACKE_zgetrf/zgetrs, beyn.c:552-564).
+ * resid = ||B - M X||_F / ||B||_F (FP64), iters = refinement steps.  Synchronous. */
+int qpms_gpu_dense_solve(int N, int nrhs, const qpms_complex_t *M, const qpms_complex_t *B,
+    qpms_complex_t *X, int mode, double *resid, int *iters);
+
+/* ---------------- Beyn contour-integral eigensolver (beyn.h) ---------------- */
+typedef int qpms_iri_t;               /* qpms_types.h:323 */
+#define QPMS_NO_IRREP ((qpms_iri_t) -1)   /* qpms_types.h:325 */
+
+/* M(z) into target (row-major m x m), beyn.h:22. */
+typedef int (*beyn_function_M_t)(qpms_complex_t *target_M, size_t m, qpms_complex_t z, void *params);
+/* M(z)^-1 Vhat (row-major m x l), beyn.h:26-27. */
+typedef int (*beyn_function_M_inv_Vhat_t)(qpms_complex_t *target_M_inv_Vhat, size_t m, size_t l,
+    const qpms_complex_t *Vhat, qpms_complex_t z, void *params);
+
+/* Integration contour, beyn.h:30-43: n nodes (z, dz) followed by one hidden
+ * entry holding the half-axes of an ellipse. */
+typedef struct beyn_contour_t {
+  size_t n;
+  qpms_complex_t centre;
+  bool (*inside_test)(struct beyn_contour_t *, qpms_complex_t z);
+  qpms_complex_t z_dz[][2];
+} beyn_contour_t;
+
+/* beyn.h:47 (beyn.c:69-86); free with free(). */
+beyn_contour_t *beyn_contour_ellipse(qpms_complex_t centre, double halfax_re, double halfax_im, size_t npoints);
+
+/* Result, beyn.h:82-94: neig eigenvalues, their error estimates (coarse minus
+ * fine contour), residuals |M(z) v|, eigenvectors as rows of length vlen, and
+ * the singular values of the rank test.  `gsl` is private here (NULL). */
+typedef struct beyn_result_t {
+  size_t neig;
+  size_t vlen;
+  qpms_complex_t *eigval;
+  qpms_complex_t *eigval_err;
+  double *residuals;
+  qpms_complex_t *eigvec;
+  double *ranktest_SV;
+  void *gsl;
+} beyn_result_t;
+
+/* beyn.h:101 */
+void beyn_result_free(beyn_result_t *result);
+
+/* beyn.h:115-125 (beyn.c:625-634 over beyn_solve_gsl, beyn.c:471-584).  The
+ * quadrature solves M(z_i) X = Vhat on the GPU (one LU per node, L right-hand
+ * sides, complex64 factors with FP64 iterative refinement); M comes from the
+ * host callback.  The probe matrix Vhat is drawn from a fixed seed (the
+ * reference seeds from the clock, beyn.c:292).  M_inv_Vhat, when given, is
+ * used in place of the LU as in the reference. */
+beyn_result_t *beyn_solve(size_t m, size_t l, beyn_function_M_t M, beyn_function_M_inv_Vhat_t M_inv_Vhat,
+    void *params, const beyn_contour_t *contour, double rank_tol, size_t rank_sel_min, double res_tol);
+
+/* scatsystem.h:649-662 (scatsystem.c:2301-2324): eigenmodes of a finite
+ * system inside an ellipse in the complex omega plane, l = fecv_size probe
+ * columns as in the reference; iri must be QPMS_NO_IRREP (irrep-packed
+ * matrices are not implemented).  M(omega) is assembled on the GPU. */
+beyn_result_t *qpms_scatsys_finite_find_eigenmodes(const qpms_scatsys_t *ss, qpms_iri_t iri,
+    qpms_complex_t omega_centre, double omega_rr, double omega_ri, size_t contour_npoints,
+    double rank_tol, size_t rank_sel_min, double res_tol);
+
+/* scatsystem.h:538-549 (scatsystem.c:2351-2372): the same for a 2D-periodic
+ * system at Bloch vector k, M = I - T W(omega, k) with the adjusted Ewald eta. */
+beyn_result_t *qpms_scatsys_periodic_find_eigenmodes(const qpms_scatsys_t *ss, const double k[3],
+    qpms_complex_t omega_centre, double omega_rr, double omega_ri, size_t contour_npoints,
+    double rank_tol, size_t rank_sel_min, double res_tol);
+
+/* Extended form of the two above (k = NULL: finite system): l probe columns
+ * (l <= fecv_size), Vhat (row-major fecv_size x l, or NULL for the seeded
+ * generator), mode 0 = plain FP64 LU per node, 1 = complex64 LU with FP64
+ * refinement to refine_tol (relative residual; <= 0 selects 1e-12). */
+beyn_result_t *qpms_gpu_scatsys_find_eigenmodes(const qpms_scatsys_t *ss, const double *k,
+    qpms_complex_t omega_centre, double omega_rr, double omega_ri, size_t contour_npoints,
+    double rank_tol, size_t rank_sel_min, double res_tol, size_t l, const qpms_complex_t *Vhat,
+    unsigned long long seed, int mode, double refine_tol);
+
+/* Extended beyn_solve: explicit probe matrix / seed and precision mode. */
+beyn_result_t *qpms_gpu_beyn_solve(size_t m, size_t l, beyn_function_M_t M, void *params,
+    const beyn_contour_t *contour, double rank_tol, size_t rank_sel_min, double res_tol,
+    const qpms_complex_t *Vhat, unsigned long long seed, int mode, double refine_tol);
+
+/* Diagnostics of a result made here: largest FP64 relative residual of the
+ * node solves, most refinement steps of one node, wall time of the contour
+ * quadrature and of the whole solve (seconds). */
+int qpms_gpu_beyn_result_stats(const beyn_result_t *result, double *max_node_resid, int *max_node_iters,
+    double *quadrature_s, double *total_s);
+
+/* The seeded probe matrix (row-major m x l, complex Gaussian) used when no
+ * Vhat is given, so that callers can reproduce it. */
+int qpms_gpu_beyn_probe_matrix(size_t m, size_t l, unsigned long long seed, qpms_complex_t *out);
+
+/* Host linear algebra of the Beyn post-processing, exposed for tests:
+ * thin SVD (column-major m x n, m >= n) and general eigenproblem (n x n). */
+int qpms_gpu_host_svd(int m, int n, const qpms_complex_t *A, qpms_complex_t *U, double *s, qpms_complex_t *V);
+int qpms_gpu_host_eig(int n, const qpms_complex_t *A, qpms_complex_t *w, qpms_complex_t *X);
+
 /* ---------------- diagnostics ---------------- */
 /* Thread-local message of the last failing call (empty string if none). */
 const char *qpms_gpu_last_error(void);

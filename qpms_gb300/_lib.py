@@ -55,10 +55,13 @@ def _declare(L):
     L.qpms_gpu_trans_AB_arrays_batch_host.argtypes = [vp, sz, vp, vp, vp, vp, ci, vp, vp]
     L.qpms_gpu_trans_multipliers_export.restype = ci
     L.qpms_gpu_trans_multipliers_export.argtypes = [ci, ci, vp, vp, vp, vp]
+    L.qpms_gpu_dense_solve.restype = ci
+    L.qpms_gpu_dense_solve.argtypes = [ci, ci, vp, vp, vp, ci, vp, vp]
     L.qpms_gpu_measure_fp64_peak.restype = ci
     L.qpms_gpu_measure_fp64_peak.argtypes = [vp]
     # complex by value is passed as two doubles (same registers on x86-64 and aarch64)
     L.qpms_trans_calculator_get_AB_arrays_ext.restype = ci
     L.qpms_trans_calculator_get_AB_arrays_ext.argtypes = [vp, vp, vp, sz, sz, cd, cd, cd, cd, ci, ci]
-    from . import scatsystem
+    from . import beyn, scatsystem
     scatsystem.declare(L)
+    beyn.declare(L)

@@ -1,0 +1,518 @@
+// Dense LU solver for large mode-problem matrices (Beyn contour nodes,
+// 14,400-unknown systems and up) on sm_103a.
+//
+// The reference factorises with LAPACKE_zgetrf (partial pivoting) and solves
+// with zgetrs (scatsystem.c:2202-2273; beyn.c:552-564).  Partial pivoting
+// serialises a global pivot search per column, the latency bound of GPU LU;
+// this solver instead
+//   1. applies a depth-2 random butterfly transform (RBT) to both sides,
+//      A' = W_u^T M W_v (Parker's randomisation, as in Baboulin, Dongarra,
+//      Herrmann, Tomov, "Accelerating linear system solutions using
+//      randomization techniques", ACM TOMS 39 (2013)), after which Gaussian
+//      elimination without pivoting is stable with high probability;
+//   2. factorises A' = L U without pivoting by blocks: an nb x nb diagonal
+//      block is factored and its triangular factors inverted in shared memory
+//      by one CTA; the panels below and to the right and the trailing update are
+//      then GEMMs (cuBLAS, tensor cores);
+//   3. solves by blocked forward/back substitution (GEMMs with the inverted
+//      diagonal blocks);
+//   4. in the mixed mode, the factorisation and substitutions run in complex64
+//      (GEMMs with FP32-accurate BF16x9 emulation on the tensor cores) and the
+//      FP64 solution is recovered by iterative refinement against the FP64
+//      matrix: x += W_v (LU)^-1 W_u^T (b - M x), residual in FP64.
+// The plain mode runs steps 1-3 in complex128 (FP64 GEMMs).
+// All matrices are column-major (LAPACK order).  The butterflies halve the
+// system twice, so it is padded internally to a multiple of 4 with identity.
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <random>
+#include <vector>
+
+#include "qg_dense.h"
+#include "qg_internal.h"
+
+namespace qg {
+int blas_handle_get(cublasHandle_t *h);
+
+namespace {
+
+template <typename T>
+struct CTraits;
+template <>
+struct CTraits<float2> {
+  typedef float real;
+  static constexpr cudaDataType_t dt = CUDA_C_32F;
+};
+template <>
+struct CTraits<double2> {
+  typedef double real;
+  static constexpr cudaDataType_t dt = CUDA_C_64F;
+};
+
+template <typename T>
+__device__ __forceinline__ T mk(typename CTraits<T>::real r, typename CTraits<T>::real i) {
+  T z;
+  z.x = r;
+  z.y = i;
+  return z;
+}
+template <typename T>
+__device__ __forceinline__ T mul(T a, T b) {
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T>
+__device__ __forceinline__ T sub(T a, T b) {
+  return mk<T>(a.x - b.x, a.y - b.y);
+}
+template <typename T>
+__device__ __forceinline__ T rcp(T b) {
+  typedef typename CTraits<T>::real R;
+  const R d = b.x * b.x + b.y * b.y;
+  return mk<T>(b.x / d, -b.y / d);
+}
+
+// ---------------- diagonal block: LU without pivoting + triangular inverses ----------------
+// D (kb x kb, column-major in global, leading dimension lda) is factored in
+// place (unit-lower L below the diagonal, U on and above); Linv and Uinv are
+// written to out (column-major kb x kb each).  info is set to 1 on an exactly
+// zero pivot.
+template <typename T>
+__global__ void __launch_bounds__(1024) diag_lu_inv_kernel(T *D, size_t lda, int kb, T *Linv, T *Uinv, int *info) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  T *S = reinterpret_cast<T *>(sm);  // [kb][kb] column-major
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int t = tid; t < kb * kb; t += nt) {
+    const int c = t / kb, r = t - c * kb;
+    S[t] = D[(size_t)c * lda + r];
+  }
+  __syncthreads();
+  for (int j = 0; j < kb; ++j) {
+    const T d = S[j * kb + j];
+    if (d.x == 0 && d.y == 0) {
+      if (tid == 0) atomicOr(info, 1);
+    }
+    const T inv = (d.x == 0 && d.y == 0) ? mk<T>(0, 0) : rcp(d);
+    for (int i = j + 1 + tid; i < kb; i += nt) S[j * kb + i] = mul(S[j * kb + i], inv);
+    __syncthreads();
+    const int w = kb - j - 1;
+    for (int t = tid; t < w * w; t += nt) {
+      const int c = j + 1 + t / w, r = j + 1 + t % w;
+      S[c * kb + r] = sub(S[c * kb + r], mul(S[j * kb + r], S[c * kb + j]));
+    }
+    __syncthreads();
+  }
+  for (int t = tid; t < kb * kb; t += nt) {
+    const int c = t / kb, r = t - c * kb;
+    D[(size_t)c * lda + r] = S[t];
+  }
+  // inverses: thread c < kb computes column c of Linv, thread kb + c column c of Uinv
+  if (tid < kb) {
+    const int c = tid;
+    for (int i = 0; i < c; ++i) Linv[c * kb + i] = mk<T>(0, 0);
+    Linv[c * kb + c] = mk<T>(1, 0);
+    for (int i = c + 1; i < kb; ++i) {
+      T s = mk<T>(0, 0);
+      for (int k = c; k < i; ++k) s = sub(s, mul(S[k * kb + i], Linv[c * kb + k]));
+      Linv[c * kb + i] = s;
+    }
+  } else if (tid < 2 * kb) {
+    const int c = tid - kb;
+    for (int i = c + 1; i < kb; ++i) Uinv[c * kb + i] = mk<T>(0, 0);
+    const T ucc = S[c * kb + c];
+    Uinv[c * kb + c] = (ucc.x == 0 && ucc.y == 0) ? mk<T>(0, 0) : rcp(ucc);
+    for (int i = c - 1; i >= 0; --i) {
+      T s = mk<T>(0, 0);
+      for (int k = i + 1; k <= c; ++k) s = sub(s, mul(S[k * kb + i], Uinv[c * kb + k]));
+      const T uii = S[i * kb + i];
+      Uinv[c * kb + i] = (uii.x == 0 && uii.y == 0) ? mk<T>(0, 0) : mul(s, rcp(uii));
+    }
+  }
+}
+
+// ---------------- random butterfly transforms (FP64) ----------------
+// Row pass: within each block of size h2 = 2h along the rows (block b covers
+// rows [b*2h, (b+1)*2h)), for i < h: top = A[i], bot = A[i + h]:
+//   transposed butterfly (left, W^T):  top' = R_i (top + bot)/sqrt2, bot' = S_i (top - bot)/sqrt2
+//   butterfly (right or solution, W):   column form uses the same pairing.
+// R and S are stored per level in d[level][N]: R at d[b*2h + i], S at d[b*2h + h + i].
+__global__ void rbt_rows_kernel(size_t N, size_t ncols, size_t ld, double2 *A, int h, const double *rs,
+                                int transposed) {
+  const double is2 = 0.70710678118654752440;
+  const size_t pairs = N / 2;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < pairs * ncols;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t col = t / pairs, p = t - col * pairs;
+    const size_t b = p / h, i = p - b * h;
+    const size_t r0 = b * 2 * h + i, r1 = r0 + h;
+    double2 *x = A + col * ld;
+    const double2 top = x[r0], bot = x[r1];
+    const double R = rs[b * 2 * h + i], S = rs[b * 2 * h + h + i];
+    if (transposed) {  // W^T: [R R; S -S] / sqrt2
+      x[r0] = make_double2(R * (top.x + bot.x) * is2, R * (top.y + bot.y) * is2);
+      x[r1] = make_double2(S * (top.x - bot.x) * is2, S * (top.y - bot.y) * is2);
+    } else {  // W: [R S; R -S] / sqrt2
+      x[r0] = make_double2((R * top.x + S * bot.x) * is2, (R * top.y + S * bot.y) * is2);
+      x[r1] = make_double2((R * top.x - S * bot.x) * is2, (R * top.y - S * bot.y) * is2);
+    }
+  }
+}
+
+// Column pass of A W (right multiplication): columns j and j + h within blocks of 2h:
+//   (A W)[:, j] = R_j (A_j + A_{j+h}) / sqrt2,  (A W)[:, j+h] = S_j (A_j - A_{j+h}) / sqrt2
+__global__ void rbt_cols_kernel(size_t N, size_t ld, double2 *A, int h, const double *rs) {
+  const double is2 = 0.70710678118654752440;
+  const size_t pairs = N / 2;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < pairs * N;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t p = t / N, row = t - p * N;  // consecutive threads walk rows (coalesced)
+    const size_t b = p / h, j = p - b * h;
+    const size_t c0 = b * 2 * h + j, c1 = c0 + h;
+    const double2 a0 = A[c0 * ld + row], a1 = A[c1 * ld + row];
+    const double R = rs[b * 2 * h + j], S = rs[b * 2 * h + h + j];
+    A[c0 * ld + row] = make_double2(R * (a0.x + a1.x) * is2, R * (a0.y + a1.y) * is2);
+    A[c1 * ld + row] = make_double2(S * (a0.x - a1.x) * is2, S * (a0.y - a1.y) * is2);
+  }
+}
+
+__global__ void d2f_kernel(size_t n, const double2 *src, float2 *dst) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    dst[t] = make_float2((float)src[t].x, (float)src[t].y);
+}
+__global__ void f2d_add_kernel(size_t n, const float2 *src, double2 *dst, int init) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const float2 v = src[t];
+    dst[t] = init ? make_double2(v.x, v.y) : make_double2(dst[t].x + v.x, dst[t].y + v.y);
+  }
+}
+__global__ void add_kernel(size_t n, const double2 *src, double2 *dst, int init) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    dst[t] = init ? src[t] : make_double2(dst[t].x + src[t].x, dst[t].y + src[t].y);
+}
+// sum of |x|^2 over n entries into out[0] (atomic)
+__global__ void norm2_kernel(size_t n, const double2 *x, double *out) {
+  double s = 0;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    s += x[t].x * x[t].x + x[t].y * x[t].y;
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+unsigned grid1(size_t n) {
+  size_t g = (n + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  return (unsigned)(g ? g : 1);
+}
+
+template <typename T>
+int gemm(cublasHandle_t h, int m, int n, int k, T alpha, const T *A, size_t lda, const T *B, size_t ldb, T beta,
+         T *C, size_t ldc, cublasComputeType_t ct) {
+  const cudaDataType_t dt = CTraits<T>::dt;
+  cublasStatus_t s = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &alpha, A, dt, (int)lda, B, dt, (int)ldb,
+                                  &beta, C, dt, (int)ldc, ct, CUBLAS_GEMM_DEFAULT);
+  if (s == CUBLAS_STATUS_NOT_SUPPORTED && ct != CUBLAS_COMPUTE_32F && ct != CUBLAS_COMPUTE_64F) {
+    ct = (dt == CUDA_C_32F) ? CUBLAS_COMPUTE_32F : CUBLAS_COMPUTE_64F;
+    s = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &alpha, A, dt, (int)lda, B, dt, (int)ldb, &beta, C, dt,
+                     (int)ldc, ct, CUBLAS_GEMM_DEFAULT);
+  }
+  if (s != CUBLAS_STATUS_SUCCESS) {
+    set_error("cublasGemmEx(%d, %d, %d) failed: status %d", m, n, k, (int)s);
+    return QPMS_ERROR;
+  }
+  g_launches.fetch_add(1);
+  return QPMS_SUCCESS;
+}
+
+template <typename T>
+T cone() {
+  T z;
+  z.x = 1;
+  z.y = 0;
+  return z;
+}
+template <typename T>
+T cval(double r) {
+  T z;
+  z.x = (typename CTraits<T>::real)r;
+  z.y = 0;
+  return z;
+}
+
+// LU without pivoting, blocked (see the header comment).
+template <typename T>
+int lu_nopiv(cublasHandle_t h, int N, int nb, T *A, size_t lda, T *Dinv, T *work, int *dinfo,
+             cublasComputeType_t ct, cudaStream_t st) {
+  const size_t smem = (size_t)nb * nb * sizeof(T);
+  QG_CUDA_TRY(cudaFuncSetAttribute(diag_lu_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  for (int k = 0, blk = 0; k < N; k += nb, ++blk) {
+    const int kb = (N - k < nb) ? N - k : nb;
+    T *Lk = Dinv + (size_t)blk * 2 * nb * nb, *Uk = Lk + (size_t)nb * nb;
+    diag_lu_inv_kernel<T><<<1, 1024, (size_t)kb * kb * sizeof(T), st>>>(A + (size_t)k * lda + k, lda, kb, Lk, Uk,
+                                                                        dinfo);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+    const int m2 = N - k - kb;
+    if (m2 <= 0) break;
+    T *A21 = A + (size_t)k * lda + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = A21 + (size_t)kb * lda;
+    int e;
+    // L21 = A21 Uinv   (m2 x kb)
+    if ((e = gemm<T>(h, m2, kb, kb, cone<T>(), A21, lda, Uk, kb, cval<T>(0), work, m2, ct))) return e;
+    QG_CUDA_TRY(cudaMemcpy2DAsync(A21, lda * sizeof(T), work, (size_t)m2 * sizeof(T), (size_t)m2 * sizeof(T), kb,
+                                  cudaMemcpyDeviceToDevice, st));
+    // U12 = Linv A12   (kb x m2)
+    if ((e = gemm<T>(h, kb, m2, kb, cone<T>(), Lk, kb, A12, lda, cval<T>(0), work, kb, ct))) return e;
+    QG_CUDA_TRY(cudaMemcpy2DAsync(A12, lda * sizeof(T), work, (size_t)kb * sizeof(T), (size_t)kb * sizeof(T), m2,
+                                  cudaMemcpyDeviceToDevice, st));
+    // A22 -= L21 U12
+    if ((e = gemm<T>(h, m2, m2, kb, cval<T>(-1), A21, lda, A12, lda, cone<T>(), A22, lda, ct))) return e;
+  }
+  return QPMS_SUCCESS;
+}
+
+// Solve (L U) X = B in place (B: N x nrhs, column-major, ldb).
+template <typename T>
+int lu_solve(cublasHandle_t h, int N, int nb, const T *A, size_t lda, const T *Dinv, T *B, size_t ldb, int nrhs,
+             T *work, cublasComputeType_t ct, cudaStream_t st) {
+  int e;
+  const int nblk = (N + nb - 1) / nb;
+  for (int blk = 0; blk < nblk; ++blk) {  // forward: L y = b
+    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
+    const T *Lk = Dinv + (size_t)blk * 2 * nb * nb;
+    if ((e = gemm<T>(h, kb, nrhs, kb, cone<T>(), Lk, kb, B + k, ldb, cval<T>(0), work, kb, ct))) return e;
+    QG_CUDA_TRY(cudaMemcpy2DAsync(B + k, ldb * sizeof(T), work, (size_t)kb * sizeof(T), (size_t)kb * sizeof(T), nrhs,
+                                  cudaMemcpyDeviceToDevice, st));
+    const int m2 = N - k - kb;
+    if (m2 > 0)
+      if ((e = gemm<T>(h, m2, nrhs, kb, cval<T>(-1), A + (size_t)k * lda + k + kb, lda, B + k, ldb, cone<T>(),
+                       B + k + kb, ldb, ct)))
+        return e;
+  }
+  for (int blk = nblk - 1; blk >= 0; --blk) {  // backward: U x = y
+    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
+    const T *Uk = Dinv + (size_t)blk * 2 * nb * nb + (size_t)nb * nb;
+    if ((e = gemm<T>(h, kb, nrhs, kb, cone<T>(), Uk, kb, B + k, ldb, cval<T>(0), work, kb, ct))) return e;
+    QG_CUDA_TRY(cudaMemcpy2DAsync(B + k, ldb * sizeof(T), work, (size_t)kb * sizeof(T), (size_t)kb * sizeof(T), nrhs,
+                                  cudaMemcpyDeviceToDevice, st));
+    if (k > 0)
+      if ((e = gemm<T>(h, k, nrhs, kb, cval<T>(-1), A + (size_t)k * lda, lda, B + k, ldb, cone<T>(), B, ldb, ct)))
+        return e;
+  }
+  return QPMS_SUCCESS;
+}
+
+}  // namespace
+
+// ---------------- solver object ----------------
+
+namespace {
+// identity on the padding rows/columns N..Np-1 of an Np x Np matrix
+__global__ void pad_identity_kernel(double2 *A, size_t Np, size_t N) {
+  for (size_t i = N + threadIdx.x; i < Np; i += blockDim.x) A[i * Np + i] = make_double2(1, 0);
+}
+cublasComputeType_t lowp_compute() {
+  const char *ev = getenv("QPMS_GB300_LU_COMPUTE");
+  if (ev && !strcmp(ev, "32F")) return CUBLAS_COMPUTE_32F;
+  if (ev && !strcmp(ev, "TF32")) return CUBLAS_COMPUTE_32F_FAST_TF32;
+  return CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+}
+}  // namespace
+
+int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed) {
+  release();
+  if (N_ <= 0 || nrhs_max_ <= 0 || (mode_ != 0 && mode_ != 1)) {
+    set_error("dense solver: invalid size N = %d, nrhs = %d or mode %d", N_, nrhs_max_, mode_);
+    return QPMS_EINVAL;
+  }
+  N = N_;
+  Np = (N + 3) / 4 * 4;
+  nrhs_max = nrhs_max_;
+  mode = mode_;
+  nb = mode ? 128 : 64;
+  const size_t esz = mode ? 8 : 16;
+  const size_t NN = (size_t)Np * Np;
+  const int nblk = (Np + nb - 1) / nb;
+  size_t wsz = std::max<size_t>((size_t)Np * nb, (size_t)nb * std::max(Np, nrhs_max)) * esz;
+  if (mode) QG_CUDA_TRY(cudaMalloc(&A, NN * esz));
+  QG_CUDA_TRY(cudaMalloc(&T64, NN * 16));
+  QG_CUDA_TRY(cudaMalloc(&Dinv, (size_t)nblk * 2 * nb * nb * esz));
+  QG_CUDA_TRY(cudaMalloc(&work, wsz));
+  QG_CUDA_TRY(cudaMalloc(&rhs_lo, (size_t)Np * nrhs_max * 8));
+  QG_CUDA_TRY(cudaMalloc(&rp, (size_t)Np * nrhs_max * 16));
+  QG_CUDA_TRY(cudaMalloc(&r64, (size_t)N * nrhs_max * 16));
+  QG_CUDA_TRY(cudaMalloc(&y64, (size_t)N * nrhs_max * 16));
+  QG_CUDA_TRY(cudaMalloc(&dinfo, 16));
+  QG_CUDA_TRY(cudaMalloc(&rs, (size_t)4 * Np * sizeof(double)));
+  // random butterfly diagonals exp(r/10), r ~ U(-1/2, 1/2): [u level1][u level2][v level1][v level2]
+  std::mt19937_64 gen(seed);
+  std::uniform_real_distribution<double> U(-0.5, 0.5);
+  std::vector<double> h(4 * (size_t)Np);
+  for (auto &v : h) v = exp(U(gen) / 10);
+  QG_CUDA_TRY(cudaMemcpy(rs, h.data(), h.size() * 8, cudaMemcpyHostToDevice));
+  return QPMS_SUCCESS;
+}
+
+void DenseSolver::release() {
+  for (void *p : {(void *)A, (void *)T64, (void *)Dinv, (void *)work, (void *)rhs_lo, (void *)rp, (void *)r64,
+                  (void *)y64, (void *)dinfo, (void *)rs})
+    if (p) cudaFree(p);
+  A = T64 = Dinv = work = rhs_lo = rp = nullptr;
+  r64 = y64 = nullptr;
+  dinfo = nullptr;
+  rs = nullptr;
+}
+
+// W_u^T (rows) of an Np x ncols FP64 block
+static int rbt_left(const DenseSolver &s, double2 *X, size_t ld, size_t ncols, cudaStream_t st) {
+  // level 2 (blocks of Np/2, halves Np/4) then level 1 (halves Np/2)
+  rbt_rows_kernel<<<grid1((size_t)s.Np / 2 * ncols), 256, 0, st>>>(s.Np, ncols, ld, X, s.Np / 4, s.rs + s.Np, 1);
+  rbt_rows_kernel<<<grid1((size_t)s.Np / 2 * ncols), 256, 0, st>>>(s.Np, ncols, ld, X, s.Np / 2, s.rs, 1);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(2);
+  return QPMS_SUCCESS;
+}
+// W_v y (rows, non-transposed): level 1 first, then level 2 (W = L2 L1)
+static int rbt_right_solution(const DenseSolver &s, double2 *X, size_t ld, size_t ncols, cudaStream_t st) {
+  rbt_rows_kernel<<<grid1((size_t)s.Np / 2 * ncols), 256, 0, st>>>(s.Np, ncols, ld, X, s.Np / 2, s.rs + 2 * s.Np,
+                                                                   0);
+  rbt_rows_kernel<<<grid1((size_t)s.Np / 2 * ncols), 256, 0, st>>>(s.Np, ncols, ld, X, s.Np / 4, s.rs + 3 * s.Np,
+                                                                   0);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(2);
+  return QPMS_SUCCESS;
+}
+
+int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st) {
+  const size_t NN = (size_t)Np * Np;
+  cublasHandle_t h;
+  int e;
+  if ((e = blas_handle_get(&h))) return e;
+  QG_BLAS_TRY(cublasSetStream(h, st));
+  QG_CUDA_TRY(cudaMemsetAsync(dinfo, 0, 4, st));
+  // T64 = W_u^T diag(M, I) W_v   (M W = column pass with level 2 first: M L2 L1)
+  if (Np != N) QG_CUDA_TRY(cudaMemsetAsync(T64, 0, NN * 16, st));
+  QG_CUDA_TRY(cudaMemcpy2DAsync(T64, (size_t)Np * 16, M64, ldm * 16, (size_t)N * 16, N, cudaMemcpyDeviceToDevice,
+                                st));
+  if (Np != N) {
+    pad_identity_kernel<<<1, 32, 0, st>>>((double2 *)T64, Np, N);
+    g_launches.fetch_add(1);
+  }
+  if ((e = rbt_left(*this, (double2 *)T64, Np, Np, st))) return e;
+  rbt_cols_kernel<<<grid1(NN / 2), 256, 0, st>>>(Np, Np, (double2 *)T64, Np / 4, rs + 3 * Np);
+  rbt_cols_kernel<<<grid1(NN / 2), 256, 0, st>>>(Np, Np, (double2 *)T64, Np / 2, rs + 2 * Np);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(2);
+  if (mode) {
+    d2f_kernel<<<grid1(NN), 256, 0, st>>>(NN, (const double2 *)T64, (float2 *)A);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+    e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo, lowp_compute(), st);
+  } else {
+    e = lu_nopiv<double2>(h, Np, nb, (double2 *)T64, Np, (double2 *)Dinv, (double2 *)work, dinfo,
+                          CUBLAS_COMPUTE_64F, st);
+  }
+  if (e) return e;
+  int info = 0;
+  QG_CUDA_TRY(cudaMemcpyAsync(&info, dinfo, 4, cudaMemcpyDeviceToHost, st));
+  QG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (info) {
+    set_error("dense LU: zero pivot");
+    return QPMS_ERROR;
+  }
+  return QPMS_SUCCESS;
+}
+
+// One application of the factorised inverse: Y = W_v (LU)^-1 W_u^T R  (FP64 in and out)
+int DenseSolver::apply_inverse(const void *R, size_t ldr, void *Y, size_t ldy, int nrhs, cudaStream_t st) {
+  cublasHandle_t h;
+  int e;
+  if ((e = blas_handle_get(&h))) return e;
+  QG_BLAS_TRY(cublasSetStream(h, st));
+  const size_t n = (size_t)Np * nrhs;
+  if (Np != N) QG_CUDA_TRY(cudaMemsetAsync(rp, 0, n * 16, st));
+  QG_CUDA_TRY(cudaMemcpy2DAsync(rp, (size_t)Np * 16, R, ldr * 16, (size_t)N * 16, nrhs, cudaMemcpyDeviceToDevice,
+                                st));
+  if ((e = rbt_left(*this, (double2 *)rp, Np, nrhs, st))) return e;
+  if (mode) {
+    d2f_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)rp, (float2 *)rhs_lo);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+    if ((e = lu_solve<float2>(h, Np, nb, (const float2 *)A, Np, (const float2 *)Dinv, (float2 *)rhs_lo, Np, nrhs,
+                              (float2 *)work, lowp_compute(), st)))
+      return e;
+    f2d_add_kernel<<<grid1(n), 256, 0, st>>>(n, (const float2 *)rhs_lo, (double2 *)rp, 1);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+  } else {
+    if ((e = lu_solve<double2>(h, Np, nb, (const double2 *)T64, Np, (const double2 *)Dinv, (double2 *)rp, Np, nrhs,
+                               (double2 *)work, CUBLAS_COMPUTE_64F, st)))
+      return e;
+  }
+  if ((e = rbt_right_solution(*this, (double2 *)rp, Np, nrhs, st))) return e;
+  QG_CUDA_TRY(cudaMemcpy2DAsync(Y, ldy * 16, rp, (size_t)Np * 16, (size_t)N * 16, nrhs, cudaMemcpyDeviceToDevice,
+                                st));
+  return QPMS_SUCCESS;
+}
+
+// X = M^-1 B with FP64 iterative refinement (mode 1) or one FP64 solve plus
+// residual check (mode 0).  M64 (ldm), B, X (ld N): device, column-major FP64.
+int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int nrhs, double tol, int max_iter,
+                       double *resid_out, int *iters_out, cudaStream_t st) {
+  if (nrhs > nrhs_max || nrhs <= 0) {
+    set_error("dense solver: nrhs %d outside 1..%d", nrhs, nrhs_max);
+    return QPMS_EINVAL;
+  }
+  cublasHandle_t h;
+  int e;
+  if ((e = blas_handle_get(&h))) return e;
+  QG_BLAS_TRY(cublasSetStream(h, st));
+  const size_t n = (size_t)N * nrhs;
+  double *nrm = (double *)dinfo + 1;  // two doubles after the info word
+  double hb = 0, hr = 0;
+  QG_CUDA_TRY(cudaMemsetAsync(nrm, 0, 8, st));
+  norm2_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)B, nrm);
+  QG_CUDA_TRY(cudaMemcpyAsync(&hb, nrm, 8, cudaMemcpyDeviceToHost, st));
+  QG_CUDA_TRY(cudaMemcpyAsync(r64, B, n * 16, cudaMemcpyDeviceToDevice, st));
+  double prev = 1e300, rel = 0;
+  int it = 0;
+  const cuDoubleComplex one = make_cuDoubleComplex(1, 0), mone = make_cuDoubleComplex(-1, 0);
+  for (it = 0; it <= max_iter; ++it) {
+    if ((e = apply_inverse(r64, N, y64, N, nrhs, st))) return e;
+    add_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)y64, (double2 *)X, it == 0);
+    // r = B - M X (FP64)
+    QG_CUDA_TRY(cudaMemcpyAsync(r64, B, n * 16, cudaMemcpyDeviceToDevice, st));
+    QG_BLAS_TRY(cublasZgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, N, nrhs, N, &mone, (const cuDoubleComplex *)M64, (int)ldm,
+                            (const cuDoubleComplex *)X, N, &one, (cuDoubleComplex *)r64, N));
+    g_launches.fetch_add(2);
+    QG_CUDA_TRY(cudaMemsetAsync(nrm, 0, 8, st));
+    norm2_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)r64, nrm);
+    QG_CUDA_TRY(cudaMemcpyAsync(&hr, nrm, 8, cudaMemcpyDeviceToHost, st));
+    QG_CUDA_TRY(cudaStreamSynchronize(st));
+    g_launches.fetch_add(1);
+    rel = sqrt(hr / (hb > 0 ? hb : 1));
+    if (!mode || rel <= tol || rel >= 0.5 * prev) break;
+    prev = rel;
+  }
+  if (resid_out) *resid_out = rel;
+  if (iters_out) *iters_out = mode ? it + 1 : 0;
+  return QPMS_SUCCESS;
+}
+
+}  // namespace qg
+
+using namespace qg;
+
+extern "C" int qpms_gpu_dense_solve(int N, int nrhs, const qpms_complex_t *M, const qpms_complex_t *B,
+                                    qpms_complex_t *X, int mode, double *resid, int *iters) {
+  clear_error();
+  if (!M || !B || !X || N <= 0 || nrhs <= 0 || (mode != 0 && mode != 1)) {
+    set_error("invalid arguments");
+    return QPMS_EINVAL;
+  }
+  DenseSolver s;
+  int e;
+  if ((e = s.init(N, nrhs, mode, 0x5eed))) return e;
+  if ((e = s.factorize(M, N, 0))) return e;
+  return s.solve(M, N, B, X, nrhs, 1e-13, 12, resid, iters, 0);
+}

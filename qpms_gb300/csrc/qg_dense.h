@@ -1,0 +1,37 @@
+// Large dense complex solver (qg_dense.cu): RBT + blocked LU without pivoting,
+// complex64 (mixed, FP64 iterative refinement) or complex128 (plain).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace qg {
+
+// The system is padded to Np = N rounded up to a multiple of 4 (identity on the
+// padding), the size the two butterfly levels halve.
+struct DenseSolver {
+  int N = 0, Np = 0, nrhs_max = 0, mode = 0, nb = 64;
+  void *A = nullptr;       // mode 1: complex64 LU factors, Np x Np (mode 0 factors T64 in place)
+  void *T64 = nullptr;     // complex128 Np x Np: W_u^T diag(M, I) W_v
+  void *Dinv = nullptr;    // per diagonal block: L^-1 and U^-1 (nb x nb each)
+  void *work = nullptr;    // panel / RHS work buffer
+  void *rhs_lo = nullptr;  // complex64 Np x nrhs_max
+  void *rp = nullptr;      // complex128 Np x nrhs_max (padded right-hand sides)
+  void *r64 = nullptr, *y64 = nullptr;  // complex128 N x nrhs_max: residual and correction
+  int *dinfo = nullptr;    // zero-pivot flag, then two doubles of norm scratch
+  double *rs = nullptr;    // butterfly diagonals [u L1][u L2][v L1][v L2], Np each
+
+  int init(int N, int nrhs_max, int mode, unsigned long long seed);
+  void release();
+  ~DenseSolver() { release(); }
+  // M64: device, column-major complex128 N x N with leading dimension ldm
+  // (kept by the caller: the refinement residual is formed with it).
+  int factorize(const void *M64, size_t ldm, cudaStream_t st);
+  // Y = M^-1 R through the factors (one application, no refinement); N x nrhs.
+  int apply_inverse(const void *R, size_t ldr, void *Y, size_t ldy, int nrhs, cudaStream_t st);
+  // X = M^-1 B (B, X: N x nrhs, leading dimension N).  Mode 1 refines in FP64
+  // until ||B - M X||_F / ||B||_F <= tol, stagnation or max_iter; mode 0
+  // solves once.  resid_out gets the final FP64 relative residual.
+  int solve(const void *M64, size_t ldm, const void *B, void *X, int nrhs, double tol, int max_iter,
+            double *resid_out, int *iters_out, cudaStream_t st);
+};
+
+}  // namespace qg

@@ -101,26 +101,9 @@ __global__ void logdet_kernel(int nb, int N, const qg_c *LU, double *out) {
 }
 
 }  // namespace
-}  // namespace qg
-
-using namespace qg;
-
-extern "C" {
-
-double qpms_ss_adjusted_eta(const qpms_scatsys_t *ss, qpms_complex_t wavenumber, const double wavevector[3]) {
-  // scatsystem.c:68-80
-  const double eta_default = ss->per.eta;
-  const double k2 = wavevector[0] * wavevector[0] + wavevector[1] * wavevector[1] + wavevector[2] * wavevector[2];
-  const double kappa2 = wavenumber.re * wavenumber.re + wavenumber.im * wavenumber.im;
-  if (kappa2 < k2) return eta_default;
-  const int maxj = ss->c->lMax;
-  const double mina = 0.5 * (ss->lattice_dimension - 1) - maxj;
-  const double eta_min = sqrt(fabs((kappa2 - k2) * (mina - 1.) / 16.));
-  return std::max(eta_default, eta_min);
-}
 
 // Batched periodic assembly into device memory: nw frequencies x nk Bloch vectors.
-static int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_host,
+int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_host,
                                     const std::vector<qg_c> &T_host, int nk, const double *beta_host,
                                     const double *eta_host, qg_c *dM, cudaStream_t st) {
   const int lMax = ss->c->lMax, np = ss->p_count;
@@ -180,6 +163,24 @@ static int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c
     return QPMS_ERROR;
   }
   return QPMS_SUCCESS;
+}
+
+}  // namespace qg
+
+using namespace qg;
+
+extern "C" {
+
+double qpms_ss_adjusted_eta(const qpms_scatsys_t *ss, qpms_complex_t wavenumber, const double wavevector[3]) {
+  // scatsystem.c:68-80
+  const double eta_default = ss->per.eta;
+  const double k2 = wavevector[0] * wavevector[0] + wavevector[1] * wavevector[1] + wavevector[2] * wavevector[2];
+  const double kappa2 = wavenumber.re * wavenumber.re + wavenumber.im * wavenumber.im;
+  if (kappa2 < k2) return eta_default;
+  const int maxj = ss->c->lMax;
+  const double mina = 0.5 * (ss->lattice_dimension - 1) - maxj;
+  const double eta_min = sqrt(fabs((kappa2 - k2) * (mina - 1.) / 16.));
+  return std::max(eta_default, eta_min);
 }
 
 qpms_complex_t *qpms_scatsyswk_build_modeproblem_matrix_full(qpms_complex_t *target,

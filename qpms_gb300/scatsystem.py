@@ -171,6 +171,30 @@ class ScatteringSystem:
         return out
 
 
+    def find_modes(self, omega_centre, omega_rr, omega_ri, iri=None, blochvector=None, contour_points=20,
+                   rank_tol=1e-4, rank_min_sel=1, res_tol=0.0, l=None, Vhat=None, seed=None, mode=None,
+                   refine_tol=0.0):
+        """Eigenmodes inside an ellipse in the complex omega plane by Beyn's
+        method (qpms_c.pyx:841-900): dict(eigval, eigval_inside_metric,
+        eigvec, residuals, eigval_err, ranktest_SV, iri, blochvector).
+
+        Extensions: l (probe columns; the reference uses fecv_size), Vhat
+        (explicit probe matrix), seed, mode (0 plain FP64, 1 mixed), refine_tol."""
+        from . import beyn
+        if iri is not None:
+            raise NotImplementedError("irrep-packed eigenmode search is not implemented")
+        if self.lattice is None and blochvector is not None:
+            raise ValueError("a Bloch vector needs a periodic system")
+        if self.lattice is not None and blochvector is None:
+            raise ValueError("a periodic system needs a Bloch vector")
+        out = beyn.scatsys_find_modes(self.s, self.fecv_size, omega_centre, omega_rr, omega_ri, blochvector,
+                                      contour_points, rank_tol, rank_min_sel, res_tol, l, Vhat, seed, mode,
+                                      refine_tol)
+        out["iri"] = iri
+        out["blochvector"] = blochvector
+        return out
+
+
 class _ScatteringSystemAtOmega:
     def __init__(self, ss, omega):
         self.ss = ss

@@ -1,0 +1,70 @@
+"""GPU dense solver (random butterfly + blocked LU without pivoting) against numpy.
+
+Tolerances: solution within 1e-10 relative (2-norm) of numpy.linalg.solve on
+well-conditioned systems and mode-problem matrices; FP64 residual
+||B - M X|| / ||B|| <= 1e-12 in both modes (the mixed mode reaches it by FP64
+iterative refinement).
+"""
+import numpy as np
+import pytest
+
+from qpms_gb300.workloads import EV, HBAR, C0
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _solve(torch, M, B, mode):
+    import ctypes as C
+    import qpms_gb300
+    dev = torch.device("cuda:0")
+    tM = torch.from_numpy(np.asfortranarray(M).reshape(-1, order="F")).to(dev)   # column-major
+    tB = torch.from_numpy(np.asfortranarray(B).reshape(-1, order="F")).to(dev)
+    tX = torch.empty_like(tB)
+    res = np.zeros(1)
+    it = np.zeros(1, dtype=np.int32)
+    N, nrhs = B.shape
+    rc = qpms_gb300.lib().qpms_gpu_dense_solve(N, nrhs, tM.data_ptr(), tB.data_ptr(), tX.data_ptr(), mode,
+                                               res.ctypes.data, it.ctypes.data)
+    assert rc == 0, qpms_gb300.last_error()
+    X = tX.cpu().numpy().reshape((N, nrhs), order="F")
+    return X, res[0], it[0]
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("N", [256, 1000])
+def test_random_system(torch_cuda, mode, N):
+    rng = np.random.default_rng(N)
+    M = (rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))) / np.sqrt(N) + 2 * np.eye(N)
+    B = rng.normal(size=(N, 8)) + 1j * rng.normal(size=(N, 8))
+    X, res, it = _solve(torch_cuda, M, B, mode)
+    ref = np.linalg.solve(M, B)
+    assert np.linalg.norm(X - ref) <= 1e-10 * np.linalg.norm(ref)
+    assert res <= 1e-12
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_modeproblem_system(torch_cuda, orc, mode):
+    """M = I - T S of a 6 x 6 sphere array (lMax 2, N = 576) at a complex frequency."""
+    lMax = 2
+    xs = (np.arange(6) - 2.5) * 400e-9
+    X_, Y_ = np.meshgrid(xs, xs, indexing="ij")
+    pos = np.stack([X_.ravel(), Y_.ravel(), np.zeros(36)], 1)
+    om = (2.1 + 0.003j) * EV / HBAR
+    c = orc.TransCalculator(lMax)
+    Td = orc.tmatrix_sphere_diag(lMax, 60e-9, om, -12 + 1.2j, 2.25)
+    T = np.stack([np.diag(Td)] * 36)
+    M = orc.finite_modeproblem(c, pos, T, np.sqrt(2.25) * om / C0)
+    rng = np.random.default_rng(3)
+    B = rng.normal(size=(M.shape[0], 16)) + 1j * rng.normal(size=(M.shape[0], 16))
+    X, res, it = _solve(torch_cuda, M, B, mode)
+    ref = np.linalg.solve(M, B)
+    assert np.linalg.norm(X - ref) <= 1e-10 * np.linalg.norm(ref)
+    assert res <= 1e-12, res
