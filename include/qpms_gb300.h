@@ -309,13 +309,17 @@ qpms_ss_LU qpms_scatsyswk_build_modeproblem_matrix_full_LU(qpms_complex_t *targe
 
 /* Batched dispersion scan of a 2D lattice (config "2D-periodic dispersion
  * scan"): for every omega (nw, real) and in-plane Bloch vector (nk, kvecs
- * [nk][2]) assemble M = I - T W (adjusted eta), LU-factorise (FP64), and write
- * logdet[w][k] = log|det M|; optionally solve for the excitation of a plane
- * wave with in-plane wavevector = Bloch vector and E along x projected
- * perpendicular to k (x-polarised at normal incidence): f_out[w][k][fecv],
- * sigma_ext = -Re(a^H f)/k^2 per cell, resid = ||M f - T a|| / ||T a||.  Synchronous. */
+ * [nk][2]) assemble M = I - T W (adjusted eta), LU-factorise and write
+ * logdet[w][k] = log|det M| (from the factors: complex128 in mode 0,
+ * complex64 in mode 1, about 1e-6 absolute); solve for the excitation of a
+ * plane wave with in-plane wavevector = Bloch vector and E along x projected
+ * perpendicular to k (x-polarised at normal incidence), in mode 1 with FP64
+ * iterative refinement to 1e-13: f_out[w][k][fecv] (may be NULL),
+ * sigma_ext = -Re(a^H f)/k^2 per cell, resid = ||M f - T a|| / ||T a||,
+ * iters = applications of the factors.  Synchronous. */
 int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *omegas, size_t nk,
-    const double *kvecs, double *logdet, qpms_complex_t *f_out, double *sigma_ext, double *resid_out);
+    const double *kvecs, int mode, double *logdet, qpms_complex_t *f_out, double *sigma_ext,
+    double *resid_out, int *iters_out);
 
 /* Plane-wave incident vector (qpms_scatsys_incident_field_vector_full with
  * qpms_incfield_planewave, scatsystem.c:1970-1983, vswf.c:480-530), real k. */
@@ -335,10 +339,11 @@ int qpms_gpu_finite_planewave_scatter(const qpms_scatsys_t *ss, size_t nw,
 
 /* Dense complex solve X = M^-1 B on DEVICE pointers (column-major, any N):
  * random butterfly transform + blocked LU without pivoting;
- * mode 0 complex128 (plain FP64), mode 1 complex64 factors with FP64
- * iterative refinement (tensor-core GEMMs).  The solver of the Beyn contour
- * nodes (the reference factorises with LAPACKE_zgetrf/zgetrs, beyn.c:552-564).
- * resid = ||B - M X||_F / ||B||_F (FP64), iters = refinement steps.  Synchronous. */
+ * mode 0 complex128 factors (plain FP64), mode 1 complex64 factors
+ * (tensor-core GEMMs); both refined with FP64 residuals to 1e-13.  The solver
+ * of the Beyn contour nodes (the reference factorises with
+ * LAPACKE_zgetrf/zgetrs, beyn.c:552-564).  resid = ||B - M X||_F / ||B||_F
+ * (FP64), iters = applications of the factors.  Synchronous. */
 int qpms_gpu_dense_solve(int N, int nrhs, const qpms_complex_t *M, const qpms_complex_t *B,
     qpms_complex_t *X, int mode, double *resid, int *iters);
 
@@ -432,6 +437,52 @@ int qpms_gpu_beyn_probe_matrix(size_t m, size_t l, unsigned long long seed, qpms
  * thin SVD (column-major m x n, m >= n) and general eigenproblem (n x n). */
 int qpms_gpu_host_svd(int m, int n, const qpms_complex_t *A, qpms_complex_t *U, double *s, qpms_complex_t *V);
 int qpms_gpu_host_eig(int n, const qpms_complex_t *A, qpms_complex_t *w, qpms_complex_t *X);
+
+/* ---------------- serving loop (continuous batching) ---------------- */
+/* One plane-wave scattering solve (the unit of work of the reference's
+ * misc/finiterectlat-scatter.py and misc/infiniterectlat-scatter.py loops):
+ * a finite system at omega with incidence direction k_dir and polarisation E,
+ * or a 2D-periodic system at omega and in-plane Bloch vector k (incidence with
+ * that in-plane wavevector, x polarisation projected perpendicular to it).
+ * Systems come from qpms_gpu_scatsys_create_spheres[_2d].  No counterpart in
+ * the reference, which solves one request at a time. */
+typedef struct qpms_gpu_request_t {
+  const qpms_scatsys_t *ss;
+  double omega;
+  double k[2];
+  double k_dir[3];
+  qpms_complex_t E[3];
+} qpms_gpu_request_t;
+
+typedef struct qpms_gpu_result_t {
+  int status;                    /* 0 = solved */
+  int iters;                     /* refinement steps (mixed mode) */
+  int batch_size;                /* requests solved together with this one */
+  double sigma_ext;              /* extinction cross-section (per unit cell if periodic) */
+  double residual;               /* FP64 relative residual |b - M x| / |b| */
+  double t_submit, t_start, t_done;   /* seconds on the server clock */
+} qpms_gpu_result_t;
+
+typedef struct qpms_gpu_server qpms_gpu_server_t;
+
+/* A serving loop on the current device: `workers` threads with one stream
+ * each, device memory from a private pool, requests admitted while their
+ * footprint fits hbm_budget_bytes (0: 60 % of free memory).  mode 1 solves in
+ * complex64 with FP64 refinement, mode 0 in plain complex128. */
+qpms_gpu_server_t *qpms_gpu_server_create(size_t hbm_budget_bytes, int mode, int workers);
+/* Queue a request; f_out (fecv_size complex, host, may be NULL) receives the
+ * scattered-field coefficients and must stay valid until qpms_gpu_server_wait. */
+int qpms_gpu_server_submit(qpms_gpu_server_t *s, const qpms_gpu_request_t *req, qpms_complex_t *f_out,
+    uint64_t *ticket);
+/* Block until the request is solved; returns its status. */
+int qpms_gpu_server_wait(qpms_gpu_server_t *s, uint64_t ticket, qpms_gpu_result_t *out);
+/* Block until nothing is queued or running. */
+int qpms_gpu_server_drain(qpms_gpu_server_t *s);
+double qpms_gpu_server_clock(qpms_gpu_server_t *s);
+int qpms_gpu_server_stats(qpms_gpu_server_t *s, size_t *completed, size_t *batches, size_t *peak_bytes,
+    int *max_concurrent, size_t *budget_bytes);
+/* Stops the workers (drain first: queued requests are dropped). */
+void qpms_gpu_server_destroy(qpms_gpu_server_t *s);
 
 /* ---------------- diagnostics ---------------- */
 /* Thread-local message of the last failing call (empty string if none). */

@@ -1,0 +1,131 @@
+// Batched solve of many small mode-problem systems (the (omega, k) points of a
+// dispersion scan, serving batches of lattice solves): one cuBLAS batched LU
+// for all systems, then the right-hand sides.  The mixed mode factorises in
+// complex64 and recovers FP64 accuracy by iterative refinement with an FP64
+// residual (residual_kernel, one warp per row), as qg_solve.cu does for the
+// finite plane-wave scatter.  The reference factorises each matrix with
+// LAPACKE_zgetrf and solves with zgetrs (scatsystem.c:2202-2273).
+#include <math.h>
+
+#include <vector>
+
+#include "qg_assembly.h"
+#include "qg_batched.h"
+
+namespace qg {
+
+namespace {
+
+size_t al(size_t b) { return (b + 255) / 256 * 256; }
+
+template <typename T>
+__global__ void logabsdet_kernel(int nm, size_t N, const T *LU, double *out) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nm) return;
+  const T *A = LU + (size_t)b * N * N;
+  double s = 0;
+  for (size_t i = 0; i < N; ++i) s += log(hypot((double)A[i * N + i].x, (double)A[i * N + i].y));
+  out[b] = s;
+}
+
+}  // namespace
+
+size_t batched_solve_bytes(int nm, size_t N, int mode) {
+  const size_t m = (size_t)nm;
+  return al(m * N * N * (mode ? 8 : 16)) + al(m * N * 4) + al(m * 4) + 2 * al(m * 8) + al(m * N * 8) +
+         al(m * N * 16) + al(2 * m * 8);
+}
+
+int batched_solve(cublasHandle_t h, cudaStream_t st, int nm, size_t N, const qg_c *dM, const qg_c *db, qg_c *dx,
+                  int mode, double tol, int max_iter, void *scratch, double *resid_host, int *iters_host,
+                  int *info_host, double *logabsdet) {
+  if (nm <= 0) return QPMS_SUCCESS;
+  const size_t m = (size_t)nm, N2 = N * N;
+  char *p = (char *)scratch;
+  void *LU = p;
+  p += al(m * N2 * (mode ? 8 : 16));
+  int *piv = (int *)p;
+  p += al(m * N * 4);
+  int *info = (int *)p;
+  p += al(m * 4);
+  void **arrA = (void **)p;
+  p += al(m * 8);
+  void **arrB = (void **)p;
+  p += al(m * 8);
+  void *cb = p;
+  p += al(m * N * 8);
+  qg_c *r = (qg_c *)p;
+  p += al(m * N * 16);
+  double *rn2 = (double *)p, *bn2 = rn2 + m;
+  QG_BLAS_TRY(cublasSetStream(h, st));
+  {
+    std::vector<void *> pa(m), pb(m);
+    for (size_t i = 0; i < m; ++i) {
+      pa[i] = (char *)LU + i * N2 * (mode ? 8 : 16);
+      pb[i] = mode ? (void *)((char *)cb + i * N * 8) : (void *)(dx + i * N);
+    }
+    QG_CUDA_TRY(cudaMemcpyAsync(arrA, pa.data(), m * 8, cudaMemcpyHostToDevice, st));
+    QG_CUDA_TRY(cudaMemcpyAsync(arrB, pb.data(), m * 8, cudaMemcpyHostToDevice, st));
+    QG_CUDA_TRY(cudaStreamSynchronize(st));  // pa, pb are local
+  }
+  std::vector<double> hr(m), hb(m);
+  std::vector<int> its(m, 0);
+  int e, hinfo = 0;
+  // the row-major buffers read column-major are M^T: factorise M^T and solve with OP_T
+  if (mode == 0) {
+    QG_CUDA_TRY(cudaMemcpyAsync(LU, dM, m * N2 * 16, cudaMemcpyDeviceToDevice, st));
+    QG_CUDA_TRY(cudaMemcpyAsync(dx, db, m * N * 16, cudaMemcpyDeviceToDevice, st));
+    QG_BLAS_TRY(cublasZgetrfBatched(h, (int)N, (cuDoubleComplex **)arrA, (int)N, piv, info, nm));
+    QG_BLAS_TRY(cublasZgetrsBatched(h, CUBLAS_OP_T, (int)N, 1, (const cuDoubleComplex *const *)arrA, (int)N, piv,
+                                    (cuDoubleComplex **)arrB, (int)N, &hinfo, nm));
+    g_launches.fetch_add(2);
+    if ((e = launch_residual(nm, N, dM, dx, db, r, rn2, bn2, st))) return e;
+    QG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, m * 8, cudaMemcpyDeviceToHost, st));
+    QG_CUDA_TRY(cudaMemcpyAsync(hb.data(), bn2, m * 8, cudaMemcpyDeviceToHost, st));
+    QG_CUDA_TRY(cudaStreamSynchronize(st));
+  } else {
+    if ((e = launch_c128_to_c64(m * N2, dM, LU, st))) return e;
+    QG_BLAS_TRY(cublasCgetrfBatched(h, (int)N, (cuComplex **)arrA, (int)N, piv, info, nm));
+    g_launches.fetch_add(1);
+    QG_CUDA_TRY(cudaMemcpyAsync(r, db, m * N * 16, cudaMemcpyDeviceToDevice, st));
+    double prev = 1e300;
+    for (int it = 0; it <= max_iter; ++it) {
+      if ((e = launch_c128_to_c64(m * N, r, cb, st))) return e;
+      QG_BLAS_TRY(cublasCgetrsBatched(h, CUBLAS_OP_T, (int)N, 1, (const cuComplex *const *)arrA, (int)N, piv,
+                                      (cuComplex **)arrB, (int)N, &hinfo, nm));
+      g_launches.fetch_add(1);
+      if ((e = launch_add_c64(m * N, cb, dx, it == 0, st))) return e;
+      if ((e = launch_residual(nm, N, dM, dx, db, r, rn2, bn2, st))) return e;
+      QG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, m * 8, cudaMemcpyDeviceToHost, st));
+      QG_CUDA_TRY(cudaMemcpyAsync(hb.data(), bn2, m * 8, cudaMemcpyDeviceToHost, st));
+      QG_CUDA_TRY(cudaStreamSynchronize(st));
+      double worst = 0;
+      for (size_t i = 0; i < m; ++i) {
+        const double rel = sqrt(hr[i] / (hb[i] > 0 ? hb[i] : 1));
+        if (rel > tol) its[i] = it + 1;
+        worst = fmax(worst, rel);
+      }
+      if (worst <= tol || worst >= 0.5 * prev) break;  // converged or stagnated
+      prev = worst;
+    }
+  }
+  if (logabsdet) {
+    if (mode)
+      logabsdet_kernel<float2><<<(nm + 127) / 128, 128, 0, st>>>(nm, N, (const float2 *)LU, logabsdet);
+    else
+      logabsdet_kernel<double2><<<(nm + 127) / 128, 128, 0, st>>>(nm, N, (const double2 *)LU, logabsdet);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+  }
+  if (info_host) {
+    QG_CUDA_TRY(cudaMemcpyAsync(info_host, info, m * 4, cudaMemcpyDeviceToHost, st));
+    QG_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  for (size_t i = 0; i < m; ++i) {
+    if (resid_host) resid_host[i] = sqrt(hr[i] / (hb[i] > 0 ? hb[i] : 1));
+    if (iters_host) iters_host[i] = mode ? its[i] + 1 : 0;
+  }
+  return QPMS_SUCCESS;
+}
+
+}  // namespace qg

@@ -311,6 +311,21 @@ namespace {
 __global__ void pad_identity_kernel(double2 *A, size_t Np, size_t N) {
   for (size_t i = N + threadIdx.x; i < Np; i += blockDim.x) A[i * Np + i] = make_double2(1, 0);
 }
+// dst (column-major, leading dimension ldd) = M for M given row-major N x N
+// with leading dimension lds: dst[i + j ldd] = src[i lds + j]; 32 x 32 tiles.
+__global__ void rowmajor_to_colmajor_kernel(size_t N, const double2 *src, size_t lds, double2 *dst, size_t ldd) {
+  __shared__ double2 tile[32][33];
+  const size_t i0 = (size_t)blockIdx.y * 32, j0 = (size_t)blockIdx.x * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {  // read rows i0 + r, columns j0 + threadIdx.x
+    const size_t i = i0 + r, j = j0 + threadIdx.x;
+    if (i < N && j < N) tile[r][threadIdx.x] = src[i * lds + j];
+  }
+  __syncthreads();
+  for (int c = threadIdx.y; c < 32; c += blockDim.y) {  // write column j0 + c, rows i0 + threadIdx.x
+    const size_t i = i0 + threadIdx.x, j = j0 + c;
+    if (i < N && j < N) dst[i + j * ldd] = tile[threadIdx.x][c];
+  }
+}
 cublasComputeType_t lowp_compute() {
   const char *ev = getenv("QPMS_GB300_LU_COMPUTE");
   if (ev && !strcmp(ev, "32F")) return CUBLAS_COMPUTE_32F;
@@ -319,8 +334,11 @@ cublasComputeType_t lowp_compute() {
 }
 }  // namespace
 
-int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed) {
+int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed, cudaMemPool_t pool_,
+                      cudaStream_t alloc_stream) {
   release();
+  pool = pool_;
+  ast = alloc_stream;
   if (N_ <= 0 || nrhs_max_ <= 0 || (mode_ != 0 && mode_ != 1)) {
     set_error("dense solver: invalid size N = %d, nrhs = %d or mode %d", N_, nrhs_max_, mode_);
     return QPMS_EINVAL;
@@ -334,29 +352,49 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed)
   const size_t NN = (size_t)Np * Np;
   const int nblk = (Np + nb - 1) / nb;
   size_t wsz = std::max<size_t>((size_t)Np * nb, (size_t)nb * std::max(Np, nrhs_max)) * esz;
-  if (mode) QG_CUDA_TRY(cudaMalloc(&A, NN * esz));
-  QG_CUDA_TRY(cudaMalloc(&T64, NN * 16));
-  QG_CUDA_TRY(cudaMalloc(&Dinv, (size_t)nblk * 2 * nb * nb * esz));
-  QG_CUDA_TRY(cudaMalloc(&work, wsz));
-  QG_CUDA_TRY(cudaMalloc(&rhs_lo, (size_t)Np * nrhs_max * 8));
-  QG_CUDA_TRY(cudaMalloc(&rp, (size_t)Np * nrhs_max * 16));
-  QG_CUDA_TRY(cudaMalloc(&r64, (size_t)N * nrhs_max * 16));
-  QG_CUDA_TRY(cudaMalloc(&y64, (size_t)N * nrhs_max * 16));
-  QG_CUDA_TRY(cudaMalloc(&dinfo, 16));
-  QG_CUDA_TRY(cudaMalloc(&rs, (size_t)4 * Np * sizeof(double)));
+  if (mode) QG_CUDA_TRY(dev_alloc(&A, NN * esz));
+  QG_CUDA_TRY(dev_alloc(&T64, NN * 16));
+  QG_CUDA_TRY(dev_alloc(&Dinv, (size_t)nblk * 2 * nb * nb * esz));
+  QG_CUDA_TRY(dev_alloc(&work, wsz));
+  QG_CUDA_TRY(dev_alloc(&rhs_lo, (size_t)Np * nrhs_max * 8));
+  QG_CUDA_TRY(dev_alloc(&rp, (size_t)Np * nrhs_max * 16));
+  QG_CUDA_TRY(dev_alloc(&r64, (size_t)N * nrhs_max * 16));
+  QG_CUDA_TRY(dev_alloc(&y64, (size_t)N * nrhs_max * 16));
+  QG_CUDA_TRY(dev_alloc(&dinfo, 16));
+  QG_CUDA_TRY(dev_alloc(&rs, (size_t)4 * Np * sizeof(double)));
   // random butterfly diagonals exp(r/10), r ~ U(-1/2, 1/2): [u level1][u level2][v level1][v level2]
   std::mt19937_64 gen(seed);
   std::uniform_real_distribution<double> U(-0.5, 0.5);
   std::vector<double> h(4 * (size_t)Np);
   for (auto &v : h) v = exp(U(gen) / 10);
-  QG_CUDA_TRY(cudaMemcpy(rs, h.data(), h.size() * 8, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpyAsync(rs, h.data(), h.size() * 8, cudaMemcpyHostToDevice, ast));
+  QG_CUDA_TRY(cudaStreamSynchronize(ast));  // h is a local buffer
   return QPMS_SUCCESS;
+}
+
+size_t DenseSolver::footprint(int N, int nrhs, int mode) {
+  const size_t Np = (size_t)(N + 3) / 4 * 4, nb = mode ? 128 : 64, esz = mode ? 8 : 16;
+  const size_t nblk = (Np + nb - 1) / nb;
+  size_t b = (mode ? Np * Np * esz : 0) + Np * Np * 16 + nblk * 2 * nb * nb * esz;
+  b += std::max<size_t>(Np * nb, nb * std::max<size_t>(Np, nrhs)) * esz;
+  b += Np * nrhs * (8 + 16) + (size_t)N * nrhs * 32 + 16 + 4 * Np * 8;
+  return b + 10 * 512;  // allocation rounding
+}
+
+cudaError_t DenseSolver::dev_alloc(void *ptr, size_t bytes) {
+  void **pp = (void **)ptr;
+  return pool ? cudaMallocFromPoolAsync(pp, bytes, pool, ast) : cudaMalloc(pp, bytes);
 }
 
 void DenseSolver::release() {
   for (void *p : {(void *)A, (void *)T64, (void *)Dinv, (void *)work, (void *)rhs_lo, (void *)rp, (void *)r64,
                   (void *)y64, (void *)dinfo, (void *)rs})
-    if (p) cudaFree(p);
+    if (p) {
+      if (pool)
+        cudaFreeAsync(p, ast);
+      else
+        cudaFree(p);
+    }
   A = T64 = Dinv = work = rhs_lo = rp = nullptr;
   r64 = y64 = nullptr;
   dinfo = nullptr;
@@ -383,7 +421,8 @@ static int rbt_right_solution(const DenseSolver &s, double2 *X, size_t ld, size_
   return QPMS_SUCCESS;
 }
 
-int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st) {
+int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st, bool rowmaj) {
+  row_major = rowmaj;
   const size_t NN = (size_t)Np * Np;
   cublasHandle_t h;
   int e;
@@ -392,8 +431,15 @@ int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st) {
   QG_CUDA_TRY(cudaMemsetAsync(dinfo, 0, 4, st));
   // T64 = W_u^T diag(M, I) W_v   (M W = column pass with level 2 first: M L2 L1)
   if (Np != N) QG_CUDA_TRY(cudaMemsetAsync(T64, 0, NN * 16, st));
-  QG_CUDA_TRY(cudaMemcpy2DAsync(T64, (size_t)Np * 16, M64, ldm * 16, (size_t)N * 16, N, cudaMemcpyDeviceToDevice,
-                                st));
+  if (rowmaj) {
+    const dim3 g((unsigned)((N + 31) / 32), (unsigned)((N + 31) / 32)), b(32, 8);
+    rowmajor_to_colmajor_kernel<<<g, b, 0, st>>>(N, (const double2 *)M64, ldm, (double2 *)T64, Np);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+  } else {
+    QG_CUDA_TRY(cudaMemcpy2DAsync(T64, (size_t)Np * 16, M64, ldm * 16, (size_t)N * 16, N,
+                                  cudaMemcpyDeviceToDevice, st));
+  }
   if (Np != N) {
     pad_identity_kernel<<<1, 32, 0, st>>>((double2 *)T64, Np, N);
     g_launches.fetch_add(1);
@@ -455,8 +501,10 @@ int DenseSolver::apply_inverse(const void *R, size_t ldr, void *Y, size_t ldy, i
   return QPMS_SUCCESS;
 }
 
-// X = M^-1 B with FP64 iterative refinement (mode 1) or one FP64 solve plus
-// residual check (mode 0).  M64 (ldm), B, X (ld N): device, column-major FP64.
+// X = M^-1 B with FP64 iterative refinement: in mode 1 it recovers FP64
+// accuracy from the complex64 factors; in mode 0 it usually stops after the
+// first solve and otherwise removes the growth of pivot-free elimination.
+// M64 (ldm), B, X (ld N): device FP64.
 int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int nrhs, double tol, int max_iter,
                        double *resid_out, int *iters_out, cudaStream_t st) {
   if (nrhs > nrhs_max || nrhs <= 0) {
@@ -482,8 +530,10 @@ int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int 
     add_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)y64, (double2 *)X, it == 0);
     // r = B - M X (FP64)
     QG_CUDA_TRY(cudaMemcpyAsync(r64, B, n * 16, cudaMemcpyDeviceToDevice, st));
-    QG_BLAS_TRY(cublasZgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, N, nrhs, N, &mone, (const cuDoubleComplex *)M64, (int)ldm,
-                            (const cuDoubleComplex *)X, N, &one, (cuDoubleComplex *)r64, N));
+    // a row-major M read column-major is M^T: multiply with OP_T
+    QG_BLAS_TRY(cublasZgemm(h, row_major ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, N, nrhs, N, &mone,
+                            (const cuDoubleComplex *)M64, (int)ldm, (const cuDoubleComplex *)X, N, &one,
+                            (cuDoubleComplex *)r64, N));
     g_launches.fetch_add(2);
     QG_CUDA_TRY(cudaMemsetAsync(nrm, 0, 8, st));
     norm2_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)r64, nrm);
@@ -491,11 +541,11 @@ int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int 
     QG_CUDA_TRY(cudaStreamSynchronize(st));
     g_launches.fetch_add(1);
     rel = sqrt(hr / (hb > 0 ? hb : 1));
-    if (!mode || rel <= tol || rel >= 0.5 * prev) break;
+    if (rel <= tol || rel >= 0.5 * prev) break;  // converged or stagnated
     prev = rel;
   }
   if (resid_out) *resid_out = rel;
-  if (iters_out) *iters_out = mode ? it + 1 : 0;
+  if (iters_out) *iters_out = it + 1;  // applications of the factors
   return QPMS_SUCCESS;
 }
 

@@ -19,19 +19,34 @@ struct DenseSolver {
   int *dinfo = nullptr;    // zero-pivot flag, then two doubles of norm scratch
   double *rs = nullptr;    // butterfly diagonals [u L1][u L2][v L1][v L2], Np each
 
-  int init(int N, int nrhs_max, int mode, unsigned long long seed);
+  // Stream-ordered allocation: with a memory pool, every buffer comes from
+  // cudaMallocFromPoolAsync on stream `ast` and returns to it in release(),
+  // so a serving loop allocates without synchronising the device.
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t ast = nullptr;
+  bool row_major = false;  // set by factorize(): M64 is row-major (the reference's layout)
+
+  int init(int N, int nrhs_max, int mode, unsigned long long seed, cudaMemPool_t pool = nullptr,
+           cudaStream_t alloc_stream = nullptr);
   void release();
   ~DenseSolver() { release(); }
-  // M64: device, column-major complex128 N x N with leading dimension ldm
-  // (kept by the caller: the refinement residual is formed with it).
-  int factorize(const void *M64, size_t ldm, cudaStream_t st);
+  // M64: device complex128 N x N with leading dimension ldm, column-major, or
+  // row-major if rowmaj (kept by the caller: the refinement residual is formed
+  // with it).
+  int factorize(const void *M64, size_t ldm, cudaStream_t st, bool rowmaj = false);
   // Y = M^-1 R through the factors (one application, no refinement); N x nrhs.
   int apply_inverse(const void *R, size_t ldr, void *Y, size_t ldy, int nrhs, cudaStream_t st);
-  // X = M^-1 B (B, X: N x nrhs, leading dimension N).  Mode 1 refines in FP64
-  // until ||B - M X||_F / ||B||_F <= tol, stagnation or max_iter; mode 0
-  // solves once.  resid_out gets the final FP64 relative residual.
+  // X = M^-1 B (B, X: N x nrhs, leading dimension N), refined with FP64
+  // residuals until ||B - M X||_F / ||B||_F <= tol, stagnation or max_iter.
+  // resid_out gets the final FP64 relative residual, iters_out the number of
+  // applications of the factors.
   int solve(const void *M64, size_t ldm, const void *B, void *X, int nrhs, double tol, int max_iter,
             double *resid_out, int *iters_out, cudaStream_t st);
+  // Device bytes init() allocates for (N, nrhs, mode).
+  static size_t footprint(int N, int nrhs, int mode);
+
+ private:
+  cudaError_t dev_alloc(void *ptr, size_t bytes);
 };
 
 }  // namespace qg

@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
   for (size_t u = blockIdx.x; u < units; u += gridDim.x) {
     const int pr = (int)(u % (size_t)(np * np));
     const size_t wk = u / (size_t)(np * np);
-    const int ik = (int)(wk % a.nk), iw = (int)(wk / a.nk);
+    const int iw = (int)(wk / a.nk), ik = a.paired ? iw : (int)(wk % a.nk);
     const int R = pr / np, C = pr - R * np;
     const qg_c k = a.k[iw];
     const double eta = a.eta[wk];

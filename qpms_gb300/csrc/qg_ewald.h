@@ -34,6 +34,7 @@ struct EwaldArgs {
   const double *eta;   // [nw * nk] Ewald parameters
   qg_c *M;             // [nw * nk][N][N]
   int *err;            // set to 1 if a unit's lattice-point range exceeded the bound
+  int paired = 0;      // 1: nk == 1 and matrix w uses Bloch vector beta[w] (a list of (omega, k) pairs)
 };
 
 // Bound on the lattice points one unit may enumerate per sum.

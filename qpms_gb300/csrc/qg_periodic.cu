@@ -7,9 +7,11 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "qg_assembly.h"
+#include "qg_batched.h"
 #include "qg_ewald.h"
 #include "qg_internal.h"
 #include "qg_specfunc.cuh"
@@ -102,15 +104,41 @@ __global__ void logdet_kernel(int nb, int N, const qg_c *LU, double *out) {
 
 }  // namespace
 
+// The lattice constants live in __constant__ memory, one lattice at a time:
+// every Ewald assembly (any thread, any stream) holds this lock from the
+// constant upload until its kernel has finished.
+std::mutex &ewald_mutex() {
+  static std::mutex m;
+  return m;
+}
+
+// Upload the lattice constants of ss and run the Ewald assembly described by
+// a (device buffers filled by the caller, *a.err zeroed here) on stream st;
+// returns after the kernel has finished.
+int ewald_assemble_locked(const qpms_scatsys_t *ss, const EwaldArgs &a, cudaStream_t st) {
+  EwaldConst ec;
+  int e;
+  if ((e = build_ewald_const(ss, ss->c->lMax, &ec))) return e;
+  std::lock_guard<std::mutex> lk(ewald_mutex());
+  QG_CUDA_TRY(cudaMemsetAsync(a.err, 0, 4, st));
+  if ((e = ewald_upload_constants(ec, st))) return e;
+  if ((e = launch_ewald_assemble(a, priv(ss->c)->dev, st))) return e;
+  int herr = 0;
+  QG_CUDA_TRY(cudaMemcpyAsync(&herr, a.err, 4, cudaMemcpyDeviceToHost, st));
+  QG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr) {
+    set_error("Ewald sum: lattice-point range above the bound (wavenumber or eta out of range)");
+    return QPMS_ERROR;
+  }
+  return QPMS_SUCCESS;
+}
+
 // Batched periodic assembly into device memory: nw frequencies x nk Bloch vectors.
 int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_host,
                                     const std::vector<qg_c> &T_host, int nk, const double *beta_host,
                                     const double *eta_host, qg_c *dM, cudaStream_t st) {
-  const int lMax = ss->c->lMax, np = ss->p_count;
-  EwaldConst ec;
+  const int np = ss->p_count;
   int e;
-  if ((e = build_ewald_const(ss, lMax, &ec))) return e;
-  if ((e = ewald_upload_constants(ec, st))) return e;
   std::vector<double> pos(3 * np);
   std::vector<int> tm(np);
   for (int i = 0; i < np; ++i) {
@@ -131,7 +159,6 @@ int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_hos
     }
   Dev dpos, dtm, dT, dk, dbeta, deta, derr;
   if ((e = dalloc(derr, 4))) return e;
-  QG_CUDA_TRY(cudaMemsetAsync(derr.p, 0, 4, st));
   if ((e = dalloc(dpos, pos.size() * 8)) || (e = dalloc(dtm, np * 4)) || (e = dalloc(dT, T_host.size() * 16)) ||
       (e = dalloc(dk, nw * 16)) || (e = dalloc(dbeta, nk * 16)) || (e = dalloc(deta, (size_t)nw * nk * 8)))
     return e;
@@ -154,15 +181,7 @@ int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_hos
   a.eta = deta.as<double>();
   a.M = dM;
   a.err = derr.as<int>();
-  if ((e = launch_ewald_assemble(a, priv(ss->c)->dev, st))) return e;
-  int herr = 0;
-  QG_CUDA_TRY(cudaMemcpyAsync(&herr, derr.p, 4, cudaMemcpyDeviceToHost, st));
-  QG_CUDA_TRY(cudaStreamSynchronize(st));
-  if (herr) {
-    set_error("Ewald sum: lattice-point range above the bound (wavenumber or eta out of range)");
-    return QPMS_ERROR;
-  }
-  return QPMS_SUCCESS;
+  return ewald_assemble_locked(ss, a, st);
 }
 
 }  // namespace qg
@@ -234,25 +253,24 @@ qpms_ss_LU qpms_scatsyswk_build_modeproblem_matrix_full_LU(qpms_complex_t *targe
 }
 
 int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *omegas, size_t nk,
-                           const double *kvecs, double *logdet, qpms_complex_t *f_out, double *sigma_ext,
-                           double *resid_out) {
+                           const double *kvecs, int mode, double *logdet, qpms_complex_t *f_out, double *sigma_ext,
+                           double *resid_out, int *iters_out) {
   clear_error();
   if (!scatsys_is_own(ss) || ss->lattice_dimension != 2) {
     set_error("system must come from qpms_gpu_scatsys_create_spheres_2d");
     return QPMS_EINVAL;
   }
   if (!omegas || !kvecs || !logdet) { set_error("NULL argument"); return QPMS_EINVAL; }
+  if (mode != 0 && mode != 1) { set_error("mode must be 0 (FP64) or 1 (mixed)"); return QPMS_EINVAL; }
   if (!nw || !nk) return QPMS_SUCCESS;
   const int lMax = scatsys_lmax(ss), np = ss->p_count, ntm = ss->tm_count, n = 2 * lMax * (lMax + 2);
   const size_t N = ss->fecv_size, N2 = N * N;
   cublasHandle_t h;
   int e;
   if ((e = blas_handle_get(&h))) return e;
-  QG_BLAS_TRY(cublasSetStream(h, 0));
   // process in chunks of whole frequencies, <= ~2 GiB of matrices per chunk
   const size_t per_w = nk * N2 * 16;
   const int wchunk = (int)std::max<size_t>(1, std::min<size_t>(nw, (size_t(2) << 30) / per_w));
-  std::vector<qg_c> coef;
   std::vector<double> pos(3 * np);
   std::vector<int> tm(np);
   for (int i = 0; i < np; ++i) {
@@ -261,26 +279,18 @@ int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *om
     pos[3 * i + 2] = ss->p[i].pos.z;
     tm[i] = ss->p[i].tmatrix_id;
   }
-  Dev dM, dLU, dpiv, dinfo, darr, darrb, dlog, dT, dtm, dpos, dk, dkv, dcoef, da, db, dx, dr, dn, dsig;
+  Dev dM, dscr, dlog, dT, dtm, dpos, dk, dkv, dcf, da, db, dx, dsig;
   const size_t nmat = (size_t)wchunk * nk;
-  if ((e = dalloc(dM, nmat * N2 * 16)) || (e = dalloc(dLU, nmat * N2 * 16)) || (e = dalloc(dpiv, nmat * N * 4)) ||
-      (e = dalloc(dinfo, nmat * 4)) || (e = dalloc(darr, nmat * 8)) || (e = dalloc(darrb, nmat * 8)) ||
+  if ((e = dalloc(dM, nmat * N2 * 16)) || (e = dalloc(dscr, batched_solve_bytes((int)nmat, N, mode))) ||
       (e = dalloc(dlog, nmat * 8)) || (e = dalloc(dtm, np * 4)) || (e = dalloc(dpos, np * 24)) ||
       (e = dalloc(da, nmat * N * 16)) || (e = dalloc(db, nmat * N * 16)) || (e = dalloc(dx, nmat * N * 16)) ||
-      (e = dalloc(dr, nmat * N * 16)) || (e = dalloc(dn, nmat * 16)) || (e = dalloc(dsig, nmat * 8)) ||
-      (e = dalloc(dk, nmat * 16)) || (e = dalloc(dkv, nmat * 24)) || (e = dalloc(dT, nmat * ntm * n * 16)))
+      (e = dalloc(dsig, nmat * 8)) || (e = dalloc(dk, nmat * 16)) || (e = dalloc(dkv, nmat * 24)) ||
+      (e = dalloc(dT, nmat * ntm * n * 16)) || (e = dalloc(dcf, nmat * n * 16)))
     return e;
   QG_CUDA_TRY(cudaMemcpy(dtm.p, tm.data(), np * 4, cudaMemcpyHostToDevice));
   QG_CUDA_TRY(cudaMemcpy(dpos.p, pos.data(), np * 24, cudaMemcpyHostToDevice));
-  {
-    std::vector<void *> pa(nmat), pb(nmat);
-    for (size_t i = 0; i < nmat; ++i) {
-      pa[i] = dLU.as<char>() + i * N2 * 16;
-      pb[i] = dx.as<char>() + i * N * 16;
-    }
-    QG_CUDA_TRY(cudaMemcpy(darr.p, pa.data(), nmat * 8, cudaMemcpyHostToDevice));
-    QG_CUDA_TRY(cudaMemcpy(darrb.p, pb.data(), nmat * 8, cudaMemcpyHostToDevice));
-  }
+  std::vector<double> res(nmat);
+  std::vector<int> its(nmat), info(nmat);
   for (size_t w0 = 0; w0 < nw; w0 += wchunk) {
     const int W = (int)std::min<size_t>(wchunk, nw - w0);
     const size_t nm = (size_t)W * nk;
@@ -322,46 +332,28 @@ int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *om
       }
     }
     if ((e = periodic_assemble_device(ss, W, k.data(), T, (int)nk, kvecs, eta.data(), dM.as<qg_c>(), 0))) return e;
-    QG_CUDA_TRY(cudaMemcpy(dLU.p, dM.p, nm * N2 * 16, cudaMemcpyDeviceToDevice));
-    // factorise M^T (the row-major buffer read column-major): same |det|
-    QG_BLAS_TRY(cublasZgetrfBatched(h, (int)N, darr.as<cuDoubleComplex *>(), (int)N, dpiv.as<int>(),
-                                    dinfo.as<int>(), (int)nm));
-    g_launches.fetch_add(1);
-    logdet_kernel<<<(unsigned)((nm + 127) / 128), 128>>>((int)nm, (int)N, dLU.as<qg_c>(), dlog.as<double>());
-    QG_CUDA_TRY(cudaGetLastError());
-    g_launches.fetch_add(1);
+    // per-matrix incidence (coefficients and phases differ per (w, k)), b = T a
+    QG_CUDA_TRY(cudaMemcpy(dcf.p, coefs.data(), coefs.size() * 16, cudaMemcpyHostToDevice));
+    QG_CUDA_TRY(cudaMemcpy(dkv.p, kvec.data(), nm * 24, cudaMemcpyHostToDevice));
+    QG_CUDA_TRY(cudaMemcpy(dk.p, kk.data(), nm * 16, cudaMemcpyHostToDevice));
+    QG_CUDA_TRY(cudaMemcpy(dT.p, Tm.data(), Tm.size() * 16, cudaMemcpyHostToDevice));
+    if ((e = launch_incident((int)nm, np, n, dcf.as<qg_c>(), dkv.as<double>(), dpos.as<double>(), da.as<qg_c>(), 0,
+                             (size_t)n)))
+      return e;
+    if ((e = launch_apply_t((int)nm, np, n, ntm, 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(), db.as<qg_c>(), 0)))
+      return e;
+    // LU (complex128, or complex64 + FP64 refinement), log|det| from the factors
+    if ((e = batched_solve(h, 0, (int)nm, N, dM.as<qg_c>(), db.as<qg_c>(), dx.as<qg_c>(), mode, 1e-13, 12, dscr.p,
+                           res.data(), its.data(), info.data(), dlog.as<double>())))
+      return e;
     QG_CUDA_TRY(cudaMemcpy(logdet + w0 * nk, dlog.p, nm * 8, cudaMemcpyDeviceToHost));
-    if (f_out || sigma_ext || resid_out) {
-      // per-matrix incidence: coefficients and phases differ per (w, k)
-      Dev dcf;
-      if ((e = dalloc(dcf, coefs.size() * 16))) return e;
-      QG_CUDA_TRY(cudaMemcpy(dcf.p, coefs.data(), coefs.size() * 16, cudaMemcpyHostToDevice));
-      QG_CUDA_TRY(cudaMemcpy(dkv.p, kvec.data(), nm * 24, cudaMemcpyHostToDevice));
-      QG_CUDA_TRY(cudaMemcpy(dk.p, kk.data(), nm * 16, cudaMemcpyHostToDevice));
-      QG_CUDA_TRY(cudaMemcpy(dT.p, Tm.data(), Tm.size() * 16, cudaMemcpyHostToDevice));
-      if ((e = launch_incident((int)nm, np, n, dcf.as<qg_c>(), dkv.as<double>(), dpos.as<double>(), da.as<qg_c>(), 0,
-                               (size_t)n)))
-        return e;
-      if ((e = launch_apply_t((int)nm, np, n, ntm, 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(), db.as<qg_c>(), 0)))
-        return e;
-      QG_CUDA_TRY(cudaMemcpy(dx.p, db.p, nm * N * 16, cudaMemcpyDeviceToDevice));
-      int info = 0;
-      QG_BLAS_TRY(cublasZgetrsBatched(h, CUBLAS_OP_T, (int)N, 1, darr.as<const cuDoubleComplex *>(), (int)N,
-                                      dpiv.as<int>(), darrb.as<cuDoubleComplex *>(), (int)N, &info, (int)nm));
-      g_launches.fetch_add(1);
-      double *rn2 = dn.as<double>(), *bn2 = rn2 + nm;
-      if ((e = launch_residual((int)nm, N, dM.as<qg_c>(), dx.as<qg_c>(), db.as<qg_c>(), dr.as<qg_c>(), rn2, bn2, 0)))
-        return e;
-      if ((e = launch_sigma_ext((int)nm, N, da.as<qg_c>(), dx.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), 0)))
-        return e;
-      if (sigma_ext) QG_CUDA_TRY(cudaMemcpy(sigma_ext + w0 * nk, dsig.p, nm * 8, cudaMemcpyDeviceToHost));
-      if (f_out) QG_CUDA_TRY(cudaMemcpy(f_out + w0 * nk * N, dx.p, nm * N * 16, cudaMemcpyDeviceToHost));
-      if (resid_out) {
-        std::vector<double> hr(nm), hb(nm);
-        QG_CUDA_TRY(cudaMemcpy(hr.data(), rn2, nm * 8, cudaMemcpyDeviceToHost));
-        QG_CUDA_TRY(cudaMemcpy(hb.data(), bn2, nm * 8, cudaMemcpyDeviceToHost));
-        for (size_t m = 0; m < nm; ++m) resid_out[w0 * nk + m] = hb[m] > 0 ? sqrt(hr[m] / hb[m]) : 0.0;
-      }
+    if ((e = launch_sigma_ext((int)nm, N, da.as<qg_c>(), dx.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), 0)))
+      return e;
+    if (sigma_ext) QG_CUDA_TRY(cudaMemcpy(sigma_ext + w0 * nk, dsig.p, nm * 8, cudaMemcpyDeviceToHost));
+    if (f_out) QG_CUDA_TRY(cudaMemcpy(f_out + w0 * nk * N, dx.p, nm * N * 16, cudaMemcpyDeviceToHost));
+    for (size_t m = 0; m < nm; ++m) {
+      if (resid_out) resid_out[w0 * nk + m] = res[m];
+      if (iters_out) iters_out[w0 * nk + m] = its[m];
     }
   }
   return QPMS_SUCCESS;

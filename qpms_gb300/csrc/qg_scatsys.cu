@@ -356,6 +356,18 @@ static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *
                                       const double *radius, const qpms_complex_t *eps_inside,
                                       qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1, const double *b2);
 
+// One translation calculator per lMax (default normalisation), built on first
+// use and shared by every system of this library for the life of the process:
+// its device tables stay resident, so making a system costs no device work.
+static qpms_trans_calculator *shared_calculator(int lMax) {
+  static std::mutex m;
+  static qpms_trans_calculator *calc[16] = {nullptr};
+  std::lock_guard<std::mutex> lk(m);
+  if (lMax < 1 || lMax >= 16) return nullptr;
+  if (!calc[lMax]) calc[lMax] = qpms_trans_calculator_init(lMax, QPMS_NORMALISATION_DEFAULT);
+  return calc[lMax];
+}
+
 qpms_scatsys_t *qpms_gpu_scatsys_create_spheres(int np, const double *pos_xyz, const int *kind, int nkinds,
                                                 const double *radius, const qpms_complex_t *eps_inside,
                                                 qpms_complex_t eps_medium, qpms_l_t lMax) {
@@ -442,7 +454,7 @@ static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *
     P.per.unitcell_volume = fabs(det);
     P.per.eta = sqrt(M_PI) / sqrt(fabs(det));
   }
-  P.c = qpms_trans_calculator_init(lMax, QPMS_NORMALISATION_DEFAULT);
+  P.c = shared_calculator(lMax);
   if (!P.c) {
     delete s;
     return nullptr;
@@ -452,9 +464,7 @@ static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *
 
 void qpms_gpu_scatsys_free(qpms_scatsys_t *ss) {
   if (!ss) return;
-  ScatsysPriv *s = sspriv(ss);
-  if (s->pub.c) qpms_trans_calculator_free(s->pub.c);
-  delete s;
+  delete sspriv(ss);  // the translation calculator is shared (shared_calculator)
 }
 
 qpms_scatsys_at_omega_t *qpms_gpu_scatsys_at_omega(const qpms_scatsys_t *ss, qpms_complex_t omega) {

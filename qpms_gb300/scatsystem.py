@@ -56,7 +56,7 @@ def declare(L):
     L.qpms_scatsyswk_build_modeproblem_matrix_full.restype = vp
     L.qpms_scatsyswk_build_modeproblem_matrix_full.argtypes = [vp, C.POINTER(_SSWK)]
     L.qpms_gpu_periodic_scan.restype = ci
-    L.qpms_gpu_periodic_scan.argtypes = [vp, sz, vp, sz, vp, vp, vp, vp, vp]
+    L.qpms_gpu_periodic_scan.argtypes = [vp, sz, vp, sz, vp, ci, vp, vp, vp, vp, vp]
     L.qpms_gpu_debug_cerfc.restype = ci
     L.qpms_gpu_debug_cerfc.argtypes = [cd, cd, vp]
     L.qpms_gpu_finite_planewave_scatter.restype = ci
@@ -125,22 +125,23 @@ class ScatteringSystem:
         kv[:len(kvec)] = kvec
         return self._L.qpms_ss_adjusted_eta(self.s, k.real, k.imag, kv.ctypes.data)
 
-    def dispersion_scan(self, omegas, kvecs, want_f=False, want_sigma=True):
+    def dispersion_scan(self, omegas, kvecs, want_f=False, want_sigma=True, mode=1):
         """Batched 2D-lattice scan: log|det M(omega, k)| for all pairs, plus the
-        plane-wave excitation (f, sigma_ext per cell, residual)."""
+        plane-wave excitation (f, sigma_ext per cell, residual, refinement
+        steps).  mode 1: complex64 LU + FP64 refinement; mode 0: complex128 LU."""
         om = np.ascontiguousarray(omegas, dtype=np.float64)
         kv = np.ascontiguousarray(kvecs, dtype=np.float64).reshape(-1, 2)
         nw, nk = om.size, kv.shape[0]
         logdet = np.empty((nw, nk))
-        sig = np.empty((nw, nk)) if want_sigma else None
-        res = np.empty((nw, nk)) if want_sigma else None
+        sig = np.empty((nw, nk))
+        res = np.empty((nw, nk))
+        its = np.empty((nw, nk), dtype=np.int32)
         f = np.empty((nw, nk, self.fecv_size), dtype=np.complex128) if want_f else None
-        rc = self._L.qpms_gpu_periodic_scan(self.s, nw, om.ctypes.data, nk, kv.ctypes.data, logdet.ctypes.data,
-                                            f.ctypes.data if want_f else None,
-                                            sig.ctypes.data if want_sigma else None,
-                                            res.ctypes.data if want_sigma else None)
+        rc = self._L.qpms_gpu_periodic_scan(self.s, nw, om.ctypes.data, nk, kv.ctypes.data, int(mode),
+                                            logdet.ctypes.data, f.ctypes.data if want_f else None,
+                                            sig.ctypes.data, res.ctypes.data, its.ctypes.data)
         _lib.check(rc, "qpms_gpu_periodic_scan")
-        out = {"logdet": logdet}
+        out = {"logdet": logdet, "iters": its}
         if want_sigma:
             out["sigma_ext"] = sig
             out["residual"] = res

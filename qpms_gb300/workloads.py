@@ -66,3 +66,43 @@ def honeycomb_path(a=580e-9, n=4096):
     """Gamma - K - M - Gamma of the hexagonal lattice with b1 = (a, 0), b2 = (a/2, a sqrt3/2)."""
     G, K, M = (0, 0), (4 * np.pi / (3 * a), 0), (np.pi / a, np.pi / (np.sqrt(3) * a))
     return kpath([G, K, M, G], n)
+
+
+def jittered_square_cluster(nspheres, rng, pitch=400e-9, jitter=0.1):
+    """nspheres positions on a square grid (row by row, side ceil(sqrt n)),
+    each displaced uniformly by up to +-jitter * pitch in x and y, centred."""
+    side = int(np.ceil(np.sqrt(nspheres)))
+    idx = np.arange(nspheres)
+    xy = np.stack([idx % side, idx // side], 1).astype(float) * pitch
+    xy += rng.uniform(-jitter, jitter, size=xy.shape) * pitch
+    xy -= xy.mean(axis=0)
+    return np.concatenate([xy, np.zeros((nspheres, 1))], axis=1)
+
+
+def serving_requests(n, seed=0, nmin=16, nmax=400, lmaxes=(2, 3, 4), finite_frac=0.7, a=580e-9):
+    """Seeded request mix of the serving workload: finite clusters (N uniform
+    in [nmin, nmax] spheres of r = 50 nm on a jittered 400 nm grid, lMax drawn
+    from lmaxes, normal incidence) and single (omega, k) solves of the square
+    and honeycomb lattices (r = 80 nm, lMax 3, a = 580 nm, k on the
+    high-symmetry paths); hbar omega uniform in 1.6-2.6 eV.  Returns specs."""
+    rng = np.random.default_rng(seed)
+    sq = square_path(a, 64)
+    hx = honeycomb_path(a, 64)
+    out = []
+    for _ in range(n):
+        om = rng.uniform(1.6, 2.6) * EV / HBAR
+        if rng.uniform() < finite_frac:
+            ns = int(rng.integers(nmin, nmax + 1))
+            out.append({"kind": "finite", "positions": jittered_square_cluster(ns, rng),
+                        "lMax": int(rng.choice(lmaxes)), "omega": om})
+        else:
+            lat = "square" if rng.uniform() < 0.5 else "honeycomb"
+            path = sq if lat == "square" else hx
+            out.append({"kind": "lattice", "lattice": lat, "k": tuple(path[rng.integers(len(path))]), "omega": om})
+    return out
+
+
+def poisson_arrivals(n, rate, seed=0):
+    """Arrival times (s) of a Poisson stream of n requests at `rate` per second."""
+    rng = np.random.default_rng(seed + 7919)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))

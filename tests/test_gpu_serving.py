@@ -1,0 +1,138 @@
+"""Serving loop (continuous batching) on the GPU.
+
+Each result must be the same alone and in the mix: the scattered-field
+coefficients of every request, solved by itself on an idle server and solved
+inside a concurrent mixed stream (batched with other lattice requests,
+overlapping with cluster solves on other workers), agree within the
+excitation-coefficient tolerance 1e-9 (relative 2-norm); both solve the
+oracle's system (the reference's M = I - T S / I - T W) to a 1e-10 normwise
+backward error and
+match its LAPACK solution to 1e-9 (scaled by cond(M) / 1e3 where that is
+larger: the matrices themselves agree to about 1e-12), and every FP64 residual
+is <= 1e-10.
+"""
+import numpy as np
+import pytest
+
+from qpms_gb300.workloads import EV, HBAR, honeycomb_lattice, jittered_square_cluster, square_lattice
+
+pytestmark = pytest.mark.gpu
+F_RTOL = 1e-9
+C0 = 299792458.0
+
+
+@pytest.fixture(scope="module")
+def mix():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import qpms_gb300
+    rng = np.random.default_rng(11)
+    b1, b2, p1 = square_lattice()
+    h1, h2, p2 = honeycomb_lattice()
+    sq = qpms_gb300.ScatteringSystem(p1, 80e-9, -12 + 1.2j, 2.25, 3, lattice=(b1, b2))
+    hc = qpms_gb300.ScatteringSystem(p2, 80e-9, -12 + 1.2j, 2.25, 3, lattice=(h1, h2))
+    reqs = []
+    for i in range(6):   # clusters: N 256 .. 1800 unknowns (batched and dense paths)
+        ns, lMax = [(16, 2), (20, 3), (40, 2), (30, 3), (18, 2), (24, 4)][i]
+        pos = jittered_square_cluster(ns, rng)
+        ss = qpms_gb300.ScatteringSystem(pos, 50e-9, -12 + 1.2j, 2.25, lMax)
+        reqs.append({"system": ss, "omega": rng.uniform(1.6, 2.6) * EV / HBAR, "positions": pos, "lMax": lMax,
+                     "radius": 50e-9})
+    a = 580e-9
+    for i in range(12):  # lattice solves, both lattices, random k in the first zone
+        ss, pos, bb = (sq, p1, (b1, b2)) if i % 2 == 0 else (hc, p2, (h1, h2))
+        k = tuple(rng.uniform(-0.4, 0.4, 2) * np.pi / a)
+        reqs.append({"system": ss, "omega": rng.uniform(1.6, 2.6) * EV / HBAR, "k": k, "positions": pos,
+                     "lMax": 3, "radius": 80e-9, "basis": bb})
+    return reqs
+
+
+def _alone(reqs, mode):
+    from qpms_gb300.serving import Server
+    srv = Server(mode=mode, workers=1)
+    out = []
+    for r in reqs:
+        t = srv.submit(r["system"], r["omega"], r.get("k", (0.0, 0.0)))
+        out.append(srv.wait(t))
+    srv.close()
+    return out
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def test_same_alone_and_in_mix(mix):
+    from qpms_gb300.serving import Server, run_trace
+    alone = _alone(mix, 1)
+    srv = Server(mode=1, workers=4)
+    together, summary = run_trace(srv, mix, None, want_f=True)
+    st = srv.stats()
+    srv.close()
+    assert summary["failed"] == 0
+    assert st["max_concurrent"] >= 2          # work overlapped on the device
+    assert summary["mean_batch"] > 1          # lattice requests were batched
+    for a, b in zip(alone, together):
+        assert a["status"] == 0 and b["status"] == 0
+        assert a["residual"] <= 1e-10 and b["residual"] <= 1e-10
+        assert _rel(b["f"], a["f"]) <= F_RTOL
+        assert abs(b["sigma_ext"] - a["sigma_ext"]) <= 1e-9 * abs(a["sigma_ext"])
+
+
+def test_mixed_matches_plain_and_oracle(mix, orc):
+    mixed = _alone(mix, 1)
+    plain = _alone(mix, 0)
+    calcs = {}
+    for r, m, p in zip(mix, mixed, plain):
+        assert _rel(m["f"], p["f"]) <= F_RTOL
+        lMax = r["lMax"]
+        calc = calcs.setdefault(lMax, orc.TransCalculator(lMax))
+        om = r["omega"]
+        Td = orc.tmatrix_sphere_diag(lMax, r["radius"], om, -12 + 1.2j, 2.25)
+        pos = r["positions"]
+        T = np.ascontiguousarray(np.broadcast_to(np.diag(Td), (pos.shape[0], Td.size, Td.size)))
+        k = 1.5 * om / C0
+        if "k" in r:
+            b1, b2 = r["basis"]
+            kv = np.array([r["k"][0], r["k"][1], 0.0])
+            eta = orc.adjusted_eta(abs(b1[0] * b2[1] - b1[1] * b2[0]), k, kv, lMax)
+            M = orc.periodic_modeproblem(calc, pos, T, k, b1, b2, kv, eta)
+            b2_ = kv[0] ** 2 + kv[1] ** 2
+            kd = np.array([kv[0], kv[1], np.sqrt(k.real ** 2 - b2_)])
+            E = np.array([1.0, 0, 0]) - kd[0] * kd / (kd @ kd)
+            E = E / np.linalg.norm(E)
+        else:
+            M = orc.finite_modeproblem(calc, pos, T, k)
+            kd = np.array([0, 0, k.real])
+            E = np.array([1.0, 0, 0])
+        a_inc = orc.planewave_full(lMax, pos, kd, E)
+        rhs = (T @ a_inc.reshape(pos.shape[0], -1, 1)).reshape(-1)
+        f_ref = np.linalg.solve(M, rhs)
+        # the library's f solves the oracle's system to the residual bound, and
+        # is within 1e-9 of the oracle's solution up to the conditioning of M
+        # (the two matrices agree to ~1e-12 relative, not exactly)
+        # normwise backward error of the library's f in the oracle's system
+        be = np.linalg.norm(M @ m["f"] - rhs) / (np.linalg.norm(M) * np.linalg.norm(m["f"]) + np.linalg.norm(rhs))
+        assert be <= 1e-10, be
+        kappa = np.linalg.cond(M)
+        assert _rel(m["f"], f_ref) <= F_RTOL * max(1.0, kappa / 1e3), (r.get("k"), lMax, kappa)
+
+
+def test_admission_by_memory(mix):
+    """A budget that holds one cluster at a time still serves everything, and a
+    request above the budget is refused at submission."""
+    from qpms_gb300 import QpmsGpuError
+    from qpms_gb300.serving import Server, run_trace
+    big = max(r["system"].fecv_size for r in mix)
+    budget = int(60 * big * big)
+    srv = Server(hbm_budget=budget, mode=1, workers=4)
+    _, summary = run_trace(srv, mix, None)
+    st = srv.stats()
+    assert summary["failed"] == 0 and st["peak_bytes"] <= budget
+    import qpms_gb300
+    huge = qpms_gb300.ScatteringSystem(jittered_square_cluster(400, np.random.default_rng(1)), 50e-9,
+                                       -12 + 1.2j, 2.25, 4)
+    with pytest.raises(QpmsGpuError):
+        srv.submit(huge, 3e15)
+    srv.close()
