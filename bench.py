@@ -14,6 +14,19 @@ e2e:    the same through the C-ABI host entry point
         (H2D of inputs and D2H of all A/B arrays inside the timed region).
 --impl reference: the CPU restatement of the reference's translation path
         (the reference itself needs GSL + AMOS, absent here) on all host cores.
+
+Secondary objects in the same JSON line (rank 0), each the other workloads of
+the path measured mixed (complex64 LU + FP64 refinement) against the plain
+FP64 GPU path at a <= 1e-10 relative residual:
+  modeproblem - finite 4x4 sphere array, lMax 2 (256 x 256), 32 frequencies:
+                assembly + LU + solve + sigma_ext per frequency;
+  dispersion  - square (30 x 30) and honeycomb (60 x 60) lattices, lMax 3:
+                (omega, k) points/s of assembly + LU + log|det| + excitation;
+  beyn        - 30 x 30 array, lMax 2 (14,400 x 14,400), 64 contour nodes,
+                64 probe columns; the plain path timed on one node x 64;
+  serving     - seeded request stream (70 % clusters of 16-400 spheres,
+                lMax 2-4; 30 % lattice points): solves/s and p50/p99 latency
+                at saturation and at Poisson arrival rates.
 """
 import argparse
 import json
@@ -43,6 +56,8 @@ def parse():
     ap.add_argument("--nvec", type=int, default=N_VEC)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--sections", default="modeproblem,dispersion,beyn,serving",
+                    help="secondary workloads reported beside the headline (comma list, or 'none')")
     return ap.parse_args()
 
 
@@ -296,6 +311,7 @@ def run_ours(args, ws, rank, local):
     if rank == 0:
         cb = None if args.no_cpu else cpu_baseline(args)
         sm = clk.summary(local)
+        sections = run_sections(args)
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -305,6 +321,7 @@ def run_ours(args, ws, rank, local):
                "per_kernel": per_kernel, "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
                "gpu_launches": int(launches), "clocks": sm,
                "plain_fp64_path": "this path is FP64 throughout (the plain path itself): ratio 1"}
+        out.update(sections)
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
@@ -366,6 +383,146 @@ def run_e2e(args, calcs, kr, th, ph, ws):
     return {"value": solves / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "ms_per_step": dt * 1e3, "host_output_buffer_vectors": {str(k): v[0] for k, v in bufs.items()},
             "path": "qpms_gpu_trans_AB_arrays_batch_host (C-ABI), pinned host buffers"}
+
+
+def _sq(nx, pitch):
+    xs = (np.arange(nx) - (nx - 1) / 2) * pitch
+    X, Y = np.meshgrid(xs, xs, indexing="ij")
+    return np.stack([X.ravel(), Y.ravel(), np.zeros(nx * nx)], 1)
+
+
+def section_modeproblem(args):
+    """Finite 4x4 array, lMax 2, 32 frequencies: plain vs mixed, and the CPU oracle."""
+    import torch
+    import qpms_gb300
+    from qpms_gb300.workloads import EV, HBAR
+    ss = qpms_gb300.ScatteringSystem(_sq(4, 400e-9), 50e-9, -12 + 1.2j, 2.25, 2)
+    om = np.linspace(1.6, 2.6, 32) * EV / HBAR
+    out = {"workload": "finite 4x4 spheres, pitch 400 nm, r 50 nm, lMax 2 (256 x 256), 32 omegas, "
+                       "normal incidence: assembly + LU + solve + sigma_ext"}
+    for mode, name in ((0, "plain_fp64"), (1, "mixed")):
+        for _ in range(3):
+            ss.planewave_scatter_batch(om, mode=mode)
+        ts = []
+        for _ in range(10):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = ss.planewave_scatter_batch(om, mode=mode)
+            ts.append(time.perf_counter() - t0)
+        ts = np.array(ts)
+        out[name] = {"solves_per_s": float(32 / np.median(ts)), "ms_per_32": float(np.median(ts) * 1e3),
+                     "p50_ms": float(np.percentile(ts, 50) * 1e3), "p99_ms": float(np.percentile(ts, 99) * 1e3),
+                     "max_residual": float(r["residual"].max())}
+    out["mixed_vs_plain"] = out["mixed"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    if not args.no_cpu:
+        from oracle import orc
+        c = orc.TransCalculator(2)
+        t0 = time.perf_counter()
+        for w in om:
+            orc.finite_sphere_scatter(c, _sq(4, 400e-9), 50e-9, -12 + 1.2j, 2.25, w)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"solves_per_s": 32 / dt, "cores": orc.num_threads(), "kind": "port",
+                               "sample": "all 32 frequencies"}
+    return out
+
+
+def section_dispersion(args):
+    import torch
+    import qpms_gb300
+    from qpms_gb300.workloads import EV, HBAR, honeycomb_lattice, honeycomb_path, square_lattice, square_path
+    out = {"workload": "sample of 32 omegas x 256 k of each 4096 k x 256 omega scan, lMax 3, r 80 nm, a 580 nm"}
+    om = np.linspace(1.6, 2.6, 32) * EV / HBAR
+    for lat in ("square", "honeycomb"):
+        b1, b2, pos = square_lattice() if lat == "square" else honeycomb_lattice()
+        ss = qpms_gb300.ScatteringSystem(pos, 80e-9, -12 + 1.2j, 2.25, 3, lattice=(b1, b2))
+        kp = (square_path if lat == "square" else honeycomb_path)(n=256)
+        ss.dispersion_scan(om[:2], kp[:8])
+        d = {}
+        for mode, name in ((0, "plain_fp64"), (1, "mixed")):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = ss.dispersion_scan(om, kp, mode=mode)
+            dt = time.perf_counter() - t0
+            d[name] = {"points_per_s": om.size * kp.shape[0] / dt, "max_residual": float(r["residual"].max()),
+                       "full_scan_s": 4096 * 256 / (om.size * kp.shape[0] / dt)}
+        d["mixed_vs_plain"] = d["mixed"]["points_per_s"] / d["plain_fp64"]["points_per_s"]
+        out[lat] = d
+    return out
+
+
+def section_beyn(args):
+    import qpms_gb300
+    from qpms_gb300.workloads import EV, HBAR
+    ss = qpms_gb300.ScatteringSystem(_sq(30, 400e-9), 60e-9, -12 + 1.2j, 2.25, 2)
+    c, rr, ri = 2.1 * EV / HBAR, 0.05 * EV / HBAR, 0.005 * EV / HBAR
+    r = ss.find_modes(c, rr, ri, contour_points=64, rank_tol=1e-4, l=64, seed=12345, mode=1)
+    out = {"workload": "30x30 spheres r 60 nm, lMax 2 (14400 x 14400), ellipse 2.1 eV +- 0.05 / 0.005 eV, "
+                       "64 nodes, L 64",
+           "mixed": {"total_s": r["total_s"], "quadrature_s": r["quadrature_s"],
+                     "node_residual_max": r["node_residual_max"], "refine_iters_max": r["node_refine_iters_max"],
+                     "neig": int(r["eigval"].size), "inside": int((r["eigval_inside_metric"] < 1).sum())}}
+    one = {}
+    for mode in (0, 1):
+        q = ss.find_modes(c, rr, ri, contour_points=1, rank_tol=1e-4, l=64, seed=12345, mode=mode)
+        one[mode] = q["quadrature_s"]
+    out["per_node_s"] = {"plain_fp64": one[0], "mixed": one[1]}
+    out["plain_fp64_estimate_s"] = 64 * one[0]
+    out["mixed_vs_plain"] = 64 * one[0] / r["quadrature_s"]
+    return out
+
+
+def section_serving(args):
+    import qpms_gb300
+    from qpms_gb300.serving import Server, run_trace
+    from qpms_gb300.workloads import honeycomb_lattice, poisson_arrivals, serving_requests, square_lattice
+    b1, b2, p1 = square_lattice()
+    h1, h2, p2 = honeycomb_lattice()
+    lat = {"square": qpms_gb300.ScatteringSystem(p1, 80e-9, -12 + 1.2j, 2.25, 3, lattice=(b1, b2)),
+           "honeycomb": qpms_gb300.ScatteringSystem(p2, 80e-9, -12 + 1.2j, 2.25, 3, lattice=(h1, h2))}
+    n = 60
+    reqs = []
+    for s in serving_requests(n, seed=5):
+        if s["kind"] == "finite":
+            reqs.append({"system": qpms_gb300.ScatteringSystem(s["positions"], 50e-9, -12 + 1.2j, 2.25, s["lMax"]),
+                         "omega": s["omega"]})
+        else:
+            reqs.append({"system": lat[s["lattice"]], "omega": s["omega"], "k": s["k"]})
+    srv = Server(mode=1, workers=4)
+    run_trace(srv, reqs[:8])
+    _, sat = run_trace(srv, reqs)
+    st = srv.stats()
+    sweep = {}
+    for rate in (5.0, 20.0):
+        _, sweep[str(rate)] = run_trace(srv, reqs, poisson_arrivals(n, rate, 1))
+    srv.close()
+    sub = reqs[:12]
+    res = {}
+    for mode, name in ((0, "plain_fp64"), (1, "mixed")):
+        srv = Server(mode=mode, workers=4)
+        _, res[name] = run_trace(srv, sub)
+        srv.close()
+    return {"workload": "%d seeded requests: 70%% clusters N 16-400 spheres (jittered 400 nm grid, r 50 nm, "
+                        "lMax 2-4), 30%% lattice (omega, k) solves; 4 worker streams" % n,
+            "mean_unknowns": float(np.mean([r["system"].fecv_size for r in reqs])),
+            "saturated": sat, "poisson": sweep, "server": st,
+            "subsample_12": res,
+            "mixed_vs_plain": res["mixed"]["solves_per_s"] / res["plain_fp64"]["solves_per_s"]}
+
+
+def run_sections(args):
+    out = {}
+    names = [x for x in args.sections.split(",") if x and x != "none"]
+    for nm in names:
+        fn = globals().get("section_" + nm)
+        if fn is None:
+            continue
+        try:
+            t0 = time.perf_counter()
+            out[nm] = fn(args)
+            out[nm]["bench_s"] = time.perf_counter() - t0
+        except Exception as e:  # a failing secondary section must not hide the headline
+            out[nm] = {"error": repr(e)}
+    return out
 
 
 def main():

@@ -247,7 +247,11 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
             uu = cmk(0.0, -g * k.re / (2 * eta));
           }
         } else {
-          const qg_c z = cscale(rk, rb);
+          // z = rb / k as C's real / complex division forms it: (rb + 0i)(conj k) / |k|^2.
+          // The sign of a zero imaginary part (rb = 0, i.e. beta on a reciprocal
+          // lattice point) picks the branch of a1 below, so it must be +0 as there.
+          const double kk2 = k.re * k.re + k.im * k.im;
+          const qg_c z = cmk((rb * k.re + 0.0 * k.im) / kk2, (0.0 * k.re - rb * k.im) / kk2);
           qg_c a1 = cmk(z.re - 1, z.im), a2 = cmk(z.re + 1, z.im);
           a2 = (a2.re < 0 && a2.im <= 0) ? cscale(csqrt_(a2), -1.0) : csqrt_(a2);
           a1 = (a1.re < 0 && a1.im >= 0) ? cscale(csqrt_(a1), -1.0) : csqrt_(a1);
@@ -256,7 +260,7 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
           const qg_c x2 = cmul(x, x);
           if (x2.re > 56.0) continue;
           uu = csqrt_(x2);
-          if (x2.re < 0 && x2.im >= 0) uu = cscale(uu, -1.0);  // branch m = -1 (ewald.c:390-393)
+          if (x2.re < 0 && !signbit(x2.im)) uu = cscale(uu, -1.0);  // branch m = -1 (ewald.c:390-393)
         }
         qg_c G[LE / 2 + 1];
         gamma_half_down(uu, LE / 2, G);
@@ -332,7 +336,7 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
         uu = cmk(0.0, -k.re / (2 * eta));
       } else {
         uu = csqrt_(z);
-        if (z.re < 0 && z.im >= 0) uu = cscale(uu, -1.0);
+        if (z.re < 0 && !signbit(z.im)) uu = cscale(uu, -1.0);  // ewald.c:266-268
       }
       qg_c G[2];
       gamma_half_down(uu, 1, G);

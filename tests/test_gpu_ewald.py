@@ -54,6 +54,30 @@ def test_periodic_M_vs_oracle(gpu, orc, lat, E, kv):
     assert np.linalg.norm(M - O) <= 1e-9 * np.linalg.norm(O - I), np.linalg.norm(M - O) / np.linalg.norm(O - I)
 
 
+CASES_COMPLEX = [("square", 1.72 + 0.05j, (0.0, 0.0)), ("square", 1.909 - 0.0788j, (0.0, 0.0)),
+                 ("square", 2.1 + 0.02j, (3e6, 1e6)), ("honeycomb", 2.3 + 0.05j, (0.0, 0.0)),
+                 ("honeycomb", 2.3 - 0.05j, (4e6, -2e6))]
+
+
+@pytest.mark.parametrize("lat,E,kv", CASES_COMPLEX)
+def test_periodic_M_complex_omega(gpu, orc, lat, E, kv):
+    """Complex frequencies (Beyn contours), both signs of Im omega, Bloch
+    vectors on and off a reciprocal lattice point; plus eta invariance."""
+    lMax = 3
+    b1, b2, pos = square_lattice() if lat == "square" else honeycomb_lattice()
+    ss = gpu.ScatteringSystem(pos, RAD, EPS_I, EPS_E, lMax, lattice=(b1, b2))
+    om = E * EV / HBAR
+    ke = np.sqrt(EPS_E) * om / C0
+    eta = ss.adjusted_eta(ke, kv)
+    M = ss(om).modeproblem_matrix_full(k=kv)
+    M2 = ss(om).modeproblem_matrix_full(k=kv, eta=1.3 * eta)
+    O = _oracle_M(orc, lMax, pos, b1, b2, om, kv, eta)
+    I = np.eye(len(M))
+    assert np.linalg.norm(M - O) <= 1e-10 * np.linalg.norm(O)
+    assert np.linalg.norm(M - O) <= 1e-9 * np.linalg.norm(O - I)
+    assert np.linalg.norm(M2 - M) <= 1e-9 * np.linalg.norm(M - I)
+
+
 def test_eta_invariance_gpu(gpu):
     lMax = 3
     b1, b2, pos = honeycomb_lattice()
