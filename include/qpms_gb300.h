@@ -162,6 +162,24 @@ typedef struct qpms_vswf_set_spec_t {                                /* qpms_typ
   qpms_normalisation_t norm;
 } qpms_vswf_set_spec_t;
 
+/* Replaces qpms_trans_calculator_get_trans_array (translations.h:129-135,
+ * translations.c:701-722): the translation operator between two VSWF sets
+ * (same normalisation as c, lMax <= c->lMax, no longitudinal waves) for one
+ * displacement kdlj, target[srci * srcstride + desti * deststride] = A or B
+ * (translations_inlines.h:8-35); computed on the GPU. */
+int qpms_trans_calculator_get_trans_array(const qpms_trans_calculator *c, qpms_complex_t *target,
+    const qpms_vswf_set_spec_t *destspec, size_t deststride,
+    const qpms_vswf_set_spec_t *srcspec, size_t srcstride,
+    csph_t kdlj, bool r_ge_d, qpms_bessel_t J);
+
+/* Replaces qpms_trans_calculator_get_trans_array_lc3p (translations.h:139-149,
+ * translations.c:796-812): the same from wavenumber k and cartesian positions,
+ * kdlj = k * (destpos - srcpos) in spherical coordinates, r_ge_d = false. */
+int qpms_trans_calculator_get_trans_array_lc3p(const qpms_trans_calculator *c, qpms_complex_t *target,
+    const qpms_vswf_set_spec_t *destspec, size_t deststride,
+    const qpms_vswf_set_spec_t *srcspec, size_t srcstride,
+    qpms_complex_t k, cart3_t destpos, cart3_t srcpos, qpms_bessel_t J);
+
 typedef struct qpms_tmatrix_t {                                      /* qpms_types.h:338-351 */
   const qpms_vswf_set_spec_t *spec;
   qpms_complex_t *m;  /* row-major spec->n x spec->n */
@@ -348,7 +366,6 @@ int qpms_gpu_dense_solve(int N, int nrhs, const qpms_complex_t *M, const qpms_co
     qpms_complex_t *X, int mode, double *resid, int *iters);
 
 /* ---------------- Beyn contour-integral eigensolver (beyn.h) ---------------- */
-typedef int qpms_iri_t;               /* qpms_types.h:323 */
 #define QPMS_NO_IRREP ((qpms_iri_t) -1)   /* qpms_types.h:325 */
 
 /* M(z) into target (row-major m x m), beyn.h:22. */

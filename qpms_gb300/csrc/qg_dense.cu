@@ -75,32 +75,54 @@ __device__ __forceinline__ T rcp(T b) {
 }
 
 // ---------------- diagonal block: LU without pivoting + triangular inverses ----------------
-// D (kb x kb, column-major in global, leading dimension lda) is factored in
-// place (unit-lower L below the diagonal, U on and above); Linv and Uinv are
-// written to out (column-major kb x kb each).  info is set to 1 on an exactly
-// zero pivot.
+// D (kb x kb, kb <= 128 and a multiple of 32 except for the last block,
+// column-major in global, leading dimension lda) is factored in place
+// (unit-lower L below the diagonal, U on and above); L^-1 and U^-1 are written
+// to Linv and Uinv (column-major kb x kb each).  info is set to 1 on an
+// exactly zero pivot.  One CTA of 1024 threads with the block in shared
+// memory:
+//   1. right-looking elimination, a 32 x 32 thread tile sweeping the trailing
+//      matrix of each step (no index division);
+//   2. the inverses by recursive doubling: each 32 x 32 diagonal block is
+//      inverted by one warp (substitution with warp barriers only), then
+//      adjacent blocks are combined level by level,
+//        [L11 0; L21 L22]^-1 = [X11 0; -X22 L21 X11  X22],
+//        [U11 U12; 0 U22]^-1 = [Y11 -Y11 U12 Y22; 0 Y22],
+//      as two small products per level through a shared-memory temporary.
+// The unit diagonal of L^-1 is implicit in shared memory (the slot holds U^-1).
+// Capacity of each doubling temporary: npair * h^2 <= 4096 for every block size
+// kb <= 128 the solver uses (h = 32: at most 2 pairs; h = 64: one pair).
+constexpr int kDiagTmp = 4096;
+
+template <typename T>
+__device__ __forceinline__ T fma_c(T acc, T a, T b) {  // acc + a b
+  return mk<T>(acc.x + a.x * b.x - a.y * b.y, acc.y + a.x * b.y + a.y * b.x);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(1024) diag_lu_inv_kernel(T *D, size_t lda, int kb, T *Linv, T *Uinv, int *info) {
   extern __shared__ __align__(16) unsigned char sm[];
-  T *S = reinterpret_cast<T *>(sm);  // [kb][kb] column-major
+  T *S = reinterpret_cast<T *>(sm);  // [kb][kb] column-major: S[c * kb + r]
+  T *TL = S + kb * kb;               // temporaries of the doubling products (kDiagTmp entries each)
+  T *TU = TL + kDiagTmp;
   const int tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5;
   for (int t = tid; t < kb * kb; t += nt) {
     const int c = t / kb, r = t - c * kb;
     S[t] = D[(size_t)c * lda + r];
   }
   __syncthreads();
+  // ---- 1. elimination ----
   for (int j = 0; j < kb; ++j) {
     const T d = S[j * kb + j];
-    if (d.x == 0 && d.y == 0) {
-      if (tid == 0) atomicOr(info, 1);
-    }
-    const T inv = (d.x == 0 && d.y == 0) ? mk<T>(0, 0) : rcp(d);
-    for (int i = j + 1 + tid; i < kb; i += nt) S[j * kb + i] = mul(S[j * kb + i], inv);
+    const bool zero = (d.x == 0 && d.y == 0);
+    if (zero && tid == 0) atomicOr(info, 1);
+    const T inv = zero ? mk<T>(0, 0) : rcp(d);
+    if (tid > j && tid < kb) S[j * kb + tid] = mul(S[j * kb + tid], inv);
     __syncthreads();
-    const int w = kb - j - 1;
-    for (int t = tid; t < w * w; t += nt) {
-      const int c = j + 1 + t / w, r = j + 1 + t % w;
-      S[c * kb + r] = sub(S[c * kb + r], mul(S[j * kb + r], S[c * kb + j]));
+    for (int c = j + 1 + warp; c < kb; c += 32) {
+      const T u = S[c * kb + j];
+      for (int r = j + 1 + lane; r < kb; r += 32) S[c * kb + r] = sub(S[c * kb + r], mul(S[j * kb + r], u));
     }
     __syncthreads();
   }
@@ -108,28 +130,99 @@ __global__ void __launch_bounds__(1024) diag_lu_inv_kernel(T *D, size_t lda, int
     const int c = t / kb, r = t - c * kb;
     D[(size_t)c * lda + r] = S[t];
   }
-  // inverses: thread c < kb computes column c of Linv, thread kb + c column c of Uinv
-  if (tid < kb) {
-    const int c = tid;
-    for (int i = 0; i < c; ++i) Linv[c * kb + i] = mk<T>(0, 0);
-    Linv[c * kb + c] = mk<T>(1, 0);
-    for (int i = c + 1; i < kb; ++i) {
-      T s = mk<T>(0, 0);
-      for (int k = c; k < i; ++k) s = sub(s, mul(S[k * kb + i], Linv[c * kb + k]));
-      Linv[c * kb + i] = s;
-    }
-  } else if (tid < 2 * kb) {
-    const int c = tid - kb;
-    for (int i = c + 1; i < kb; ++i) Uinv[c * kb + i] = mk<T>(0, 0);
-    const T ucc = S[c * kb + c];
-    Uinv[c * kb + c] = (ucc.x == 0 && ucc.y == 0) ? mk<T>(0, 0) : rcp(ucc);
-    for (int i = c - 1; i >= 0; --i) {
-      T s = mk<T>(0, 0);
-      for (int k = i + 1; k <= c; ++k) s = sub(s, mul(S[k * kb + i], Uinv[c * kb + k]));
-      const T uii = S[i * kb + i];
-      Uinv[c * kb + i] = (uii.x == 0 && uii.y == 0) ? mk<T>(0, 0) : mul(s, rcp(uii));
+  // ---- 2a. 32 x 32 diagonal blocks, one warp each: warps [0, nblk) L, [16, 16 + nblk) U ----
+  const int nb32 = (kb + 31) / 32;
+  if (warp < nb32 || (warp >= 16 && warp < 16 + nb32)) {
+    const bool isL = warp < 16;
+    const int o = (isL ? warp : warp - 16) * 32;
+    const int s = min(32, kb - o);  // block size (the last block may be short)
+    const int i = lane;
+    if (isL) {
+      // X(i, j) = -(L(i, j) + sum_{j<k<i} X(i, k) L(k, j)), columns from the right
+      for (int j = s - 2; j >= 0; --j) {
+        T acc = mk<T>(0, 0);
+        if (i > j && i < s) {
+          acc = S[(o + j) * kb + o + i];
+          for (int k = j + 1; k < i; ++k) acc = fma_c(acc, S[(o + k) * kb + o + i], S[(o + j) * kb + o + k]);
+        }
+        __syncwarp();
+        if (i > j && i < s) S[(o + j) * kb + o + i] = mk<T>(-acc.x, -acc.y);
+        __syncwarp();
+      }
+    } else {
+      // Y(j, j) = 1 / U(j, j); Y(i, j) = -(sum_{i<=k<j} Y(i, k) U(k, j)) Y(j, j), columns from the left
+      for (int j = 0; j < s; ++j) {
+        const T u = S[(o + j) * kb + o + j];
+        const T dj = (u.x == 0 && u.y == 0) ? mk<T>(0, 0) : rcp(u);
+        T acc = mk<T>(0, 0);
+        if (i < j) {
+          for (int k = i; k < j; ++k) {
+            const T yik = (k == i) ? S[(o + i) * kb + o + i] : S[(o + k) * kb + o + i];
+            acc = fma_c(acc, yik, S[(o + j) * kb + o + k]);
+          }
+        }
+        __syncwarp();
+        if (i < j) S[(o + j) * kb + o + i] = mk<T>(-(acc.x * dj.x - acc.y * dj.y), -(acc.x * dj.y + acc.y * dj.x));
+        if (i == j) S[(o + j) * kb + o + j] = dj;
+        __syncwarp();
+      }
     }
   }
+  __syncthreads();
+  // ---- 2b. doubling: blocks of size h are combined into blocks of size 2h ----
+  for (int h = 32; h < kb; h *= 2) {
+    const int npair = kb / (2 * h) + ((kb % (2 * h)) > h ? 1 : 0);
+    // products 1: TL = L21 X11, TU = U12 Y22 (h2 = rows / cols of the second block)
+    for (int t = tid; t < 2 * npair * h * h; t += nt) {
+      const bool isL = t < npair * h * h;
+      const int tt = isL ? t : t - npair * h * h;
+      const int p = tt / (h * h), e = tt - p * h * h, r = e % h, c = e / h;
+      const int o = p * 2 * h, h2 = min(h, kb - o - h);
+      if (r >= h2 && isL) continue;   // rows of L21 beyond the short block
+      if (c >= h2 && !isL) continue;  // columns of U12 beyond the short block
+      T acc = mk<T>(0, 0);
+      if (isL) {  // T(r, c) = sum_{k >= c} L21(r, k) X11(k, c), X11(c, c) = 1
+        acc = S[(o + c) * kb + o + h + r];
+        for (int k = c + 1; k < h; ++k) acc = fma_c(acc, S[(o + k) * kb + o + h + r], S[(o + c) * kb + o + k]);
+        TL[p * h * h + c * h + r] = acc;
+      } else {    // T(r, c) = sum_{k <= c} U12(r, k) Y22(k, c)
+        for (int k = 0; k <= c; ++k) acc = fma_c(acc, S[(o + h + k) * kb + o + r], S[(o + h + c) * kb + o + h + k]);
+        TU[p * h * h + c * h + r] = acc;
+      }
+    }
+    __syncthreads();
+    // products 2: X21 = -X22 TL, Y12 = -Y11 TU, written over L21 / U12
+    for (int t = tid; t < 2 * npair * h * h; t += nt) {
+      const bool isL = t < npair * h * h;
+      const int tt = isL ? t : t - npair * h * h;
+      const int p = tt / (h * h), e = tt - p * h * h, r = e % h, c = e / h;
+      const int o = p * 2 * h, h2 = min(h, kb - o - h);
+      T acc = mk<T>(0, 0);
+      if (isL) {  // X21(r, c) = -(T(r, c) + sum_{k < r} X22(r, k) T(k, c)), X22 unit lower
+        if (r >= h2) continue;
+        acc = TL[p * h * h + c * h + r];
+        for (int k = 0; k < r; ++k) acc = fma_c(acc, S[(o + h + k) * kb + o + h + r], TL[p * h * h + c * h + k]);
+        S[(o + c) * kb + o + h + r] = mk<T>(-acc.x, -acc.y);
+      } else {    // Y12(r, c) = -sum_{k >= r} Y11(r, k) T(k, c)
+        if (c >= h2) continue;
+        for (int k = r; k < h; ++k) acc = fma_c(acc, S[(o + k) * kb + o + r], TU[p * h * h + c * h + k]);
+        S[(o + h + c) * kb + o + r] = mk<T>(-acc.x, -acc.y);
+      }
+    }
+    __syncthreads();
+  }
+  for (int t = tid; t < kb * kb; t += nt) {
+    const int c = t / kb, r = t - c * kb;
+    const T v = S[t];
+    Linv[t] = r > c ? v : (r == c ? mk<T>(1, 0) : mk<T>(0, 0));
+    Uinv[t] = r <= c ? v : mk<T>(0, 0);
+  }
+}
+
+// shared memory of diag_lu_inv_kernel for block size kb
+template <typename T>
+size_t diag_smem(int kb) {
+  return ((size_t)kb * kb + 2 * (size_t)kDiagTmp) * sizeof(T);
 }
 
 // ---------------- random butterfly transforms (FP64) ----------------
@@ -210,6 +303,17 @@ template <typename T>
 int gemm(cublasHandle_t h, int m, int n, int k, T alpha, const T *A, size_t lda, const T *B, size_t ldb, T beta,
          T *C, size_t ldc, cublasComputeType_t ct) {
   const cudaDataType_t dt = CTraits<T>::dt;
+  // cuBLAS's default (performant) strategy keeps complex64 GEMMs on the SIMT
+  // path; eager emulation runs them as BF16x9 on the tensor cores, 2.5x faster
+  // on the trailing updates (and closer to FP32 than the SIMT kernels) but
+  // slower on skinny shapes (panels, right-hand sides), whose per-call
+  // overhead dominates: those stay on FP32 SIMT.
+  if (ct == CUBLAS_COMPUTE_32F_EMULATED_16BFX9) {
+    if ((double)m * n * k >= 2.7e8)
+      cublasSetEmulationStrategy(h, CUBLAS_EMULATION_STRATEGY_EAGER);
+    else
+      ct = CUBLAS_COMPUTE_32F;
+  }
   cublasStatus_t s = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &alpha, A, dt, (int)lda, B, dt, (int)ldb,
                                   &beta, C, dt, (int)ldc, ct, CUBLAS_GEMM_DEFAULT);
   if (s == CUBLAS_STATUS_NOT_SUPPORTED && ct != CUBLAS_COMPUTE_32F && ct != CUBLAS_COMPUTE_64F) {
@@ -244,13 +348,12 @@ T cval(double r) {
 template <typename T>
 int lu_nopiv(cublasHandle_t h, int N, int nb, T *A, size_t lda, T *Dinv, T *work, int *dinfo,
              cublasComputeType_t ct, cudaStream_t st) {
-  const size_t smem = (size_t)nb * nb * sizeof(T);
+  const size_t smem = diag_smem<T>(nb);
   QG_CUDA_TRY(cudaFuncSetAttribute(diag_lu_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   for (int k = 0, blk = 0; k < N; k += nb, ++blk) {
     const int kb = (N - k < nb) ? N - k : nb;
     T *Lk = Dinv + (size_t)blk * 2 * nb * nb, *Uk = Lk + (size_t)nb * nb;
-    diag_lu_inv_kernel<T><<<1, 1024, (size_t)kb * kb * sizeof(T), st>>>(A + (size_t)k * lda + k, lda, kb, Lk, Uk,
-                                                                        dinfo);
+    diag_lu_inv_kernel<T><<<1, 1024, diag_smem<T>(kb), st>>>(A + (size_t)k * lda + k, lda, kb, Lk, Uk, dinfo);
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
     const int m2 = N - k - kb;

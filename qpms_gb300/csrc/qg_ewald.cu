@@ -234,14 +234,17 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
         const double rb = sqrt(qx * qx + qy * qy);
         qg_c gam, uu;
         if (kreal) {
+          // clilgamma(rb / k) (ewald.h:157-170) for real k: sqrt(t - 1) sqrt(t + 1)
+          // with t - 1 exact; near a Rayleigh anomaly (t -> 1) the 1/gamma terms
+          // dominate, so gamma is formed from the exact differences as there
           const double tt = rb / k.re;
           if (tt >= 1.0) {
-            gam = cmk(sqrt(tt * tt - 1.0), 0.0);
+            gam = cmk(sqrt(tt - 1.0) * sqrt(tt + 1.0), 0.0);
             const double x = gam.re * k.re / (2 * eta);
             if (x * x > 56.0) continue;
             uu = cmk(x, 0.0);
           } else {
-            const double g = sqrt((1.0 - tt) * (1.0 + tt));
+            const double g = sqrt(1.0 - tt) * sqrt(1.0 + tt);
             gam = cmk(0.0, -g);  // -i sqrt(1 - t^2)
             // x^2 = -(g k / 2 eta)^2, approached from below the negative axis: sqrt -> -i c
             uu = cmk(0.0, -g * k.re / (2 * eta));

@@ -322,6 +322,62 @@ int qpms_trans_calculator_get_AB_arrays(const qpms_trans_calculator *c, qpms_com
                                                  kdlj.phi, r_ge_d ? 1 : 0, J);
 }
 
+int qpms_trans_calculator_get_trans_array(const qpms_trans_calculator *c, qpms_complex_t *target,
+                                          const qpms_vswf_set_spec_t *destspec, size_t deststride,
+                                          const qpms_vswf_set_spec_t *srcspec, size_t srcstride, csph_t kdlj,
+                                          bool r_ge_d, qpms_bessel_t J) {
+  clear_error();
+  if (!c || !target || !destspec || !srcspec) {
+    set_error("NULL argument");
+    return QPMS_EINVAL;
+  }
+  if (destspec->norm != c->normalisation || srcspec->norm != c->normalisation || destspec->lMax > c->lMax ||
+      srcspec->lMax > c->lMax || destspec->lMax_L >= 0 || srcspec->lMax_L >= 0) {
+    set_error("VSWF sets must share the calculator's normalisation, lMax <= %d, no longitudinal waves", c->lMax);
+    return QPMS_EINVAL;
+  }
+  const size_t ne = c->nelem;
+  std::vector<qpms_complex_t> A(ne * ne), B(ne * ne);
+  const int rc = qpms_trans_calculator_get_AB_arrays(c, A.data(), B.data(), ne, 1, kdlj, r_ge_d, J);
+  if (rc) return rc;
+  // qpms_trans_array_from_AB (translations_inlines.h:8-35); u = 4 (y + 1) + type (indexing.h:83-90)
+  for (size_t di = 0; di < destspec->n; ++di) {
+    const qpms_uvswfi_t ud = destspec->ilist[di];
+    const unsigned td = (unsigned)(ud & 3);
+    const long long yd = (long long)(ud / 4) - 1;
+    if (td == 0 || td == 3 || yd < 0 || (size_t)yd >= ne) {
+      set_error("invalid VSWF index %llx", (unsigned long long)ud);
+      return QPMS_EINVAL;
+    }
+    for (size_t si = 0; si < srcspec->n; ++si) {
+      const qpms_uvswfi_t us = srcspec->ilist[si];
+      const unsigned ts = (unsigned)(us & 3);
+      const long long ys = (long long)(us / 4) - 1;
+      if (ts == 0 || ts == 3 || ys < 0 || (size_t)ys >= ne) {
+        set_error("invalid VSWF index %llx", (unsigned long long)us);
+        return QPMS_EINVAL;
+      }
+      target[si * srcstride + di * deststride] = (ts == td) ? A[yd * ne + ys] : B[yd * ne + ys];
+    }
+  }
+  return QPMS_SUCCESS;
+}
+
+int qpms_trans_calculator_get_trans_array_lc3p(const qpms_trans_calculator *c, qpms_complex_t *target,
+                                               const qpms_vswf_set_spec_t *destspec, size_t deststride,
+                                               const qpms_vswf_set_spec_t *srcspec, size_t srcstride,
+                                               qpms_complex_t k, cart3_t destpos, cart3_t srcpos, qpms_bessel_t J) {
+  // cart2csph (vectors.h:359-365) of destpos - srcpos, then r *= k
+  const double x = destpos.x - srcpos.x, y = destpos.y - srcpos.y, z = destpos.z - srcpos.z;
+  const double r = sqrt(x * x + y * y + z * z);
+  csph_t kd;
+  kd.r.re = r * k.re;
+  kd.r.im = r * k.im;
+  kd.theta = r ? acos(z / r) : M_PI_2;
+  kd.phi = atan2(y, x);
+  return qpms_trans_calculator_get_trans_array(c, target, destspec, deststride, srcspec, srcstride, kd, false, J);
+}
+
 }  // extern "C"
 
 extern "C" int qpms_gpu_trans_multipliers_export(qpms_l_t lMax, qpms_normalisation_t nt, qpms_complex_t *A_out,

@@ -142,3 +142,49 @@ def test_full_size_parity_symmetry(torch_cuda, orc):
     tidx = torch.from_numpy(idx).to(dev)
     _check(A[tidx].cpu().numpy(), oA, "A")
     _check(B[tidx].cpu().numpy(), oB, "B")
+
+
+def test_trans_array_lc3p_vs_oracle(torch_cuda, orc):
+    """qpms_trans_calculator_get_trans_array_lc3p: a full bspec (N then M
+    waves, lMax 3) between two positions, against the oracle's A/B arranged by
+    qpms_trans_array_from_AB (translations_inlines.h:8-35)."""
+    import ctypes as C
+    import qpms_gb300
+
+    class Cplx(C.Structure):
+        _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+    class Cart3(C.Structure):
+        _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+    class Spec(C.Structure):
+        _fields_ = [("n", C.c_size_t), ("ilist", C.c_void_p), ("lMax", C.c_int), ("lMax_M", C.c_int),
+                    ("lMax_N", C.c_int), ("lMax_L", C.c_int), ("capacity", C.c_size_t), ("norm", C.c_int)]
+
+    lMax = 3
+    L = qpms_gb300.lib()
+    L.qpms_trans_calculator_get_trans_array_lc3p.restype = C.c_int
+    L.qpms_trans_calculator_get_trans_array_lc3p.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(Spec), C.c_size_t,
+                                                              C.POINTER(Spec), C.c_size_t, Cplx, Cart3, Cart3, C.c_int]
+    ys = [(t, n * (n + 1) + m) for t in (2, 1) for n in range(1, lMax + 1) for m in range(-n, n + 1)]
+    il = np.array([t + 4 * y for t, y in ys], dtype=np.uint64)
+    spec = Spec(len(ys), il.ctypes.data, lMax, lMax, lMax, -1, len(ys), 65536 | 8)
+    calc = qpms_gb300.trans_calculator(lMax)
+    rng = np.random.default_rng(5)
+    c = orc.TransCalculator(lMax)
+    for _ in range(4):
+        d = rng.normal(size=3) * 400e-9
+        k = complex(1.2e7, rng.uniform(0, 1e4))
+        for J in (1, 3):
+            out = np.zeros((len(ys), len(ys)), dtype=np.complex128)
+            rc = L.qpms_trans_calculator_get_trans_array_lc3p(calc.c, out.ctypes.data, C.byref(spec), len(ys),
+                                                              C.byref(spec), 1, Cplx(k.real, k.imag),
+                                                              Cart3(*d), Cart3(0, 0, 0), J)
+            assert rc == 0, qpms_gb300.last_error()
+            r = np.linalg.norm(d)
+            A, B = c.get_AB_arrays_single(k * r, np.arccos(d[2] / r), np.arctan2(d[1], d[0]), False, J)
+            ref = np.empty_like(out)
+            for di, (td, yd) in enumerate(ys):
+                for si, (ts, y2) in enumerate(ys):
+                    ref[di, si] = (A if ts == td else B)[yd - 1, y2 - 1]
+            assert np.linalg.norm(out - ref) <= RTOL * np.linalg.norm(ref)
