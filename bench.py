@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sections", default="modeproblem,dispersion,beyn,serving",
                     help="secondary workloads reported beside the headline (comma list, or 'none')")
+    ap.add_argument("--case", default=None,
+                    help="run one small case for a profiler and exit: dense:N:NRHS:MODE, "
+                         "scan:LATTICE:NW:NK:MODE, beyn:NX:NODES:MODE")
     return ap.parse_args()
 
 
@@ -525,8 +528,51 @@ def run_sections(args):
     return out
 
 
+def run_case(spec):
+    """One workload for a profiler (ncu) run: no timing, prints a checksum."""
+    import torch
+    import qpms_gb300
+    from qpms_gb300.workloads import EV, HBAR
+    f = spec.split(":")
+    if f[0] == "dense":
+        N, nrhs, mode = int(f[1]), int(f[2]), int(f[3])
+        dev = torch.device("cuda:0")
+        g = torch.Generator(device=dev)
+        g.manual_seed(N)
+        M = torch.randn(N, N, dtype=torch.complex128, device=dev, generator=g) / N ** 0.5
+        M += 2 * torch.eye(N, dtype=torch.complex128, device=dev)
+        B = torch.randn(nrhs, N, dtype=torch.complex128, device=dev, generator=g)
+        X = torch.empty_like(B)
+        res = np.zeros(1)
+        it = np.zeros(1, dtype=np.int32)
+        rc = qpms_gb300.lib().qpms_gpu_dense_solve(N, nrhs, M.data_ptr(), B.data_ptr(), X.data_ptr(), mode,
+                                                  res.ctypes.data, it.ctypes.data)
+        print("dense", N, nrhs, mode, "rc", rc, "resid", res[0], "iters", it[0])
+    elif f[0] == "scan":
+        from qpms_gb300.workloads import honeycomb_lattice, honeycomb_path, square_lattice, square_path
+        lat, nw, nk, mode = f[1], int(f[2]), int(f[3]), int(f[4])
+        b1, b2, pos = square_lattice() if lat == "square" else honeycomb_lattice()
+        ss = qpms_gb300.ScatteringSystem(pos, 80e-9, -12 + 1.2j, 2.25, 3, lattice=(b1, b2))
+        kp = (square_path if lat == "square" else honeycomb_path)(n=nk)
+        r = ss.dispersion_scan(np.linspace(1.6, 2.6, nw) * EV / HBAR, kp, mode=mode)
+        print("scan", lat, nw, nk, "logdet sum", float(np.sum(r["logdet"])), "max resid", float(r["residual"].max()))
+    elif f[0] == "beyn":
+        nx, nodes, mode = int(f[1]), int(f[2]), int(f[3])
+        xs = (np.arange(nx) - (nx - 1) / 2) * 400e-9
+        X_, Y_ = np.meshgrid(xs, xs, indexing="ij")
+        pos = np.stack([X_.ravel(), Y_.ravel(), np.zeros(nx * nx)], 1)
+        ss = qpms_gb300.ScatteringSystem(pos, 60e-9, -12 + 1.2j, 2.25, 2)
+        r = ss.find_modes(2.1 * EV / HBAR, 0.05 * EV / HBAR, 0.005 * EV / HBAR, contour_points=nodes,
+                          rank_tol=1e-4, l=64, seed=12345, mode=mode)
+        print("beyn", nx, nodes, "neig", r["eigval"].size, "node resid", r["node_residual_max"])
+    torch.cuda.synchronize()
+
+
 def main():
     args = parse()
+    if args.case:
+        run_case(args.case)
+        return
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, ws, rank)

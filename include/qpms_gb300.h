@@ -150,6 +150,7 @@ int qpms_gpu_trans_multipliers_export(qpms_l_t lMax, qpms_normalisation_t nt,
  * path never reads (symmetry orbits, irrep bases, generator tables) are kept as
  * opaque pointers of the same size. */
 typedef struct cart3_t { double x, y, z; } cart3_t;                 /* qpms_types.h:186-189 */
+typedef struct cart2_t { double x, y; } cart2_t;                     /* qpms_types.h:202-204 */
 typedef unsigned long long qpms_uvswfi_t;                            /* qpms_types.h:81 */
 typedef int qpms_iri_t;                                              /* qpms_types.h:323 */
 typedef int32_t qpms_ss_tmi_t, qpms_ss_tmgi_t, qpms_ss_pi_t;         /* qpms_types.h:310-316 */
@@ -324,6 +325,21 @@ qpms_complex_t *qpms_scatsyswk_build_modeproblem_matrix_full(qpms_complex_t *tar
 /* Replaces qpms_scatsyswk_build_modeproblem_matrix_full_LU (scatsystem.h:523-527). */
 qpms_ss_LU qpms_scatsyswk_build_modeproblem_matrix_full_LU(qpms_complex_t *target, int *target_piv,
     const qpms_scatsys_at_omega_k_t *sswk);
+
+/* Replace qpms_trans_calculator_get_AB_arrays_e32(_e) (translations.h:158-177,
+ * translations.c:926-1078): lattice-summed A, B (2D xy lattice b1, b2, Bloch
+ * vector beta, particle_shift in the plane, Ewald parameter eta) for the
+ * calculator's normalisation, evaluated by the GPU Ewald kernel.  parts must be
+ * QPMS_EWALD_FULL (7); maxR / maxK are not used (the kernel truncates where the
+ * terms fall below e^-56 of the leading ones); Aerr / Berr are zero-filled. */
+int qpms_trans_calculator_get_AB_arrays_e32(const qpms_trans_calculator *c,
+    qpms_complex_t *Adest, double *Aerr, qpms_complex_t *Bdest, double *Berr,
+    ptrdiff_t deststride, ptrdiff_t srcstride, double eta, qpms_complex_t wavenumber,
+    cart2_t b1, cart2_t b2, cart2_t beta, cart3_t particle_shift, double maxR, double maxK);
+int qpms_trans_calculator_get_AB_arrays_e32_e(const qpms_trans_calculator *c,
+    qpms_complex_t *Adest, double *Aerr, qpms_complex_t *Bdest, double *Berr,
+    ptrdiff_t deststride, ptrdiff_t srcstride, double eta, qpms_complex_t wavenumber,
+    cart2_t b1, cart2_t b2, cart2_t beta, cart3_t particle_shift, double maxR, double maxK, int parts);
 
 /* Batched dispersion scan of a 2D lattice (config "2D-periodic dispersion
  * scan"): for every omega (nw, real) and in-plane Bloch vector (nk, kvecs

@@ -269,7 +269,8 @@ def _declare_ewald(L):
     L.orc_ewald_sr_integral_ri.restype = None
     L.orc_ewald_sr_integral_ri.argtypes = [cd, cd, cd, ci, cd, vp]
     L.orc_adjusted_eta.restype = cd
-    L.orc_adjusted_eta.argtypes = [cd, C.c_double * 2, vp, ci]
+    # double complex by value = two doubles (same registers on x86-64 and aarch64)
+    L.orc_adjusted_eta.argtypes = [cd, cd, cd, vp, ci]
 
 
 def ewald_sigma_xy(lMax_e, eta, k, b1, b2, beta, shift, maxR, maxK, parts=7, csphase=-1):
@@ -333,4 +334,4 @@ def adjusted_eta(area, wavenumber, kvec, lMax):
     kv = np.zeros(3)
     kv[:len(kvec)] = kvec
     w = complex(wavenumber)
-    return lib().orc_adjusted_eta(float(area), (C.c_double * 2)(w.real, w.imag), kv.ctypes.data, int(lMax))
+    return lib().orc_adjusted_eta(float(area), w.real, w.imag, kv.ctypes.data, int(lMax))

@@ -303,17 +303,7 @@ template <typename T>
 int gemm(cublasHandle_t h, int m, int n, int k, T alpha, const T *A, size_t lda, const T *B, size_t ldb, T beta,
          T *C, size_t ldc, cublasComputeType_t ct) {
   const cudaDataType_t dt = CTraits<T>::dt;
-  // cuBLAS's default (performant) strategy keeps complex64 GEMMs on the SIMT
-  // path; eager emulation runs them as BF16x9 on the tensor cores, 2.5x faster
-  // on the trailing updates (and closer to FP32 than the SIMT kernels) but
-  // slower on skinny shapes (panels, right-hand sides), whose per-call
-  // overhead dominates: those stay on FP32 SIMT.
-  if (ct == CUBLAS_COMPUTE_32F_EMULATED_16BFX9) {
-    if ((double)m * n * k >= 2.7e8)
-      cublasSetEmulationStrategy(h, CUBLAS_EMULATION_STRATEGY_EAGER);
-    else
-      ct = CUBLAS_COMPUTE_32F;
-  }
+  if (ct == CUBLAS_COMPUTE_32F_EMULATED_16BFX9) cublasSetEmulationStrategy(h, CUBLAS_EMULATION_STRATEGY_EAGER);
   cublasStatus_t s = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &alpha, A, dt, (int)lda, B, dt, (int)ldb,
                                   &beta, C, dt, (int)ldc, ct, CUBLAS_GEMM_DEFAULT);
   if (s == CUBLAS_STATUS_NOT_SUPPORTED && ct != CUBLAS_COMPUTE_32F && ct != CUBLAS_COMPUTE_64F) {
@@ -361,11 +351,12 @@ int lu_nopiv(cublasHandle_t h, int N, int nb, T *A, size_t lda, T *Dinv, T *work
     T *A21 = A + (size_t)k * lda + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = A21 + (size_t)kb * lda;
     int e;
     // L21 = A21 Uinv   (m2 x kb)
-    if ((e = gemm<T>(h, m2, kb, kb, cone<T>(), A21, lda, Uk, kb, cval<T>(0), work, m2, ct))) return e;
+    const cublasComputeType_t cp = (sizeof(T) == 8) ? CUBLAS_COMPUTE_32F : CUBLAS_COMPUTE_64F;  // panels
+    if ((e = gemm<T>(h, m2, kb, kb, cone<T>(), A21, lda, Uk, kb, cval<T>(0), work, m2, cp))) return e;
     QG_CUDA_TRY(cudaMemcpy2DAsync(A21, lda * sizeof(T), work, (size_t)m2 * sizeof(T), (size_t)m2 * sizeof(T), kb,
                                   cudaMemcpyDeviceToDevice, st));
     // U12 = Linv A12   (kb x m2)
-    if ((e = gemm<T>(h, kb, m2, kb, cone<T>(), Lk, kb, A12, lda, cval<T>(0), work, kb, ct))) return e;
+    if ((e = gemm<T>(h, kb, m2, kb, cone<T>(), Lk, kb, A12, lda, cval<T>(0), work, kb, cp))) return e;
     QG_CUDA_TRY(cudaMemcpy2DAsync(A12, lda * sizeof(T), work, (size_t)kb * sizeof(T), (size_t)kb * sizeof(T), m2,
                                   cudaMemcpyDeviceToDevice, st));
     // A22 -= L21 U12
@@ -429,11 +420,22 @@ __global__ void rowmajor_to_colmajor_kernel(size_t N, const double2 *src, size_t
     if (i < N && j < N) dst[i + j * ldd] = tile[threadIdx.x][c];
   }
 }
-cublasComputeType_t lowp_compute() {
+// Compute type of the complex64 trailing updates (the bulk of the LU flops).
+// Measured on the LU's shrinking sequence of strided rank-128 updates at
+// N = 8192: FP32 SIMT 57-59 TF/s, BF16x9 emulation 33 TF/s (slower here than
+// on packed beta = 0 products), TF32 tensor cores 166-183 TF/s with ~3e-4
+// relative product error.  With one or a few right-hand sides the FP64
+// refinement steps are cheap, so the TF32 factors are used and refinement
+// recovers FP64 accuracy (falling back to FP32 factors if it stalls); with
+// many right-hand sides each refinement step costs an FP64 GEMM, so FP32
+// factors (fewer steps) are used.  QPMS_GB300_LU_COMPUTE = 32F / TF32 / BF16X9
+// overrides the choice.
+cublasComputeType_t trailing_compute(int nrhs_max) {
   const char *ev = getenv("QPMS_GB300_LU_COMPUTE");
   if (ev && !strcmp(ev, "32F")) return CUBLAS_COMPUTE_32F;
   if (ev && !strcmp(ev, "TF32")) return CUBLAS_COMPUTE_32F_FAST_TF32;
-  return CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+  if (ev && !strcmp(ev, "BF16X9")) return CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+  return nrhs_max <= 4 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F;
 }
 }  // namespace
 
@@ -450,6 +452,10 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   Np = (N + 3) / 4 * 4;
   nrhs_max = nrhs_max_;
   mode = mode_;
+  trail_ct = (int)trailing_compute(nrhs_max);
+  refactors = 0;
+  base_mode = mode;
+  base_trail = trail_ct;
   nb = mode ? 128 : 64;
   const size_t esz = mode ? 8 : 16;
   const size_t NN = (size_t)Np * Np;
@@ -526,6 +532,14 @@ static int rbt_right_solution(const DenseSolver &s, double2 *X, size_t ld, size_
 
 int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st, bool rowmaj) {
   row_major = rowmaj;
+  mode = base_mode;
+  trail_ct = base_trail;
+  nb = mode ? 128 : 64;
+  return factorize_current(M64, ldm, st);
+}
+
+int DenseSolver::factorize_current(const void *M64, size_t ldm, cudaStream_t st) {
+  const bool rowmaj = row_major;
   const size_t NN = (size_t)Np * Np;
   cublasHandle_t h;
   int e;
@@ -556,7 +570,8 @@ int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st, bool ro
     d2f_kernel<<<grid1(NN), 256, 0, st>>>(NN, (const double2 *)T64, (float2 *)A);
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
-    e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo, lowp_compute(), st);
+    e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
+                         (cublasComputeType_t)trail_ct, st);
   } else {
     e = lu_nopiv<double2>(h, Np, nb, (double2 *)T64, Np, (double2 *)Dinv, (double2 *)work, dinfo,
                           CUBLAS_COMPUTE_64F, st);
@@ -588,7 +603,7 @@ int DenseSolver::apply_inverse(const void *R, size_t ldr, void *Y, size_t ldy, i
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
     if ((e = lu_solve<float2>(h, Np, nb, (const float2 *)A, Np, (const float2 *)Dinv, (float2 *)rhs_lo, Np, nrhs,
-                              (float2 *)work, lowp_compute(), st)))
+                              (float2 *)work, CUBLAS_COMPUTE_32F, st)))
       return e;
     f2d_add_kernel<<<grid1(n), 256, 0, st>>>(n, (const float2 *)rhs_lo, (double2 *)rp, 1);
     QG_CUDA_TRY(cudaGetLastError());
@@ -628,9 +643,12 @@ int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int 
   double prev = 1e300, rel = 0;
   int it = 0;
   const cuDoubleComplex one = make_cuDoubleComplex(1, 0), mone = make_cuDoubleComplex(-1, 0);
-  for (it = 0; it <= max_iter; ++it) {
+  bool first = true;
+  int extra = 0;  // iterations granted again after a refactorisation
+  for (it = 0; it <= max_iter + extra; ++it) {
     if ((e = apply_inverse(r64, N, y64, N, nrhs, st))) return e;
-    add_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)y64, (double2 *)X, it == 0);
+    add_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)y64, (double2 *)X, first);
+    first = false;
     // r = B - M X (FP64)
     QG_CUDA_TRY(cudaMemcpyAsync(r64, B, n * 16, cudaMemcpyDeviceToDevice, st));
     // a row-major M read column-major is M^T: multiply with OP_T
@@ -644,7 +662,29 @@ int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int 
     QG_CUDA_TRY(cudaStreamSynchronize(st));
     g_launches.fetch_add(1);
     rel = sqrt(hr / (hb > 0 ? hb : 1));
-    if (rel <= tol || rel >= 0.5 * prev) break;  // converged or stagnated
+    if (rel <= tol) break;
+    if (rel >= 0.5 * prev || it == max_iter + extra) {  // stagnated
+      if (mode) {
+        // factors too coarse for this matrix (the refinement contracts by about
+        // cond x the factors' error): TF32 -> FP32 -> FP64 factors, continue from x.
+        // mode 0 reuses the same buffers: T64 is factored in place, Dinv and
+        // work hold 2 x (64 x 64 x 16 B) per 64 rows as 2 x (128 x 128 x 8 B) per 128
+        if (trail_ct != (int)CUBLAS_COMPUTE_32F) {
+          trail_ct = (int)CUBLAS_COMPUTE_32F;
+        } else {
+          mode = 0;
+          nb = 64;
+        }
+        ++refactors;
+        if ((e = factorize_current(M64, ldm, st))) return e;
+        if ((e = blas_handle_get(&h))) return e;
+        QG_BLAS_TRY(cublasSetStream(h, st));
+        prev = 1e300;
+        extra = it + 1;
+        continue;
+      }
+      break;
+    }
     prev = rel;
   }
   if (resid_out) *resid_out = rel;

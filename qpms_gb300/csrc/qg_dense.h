@@ -25,6 +25,9 @@ struct DenseSolver {
   cudaMemPool_t pool = nullptr;
   cudaStream_t ast = nullptr;
   bool row_major = false;  // set by factorize(): M64 is row-major (the reference's layout)
+  int trail_ct = 0;        // cublasComputeType_t of the complex64 trailing updates (mode 1)
+  int refactors = 0;       // refinement stalls answered by more precise factors
+  int base_mode = 0, base_trail = 0;  // what factorize() starts from (the fallbacks change mode / trail_ct)
 
   int init(int N, int nrhs_max, int mode, unsigned long long seed, cudaMemPool_t pool = nullptr,
            cudaStream_t alloc_stream = nullptr);
@@ -34,6 +37,7 @@ struct DenseSolver {
   // row-major if rowmaj (kept by the caller: the refinement residual is formed
   // with it).
   int factorize(const void *M64, size_t ldm, cudaStream_t st, bool rowmaj = false);
+  int factorize_current(const void *M64, size_t ldm, cudaStream_t st);  // with the current mode / trail_ct
   // Y = M^-1 R through the factors (one application, no refinement); N x nrhs.
   int apply_inverse(const void *R, size_t ldr, void *Y, size_t ldy, int nrhs, cudaStream_t st);
   // X = M^-1 B (B, X: N x nrhs, leading dimension N), refined with FP64

@@ -4,6 +4,7 @@
 // plane-wave excitation).
 #include <cublas_v2.h>
 #include <math.h>
+#include <stddef.h>
 #include <string.h>
 
 #include <algorithm>
@@ -49,7 +50,7 @@ double fact(int n) {
 }
 
 // Lattice constants of the Ewald kernel (ewald.c:104-157, 228-241).
-int build_ewald_const(const qpms_scatsys_t *ss, int lMax, EwaldConst *c) {
+int build_ewald_const(const qpms_scatsys_t *ss, int lMax, EwaldConst *c, int csphase = -1) {
   const int LE = 2 * lMax + 1;
   if (LE > kEwLE) {
     set_error("periodic systems support lMax <= %d", (kEwLE - 1) / 2);
@@ -75,7 +76,9 @@ int build_ewald_const(const qpms_scatsys_t *ss, int lMax, EwaldConst *c) {
     for (int m = -n; m <= n; ++m) {
       const int y = n * (n + 1) + m, am = m < 0 ? -m : m;
       const double sgn = (m < 0 && (m % 2)) ? -1.0 : 1.0;
-      c->leg0m[y] = P[n * (n + 1) / 2 + am] * sgn;
+      // legendre_column carries the Condon-Shortley phase (-1)^m; csphase +1 drops it
+      const double cs = (csphase == -1 || (am % 2) == 0) ? 1.0 : -1.0;
+      c->leg0m[y] = P[n * (n + 1) / 2 + am] * sgn * cs;
       c->s1off[y] = off;
       if ((m + n) % 2 == 0) {
         static const double ipr[4][2] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}};
@@ -118,7 +121,8 @@ std::mutex &ewald_mutex() {
 int ewald_assemble_locked(const qpms_scatsys_t *ss, const EwaldArgs &a, cudaStream_t st) {
   EwaldConst ec;
   int e;
-  if ((e = build_ewald_const(ss, ss->c->lMax, &ec))) return e;
+  const int csphase = (ss->c->normalisation & QPMS_NORMALISATION_CSPHASE) ? -1 : 1;
+  if ((e = build_ewald_const(ss, ss->c->lMax, &ec, csphase))) return e;
   std::lock_guard<std::mutex> lk(ewald_mutex());
   QG_CUDA_TRY(cudaMemsetAsync(a.err, 0, 4, st));
   if ((e = ewald_upload_constants(ec, st))) return e;
@@ -357,6 +361,82 @@ int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *om
     }
   }
   return QPMS_SUCCESS;
+}
+
+
+// qpms_trans_calculator_get_AB_arrays_e32_e (translations.h:167-177,
+// translations.c:926-1078): the lattice-summed A, B for one Bloch vector and
+// particle shift.  Evaluated by the Ewald assembly kernel on a two-particle
+// cell (positions shift and 0) with T = -1, whose off-diagonal block is then
+// exactly W(shift) = [A B; B A].  Only the full sum is available (parts must
+// be QPMS_EWALD_FULL); the kernel's cutoffs are set by the exponential decay
+// of the terms (|R| eta <= 7.5, x^2 <= 56), so maxR / maxK are not used;
+// Aerr / Berr, if given, are zero-filled (no error estimate is formed).
+int qpms_trans_calculator_get_AB_arrays_e32_e(const qpms_trans_calculator *c, qpms_complex_t *Adest, double *Aerr,
+                                              qpms_complex_t *Bdest, double *Berr, ptrdiff_t deststride,
+                                              ptrdiff_t srcstride, double eta, qpms_complex_t wavenumber,
+                                              cart2_t b1, cart2_t b2, cart2_t beta, cart3_t particle_shift,
+                                              double maxR, double maxK, int parts) {
+  (void)maxR;
+  (void)maxK;
+  clear_error();
+  if (!c || !Adest || !Bdest) { set_error("NULL argument"); return QPMS_EINVAL; }
+  if (parts != 7) { set_error("only the full Ewald sum (QPMS_EWALD_FULL) is implemented"); return QPMS_EINVAL; }
+  if (particle_shift.z != 0) { set_error("particle shift must lie in the lattice plane"); return QPMS_EINVAL; }
+  if (c->lMax > 4) { set_error("lattice sums need lMax <= 4"); return QPMS_EINVAL; }
+  const double pos[6] = {particle_shift.x, particle_shift.y, 0, 0, 0, 0};
+  const int kind[2] = {0, 0};
+  const double rad = 1.0;
+  qpms_complex_t eps_in, eps_med;
+  eps_in.re = 2.0;
+  eps_in.im = 0;
+  eps_med.re = 1.0;
+  eps_med.im = 0;
+  const double bb1[2] = {b1.x, b1.y}, bb2[2] = {b2.x, b2.y};
+  qpms_scatsys_t *ss = qpms_gpu_scatsys_create_spheres_2d(2, pos, kind, 1, &rad, &eps_in, eps_med, c->lMax, bb1, bb2);
+  if (!ss) return QPMS_ERROR;
+  qpms_trans_calculator *own = ss->c;
+  ss->c = const_cast<qpms_trans_calculator *>(c);  // the caller's normalisation and tables
+  const int ne = c->nelem, n = 2 * ne, N = 2 * n;
+  std::vector<qg_c> T(n, cmk(-1.0, 0.0));
+  const qg_c k = cmk(wavenumber.re, wavenumber.im);
+  const double bt[2] = {beta.x, beta.y};
+  int e = QPMS_SUCCESS;
+  std::vector<qg_c> M((size_t)N * N);
+  {
+    Dev dM;
+    if (!(e = dalloc(dM, (size_t)N * N * 16)))
+      if (!(e = periodic_assemble_device(ss, 1, &k, T, 1, bt, &eta, dM.as<qg_c>(), 0)))
+        if (cudaMemcpy(M.data(), dM.p, (size_t)N * N * 16, cudaMemcpyDeviceToHost) != cudaSuccess) {
+          set_error("device to host copy failed");
+          e = QPMS_ERROR;
+        }
+  }
+  ss->c = own;
+  qpms_gpu_scatsys_free(ss);
+  if (e) return e;
+  // block (particle 0 <- particle 1): rows 0..n-1, columns n..2n-1
+  for (int y = 0; y < ne; ++y)
+    for (int yu = 0; yu < ne; ++yu) {
+      const qg_c a = M[(size_t)y * N + n + yu], b = M[(size_t)y * N + n + ne + yu];
+      Adest[deststride * y + srcstride * yu].re = a.re;
+      Adest[deststride * y + srcstride * yu].im = a.im;
+      Bdest[deststride * y + srcstride * yu].re = b.re;
+      Bdest[deststride * y + srcstride * yu].im = b.im;
+      if (Aerr) Aerr[deststride * y + srcstride * yu] = 0;
+      if (Berr) Berr[deststride * y + srcstride * yu] = 0;
+    }
+  return QPMS_SUCCESS;
+}
+
+// translations.h:158-166: the full sum.
+int qpms_trans_calculator_get_AB_arrays_e32(const qpms_trans_calculator *c, qpms_complex_t *Adest, double *Aerr,
+                                            qpms_complex_t *Bdest, double *Berr, ptrdiff_t deststride,
+                                            ptrdiff_t srcstride, double eta, qpms_complex_t wavenumber, cart2_t b1,
+                                            cart2_t b2, cart2_t beta, cart3_t particle_shift, double maxR,
+                                            double maxK) {
+  return qpms_trans_calculator_get_AB_arrays_e32_e(c, Adest, Aerr, Bdest, Berr, deststride, srcstride, eta,
+                                                   wavenumber, b1, b2, beta, particle_shift, maxR, maxK, 7);
 }
 
 }  // extern "C"

@@ -68,3 +68,20 @@ def test_modeproblem_system(torch_cuda, orc, mode):
     ref = np.linalg.solve(M, B)
     assert np.linalg.norm(X - ref) <= 1e-10 * np.linalg.norm(ref)
     assert res <= 1e-12, res
+
+
+@pytest.mark.parametrize("cond", [1e2, 1e5])
+def test_single_rhs_refinement(torch_cuda, cond):
+    """One right-hand side: complex64 factors with TF32 trailing updates, FP64
+    refinement to 1e-13 (falling back to FP32 factors if it stalls), on a
+    matrix of prescribed condition number."""
+    N = 768
+    rng = np.random.default_rng(int(cond))
+    Q1, _ = np.linalg.qr(rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N)))
+    Q2, _ = np.linalg.qr(rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N)))
+    M = (Q1 * np.logspace(0, -np.log10(cond), N)) @ Q2
+    B = rng.normal(size=(N, 1)) + 1j * rng.normal(size=(N, 1))
+    X, res, it = _solve(torch_cuda, M, B, 1)
+    ref = np.linalg.solve(M, B)
+    assert res <= 1e-12, (res, it)
+    assert np.linalg.norm(X - ref) <= cond * 1e-13 * np.linalg.norm(ref)

@@ -125,3 +125,41 @@ def test_dispersion_scan_vs_oracle(gpu, orc, lat, mode):
             assert np.linalg.norm(out["f"][i, j] - f) <= 1e-9 * np.linalg.norm(f)
             sig = -np.vdot(a, f).real / ke ** 2
             assert abs(out["sigma_ext"][i, j] - sig) <= 1e-9 * abs(sig)
+
+
+@pytest.mark.parametrize("norm", [65536 | 8, 65536, 65536 * 3 | 8])
+@pytest.mark.parametrize("k,beta,shift", [(2.3, (2.7, 1.0), (0.5, 0.1325)), (2.3 + 0.1j, (2.7, 1.0), (0.0, 0.0)),
+                                          (2.3 - 0.1j, (0.3, -0.2), (0.25, 0.4))])
+def test_AB_arrays_e32_vs_oracle(gpu, orc, norm, k, beta, shift):
+    """qpms_trans_calculator_get_AB_arrays_e32 (unit square lattice, lMax 3,
+    eta 1.6: the reference's eta-invariance parameter sets) against the oracle,
+    for several normalisations (csphase on and off)."""
+    import ctypes as C
+
+    class Cplx(C.Structure):
+        _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+    class Cart2(C.Structure):
+        _fields_ = [("x", C.c_double), ("y", C.c_double)]
+
+    class Cart3(C.Structure):
+        _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+    L = gpu.lib()
+    f = L.qpms_trans_calculator_get_AB_arrays_e32
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_ssize_t, C.c_ssize_t, C.c_double,
+                  Cplx, Cart2, Cart2, Cart2, Cart3, C.c_double, C.c_double]
+    lMax = 3
+    calc = gpu.trans_calculator(lMax, norm)
+    ne = lMax * (lMax + 2)
+    A = np.zeros((ne, ne), dtype=np.complex128)
+    B = np.zeros((ne, ne), dtype=np.complex128)
+    kc = complex(k)
+    rc = f(calc.c, A.ctypes.data, None, B.ctypes.data, None, ne, 1, 1.6, Cplx(kc.real, kc.imag), Cart2(1, 0),
+           Cart2(0, 1), Cart2(*beta), Cart3(shift[0], shift[1], 0.0), 20.0, 160.0)
+    assert rc == 0, gpu.last_error()
+    oc = orc.TransCalculator(lMax, norm)
+    Ao, Bo = orc.get_AB_arrays_e32(oc, 1.6, kc, (1, 0), (0, 1), beta, shift, 20, 160)
+    assert np.linalg.norm(A - Ao) <= 1e-11 * np.linalg.norm(Ao)
+    assert np.linalg.norm(B - Bo) <= 1e-11 * np.linalg.norm(Bo)

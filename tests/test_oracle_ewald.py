@@ -54,3 +54,15 @@ def test_sigma_parts_consistency(orc):
     tot0, s0, l0 = orc.ewald_sigma_xy(3, 1.6, 2.3, (1, 0), (0, 1), (2.7, 1), (0, 0), 20, 160)
     d = tot0 - s0 - l0
     assert abs(d[0]) > 0 and np.allclose(d[1:], 0, atol=1e-15 * np.abs(tot0).max())
+
+
+def test_adjusted_eta(orc):
+    """qpms_ss_adjusted_eta (scatsystem.c:68-80): max(sqrt(pi / A),
+    sqrt(|kappa^2 - |k|^2| (lMax + 1/2) / 16)) for kappa^2 >= |k|^2, else sqrt(pi / A)."""
+    A = 580e-9 ** 2 * np.sqrt(3) / 2
+    for kap, kv in [(1.9e7, (5e5, 1e6, 0)), (1.2e7 + 3e5j, (0, 0, 0)), (1e6, (4e6, 0, 0))]:
+        k2 = sum(x * x for x in kv)
+        exp = np.sqrt(np.pi / A)
+        if abs(kap) ** 2 >= k2:
+            exp = max(exp, np.sqrt(abs(abs(kap) ** 2 - k2) * (3 + 0.5) / 16))
+        assert abs(orc.adjusted_eta(A, kap, kv, 3) - exp) <= 1e-14 * exp
