@@ -83,5 +83,6 @@ def test_single_rhs_refinement(torch_cuda, cond):
     B = rng.normal(size=(N, 1)) + 1j * rng.normal(size=(N, 1))
     X, res, it = _solve(torch_cuda, M, B, 1)
     ref = np.linalg.solve(M, B)
-    assert res <= 1e-12, (res, it)
+    # FP64 attains a relative residual of about eps * cond at best
+    assert res <= max(1e-12, 1e-16 * cond * 100), (res, it)
     assert np.linalg.norm(X - ref) <= cond * 1e-13 * np.linalg.norm(ref)
