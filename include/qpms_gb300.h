@@ -456,6 +456,19 @@ beyn_result_t *qpms_gpu_beyn_solve(size_t m, size_t l, beyn_function_M_t M, void
     const beyn_contour_t *contour, double rank_tol, size_t rank_sel_min, double res_tol,
     const qpms_complex_t *Vhat, unsigned long long seed, int mode, double refine_tol);
 
+/* Sharding the contour over processes or devices (replicas with one exchange
+ * step): each part sums nodes [node_begin, node_end) of the contour into the
+ * host column-major fecv_size x l arrays A0, A1 and the coarse A0c, A1c (the
+ * parts add up to the full quadrature; Vhat / seed as above, identical on
+ * every part); the summed arrays then go to qpms_gpu_beyn_process (host only,
+ * no residual filter) on one process.  No counterpart in the reference. */
+int qpms_gpu_scatsys_beyn_quadrature(const qpms_scatsys_t *ss, const double *k, const beyn_contour_t *contour,
+    size_t node_begin, size_t node_end, size_t l, const qpms_complex_t *Vhat, unsigned long long seed, int mode,
+    double refine_tol, qpms_complex_t *A0, qpms_complex_t *A1, qpms_complex_t *A0c, qpms_complex_t *A1c);
+beyn_result_t *qpms_gpu_beyn_process(size_t m, size_t l, const qpms_complex_t *A0, const qpms_complex_t *A1,
+    const qpms_complex_t *A0c, const qpms_complex_t *A1c, qpms_complex_t z0, double rank_tol,
+    size_t rank_sel_min);
+
 /* Diagnostics of a result made here: largest FP64 relative residual of the
  * node solves, most refinement steps of one node, wall time of the contour
  * quadrature and of the whole solve (seconds). */

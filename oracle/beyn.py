@@ -79,14 +79,24 @@ def beyn_solve(M_function, m, l, contour, Vhat, rank_tol=1e-4, rank_sel_min=1, r
     residuals, eigvec (rows), ranktest_SV.
     """
     z, dz, z0 = contour
-    n = len(z)
     Vhat = np.asarray(Vhat, dtype=np.complex128)
     assert Vhat.shape == (m, l) and l <= m
-    A0 = np.zeros((m, l), dtype=np.complex128)
+    A0, A1, A0c, A1c = quadrature(M_function, contour, Vhat, 0, len(z))
+    _, err, _, _, _ = _process_matrices(A0c, A1c, z0, rank_tol, rank_sel_min, res_tol, M_function, False)
+    K, ev, vec, res, sigma = _process_matrices(A0, A1, z0, rank_tol, rank_sel_min, res_tol, M_function, True)
+    return {"neig": K, "eigval": ev[:K], "eigval_err": (err - ev)[:K], "residuals": res[:K],
+            "eigvec": vec[:K], "ranktest_SV": sigma, "A0": A0, "A1": A1}
+
+
+def quadrature(M_function, contour, Vhat, node_begin, node_end):
+    """Beyn step 2 over nodes [node_begin, node_end) (beyn.c:524-581): the
+    sums A0, A1 and the coarse A0c, A1c (even global node indices, twice)."""
+    z, dz, z0 = contour
+    A0 = np.zeros(Vhat.shape, dtype=np.complex128)
     A1 = np.zeros_like(A0)
     A0c = np.zeros_like(A0)
     A1c = np.zeros_like(A0)
-    for i in range(n):
+    for i in range(node_begin, node_end):
         X = np.linalg.solve(M_function(z[i]), Vhat)             # zgetrf + zgetrs
         X *= dz[i]
         A0 += X
@@ -98,10 +108,7 @@ def beyn_solve(M_function, m, l, contour, Vhat, rank_tol=1e-4, rank_sel_min=1, r
         if i % 2 == 0:
             A1c += X
             A1c += X
-    _, err, _, _, _ = _process_matrices(A0c, A1c, z0, rank_tol, rank_sel_min, res_tol, M_function, False)
-    K, ev, vec, res, sigma = _process_matrices(A0, A1, z0, rank_tol, rank_sel_min, res_tol, M_function, True)
-    return {"neig": K, "eigval": ev[:K], "eigval_err": (err - ev)[:K], "residuals": res[:K],
-            "eigvec": vec[:K], "ranktest_SV": sigma, "A0": A0, "A1": A1}
+    return A0, A1, A0c, A1c
 
 
 def ellipse(centre, rRe, rIm, n):

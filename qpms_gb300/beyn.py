@@ -49,6 +49,10 @@ def declare(L):
     L.qpms_gpu_host_svd.argtypes = [ci, ci, vp, vp, vp, vp]
     L.qpms_gpu_host_eig.restype = ci
     L.qpms_gpu_host_eig.argtypes = [ci, vp, vp, vp]
+    L.qpms_gpu_scatsys_beyn_quadrature.restype = ci
+    L.qpms_gpu_scatsys_beyn_quadrature.argtypes = [vp, vp, vp, sz, sz, sz, vp, u64, ci, cd, vp, vp, vp, vp]
+    L.qpms_gpu_beyn_process.restype = R
+    L.qpms_gpu_beyn_process.argtypes = [sz, sz, vp, vp, vp, vp, cd, cd, cd, sz]
 
 
 def _carray(addr, n, dtype):
@@ -188,3 +192,75 @@ def host_eig(A):
     if lib().qpms_gpu_host_eig(n, A.ctypes.data, w.ctypes.data, X.ctypes.data):
         raise QpmsGpuError("host eig failed")
     return w, X
+
+
+# ---------------- sharding the contour (replicas with one exchange step) ----------------
+
+def node_range(n_nodes, rank, world):
+    """Contiguous share [begin, end) of n_nodes contour nodes for `rank` of `world`."""
+    base, extra = divmod(n_nodes, world)
+    begin = rank * base + min(rank, extra)
+    return begin, begin + base + (1 if rank < extra else 0)
+
+
+def scatsys_quadrature(ss_ptr, fecv_size, omega_centre, omega_rr, omega_ri, contour_points, node_begin, node_end,
+                       l, blochvector=None, Vhat=None, seed=DEFAULT_SEED, mode=1, refine_tol=0.0):
+    """Partial contour sums (A0, A1, A0c, A1c), each fecv_size x l, of the nodes
+    [node_begin, node_end) of a scattering system's elliptic contour (GPU)."""
+    L = lib()
+    c = complex(omega_centre)
+    contour = L.beyn_contour_ellipse(c.real, c.imag, omega_rr, omega_ri, contour_points)
+    if not contour:
+        raise QpmsGpuError(last_error())
+    out = [np.zeros((fecv_size, l), dtype=np.complex128, order="F") for _ in range(4)]
+    kv = None
+    if blochvector is not None:
+        kv = np.zeros(3)
+        kv[:len(blochvector)] = blochvector
+    V = None if Vhat is None else np.ascontiguousarray(Vhat, dtype=np.complex128)
+    try:
+        rc = L.qpms_gpu_scatsys_beyn_quadrature(ss_ptr, kv.ctypes.data if kv is not None else None, contour,
+                                                node_begin, node_end, l, V.ctypes.data if V is not None else None,
+                                                seed, mode, refine_tol, *[a.ctypes.data for a in out])
+    finally:
+        C.CDLL(None).free(C.c_void_p(contour))
+    if rc:
+        raise QpmsGpuError("Beyn quadrature: " + last_error())
+    return tuple(out)
+
+
+def process(A0, A1, A0c, A1c, z0, rank_tol=1e-4, rank_sel_min=1):
+    """Beyn steps 3-6 on summed quadratures (host; no residual filter)."""
+    arrs = [np.asfortranarray(a, dtype=np.complex128) for a in (A0, A1, A0c, A1c)]
+    m, l = arrs[0].shape
+    z = complex(z0)
+    res = lib().qpms_gpu_beyn_process(m, l, *[a.ctypes.data for a in arrs], z.real, z.imag, rank_tol, rank_sel_min)
+    return _collect(res, l)
+
+
+def allreduce_sum(arrays, group=None):
+    """Sum complex128 arrays over the ranks of `group` (torch.distributed),
+    staged through host memory: CPU tensors on a gloo group."""
+    import torch
+    import torch.distributed as dist
+    out = []
+    for a in arrays:
+        a = np.asfortranarray(a, dtype=np.complex128)
+        t = torch.from_numpy(a.reshape(-1, order="F").view(np.float64).copy())
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+        out.append(t.numpy().view(np.complex128).reshape(a.shape, order="F"))
+    return out
+
+
+def sharded_find_modes(ss, omega_centre, omega_rr, omega_ri, contour_points, l, rank_tol=1e-4, rank_sel_min=1,
+                       blochvector=None, Vhat=None, seed=DEFAULT_SEED, mode=1, group=None):
+    """find_modes with the contour nodes split over the ranks of `group`: each
+    rank sums its share on its GPU, the sums are added (host-staged), rank 0
+    processes them and returns the result dict (other ranks return None)."""
+    import torch.distributed as dist
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    b, e = node_range(contour_points, rank, world)
+    parts = scatsys_quadrature(ss.s, ss.fecv_size, omega_centre, omega_rr, omega_ri, contour_points, b, e, l,
+                               blochvector, Vhat, seed, mode)
+    total = allreduce_sum(parts, group)
+    return process(*total, omega_centre, rank_tol, rank_sel_min) if rank == 0 else None

@@ -5,8 +5,8 @@
 // Per contour node z_i the matrix M(z_i) is built straight into device memory
 // (assembly kernels for scattering systems, or one host->device copy for a
 // user callback), factorised once by the dense solver (random butterfly +
-// blocked LU on the tensor cores, complex64 with FP64 iterative refinement, or
-// plain complex128) and applied to the L probe columns; the quadrature sums
+// blocked LU, complex64 with FP64 iterative refinement, or plain complex128)
+// and applied to the L probe columns; the quadrature sums
 // A0 = sum dz X, A1 = sum dz (z - z0) X and their every-second-node coarse
 // versions accumulate on the device.  The m x L results come back once; the
 // SVD rank test, the L x L projected eigenproblem and the eigenvectors run on
@@ -266,66 +266,62 @@ unsigned grid1(size_t n) {
   return (unsigned)(g ? g : 1);
 }
 
-BeynResultPriv *beyn_core(MSource &src, beyn_function_M_inv_Vhat_t minv, void *minv_params, size_t m, size_t l,
-                          const beyn_contour_t *contour, double rank_tol, size_t rank_sel_min, double res_tol,
-                          const qpms_complex_t *Vhat, unsigned long long seed, int mode, double refine_tol) {
-  const auto t0 = std::chrono::steady_clock::now();
-  if (!contour || contour->n < 1 || m < 1 || l < 1 || l > m || (mode != 0 && mode != 1)) {
-    set_error("Beyn: invalid arguments (need a contour, 1 <= l <= m, mode 0 or 1)");
-    return nullptr;
-  }
-  if (refine_tol <= 0) refine_tol = kDefaultRefineTol;
-  // probe matrix (row-major m x l as the reference's VHat), device copy column-major
-  std::vector<cd> Vh(m * l), Vc(m * l);
-  if (Vhat)
-    for (size_t i = 0; i < m * l; ++i) Vh[i] = to_cd(Vhat[i]);
-  else
-    hostla::probe_matrix(m, l, seed, Vh.data());
+// Contour quadrature over nodes [nb, ne) (beyn.c:524-581): A0 = sum dz X,
+// A1 = sum (z - z0) dz X, coarse sums over even node indices (global index),
+// X = M(z)^-1 Vhat on the GPU.  Vh: host row-major m x l; outputs host
+// column-major m x l.  Splitting the node range lets several processes or
+// devices each sum a part; the parts add up to the full sums.
+int beyn_quadrature(MSource &src, beyn_function_M_inv_Vhat_t minv, void *minv_params, size_t m, size_t l,
+                    const beyn_contour_t *contour, size_t nb, size_t ne, const std::vector<cd> &Vh, int mode,
+                    double refine_tol, unsigned long long seed, std::vector<cd> &A0, std::vector<cd> &A1,
+                    std::vector<cd> &A0c, std::vector<cd> &A1c, double *max_res_out, int *max_it_out) {
+  const size_t nml = m * l;
+  std::vector<cd> Vc(nml);
   for (size_t i = 0; i < m; ++i)
     for (size_t j = 0; j < l; ++j) Vc[i + j * m] = Vh[i * l + j];
-  const size_t nml = m * l;
-  DevPtr dM, dV, dX, dA[4];
-  if (cudaMalloc(&dM.p, m * m * 16) != cudaSuccess || cudaMalloc(&dV.p, nml * 16) != cudaSuccess ||
-      cudaMalloc(&dX.p, nml * 16) != cudaSuccess) {
+  DevPtr dV, dX, dA[4];
+  if (cudaMalloc(&dV.p, nml * 16) != cudaSuccess || cudaMalloc(&dX.p, nml * 16) != cudaSuccess) {
     set_error("Beyn: out of device memory (m = %zu, l = %zu)", m, l);
-    return nullptr;
+    return QPMS_ENOMEM;
   }
   for (auto &a : dA)
     if (cudaMalloc(&a.p, nml * 16) != cudaSuccess || cudaMemset(a.p, 0, nml * 16) != cudaSuccess) {
       set_error("Beyn: out of device memory (m = %zu, l = %zu)", m, l);
-      return nullptr;
+      return QPMS_ENOMEM;
     }
   if (cudaMemcpy(dV.p, Vc.data(), nml * 16, cudaMemcpyHostToDevice) != cudaSuccess) {
     set_error("Beyn: host to device copy failed");
-    return nullptr;
+    return QPMS_ERROR;
   }
   DenseSolver ds;
-  if (!minv && ds.init((int)m, (int)l, mode, seed ^ 0x9e3779b97f4a7c15ULL)) return nullptr;
+  int e;
+  if (!minv && (e = ds.init((int)m, (int)l, mode, seed ^ 0x9e3779b97f4a7c15ULL))) return e;
   std::vector<qpms_complex_t> hx;
   double max_res = 0;
   int max_it = 0;
   const cd z0 = to_cd(contour->centre);
-  for (size_t i = 0; i < contour->n; ++i) {
+  for (size_t i = nb; i < ne; ++i) {
     const cd z = to_cd(contour->z_dz[i][0]), dz = to_cd(contour->z_dz[i][1]);
     if (minv) {  // user-supplied M(z)^-1 Vhat (row-major m x l)
       hx.resize(nml);
-      const int rc = minv(hx.data(), m, l, Vhat ? Vhat : (const qpms_complex_t *)Vh.data(), from_cd(z), minv_params);
+      const int rc = minv(hx.data(), m, l, (const qpms_complex_t *)Vh.data(), from_cd(z), minv_params);
       if (rc) {
         set_error("M^-1 Vhat callback returned %d", rc);
-        return nullptr;
+        return rc;
       }
       for (size_t r = 0; r < m; ++r)
         for (size_t c = 0; c < l; ++c) Vc[r + c * m] = to_cd(hx[r * l + c]);
       if (cudaMemcpy(dX.p, Vc.data(), nml * 16, cudaMemcpyHostToDevice) != cudaSuccess) {
         set_error("Beyn: host to device copy failed");
-        return nullptr;
+        return QPMS_ERROR;
       }
     } else {
       double res = 0;
       int it = 0;
-      if (src.build(z, (qg_c *)dM.p, 0)) return nullptr;
-      if (ds.factorize(dM.p, m, 0)) return nullptr;
-      if (ds.solve(dM.p, m, dV.p, dX.p, (int)l, refine_tol, kMaxRefine, &res, &it, 0)) return nullptr;
+      if ((e = src.build_rowmajor(z, 0))) return e;
+      // the staged row-major M(z) goes straight to the solver (transposed on the fly)
+      if ((e = ds.factorize(src.stage, m, 0, true))) return e;
+      if ((e = ds.solve(src.stage, m, dV.p, dX.p, (int)l, refine_tol, kMaxRefine, &res, &it, 0))) return e;
       if (!(res <= max_res)) max_res = res;  // NaN-propagating max
       if (it > max_it) max_it = it;
     }
@@ -335,27 +331,38 @@ BeynResultPriv *beyn_core(MSource &src, beyn_function_M_inv_Vhat_t minv, void *m
                                                 (double2 *)dA[3].p);
     if (cudaGetLastError() != cudaSuccess) {
       set_error("Beyn: accumulation kernel launch failed");
-      return nullptr;
+      return QPMS_ERROR;
     }
     g_launches.fetch_add(1);
   }
-  std::vector<cd> A0(nml), A1(nml), A0c(nml), A1c(nml);
+  A0.resize(nml);
+  A1.resize(nml);
+  A0c.resize(nml);
+  A1c.resize(nml);
   if (cudaMemcpy(A0.data(), dA[0].p, nml * 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(A1.data(), dA[1].p, nml * 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(A0c.data(), dA[2].p, nml * 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(A1c.data(), dA[3].p, nml * 16, cudaMemcpyDeviceToHost) != cudaSuccess) {
     set_error("Beyn: device to host copy failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return QPMS_ERROR;
+  }
+  if (max_res_out) *max_res_out = max_res;
+  if (max_it_out) *max_it_out = max_it;
+  return QPMS_SUCCESS;
+}
+
+// Beyn steps 3-6 on the summed quadratures, coarse then fine, into a result
+// (beyn.c:584-606).  resid may be NULL when res_tol <= 0.
+BeynResultPriv *beyn_postprocess(Residual *resid, size_t m, size_t l, cd z0, const std::vector<cd> &A0,
+                                 const std::vector<cd> &A1, const std::vector<cd> &A0c, const std::vector<cd> &A1c,
+                                 double rank_tol, size_t rank_sel_min, double res_tol) {
+  if (res_tol > 0 && !resid) {
+    set_error("Beyn: residual filtering needs M(z)");
     return nullptr;
   }
-  const auto t1 = std::chrono::steady_clock::now();
-  Residual resid;
-  resid.src = &src;
-  resid.m = m;
-  resid.dM = (qg_c *)dM.p;
   Processed coarse, fine;
-  if (process(A0c, A1c, m, l, z0, rank_tol, rank_sel_min, res_tol, false, &resid, coarse)) return nullptr;
-  if (process(A0, A1, m, l, z0, rank_tol, rank_sel_min, res_tol, true, &resid, fine)) return nullptr;
-
+  if (process(A0c, A1c, m, l, z0, rank_tol, rank_sel_min, res_tol, false, resid, coarse)) return nullptr;
+  if (process(A0, A1, m, l, z0, rank_tol, rank_sel_min, res_tol, true, resid, fine)) return nullptr;
   BeynResultPriv *r = new (std::nothrow) BeynResultPriv();
   if (!r) {
     set_error("out of host memory");
@@ -392,6 +399,49 @@ BeynResultPriv *beyn_core(MSource &src, beyn_function_M_inv_Vhat_t minv, void *m
     for (size_t i = 0; i < m; ++i) p.eigvec[(size_t)k * m + i] = from_cd(fine.eigvec[(size_t)k * m + i]);
   }
   for (size_t k = 0; k < l; ++k) p.ranktest_SV[k] = fine.sigma[k];
+  return r;
+}
+
+std::vector<cd> probe_or_given(size_t m, size_t l, const qpms_complex_t *Vhat, unsigned long long seed) {
+  std::vector<cd> Vh(m * l);
+  if (Vhat)
+    for (size_t i = 0; i < m * l; ++i) Vh[i] = to_cd(Vhat[i]);
+  else
+    hostla::probe_matrix(m, l, seed, Vh.data());
+  return Vh;
+}
+
+BeynResultPriv *beyn_core(MSource &src, beyn_function_M_inv_Vhat_t minv, void *minv_params, size_t m, size_t l,
+                          const beyn_contour_t *contour, double rank_tol, size_t rank_sel_min, double res_tol,
+                          const qpms_complex_t *Vhat, unsigned long long seed, int mode, double refine_tol) {
+  const auto t0 = std::chrono::steady_clock::now();
+  if (!contour || contour->n < 1 || m < 1 || l < 1 || l > m || (mode != 0 && mode != 1)) {
+    set_error("Beyn: invalid arguments (need a contour, 1 <= l <= m, mode 0 or 1)");
+    return nullptr;
+  }
+  if (refine_tol <= 0) refine_tol = kDefaultRefineTol;
+  const std::vector<cd> Vh = probe_or_given(m, l, Vhat, seed);
+  std::vector<cd> A0, A1, A0c, A1c;
+  double max_res = 0;
+  int max_it = 0;
+  if (beyn_quadrature(src, minv, minv_params, m, l, contour, 0, contour->n, Vh, mode, refine_tol, seed, A0, A1, A0c,
+                      A1c, &max_res, &max_it))
+    return nullptr;
+  const auto t1 = std::chrono::steady_clock::now();
+  DevPtr dM;
+  Residual resid;
+  if (res_tol > 0) {
+    if (cudaMalloc(&dM.p, m * m * 16) != cudaSuccess) {
+      set_error("Beyn: out of device memory for the residuals");
+      return nullptr;
+    }
+    resid.src = &src;
+    resid.m = m;
+    resid.dM = (qg_c *)dM.p;
+  }
+  BeynResultPriv *r = beyn_postprocess(res_tol > 0 ? &resid : nullptr, m, l, to_cd(contour->centre), A0, A1, A0c,
+                                       A1c, rank_tol, rank_sel_min, res_tol);
+  if (!r) return nullptr;
   r->max_node_resid = max_res;
   r->max_node_iters = max_it;
   const auto t2 = std::chrono::steady_clock::now();
@@ -567,6 +617,71 @@ beyn_result_t *qpms_scatsys_periodic_find_eigenmodes(const qpms_scatsys_t *ss, c
   }
   BeynResultPriv *r = scatsys_beyn(ss, k, omega_centre, omega_rr, omega_ri, contour_npoints, rank_tol, rank_sel_min,
                                    res_tol, 0, nullptr, kDefaultSeed, 1, kDefaultRefineTol);
+  return r ? &r->pub : nullptr;
+}
+
+int qpms_gpu_scatsys_beyn_quadrature(const qpms_scatsys_t *ss, const double *k, const beyn_contour_t *contour,
+                                     size_t node_begin, size_t node_end, size_t l, const qpms_complex_t *Vhat,
+                                     unsigned long long seed, int mode, double refine_tol, qpms_complex_t *A0,
+                                     qpms_complex_t *A1, qpms_complex_t *A0c, qpms_complex_t *A1c) {
+  clear_error();
+  if (!ss || !scatsys_is_own(ss) || !contour || !A0 || !A1 || !A0c || !A1c || node_begin > node_end ||
+      node_end > contour->n || (mode != 0 && mode != 1)) {
+    set_error("invalid arguments");
+    return QPMS_EINVAL;
+  }
+  if ((k && ss->lattice_dimension != 2) || (!k && ss->lattice_dimension != 0)) {
+    set_error("a Bloch vector goes with a 2D-periodic system, none with a finite one");
+    return QPMS_EINVAL;
+  }
+  const size_t m = ss->fecv_size;
+  if (l < 1 || l > m) {
+    set_error("1 <= l <= fecv_size");
+    return QPMS_EINVAL;
+  }
+  FiniteSource fs;
+  PeriodicSource ps;
+  MSource *src = k ? (MSource *)&ps : (MSource *)&fs;
+  fs.ss = ps.ss = ss;
+  if (k) {
+    ps.kvec[0] = k[0];
+    ps.kvec[1] = k[1];
+    ps.kvec[2] = k[2];
+  }
+  src->m = m;
+  int e;
+  if ((e = src->init_stage())) return e;
+  const std::vector<cd> Vh = probe_or_given(m, l, Vhat, seed);
+  std::vector<cd> a0, a1, a0c, a1c;
+  if ((e = beyn_quadrature(*src, nullptr, nullptr, m, l, contour, node_begin, node_end, Vh, mode,
+                           refine_tol > 0 ? refine_tol : kDefaultRefineTol, seed, a0, a1, a0c, a1c, nullptr,
+                           nullptr)))
+    return e;
+  for (size_t i = 0; i < m * l; ++i) {
+    A0[i] = from_cd(a0[i]);
+    A1[i] = from_cd(a1[i]);
+    A0c[i] = from_cd(a0c[i]);
+    A1c[i] = from_cd(a1c[i]);
+  }
+  return QPMS_SUCCESS;
+}
+
+beyn_result_t *qpms_gpu_beyn_process(size_t m, size_t l, const qpms_complex_t *A0, const qpms_complex_t *A1,
+                                     const qpms_complex_t *A0c, const qpms_complex_t *A1c, qpms_complex_t z0,
+                                     double rank_tol, size_t rank_sel_min) {
+  clear_error();
+  if (!A0 || !A1 || !A0c || !A1c || m < 1 || l < 1 || l > m) {
+    set_error("invalid arguments");
+    return nullptr;
+  }
+  std::vector<cd> a0(m * l), a1(m * l), a0c(m * l), a1c(m * l);
+  for (size_t i = 0; i < m * l; ++i) {
+    a0[i] = to_cd(A0[i]);
+    a1[i] = to_cd(A1[i]);
+    a0c[i] = to_cd(A0c[i]);
+    a1c[i] = to_cd(A1c[i]);
+  }
+  BeynResultPriv *r = beyn_postprocess(nullptr, m, l, to_cd(z0), a0, a1, a0c, a1c, rank_tol, rank_sel_min, 0.0);
   return r ? &r->pub : nullptr;
 }
 

@@ -29,6 +29,13 @@ namespace qg {
 namespace {
 
 constexpr int kThreads = 256;
+// Output-row stage buffers: 2 overlaps the TMA store of one row with the next
+// row's arithmetic; 1 frees shared memory for the L1 that caches the
+// multiplier tables.
+#ifndef QG_TRANS_STAGES
+#define QG_TRANS_STAGES 2
+#endif
+constexpr int kStages = QG_TRANS_STAGES;
 
 template <int LMAX>
 struct TransShape {
@@ -39,7 +46,7 @@ struct TransShape {
   static constexpr int NE2 = NE * NE;
   // translations per chunk: keep the w tables ~25-40 KB
   static constexpr int V = LMAX <= 3 ? 32 : (LMAX <= 5 ? 16 : (LMAX <= 7 ? 8 : 4));
-  static constexpr bool kStaged = (2 * NE2 * 16 + V * (S * 16 + 2 * (L + 1) * 16 + NL * 8 + 16)) <= 200 * 1024;
+  static constexpr bool kStaged = (kStages * NE2 * 16 + V * (S * 16 + 2 * (L + 1) * 16 + NL * 8 + 16)) <= 200 * 1024;
 };
 
 struct __align__(16) VecInfo {
@@ -52,7 +59,7 @@ template <int LMAX>
 constexpr size_t trans_smem_bytes(bool staged) {
   using Sh = TransShape<LMAX>;
   return (size_t)Sh::V * Sh::S * 16 + (size_t)Sh::V * (Sh::L + 1) * 16 * 2 + (size_t)Sh::V * Sh::NL * 8 +
-         (size_t)Sh::V * sizeof(VecInfo) + (staged ? (size_t)2 * Sh::NE2 * 16 : 0);
+         (size_t)Sh::V * sizeof(VecInfo) + (staged ? (size_t)kStages * Sh::NE2 * 16 : 0);
 }
 
 __device__ __forceinline__ void bulk_store_row(void *gdst, const void *ssrc, uint32_t bytes) {
@@ -60,6 +67,9 @@ __device__ __forceinline__ void bulk_store_row(void *gdst, const void *ssrc, uin
   asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(gdst), "r"(s), "r"(bytes)
                : "memory");
   asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read_le0() {
+  asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
 }
 __device__ __forceinline__ void bulk_wait_read_le1() {
   asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
@@ -76,14 +86,14 @@ __global__ void __launch_bounds__(kThreads) trans_ab_kernel(TransDevTables T, si
                                                             const unsigned char *__restrict__ r_ge_d, int J,
                                                             qg_c *__restrict__ A, qg_c *__restrict__ B) {
   using Sh = TransShape<LMAX>;
-  constexpr int L = Sh::L, S = Sh::S, NL = Sh::NL, NE2 = Sh::NE2, V = Sh::V, TQ = LMAX + 1;
+  constexpr int L = Sh::L, S = Sh::S, NL = Sh::NL, NE2 = Sh::NE2, V = Sh::V;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   qg_c *w = reinterpret_cast<qg_c *>(smem_raw);  // [V][S]
   qg_c *zb = w + V * S;                           // [V][L+1]
   qg_c *eph = zb + V * (L + 1);                   // [V][L+1]
   double *leg = reinterpret_cast<double *>(eph + V * (L + 1));  // [V][NL]
   VecInfo *info = reinterpret_cast<VecInfo *>(leg + V * NL);    // [V]
-  qg_c *stage = reinterpret_cast<qg_c *>(info + V);             // [2][NE2] if STAGED
+  qg_c *stage = reinterpret_cast<qg_c *>(info + V);             // [kStages][NE2] if STAGED
 
   const int tid = threadIdx.x;
   const size_t nchunks = (n + V - 1) / V;
@@ -162,8 +172,13 @@ __global__ void __launch_bounds__(kThreads) trans_ab_kernel(TransDevTables T, si
         qg_c *out = (which ? B : A) + (base + v) * (size_t)NE2;
         qg_c *buf = nullptr;
         if (STAGED) {
-          buf = stage + (row_counter & 1) * NE2;
-          if (tid == 0) bulk_wait_read_le1();  // the copy that last read this buffer is done
+          buf = stage + (row_counter % kStages) * NE2;
+          if (tid == 0) {  // the copy that last read this buffer is done
+            if (kStages == 2)
+              bulk_wait_read_le1();
+            else
+              bulk_wait_read_le0();
+          }
           __syncthreads();
         }
         for (int k = tid; k < NE2; k += kThreads) {
