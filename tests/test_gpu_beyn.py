@@ -149,14 +149,21 @@ def test_periodic_gamma(qb, orc):
 
 def test_split_quadrature_matches_whole(qb):
     """The contour split in two node ranges (as sharded ranks would) and summed
-    gives the same eigenvalues as the whole quadrature (6 x 6 cluster, l = 40)."""
+    gives the eigenvalues of the whole quadrature (6 x 6 cluster, l = 40; rank
+    tolerance at the singular-value gap, where the eigenvalues are well
+    conditioned)."""
     import qpms_gb300
     pos = _square(6, 400e-9)
     ss = qpms_gb300.ScatteringSystem(pos, 60e-9, -12 + 1.2j, 2.25, 2)
     c, rr, ri = (2.1 - 0.05j) * EV / HBAR, 0.1 * EV / HBAR, 0.06 * EV / HBAR
-    whole = ss.find_modes(c, rr, ri, contour_points=64, rank_tol=1e-4, l=40, seed=77, mode=1)
+    whole = qb.scatsys_quadrature(ss.s, ss.fecv_size, c, rr, ri, 64, 0, 64, 40, seed=77, mode=1)
     p1 = qb.scatsys_quadrature(ss.s, ss.fecv_size, c, rr, ri, 64, 0, 29, 40, seed=77, mode=1)
     p2 = qb.scatsys_quadrature(ss.s, ss.fecv_size, c, rr, ri, 64, 29, 64, 40, seed=77, mode=1)
-    split = qb.process(*[a + b for a, b in zip(p1, p2)], c, 1e-4, 1)
-    assert split["eigval"].size == whole["eigval"].size
-    _match(whole["eigval"], split["eigval"], rtol=1e-10)
+    for a, b, w in zip(p1, p2, whole):
+        assert np.linalg.norm(a + b - w) <= 1e-13 * np.linalg.norm(w)
+    sv = qb.process(*whole, c, 1e300, 1)["ranktest_SV"]
+    tol = 1e-4 * sv[0]
+    r_whole = qb.process(*whole, c, tol, 1)
+    r_split = qb.process(*[a + b for a, b in zip(p1, p2)], c, tol, 1)
+    assert r_split["eigval"].size == r_whole["eigval"].size >= 1
+    _match(r_whole["eigval"], r_split["eigval"], rtol=1e-10)
