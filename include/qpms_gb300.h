@@ -370,6 +370,13 @@ int qpms_gpu_incident_planewave_full(qpms_complex_t *target_full, const qpms_sca
 int qpms_gpu_finite_planewave_scatter(const qpms_scatsys_t *ss, size_t nw,
     const double *omegas, const double k_dir[3], const qpms_complex_t E_cart[3], int mode,
     qpms_complex_t *f_out, double *sigma_ext, double *resid_out, int *iters_out);
+/* The same with sigma_scat (may be NULL) = Re(f^H (I + R) f) / k^2, R the
+ * regular-wave translation matrix with zero self blocks, the reference
+ * script's scattering cross-section (misc/finiterectlat-scatter.py:98-111);
+ * sigma_abs = sigma_ext - sigma_scat. */
+int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw,
+    const double *omegas, const double k_dir[3], const qpms_complex_t E_cart[3], int mode,
+    qpms_complex_t *f_out, double *sigma_ext, double *sigma_scat, double *resid_out, int *iters_out);
 
 /* Dense complex solve X = M^-1 B on DEVICE pointers (column-major, any N):
  * random butterfly transform + blocked LU without pivoting;

@@ -239,6 +239,14 @@ int qpms_gpu_incident_planewave_full(qpms_complex_t *target_full, const qpms_sca
 int qpms_gpu_finite_planewave_scatter(const qpms_scatsys_t *ss, size_t nw, const double *omegas,
                                       const double k_dir[3], const qpms_complex_t E_cart[3], int mode,
                                       qpms_complex_t *f_out, double *sigma_ext, double *resid_out, int *iters_out) {
+  return qpms_gpu_finite_planewave_scatter_ext(ss, nw, omegas, k_dir, E_cart, mode, f_out, sigma_ext, nullptr,
+                                               resid_out, iters_out);
+}
+
+int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw, const double *omegas,
+                                          const double k_dir[3], const qpms_complex_t E_cart[3], int mode,
+                                          qpms_complex_t *f_out, double *sigma_ext, double *sigma_scat,
+                                          double *resid_out, int *iters_out) {
   clear_error();
   if (!scatsys_is_own(ss)) { set_error("system must come from qpms_gpu_scatsys_create_spheres"); return QPMS_EINVAL; }
   if (!omegas || !k_dir || !E_cart || !sigma_ext) { set_error("NULL argument"); return QPMS_EINVAL; }
@@ -357,6 +365,31 @@ int qpms_gpu_finite_planewave_scatter(const qpms_scatsys_t *ss, size_t nw, const
   }
   if ((e = launch_sigma_ext(W, N, da.as<qg_c>(), dx.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), st))) return e;
   QG_CUDA_TRY(cudaMemcpy(sigma_ext, dsig.p, W * 8, cudaMemcpyDeviceToHost));
+  if (sigma_scat) {
+    // sigma_scat = Re(f^H (I + R) f) / k^2 with R the regular-wave translation
+    // matrix, zero self blocks (misc/finiterectlat-scatter.py:98-111): the
+    // assembly with J = 1 and T = -1 builds I + R in place of M
+    std::vector<qg_c> mone(T.size(), cmk(-1.0, 0.0));
+    QG_CUDA_TRY(cudaMemcpy(dT.p, mone.data(), mone.size() * 16, cudaMemcpyHostToDevice));
+    AsmArgs a;
+    a.nw = W;
+    a.np = np;
+    a.ntm = ntm;
+    a.dense = 0;
+    a.J = 1;
+    a.pos = dpos.as<double>();
+    a.tmid = dtm.as<int>();
+    a.T = dT.as<qg_c>();
+    a.k = dk.as<qg_c>();
+    a.M = dM.as<qg_c>();
+    if ((e = launch_assemble(a, priv(ss->c)->dev, st))) return e;
+    // r = 0 - (I + R) f, then -Re(f^H r) / k^2
+    QG_CUDA_TRY(cudaMemsetAsync(db.p, 0, N * W * 16, st));
+    if ((e = launch_residual(W, N, dM.as<qg_c>(), dx.as<qg_c>(), db.as<qg_c>(), dr.as<qg_c>(), rn2, bn2, st)))
+      return e;
+    if ((e = launch_sigma_ext(W, N, dx.as<qg_c>(), dr.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), st))) return e;
+    QG_CUDA_TRY(cudaMemcpy(sigma_scat, dsig.p, W * 8, cudaMemcpyDeviceToHost));
+  }
   if (f_out) QG_CUDA_TRY(cudaMemcpy(f_out, dx.p, N * W * 16, cudaMemcpyDeviceToHost));
   for (int w = 0; w < W; ++w) {
     if (resid_out) resid_out[w] = sqrt(hr[w] / (hb[w] > 0 ? hb[w] : 1));

@@ -61,6 +61,8 @@ def declare(L):
     L.qpms_gpu_debug_cerfc.argtypes = [cd, cd, vp]
     L.qpms_gpu_finite_planewave_scatter.restype = ci
     L.qpms_gpu_finite_planewave_scatter.argtypes = [vp, sz, vp, vp, vp, ci, vp, vp, vp, vp]
+    L.qpms_gpu_finite_planewave_scatter_ext.restype = ci
+    L.qpms_gpu_finite_planewave_scatter_ext.argtypes = [vp, sz, vp, vp, vp, ci, vp, vp, vp, vp, vp]
 
 
 class ScatteringSystem:
@@ -150,23 +152,29 @@ class ScatteringSystem:
         return out
 
     def planewave_scatter_batch(self, omegas, k_dir=(0.0, 0.0, 1.0), E_cart=(1.0, 0.0, 0.0), mode=1,
-                                want_f=False):
+                                want_f=False, want_scat=False):
         """Batched loop of misc/finiterectlat-scatter.py over frequencies:
-        returns dict(sigma_ext, residual, iters[, f]).  mode 0: FP64 LU;
-        mode 1: complex64 LU + FP64 refinement."""
+        returns dict(sigma_ext, residual, iters[, f][, sigma_scat, sigma_abs]).
+        mode 0: FP64 LU; mode 1: complex64 LU + FP64 refinement."""
         om = np.ascontiguousarray(omegas, dtype=np.float64)
         kd = np.ascontiguousarray(k_dir, dtype=np.float64)
         E = np.ascontiguousarray(E_cart, dtype=np.complex128)
         nw = om.size
         sig = np.empty(nw)
+        scat = np.empty(nw) if want_scat else None
         res = np.empty(nw)
         it = np.empty(nw, dtype=np.int32)
         f = np.empty((nw, self.fecv_size), dtype=np.complex128) if want_f else None
-        rc = self._L.qpms_gpu_finite_planewave_scatter(self.s, nw, om.ctypes.data, kd.ctypes.data, E.ctypes.data,
-                                                       int(mode), f.ctypes.data if want_f else None,
-                                                       sig.ctypes.data, res.ctypes.data, it.ctypes.data)
+        rc = self._L.qpms_gpu_finite_planewave_scatter_ext(self.s, nw, om.ctypes.data, kd.ctypes.data,
+                                                           E.ctypes.data, int(mode),
+                                                           f.ctypes.data if want_f else None, sig.ctypes.data,
+                                                           scat.ctypes.data if want_scat else None,
+                                                           res.ctypes.data, it.ctypes.data)
         _lib.check(rc, "qpms_gpu_finite_planewave_scatter")
         out = {"sigma_ext": sig, "residual": res, "iters": it}
+        if want_scat:
+            out["sigma_scat"] = scat
+            out["sigma_abs"] = sig - scat
         if want_f:
             out["f"] = f
         return out

@@ -118,3 +118,26 @@ def test_energy_conservation_gpu(gpu):
         f = out["f"][i]
         sscat = np.vdot(f, (S1 + np.eye(len(f))) @ f).real / ke ** 2
         assert abs(out["sigma_ext"][i] - sscat) <= 1e-9 * abs(sscat)
+
+
+@pytest.mark.parametrize("eps_in", [4.0, EPS_I])
+def test_sigma_scat_vs_oracle(gpu, orc, eps_in):
+    """sigma_scat = Re(f^H (I + R) f) / k^2 (misc/finiterectlat-scatter.py:98-111)
+    from the library against the oracle's regular translation matrix and f;
+    lossless spheres conserve energy (sigma_ext = sigma_scat), lossy ones absorb."""
+    lMax = 2
+    pos = square_array(3, 3, 400e-9)
+    ss = gpu.ScatteringSystem(pos, 50e-9, eps_in, EPS_E, lMax)
+    om = np.array([1.7, 2.1, 2.5]) * EV / HBAR
+    out = ss.planewave_scatter_batch(om, mode=1, want_scat=True)
+    c = orc.TransCalculator(lMax)
+    for i, w in enumerate(om):
+        ke = np.sqrt(EPS_E) * w / C0
+        f, _, sig = orc.finite_sphere_scatter(c, pos, 50e-9, eps_in, EPS_E, w)
+        R = orc.finite_translation_matrix(c, pos, ke, 1)
+        ref = np.vdot(f, (R + np.eye(len(f))) @ f).real / ke ** 2
+        assert abs(out["sigma_scat"][i] - ref) <= 1e-9 * abs(ref)
+        if np.imag(eps_in) == 0:
+            assert abs(out["sigma_ext"][i] - out["sigma_scat"][i]) <= 1e-9 * abs(ref)
+        else:
+            assert out["sigma_abs"][i] > 0
