@@ -262,6 +262,31 @@ typedef struct qpms_ss_LU {                                          /* scatsyst
 /* -- constructors of this library (the reference builds systems through its
  *    symmetry machinery, scatsystem.c:233-604, which is outside the hot path) -- */
 
+/* ---------------- materials (materials.h) ---------------- */
+typedef struct qpms_ldparams_triple_t {                              /* materials.h:54-58 */
+  double f;
+  double omega;
+  double gamma;
+} qpms_ldparams_triple_t;
+
+typedef struct qpms_ldparams_t {                                     /* materials.h:66-71 */
+  qpms_complex_t eps_inf;
+  double omega_p;
+  size_t n;
+  qpms_ldparams_triple_t data[];
+} qpms_ldparams_t;
+
+/* Lorentz-Drude fits of metals (materials.h:73-77; Rakic et al., Appl. Opt. 37, 5271 (1998)). */
+extern const qpms_ldparams_t *const QPMS_LDPARAMS_AG;
+extern const qpms_ldparams_t *const QPMS_LDPARAMS_AU;
+extern const qpms_ldparams_t *const QPMS_LDPARAMS_CU;
+extern const qpms_ldparams_t *const QPMS_LDPARAMS_AL;
+extern const qpms_ldparams_t *const QPMS_LDPARAMS_CR;
+
+/* materials.c:156-164: sum_j f_j omega_p^2 / (omega_j^2 - omega^2 - i omega gamma_j).
+ * As in the reference, eps_inf is not added. */
+qpms_complex_t qpms_lorentzdrude_eps(qpms_complex_t omega, const qpms_ldparams_t *p);
+
 /* Finite system of spheres with constant permittivities (Mie T-matrices,
  * tmatrices.c:580-606) in a constant medium; bspec from lMax (vswf.c:76-92).
  * kind[i] in [0, nkinds) selects radius[kind] and eps_inside[kind]. */
@@ -276,6 +301,15 @@ void qpms_gpu_scatsys_free(qpms_scatsys_t *ss);
 qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_2d(int np, const double *pos_xyz, const int *kind,
     int nkinds, const double *radius, const qpms_complex_t *eps_inside,
     qpms_complex_t eps_medium, qpms_l_t lMax, const double b1[2], const double b2[2]);
+
+/* The same with dispersive spheres: kind t uses the Lorentz-Drude model
+ * ld_inside[t] when that pointer is non-NULL (copied), else eps_inside[t]
+ * (eps_inside may be NULL when every kind has a model); b1 = b2 = NULL for a
+ * finite system, else a 2D lattice.  The T-matrices of every entry point
+ * follow omega through the model. */
+qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_ld(int np, const double *pos_xyz, const int *kind, int nkinds,
+    const double *radius, const qpms_complex_t *eps_inside, const qpms_ldparams_t *const *ld_inside,
+    qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1, const double *b2);
 
 /* Evaluates the medium and the T-matrices at omega, like qpms_scatsys_at_omega
  * (scatsystem.c:606-630). */

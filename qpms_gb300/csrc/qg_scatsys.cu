@@ -145,8 +145,22 @@ void planewave_coeffs(int lMax, double theta, double phi, const cd Es[3], cd *el
 // ---------------- system object ----------------
 struct SphereKind {
   double radius;
-  cd eps;
+  cd eps;                                 // constant permittivity, or
+  std::vector<qpms_ldparams_triple_t> ld;  // Lorentz-Drude oscillators (non-empty: used)
+  double ld_omega_p = 0;
 };
+
+// qpms_lorentzdrude_eps (materials.c:156-164): sum_j f_j wp^2 / (w_j^2 - w^2 - i w g_j).
+// As there, eps_inf is not added (the parameter sets carry eps_inf = 1).
+cd lorentzdrude_eps(cd omega, double omega_p, const qpms_ldparams_triple_t *d, size_t n) {
+  cd eps = 0;
+  for (size_t j = 0; j < n; ++j)
+    eps += d[j].f * omega_p * omega_p / (d[j].omega * d[j].omega - omega * omega - cd(0, 1) * omega * d[j].gamma);
+  return eps;
+}
+cd kind_eps(const SphereKind &k, cd omega) {
+  return k.ld.empty() ? k.eps : lorentzdrude_eps(omega, k.ld_omega_p, k.ld.data(), k.ld.size());
+}
 
 struct ScatsysPriv {
   qpms_scatsys_t pub;  // first member: the public, reference-layout view
@@ -181,7 +195,7 @@ qpms_epsmu_t epsmu_const_fn(qpms_complex_t, const void *params) {
 // T diagonal (bspec order: electric block then magnetic block) of kind t at omega
 void sphere_tdiag(const ScatsysPriv *s, int t, cd omega, std::vector<cd> &out) {
   const int lMax = s->lMax, ne = lMax * (lMax + 2);
-  const cd k_i = std::sqrt(s->kinds[t].eps) * omega / kC0, k_e = std::sqrt(s->eps_medium) * omega / kC0;
+  const cd k_i = std::sqrt(kind_eps(s->kinds[t], omega)) * omega / kC0, k_e = std::sqrt(s->eps_medium) * omega / kC0;
   std::vector<cd> RV(lMax + 1), RH(lMax + 1);
   mie_coefficients(lMax, s->kinds[t].radius, k_i, k_e, 1.0, 1.0, RV.data(), RH.data());
   out.assign(2 * ne, 0);
@@ -354,7 +368,8 @@ extern "C" {
 
 static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *kind, int nkinds,
                                       const double *radius, const qpms_complex_t *eps_inside,
-                                      qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1, const double *b2);
+                                      qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1, const double *b2,
+                                      const qpms_ldparams_t *const *ld_inside = nullptr);
 
 // One translation calculator per lMax (default normalisation), built on first
 // use and shared by every system of this library for the life of the process:
@@ -374,6 +389,37 @@ qpms_scatsys_t *qpms_gpu_scatsys_create_spheres(int np, const double *pos_xyz, c
   return create_spheres(np, pos_xyz, kind, nkinds, radius, eps_inside, eps_medium, lMax, nullptr, nullptr);
 }
 
+qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_ld(int np, const double *pos_xyz, const int *kind, int nkinds,
+                                                   const double *radius, const qpms_complex_t *eps_inside,
+                                                   const qpms_ldparams_t *const *ld_inside,
+                                                   qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1,
+                                                   const double *b2) {
+  if ((b1 == nullptr) != (b2 == nullptr)) {
+    set_error("give both lattice vectors or neither");
+    return nullptr;
+  }
+  if (!eps_inside && !ld_inside) {
+    set_error("NULL permittivities");
+    return nullptr;
+  }
+  std::vector<qpms_complex_t> eps(nkinds);
+  for (int t = 0; t < nkinds; ++t) {
+    eps[t].re = eps_inside ? eps_inside[t].re : 1.0;
+    eps[t].im = eps_inside ? eps_inside[t].im : 0.0;
+  }
+  return create_spheres(np, pos_xyz, kind, nkinds, radius, eps.data(), eps_medium, lMax, b1, b2, ld_inside);
+}
+
+qpms_complex_t qpms_lorentzdrude_eps(qpms_complex_t omega, const qpms_ldparams_t *p) {
+  qpms_complex_t r;
+  r.re = r.im = 0;
+  if (!p) return r;
+  const cd e = lorentzdrude_eps(to_cd(omega), p->omega_p, p->data, p->n);
+  r.re = e.real();
+  r.im = e.imag();
+  return r;
+}
+
 qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_2d(int np, const double *pos_xyz, const int *kind, int nkinds,
                                                    const double *radius, const qpms_complex_t *eps_inside,
                                                    qpms_complex_t eps_medium, qpms_l_t lMax, const double b1[2],
@@ -387,7 +433,8 @@ qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_2d(int np, const double *pos_xyz
 
 static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *kind, int nkinds,
                                       const double *radius, const qpms_complex_t *eps_inside,
-                                      qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1, const double *b2) {
+                                      qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1, const double *b2,
+                                      const qpms_ldparams_t *const *ld_inside) {
   clear_error();
   if (np < 1 || !pos_xyz || nkinds < 1 || !radius || !eps_inside || lMax < 1 || lMax > 6) {
     set_error("invalid arguments (np >= 1, 1 <= lMax <= 6)");
@@ -398,7 +445,16 @@ static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *
   memset(&s->pub, 0, sizeof(s->pub));
   s->lMax = lMax;
   s->eps_medium = to_cd(eps_medium);
-  for (int t = 0; t < nkinds; ++t) s->kinds.push_back({radius[t], to_cd(eps_inside[t])});
+  for (int t = 0; t < nkinds; ++t) {
+    SphereKind k;
+    k.radius = radius[t];
+    k.eps = to_cd(eps_inside[t]);
+    if (ld_inside && ld_inside[t]) {  // copied: the caller's parameter block may go away
+      k.ld.assign(ld_inside[t]->data, ld_inside[t]->data + ld_inside[t]->n);
+      k.ld_omega_p = ld_inside[t]->omega_p;
+    }
+    s->kinds.push_back(k);
+  }
   const int ne = lMax * (lMax + 2);
   for (int it = 0; it < 2; ++it)
     for (int n = 1; n <= lMax; ++n)

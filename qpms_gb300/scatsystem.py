@@ -71,9 +71,14 @@ class ScatteringSystem:
     def __init__(self, positions, radius, eps_inside, eps_medium, lMax, kinds=None, lattice=None):
         """lattice: None (finite system) or (b1, b2), 2D basis vectors in the xy plane."""
         self._L = _lib.lib()
+        from .materials import LorentzDrude
         pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
         radius = np.atleast_1d(np.asarray(radius, dtype=np.float64))
-        eps_in = np.ascontiguousarray(np.atleast_1d(np.asarray(eps_inside, dtype=np.complex128)))
+        eps_list = list(eps_inside) if isinstance(eps_inside, (list, tuple)) else [eps_inside]
+        models = [e if isinstance(e, LorentzDrude) else None for e in eps_list]
+        eps_in = np.ascontiguousarray([0 if m is not None else complex(e) for e, m in zip(eps_list, models)],
+                                      dtype=np.complex128)
+        self._models = models
         if kinds is None:
             kinds = np.zeros(pos.shape[0], dtype=np.int32)
         kinds = np.ascontiguousarray(kinds, dtype=np.int32)
@@ -81,7 +86,17 @@ class ScatteringSystem:
         self.positions = pos
         self.lMax = int(lMax)
         self.lattice = lattice
-        if lattice is None:
+        if any(m is not None for m in models):
+            ptrs = (C.c_void_p * len(models))(*[m.ptr if m is not None else None for m in models])
+            b1 = b2 = None
+            if lattice is not None:
+                b1 = np.ascontiguousarray(lattice[0][:2], dtype=np.float64)
+                b2 = np.ascontiguousarray(lattice[1][:2], dtype=np.float64)
+            self.s = self._L.qpms_gpu_scatsys_create_spheres_ld(
+                pos.shape[0], pos.ctypes.data, kinds.ctypes.data, radius.size, radius.ctypes.data,
+                eps_in.ctypes.data, C.addressof(ptrs), em.real, em.imag, self.lMax,
+                b1.ctypes.data if b1 is not None else None, b2.ctypes.data if b2 is not None else None)
+        elif lattice is None:
             self.s = self._L.qpms_gpu_scatsys_create_spheres(pos.shape[0], pos.ctypes.data, kinds.ctypes.data,
                                                              radius.size, radius.ctypes.data, eps_in.ctypes.data,
                                                              em.real, em.imag, self.lMax)

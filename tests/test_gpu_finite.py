@@ -141,3 +141,20 @@ def test_sigma_scat_vs_oracle(gpu, orc, eps_in):
             assert abs(out["sigma_ext"][i] - out["sigma_scat"][i]) <= 1e-9 * abs(ref)
         else:
             assert out["sigma_abs"][i] > 0
+
+
+def test_lorentz_drude_spheres_vs_oracle(gpu, orc):
+    """Gold spheres (Lorentz-Drude model, the permittivity following omega):
+    the batched scatter against the oracle at eps(omega) evaluated by the model."""
+    from qpms_gb300.materials import lorentz_drude
+    au = lorentz_drude["Au"]
+    lMax = 2
+    pos = square_array(3, 3, 400e-9)
+    ss = gpu.ScatteringSystem(pos, 50e-9, au, EPS_E, lMax)
+    om = np.array([1.7, 2.1, 2.5]) * EV / HBAR
+    out = ss.planewave_scatter_batch(om, mode=1, want_f=True)
+    c = orc.TransCalculator(lMax)
+    for i, w in enumerate(om):
+        f, _, sig = orc.finite_sphere_scatter(c, pos, 50e-9, au(w), EPS_E, w)
+        assert np.linalg.norm(out["f"][i] - f) <= 1e-9 * np.linalg.norm(f)
+        assert abs(out["sigma_ext"][i] - sig) <= 1e-9 * abs(sig)
