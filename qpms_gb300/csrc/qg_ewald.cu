@@ -396,12 +396,19 @@ int launch_ew(const EwaldArgs &a, const TransDevTables &T, cudaStream_t st) {
 }  // namespace
 
 int ewald_upload_constants(const EwaldConst &c, cudaStream_t st) {
-  static bool wd_done = false;
-  if (!wd_done) {
+  // the Faddeeva coefficients: once per device (callers hold the Ewald lock)
+  static bool wd_done[64] = {false};
+  int dev = 0;
+  QG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) {
+    set_error("device index %d out of range", dev);
+    return QPMS_EINVAL;
+  }
+  if (!wd_done[dev]) {
     WeidemanCoeffs w;
     weideman_coeffs(&w);
     QG_CUDA_TRY(cudaMemcpyToSymbol(c_wd, &w, sizeof w));
-    wd_done = true;
+    wd_done[dev] = true;
   }
   QG_CUDA_TRY(cudaMemcpyToSymbolAsync(c_ew, &c, sizeof c, 0, cudaMemcpyHostToDevice, st));
   return QPMS_SUCCESS;
