@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--nvec", type=int, default=N_VEC)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--sections", default="modeproblem,dispersion,beyn,serving",
+    ap.add_argument("--sections", default="modeproblem,dispersion,beyn,serving,field",
                     help="secondary workloads reported beside the headline (comma list, or 'none')")
     ap.add_argument("--case", default=None,
                     help="run one small case for a profiler and exit: dense:N:NRHS:MODE, "
@@ -512,6 +512,64 @@ def section_serving(args):
             "mixed_vs_plain": res["mixed"]["solves_per_s"] / res["plain_fp64"]["solves_per_s"]}
 
 
+def section_field(args):
+    """Scattered-field map of a solved 30 x 30 sphere array (lMax 3): a 512 x 512
+    grid 100 nm above the particle plane, every point summed over all 900 particles."""
+    import torch
+    import qpms_gb300
+    from qpms_gb300.workloads import EV, HBAR
+    pos = _sq(30, 400e-9)
+    lMax = 3
+    ss = qpms_gb300.ScatteringSystem(pos, 60e-9, -12 + 1.2j, 2.25, lMax)
+    om = 2.1 * EV / HBAR
+    k = np.sqrt(2.25) * om / 299792458.0
+    f = ss.planewave_scatter_batch(np.array([om]), mode=1, want_f=True)["f"][0]
+    g = np.linspace(-6.5e-6, 6.5e-6, 512)
+    X, Y = np.meshgrid(g, g, indexing="ij")
+    pts = np.ascontiguousarray(np.stack([X.ravel(), Y.ravel(), np.full(X.size, 1e-7)], 1))
+    npts, pairs = pts.shape[0], pts.shape[0] * pos.shape[0]
+    dev = torch.device("cuda:0")
+    tf = torch.from_numpy(f).to(dev)
+    tp = torch.from_numpy(pts).to(dev)
+    out = torch.empty((npts, 3), dtype=torch.complex128, device=dev)
+    st = torch.cuda.current_stream(dev)
+    for _ in range(3):
+        ss.scattered_E_device(k, tf, tp, out, stream=st)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        ss.scattered_E_device(k, tf, tp, out, stream=st)
+    e1.record(st)
+    torch.cuda.synchronize()
+    dms = e0.elapsed_time(e1) / reps
+    # end to end through the host API (points H2D, field D2H inside)
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        E = ss.scattered_E(k, f, pts)
+        ts.append(time.perf_counter() - t0)
+    e2e = float(np.median(ts))
+    res = {"workload": "field map: 30x30 spheres (pitch 400 nm, r 60 nm, lMax 3, solved at 2.1 eV), "
+                       "512x512 points 100 nm above the array, all 900 particles per point",
+           "device": {"ms_per_map": dms, "points_per_s": npts / dms * 1e3, "pairs_per_s": pairs / dms * 1e3},
+           "e2e": {"ms_per_map": e2e * 1e3, "points_per_s": npts / e2e,
+                   "h2d_bytes": int(pts.nbytes + f.nbytes), "d2h_bytes": int(E.nbytes)}}
+    if not args.no_cpu:
+        from oracle import orc
+        ns = 256
+        t0 = time.perf_counter()
+        O = orc.scattered_E(lMax, pos, 3, k, f, pts[:ns])
+        dt = time.perf_counter() - t0
+        err = np.abs(E[:ns] - O).max() / np.abs(O).max()
+        res["cpu_baseline"] = {"points_per_s": ns / dt, "pairs_per_s": ns * pos.shape[0] / dt, "cores": 1,
+                               "kind": "port", "sample": "first %d points of the map" % ns,
+                               "max_rel_diff_vs_gpu": float(err)}
+        res["gpu_vs_cpu"] = res["device"]["points_per_s"] / res["cpu_baseline"]["points_per_s"]
+    return res
+
+
 def run_sections(args):
     out = {}
     names = [x for x in args.sections.split(",") if x and x != "none"]
@@ -556,6 +614,15 @@ def run_case(spec):
         kp = (square_path if lat == "square" else honeycomb_path)(n=nk)
         r = ss.dispersion_scan(np.linspace(1.6, 2.6, nw) * EV / HBAR, kp, mode=mode)
         print("scan", lat, nw, nk, "logdet sum", float(np.sum(r["logdet"])), "max resid", float(r["residual"].max()))
+    elif f[0] == "field":
+        nx, npts, lMax = int(f[1]), int(f[2]), int(f[3])
+        pos = _sq(nx, 400e-9)
+        ss = qpms_gb300.ScatteringSystem(pos, 60e-9, -12 + 1.2j, 2.25, lMax)
+        rng = np.random.default_rng(1)
+        cv = rng.normal(size=ss.fecv_size) + 1j * rng.normal(size=ss.fecv_size)
+        pts = rng.uniform(-nx * 2e-7, nx * 2e-7, size=(npts, 3))
+        E = ss.scattered_E(1.6e7, cv, pts)
+        print("field", nx, npts, lMax, "sum |E|", float(np.abs(E).sum()))
     elif f[0] == "beyn":
         nx, nodes, mode = int(f[1]), int(f[2]), int(f[3])
         xs = (np.arange(nx) - (nx - 1) / 2) * 400e-9

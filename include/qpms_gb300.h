@@ -151,6 +151,7 @@ int qpms_gpu_trans_multipliers_export(qpms_l_t lMax, qpms_normalisation_t nt,
  * opaque pointers of the same size. */
 typedef struct cart3_t { double x, y, z; } cart3_t;                 /* qpms_types.h:186-189 */
 typedef struct cart2_t { double x, y; } cart2_t;                     /* qpms_types.h:202-204 */
+typedef struct ccart3_t { qpms_complex_t x, y, z; } ccart3_t;        /* qpms_types.h:192-195 */
 typedef unsigned long long qpms_uvswfi_t;                            /* qpms_types.h:81 */
 typedef int qpms_iri_t;                                              /* qpms_types.h:323 */
 typedef int32_t qpms_ss_tmi_t, qpms_ss_tmgi_t, qpms_ss_pi_t;         /* qpms_types.h:310-316 */
@@ -411,6 +412,44 @@ int qpms_gpu_finite_planewave_scatter(const qpms_scatsys_t *ss, size_t nw,
 int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw,
     const double *omegas, const double k_dir[3], const qpms_complex_t E_cart[3], int mode,
     qpms_complex_t *f_out, double *sigma_ext, double *sigma_scat, double *resid_out, int *iters_out);
+
+/* ---------------- scattered field (scatsystem.h:700-790) ----------------
+ * E(where) = sum over particles of the outgoing (btyp 3: Hankel h+) or other
+ * (1 j, 2 y, 4 h-) VSWF expansion with the full coefficient vector cvf,
+ * cartesian components.  Finite systems, default normalisation.  At a
+ * particle centre the Hankel field is singular (non-finite), as in the
+ * reference.  A failure returns a NaN field; qpms_gpu_last_error() tells why. */
+ccart3_t qpms_scatsys_scattered_E(const qpms_scatsys_t *ss, qpms_bessel_t btyp,     /* scatsystem.c:2013-2039 */
+    qpms_complex_t wavenumber, const qpms_complex_t *cvf, cart3_t where);
+ccart3_t qpms_scatsysw_scattered_E(const qpms_scatsys_at_omega_t *ssw,            /* scatsystem.c:2041-2046 */
+    qpms_bessel_t btyp, const qpms_complex_t *cvf, cart3_t where);
+/* The reference's alternative route through the translation operator
+ * (scatsystem.c:2048-2112) evaluates the same field; these run the direct kernel. */
+ccart3_t qpms_scatsys_scattered_E__alt(const qpms_scatsys_t *ss, qpms_bessel_t btyp,
+    qpms_complex_t wavenumber, const qpms_complex_t *cvf, cart3_t where);
+ccart3_t qpms_scatsysw_scattered_E__alt(const qpms_scatsys_at_omega_t *ssw,
+    qpms_bessel_t btyp, const qpms_complex_t *cvf, cart3_t where);
+/* Batched over points, HOST buffers (the loop of qpms_c.pyx:904-927 in one
+ * call): where_xyz [npoints][3], E_xyz [npoints][3] complex. */
+int qpms_gpu_scatsys_scattered_E(const qpms_scatsys_t *ss, qpms_bessel_t btyp,
+    qpms_complex_t wavenumber, const qpms_complex_t *cvf, size_t npoints,
+    const double *where_xyz, qpms_complex_t *E_xyz);
+/* The same on DEVICE buffers, stream-ordered on `stream` (a cudaStream_t). */
+int qpms_gpu_scatsys_scattered_E_device(const qpms_scatsys_t *ss, qpms_bessel_t btyp,
+    qpms_complex_t wavenumber, const qpms_complex_t *d_cvf, size_t npoints,
+    const double *d_where_xyz, qpms_complex_t *d_E_xyz, void *stream);
+
+/* FP64-accurate residual R = B - M X (DEVICE pointers, complex128; M N x N
+ * with leading dimension ldm, column-major or row-major; X, B, R N x nrhs
+ * column-major) formed from bf16 digit products on the tensor cores, the
+ * residual of the dense solver for nrhs >= 8.  No counterpart in the
+ * reference (it calls zgetrs in FP64, scatsystem.c:2262-2273). */
+int qpms_gpu_ozaki_residual(int N, int nrhs, const qpms_complex_t *M, size_t ldm, int row_major,
+    const qpms_complex_t *X, const qpms_complex_t *B, qpms_complex_t *R);
+/* C = A B for bf16 A (m x k), B (k x n) column-major and FP32 C on DEVICE
+ * pointers: the cuBLAS call of the digit products, exposed for its exactness
+ * test. */
+int qpms_gpu_bf16_gemm(int m, int n, int k, const void *A, const void *B, float *C);
 
 /* Dense complex solve X = M^-1 B on DEVICE pointers (column-major, any N):
  * random butterfly transform + blocked LU without pivoting;

@@ -103,6 +103,11 @@ int orc_finite_sphere_scatter(const orc_trans_calculator *c, int np, const doubl
                               double complex *f_out, double complex *a_out, double *sigma_ext,
                               double complex *M_out);
 
+/* Scattered field at npts points where[q][3] of the full coefficient vector
+ * cvf (np particles, common lMax); E[q][3] (scatsystem.c:2013-2039). */
+void orc_scattered_E(int lMax, int np, const double *pos, int J, double complex k, const double complex *cvf,
+                     int npts, const double *where, double complex *E);
+
 /* ---- 2D Ewald sums and the lattice translation operator (orc_ewald.c) ---- */
 typedef struct orc_c2 { double x, y; } orc_c2;
 void orc_l2d_reduceBasis(orc_c2 b1, orc_c2 b2, orc_c2 *o1, orc_c2 *o2);

@@ -174,6 +174,8 @@ def _declare_scatsys(L):
     L.orc_lu_factor.argtypes = [sz, vp, vp]
     L.orc_lu_solve.restype = None
     L.orc_lu_solve.argtypes = [sz, vp, vp, vp, sz]
+    L.orc_scattered_E_ri.restype = None
+    L.orc_scattered_E_ri.argtypes = [ci, ci, vp, ci, cd, cd, vp, ci, vp, vp]
 
 
 C0 = 299792458.0
@@ -218,6 +220,22 @@ def planewave_full(lMax, pos, k_cart, E_cart):
     lib().orc_planewave_full(lMax, pos.shape[0], pos.ctypes.data, kc.ctypes.data, Ec.ctypes.data,
                              out.ctypes.data)
     return out
+
+
+def scattered_E(lMax, pos, J, k, cvf, where):
+    """Field of the full coefficient vector cvf at points where [..., 3]
+    (qpms_scatsys_scattered_E, scatsystem.c:2013-2039); returns [..., 3] complex."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    w = np.ascontiguousarray(where, dtype=np.float64)
+    shape = w.shape
+    w = w.reshape(-1, 3)
+    cv = np.ascontiguousarray(cvf, dtype=np.complex128)
+    assert cv.size == pos.shape[0] * 2 * lMax * (lMax + 2)
+    E = np.empty((w.shape[0], 3), dtype=np.complex128)
+    k = complex(k)
+    lib().orc_scattered_E_ri(lMax, pos.shape[0], pos.ctypes.data, int(J), k.real, k.imag, cv.ctypes.data,
+                             w.shape[0], w.ctypes.data, E.ctypes.data)
+    return E.reshape(shape)
 
 
 def finite_sphere_scatter(calc, pos, radius, eps_i, eps_e, omega, k_dir=(0, 0, 1), E_cart=(1, 0, 0),

@@ -343,3 +343,68 @@ int orc_finite_sphere_scatter_ri(const orc_trans_calculator *c, int np, const do
   return orc_finite_sphere_scatter(c, np, pos, radius, eir + I * eii, eer + I * eei, omega, k_dir, E_cart,
                                    f_out, a_out, sigma_ext, M_out);
 }
+
+/* ---- scattered field of a finite system ----
+ * qpms_scatsys_scattered_E (scatsystem.c:2013-2039): for every particle,
+ * kr = k * cart2sph(where - pos) (vectors.h:134-140, sph_cscale :262-265), the
+ * field of its outgoing-wave coefficients by qpms_eval_uvswf (vswf.c:611-650)
+ * -> qpms_eval_vswf_csph (vswf.c:533-560: Kahan sums over y of the electric and
+ * the magnetic terms, then esum += msum) with the VSWFs of qpms_vswf_fill_csph
+ * (vswf.c:230-288), turned to cartesian by csphvec2ccart (vectors.h:272-303) and
+ * Kahan-summed over the particles.  QPMS_NORMALISATION_DEFAULT (qpms_types.h:167):
+ * Condon-Shortley phase, azimuthal part e^{i m phi} and derivative / m = i e^{i m phi}
+ * (normalisation.h:159-212), all normalisation factors 1.  Coefficients per particle
+ * in bspec order (electric block, then magnetic). */
+static void ckadd(double complex *s, double complex *c, double complex in) {
+  double complex y = in - *c, t = *s + y;
+  *c = (t - *s) - y;
+  *s = t;
+}
+
+void orc_scattered_E(int lMax, int np, const double *pos, int J, double complex k, const double complex *cvf,
+                     int npts, const double *where, double complex *E) {
+  const int ne = lMax * (lMax + 2);
+  double leg[ne], pi[ne], tau[ne];
+  double complex bes[lMax + 1];
+  for (int q = 0; q < npts; ++q) {
+    double complex res[3] = {0, 0, 0}, rc[3] = {0, 0, 0};
+    for (int p = 0; p < np; ++p) {
+      const double dx = where[3 * q] - pos[3 * p], dy = where[3 * q + 1] - pos[3 * p + 1],
+                   dz = where[3 * q + 2] - pos[3 * p + 2];
+      const double r = sqrt(dx * dx + dy * dy + dz * dz);
+      const double theta = r ? acos(dz / r) : M_PI_2, phi = atan2(dy, dx);
+      const double complex kr = k * r;
+      orc_sph_bessel_fill(J, lMax, kr, bes);
+      orc_pitau(theta, lMax, -1.0, leg, pi, tau);
+      const double complex *cv = cvf + (size_t)p * 2 * ne;
+      double complex es[3] = {0, 0, 0}, ec[3] = {0, 0, 0}, ms[3] = {0, 0, 0}, mc[3] = {0, 0, 0};
+      for (int l = 1, y = 0; l <= lMax; ++l) {
+        double complex besfac = r ? bes[l] / kr : ((1 == l) ? 1 / 3. : 0);
+        double complex besderfac = bes[l - 1] - l * besfac;
+        for (int m = -l; m <= l; ++m, ++y) {
+          double complex eimf = cexp(I * m * phi), deimf = m ? I * cexp(I * m * phi) : 0;
+          double complex N[3] = {l * (l + 1) * leg[y] * besfac * eimf, tau[y] * besderfac * eimf,
+                                 pi[y] * besderfac * deimf};
+          double complex M[3] = {0, pi[y] * bes[l] * deimf, -tau[y] * bes[l] * eimf};
+          for (int c = 0; c < 3; ++c) {
+            ckadd(&es[c], &ec[c], cv[y] * N[c]);
+            ckadd(&ms[c], &mc[c], cv[ne + y] * M[c]);
+          }
+        }
+      }
+      for (int c = 0; c < 3; ++c) ckadd(&es[c], &ec[c], ms[c]);
+      const double st = sin(theta), ct = cos(theta), sf = sin(phi), cf = cos(phi);
+      double complex Ec[3];
+      Ec[0] = st * cf * es[0] + ct * cf * es[1] - sf * es[2];
+      Ec[1] = st * sf * es[0] + ct * sf * es[1] + cf * es[2];
+      Ec[2] = ct * es[0] - st * es[1];
+      for (int c = 0; c < 3; ++c) ckadd(&res[c], &rc[c], Ec[c]);
+    }
+    for (int c = 0; c < 3; ++c) E[3 * q + c] = res[c];
+  }
+}
+
+void orc_scattered_E_ri(int lMax, int np, const double *pos, int J, double kr_, double ki_,
+                        const double complex *cvf, int npts, const double *where, double complex *E) {
+  orc_scattered_E(lMax, np, pos, J, kr_ + I * ki_, cvf, npts, where, E);
+}

@@ -57,6 +57,10 @@ def _declare(L):
     L.qpms_gpu_trans_multipliers_export.argtypes = [ci, ci, vp, vp, vp, vp]
     L.qpms_gpu_dense_solve.restype = ci
     L.qpms_gpu_dense_solve.argtypes = [ci, ci, vp, vp, vp, ci, vp, vp]
+    L.qpms_gpu_ozaki_residual.restype = ci
+    L.qpms_gpu_ozaki_residual.argtypes = [ci, ci, vp, sz, ci, vp, vp, vp]
+    L.qpms_gpu_bf16_gemm.restype = ci
+    L.qpms_gpu_bf16_gemm.argtypes = [ci, ci, ci, vp, vp, vp]
     L.qpms_gpu_measure_fp64_peak.restype = ci
     L.qpms_gpu_measure_fp64_peak.argtypes = [vp]
     # complex by value is passed as two doubles (same registers on x86-64 and aarch64)

@@ -26,6 +26,7 @@
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <random>
@@ -471,6 +472,20 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   QG_CUDA_TRY(dev_alloc(&y64, (size_t)N * nrhs_max * 16));
   QG_CUDA_TRY(dev_alloc(&dinfo, 16));
   QG_CUDA_TRY(dev_alloc(&rs, (size_t)4 * Np * sizeof(double)));
+  use_ozaki = ozaki_wanted(nrhs_max);
+  if (use_ozaki && (dev_alloc(&oz_mat, ozaki_matrix_bytes(N)) != cudaSuccess ||
+                    dev_alloc(&oz_work, ozaki_work_bytes(N, nrhs_max)) != cudaSuccess)) {
+    cudaGetLastError();  // no room for the slices: keep the complex128 residual
+    for (void **q : {&oz_mat, &oz_work})
+      if (*q) {
+        if (pool)
+          cudaFreeAsync(*q, ast);
+        else
+          cudaFree(*q);
+        *q = nullptr;
+      }
+    use_ozaki = false;
+  }
   // random butterfly diagonals exp(r/10), r ~ U(-1/2, 1/2): [u level1][u level2][v level1][v level2]
   std::mt19937_64 gen(seed);
   std::uniform_real_distribution<double> U(-0.5, 0.5);
@@ -487,7 +502,14 @@ size_t DenseSolver::footprint(int N, int nrhs, int mode) {
   size_t b = (mode ? Np * Np * esz : 0) + Np * Np * 16 + nblk * 2 * nb * nb * esz;
   b += std::max<size_t>(Np * nb, nb * std::max<size_t>(Np, nrhs)) * esz;
   b += Np * nrhs * (8 + 16) + (size_t)N * nrhs * 32 + 16 + 4 * Np * 8;
-  return b + 10 * 512;  // allocation rounding
+  if (ozaki_wanted(nrhs)) b += ozaki_matrix_bytes(N) + ozaki_work_bytes(N, nrhs);
+  return b + 12 * 512;  // allocation rounding
+}
+
+bool ozaki_wanted(int nrhs_max) {
+  if (nrhs_max < kOzakiMinRhs) return false;
+  const char *e = getenv("QPMS_GB300_RESIDUAL");
+  return !(e && !strcmp(e, "ZGEMM"));
 }
 
 cudaError_t DenseSolver::dev_alloc(void *ptr, size_t bytes) {
@@ -497,7 +519,7 @@ cudaError_t DenseSolver::dev_alloc(void *ptr, size_t bytes) {
 
 void DenseSolver::release() {
   for (void *p : {(void *)A, (void *)T64, (void *)Dinv, (void *)work, (void *)rhs_lo, (void *)rp, (void *)r64,
-                  (void *)y64, (void *)dinfo, (void *)rs})
+                  (void *)y64, (void *)dinfo, (void *)rs, oz_mat, oz_work})
     if (p) {
       if (pool)
         cudaFreeAsync(p, ast);
@@ -508,6 +530,8 @@ void DenseSolver::release() {
   r64 = y64 = nullptr;
   dinfo = nullptr;
   rs = nullptr;
+  oz_mat = oz_work = nullptr;
+  use_ozaki = false;
 }
 
 // W_u^T (rows) of an Np x ncols FP64 block
@@ -535,6 +559,10 @@ int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st, bool ro
   mode = base_mode;
   trail_ct = base_trail;
   nb = mode ? 128 : 64;
+  if (use_ozaki) {
+    int e;
+    if ((e = ozaki_split_matrix(M64, ldm, rowmaj, N, oz_mat, &oz, st))) return e;
+  }
   return factorize_current(M64, ldm, st);
 }
 
@@ -649,13 +677,17 @@ int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int 
     if ((e = apply_inverse(r64, N, y64, N, nrhs, st))) return e;
     add_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)y64, (double2 *)X, first);
     first = false;
-    // r = B - M X (FP64)
-    QG_CUDA_TRY(cudaMemcpyAsync(r64, B, n * 16, cudaMemcpyDeviceToDevice, st));
-    // a row-major M read column-major is M^T: multiply with OP_T
-    QG_BLAS_TRY(cublasZgemm(h, row_major ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, N, nrhs, N, &mone,
-                            (const cuDoubleComplex *)M64, (int)ldm, (const cuDoubleComplex *)X, N, &one,
-                            (cuDoubleComplex *)r64, N));
-    g_launches.fetch_add(2);
+    // r = B - M X (FP64 accuracy)
+    if (use_ozaki && nrhs >= kOzakiMinRhs) {
+      if ((e = ozaki_residual(h, oz, X, B, r64, nrhs, oz_work, st))) return e;
+    } else {
+      QG_CUDA_TRY(cudaMemcpyAsync(r64, B, n * 16, cudaMemcpyDeviceToDevice, st));
+      // a row-major M read column-major is M^T: multiply with OP_T
+      QG_BLAS_TRY(cublasZgemm(h, row_major ? CUBLAS_OP_T : CUBLAS_OP_N, CUBLAS_OP_N, N, nrhs, N, &mone,
+                              (const cuDoubleComplex *)M64, (int)ldm, (const cuDoubleComplex *)X, N, &one,
+                              (cuDoubleComplex *)r64, N));
+      g_launches.fetch_add(2);
+    }
     QG_CUDA_TRY(cudaMemsetAsync(nrm, 0, 8, st));
     norm2_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)r64, nrm);
     QG_CUDA_TRY(cudaMemcpyAsync(&hr, nrm, 8, cudaMemcpyDeviceToHost, st));

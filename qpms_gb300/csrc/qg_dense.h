@@ -3,7 +3,16 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "qg_ozaki.h"
+
 namespace qg {
+
+// Right-hand-side count from which the refinement residual runs as digit
+// products on the bf16 tensor cores (qg_ozaki.cu) instead of a complex128
+// GEMM; below it the residual is bandwidth-bound on M and the FP64 GEMM is
+// cheaper.  QPMS_GB300_RESIDUAL=ZGEMM turns the digit path off.
+constexpr int kOzakiMinRhs = 8;
+bool ozaki_wanted(int nrhs_max);
 
 // The system is padded to Np = N rounded up to a multiple of 4 (identity on the
 // padding), the size the two butterfly levels halve.
@@ -28,6 +37,10 @@ struct DenseSolver {
   int trail_ct = 0;        // cublasComputeType_t of the complex64 trailing updates (mode 1)
   int refactors = 0;       // refinement stalls answered by more precise factors
   int base_mode = 0, base_trail = 0;  // what factorize() starts from (the fallbacks change mode / trail_ct)
+  // digit slices of M for the tensor-core residual (nrhs_max >= kOzakiMinRhs)
+  bool use_ozaki = false;
+  void *oz_mat = nullptr, *oz_work = nullptr;
+  OzakiMatrix oz;
 
   int init(int N, int nrhs_max, int mode, unsigned long long seed, cudaMemPool_t pool = nullptr,
            cudaStream_t alloc_stream = nullptr);

@@ -1,0 +1,331 @@
+// FP64-accurate residual R = B - M X on the bf16 tensor cores (error-free
+// splitting after Ozaki, Ogita, Oishi and Rump, "Error-free transformations of
+// matrix multiplication by using fast routines of matrix multiplication and
+// its applications", Numer. Algorithms 59 (2012) 95-118).
+//
+// GB300 runs FP64 at about 1.2 TFLOP/s (DMMA) but bf16 at about 2 PFLOP/s.
+// The refinement residual of the dense solver is a complex128 GEMM of the
+// N x N matrix with the N x nrhs iterate: at N = 14400, nrhs = 64 it is
+// about 1e11 FP64 flops, 0.1 s per application on the FP64 pipe.  Here the
+// real matrix [Re M; Im M] (2N x N) is cut row by row into p digits of s bits
+// (integers, exact in bf16), the iterate [Re X, Im X] (N x 2 nrhs) column by
+// column likewise, and every product of digits D_i E_j is formed by a bf16
+// GEMM with FP32 accumulation.  s is chosen so that every partial sum is an
+// integer below 2^24 (ozaki_digits): the GEMMs are exact whatever their
+// summation order or split-K.  The products with i + j <= p - 1 are summed in
+// FP64, scaled back by the powers of two of the rows and columns; the result
+// carries the normwise error of an FP64 GEMM (55 bits of digits).
+//
+// One GEMM per row digit i multiplies D_i with the concatenation
+// [E_0 | ... | E_{p-1-i}] (the column digits are stored contiguously, so
+// that concatenation is a prefix): p GEMMs of 2N x 2 nrhs (p - i) x N.
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include "qg_internal.h"
+#include "qg_ozaki.h"
+
+namespace qg {
+int blas_handle_get(cublasHandle_t *h);
+
+namespace {
+
+size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+unsigned grid1(size_t n) { return (unsigned)((n + 255) / 256); }
+
+__device__ __forceinline__ void umax(unsigned long long *a, double v) {
+  atomicMax(a, (unsigned long long)__double_as_longlong(v));
+}
+
+// max |Re|, |Im| per row of a row-major M: one block per row.
+__global__ void rowmax_rowmajor_kernel(const double2 *__restrict__ M, size_t ldm, int N,
+                                       unsigned long long *rowmax) {
+  const int r = blockIdx.x;
+  double mr = 0, mi = 0;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    const double2 v = M[(size_t)r * ldm + k];
+    mr = fmax(mr, fabs(v.x));
+    mi = fmax(mi, fabs(v.y));
+  }
+  for (int o = 16; o; o >>= 1) {
+    mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    mi = fmax(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    umax(rowmax + r, mr);
+    umax(rowmax + N + r, mi);
+  }
+}
+
+// The same for a column-major M: a thread per row, columns split over grid.y.
+__global__ void rowmax_colmajor_kernel(const double2 *__restrict__ M, size_t ldm, int N, int kchunk,
+                                       unsigned long long *rowmax) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  const int k0 = blockIdx.y * kchunk, k1 = min(N, k0 + kchunk);
+  double mr = 0, mi = 0;
+  for (int k = k0; k < k1; ++k) {
+    const double2 v = M[(size_t)k * ldm + r];
+    mr = fmax(mr, fabs(v.x));
+    mi = fmax(mi, fabs(v.y));
+  }
+  umax(rowmax + r, mr);
+  umax(rowmax + N + r, mi);
+}
+
+// sigma = 2^e with max / sigma in [1/2, 1) (1 for a zero row).
+__global__ void scale_kernel(const unsigned long long *rowmax, int n, double *scale) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double m = __longlong_as_double((long long)rowmax[i]);
+  int e = 0;
+  if (m > 0) frexp(m, &e);
+  scale[i] = ldexp(1.0, e);
+}
+
+// p digits of v in (-1, 1): t = v 2^s, d = rint(t), v = t - d (all exact).
+template <typename Store>
+__device__ __forceinline__ void digits(double v, int s, int p, Store st) {
+  const double two_s = ldexp(1.0, s);
+  for (int i = 0; i < p; ++i) {
+    const double t = v * two_s;
+    const double d = rint(t);
+    v = t - d;
+    st(i, __double2bfloat16(d));
+  }
+}
+
+// Slices of [Re M; Im M]; element (R, k) of digit i at
+//   row-major layout: sl[i 2N N + R N + k]   (rows contiguous, GEMM op T)
+//   column-major:     sl[i 2N N + k 2N + R]  (GEMM op N)
+__global__ void split_matrix_kernel(const double2 *__restrict__ M, size_t ldm, int N, bool row_major,
+                                    const double *__restrict__ scale, int s, int p, __nv_bfloat16 *sl) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t NN = (size_t)N * N;
+  if (idx >= NN) return;
+  int r, k;
+  if (row_major) {
+    r = (int)(idx / N);
+    k = (int)(idx % N);
+  } else {
+    k = (int)(idx / N);
+    r = (int)(idx % N);
+  }
+  const double2 v = row_major ? M[(size_t)r * ldm + k] : M[(size_t)k * ldm + r];
+  const size_t slab = 2 * NN;
+  const size_t oR = row_major ? (size_t)r * N + k : (size_t)k * 2 * N + r;
+  const size_t oI = row_major ? (size_t)(N + r) * N + k : (size_t)k * 2 * N + N + r;
+  digits(v.x / scale[r], s, p, [&](int i, __nv_bfloat16 d) { sl[i * slab + oR] = d; });
+  digits(v.y / scale[N + r], s, p, [&](int i, __nv_bfloat16 d) { sl[i * slab + oI] = d; });
+}
+
+// max |entry| per column of [Re X, Im X] (N x 2 nrhs): one block per column.
+__global__ void colmax_kernel(const double2 *__restrict__ X, int N, int nrhs, double *tau) {
+  const int C = blockIdx.x;
+  const int c = C % nrhs;
+  const bool im = C >= nrhs;
+  double m = 0;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    const double2 v = X[(size_t)c * N + k];
+    m = fmax(m, fabs(im ? v.y : v.x));
+  }
+  __shared__ double red[32];
+  for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+    int e = 0;
+    if (m > 0) frexp(m, &e);
+    tau[C] = ldexp(1.0, e);
+  }
+}
+
+// Column digits: element (k, C) of digit j at bsl[(j 2nrhs + C) N + k].
+__global__ void split_rhs_kernel(const double2 *__restrict__ X, int N, int nrhs, const double *__restrict__ tau,
+                                 int s, int p, __nv_bfloat16 *bsl) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)N * nrhs) return;
+  const int c = (int)(idx / N), k = (int)(idx % N);
+  const double2 v = X[idx];
+  const size_t w = (size_t)2 * nrhs * N;
+  digits(v.x / tau[c], s, p, [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)c * N + k] = d; });
+  digits(v.y / tau[nrhs + c], s, p,
+         [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)(nrhs + c) * N + k] = d; });
+}
+
+// P[R, C] (+)= sum_{j <= p-1-i} 2^{-s (i+j+2)} G[R, j 2nrhs + C], j descending
+// (smallest terms first); G = D_i [E_0 | ... ] exact in FP32.
+__global__ void accumulate_kernel(const float *__restrict__ G, int twoN, int twonrhs, int i, int s, int p,
+                                  bool first, double *P) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)twoN * twonrhs) return;
+  const int C = (int)(idx / twoN), R = (int)(idx % twoN);
+  double acc = 0;
+  for (int j = p - 1 - i; j >= 0; --j)
+    acc += ldexp((double)G[(size_t)(j * twonrhs + C) * twoN + R], -s * (i + j + 2));
+  P[idx] = first ? acc : P[idx] + acc;
+}
+
+// R = B - M X from P = [Re M; Im M] [Re X, Im X] (unscaled digits sums).
+__global__ void combine_kernel(const double *__restrict__ P, const double *__restrict__ sigma,
+                               const double *__restrict__ tau, int N, int nrhs, const double2 *__restrict__ B,
+                               double2 *__restrict__ Rout) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)N * nrhs) return;
+  const int c = (int)(idx / N), r = (int)(idx % N);
+  const size_t twoN = 2 * (size_t)N;
+  const double sr = sigma[r], si = sigma[N + r], tr = tau[c], ti = tau[nrhs + c];
+  const double pRR = P[(size_t)c * twoN + r] * sr * tr;
+  const double pII = P[(size_t)(nrhs + c) * twoN + N + r] * si * ti;
+  const double pRI = P[(size_t)(nrhs + c) * twoN + r] * sr * ti;
+  const double pIR = P[(size_t)c * twoN + N + r] * si * tr;
+  const double2 b = B[idx];
+  Rout[idx] = make_double2(b.x - (pRR - pII), b.y - (pRI + pIR));
+}
+
+}  // namespace
+
+void ozaki_digits(int K, int *s, int *p) {
+  int lk = 0;
+  while ((1LL << lk) < (long long)K) ++lk;  // ceil(log2 K)
+  int ss = (24 - lk) / 2;
+  if (ss > 8) ss = 8;  // bf16 holds integers up to 2^8 exactly
+  if (ss < 1) ss = 1;
+  *s = ss;
+  *p = (55 + ss - 1) / ss;
+}
+
+size_t ozaki_matrix_bytes(int N) {
+  int s, p;
+  ozaki_digits(N, &s, &p);
+  return al256((size_t)p * 2 * N * N * 2) + 2 * al256((size_t)2 * N * 8);
+}
+
+size_t ozaki_work_bytes(int N, int nrhs) {
+  int s, p;
+  ozaki_digits(N, &s, &p);
+  const size_t tn = 2 * (size_t)nrhs;
+  return al256((size_t)p * N * tn * 2) + al256(tn * 8) + al256((size_t)2 * N * tn * p * 4) +
+         al256((size_t)2 * N * tn * 8);
+}
+
+int ozaki_split_matrix(const void *M, size_t ldm, bool row_major, int N, void *buf, OzakiMatrix *om,
+                       cudaStream_t st) {
+  int s, p;
+  ozaki_digits(N, &s, &p);
+  char *b = (char *)buf;
+  om->N = N;
+  om->s = s;
+  om->p = p;
+  om->row_major = row_major;
+  om->slices = b;
+  b += al256((size_t)p * 2 * N * N * 2);
+  om->scale = (double *)b;
+  b += al256((size_t)2 * N * 8);
+  om->rowmax = (unsigned long long *)b;
+  const double2 *Md = (const double2 *)M;
+  QG_CUDA_TRY(cudaMemsetAsync(om->rowmax, 0, (size_t)2 * N * 8, st));
+  if (row_major) {
+    rowmax_rowmajor_kernel<<<N, 256, 0, st>>>(Md, ldm, N, om->rowmax);
+  } else {
+    const int kchunk = 256;
+    rowmax_colmajor_kernel<<<dim3((N + 255) / 256, (N + kchunk - 1) / kchunk), 256, 0, st>>>(Md, ldm, N, kchunk,
+                                                                                           om->rowmax);
+  }
+  QG_CUDA_TRY(cudaGetLastError());
+  scale_kernel<<<grid1(2 * (size_t)N), 256, 0, st>>>(om->rowmax, 2 * N, om->scale);
+  QG_CUDA_TRY(cudaGetLastError());
+  split_matrix_kernel<<<grid1((size_t)N * N), 256, 0, st>>>(Md, ldm, N, row_major, om->scale, s, p,
+                                                            (__nv_bfloat16 *)om->slices);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(3);
+  return QPMS_SUCCESS;
+}
+
+int ozaki_residual(cublasHandle_t h, const OzakiMatrix &om, const void *X, const void *B, void *R, int nrhs,
+                   void *work, cudaStream_t st) {
+  const int N = om.N, s = om.s, p = om.p, tn = 2 * nrhs, twoN = 2 * N;
+  char *w = (char *)work;
+  __nv_bfloat16 *bsl = (__nv_bfloat16 *)w;
+  w += al256((size_t)p * N * tn * 2);
+  double *tau = (double *)w;
+  w += al256((size_t)tn * 8);
+  float *G = (float *)w;
+  w += al256((size_t)twoN * tn * p * 4);
+  double *P = (double *)w;
+  colmax_kernel<<<tn, 256, 0, st>>>((const double2 *)X, N, nrhs, tau);
+  QG_CUDA_TRY(cudaGetLastError());
+  split_rhs_kernel<<<grid1((size_t)N * nrhs), 256, 0, st>>>((const double2 *)X, N, nrhs, tau, s, p, bsl);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(2);
+  const float one = 1.0f, zero = 0.0f;
+  const cublasOperation_t opA = om.row_major ? CUBLAS_OP_T : CUBLAS_OP_N;
+  const int lda = om.row_major ? N : twoN;
+  for (int i = p - 1; i >= 0; --i) {  // smallest contributions first
+    const int n = tn * (p - i);
+    const __nv_bfloat16 *Ai = (const __nv_bfloat16 *)om.slices + (size_t)i * twoN * N;
+    QG_BLAS_TRY(cublasGemmEx(h, opA, CUBLAS_OP_N, twoN, n, N, &one, Ai, CUDA_R_16BF, lda, bsl, CUDA_R_16BF, N,
+                             &zero, G, CUDA_R_32F, twoN, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT));
+    accumulate_kernel<<<grid1((size_t)twoN * tn), 256, 0, st>>>(G, twoN, tn, i, s, p, i == p - 1, P);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(2);
+  }
+  combine_kernel<<<grid1((size_t)N * nrhs), 256, 0, st>>>(P, om.scale, tau, N, nrhs, (const double2 *)B,
+                                                          (double2 *)R);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(1);
+  return QPMS_SUCCESS;
+}
+
+}  // namespace qg
+
+using namespace qg;
+
+// Test entry: R = B - M X (device complex128; M column-major or row-major
+// N x N with leading dimension ldm; X, B, R N x nrhs, leading dimension N)
+// through the digit GEMMs.  Allocates its own buffers.
+extern "C" int qpms_gpu_ozaki_residual(int N, int nrhs, const qpms_complex_t *M, size_t ldm, int row_major,
+                                       const qpms_complex_t *X, const qpms_complex_t *B, qpms_complex_t *R) {
+  clear_error();
+  if (N <= 0 || nrhs <= 0 || !M || !X || !B || !R || ldm < (size_t)N) {
+    set_error("invalid arguments");
+    return QPMS_EINVAL;
+  }
+  cublasHandle_t h;
+  int e;
+  if ((e = blas_handle_get(&h))) return e;
+  QG_BLAS_TRY(cublasSetStream(h, 0));
+  void *mb = nullptr, *wb = nullptr;
+  QG_CUDA_TRY(cudaMalloc(&mb, ozaki_matrix_bytes(N)));
+  if (cudaMalloc(&wb, ozaki_work_bytes(N, nrhs)) != cudaSuccess) {
+    cudaFree(mb);
+    set_error("ozaki workspace: out of memory");
+    return QPMS_ERROR;
+  }
+  OzakiMatrix om;
+  e = ozaki_split_matrix(M, ldm, row_major != 0, N, mb, &om, 0);
+  if (!e) e = ozaki_residual(h, om, X, B, R, nrhs, wb, 0);
+  cudaError_t se = cudaDeviceSynchronize();
+  cudaFree(mb);
+  cudaFree(wb);
+  if (e) return e;
+  QG_CUDA_TRY(se);
+  return QPMS_SUCCESS;
+}
+
+// Test entry: C = A B for bf16 A (m x k), B (k x n) column-major, FP32 C,
+// through the same cuBLAS call as the digit products (checks that integer
+// products with partial sums below 2^24 come out exact).
+extern "C" int qpms_gpu_bf16_gemm(int m, int n, int k, const void *A, const void *B, float *C) {
+  clear_error();
+  cublasHandle_t h;
+  int e;
+  if ((e = blas_handle_get(&h))) return e;
+  QG_BLAS_TRY(cublasSetStream(h, 0));
+  const float one = 1.0f, zero = 0.0f;
+  QG_BLAS_TRY(cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A, CUDA_R_16BF, m, B, CUDA_R_16BF, k, &zero,
+                           C, CUDA_R_32F, m, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT));
+  QG_CUDA_TRY(cudaDeviceSynchronize());
+  return QPMS_SUCCESS;
+}

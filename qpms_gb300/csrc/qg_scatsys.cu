@@ -300,6 +300,8 @@ void lattice_reduce(double *b1, double *b2) {
   }
 }
 
+void field_forget_system(const qpms_scatsys_t *ss);  // qg_field.cu
+
 // Accessors used by qg_solve.cu.
 bool scatsys_is_own(const qpms_scatsys_t *ss) { return ss && ss->medium.function == epsmu_const_fn; }
 int scatsys_lmax(const qpms_scatsys_t *ss) { return sspriv(ss)->lMax; }
@@ -520,6 +522,7 @@ static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *
 
 void qpms_gpu_scatsys_free(qpms_scatsys_t *ss) {
   if (!ss) return;
+  field_forget_system(ss);
   delete sspriv(ss);  // the translation calculator is shared (shared_calculator)
 }
 

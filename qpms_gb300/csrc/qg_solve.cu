@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "qg_assembly.h"
+#include "qg_dense.h"
 #include "qg_internal.h"
 
 namespace qg {
@@ -54,6 +55,87 @@ int ptr_array(Dev &arr, void *base, size_t stride_bytes, int nb) {
   int e;
   if ((e = dalloc(arr, sizeof(void *) * nb))) return e;
   QG_CUDA_TRY(cudaMemcpy(arr.p, h.data(), sizeof(void *) * nb, cudaMemcpyHostToDevice));
+  return QPMS_SUCCESS;
+}
+
+// Above this size the batched (one kernel per small matrix) LU is slow and
+// each frequency runs through the dense solver (RBT + blocked LU) instead.
+constexpr size_t kBatchedMaxN = 512;
+
+// The finite plane-wave scatter for large systems: one frequency at a time
+// (one N x N matrix resident), assembly -> incidence -> T a -> dense solve
+// with FP64 refinement -> sigma_ext (and sigma_scat).
+int finite_scatter_dense(const qpms_scatsys_t *ss, int W, const std::vector<qg_c> &T, const std::vector<qg_c> &k,
+                         const std::vector<double> &kvec, const std::vector<qg_c> &coef, int mode, qpms_complex_t *f_out,
+                         double *sigma_ext, double *sigma_scat, double *resid_out, int *iters_out) {
+  const int lMax = scatsys_lmax(ss), np = ss->p_count, ntm = ss->tm_count;
+  const int n = 2 * lMax * (lMax + 2);
+  const size_t N = ss->fecv_size, N2 = N * N;
+  const size_t tper = T.size() / W;
+  cudaStream_t st = 0;
+  int e;
+  Dev dM, dT, dtm, dpos, dk, dkv, dcoef, da, db, dx, dr, dn, dsig;
+  if ((e = dalloc(dM, N2 * 16)) || (e = dalloc(dT, tper * 16)) || (e = dalloc(dtm, np * 4)) ||
+      (e = dalloc(dpos, np * 24)) || (e = dalloc(dk, 16)) || (e = dalloc(dkv, 24)) || (e = dalloc(dcoef, n * 16)) ||
+      (e = dalloc(da, N * 16)) || (e = dalloc(db, N * 16)) || (e = dalloc(dx, N * 16)) || (e = dalloc(dr, N * 16)) ||
+      (e = dalloc(dn, 16)) || (e = dalloc(dsig, 8)))
+    return e;
+  std::vector<double> pos(3 * np);
+  std::vector<int> tm(np);
+  for (int i = 0; i < np; ++i) {
+    pos[3 * i] = ss->p[i].pos.x;
+    pos[3 * i + 1] = ss->p[i].pos.y;
+    pos[3 * i + 2] = ss->p[i].pos.z;
+    tm[i] = ss->p[i].tmatrix_id;
+  }
+  QG_CUDA_TRY(cudaMemcpy(dtm.p, tm.data(), np * 4, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpy(dpos.p, pos.data(), np * 24, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpy(dcoef.p, coef.data(), n * 16, cudaMemcpyHostToDevice));
+  DenseSolver ds;
+  if ((e = ds.init((int)N, 1, mode, 0x5eedbe11))) return e;
+  auto assemble = [&](int J, const qg_c *Tsrc) -> int {
+    QG_CUDA_TRY(cudaMemcpy(dT.p, Tsrc, tper * 16, cudaMemcpyHostToDevice));
+    AsmArgs a;
+    a.nw = 1;
+    a.np = np;
+    a.ntm = ntm;
+    a.dense = 0;
+    a.J = J;
+    a.pos = dpos.as<double>();
+    a.tmid = dtm.as<int>();
+    a.T = dT.as<qg_c>();
+    a.k = dk.as<qg_c>();
+    a.M = dM.as<qg_c>();
+    return launch_assemble(a, priv(ss->c)->dev, st);
+  };
+  const std::vector<qg_c> mone(tper, cmk(-1.0, 0.0));
+  for (int w = 0; w < W; ++w) {
+    QG_CUDA_TRY(cudaMemcpy(dk.p, &k[w], 16, cudaMemcpyHostToDevice));
+    QG_CUDA_TRY(cudaMemcpy(dkv.p, &kvec[3 * w], 24, cudaMemcpyHostToDevice));
+    if ((e = assemble(3, T.data() + w * tper))) return e;  // row-major M = I - T S
+    if ((e = launch_incident(1, np, n, dcoef.as<qg_c>(), dkv.as<double>(), dpos.as<double>(), da.as<qg_c>(), st)))
+      return e;
+    if ((e = launch_apply_t(1, np, n, ntm, 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(), db.as<qg_c>(), st)))
+      return e;
+    if ((e = ds.factorize(dM.p, N, st, true))) return e;
+    double res = 0;
+    int it = 0;
+    if ((e = ds.solve(dM.p, N, db.p, dx.p, 1, 1e-13, 12, &res, &it, st))) return e;
+    if (resid_out) resid_out[w] = res;
+    if (iters_out) iters_out[w] = it;
+    if ((e = launch_sigma_ext(1, N, da.as<qg_c>(), dx.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), st))) return e;
+    QG_CUDA_TRY(cudaMemcpy(sigma_ext + w, dsig.p, 8, cudaMemcpyDeviceToHost));
+    if (sigma_scat) {
+      if ((e = assemble(1, mone.data()))) return e;  // I + R (regular waves, zero self blocks)
+      QG_CUDA_TRY(cudaMemsetAsync(db.p, 0, N * 16, st));
+      double *rn2 = dn.as<double>();
+      if ((e = launch_residual(1, N, dM.as<qg_c>(), dx.as<qg_c>(), db.as<qg_c>(), dr.as<qg_c>(), rn2, rn2 + 1, st)))
+        return e;
+      if ((e = launch_sigma_ext(1, N, dx.as<qg_c>(), dr.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), st))) return e;
+      QG_CUDA_TRY(cudaMemcpy(sigma_scat + w, dsig.p, 8, cudaMemcpyDeviceToHost));
+    }
+    if (f_out) QG_CUDA_TRY(cudaMemcpy(f_out + w * N, dx.p, N * 16, cudaMemcpyDeviceToHost));
+  }
   return QPMS_SUCCESS;
 }
 
@@ -270,6 +352,8 @@ int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw, c
     for (int c = 0; c < 3; ++c) kvec[3 * w + c] = k[w].re * k_dir[c] / kn;
   }
   planewave_direction_coeffs(lMax, k_dir, E_cart, coef);
+  if (N > kBatchedMaxN)
+    return finite_scatter_dense(ss, W, T, k, kvec, coef, mode, f_out, sigma_ext, sigma_scat, resid_out, iters_out);
   cudaStream_t st = 0;
   cublasHandle_t h;
   int e;

@@ -18,9 +18,38 @@ class _SSWK(C.Structure):
     _fields_ = [("ssw", C.c_void_p), ("k", C.c_double * 3), ("eta", C.c_double)]
 
 
+class _SSW(C.Structure):
+    _fields_ = [("ss", C.c_void_p), ("tm", C.c_void_p), ("omega", C.c_double * 2),
+                ("medium", C.c_double * 4), ("wavenumber", C.c_double * 2)]
+
+
 class _LU(C.Structure):
     _fields_ = [("ssw", C.c_void_p), ("sswk", C.c_void_p), ("full", C.c_bool), ("iri", C.c_int),
                 ("a", C.c_void_p), ("ipiv", C.c_void_p)]
+
+
+class _Cart3(C.Structure):
+    _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+
+class _CCart3(C.Structure):
+    _fields_ = [("v", C.c_double * 6)]
+
+
+def _scattered_E(L, s, wavenumber, cvf, evalpos, n, btyp):
+    """qpms_c.pyx:904-927: evalpos [..., 3] -> E [..., 3] complex, one batched call."""
+    evalpos = np.asarray(evalpos, dtype=np.float64)
+    if evalpos.shape[-1] != 3:
+        raise ValueError("Last dimension of evalpos has to be 3")
+    w = np.ascontiguousarray(evalpos.reshape(-1, 3))
+    cv = np.ascontiguousarray(cvf, dtype=np.complex128)
+    if cv.size != n:
+        raise ValueError("Length of a full coefficient vector has to be %d, not %d" % (n, cv.size))
+    E = np.empty((w.shape[0], 3), dtype=np.complex128)
+    k = complex(wavenumber)
+    _lib.check(L.qpms_gpu_scatsys_scattered_E(s, int(btyp), k.real, k.imag, cv.ctypes.data, w.shape[0],
+                                              w.ctypes.data, E.ctypes.data), "qpms_gpu_scatsys_scattered_E")
+    return E.reshape(evalpos.shape)
 
 
 def declare(L):
@@ -62,6 +91,16 @@ def declare(L):
     L.qpms_gpu_finite_planewave_scatter.restype = ci
     L.qpms_gpu_finite_planewave_scatter.argtypes = [vp, sz, vp, vp, vp, ci, vp, vp, vp, vp]
     L.qpms_gpu_finite_planewave_scatter_ext.restype = ci
+    L.qpms_gpu_scatsys_scattered_E.restype = ci
+    L.qpms_gpu_scatsys_scattered_E.argtypes = [vp, ci, cd, cd, vp, sz, vp, vp]
+    L.qpms_gpu_scatsys_scattered_E_device.restype = ci
+    L.qpms_gpu_scatsys_scattered_E_device.argtypes = [vp, ci, cd, cd, vp, sz, vp, vp, vp]
+    for name in ("qpms_scatsys_scattered_E", "qpms_scatsys_scattered_E__alt"):
+        getattr(L, name).restype = _CCart3
+        getattr(L, name).argtypes = [vp, ci, cd, cd, vp, _Cart3]
+    for name in ("qpms_scatsysw_scattered_E", "qpms_scatsysw_scattered_E__alt"):
+        getattr(L, name).restype = _CCart3
+        getattr(L, name).argtypes = [vp, ci, vp, _Cart3]
     L.qpms_gpu_finite_planewave_scatter_ext.argtypes = [vp, sz, vp, vp, vp, ci, vp, vp, vp, vp, vp]
 
 
@@ -125,6 +164,27 @@ class ScatteringSystem:
         out = np.empty(self.fecv_size, dtype=np.complex128)
         _lib.check(self._L.qpms_gpu_incident_planewave_full(out.ctypes.data, self.s, k.ctypes.data, E.ctypes.data),
                    "qpms_gpu_incident_planewave_full")
+        return out
+
+    def scattered_E(self, wavenumber, scatcoeffvector_full, evalpos, alt=False, btyp=QPMS_HANKEL_PLUS):
+        """Field of the full coefficient vector at the points evalpos [..., 3]
+        (qpms_c.pyx:904-927); ``alt`` selects the reference's alternative route,
+        which evaluates the same field."""
+        return _scattered_E(self._L, self.s, wavenumber, scatcoeffvector_full, evalpos, self.fecv_size, btyp)
+
+    def scattered_E_device(self, wavenumber, cvf, evalpos, out=None, btyp=QPMS_HANKEL_PLUS, stream=None):
+        """Device-tensor variant: cvf (fecv_size,) complex128, evalpos (n, 3)
+        float64 and out (n, 3) complex128 CUDA tensors; runs on `stream`
+        (default: torch's current stream)."""
+        import torch
+        if out is None:
+            out = torch.empty((evalpos.shape[0], 3), dtype=torch.complex128, device=evalpos.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(evalpos.device)
+        k = complex(wavenumber)
+        _lib.check(self._L.qpms_gpu_scatsys_scattered_E_device(
+            self.s, int(btyp), k.real, k.imag, cvf.data_ptr(), evalpos.shape[0], evalpos.data_ptr(),
+            out.data_ptr(), stream.cuda_stream), "qpms_gpu_scatsys_scattered_E_device")
         return out
 
     def translation_matrix_full(self, wavenumber, J=QPMS_HANKEL_PLUS):
@@ -262,6 +322,15 @@ class _ScatteringSystemAtOmega:
 
     def scatter_solver(self):
         return ScatteringMatrix(self)
+
+    def wavenumber(self):
+        """ssw->wavenumber of the C structure (scatsystem.h:239-249)."""
+        w = C.cast(self.ssw, C.POINTER(_SSW)).contents
+        return complex(w.wavenumber[0], w.wavenumber[1])
+
+    def scattered_E(self, scatcoeffvector_full, evalpos, alt=False, btyp=QPMS_HANKEL_PLUS):
+        """qpms_c.pyx:1118-1141, at this frequency's wavenumber."""
+        return self.ss.scattered_E(self.wavenumber(), scatcoeffvector_full, evalpos, alt, btyp)
 
 
 class ScatteringMatrix:

@@ -158,3 +158,26 @@ def test_lorentz_drude_spheres_vs_oracle(gpu, orc):
         f, _, sig = orc.finite_sphere_scatter(c, pos, 50e-9, au(w), EPS_E, w)
         assert np.linalg.norm(out["f"][i] - f) <= 1e-9 * np.linalg.norm(f)
         assert abs(out["sigma_ext"][i] - sig) <= 1e-9 * abs(sig)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_large_system_dense_path_vs_oracle(gpu, orc, mode):
+    """N = 768 > 512: each frequency runs through the dense solver (random
+    butterfly + LU without pivoting, FP64 refinement) instead of the batched
+    LU; f, sigma_ext and sigma_scat against the oracle's LAPACK-style solve."""
+    lMax = 4
+    pos = square_array(4, 4, 400e-9)
+    ss = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax)
+    assert ss.fecv_size == 768
+    om = np.array([1.8, 2.3]) * EV / HBAR
+    out = ss.planewave_scatter_batch(om, mode=mode, want_f=True, want_scat=True)
+    c = orc.TransCalculator(lMax)
+    for i, w in enumerate(om):
+        ke = np.sqrt(EPS_E) * w / C0
+        f, _, sig = orc.finite_sphere_scatter(c, pos, 50e-9, EPS_I, EPS_E, w)
+        assert out["residual"][i] <= 1e-12
+        assert np.linalg.norm(out["f"][i] - f) <= 1e-9 * np.linalg.norm(f)
+        assert abs(out["sigma_ext"][i] - sig) <= 1e-9 * abs(sig)
+        R = orc.finite_translation_matrix(c, pos, ke, 1)
+        ref = np.vdot(f, (R + np.eye(len(f))) @ f).real / ke ** 2
+        assert abs(out["sigma_scat"][i] - ref) <= 1e-9 * abs(ref)
