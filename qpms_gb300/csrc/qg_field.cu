@@ -227,6 +227,34 @@ __global__ void field_reduce_kernel(const qg_c *__restrict__ part, int nsplit, s
   out[i] = s;
 }
 
+// Resident blocks of the lMax kernel on the whole device (one wave).
+template <int L>
+long field_wave_L() {
+  int dev = 0, nsm = 152, per = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, scattered_field_kernel<L>, kFieldThreads, 0) !=
+          cudaSuccess ||
+      per < 1) {
+    cudaGetLastError();
+    per = 1;
+  }
+  return (long)nsm * per;
+}
+
+long field_wave(int lMax) {
+  switch (lMax) {
+    case 1: return field_wave_L<1>();
+    case 2: return field_wave_L<2>();
+    case 3: return field_wave_L<3>();
+    case 4: return field_wave_L<4>();
+    case 5: return field_wave_L<5>();
+    case 6: return field_wave_L<6>();
+    case 7: return field_wave_L<7>();
+    default: return field_wave_L<8>();
+  }
+}
+
 template <int L>
 cudaError_t launch_field_L(const FieldArgs &a, int nsplit, cudaStream_t st) {
   dim3 grid((a.npts + kFieldThreads - 1) / kFieldThreads, nsplit);
@@ -329,17 +357,23 @@ int field_device(const qpms_scatsys_t *ss, int btyp, qg_c k, const qg_c *d_cvf, 
   a.pos = d_pos;
   a.cvf = d_cvf;
   a.tb = field_tables();
-  // enough blocks for two waves of ~4 resident blocks per SM; >= 8 particles per split
-  int nsm = 152;
-  {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  }
+  // Split the particles over grid.y so that the grid fills whole waves of
+  // resident blocks (at least two waves), with >= 8 particles per split.
   const long bx = ((long)npoints + kFieldThreads - 1) / kFieldThreads;
-  long nsplit = (8L * nsm + bx - 1) / bx;
-  nsplit = std::min<long>(nsplit, std::max(1, a.np / 8));
-  nsplit = std::max<long>(1, std::min<long>(nsplit, 65535));
+  const long wave = field_wave(lMax);
+  const long maxsplit = std::max(1, std::min(a.np / 8, 65535));
+  long nsplit = 1;
+  double best = 2.0;
+  for (long sp = 1; sp <= maxsplit; ++sp) {
+    const long tot = bx * sp, waves = (tot + wave - 1) / wave;
+    if (waves < 2 && sp < maxsplit) continue;
+    const double idle = (double)(waves * wave - tot) / (double)(waves * wave);
+    if (idle < best - 0.02) {  // a smaller split unless a larger one idles clearly less
+      best = idle;
+      nsplit = sp;
+    }
+    if (tot >= 16 * wave) break;
+  }
   a.chunk = (int)((a.np + nsplit - 1) / nsplit);
   nsplit = (a.np + a.chunk - 1) / a.chunk;
   if (nsplit == 1) {
