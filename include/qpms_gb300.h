@@ -37,7 +37,15 @@ typedef int qpms_bessel_t;            /* enum, qpms_types.h:176-182: 1 j, 2 y, 3
 #define QPMS_ERROR 1
 #define QPMS_ENOMEM 12
 #define QPMS_EINVAL 22
+#define QPMS_NAN_ENCOUNTERED 1024  /* qpms_types.h:91 */
+#define QPMS_NORMALISATION_INVERSE 1
+#define QPMS_NORMALISATION_REVERSE_AZIMUTHAL_PHASE 2
+#define QPMS_NORMALISATION_SPHARM_REAL 4
 #define QPMS_NORMALISATION_CSPHASE 8
+#define QPMS_NORMALISATION_M_I 16
+#define QPMS_NORMALISATION_M_MINUS 32
+#define QPMS_NORMALISATION_N_I 64
+#define QPMS_NORMALISATION_N_MINUS 128
 #define QPMS_NORMALISATION_NORM_POWER 65536
 #define QPMS_NORMALISATION_NORM_NONE (65536 * 2)
 #define QPMS_NORMALISATION_NORM_SPHARM (65536 * 3)
@@ -287,6 +295,76 @@ extern const qpms_ldparams_t *const QPMS_LDPARAMS_CR;
 /* materials.c:156-164: sum_j f_j omega_p^2 / (omega_j^2 - omega^2 - i omega gamma_j).
  * As in the reference, eps_inf is not added. */
 qpms_complex_t qpms_lorentzdrude_eps(qpms_complex_t omega, const qpms_ldparams_t *p);
+
+/* ---- tabulated data: interpolators (materials.h:101-145, tmatrices.h:285-330) ----
+ * qpms_interp_type_t stands for the reference's gsl_interp_type: the two
+ * kinds its Python layer uses, piecewise linear and the natural cubic spline
+ * (gsl_interp_linear, gsl_interp_cspline).  Outside the tabulated range an
+ * evaluation gives NaN. */
+typedef struct qpms_interp_type_t qpms_interp_type_t;
+extern const qpms_interp_type_t *const qpms_interp_linear;
+extern const qpms_interp_type_t *const qpms_interp_cspline;
+
+typedef struct qpms_permittivity_interpolator_t qpms_permittivity_interpolator_t;  /* opaque */
+qpms_permittivity_interpolator_t *qpms_permittivity_interpolator_create(size_t incount,  /* materials.h:115-120 */
+    const double *wavelength_m, const double *n, const double *k, const qpms_interp_type_t *iptype);
+/* refractiveindex.info file, the "data: |" block of "wavelength_um n k" lines (materials.c:43-118) */
+int qpms_load_refractiveindex_yml(const char *path, size_t *count, double **lambdas_m, double **n, double **k);
+qpms_permittivity_interpolator_t *qpms_permittivity_interpolator_from_yml(const char *path,  /* materials.h:122-126 */
+    const qpms_interp_type_t *iptype);
+void qpms_permittivity_interpolator_free(qpms_permittivity_interpolator_t *interp);
+qpms_complex_t qpms_permittivity_interpolator_eps_at_omega(                               /* materials.h:128-131 */
+    const qpms_permittivity_interpolator_t *interp, double omega_SI);
+qpms_epsmu_t qpms_permittivity_interpolator_epsmu_g(qpms_complex_t omega, const void *interp);  /* materials.h:133-139 */
+double qpms_permittivity_interpolator_omega_min(const qpms_permittivity_interpolator_t *ip);
+double qpms_permittivity_interpolator_omega_max(const qpms_permittivity_interpolator_t *ip);
+
+/* VSWF sets and T-matrices (vswf.c:76-97, tmatrices.c:56-75) */
+qpms_vswf_set_spec_t *qpms_vswf_set_spec_from_lMax(qpms_l_t lMax, qpms_normalisation_t norm);
+void qpms_vswf_set_spec_free(qpms_vswf_set_spec_t *s);
+qpms_tmatrix_t *qpms_tmatrix_init(const qpms_vswf_set_spec_t *bspec);
+void qpms_tmatrix_free(qpms_tmatrix_t *t);
+
+typedef struct qpms_tmatrix_interpolator_t qpms_tmatrix_interpolator_t;  /* opaque; copies the basis */
+qpms_tmatrix_interpolator_t *qpms_tmatrix_interpolator_create(size_t n,                 /* tmatrices.h:318-323 */
+    const double *freqs, const qpms_tmatrix_t *tmatrices_array, const qpms_interp_type_t *iptype);
+void qpms_tmatrix_interpolator_free(qpms_tmatrix_interpolator_t *interp);
+int qpms_tmatrix_interpolator_eval_fill(qpms_tmatrix_t *target,                          /* tmatrices.h:307-309 */
+    const qpms_tmatrix_interpolator_t *interp, double freq);
+qpms_tmatrix_t *qpms_tmatrix_interpolator_eval(const qpms_tmatrix_interpolator_t *interp, double freq);
+int qpms_tmatrix_generator_interpolator(qpms_tmatrix_t *t, qpms_complex_t omega,         /* tmatrices.h:326-330 */
+    const void *interpolator);
+const qpms_vswf_set_spec_t *qpms_tmatrix_interpolator_bspec(const qpms_tmatrix_interpolator_t *interp);
+/* All elements of T(freqs[w]) for nf frequencies, out[w][n][n] row-major;
+ * DEVICE pointers, stream-ordered on `stream` (a cudaStream_t). */
+int qpms_gpu_tmatrix_interpolator_eval_batch(const qpms_tmatrix_interpolator_t *interp, size_t nf,
+    const double *d_freqs, qpms_complex_t *d_out, void *stream);
+/* SCUFF-EM T-matrix file (tmatrices.h:258-283, tmatrices.c:367-490): T-matrices
+ * in the basis bs, frequencies in rad/s (and in SCUFF units); the arrays are
+ * malloc'ed for the caller.  Returns QPMS_NAN_ENCOUNTERED if an element of the
+ * basis is missing for some frequency. */
+int qpms_load_scuff_tmatrix(const char *path, const qpms_vswf_set_spec_t *bs, size_t *n, double **freqs,
+    double **freqs_su, qpms_tmatrix_t **tmatrices_array, qpms_complex_t **tmdata);
+
+/* One particle kind of qpms_gpu_scatsys_create. */
+typedef struct qpms_gpu_particle_kind_t {
+  int type;             /* 0: sphere (Mie T-matrix), 1: tabulated T-matrix */
+  double radius;        /* sphere radius */
+  qpms_complex_t eps;   /* sphere: constant permittivity, used when neither ld nor eps_interp is set */
+  const qpms_ldparams_t *ld;                             /* sphere: Lorentz-Drude medium (copied) */
+  const qpms_permittivity_interpolator_t *eps_interp;    /* sphere: tabulated n, k (kept by reference) */
+  const qpms_tmatrix_interpolator_t *tmatrix;            /* type 1: T(omega) in the lMax basis of the system
+                                                             (kept by reference) */
+} qpms_gpu_particle_kind_t;
+
+/* General constructor: np particles at pos_xyz, kind[i] in [0, nkinds),
+ * constant medium, lMax basis (vswf.c:76-92); b1 = b2 = NULL for a finite
+ * system, else a 2D lattice.  With tabulated T-matrix kinds every T is dense
+ * (spheres included) and the system must be finite.  Interpolated quantities
+ * use Re omega (materials.c:131-142, tmatrices.c:351-356). */
+qpms_scatsys_t *qpms_gpu_scatsys_create(int np, const double *pos_xyz, const int *kind, int nkinds,
+    const qpms_gpu_particle_kind_t *kinds, qpms_complex_t eps_medium, qpms_l_t lMax,
+    const double *b1, const double *b2);
 
 /* Finite system of spheres with constant permittivities (Mie T-matrices,
  * tmatrices.c:580-606) in a constant medium; bspec from lMax (vswf.c:76-92).

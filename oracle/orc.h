@@ -108,6 +108,10 @@ int orc_finite_sphere_scatter(const orc_trans_calculator *c, int np, const doubl
 void orc_scattered_E(int lMax, int np, const double *pos, int J, double complex k, const double complex *cvf,
                      int npts, const double *where, double complex *E);
 
+/* ---- interpolation (orc_interp.c) ---- */
+/* kind 0 linear, 1 natural cubic spline; out[q] = S(xq[q]), NaN outside the knots */
+void orc_spline_eval(int kind, int n, const double *x, const double *y, int nq, const double *xq, double *out);
+
 /* ---- 2D Ewald sums and the lattice translation operator (orc_ewald.c) ---- */
 typedef struct orc_c2 { double x, y; } orc_c2;
 void orc_l2d_reduceBasis(orc_c2 b1, orc_c2 b2, orc_c2 *o1, orc_c2 *o2);

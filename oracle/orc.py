@@ -174,6 +174,8 @@ def _declare_scatsys(L):
     L.orc_lu_factor.argtypes = [sz, vp, vp]
     L.orc_lu_solve.restype = None
     L.orc_lu_solve.argtypes = [sz, vp, vp, vp, sz]
+    L.orc_spline_eval.restype = None
+    L.orc_spline_eval.argtypes = [ci, ci, vp, vp, ci, vp, vp]
     L.orc_scattered_E_ri.restype = None
     L.orc_scattered_E_ri.argtypes = [ci, ci, vp, ci, cd, cd, vp, ci, vp, vp]
 
@@ -219,6 +221,16 @@ def planewave_full(lMax, pos, k_cart, E_cart):
     out = np.empty(pos.shape[0] * 2 * lMax * (lMax + 2), dtype=np.complex128)
     lib().orc_planewave_full(lMax, pos.shape[0], pos.ctypes.data, kc.ctypes.data, Ec.ctypes.data,
                              out.ctypes.data)
+    return out
+
+
+def spline_eval(kind, x, y, xq):
+    """kind 0 linear, 1 natural cubic spline (the reference's gsl_interp_cspline)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    q = np.ascontiguousarray(np.atleast_1d(xq), dtype=np.float64)
+    out = np.empty(q.size)
+    lib().orc_spline_eval(int(kind), x.size, x.ctypes.data, y.ctypes.data, q.size, q.ctypes.data, out.ctypes.data)
     return out
 
 

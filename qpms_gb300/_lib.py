@@ -66,8 +66,9 @@ def _declare(L):
     # complex by value is passed as two doubles (same registers on x86-64 and aarch64)
     L.qpms_trans_calculator_get_AB_arrays_ext.restype = ci
     L.qpms_trans_calculator_get_AB_arrays_ext.argtypes = [vp, vp, vp, sz, sz, cd, cd, cd, cd, ci, ci]
-    from . import beyn, materials, scatsystem, serving
+    from . import beyn, materials, scatsystem, serving, tmatrices
     scatsystem.declare(L)
+    tmatrices.declare(L)
     beyn.declare(L)
     serving.declare(L)
     materials.declare(L)

@@ -28,6 +28,7 @@
 
 namespace qg {
 bool scatsys_is_own(const qpms_scatsys_t *ss);
+bool scatsys_dense(const qpms_scatsys_t *ss);
 void scatsys_tdiag(const qpms_scatsys_t *ss, int t, double om_re, double om_im, std::vector<qg_c> &out);
 qg_c scatsys_wavenumber(const qpms_scatsys_t *ss, double om_re, double om_im);
 int blas_handle_get(cublasHandle_t *h);
@@ -143,7 +144,7 @@ struct FiniteSource : MSource {
       T.insert(T.end(), d.begin(), d.end());
     }
     std::vector<qg_c> k(1, scatsys_wavenumber(ss, z.real(), z.imag()));
-    return assemble_modeproblem_device(ss, 1, T, false, k, QPMS_HANKEL_PLUS, stage, st);
+    return assemble_modeproblem_device(ss, 1, T, scatsys_dense(ss), k, QPMS_HANKEL_PLUS, stage, st);
   }
 };
 

@@ -18,6 +18,9 @@
 #include "qg_specfunc.cuh"
 
 namespace qg {
+std::complex<double> permittivity_interp_eps(const qpms_permittivity_interpolator_t *ip, double omega);  // qg_interp.cu
+void tmatrix_interp_eval(const qpms_tmatrix_interpolator_t *ip, double freq, qg_c *out);
+const qpms_vswf_set_spec_t *tmatrix_interp_spec(const qpms_tmatrix_interpolator_t *ip);
 namespace {
 
 typedef std::complex<double> cd;
@@ -146,8 +149,10 @@ void planewave_coeffs(int lMax, double theta, double phi, const cd Es[3], cd *el
 struct SphereKind {
   double radius;
   cd eps;                                 // constant permittivity, or
-  std::vector<qpms_ldparams_triple_t> ld;  // Lorentz-Drude oscillators (non-empty: used)
+  std::vector<qpms_ldparams_triple_t> ld;  // Lorentz-Drude oscillators (non-empty: used), or
   double ld_omega_p = 0;
+  const qpms_permittivity_interpolator_t *pint = nullptr;  // tabulated n, k (set: used)
+  const qpms_tmatrix_interpolator_t *tmi = nullptr;        // set: tabulated T(omega), not a sphere
 };
 
 // qpms_lorentzdrude_eps (materials.c:156-164): sum_j f_j wp^2 / (w_j^2 - w^2 - i w g_j).
@@ -159,6 +164,7 @@ cd lorentzdrude_eps(cd omega, double omega_p, const qpms_ldparams_triple_t *d, s
   return eps;
 }
 cd kind_eps(const SphereKind &k, cd omega) {
+  if (k.pint) return permittivity_interp_eps(k.pint, omega.real());  // Im omega discarded, materials.c:131-142
   return k.ld.empty() ? k.eps : lorentzdrude_eps(omega, k.ld_omega_p, k.ld.data(), k.ld.size());
 }
 
@@ -172,6 +178,7 @@ struct ScatsysPriv {
   cd eps_medium;
   qpms_epsmu_t medium_const;  // params of the constant-medium generator
   int lMax = 0;
+  bool dense = false;  // some kind has a tabulated (full) T-matrix: every T is passed dense
   // device copies
   double *d_pos = nullptr;
   int *d_tmid = nullptr;
@@ -302,14 +309,34 @@ void lattice_reduce(double *b1, double *b2) {
 
 void field_forget_system(const qpms_scatsys_t *ss);  // qg_field.cu
 
+// T-matrix of kind t at omega: the diagonal (n values) for a system of
+// spheres, the full row-major n x n matrix when the system is dense.
+void kind_tmat(const ScatsysPriv *s, int t, cd om, std::vector<qg_c> &out) {
+  const size_t n = s->spec.n;
+  const SphereKind &K = s->kinds[t];
+  if (K.tmi) {  // tabulated: tmatrices.c:351-356 uses Re omega
+    out.assign(n * n, cmk(0, 0));
+    tmatrix_interp_eval(K.tmi, om.real(), out.data());
+    return;
+  }
+  std::vector<cd> d;
+  sphere_tdiag(s, t, om, d);
+  if (!s->dense) {
+    out.resize(n);
+    for (size_t i = 0; i < n; ++i) out[i] = cmk(d[i].real(), d[i].imag());
+  } else {
+    out.assign(n * n, cmk(0, 0));
+    for (size_t i = 0; i < n; ++i) out[i * n + i] = cmk(d[i].real(), d[i].imag());
+  }
+}
+
 // Accessors used by qg_solve.cu.
 bool scatsys_is_own(const qpms_scatsys_t *ss) { return ss && ss->medium.function == epsmu_const_fn; }
 int scatsys_lmax(const qpms_scatsys_t *ss) { return sspriv(ss)->lMax; }
+bool scatsys_dense(const qpms_scatsys_t *ss) { return sspriv(ss)->dense; }
+// T of kind t at omega, diagonal or dense as scatsys_dense(ss) says.
 void scatsys_tdiag(const qpms_scatsys_t *ss, int t, double om_re, double om_im, std::vector<qg_c> &out) {
-  std::vector<cd> d;
-  sphere_tdiag(sspriv(ss), t, cd(om_re, om_im), d);
-  out.resize(d.size());
-  for (size_t i = 0; i < d.size(); ++i) out[i] = cmk(d[i].real(), d[i].imag());
+  kind_tmat(sspriv(ss), t, cd(om_re, om_im), out);
 }
 qg_c scatsys_wavenumber(const qpms_scatsys_t *ss, double om_re, double om_im) {
   const cd k = std::sqrt(sspriv(ss)->eps_medium) * cd(om_re, om_im) / kC0;
@@ -410,6 +437,58 @@ qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_ld(int np, const double *pos_xyz
     eps[t].im = eps_inside ? eps_inside[t].im : 0.0;
   }
   return create_spheres(np, pos_xyz, kind, nkinds, radius, eps.data(), eps_medium, lMax, b1, b2, ld_inside);
+}
+
+qpms_scatsys_t *qpms_gpu_scatsys_create(int np, const double *pos_xyz, const int *kind, int nkinds,
+                                        const qpms_gpu_particle_kind_t *kinds, qpms_complex_t eps_medium,
+                                        qpms_l_t lMax, const double *b1, const double *b2) {
+  clear_error();
+  if (!kinds || nkinds < 1) { set_error("no particle kinds"); return nullptr; }
+  if ((b1 == nullptr) != (b2 == nullptr)) { set_error("give both lattice vectors or neither"); return nullptr; }
+  std::vector<double> radius(nkinds);
+  std::vector<qpms_complex_t> eps(nkinds);
+  std::vector<const qpms_ldparams_t *> ld(nkinds, nullptr);
+  bool dense = false;
+  for (int t = 0; t < nkinds; ++t) {
+    const qpms_gpu_particle_kind_t &K = kinds[t];
+    if (K.type != 0 && K.type != 1) { set_error("kind %d: type must be 0 (sphere) or 1 (T-matrix)", t); return nullptr; }
+    radius[t] = K.type == 0 ? K.radius : 1.0;
+    eps[t] = K.eps;
+    ld[t] = K.type == 0 ? K.ld : nullptr;
+    if (K.type == 1) {
+      if (!K.tmatrix) { set_error("kind %d: NULL T-matrix interpolator", t); return nullptr; }
+      const qpms_vswf_set_spec_t *sp = tmatrix_interp_spec(K.tmatrix);
+      const int ne = lMax * (lMax + 2);
+      bool ok = sp->n == (size_t)(2 * ne) && sp->norm == QPMS_NORMALISATION_DEFAULT;
+      for (int it = 0, i = 0; ok && it < 2; ++it)
+        for (int l = 1; ok && l <= lMax; ++l)
+          for (int m = -l; ok && m <= l; ++m, ++i)
+            ok = sp->ilist[i] == (qpms_uvswfi_t)((it ? 1 : 2) + 4 * (qpms_uvswfi_t)(l * (l + 1) + m));
+      if (!ok) {
+        set_error("kind %d: the T-matrix basis must be the default lMax = %d basis (qpms_vswf_set_spec_from_lMax)",
+                  t, lMax);
+        return nullptr;
+      }
+      dense = true;
+    } else if (!(K.radius > 0)) {
+      set_error("kind %d: sphere radius must be positive", t);
+      return nullptr;
+    }
+  }
+  if (dense && b1) {
+    set_error("tabulated T-matrices: finite systems only (the lattice sums take diagonal T-matrices)");
+    return nullptr;
+  }
+  qpms_scatsys_t *ss = create_spheres(np, pos_xyz, kind, nkinds, radius.data(), eps.data(), eps_medium, lMax, b1,
+                                      b2, ld.data());
+  if (!ss) return nullptr;
+  ScatsysPriv *s = sspriv(ss);
+  for (int t = 0; t < nkinds; ++t) {
+    s->kinds[t].pint = kinds[t].type == 0 ? kinds[t].eps_interp : nullptr;
+    s->kinds[t].tmi = kinds[t].type == 1 ? kinds[t].tmatrix : nullptr;
+  }
+  s->dense = dense;
+  return ss;
 }
 
 qpms_complex_t qpms_lorentzdrude_eps(qpms_complex_t omega, const qpms_ldparams_t *p) {
@@ -538,10 +617,14 @@ qpms_scatsys_at_omega_t *qpms_gpu_scatsys_at_omega(const qpms_scatsys_t *ss, qpm
   w->tmp.resize(ss->tm_count);
   w->tdata.resize(ss->tm_count);
   for (int t = 0; t < ss->tm_count; ++t) {
-    std::vector<cd> d;
-    sphere_tdiag(s, t, om, d);
-    w->tdata[t].assign(n * n, cmk(0, 0));
-    for (size_t i = 0; i < n; ++i) w->tdata[t][i * n + i] = cmk(d[i].real(), d[i].imag());
+    std::vector<qg_c> d;
+    kind_tmat(s, t, om, d);
+    if (d.size() == n * n) {
+      w->tdata[t] = d;
+    } else {
+      w->tdata[t].assign(n * n, cmk(0, 0));
+      for (size_t i = 0; i < n; ++i) w->tdata[t][i * n + i] = d[i];
+    }
     w->tms[t].spec = &s->spec;
     w->tms[t].m = (qpms_complex_t *)w->tdata[t].data();
     w->tms[t].owns_m = false;

@@ -44,6 +44,7 @@
 namespace qg {
 bool scatsys_is_own(const qpms_scatsys_t *ss);
 int scatsys_lmax(const qpms_scatsys_t *ss);
+bool scatsys_dense(const qpms_scatsys_t *ss);
 void scatsys_tdiag(const qpms_scatsys_t *ss, int t, double om_re, double om_im, std::vector<qg_c> &out);
 qg_c scatsys_wavenumber(const qpms_scatsys_t *ss, double om_re, double om_im);
 void planewave_direction_coeffs(int lMax, const double k_dir[3], const qpms_complex_t E_cart[3],
@@ -300,7 +301,7 @@ struct qpms_gpu_server {
     QG_CUDA_TRY(cudaMemcpyAsync(dkv, kvec, 24, cudaMemcpyHostToDevice, st));
     if ((e = assemble(j->periodic, ss, 1, sd, dT, dk, &j->req, &k, dbeta, deta, derr, dM, st))) return e;
     if ((e = launch_incident(1, np, n, dcoef, dkv, sd.pos, da, st))) return e;
-    if ((e = launch_apply_t(1, np, n, ntm, 0, sd.tmid, dT, da, db, st))) return e;
+    if ((e = launch_apply_t(1, np, n, ntm, scatsys_dense(ss) ? 1 : 0, sd.tmid, dT, da, db, st))) return e;
     DenseSolver ds;
     double res = 0;
     int it = 0;
@@ -371,7 +372,7 @@ struct qpms_gpu_server {
     QG_CUDA_TRY(cudaMemcpyAsync(deta, eta.data(), nb * 8, cudaMemcpyHostToDevice, st));
     if ((e = assemble(periodic, ss, nb, sd, dT, dk, nullptr, nullptr, dbeta, deta, derr, dM, st))) return e;
     if ((e = launch_incident(nb, np, n, dcoef, dkv, sd.pos, da, st, (size_t)n))) return e;
-    if ((e = launch_apply_t(nb, np, n, ntm, 0, sd.tmid, dT, da, db, st))) return e;
+    if ((e = launch_apply_t(nb, np, n, ntm, scatsys_dense(ss) ? 1 : 0, sd.tmid, dT, da, db, st))) return e;
     std::vector<double> res(nb), sig(nb);
     std::vector<int> its(nb), info(nb);
     if ((e = batched_solve(h, st, nb, N, dM, db, dx, mode, kRefineTol, kMaxRefine, scratch, res.data(), its.data(),
@@ -442,7 +443,7 @@ struct qpms_gpu_server {
       a.nw = nb;
       a.np = ss->p_count;
       a.ntm = ss->tm_count;
-      a.dense = 0;
+      a.dense = scatsys_dense(ss) ? 1 : 0;
       a.J = QPMS_HANKEL_PLUS;
       a.pos = sd.pos;
       a.tmid = sd.tmid;

@@ -21,6 +21,7 @@
 namespace qg {
 bool scatsys_is_own(const qpms_scatsys_t *ss);
 int scatsys_lmax(const qpms_scatsys_t *ss);
+bool scatsys_dense(const qpms_scatsys_t *ss);
 void scatsys_tdiag(const qpms_scatsys_t *ss, int t, double om_re, double om_im, std::vector<qg_c> &out);
 qg_c scatsys_wavenumber(const qpms_scatsys_t *ss, double om_re, double om_im);
 void planewave_direction_coeffs(int lMax, const double k_dir[3], const qpms_complex_t E_cart[3],
@@ -93,13 +94,14 @@ int finite_scatter_dense(const qpms_scatsys_t *ss, int W, const std::vector<qg_c
   QG_CUDA_TRY(cudaMemcpy(dcoef.p, coef.data(), n * 16, cudaMemcpyHostToDevice));
   DenseSolver ds;
   if ((e = ds.init((int)N, 1, mode, 0x5eedbe11))) return e;
-  auto assemble = [&](int J, const qg_c *Tsrc) -> int {
-    QG_CUDA_TRY(cudaMemcpy(dT.p, Tsrc, tper * 16, cudaMemcpyHostToDevice));
+  const bool dense = scatsys_dense(ss);
+  auto assemble = [&](int J, const qg_c *Tsrc, size_t count, bool dn) -> int {
+    QG_CUDA_TRY(cudaMemcpy(dT.p, Tsrc, count * 16, cudaMemcpyHostToDevice));
     AsmArgs a;
     a.nw = 1;
     a.np = np;
     a.ntm = ntm;
-    a.dense = 0;
+    a.dense = dn ? 1 : 0;
     a.J = J;
     a.pos = dpos.as<double>();
     a.tmid = dtm.as<int>();
@@ -108,14 +110,15 @@ int finite_scatter_dense(const qpms_scatsys_t *ss, int W, const std::vector<qg_c
     a.M = dM.as<qg_c>();
     return launch_assemble(a, priv(ss->c)->dev, st);
   };
-  const std::vector<qg_c> mone(tper, cmk(-1.0, 0.0));
+  const std::vector<qg_c> mone((size_t)ntm * n, cmk(-1.0, 0.0));  // diagonal -1
   for (int w = 0; w < W; ++w) {
     QG_CUDA_TRY(cudaMemcpy(dk.p, &k[w], 16, cudaMemcpyHostToDevice));
     QG_CUDA_TRY(cudaMemcpy(dkv.p, &kvec[3 * w], 24, cudaMemcpyHostToDevice));
-    if ((e = assemble(3, T.data() + w * tper))) return e;  // row-major M = I - T S
+    if ((e = assemble(3, T.data() + w * tper, tper, dense))) return e;  // row-major M = I - T S
     if ((e = launch_incident(1, np, n, dcoef.as<qg_c>(), dkv.as<double>(), dpos.as<double>(), da.as<qg_c>(), st)))
       return e;
-    if ((e = launch_apply_t(1, np, n, ntm, 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(), db.as<qg_c>(), st)))
+    if ((e = launch_apply_t(1, np, n, ntm, dense ? 1 : 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(),
+                            db.as<qg_c>(), st)))
       return e;
     if ((e = ds.factorize(dM.p, N, st, true))) return e;
     double res = 0;
@@ -126,7 +129,7 @@ int finite_scatter_dense(const qpms_scatsys_t *ss, int W, const std::vector<qg_c
     if ((e = launch_sigma_ext(1, N, da.as<qg_c>(), dx.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), st))) return e;
     QG_CUDA_TRY(cudaMemcpy(sigma_ext + w, dsig.p, 8, cudaMemcpyDeviceToHost));
     if (sigma_scat) {
-      if ((e = assemble(1, mone.data()))) return e;  // I + R (regular waves, zero self blocks)
+      if ((e = assemble(1, mone.data(), mone.size(), false))) return e;  // I + R (regular waves, zero self blocks)
       QG_CUDA_TRY(cudaMemsetAsync(db.p, 0, N * 16, st));
       double *rn2 = dn.as<double>();
       if ((e = launch_residual(1, N, dM.as<qg_c>(), dx.as<qg_c>(), db.as<qg_c>(), dr.as<qg_c>(), rn2, rn2 + 1, st)))
@@ -387,7 +390,7 @@ int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw, c
     a.nw = W;
     a.np = np;
     a.ntm = ntm;
-    a.dense = 0;
+    a.dense = scatsys_dense(ss) ? 1 : 0;
     a.J = 3;
     a.pos = dpos.as<double>();
     a.tmid = dtm.as<int>();
@@ -398,7 +401,8 @@ int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw, c
   }
   if ((e = launch_incident(W, np, n, dcoef.as<qg_c>(), dkv.as<double>(), dpos.as<double>(), da.as<qg_c>(), st)))
     return e;
-  if ((e = launch_apply_t(W, np, n, ntm, 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(), db.as<qg_c>(), st)))
+  if ((e = launch_apply_t(W, np, n, ntm, scatsys_dense(ss) ? 1 : 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(),
+                          db.as<qg_c>(), st)))
     return e;
   double *rn2 = dn.as<double>(), *bn2 = rn2 + W;
   std::vector<double> hr(W), hb(W);
@@ -453,7 +457,7 @@ int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw, c
     // sigma_scat = Re(f^H (I + R) f) / k^2 with R the regular-wave translation
     // matrix, zero self blocks (misc/finiterectlat-scatter.py:98-111): the
     // assembly with J = 1 and T = -1 builds I + R in place of M
-    std::vector<qg_c> mone(T.size(), cmk(-1.0, 0.0));
+    std::vector<qg_c> mone((size_t)W * ntm * n, cmk(-1.0, 0.0));  // diagonal -1 (dT holds at least this)
     QG_CUDA_TRY(cudaMemcpy(dT.p, mone.data(), mone.size() * 16, cudaMemcpyHostToDevice));
     AsmArgs a;
     a.nw = W;

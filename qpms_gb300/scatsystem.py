@@ -23,6 +23,16 @@ class _SSW(C.Structure):
                 ("medium", C.c_double * 4), ("wavenumber", C.c_double * 2)]
 
 
+class _Cplx2(C.Structure):
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class _Kind(C.Structure):
+    """qpms_gpu_particle_kind_t"""
+    _fields_ = [("type", C.c_int), ("radius", C.c_double), ("eps", _Cplx2), ("ld", C.c_void_p),
+                ("eps_interp", C.c_void_p), ("tmatrix", C.c_void_p)]
+
+
 class _LU(C.Structure):
     _fields_ = [("ssw", C.c_void_p), ("sswk", C.c_void_p), ("full", C.c_bool), ("iri", C.c_int),
                 ("a", C.c_void_p), ("ipiv", C.c_void_p)]
@@ -56,6 +66,8 @@ def declare(L):
     vp, ci, cd, sz = C.c_void_p, C.c_int, C.c_double, C.c_size_t
     L.qpms_gpu_scatsys_create_spheres.restype = vp
     L.qpms_gpu_scatsys_create_spheres.argtypes = [ci, vp, vp, ci, vp, vp, cd, cd, ci]
+    L.qpms_gpu_scatsys_create.restype = vp
+    L.qpms_gpu_scatsys_create.argtypes = [ci, vp, vp, ci, vp, cd, cd, ci, vp, vp]
     L.qpms_gpu_scatsys_free.restype = None
     L.qpms_gpu_scatsys_free.argtypes = [vp]
     L.qpms_gpu_scatsys_at_omega.restype = vp
@@ -108,16 +120,39 @@ class ScatteringSystem:
     """Finite system of spheres; ``ss(omega)`` evaluates it at a frequency."""
 
     def __init__(self, positions, radius, eps_inside, eps_medium, lMax, kinds=None, lattice=None):
-        """lattice: None (finite system) or (b1, b2), 2D basis vectors in the xy plane."""
+        """lattice: None (finite system) or (b1, b2), 2D basis vectors in the xy plane.
+
+        eps_inside: one entry per particle kind (or a single one): a constant
+        permittivity, a ``materials.LorentzDrude`` model, a
+        ``materials.MaterialInterpolator`` (tabulated n, k) or a
+        ``tmatrices.TMatrixInterpolator`` (a tabulated T-matrix kind; its radius
+        entry is ignored).  kinds[i] selects the kind of particle i."""
         self._L = _lib.lib()
-        from .materials import LorentzDrude
+        from .materials import LorentzDrude, MaterialInterpolator
+        from .tmatrices import TMatrixInterpolator
         pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
-        radius = np.atleast_1d(np.asarray(radius, dtype=np.float64))
         eps_list = list(eps_inside) if isinstance(eps_inside, (list, tuple)) else [eps_inside]
-        models = [e if isinstance(e, LorentzDrude) else None for e in eps_list]
-        eps_in = np.ascontiguousarray([0 if m is not None else complex(e) for e, m in zip(eps_list, models)],
-                                      dtype=np.complex128)
-        self._models = models
+        nk = len(eps_list)
+        radius = np.broadcast_to(np.atleast_1d(np.asarray(radius, dtype=np.float64)), (nk,))
+        karr = (_Kind * nk)()
+        self._keep = []  # interpolators and models referenced by the system
+        for t, e in enumerate(eps_list):
+            K = karr[t]
+            K.radius = float(radius[t])
+            if isinstance(e, TMatrixInterpolator):
+                K.type = 1
+                K.tmatrix = e.ptr
+                self._keep.append(e)
+            elif isinstance(e, LorentzDrude):
+                K.ld = e.ptr
+                self._keep.append(e)
+            elif isinstance(e, MaterialInterpolator):
+                K.eps_interp = e.ptr
+                self._keep.append(e)
+            else:
+                c = complex(e)
+                K.eps = _Cplx2(c.real, c.imag)
+        self._models = [e if isinstance(e, LorentzDrude) else None for e in eps_list]
         if kinds is None:
             kinds = np.zeros(pos.shape[0], dtype=np.int32)
         kinds = np.ascontiguousarray(kinds, dtype=np.int32)
@@ -125,28 +160,16 @@ class ScatteringSystem:
         self.positions = pos
         self.lMax = int(lMax)
         self.lattice = lattice
-        if any(m is not None for m in models):
-            ptrs = (C.c_void_p * len(models))(*[m.ptr if m is not None else None for m in models])
-            b1 = b2 = None
-            if lattice is not None:
-                b1 = np.ascontiguousarray(lattice[0][:2], dtype=np.float64)
-                b2 = np.ascontiguousarray(lattice[1][:2], dtype=np.float64)
-            self.s = self._L.qpms_gpu_scatsys_create_spheres_ld(
-                pos.shape[0], pos.ctypes.data, kinds.ctypes.data, radius.size, radius.ctypes.data,
-                eps_in.ctypes.data, C.addressof(ptrs), em.real, em.imag, self.lMax,
-                b1.ctypes.data if b1 is not None else None, b2.ctypes.data if b2 is not None else None)
-        elif lattice is None:
-            self.s = self._L.qpms_gpu_scatsys_create_spheres(pos.shape[0], pos.ctypes.data, kinds.ctypes.data,
-                                                             radius.size, radius.ctypes.data, eps_in.ctypes.data,
-                                                             em.real, em.imag, self.lMax)
-        else:
+        self.eps_medium = em
+        b1 = b2 = None
+        if lattice is not None:
             b1 = np.ascontiguousarray(lattice[0][:2], dtype=np.float64)
             b2 = np.ascontiguousarray(lattice[1][:2], dtype=np.float64)
-            self.s = self._L.qpms_gpu_scatsys_create_spheres_2d(
-                pos.shape[0], pos.ctypes.data, kinds.ctypes.data, radius.size, radius.ctypes.data,
-                eps_in.ctypes.data, em.real, em.imag, self.lMax, b1.ctypes.data, b2.ctypes.data)
+        self.s = self._L.qpms_gpu_scatsys_create(
+            pos.shape[0], pos.ctypes.data, kinds.ctypes.data, nk, C.addressof(karr), em.real, em.imag, self.lMax,
+            b1.ctypes.data if b1 is not None else None, b2.ctypes.data if b2 is not None else None)
         if not self.s:
-            raise _lib.QpmsGpuError("qpms_gpu_scatsys_create_spheres: " + _lib.last_error())
+            raise _lib.QpmsGpuError("qpms_gpu_scatsys_create: " + _lib.last_error())
         self.fecv_size = pos.shape[0] * 2 * self.lMax * (self.lMax + 2)
 
     def __del__(self):
