@@ -360,7 +360,7 @@ typedef struct qpms_gpu_particle_kind_t {
 /* General constructor: np particles at pos_xyz, kind[i] in [0, nkinds),
  * constant medium, lMax basis (vswf.c:76-92); b1 = b2 = NULL for a finite
  * system, else a 2D lattice.  With tabulated T-matrix kinds every T is dense
- * (spheres included) and the system must be finite.  Interpolated quantities
+ * (spheres included).  Interpolated quantities
  * use Re omega (materials.c:131-142, tmatrices.c:351-356). */
 qpms_scatsys_t *qpms_gpu_scatsys_create(int np, const double *pos_xyz, const int *kind, int nkinds,
     const qpms_gpu_particle_kind_t *kinds, qpms_complex_t eps_medium, qpms_l_t lMax,

@@ -25,6 +25,7 @@ qg_c scatsys_wavenumber(const qpms_scatsys_t *ss, double om_re, double om_im);
 void planewave_direction_coeffs(int lMax, const double k_dir[3], const qpms_complex_t E_cart[3],
                                 std::vector<qg_c> &coef);
 int blas_handle_get(cublasHandle_t *h);
+bool scatsys_dense(const qpms_scatsys_t *ss);
 
 namespace {
 
@@ -137,6 +138,96 @@ int ewald_assemble_locked(const qpms_scatsys_t *ss, const EwaldArgs &a, cudaStre
   return QPMS_SUCCESS;
 }
 
+namespace {
+// Pointer arrays of the batched GEMM C_R = -T_R X_R (one entry per (matrix,
+// particle)): X_R,: is rows [R n, R n + n) of the row-major N x N matrix X,
+// i.e. the column-major N x n matrix X_R^T (ld N); T_R row-major is the
+// column-major T_R^T (ld n); C_R^T = X_R^T T_R^T.
+__global__ void dense_t_ptrs_kernel(int nmat, int np, int n, int N, int ntm, int nk, int paired,
+                                    const int *__restrict__ tmid, const qg_c *X, const qg_c *T, qg_c *M,
+                                    const void **pa, const void **pb, void **pc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nmat * np) return;
+  const int m = i / np, R = i % np, w = paired ? m : m / nk;
+  const size_t off = (size_t)m * N * N + (size_t)R * n * N;
+  pa[i] = X + off;
+  pb[i] = T + ((size_t)w * ntm + tmid[R]) * n * n;
+  pc[i] = M + off;
+}
+
+// M (already -T_R X_R,:) += I + T_R on the diagonal blocks.
+__global__ void dense_t_diag_kernel(int nmat, int np, int n, int N, int ntm, int nk, int paired,
+                                    const int *__restrict__ tmid, const qg_c *__restrict__ T, qg_c *M) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t nn = (size_t)n * n;
+  if (i >= (size_t)nmat * np * nn) return;
+  const int m = (int)(i / ((size_t)np * nn));
+  const int R = (int)((i / nn) % np);
+  const int a = (int)((i % nn) / n), b = (int)(i % n);
+  const int w = paired ? m : m / nk;
+  qg_c t = T[((size_t)w * ntm + tmid[R]) * nn + (size_t)a * n + b];
+  if (a == b) t.re += 1.0;
+  qg_c &o = M[(size_t)m * N * N + (size_t)(R * n + a) * N + R * n + b];
+  o = cadd(o, t);
+}
+}  // namespace
+
+// The lattice assembly for dense T-matrices (a.T: [nw][ntm][n][n] row-major):
+// the Ewald kernel scales rows by a diagonal T, so it builds X = I + W with
+// T = -1 first; then M_R,: = (I + T_R) delta_R,: - T_R X_R,: by one batched
+// complex GEMM per (matrix, particle) block row and a diagonal-block kernel.
+int ewald_assemble_dense(const qpms_scatsys_t *ss, const EwaldArgs &a, int n, cudaStream_t st) {
+  const int np = a.np, N = np * n;
+  const int nmat = a.paired ? a.nw : a.nw * a.nk;
+  const size_t NN = (size_t)N * N, nb = (size_t)nmat * np;
+  void *buf = nullptr;
+  const size_t bx = (size_t)nmat * NN * 16, bm = ((size_t)a.nw * a.ntm * n * 16 + 255) / 256 * 256,
+               bp = 3 * nb * sizeof(void *);
+  QG_CUDA_TRY(cudaMallocAsync(&buf, bx + bm + bp, st));
+  qg_c *X = (qg_c *)buf;
+  qg_c *Tm1 = (qg_c *)((char *)buf + bx);
+  void **ptrs = (void **)((char *)buf + bx + bm);
+  int e = QPMS_SUCCESS;
+  {
+    std::vector<qg_c> m1((size_t)a.nw * a.ntm * n, cmk(-1.0, 0.0));
+    cudaError_t ce = cudaMemcpyAsync(Tm1, m1.data(), m1.size() * 16, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);  // m1 is a local buffer
+    if (ce != cudaSuccess) {
+      cudaFreeAsync(buf, st);
+      QG_CUDA_TRY(ce);
+    }
+  }
+  EwaldArgs ax = a;
+  ax.T = Tm1;
+  ax.M = X;
+  e = ewald_assemble_locked(ss, ax, st);
+  cublasHandle_t h;
+  if (!e) e = blas_handle_get(&h);
+  if (!e) {
+    dense_t_ptrs_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(
+        nmat, np, n, N, a.ntm, a.nk, a.paired, a.tmid, X, a.T, a.M, (const void **)ptrs, (const void **)(ptrs + nb),
+        ptrs + 2 * nb);
+    g_launches.fetch_add(1);
+    const cuDoubleComplex mone = make_cuDoubleComplex(-1, 0), zero = make_cuDoubleComplex(0, 0);
+    if (cudaGetLastError() != cudaSuccess || cublasSetStream(h, st) != CUBLAS_STATUS_SUCCESS ||
+        cublasZgemmBatched(h, CUBLAS_OP_N, CUBLAS_OP_N, N, n, n, &mone, (const cuDoubleComplex **)ptrs, N,
+                           (const cuDoubleComplex **)(ptrs + nb), n, &zero, (cuDoubleComplex **)(ptrs + 2 * nb), N,
+                           (int)nb) != CUBLAS_STATUS_SUCCESS) {
+      set_error("dense T: batched GEMM failed");
+      e = QPMS_ERROR;
+    } else {
+      g_launches.fetch_add(1);
+      const size_t tot = nb * n * n;
+      dense_t_diag_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(nmat, np, n, N, a.ntm, a.nk, a.paired,
+                                                                         a.tmid, a.T, a.M);
+      g_launches.fetch_add(1);
+      if (cudaGetLastError() != cudaSuccess) { set_error("dense T: diagonal-block kernel failed"); e = QPMS_ERROR; }
+    }
+  }
+  cudaFreeAsync(buf, st);
+  return e;
+}
+
 // Batched periodic assembly into device memory: nw frequencies x nk Bloch vectors.
 int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_host,
                                     const std::vector<qg_c> &T_host, int nk, const double *beta_host,
@@ -185,6 +276,8 @@ int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_hos
   a.eta = deta.as<double>();
   a.M = dM;
   a.err = derr.as<int>();
+  const int n = (int)(ss->fecv_size / np);
+  if (T_host.size() == (size_t)nw * ss->tm_count * n * n && n > 1) return ewald_assemble_dense(ss, a, n, st);
   return ewald_assemble_locked(ss, a, st);
 }
 
@@ -216,13 +309,17 @@ qpms_complex_t *qpms_scatsyswk_build_modeproblem_matrix_full(qpms_complex_t *tar
   if (sswk->k[2] != 0) { set_error("Bloch vector must lie in the xy plane"); return nullptr; }
   const size_t N = ss->fecv_size, n = ssw->tm[0]->spec->n;
   std::vector<qg_c> T;
+  bool diag = true;
+  for (int t = 0; t < ss->tm_count; ++t)
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = 0; j < n; ++j)
+        if (i != j && (ssw->tm[t]->m[i * n + j].re != 0 || ssw->tm[t]->m[i * n + j].im != 0)) diag = false;
   for (int t = 0; t < ss->tm_count; ++t)
     for (size_t i = 0; i < n; ++i) {
-      for (size_t j = 0; j < n; ++j)
-        if (i != j && (ssw->tm[t]->m[i * n + j].re != 0 || ssw->tm[t]->m[i * n + j].im != 0)) {
-          set_error("periodic assembly supports diagonal T-matrices");
-          return nullptr;
-        }
+      if (!diag) {  // dense T-matrices: the GEMM path of the lattice assembly
+        for (size_t j = 0; j < n; ++j) T.push_back(*(const qg_c *)&ssw->tm[t]->m[i * n + j]);
+        continue;
+      }
       T.push_back(*(const qg_c *)&ssw->tm[t]->m[i * n + i]);
     }
   const qg_c k = *(const qg_c *)&ssw->wavenumber;
@@ -289,7 +386,8 @@ int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *om
       (e = dalloc(dlog, nmat * 8)) || (e = dalloc(dtm, np * 4)) || (e = dalloc(dpos, np * 24)) ||
       (e = dalloc(da, nmat * N * 16)) || (e = dalloc(db, nmat * N * 16)) || (e = dalloc(dx, nmat * N * 16)) ||
       (e = dalloc(dsig, nmat * 8)) || (e = dalloc(dk, nmat * 16)) || (e = dalloc(dkv, nmat * 24)) ||
-      (e = dalloc(dT, nmat * ntm * n * 16)) || (e = dalloc(dcf, nmat * n * 16)))
+      (e = dalloc(dT, nmat * ntm * (scatsys_dense(ss) ? (size_t)n * n : n) * 16)) ||
+      (e = dalloc(dcf, nmat * n * 16)))
     return e;
   QG_CUDA_TRY(cudaMemcpy(dtm.p, tm.data(), np * 4, cudaMemcpyHostToDevice));
   QG_CUDA_TRY(cudaMemcpy(dpos.p, pos.data(), np * 24, cudaMemcpyHostToDevice));
@@ -331,8 +429,9 @@ int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *om
         const bool prop = kap * kap > b2;
         for (int i = 0; i < n; ++i) coefs[m * n + i] = prop ? cf[i] : cmk(0, 0);
         for (int c = 0; c < 3; ++c) kvec[3 * m + c] = kd[c];
-        for (int t = 0; t < ntm; ++t) Tm.insert(Tm.end(), T.begin() + ((size_t)w * ntm + t) * n,
-                                                T.begin() + ((size_t)w * ntm + t + 1) * n);
+        const size_t tsz = scatsys_dense(ss) ? (size_t)n * n : (size_t)n;
+        for (int t = 0; t < ntm; ++t) Tm.insert(Tm.end(), T.begin() + ((size_t)w * ntm + t) * tsz,
+                                                T.begin() + ((size_t)w * ntm + t + 1) * tsz);
       }
     }
     if ((e = periodic_assemble_device(ss, W, k.data(), T, (int)nk, kvecs, eta.data(), dM.as<qg_c>(), 0))) return e;
@@ -344,7 +443,8 @@ int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *om
     if ((e = launch_incident((int)nm, np, n, dcf.as<qg_c>(), dkv.as<double>(), dpos.as<double>(), da.as<qg_c>(), 0,
                              (size_t)n)))
       return e;
-    if ((e = launch_apply_t((int)nm, np, n, ntm, 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(), db.as<qg_c>(), 0)))
+    if ((e = launch_apply_t((int)nm, np, n, ntm, scatsys_dense(ss) ? 1 : 0, dtm.as<int>(), dT.as<qg_c>(),
+                            da.as<qg_c>(), db.as<qg_c>(), 0)))
       return e;
     // LU (complex128, or complex64 + FP64 refinement), log|det| from the factors
     if ((e = batched_solve(h, 0, (int)nm, N, dM.as<qg_c>(), db.as<qg_c>(), dx.as<qg_c>(), mode, 1e-13, 12, dscr.p,

@@ -475,10 +475,6 @@ qpms_scatsys_t *qpms_gpu_scatsys_create(int np, const double *pos_xyz, const int
       return nullptr;
     }
   }
-  if (dense && b1) {
-    set_error("tabulated T-matrices: finite systems only (the lattice sums take diagonal T-matrices)");
-    return nullptr;
-  }
   qpms_scatsys_t *ss = create_spheres(np, pos_xyz, kind, nkinds, radius.data(), eps.data(), eps_medium, lMax, b1,
                                       b2, ld.data());
   if (!ss) return nullptr;

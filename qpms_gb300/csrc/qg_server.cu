@@ -51,6 +51,7 @@ void planewave_direction_coeffs(int lMax, const double k_dir[3], const qpms_comp
                                 std::vector<qg_c> &coef);
 int blas_handle_get(cublasHandle_t *h);
 int ewald_assemble_locked(const qpms_scatsys_t *ss, const EwaldArgs &a, cudaStream_t st);
+int ewald_assemble_dense(const qpms_scatsys_t *ss, const EwaldArgs &a, int n, cudaStream_t st);
 }  // namespace qg
 
 using namespace qg;
@@ -476,6 +477,7 @@ struct qpms_gpu_server {
     a.eta = deta;
     a.M = dM;
     a.err = derr;
+    if (scatsys_dense(ss)) return ewald_assemble_dense(ss, a, (int)(ss->fecv_size / ss->p_count), st);
     return ewald_assemble_locked(ss, a, st);
   }
 };

@@ -176,7 +176,6 @@ def test_server_and_errors(gpu, orc):
     from qpms_gb300 import QpmsGpuError
     from qpms_gb300.serving import Server
     from qpms_gb300.tmatrices import TMatrixInterpolator
-    from qpms_gb300.workloads import square_lattice
     lMax = 2
     fr, T = _table(orc, lMax, 50e-9, offdiag=0.05, seed=7)
     ti = TMatrixInterpolator.from_arrays(fr, T, lMax)
@@ -189,8 +188,53 @@ def test_server_and_errors(gpu, orc):
     srv.close()
     assert r["status"] == 0
     assert np.linalg.norm(r["f"] - ref) <= 1e-9 * np.linalg.norm(ref)
-    b1, b2, p1 = square_lattice()
-    with pytest.raises(QpmsGpuError):
-        gpu.ScatteringSystem(p1, 80e-9, [ti], EPS_E, lMax, lattice=(b1, b2))
     with pytest.raises(QpmsGpuError):  # basis of another lMax
         gpu.ScatteringSystem(pos, 50e-9, [ti], EPS_E, 3)
+
+
+def _lattice_oracle(orc, lMax, pos, Tp, w, b1, b2, kxy):
+    """Oracle M = I - T W(k) and the plane-wave solve with the incidence of
+    the library's lattice paths (in-plane wavevector k, E = x projected
+    perpendicular to the propagation direction)."""
+    calc = orc.TransCalculator(lMax)
+    k = np.sqrt(EPS_E) * w / C0
+    kv = np.array([kxy[0], kxy[1], 0.0])
+    eta = orc.adjusted_eta(abs(b1[0] * b2[1] - b1[1] * b2[0]), k, kv, lMax)
+    M = orc.periodic_modeproblem(calc, pos, Tp, k, b1, b2, kv, eta)
+    kd = np.array([kv[0], kv[1], np.sqrt(k.real ** 2 - kv[0] ** 2 - kv[1] ** 2)])
+    E = np.array([1.0, 0, 0]) - kd[0] * kd / (kd @ kd)
+    a = orc.planewave_full(lMax, pos, kd, E / np.linalg.norm(E))
+    n = Tp.shape[1]
+    rhs = (Tp @ a.reshape(pos.shape[0], n, 1)).reshape(-1)
+    return M, np.linalg.solve(M, rhs)
+
+
+def test_tabulated_kinds_in_a_lattice(gpu, orc):
+    """Dense T in the lattice sums: X = I + W from the Ewald kernel with T = -1,
+    then M = I + T - T X by a batched GEMM; the matrix (reference-layout
+    path), the dispersion scan and a serving request against the oracle."""
+    from qpms_gb300.serving import Server
+    from qpms_gb300.tmatrices import TMatrixInterpolator
+    from qpms_gb300.workloads import honeycomb_lattice
+    lMax = 2
+    fr, T = _table(orc, lMax, 80e-9, offdiag=0.05, seed=11)
+    ti = TMatrixInterpolator.from_arrays(fr, T, lMax)
+    b1, b2, pos = honeycomb_lattice()
+    ss = gpu.ScatteringSystem(pos, 80e-9, [EPS_I, ti], EPS_E, lMax, kinds=[0, 1], lattice=(b1, b2))
+    w = 2.15 * EV / HBAR
+    kxy = (0.11 * np.pi / 580e-9, -0.07 * np.pi / 580e-9)
+    Tw = _oracle_T(orc, fr, T, w)
+    Ts = np.diag(orc.tmatrix_sphere_diag(lMax, 80e-9, w, EPS_I, EPS_E))
+    Tp = np.stack([Ts, Tw])
+    Mo, fo = _lattice_oracle(orc, lMax, pos, Tp, w, b1, b2, kxy)
+    M = ss(w).modeproblem_matrix_full(k=kxy)
+    assert np.linalg.norm(M - Mo) <= 1e-10 * np.linalg.norm(Mo)
+    for mode in (0, 1):
+        r = ss.dispersion_scan(np.array([w]), np.array([kxy]), want_f=True, mode=mode)
+        assert r["residual"][0, 0] <= 1e-12
+        assert np.linalg.norm(r["f"][0, 0] - fo) <= 1e-9 * np.linalg.norm(fo)
+    srv = Server(mode=1, workers=2)
+    res = srv.wait(srv.submit(ss, w, kxy))
+    srv.close()
+    assert res["status"] == 0
+    assert np.linalg.norm(res["f"] - fo) <= 1e-9 * np.linalg.norm(fo)
