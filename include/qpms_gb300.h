@@ -507,6 +507,15 @@ ccart3_t qpms_scatsys_scattered_E__alt(const qpms_scatsys_t *ss, qpms_bessel_t b
     qpms_complex_t wavenumber, const qpms_complex_t *cvf, cart3_t where);
 ccart3_t qpms_scatsysw_scattered_E__alt(const qpms_scatsys_at_omega_t *ssw,
     qpms_bessel_t btyp, const qpms_complex_t *cvf, cart3_t where);
+/* 2D-periodic system (scatsystem.c:2114-2188): the field of the lattice of
+ * particles with Bloch vector sswk->k at points in the particles' plane,
+ * btyp 3 only (as in the reference); sswk->eta = 0 selects
+ * qpms_ss_adjusted_eta.  Points off that plane need the shifted-layer lattice
+ * sums and are refused. */
+ccart3_t qpms_scatsyswk_scattered_E(const qpms_scatsys_at_omega_k_t *sswk, qpms_bessel_t btyp,
+    const qpms_complex_t *cvf, cart3_t where);
+int qpms_gpu_scatsyswk_scattered_E(const qpms_scatsys_at_omega_k_t *sswk, qpms_bessel_t btyp,
+    const qpms_complex_t *cvf, size_t npoints, const double *where_xyz, qpms_complex_t *E_xyz);
 /* Batched over points, HOST buffers (the loop of qpms_c.pyx:904-927 in one
  * call): where_xyz [npoints][3], E_xyz [npoints][3] complex. */
 int qpms_gpu_scatsys_scattered_E(const qpms_scatsys_t *ss, qpms_bessel_t btyp,

@@ -125,13 +125,15 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
   __shared__ qg_c red[kEThreads / 32][NEV];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int np = a.np;
-  const size_t units = (size_t)a.nw * a.nk * np * np;
+  const size_t per = a.npairs ? (size_t)a.npairs : (size_t)np * np;  // blocks per matrix
+  const size_t units = (size_t)a.nw * a.nk * per;
   const size_t N = (size_t)np * NB;
   for (size_t u = blockIdx.x; u < units; u += gridDim.x) {
-    const int pr = (int)(u % (size_t)(np * np));
-    const size_t wk = u / (size_t)(np * np);
+    const int pr = (int)(u % per);
+    const size_t wk = u / per;
     const int iw = (int)(wk / a.nk), ik = a.paired ? iw : (int)(wk % a.nk);
-    const int R = pr / np, C = pr - R * np;
+    const int R = a.npairs ? a.pairs[2 * pr] : pr / np;
+    const int C = a.npairs ? a.pairs[2 * pr + 1] : pr - R * np;
     const qg_c k = a.k[iw];
     const double eta = a.eta[wk];
     const double bx = a.beta[2 * ik], by = a.beta[2 * ik + 1];
@@ -347,8 +349,10 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
     }
     __syncthreads();
     // ---------------- contraction into the M block ----------------
-    qg_c *M = a.M + wk * N * N;
-    const size_t row0 = (size_t)R * NB, col0 = (size_t)C * NB;
+    // full matrix: block (R, C) of the N x N matrix wk; pair list: block pr alone (ld NB)
+    qg_c *M = a.npairs ? a.M + (wk * per + pr) * NB * NB : a.M + wk * N * N;
+    const size_t ldm = a.npairs ? (size_t)NB : N;
+    const size_t row0 = a.npairs ? 0 : (size_t)R * NB, col0 = a.npairs ? 0 : (size_t)C * NB;
     const qg_c *TR = a.T + ((size_t)iw * a.ntm + a.tmid[R]) * NB;
 #pragma unroll 1
     for (int which = 0; which < 2; ++which) {
@@ -371,8 +375,8 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
         const int r1 = yi, c1 = which ? NE + yj : yj;
         const int r2 = NE + yi, c2 = which ? yj : NE + yj;
         const qg_c m1 = cscale(cmul(TR[r1], v), -1.0), m2 = cscale(cmul(TR[r2], v), -1.0);
-        M[(row0 + r1) * N + col0 + c1] = (R == C && r1 == c1) ? cadd(m1, cmk(1, 0)) : m1;
-        M[(row0 + r2) * N + col0 + c2] = (R == C && r2 == c2) ? cadd(m2, cmk(1, 0)) : m2;
+        M[(row0 + r1) * ldm + col0 + c1] = (R == C && r1 == c1) ? cadd(m1, cmk(1, 0)) : m1;
+        M[(row0 + r2) * ldm + col0 + c2] = (R == C && r2 == c2) ? cadd(m2, cmk(1, 0)) : m2;
       }
     }
     __syncthreads();
@@ -381,7 +385,7 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
 
 template <int LMAX>
 int launch_ew(const EwaldArgs &a, const TransDevTables &T, cudaStream_t st) {
-  const size_t units = (size_t)a.nw * a.nk * a.np * a.np;
+  const size_t units = (size_t)a.nw * a.nk * (a.npairs ? (size_t)a.npairs : (size_t)a.np * a.np);
   if (!units) return QPMS_SUCCESS;
   int dev = 0, nsm = 0;
   QG_CUDA_TRY(cudaGetDevice(&dev));

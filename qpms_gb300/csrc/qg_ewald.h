@@ -35,6 +35,11 @@ struct EwaldArgs {
   qg_c *M;             // [nw * nk][N][N]
   int *err;            // set to 1 if a unit's lattice-point range exceeded the bound
   int paired = 0;      // 1: nk == 1 and matrix w uses Bloch vector beta[w] (a list of (omega, k) pairs)
+  // Optional list of particle pairs (R, C): only those blocks are formed,
+  // block p of matrix wk at M + (wk * npairs + p) * NB * NB (row-major NB x NB)
+  // instead of the full N x N matrices.
+  int npairs = 0;
+  const int *pairs = nullptr;  // [npairs][2]
 };
 
 // Bound on the lattice points one unit may enumerate per sum.

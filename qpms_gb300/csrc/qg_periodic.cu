@@ -285,6 +285,145 @@ int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_hos
 
 using namespace qg;
 
+namespace qg {
+namespace {
+// Field of a 2D-periodic array at in-plane points from the lattice-summed
+// blocks W(point <- particle) (pair-list Ewald assembly with T = -1, so a
+// block is W itself): a = sum_p W_qp f_p, of which only the electric l = 1
+// regular waves are non-zero at the point itself; E = sum_m a_(N,1,m) D_m with
+// D_m the cartesian value of the regular electric dipole wave at r = 0.
+// One block per point, deterministic reduction order.
+__global__ void periodic_field_kernel(int npts, int np, int n, const qg_c *__restrict__ W,
+                                      const qg_c *__restrict__ f, const qg_c *__restrict__ D,
+                                      qg_c *__restrict__ E) {
+  const int q = blockIdx.x;
+  if (q >= npts) return;
+  __shared__ qg_c red[3][128];
+  qg_c acc[3] = {cmk(0, 0), cmk(0, 0), cmk(0, 0)};
+  const int tot = np * n;
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+    const int p = t / n, c = t - p * n;
+    const qg_c fc = f[(size_t)p * n + c];
+    const qg_c *Wb = W + ((size_t)q * np + p) * n * n;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) acc[j] = cadd(acc[j], cmul(Wb[(size_t)j * n + c], fc));
+  }
+  for (int j = 0; j < 3; ++j) red[j][threadIdx.x] = acc[j];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+      for (int j = 0; j < 3; ++j) red[j][threadIdx.x] = cadd(red[j][threadIdx.x], red[j][threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) {
+    const int x = threadIdx.x;
+    qg_c e = cmk(0, 0);
+    for (int j = 0; j < 3; ++j) e = cadd(e, cmul(red[j][0], D[3 * j + x]));
+    E[(size_t)q * 3 + x] = e;
+  }
+}
+}  // namespace
+
+// Regular electric dipole waves N_(1,m), m = -1, 0, 1, at r = 0 in cartesian
+// components, default normalisation (qpms_vswf_fill_csph at kr = 0: besfac
+// 1/3, besderfac 2/3, evaluated at theta = pi/2, phi = 0 as
+// scatsystem.c:2118-2124 does): D[3 m' + x].
+void regular_dipoles_at_origin(qg_c *D) {
+  const double leg1 = -sqrt(3.0 / (16 * M_PI));          // leg(1, 1) = pi(1, +-1)
+  const double tau0 = -sqrt(3.0 / (4 * M_PI)) / sqrt(2.0);  // tau(1, 0)
+  // (r, theta, phi) components -> cartesian at theta = pi/2, phi = 0: x = r, y = phi, z = -theta
+  const qg_c Nm1[3] = {cmk(-2.0 / 3 * leg1, 0), cmk(0, 2.0 / 3 * leg1), cmk(0, 0)};
+  const qg_c N0[3] = {cmk(0, 0), cmk(0, 0), cmk(-2.0 / 3 * tau0, 0)};
+  const qg_c Np1[3] = {cmk(2.0 / 3 * leg1, 0), cmk(0, 2.0 / 3 * leg1), cmk(0, 0)};
+  for (int x = 0; x < 3; ++x) {
+    D[x] = Nm1[x];
+    D[3 + x] = N0[x];
+    D[6 + x] = Np1[x];
+  }
+}
+
+// E at npts in-plane points (host where / E), lattice sums at (k, beta, eta).
+int periodic_field(const qpms_scatsys_t *ss, qg_c k, const double beta[2], double eta, const qg_c *cvf_host,
+                   size_t npts, const double *where, qg_c *E_host) {
+  const int np = ss->p_count;
+  const int n = (int)(ss->fecv_size / np);
+  const double z0 = ss->p[0].pos.z;
+  for (int i = 0; i < np; ++i)
+    if (ss->p[i].pos.z != z0) { set_error("particles must share one z plane"); return QPMS_EINVAL; }
+  for (size_t q = 0; q < npts; ++q)
+    if (where[3 * q + 2] != z0) {
+      set_error("periodic field: points must lie in the particles' plane z = %g (off-plane points need the "
+                "shifted-layer lattice sums)", z0);
+      return QPMS_EINVAL;
+    }
+  if (!(eta >= 0.05 * ss->per.eta && eta <= 50 * ss->per.eta)) {
+    set_error("Ewald eta %g outside [0.05, 50] x the lattice default %g", eta, ss->per.eta);
+    return QPMS_EINVAL;
+  }
+  if (npts == 0) return QPMS_SUCCESS;
+  // points per chunk: the W blocks of a chunk stay below 256 MiB
+  const size_t per_pt = (size_t)np * n * n * 16;
+  const size_t chunk = std::max<size_t>(1, std::min<size_t>(npts, ((size_t)256 << 20) / per_pt));
+  qg_c D[9];
+  regular_dipoles_at_origin(D);
+  std::vector<qg_c> Tm1(n, cmk(-1.0, 0.0));
+  Dev dpos, dtm, dT, dk, dbeta, deta, derr, dpairs, dW, df, dD, dE;
+  int e;
+  if ((e = dalloc(dpos, (np + chunk) * 24)) || (e = dalloc(dtm, (np + chunk) * 4)) || (e = dalloc(dT, n * 16)) ||
+      (e = dalloc(dk, 16)) || (e = dalloc(dbeta, 16)) || (e = dalloc(deta, 8)) || (e = dalloc(derr, 4)) ||
+      (e = dalloc(dpairs, chunk * np * 8)) || (e = dalloc(dW, chunk * per_pt)) ||
+      (e = dalloc(df, ss->fecv_size * 16)) || (e = dalloc(dD, 9 * 16)) || (e = dalloc(dE, chunk * 48)))
+    return e;
+  std::vector<int> tm(np + chunk, 0), pairs(2 * chunk * np);
+  QG_CUDA_TRY(cudaMemcpy(dtm.p, tm.data(), tm.size() * 4, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpy(dT.p, Tm1.data(), n * 16, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpy(dk.p, &k, 16, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpy(dbeta.p, beta, 16, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpy(deta.p, &eta, 8, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpy(df.p, cvf_host, ss->fecv_size * 16, cudaMemcpyHostToDevice));
+  QG_CUDA_TRY(cudaMemcpy(dD.p, D, 9 * 16, cudaMemcpyHostToDevice));
+  std::vector<double> pos(3 * (np + chunk));
+  for (int i = 0; i < np; ++i) {
+    pos[3 * i] = ss->p[i].pos.x;
+    pos[3 * i + 1] = ss->p[i].pos.y;
+    pos[3 * i + 2] = ss->p[i].pos.z;
+  }
+  for (size_t q0 = 0; q0 < npts; q0 += chunk) {
+    const size_t m = std::min(chunk, npts - q0);
+    memcpy(&pos[3 * np], where + 3 * q0, m * 24);
+    for (size_t q = 0; q < m; ++q)
+      for (int p = 0; p < np; ++p) {
+        pairs[2 * (q * np + p)] = (int)(np + q);  // destination: the point
+        pairs[2 * (q * np + p) + 1] = p;          // source: particle p
+      }
+    QG_CUDA_TRY(cudaMemcpy(dpos.p, pos.data(), (np + m) * 24, cudaMemcpyHostToDevice));
+    QG_CUDA_TRY(cudaMemcpy(dpairs.p, pairs.data(), m * np * 8, cudaMemcpyHostToDevice));
+    EwaldArgs a;
+    a.nw = 1;
+    a.nk = 1;
+    a.np = (int)(np + m);
+    a.ntm = 1;
+    a.pos = dpos.as<double>();
+    a.tmid = dtm.as<int>();
+    a.T = dT.as<qg_c>();
+    a.k = dk.as<qg_c>();
+    a.beta = dbeta.as<double>();
+    a.eta = deta.as<double>();
+    a.M = dW.as<qg_c>();
+    a.err = derr.as<int>();
+    a.npairs = (int)(m * np);
+    a.pairs = dpairs.as<int>();
+    if ((e = ewald_assemble_locked(ss, a, 0))) return e;
+    periodic_field_kernel<<<(unsigned)m, 128>>>((int)m, np, n, dW.as<qg_c>(), df.as<qg_c>(), dD.as<qg_c>(),
+                                                dE.as<qg_c>());
+    g_launches.fetch_add(1);
+    QG_CUDA_TRY(cudaGetLastError());
+    QG_CUDA_TRY(cudaMemcpy(E_host + 3 * q0, dE.p, m * 48, cudaMemcpyDeviceToHost));
+  }
+  return QPMS_SUCCESS;
+}
+}  // namespace qg
+
 extern "C" {
 
 double qpms_ss_adjusted_eta(const qpms_scatsys_t *ss, qpms_complex_t wavenumber, const double wavevector[3]) {
@@ -537,6 +676,39 @@ int qpms_trans_calculator_get_AB_arrays_e32(const qpms_trans_calculator *c, qpms
                                             double maxK) {
   return qpms_trans_calculator_get_AB_arrays_e32_e(c, Adest, Aerr, Bdest, Berr, deststride, srcstride, eta,
                                                    wavenumber, b1, b2, beta, particle_shift, maxR, maxK, 7);
+}
+
+// Field of the periodic system at in-plane points (qpms_scatsyswk_scattered_E,
+// scatsystem.c:2114-2188): batched over points, host buffers.
+int qpms_gpu_scatsyswk_scattered_E(const qpms_scatsys_at_omega_k_t *sswk, qpms_bessel_t btyp,
+                                   const qpms_complex_t *cvf, size_t npoints, const double *where_xyz,
+                                   qpms_complex_t *E_xyz) {
+  clear_error();
+  if (!sswk || !sswk->ssw || !cvf || (npoints && (!where_xyz || !E_xyz))) { set_error("NULL argument"); return QPMS_EINVAL; }
+  const qpms_scatsys_t *ss = sswk->ssw->ss;
+  if (btyp != QPMS_HANKEL_PLUS) {
+    set_error("Only scattered field with first kind Hankel functions currently implemented.");
+    return QPMS_EINVAL;
+  }
+  if (ss->lattice_dimension != 2) { set_error("Only 2D-periodic lattices implemented"); return QPMS_EINVAL; }
+  if (sswk->k[2] != 0) { set_error("Bloch vector must lie in the xy plane"); return QPMS_EINVAL; }
+  const qg_c k = *(const qg_c *)&sswk->ssw->wavenumber;
+  double eta = sswk->eta;
+  if (eta == 0 || isnan(eta)) eta = qpms_ss_adjusted_eta(ss, sswk->ssw->wavenumber, sswk->k);
+  const double beta[2] = {sswk->k[0], sswk->k[1]};
+  return periodic_field(ss, k, beta, eta, (const qg_c *)cvf, npoints, where_xyz, (qg_c *)E_xyz);
+}
+
+ccart3_t qpms_scatsyswk_scattered_E(const qpms_scatsys_at_omega_k_t *sswk, qpms_bessel_t btyp,
+                                    const qpms_complex_t *cvf, cart3_t where) {
+  ccart3_t res;
+  const double w[3] = {where.x, where.y, where.z};
+  if (qpms_gpu_scatsyswk_scattered_E(sswk, btyp, cvf, 1, w, &res.x)) {
+    qpms_complex_t nanc;
+    nanc.re = nanc.im = NAN;
+    res.x = res.y = res.z = nanc;
+  }
+  return res;
 }
 
 }  // extern "C"

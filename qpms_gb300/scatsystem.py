@@ -105,6 +105,8 @@ def declare(L):
     L.qpms_gpu_finite_planewave_scatter_ext.restype = ci
     L.qpms_gpu_scatsys_scattered_E.restype = ci
     L.qpms_gpu_scatsys_scattered_E.argtypes = [vp, ci, cd, cd, vp, sz, vp, vp]
+    L.qpms_gpu_scatsyswk_scattered_E.restype = ci
+    L.qpms_gpu_scatsyswk_scattered_E.argtypes = [C.POINTER(_SSWK), ci, vp, sz, vp, vp]
     L.qpms_gpu_scatsys_scattered_E_device.restype = ci
     L.qpms_gpu_scatsys_scattered_E_device.argtypes = [vp, ci, cd, cd, vp, sz, vp, vp, vp]
     for name in ("qpms_scatsys_scattered_E", "qpms_scatsys_scattered_E__alt"):
@@ -351,9 +353,30 @@ class _ScatteringSystemAtOmega:
         w = C.cast(self.ssw, C.POINTER(_SSW)).contents
         return complex(w.wavenumber[0], w.wavenumber[1])
 
-    def scattered_E(self, scatcoeffvector_full, evalpos, alt=False, btyp=QPMS_HANKEL_PLUS):
-        """qpms_c.pyx:1118-1141, at this frequency's wavenumber."""
-        return self.ss.scattered_E(self.wavenumber(), scatcoeffvector_full, evalpos, alt, btyp)
+    def scattered_E(self, scatcoeffvector_full, evalpos, alt=False, btyp=QPMS_HANKEL_PLUS, k=None, eta=0.0):
+        """qpms_c.pyx:1118-1141, at this frequency's wavenumber; for a 2D lattice
+        give the Bloch vector k (qpms_c.pyx:974-996, points in the particles'
+        plane; eta = 0 selects the adjusted Ewald parameter)."""
+        if k is None:
+            return self.ss.scattered_E(self.wavenumber(), scatcoeffvector_full, evalpos, alt, btyp)
+        evalpos = np.asarray(evalpos, dtype=np.float64)
+        if evalpos.shape[-1] != 3:
+            raise ValueError("Last dimension of evalpos has to be 3")
+        w = np.ascontiguousarray(evalpos.reshape(-1, 3))
+        cv = np.ascontiguousarray(scatcoeffvector_full, dtype=np.complex128)
+        if cv.size != self.ss.fecv_size:
+            raise ValueError("Length of a full coefficient vector has to be %d, not %d" % (self.ss.fecv_size, cv.size))
+        wk = _SSWK()
+        wk.ssw = self.ssw
+        kk = list(k) + [0.0] * (3 - len(k))
+        for i in range(3):
+            wk.k[i] = kk[i]
+        wk.eta = float(eta)
+        E = np.empty((w.shape[0], 3), dtype=np.complex128)
+        _lib.check(self._L.qpms_gpu_scatsyswk_scattered_E(C.byref(wk), int(btyp), cv.ctypes.data, w.shape[0],
+                                                          w.ctypes.data, E.ctypes.data),
+                   "qpms_gpu_scatsyswk_scattered_E")
+        return E.reshape(evalpos.shape)
 
 
 class ScatteringMatrix:

@@ -160,3 +160,40 @@ def test_errors(gpu):
         fin.scattered_E(1.7e7, np.zeros(fin.fecv_size, complex), np.ones((2, 3)), btyp=7)
     with pytest.raises(ValueError):
         fin.scattered_E(1.7e7, np.zeros(3, complex), np.ones((2, 3)))
+
+
+def test_periodic_field_vs_oracle(gpu, orc):
+    """Field of a 2D lattice at in-plane points (qpms_scatsyswk_scattered_E):
+    the lattice-summed translation W(point <- particle) applied to f, of which
+    the regular electric dipole waves give the field at the point.  Oracle:
+    the same blocks from its Ewald mode-problem builder with the point as an
+    extra particle (T = -1), and its regular-wave field at r = 0."""
+    from qpms_gb300 import QpmsGpuError
+    from qpms_gb300.workloads import honeycomb_lattice
+    lMax = 2
+    b1, b2, pos = honeycomb_lattice()
+    ss = gpu.ScatteringSystem(pos, 80e-9, EPS_I, EPS_E, lMax, lattice=(b1, b2))
+    om = 2.1 * EV / HBAR
+    k = np.sqrt(EPS_E) * om / C0
+    kxy = (0.13 * np.pi / 580e-9, 0.05 * np.pi / 580e-9)
+    kv = np.array([kxy[0], kxy[1], 0.0])
+    rng = np.random.default_rng(17)
+    f = rng.normal(size=ss.fecv_size) + 1j * rng.normal(size=ss.fecv_size)
+    pts = np.zeros((12, 3))
+    pts[:, :2] = rng.uniform(-700e-9, 700e-9, size=(12, 2))
+    eta = orc.adjusted_eta(abs(b1[0] * b2[1] - b1[1] * b2[0]), k, kv, lMax)
+    E = ss(om).scattered_E(f, pts, k=kxy, eta=eta)
+    calc = orc.TransCalculator(lMax)
+    n = 2 * lMax * (lMax + 2)
+    for q, r in enumerate(pts):
+        pa = np.vstack([pos, r])
+        T = np.ascontiguousarray(np.broadcast_to(-np.eye(n), (3, n, n)), dtype=complex)
+        X = orc.periodic_modeproblem(calc, pa, T, k, b1, b2, kv, eta)   # I + W
+        a = sum(X[2 * n:3 * n, p * n:(p + 1) * n] @ f[p * n:(p + 1) * n] for p in range(2))
+        ref = orc.scattered_E(lMax, r[None, :], 1, k, a, r[None, :])[0]
+        assert np.linalg.norm(E[q] - ref) <= 1e-9 * np.linalg.norm(ref), (q, E[q], ref)
+    # the single-point reference form and the errors
+    with pytest.raises(QpmsGpuError):
+        ss(om).scattered_E(f, np.array([[0, 0, 1e-7]]), k=kxy)       # off the particles' plane
+    with pytest.raises(QpmsGpuError):
+        ss(om).scattered_E(f, pts[:1], k=kxy, btyp=1)                 # Hankel waves only
