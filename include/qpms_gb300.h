@@ -390,12 +390,44 @@ qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_ld(int np, const double *pos_xyz
     const double *radius, const qpms_complex_t *eps_inside, const qpms_ldparams_t *const *ld_inside,
     qpms_complex_t eps_medium, qpms_l_t lMax, const double *b1, const double *b2);
 
+/* ---------------- point symmetry and irreps (scatsystem.h:300-430) ----------------
+ * qpms_gpu_scatsys_set_symmetry gives a finite system one of the reference's
+ * point groups generated by coordinate mirror operations ("trivial", "C2",
+ * "C2v", "D2h"; symmetries.py point_group_info), with its irrep names and
+ * order (names sorted).  The packed (symmetry-adapted) basis is this
+ * library's: packed vectors of the reference differ by a unitary change of
+ * basis inside each irrep; eigenvalues, determinants and unpacked solutions
+ * agree.  ss->saecv_sizes is set. */
+int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group);
+int qpms_gpu_scatsys_nirreps(const qpms_scatsys_t *ss);
+const char *qpms_gpu_scatsys_irrep_name(const qpms_scatsys_t *ss, int iri);
+const size_t *qpms_gpu_scatsys_saecv_sizes(const qpms_scatsys_t *ss);
+qpms_complex_t *qpms_scatsys_irrep_transform_matrix(qpms_complex_t *target_U,       /* scatsystem.h:313-314 */
+    const qpms_scatsys_t *ss, int iri);
+qpms_complex_t *qpms_scatsys_irrep_pack_matrix(qpms_complex_t *target_packed,       /* scatsystem.h:330-333 */
+    const qpms_complex_t *orig_full, const qpms_scatsys_t *ss, int iri);
+qpms_complex_t *qpms_scatsys_irrep_unpack_matrix(qpms_complex_t *target_full,       /* scatsystem.h:336-338 */
+    const qpms_complex_t *orig_packed, const qpms_scatsys_t *ss, int iri, bool add);
+qpms_complex_t *qpms_scatsys_irrep_pack_vector(qpms_complex_t *target_packed,       /* scatsystem.h:342-345 */
+    const qpms_complex_t *orig_full, const qpms_scatsys_t *ss, int iri);
+qpms_complex_t *qpms_scatsys_irrep_unpack_vector(qpms_complex_t *target_full,       /* scatsystem.h:348-351 */
+    const qpms_complex_t *orig_packed, const qpms_scatsys_t *ss, int iri, bool add);
+qpms_complex_t *qpms_scatsys_build_translation_matrix_e_irrep_packed(               /* scatsystem.h:390-397 */
+    qpms_complex_t *target, const qpms_scatsys_t *ss, int iri, qpms_complex_t k, qpms_bessel_t J);
+
 /* Evaluates the medium and the T-matrices at omega, like qpms_scatsys_at_omega
  * (scatsystem.c:606-630). */
 qpms_scatsys_at_omega_t *qpms_gpu_scatsys_at_omega(const qpms_scatsys_t *ss, qpms_complex_t omega);
 void qpms_gpu_scatsys_at_omega_free(qpms_scatsys_at_omega_t *ssw);
 
 /* -- drop-in replacements of the reference's hot-path functions -- */
+
+/* Irrep-packed mode problem (scatsystem.h:403-407, 451-473): assembled and
+ * packed on the GPU; the LU and solve take packed vectors (qpms_ss_LU.full
+ * false, .iri set). */
+qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_irrep_packed(qpms_complex_t *target,
+    const qpms_scatsys_at_omega_t *ssw, int iri);
+
 
 /* Replaces qpms_scatsysw_build_modeproblem_matrix_full (scatsystem.h:368-372,
  * scatsystem.c:1345-1350): M = I - T S on the GPU (finite systems: S(R<-R) = 0,
@@ -417,6 +449,10 @@ qpms_ss_LU qpms_scatsysw_modeproblem_matrix_full_factorise(qpms_complex_t *mpmat
     int *target_piv, const qpms_scatsys_at_omega_t *ssw, const qpms_scatsys_at_omega_k_t *sswk);
 qpms_ss_LU qpms_scatsysw_build_modeproblem_matrix_full_LU(qpms_complex_t *target,
     int *target_piv, const qpms_scatsys_at_omega_t *ssw);
+qpms_ss_LU qpms_scatsysw_build_modeproblem_matrix_irrep_packed_LU(qpms_complex_t *target,
+    int *target_piv, const qpms_scatsys_at_omega_t *ssw, int iri);
+qpms_ss_LU qpms_scatsysw_modeproblem_matrix_irrep_packed_factorise(qpms_complex_t *mpmatrix_packed,
+    int *target_piv, const qpms_scatsys_at_omega_t *ssw, int iri);
 qpms_complex_t *qpms_scatsys_scatter_solve(qpms_complex_t *f, const qpms_complex_t *a_inc,
     qpms_ss_LU lu);
 void qpms_ss_LU_free(qpms_ss_LU lu);
@@ -432,7 +468,7 @@ double qpms_ss_adjusted_eta(const qpms_scatsys_t *ss, qpms_complex_t wavenumber,
 /* Replaces qpms_scatsyswk_build_modeproblem_matrix_full (scatsystem.h:498-502,
  * scatsystem.c:1352-1357): M = I - T W(omega, k) of a 2D lattice, W from the
  * Ewald sums (short range, long range, sigma0) on the GPU; eta = sswk->eta or,
- * if 0/NaN, qpms_ss_adjusted_eta.  Diagonal T-matrices. */
+ * if 0/NaN, qpms_ss_adjusted_eta. */
 qpms_complex_t *qpms_scatsyswk_build_modeproblem_matrix_full(qpms_complex_t *target,
     const qpms_scatsys_at_omega_k_t *sswk);
 /* Replaces qpms_scatsyswk_build_modeproblem_matrix_full_LU (scatsystem.h:523-527). */

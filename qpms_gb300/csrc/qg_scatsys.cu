@@ -308,6 +308,7 @@ void lattice_reduce(double *b1, double *b2) {
 }
 
 void field_forget_system(const qpms_scatsys_t *ss);  // qg_field.cu
+void sym_forget_system(const qpms_scatsys_t *ss);    // qg_sym.cu
 
 // T-matrix of kind t at omega: the diagonal (n values) for a system of
 // spheres, the full row-major n x n matrix when the system is dense.
@@ -328,6 +329,34 @@ void kind_tmat(const ScatsysPriv *s, int t, cd om, std::vector<qg_c> &out) {
     out.assign(n * n, cmk(0, 0));
     for (size_t i = 0; i < n; ++i) out[i * n + i] = cmk(d[i].real(), d[i].imag());
   }
+}
+
+int assemble_modeproblem_device(const qpms_scatsys_t *ss, int nw, const std::vector<qg_c> &T_host, bool dense,
+                                const std::vector<qg_c> &k_host, int J, qg_c *dM, cudaStream_t st);
+
+// M = I - T S of ssw (any T-matrices in one basis) on the device, row-major.
+int ssw_modeproblem_device(const qpms_scatsys_at_omega_t *ssw, qg_c *dM, cudaStream_t st) {
+  int lMax;
+  size_t n;
+  if (check_uniform_bspec(ssw, &lMax, &n)) return QPMS_EINVAL;
+  const bool diag = tm_all_diagonal(ssw, n);
+  std::vector<qg_c> T;
+  for (int t = 0; t < ssw->ss->tm_count; ++t)
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = 0; j < n; ++j)
+        if (!diag || i == j) T.push_back(*(const qg_c *)&ssw->tm[t]->m[i * n + j]);
+  std::vector<qg_c> k(1, *(const qg_c *)&ssw->wavenumber);
+  return assemble_modeproblem_device(ssw->ss, 1, T, !diag, k, 3, dM, st);
+}
+
+// I + S (translation matrix with Bessel kind J, zero self blocks) on the device:
+// the assembly with T = -1.  Callers subtract I where they want S.
+int ss_translation_device(const qpms_scatsys_t *ss, qg_c k, int J, qg_c *dM, cudaStream_t st) {
+  const ScatsysPriv *s = sspriv(ss);
+  std::vector<qg_c> T((size_t)ss->tm_count * s->spec.n, cmk(-1.0, 0.0));
+  std::vector<qg_c> kk(1, k);
+  // a dense system still takes the diagonal -1 here
+  return assemble_modeproblem_device(ss, 1, T, false, kk, J, dM, st);
 }
 
 // Accessors used by qg_solve.cu.
@@ -598,6 +627,7 @@ static qpms_scatsys_t *create_spheres(int np, const double *pos_xyz, const int *
 void qpms_gpu_scatsys_free(qpms_scatsys_t *ss) {
   if (!ss) return;
   field_forget_system(ss);
+  sym_forget_system(ss);
   delete sspriv(ss);  // the translation calculator is shared (shared_calculator)
 }
 
@@ -644,20 +674,10 @@ qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_full(qpms_complex_t *targ
   clear_error();
   if (!ssw || !ssw->ss) { set_error("NULL ssw"); return nullptr; }
   if (ssw->ss->lattice_dimension != 0) { set_error("periodic system: use qpms_scatsyswk_build_modeproblem_matrix_full"); return nullptr; }
-  int lMax;
-  size_t n;
-  if (check_uniform_bspec(ssw, &lMax, &n)) return nullptr;
   const size_t N = ssw->ss->fecv_size;
-  const bool diag = tm_all_diagonal(ssw, n);
-  std::vector<qg_c> T;
-  for (int t = 0; t < ssw->ss->tm_count; ++t)
-    for (size_t i = 0; i < n; ++i)
-      for (size_t j = 0; j < n; ++j)
-        if (!diag || i == j) T.push_back(*(const qg_c *)&ssw->tm[t]->m[i * n + j]);
-  std::vector<qg_c> k(1, *(const qg_c *)&ssw->wavenumber);
   DevBuf dM;
   if (dalloc(dM, N * N * 16)) return nullptr;
-  if (assemble_modeproblem_device(ssw->ss, 1, T, !diag, k, 3, (qg_c *)dM.p, 0)) return nullptr;
+  if (ssw_modeproblem_device(ssw, (qg_c *)dM.p, 0)) return nullptr;
   bool own = false;
   if (!target) {
     target = (qpms_complex_t *)malloc(N * N * 16);
@@ -679,12 +699,10 @@ qpms_complex_t *qpms_scatsys_build_translation_matrix_e_full(qpms_complex_t *tar
   if (J < 1 || J > 4) { set_error("invalid J"); return nullptr; }
   const ScatsysPriv *s = sspriv(ss);
   const size_t n = s->spec.n, N = ss->fecv_size;
-  // S = -(M - I) with T = -1: M = I + S off the diagonal, I on it; subtract I below
-  std::vector<qg_c> T((size_t)ss->tm_count * n, cmk(-1.0, 0.0));
-  std::vector<qg_c> kk(1, cmk(k.re, k.im));
+  (void)n;
   DevBuf dM;
   if (dalloc(dM, N * N * 16)) return nullptr;
-  if (assemble_modeproblem_device(ss, 1, T, false, kk, J, (qg_c *)dM.p, 0)) return nullptr;
+  if (ss_translation_device(ss, cmk(k.re, k.im), J, (qg_c *)dM.p, 0)) return nullptr;
   bool own = false;
   if (!target) {
     target = (qpms_complex_t *)malloc(N * N * 16);

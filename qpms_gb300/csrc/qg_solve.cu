@@ -149,19 +149,47 @@ using namespace qg;
 
 extern "C" {
 
+static qpms_ss_LU factorise_any(qpms_complex_t *mpmatrix_full, int *target_piv, const qpms_scatsys_at_omega_t *ssw,
+                                const qpms_scatsys_at_omega_k_t *sswk, int iri);
+
 qpms_ss_LU qpms_scatsysw_modeproblem_matrix_full_factorise(qpms_complex_t *mpmatrix_full, int *target_piv,
                                                            const qpms_scatsys_at_omega_t *ssw,
                                                            const qpms_scatsys_at_omega_k_t *sswk) {
+  return factorise_any(mpmatrix_full, target_piv, ssw, sswk, -1);
+}
+
+// Irrep-packed counterpart (scatsystem.h:467-473): the matrix is
+// saecv_sizes[iri] squared.
+qpms_ss_LU qpms_scatsysw_modeproblem_matrix_irrep_packed_factorise(qpms_complex_t *mpmatrix_packed, int *target_piv,
+                                                                   const qpms_scatsys_at_omega_t *ssw, int iri) {
+  return factorise_any(mpmatrix_packed, target_piv, ssw, nullptr, iri);
+}
+
+qpms_ss_LU qpms_scatsysw_build_modeproblem_matrix_irrep_packed_LU(qpms_complex_t *target, int *target_piv,
+                                                                  const qpms_scatsys_at_omega_t *ssw, int iri) {
+  qpms_complex_t *M = qpms_scatsysw_build_modeproblem_matrix_irrep_packed(target, ssw, iri);
+  if (!M) {
+    qpms_ss_LU lu;
+    memset(&lu, 0, sizeof lu);
+    return lu;
+  }
+  return factorise_any(M, target_piv, ssw, nullptr, iri);
+}
+
+static qpms_ss_LU factorise_any(qpms_complex_t *mpmatrix_full, int *target_piv, const qpms_scatsys_at_omega_t *ssw,
+                                const qpms_scatsys_at_omega_k_t *sswk, int iri) {
   clear_error();
   qpms_ss_LU lu;
   memset(&lu, 0, sizeof lu);
   if (sswk && !ssw) ssw = sswk->ssw;
   lu.ssw = ssw;
   lu.sswk = sswk;
-  lu.full = true;
-  lu.iri = -1;
+  lu.full = iri < 0;
+  lu.iri = iri < 0 ? -1 : iri;
   if (!mpmatrix_full || !ssw) { set_error("NULL matrix or ssw"); return lu; }
-  const size_t N = ssw->ss->fecv_size;
+  if (iri >= 0 && !ssw->ss->saecv_sizes) { set_error("the system has no point symmetry"); return lu; }
+  const size_t N = iri < 0 ? ssw->ss->fecv_size : ssw->ss->saecv_sizes[iri];
+  if (N == 0) { set_error("empty irrep"); return lu; }
   bool own_piv = false;
   if (!target_piv) {
     target_piv = (int *)malloc(sizeof(int) * N);
@@ -216,7 +244,8 @@ qpms_ss_LU qpms_scatsysw_build_modeproblem_matrix_full_LU(qpms_complex_t *target
 qpms_complex_t *qpms_scatsys_scatter_solve(qpms_complex_t *f, const qpms_complex_t *a_inc, qpms_ss_LU lu) {
   clear_error();
   if (!lu.a || !lu.ipiv || !lu.ssw || !a_inc) { set_error("invalid LU or a_inc"); return nullptr; }
-  const size_t N = lu.ssw->ss->fecv_size;
+  // full or irrep-packed vectors (scatsystem.c:2262-2273)
+  const size_t N = lu.full ? lu.ssw->ss->fecv_size : lu.ssw->ss->saecv_sizes[lu.iri];
   cublasHandle_t h;
   Dev dA, dT, dP, dB, arrA, arrB;
   if (blas_handle_get(&h) || dalloc(dA, N * N * 16) || dalloc(dT, N * N * 16) || dalloc(dP, N * 4) ||

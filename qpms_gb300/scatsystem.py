@@ -68,6 +68,28 @@ def declare(L):
     L.qpms_gpu_scatsys_create_spheres.argtypes = [ci, vp, vp, ci, vp, vp, cd, cd, ci]
     L.qpms_gpu_scatsys_create.restype = vp
     L.qpms_gpu_scatsys_create.argtypes = [ci, vp, vp, ci, vp, cd, cd, ci, vp, vp]
+    L.qpms_gpu_scatsys_set_symmetry.restype = ci
+    L.qpms_gpu_scatsys_set_symmetry.argtypes = [vp, C.c_char_p]
+    L.qpms_gpu_scatsys_nirreps.restype = ci
+    L.qpms_gpu_scatsys_nirreps.argtypes = [vp]
+    L.qpms_gpu_scatsys_irrep_name.restype = C.c_char_p
+    L.qpms_gpu_scatsys_irrep_name.argtypes = [vp, ci]
+    L.qpms_gpu_scatsys_saecv_sizes.restype = vp
+    L.qpms_gpu_scatsys_saecv_sizes.argtypes = [vp]
+    for name in ("qpms_scatsys_irrep_pack_vector", "qpms_scatsys_irrep_pack_matrix"):
+        getattr(L, name).restype = vp
+        getattr(L, name).argtypes = [vp, vp, vp, ci]
+    for name in ("qpms_scatsys_irrep_unpack_vector", "qpms_scatsys_irrep_unpack_matrix"):
+        getattr(L, name).restype = vp
+        getattr(L, name).argtypes = [vp, vp, vp, ci, C.c_bool]
+    L.qpms_scatsys_irrep_transform_matrix.restype = vp
+    L.qpms_scatsys_irrep_transform_matrix.argtypes = [vp, vp, ci]
+    L.qpms_scatsysw_build_modeproblem_matrix_irrep_packed.restype = vp
+    L.qpms_scatsysw_build_modeproblem_matrix_irrep_packed.argtypes = [vp, vp, ci]
+    L.qpms_scatsys_build_translation_matrix_e_irrep_packed.restype = vp
+    L.qpms_scatsys_build_translation_matrix_e_irrep_packed.argtypes = [vp, vp, ci, cd, cd, ci]
+    L.qpms_scatsysw_build_modeproblem_matrix_irrep_packed_LU.restype = _LU
+    L.qpms_scatsysw_build_modeproblem_matrix_irrep_packed_LU.argtypes = [vp, vp, vp, ci]
     L.qpms_gpu_scatsys_free.restype = None
     L.qpms_gpu_scatsys_free.argtypes = [vp]
     L.qpms_gpu_scatsys_at_omega.restype = vp
@@ -121,7 +143,7 @@ def declare(L):
 class ScatteringSystem:
     """Finite system of spheres; ``ss(omega)`` evaluates it at a frequency."""
 
-    def __init__(self, positions, radius, eps_inside, eps_medium, lMax, kinds=None, lattice=None):
+    def __init__(self, positions, radius, eps_inside, eps_medium, lMax, kinds=None, lattice=None, sym=None):
         """lattice: None (finite system) or (b1, b2), 2D basis vectors in the xy plane.
 
         eps_inside: one entry per particle kind (or a single one): a constant
@@ -172,6 +194,10 @@ class ScatteringSystem:
             b1.ctypes.data if b1 is not None else None, b2.ctypes.data if b2 is not None else None)
         if not self.s:
             raise _lib.QpmsGpuError("qpms_gpu_scatsys_create: " + _lib.last_error())
+        self.sym = sym
+        if sym is not None:  # point group: "trivial", "C2", "C2v" or "D2h"
+            _lib.check(self._L.qpms_gpu_scatsys_set_symmetry(self.s, str(sym).encode()),
+                       "qpms_gpu_scatsys_set_symmetry")
         self.fecv_size = pos.shape[0] * 2 * self.lMax * (self.lMax + 2)
 
     def __del__(self):
@@ -189,6 +215,81 @@ class ScatteringSystem:
         out = np.empty(self.fecv_size, dtype=np.complex128)
         _lib.check(self._L.qpms_gpu_incident_planewave_full(out.ctypes.data, self.s, k.ctypes.data, E.ctypes.data),
                    "qpms_gpu_incident_planewave_full")
+        return out
+
+    # ---- irreps (qpms_c.pyx:541-560, 590-730, 777-786) ----
+    @property
+    def nirreps(self):
+        return self._L.qpms_gpu_scatsys_nirreps(self.s)
+
+    @property
+    def irrep_names(self):
+        return [self._L.qpms_gpu_scatsys_irrep_name(self.s, i).decode() for i in range(self.nirreps)]
+
+    @property
+    def saecv_sizes(self):
+        p = C.cast(self._L.qpms_gpu_scatsys_saecv_sizes(self.s), C.POINTER(C.c_size_t))
+        return [p[i] for i in range(self.nirreps)]
+
+    def _check_iri(self, iri):
+        if not 0 <= int(iri) < self.nirreps:
+            raise ValueError("Invalid irrep index %s (of %d irreps)" % (iri, self.nirreps))
+        return int(iri)
+
+    def pack_vector(self, vect, iri):
+        iri = self._check_iri(iri)
+        v = np.ascontiguousarray(vect, dtype=np.complex128)
+        if v.size != self.fecv_size:
+            raise ValueError("Length of a full vector has to be %d, not %d" % (self.fecv_size, v.size))
+        out = np.empty(self.saecv_sizes[iri], dtype=np.complex128)
+        if not self._L.qpms_scatsys_irrep_pack_vector(out.ctypes.data, v.ctypes.data, self.s, iri):
+            raise _lib.QpmsGpuError("pack_vector: " + _lib.last_error())
+        return out
+
+    def unpack_vector(self, packed, iri):
+        iri = self._check_iri(iri)
+        p = np.ascontiguousarray(packed, dtype=np.complex128)
+        if p.size != self.saecv_sizes[iri]:
+            raise ValueError("Length of %d. irrep-packed vector has to be %d, not %d"
+                             % (iri, self.saecv_sizes[iri], p.size))
+        out = np.empty(self.fecv_size, dtype=np.complex128)
+        if not self._L.qpms_scatsys_irrep_unpack_vector(out.ctypes.data, p.ctypes.data, self.s, iri, False):
+            raise _lib.QpmsGpuError("unpack_vector: " + _lib.last_error())
+        return out
+
+    def pack_matrix(self, fullmatrix, iri):
+        iri = self._check_iri(iri)
+        M = np.ascontiguousarray(fullmatrix, dtype=np.complex128)
+        n = self.saecv_sizes[iri]
+        out = np.empty((n, n), dtype=np.complex128)
+        if not self._L.qpms_scatsys_irrep_pack_matrix(out.ctypes.data, M.ctypes.data, self.s, iri):
+            raise _lib.QpmsGpuError("pack_matrix: " + _lib.last_error())
+        return out
+
+    def unpack_matrix(self, packedmatrix, iri):
+        iri = self._check_iri(iri)
+        P = np.ascontiguousarray(packedmatrix, dtype=np.complex128)
+        out = np.empty((self.fecv_size, self.fecv_size), dtype=np.complex128)
+        if not self._L.qpms_scatsys_irrep_unpack_matrix(out.ctypes.data, P.ctypes.data, self.s, iri, False):
+            raise _lib.QpmsGpuError("unpack_matrix: " + _lib.last_error())
+        return out
+
+    def irrep_transform_matrix(self, iri):
+        """U (saecv_sizes[iri] x fecv_size): packed = U full."""
+        iri = self._check_iri(iri)
+        out = np.empty((self.saecv_sizes[iri], self.fecv_size), dtype=np.complex128)
+        if not self._L.qpms_scatsys_irrep_transform_matrix(out.ctypes.data, self.s, iri):
+            raise _lib.QpmsGpuError("irrep_transform_matrix: " + _lib.last_error())
+        return out
+
+    def translation_matrix_packed(self, wavenumber, iri, J=QPMS_HANKEL_PLUS):
+        iri = self._check_iri(iri)
+        k = complex(wavenumber)
+        n = self.saecv_sizes[iri]
+        out = np.empty((n, n), dtype=np.complex128)
+        if not self._L.qpms_scatsys_build_translation_matrix_e_irrep_packed(out.ctypes.data, self.s, iri, k.real,
+                                                                            k.imag, int(J)):
+            raise _lib.QpmsGpuError("translation_matrix_packed: " + _lib.last_error())
         return out
 
     def scattered_E(self, wavenumber, scatcoeffvector_full, evalpos, alt=False, btyp=QPMS_HANKEL_PLUS):
@@ -345,8 +446,16 @@ class _ScatteringSystemAtOmega:
             raise _lib.QpmsGpuError("apply_Tmatrices_full: " + _lib.last_error())
         return out
 
-    def scatter_solver(self):
-        return ScatteringMatrix(self)
+    def scatter_solver(self, iri=None):
+        return ScatteringMatrix(self, iri)
+
+    def modeproblem_matrix_packed(self, iri):
+        """(I - T S) projected on irrep iri (qpms_c.pyx:1084-1098)."""
+        n = self.ss.saecv_sizes[iri]
+        out = np.empty((n, n), dtype=np.complex128)
+        if not self._L.qpms_scatsysw_build_modeproblem_matrix_irrep_packed(out.ctypes.data, self.ssw, int(iri)):
+            raise _lib.QpmsGpuError("modeproblem_matrix_packed: " + _lib.last_error())
+        return out
 
     def wavenumber(self):
         """ssw->wavenumber of the C structure (scatsystem.h:239-249)."""
@@ -380,12 +489,17 @@ class _ScatteringSystemAtOmega:
 
 
 class ScatteringMatrix:
-    """LU-factorised (I - T S) (qpms_ss_LU); calling it solves for f."""
+    """LU-factorised (I - T S) (qpms_ss_LU), full or projected on irrep ``iri``
+    (qpms_c.pyx:1144-1195); calling it solves for f (full or packed)."""
 
-    def __init__(self, ssw):
+    def __init__(self, ssw, iri=None):
         self.ssw = ssw
         self._L = ssw._L
-        self.lu = self._L.qpms_scatsysw_build_modeproblem_matrix_full_LU(None, None, ssw.ssw)
+        self.iri = iri
+        if iri is None:
+            self.lu = self._L.qpms_scatsysw_build_modeproblem_matrix_full_LU(None, None, ssw.ssw)
+        else:
+            self.lu = self._L.qpms_scatsysw_build_modeproblem_matrix_irrep_packed_LU(None, None, ssw.ssw, int(iri))
         if not self.lu.a:
             raise _lib.QpmsGpuError("LU: " + _lib.last_error())
 
@@ -396,10 +510,11 @@ class ScatteringMatrix:
             self.lu = None
 
     def __call__(self, a_inc):
-        n = self.ssw.ss.fecv_size
+        n = self.ssw.ss.fecv_size if self.iri is None else self.ssw.ss.saecv_sizes[self.iri]
         a = np.ascontiguousarray(a_inc, dtype=np.complex128)
         if a.size != n:
-            raise ValueError("Length of a full coefficient vector has to be %d, not %d" % (n, a.size))
+            raise ValueError("Length of a %s coefficient vector has to be %d, not %d"
+                             % ("full" if self.iri is None else "packed", n, a.size))
         f = np.empty(n, dtype=np.complex128)
         if not self._L.qpms_scatsys_scatter_solve(f.ctypes.data, a.ctypes.data, self.lu):
             raise _lib.QpmsGpuError("scatter_solve: " + _lib.last_error())
