@@ -633,8 +633,10 @@ beyn_result_t *beyn_solve(size_t m, size_t l, beyn_function_M_t M, beyn_function
 
 /* scatsystem.h:649-662 (scatsystem.c:2301-2324): eigenmodes of a finite
  * system inside an ellipse in the complex omega plane, l = fecv_size probe
- * columns as in the reference; iri must be QPMS_NO_IRREP (irrep-packed
- * matrices are not implemented).  M(omega) is assembled on the GPU. */
+ * columns as in the reference; iri = QPMS_NO_IRREP for the full M, else M
+ * projected on that irrep of the system's point group (saecv_sizes[iri]
+ * probe columns, eigenvectors in the packed basis).  M(omega) is assembled
+ * (and packed) on the GPU. */
 beyn_result_t *qpms_scatsys_finite_find_eigenmodes(const qpms_scatsys_t *ss, qpms_iri_t iri,
     qpms_complex_t omega_centre, double omega_rr, double omega_ri, size_t contour_npoints,
     double rank_tol, size_t rank_sel_min, double res_tol);
@@ -650,6 +652,13 @@ beyn_result_t *qpms_scatsys_periodic_find_eigenmodes(const qpms_scatsys_t *ss, c
  * generator), mode 0 = plain FP64 LU per node, 1 = complex64 LU with FP64
  * refinement to refine_tol (relative residual; <= 0 selects 1e-12). */
 beyn_result_t *qpms_gpu_scatsys_find_eigenmodes(const qpms_scatsys_t *ss, const double *k,
+    qpms_complex_t omega_centre, double omega_rr, double omega_ri, size_t contour_npoints,
+    double rank_tol, size_t rank_sel_min, double res_tol, size_t l, const qpms_complex_t *Vhat,
+    unsigned long long seed, int mode, double refine_tol);
+
+/* The extended form on irrep iri of a finite system with point symmetry
+ * (l <= saecv_sizes[iri], Vhat saecv_sizes[iri] x l). */
+beyn_result_t *qpms_gpu_scatsys_find_eigenmodes_irrep(const qpms_scatsys_t *ss, int iri,
     qpms_complex_t omega_centre, double omega_rr, double omega_ri, size_t contour_npoints,
     double rank_tol, size_t rank_sel_min, double res_tol, size_t l, const qpms_complex_t *Vhat,
     unsigned long long seed, int mode, double refine_tol);

@@ -41,6 +41,8 @@ def declare(L):
     L.qpms_scatsys_periodic_find_eigenmodes.argtypes = [vp, vp, cd, cd, cd, cd, sz, cd, sz, cd]
     L.qpms_gpu_scatsys_find_eigenmodes.restype = R
     L.qpms_gpu_scatsys_find_eigenmodes.argtypes = [vp, vp, cd, cd, cd, cd, sz, cd, sz, cd, sz, vp, u64, ci, cd]
+    L.qpms_gpu_scatsys_find_eigenmodes_irrep.restype = R
+    L.qpms_gpu_scatsys_find_eigenmodes_irrep.argtypes = [vp, ci, cd, cd, cd, cd, sz, cd, sz, cd, sz, vp, u64, ci, cd]
     L.qpms_gpu_beyn_result_stats.restype = ci
     L.qpms_gpu_beyn_result_stats.argtypes = [R, vp, vp, vp, vp]
     L.qpms_gpu_beyn_probe_matrix.restype = ci
@@ -140,11 +142,25 @@ def beyn_solve(M_function, m, l, omega_centre, omega_rr, omega_ri, contour_point
 
 def scatsys_find_modes(ss_ptr, fecv_size, omega_centre, omega_rr, omega_ri, blochvector=None, contour_points=20,
                        rank_tol=1e-4, rank_min_sel=1, res_tol=0.0, l=None, Vhat=None, seed=None, mode=None,
-                       refine_tol=0.0):
+                       refine_tol=0.0, iri=None):
     """qpms_scatsys_{finite,periodic}_find_eigenmodes, or the extended entry
-    point when l, Vhat, seed or mode is given."""
+    point when l, Vhat, seed or mode is given.  With iri, fecv_size is the
+    packed size of that irrep."""
     L = lib()
     c = complex(omega_centre)
+    if iri is not None:
+        V = None
+        if Vhat is not None:
+            V = np.ascontiguousarray(Vhat, dtype=np.complex128)
+            l = V.shape[1]
+            assert V.shape[0] == fecv_size
+        l = fecv_size if l is None else int(l)
+        res = L.qpms_gpu_scatsys_find_eigenmodes_irrep(ss_ptr, int(iri), c.real, c.imag, omega_rr, omega_ri,
+                                                        contour_points, rank_tol, rank_min_sel, res_tol, l,
+                                                        V.ctypes.data if V is not None else None,
+                                                        DEFAULT_SEED if seed is None else seed,
+                                                        1 if mode is None else mode, refine_tol)
+        return _collect(res, l, c, omega_rr, omega_ri)
     kv = None
     if blochvector is not None:
         kv = np.zeros(3)

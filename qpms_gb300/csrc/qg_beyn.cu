@@ -29,6 +29,10 @@
 namespace qg {
 bool scatsys_is_own(const qpms_scatsys_t *ss);
 bool scatsys_dense(const qpms_scatsys_t *ss);
+int sym_pack_matrix_device(const qpms_scatsys_t *ss, int iri, const qg_c *dM, size_t ldm, qg_c *dout,
+                           cudaStream_t st);
+size_t sym_size(const qpms_scatsys_t *ss, int iri);
+int sym_nirreps(const qpms_scatsys_t *ss);
 void scatsys_tdiag(const qpms_scatsys_t *ss, int t, double om_re, double om_im, std::vector<qg_c> &out);
 qg_c scatsys_wavenumber(const qpms_scatsys_t *ss, double om_re, double om_im);
 int blas_handle_get(cublasHandle_t *h);
@@ -134,9 +138,15 @@ struct CallbackSource : MSource {
   }
 };
 
-// M(omega) = I - T S of a finite system (scatsystem.c:2280-2299, QPMS_NO_IRREP)
+// M(omega) = I - T S of a finite system (scatsystem.c:2280-2299), full or
+// projected on irrep iri (assembled full, packed on the device).
 struct FiniteSource : MSource {
   const qpms_scatsys_t *ss = nullptr;
+  int iri = -1;
+  qg_c *full = nullptr;  // N x N when packing
+  ~FiniteSource() override {
+    if (full) cudaFree(full);
+  }
   int build_rowmajor(cd z, cudaStream_t st) override {
     std::vector<qg_c> T, d;
     for (int t = 0; t < ss->tm_count; ++t) {
@@ -144,7 +154,12 @@ struct FiniteSource : MSource {
       T.insert(T.end(), d.begin(), d.end());
     }
     std::vector<qg_c> k(1, scatsys_wavenumber(ss, z.real(), z.imag()));
-    return assemble_modeproblem_device(ss, 1, T, scatsys_dense(ss), k, QPMS_HANKEL_PLUS, stage, st);
+    if (iri < 0) return assemble_modeproblem_device(ss, 1, T, scatsys_dense(ss), k, QPMS_HANKEL_PLUS, stage, st);
+    const size_t N = ss->fecv_size;
+    if (!full) QG_CUDA_TRY(cudaMalloc(&full, N * N * 16));
+    int e;
+    if ((e = assemble_modeproblem_device(ss, 1, T, scatsys_dense(ss), k, QPMS_HANKEL_PLUS, full, st))) return e;
+    return sym_pack_matrix_device(ss, iri, full, N, stage, st);
   }
 };
 
@@ -454,7 +469,7 @@ BeynResultPriv *beyn_core(MSource &src, beyn_function_M_inv_Vhat_t minv, void *m
 BeynResultPriv *scatsys_beyn(const qpms_scatsys_t *ss, const double *k, qpms_complex_t omega_centre,
                              double omega_rr, double omega_ri, size_t npoints, double rank_tol, size_t rank_sel_min,
                              double res_tol, size_t l, const qpms_complex_t *Vhat, unsigned long long seed, int mode,
-                             double refine_tol) {
+                             double refine_tol, int iri = -1) {
   if (!ss || !scatsys_is_own(ss)) {
     set_error("Beyn on a scattering system needs one made by qpms_gpu_scatsys_create_spheres[_2d]");
     return nullptr;
@@ -467,13 +482,23 @@ BeynResultPriv *scatsys_beyn(const qpms_scatsys_t *ss, const double *k, qpms_com
     set_error("finite eigenmode search on a periodic system (give a Bloch vector)");
     return nullptr;
   }
-  const size_t m = ss->fecv_size;
+  if (iri >= 0 && (k || iri >= sym_nirreps(ss))) {
+    set_error(k ? "Irreps decomposition not yet supported for periodic systems"
+                : "invalid irrep index (qpms_gpu_scatsys_set_symmetry gives the irreps)");
+    return nullptr;
+  }
+  const size_t m = iri >= 0 ? sym_size(ss, iri) : ss->fecv_size;
+  if (m == 0) {
+    set_error("empty irrep");
+    return nullptr;
+  }
   beyn_contour_t *c = beyn_contour_ellipse(omega_centre, omega_rr, omega_ri, npoints);
   if (!c) return nullptr;
   FiniteSource fs;
   PeriodicSource ps;
   MSource *src = k ? (MSource *)&ps : (MSource *)&fs;
   fs.ss = ps.ss = ss;
+  fs.iri = iri;
   if (k) {
     ps.kvec[0] = k[0];
     ps.kvec[1] = k[1];
@@ -598,12 +623,28 @@ beyn_result_t *qpms_scatsys_finite_find_eigenmodes(const qpms_scatsys_t *ss, qpm
                                                    size_t contour_npoints, double rank_tol, size_t rank_sel_min,
                                                    double res_tol) {
   clear_error();
-  if (iri != QPMS_NO_IRREP) {
-    set_error("irrep-packed eigenmode search is not implemented (use QPMS_NO_IRREP)");
+  // iri: QPMS_NO_IRREP for the full system, else M projected on the irrep
+  // (eigenvectors in the packed basis)
+  BeynResultPriv *r = scatsys_beyn(ss, nullptr, omega_centre, omega_rr, omega_ri, contour_npoints, rank_tol,
+                                   rank_sel_min, res_tol, 0, nullptr, kDefaultSeed, 1, kDefaultRefineTol,
+                                   iri == QPMS_NO_IRREP ? -1 : iri);
+  return r ? &r->pub : nullptr;
+}
+
+// The extended finite search on one irrep (probe columns, probe matrix or
+// seed, precision mode, refinement tolerance as qpms_gpu_scatsys_find_eigenmodes).
+beyn_result_t *qpms_gpu_scatsys_find_eigenmodes_irrep(const qpms_scatsys_t *ss, int iri, qpms_complex_t omega_centre,
+                                                      double omega_rr, double omega_ri, size_t contour_npoints,
+                                                      double rank_tol, size_t rank_sel_min, double res_tol, size_t l,
+                                                      const qpms_complex_t *Vhat, unsigned long long seed, int mode,
+                                                      double refine_tol) {
+  clear_error();
+  if (iri < 0) {
+    set_error("invalid irrep index %d", iri);
     return nullptr;
   }
   BeynResultPriv *r = scatsys_beyn(ss, nullptr, omega_centre, omega_rr, omega_ri, contour_npoints, rank_tol,
-                                   rank_sel_min, res_tol, 0, nullptr, kDefaultSeed, 1, kDefaultRefineTol);
+                                   rank_sel_min, res_tol, l, Vhat, seed, mode, refine_tol, iri);
   return r ? &r->pub : nullptr;
 }
 

@@ -12,6 +12,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
+#include <memory>
 #include <vector>
 
 #include "qg_assembly.h"
@@ -22,6 +24,14 @@ namespace qg {
 bool scatsys_is_own(const qpms_scatsys_t *ss);
 int scatsys_lmax(const qpms_scatsys_t *ss);
 bool scatsys_dense(const qpms_scatsys_t *ss);
+int sym_nirreps(const qpms_scatsys_t *ss);
+size_t sym_size(const qpms_scatsys_t *ss, int iri);
+int sym_pack_matrix_device(const qpms_scatsys_t *ss, int iri, const qg_c *dM, size_t ldm, qg_c *dout,
+                           cudaStream_t st);
+int sym_pack_vectors_device(const qpms_scatsys_t *ss, int iri, const qg_c *dv, int nrhs, size_t ldv, qg_c *dout,
+                            size_t ldo, cudaStream_t st);
+int sym_unpack_add_vectors_device(const qpms_scatsys_t *ss, int iri, const qg_c *dp, int nrhs, size_t ldp,
+                                  qg_c *dfull, size_t ldf, cudaStream_t st);
 void scatsys_tdiag(const qpms_scatsys_t *ss, int t, double om_re, double om_im, std::vector<qg_c> &out);
 qg_c scatsys_wavenumber(const qpms_scatsys_t *ss, double om_re, double om_im);
 void planewave_direction_coeffs(int lMax, const double k_dir[3], const qpms_complex_t E_cart[3],
@@ -92,8 +102,27 @@ int finite_scatter_dense(const qpms_scatsys_t *ss, int W, const std::vector<qg_c
   QG_CUDA_TRY(cudaMemcpy(dtm.p, tm.data(), np * 4, cudaMemcpyHostToDevice));
   QG_CUDA_TRY(cudaMemcpy(dpos.p, pos.data(), np * 24, cudaMemcpyHostToDevice));
   QG_CUDA_TRY(cudaMemcpy(dcoef.p, coef.data(), n * 16, cudaMemcpyHostToDevice));
+  // With a point symmetry the system splits into one independent system per
+  // irrep (about N / |G| unknowns each: |G|^2 fewer LU flops): M and T a are
+  // packed on the device, each irrep is solved, and the solutions unpacked.
+  const int nir = sym_nirreps(ss);
   DenseSolver ds;
-  if ((e = ds.init((int)N, 1, mode, 0x5eedbe11))) return e;
+  std::vector<std::unique_ptr<DenseSolver>> dsi(nir);
+  Dev dMp, dbp, dxp;
+  size_t namax = 0;
+  for (int i = 0; i < nir; ++i) namax = std::max(namax, sym_size(ss, i));
+  if (nir == 0) {
+    if ((e = ds.init((int)N, 1, mode, 0x5eedbe11))) return e;
+  } else {
+    if ((e = dalloc(dMp, namax * namax * 16)) || (e = dalloc(dbp, namax * 16)) || (e = dalloc(dxp, namax * 16)))
+      return e;
+    for (int i = 0; i < nir; ++i) {
+      const size_t na = sym_size(ss, i);
+      if (!na) continue;
+      dsi[i].reset(new DenseSolver());
+      if ((e = dsi[i]->init((int)na, 1, mode, 0x5eedbe11 + i))) return e;
+    }
+  }
   const bool dense = scatsys_dense(ss);
   auto assemble = [&](int J, const qg_c *Tsrc, size_t count, bool dn) -> int {
     QG_CUDA_TRY(cudaMemcpy(dT.p, Tsrc, count * 16, cudaMemcpyHostToDevice));
@@ -120,10 +149,33 @@ int finite_scatter_dense(const qpms_scatsys_t *ss, int W, const std::vector<qg_c
     if ((e = launch_apply_t(1, np, n, ntm, dense ? 1 : 0, dtm.as<int>(), dT.as<qg_c>(), da.as<qg_c>(),
                             db.as<qg_c>(), st)))
       return e;
-    if ((e = ds.factorize(dM.p, N, st, true))) return e;
     double res = 0;
     int it = 0;
-    if ((e = ds.solve(dM.p, N, db.p, dx.p, 1, 1e-13, 12, &res, &it, st))) return e;
+    if (nir == 0) {
+      if ((e = ds.factorize(dM.p, N, st, true))) return e;
+      if ((e = ds.solve(dM.p, N, db.p, dx.p, 1, 1e-13, 12, &res, &it, st))) return e;
+    } else {
+      QG_CUDA_TRY(cudaMemsetAsync(dx.p, 0, N * 16, st));
+      for (int i = 0; i < nir; ++i) {
+        const size_t na = sym_size(ss, i);
+        if (!na) continue;
+        double ri = 0;
+        int iti = 0;
+        if ((e = sym_pack_matrix_device(ss, i, dM.as<qg_c>(), N, dMp.as<qg_c>(), st)) ||
+            (e = sym_pack_vectors_device(ss, i, db.as<qg_c>(), 1, N, dbp.as<qg_c>(), na, st)) ||
+            (e = dsi[i]->factorize(dMp.p, na, st, true)) ||
+            (e = dsi[i]->solve(dMp.p, na, dbp.p, dxp.p, 1, 1e-13, 12, &ri, &iti, st)) ||
+            (e = sym_unpack_add_vectors_device(ss, i, dxp.as<qg_c>(), 1, na, dx.as<qg_c>(), N, st)))
+          return e;
+        it = std::max(it, iti);
+      }
+      // the residual of the unpacked solution in the full system (FP64)
+      double *rn2 = dn.as<double>(), h2[2];
+      if ((e = launch_residual(1, N, dM.as<qg_c>(), dx.as<qg_c>(), db.as<qg_c>(), dr.as<qg_c>(), rn2, rn2 + 1, st)))
+        return e;
+      QG_CUDA_TRY(cudaMemcpy(h2, rn2, 16, cudaMemcpyDeviceToHost));
+      res = sqrt(h2[0] / (h2[1] > 0 ? h2[1] : 1));
+    }
     if (resid_out) resid_out[w] = res;
     if (iters_out) iters_out[w] = it;
     if ((e = launch_sigma_ext(1, N, da.as<qg_c>(), dx.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), st))) return e;

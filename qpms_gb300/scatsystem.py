@@ -392,7 +392,15 @@ class ScatteringSystem:
         (explicit probe matrix), seed, mode (0 plain FP64, 1 mixed), refine_tol."""
         from . import beyn
         if iri is not None:
-            raise NotImplementedError("irrep-packed eigenmode search is not implemented")
+            if blochvector is not None:
+                raise NotImplementedError("Irreps decomposition not yet supported for periodic systems")
+            iri = self._check_iri(iri)
+            out = beyn.scatsys_find_modes(self.s, self.saecv_sizes[iri], omega_centre, omega_rr, omega_ri, None,
+                                          contour_points, rank_tol, rank_min_sel, res_tol, l, Vhat, seed, mode,
+                                          refine_tol, iri=iri)
+            out["iri"] = iri
+            out["blochvector"] = None
+            return out
         if self.lattice is None and blochvector is not None:
             raise ValueError("a Bloch vector needs a periodic system")
         if self.lattice is not None and blochvector is None:

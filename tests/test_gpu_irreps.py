@@ -116,3 +116,46 @@ def test_errors(gpu):
     pos = rect_array(2, 1, 4e-7, 4e-7)
     with pytest.raises(QpmsGpuError):
         gpu.ScatteringSystem(pos, [50e-9, 60e-9], [EPS_I, EPS_I], EPS_E, 2, kinds=[0, 1], sym="C2v")
+
+
+def test_symmetric_large_scatter_vs_full(gpu, orc):
+    """720 unknowns (> 512) with D2h: each frequency is solved per irrep (8
+    systems of about 90 unknowns) and unpacked; the same as the system without
+    symmetry and as the oracle's full solve."""
+    lMax = 3
+    pos = rect_array(6, 4, 400e-9, 350e-9)
+    om = np.array([1.95, 2.35]) * EV / HBAR
+    sym = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax, sym="D2h")
+    full = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax)
+    assert sym.fecv_size == 720
+    a = sym.planewave_scatter_batch(om, mode=1, want_f=True, want_scat=True)
+    b = full.planewave_scatter_batch(om, mode=1, want_f=True, want_scat=True)
+    calc = orc.TransCalculator(lMax)
+    for i, w in enumerate(om):
+        assert a["residual"][i] <= 1e-12
+        assert np.linalg.norm(a["f"][i] - b["f"][i]) <= 1e-9 * np.linalg.norm(b["f"][i])
+        f, _, sig = orc.finite_sphere_scatter(calc, pos, 50e-9, EPS_I, EPS_E, w)
+        assert np.linalg.norm(a["f"][i] - f) <= 1e-9 * np.linalg.norm(f)
+        assert abs(a["sigma_ext"][i] - sig) <= 1e-9 * abs(sig)
+        assert abs(a["sigma_scat"][i] - b["sigma_scat"][i]) <= 1e-9 * abs(b["sigma_scat"][i])
+
+
+def test_beyn_per_irrep(gpu):
+    """Eigenmodes of a symmetric 2 x 2 cluster searched irrep by irrep: every
+    mode of the full search is found in one of the irreps (packed problems of
+    8 unknowns instead of 64)."""
+    pos = rect_array(2, 2, 400e-9, 400e-9)
+    ss = gpu.ScatteringSystem(pos, 60e-9, EPS_I, EPS_E, 2, sym="D2h")
+    c, rr, ri = (2.52 - 0.3j) * EV / HBAR, 0.1 * EV / HBAR, 0.1 * EV / HBAR
+    full0 = ss.find_modes(c, rr, ri, contour_points=64, rank_tol=1e300)
+    full = ss.find_modes(c, rr, ri, contour_points=64, rank_tol=1e-10 * full0["ranktest_SV"][0])
+    assert full["eigval"].size == 3
+    found = []
+    for i in range(ss.nirreps):
+        r0 = ss.find_modes(c, rr, ri, iri=i, contour_points=64, rank_tol=1e300)
+        r = ss.find_modes(c, rr, ri, iri=i, contour_points=64, rank_tol=1e-10 * r0["ranktest_SV"][0])
+        assert r["eigvec"].shape[1] == ss.saecv_sizes[i]
+        found.extend(r["eigval"][r["residuals"] < 1e-6 * np.abs(r["eigval"])] if r["eigval"].size else [])
+    found = np.array(found)
+    for e in full["eigval"]:
+        assert np.min(np.abs(found - e)) <= 1e-8 * abs(e), e
