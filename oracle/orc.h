@@ -121,13 +121,16 @@ double complex orc_complex_gamma_inc(double a, double complex x, int m);
 double complex orc_ewald_sr_integral(double r, double complex k, int n, double eta);
 typedef double (*orc_fn_t)(double, const void *);
 double orc_qagiu(orc_fn_t f, const void *p, double a, double epsabs, double epsrel, double *abserr);
+/* shift_z: height of the shift above the lattice plane (0: the xy sums) */
 void orc_ewald3_sigma_xy(int lMax_e, int csphase, double eta, double complex k, orc_c2 b1, orc_c2 b2, orc_c2 beta,
-                         orc_c2 shift, double maxR, double maxK, int parts, double complex *sigma_out,
+                         orc_c2 shift, double shift_z, double maxR, double maxK, int parts, double complex *sigma_out,
                          double complex *sigma_short_out, double complex *sigma_long_out);
+void orc_sigma_direct(int lMax_e, int csphase, double complex k, orc_c2 b1, orc_c2 b2, orc_c2 beta, orc_c2 shift,
+                      double shift_z, int nlayers, double complex *out);
 int orc_trans_calculator_get_AB_arrays_e32(const orc_trans_calculator *c, double complex *Adest,
                                            double complex *Bdest, size_t deststride, size_t srcstride, double eta,
                                            double complex k, orc_c2 b1, orc_c2 b2, orc_c2 beta, orc_c2 shift,
-                                           double maxR, double maxK, int parts);
+                                           double shift_z, double maxR, double maxK, int parts);
 double orc_adjusted_eta(double unitcell_area, double complex wavenumber, const double kvec[3], int lMax);
 int orc_periodic_modeproblem(const orc_trans_calculator *c, int np, const double *pos, const double complex *T,
                              double complex k, orc_c2 b1, orc_c2 b2, const double kvec[2], double eta,

@@ -292,6 +292,8 @@ def _declare_ewald(L):
     L.orc_ewald3_sigma_xy_ri.argtypes = [ci, ci, cd, cd, cd, vp, vp, vp, cd, cd, ci, vp, vp, vp]
     L.orc_get_AB_arrays_e32_ri.restype = ci
     L.orc_get_AB_arrays_e32_ri.argtypes = [vp, vp, vp, cd, cd, cd, vp, vp, vp, cd, cd, ci]
+    L.orc_sigma_direct_ri.restype = None
+    L.orc_sigma_direct_ri.argtypes = [ci, ci, cd, cd, vp, vp, vp, ci, vp]
     L.orc_periodic_modeproblem_ri.restype = ci
     L.orc_periodic_modeproblem_ri.argtypes = [vp, ci, vp, vp, cd, cd, vp, vp, cd, vp]
     L.orc_complex_gamma_inc_ri.restype = None
@@ -310,7 +312,7 @@ def ewald_sigma_xy(lMax_e, eta, k, b1, b2, beta, shift, maxR, maxK, parts=7, csp
     out = [np.zeros(ne, dtype=np.complex128) for _ in range(3)]
     b12 = np.array([b1[0], b1[1], b2[0], b2[1]], dtype=np.float64)
     be = np.array(beta[:2], dtype=np.float64)
-    sh = np.array(shift[:2], dtype=np.float64)
+    sh = np.array(list(shift[:3]) + [0.0] * (3 - len(shift[:3])), dtype=np.float64)
     k = complex(k)
     L.orc_ewald3_sigma_xy_ri(lMax_e, csphase, float(eta), k.real, k.imag, b12.ctypes.data, be.ctypes.data,
                              sh.ctypes.data, float(maxR), float(maxK), int(parts), out[0].ctypes.data,
@@ -325,7 +327,7 @@ def get_AB_arrays_e32(calc, eta, k, b1, b2, beta, shift, maxR, maxK, parts=7):
     B = np.zeros((ne, ne), dtype=np.complex128)
     b12 = np.array([b1[0], b1[1], b2[0], b2[1]], dtype=np.float64)
     be = np.array(beta[:2], dtype=np.float64)
-    sh = np.array(shift[:2], dtype=np.float64)
+    sh = np.array(list(shift[:3]) + [0.0] * (3 - len(shift[:3])), dtype=np.float64)
     k = complex(k)
     L.orc_get_AB_arrays_e32_ri(calc.ptr, A.ctypes.data, B.ctypes.data, float(eta), k.real, k.imag, b12.ctypes.data,
                                be.ctypes.data, sh.ctypes.data, float(maxR), float(maxK), int(parts))
@@ -344,6 +346,19 @@ def periodic_modeproblem(calc, pos, T, k, b1, b2, kvec, eta):
     lib().orc_periodic_modeproblem_ri(calc.ptr, np_, pos.ctypes.data, T.ctypes.data, k.real, k.imag,
                                       b12.ctypes.data, kv.ctypes.data, float(eta), M.ctypes.data)
     return M
+
+
+def sigma_direct(lMax_e, k, b1, b2, beta, shift, nlayers, csphase=-1):
+    """Direct (non-Ewald) lattice sum of h_n(k r) leg_nm e^{i m phi} e^{i beta.(R - s)},
+    |i|, |j| <= nlayers; converges for Im k > 0."""
+    out = np.zeros((lMax_e + 1) ** 2, dtype=np.complex128)
+    b12 = np.array([b1[0], b1[1], b2[0], b2[1]], dtype=np.float64)
+    be = np.array(beta[:2], dtype=np.float64)
+    sh = np.array(list(shift[:3]) + [0.0] * (3 - len(shift[:3])), dtype=np.float64)
+    k = complex(k)
+    lib().orc_sigma_direct_ri(lMax_e, csphase, k.real, k.imag, b12.ctypes.data, be.ctypes.data, sh.ctypes.data,
+                              int(nlayers), out.ctypes.data)
+    return out
 
 
 def complex_gamma_inc(a, x, m=0):

@@ -21,6 +21,21 @@
  *   trans array e32          translations.c:724-776
  *   periodic M = I - T W     scatsystem.c:1219-1237, 1283-1343
  *   adjusted eta             scatsystem.c:68-80, default eta scatsystem.c:194-207
+ *
+ * Particle shifts off the lattice plane (shift.z != 0, layers of a 2D lattice
+ * at different heights; e32 with LAT_2D_IN_3D short range):
+ *   short-range sum          ewald.c:742-920, general branch (Legendre at cos theta, all (n, m))
+ *   long-range sum           ewald.c:441-469 structure: per reciprocal point the double sum
+ *                            over (j, s) of S1[y][j, s] (-k z)^(2j - s) (|beta + K| / k)^(n - s)
+ *                            gamma^(2j - 1) Delta_j, and Kambe's Delta_j (ewaldsf.c:344-402,
+ *                            series in z^2 / 4 over incomplete gammas).  The reference marks
+ *                            this branch untested and it is not consistent as it stands (the
+ *                            S1 constants of ewald.c:179-197 carry no Legendre factor, Delta
+ *                            is called with x instead of x^2 at ewald.c:403); the constants
+ *                            here are derived from the sum itself (2D Poisson summation of
+ *                            the Gaussian-regularised h_n Y_nm with the z derivatives as
+ *                            Hermite polynomials) and reduce to the s1 constants at z = 0.
+ *                            Pinned by eta invariance and by direct summation at complex k.
  */
 #include "orc.h"
 #include <float.h>
@@ -533,19 +548,207 @@ static void sigma_short(const e3c_t *c, double complex *target, double eta, doub
   free(tc);
 }
 
-/* sigma = sigma_S + sigma_L (+ sigma0 when the shift vanishes), all nelem_sc */
+/* ---------------- shifted layers (shift.z != 0) ---------------- */
+
+/* ewald.c:742-920, general branch: all (n, m), Legendre at cos theta of R - shift */
+static void sigma_short_z(const e3c_t *c, int csphase, double complex *target, double eta, double complex k,
+                          orc_c2 b1, orc_c2 b2, double maxR, orc_c2 beta, orc_c2 shift, double shift_z) {
+  const int nelem_sc = c->nelem_sc, lMax = c->lMax;
+  const int k_is_real = (cimag(k) == 0);
+  double complex *tc = calloc(nelem_sc, sizeof(double complex));
+  double *leg = malloc(sizeof(double) * (lMax + 1) * (lMax + 2) / 2);
+  memset(target, 0, sizeof(double complex) * nelem_sc);
+  size_t lw = 1, li = 0;
+  double lsum = 0, lsum_c = 0;
+  xyweb g;
+  xyweb_init(&g, b1, b2, 1e-13, 0, 1, maxR, 0);
+  orc_c2 Rb;
+  while (xyweb_next(&g, &Rb)) {
+    orc_c2 Rs = sub2(Rb, shift);
+    const double dz = -shift_z;
+    const double arg = atan2(Rs.y, Rs.x);
+    const double r = sqrt(dot2(Rs, Rs) + dz * dz);
+    orc_legendre_array(lMax, dz / r, csphase, leg);
+    const double complex e_beta = cexp(I * dot2(beta, Rs));
+    for (int n = 0; n <= lMax; ++n) {
+      const double complex prefacn = -I * (k_is_real ? pow(2. / creal(k), n + 1) : cpow(2. / k, n + 1)) / ORC_SQRTPI;
+      const double complex in = orc_ewald_sr_integral(r, k, n, eta);
+      for (int m = -n; m <= n; ++m) {
+        const int y = n * (n + 1) + m;
+        double complex v = prefacn * pow(r, n) * leg[leg_idx(n, abs(m))] * in * e_beta * cexp(I * m * arg) *
+                           m1pow_m_neg(m);
+        ckahanadd(target + y, tc + y, v);
+        kahanadd(&lsum, &lsum_c, cabs(v));
+      }
+    }
+    ++li;
+    double cursum_min = INFINITY;
+    for (int y = 0; y < nelem_sc; ++y) {
+      const double a = cabs(target[y]);
+      if (a && a < cursum_min) cursum_min = a;
+    }
+    if (li >= 12 * lw + 1) {
+      if (lsum < DBL_EPSILON * cursum_min) break;
+      lsum = lsum_c = 0;
+      li = 0;
+      ++lw;
+    }
+  }
+  free(leg);
+  free(tc);
+}
+
+static double binom(int n, int k) { return factorial(n) / (factorial(k) * factorial(n - k)); }
+
+/* S1[y][j, s] for the shifted long-range sum, y = n(n+1) + m, j = 0..n-|m|,
+ * s = n-|m|, n-|m|-2, ... >= 0 with s <= 2j, j >= s/2.  Derivation: with
+ * Y(d) = |d|^n leg_nm(cos theta) e^{i m phi} a solid harmonic,
+ * Y(d) xi^(2n) e^{-xi^2 d^2} = (-1/2)^n Y(grad) e^{-xi^2 d^2}; the in-plane
+ * Fourier transform turns (x, y) derivatives into -i (beta + K), the z
+ * derivatives give (-xi)^s H_s(xi z) e^{-xi^2 z^2}, and the xi integral over
+ * (0, eta) is (1/2) (gamma k / 2)^(2j - 1) Delta_j with t = (gamma k)^2 / (4 xi^2).
+ * With r^n P_n^mu(cos theta) (no Condon-Shortley phase) = rho^mu sum_t c_t
+ * rho^(2t) z^(n - mu - 2t):
+ *   S1 = -i (-1)^n 2 sqrt(pi) L_nm (-i)^mu c_t (-1)^(t+s) H_{s, s-j} 2^-s,
+ * t = (n - mu - s) / 2, H_{s,l} = s! (-1)^l / (l! (s - 2l)!), L_nm the sign
+ * factors of leg_nm.  At z = 0 only 2j = s remains and S1 equals the xy
+ * constants s1[y][j] times leg_nm(0) (ewald.c:142-146, 425). */
+static double complex s1_shifted(int n, int m, int j, int s, int csphase) {
+  const int mu = abs(m);
+  const double L = ((csphase == -1) ? m1pow(mu) : 1) * m1pow_m_neg(m);
+  const double complex pref = -I * m1pow(n) * 2 * ORC_SQRTPI * L * cpow(-I, mu);
+  const int t = (n - mu - s) / 2, l = s - j;
+  double ct = 0;
+  for (int kk = t; kk <= (n - mu) / 2; ++kk)
+    ct += ldexp(1.0, -n) * m1pow(kk) * binom(n, kk) * binom(2 * n - 2 * kk, n) * factorial(n - 2 * kk) /
+          factorial(n - 2 * kk - mu) * binom(kk, t);
+  const double h = factorial(s) * m1pow(l) / (factorial(l) * factorial(s - 2 * l));
+  return pref * ct * m1pow(t + s) * h * ldexp(1.0, -s);
+}
+
+/* Kambe's Delta_j(X, z) = int_X^inf t^(-1/2-j) exp(-t + z^2 / 4t) dt, j = 0..jmax,
+ * by the series sum_q (z^2/4)^q / q! Gamma(1/2 - j - q, X) (ewaldsf.c:344-402),
+ * Gamma on the branch m of the unshifted sum. */
+static void kambe_delta(int jmax, double complex X, int branch, double complex z, double complex *D) {
+  const double complex w = 0.25 * z * z;
+  for (int j = 0; j <= jmax; ++j) {
+    double complex sum = 0, sc = 0, wq = 1;
+    for (int q = 0; q < 400; ++q) {
+      const double complex term = wq * orc_complex_gamma_inc(0.5 - j - q, X, branch);
+      ckahanadd(&sum, &sc, term);
+      if (q > 4 && cabs(term) < 1e-18 * cabs(sum)) break;
+      wq *= w / (q + 1);
+    }
+    D[j] = sum;
+  }
+}
+
+/* ewald.c:441-469 structure with the S1 constants above */
+static void sigma_long_z(const e3c_t *c, int csphase, double complex *target, double eta, double complex k, double A,
+                         orc_c2 rb1, orc_c2 rb2, double maxK, orc_c2 beta, orc_c2 shift, double shift_z) {
+  const int nelem_sc = c->nelem_sc, lMax = c->lMax;
+  double complex *tc = calloc(nelem_sc, sizeof(double complex));
+  memset(target, 0, sizeof(double complex) * nelem_sc);
+  size_t lw = 1, li = 0;
+  double lsum = 0, lsum_c = 0;
+  const double complex commonfac = 1 / (k * k * A);
+  xyweb g;
+  xyweb_init(&g, rb1, rb2, 1e-13, 0, 1, maxK, 0);
+  orc_c2 K;
+  double complex D[lMax + 1];
+  while (xyweb_next(&g, &K)) {
+    orc_c2 bK = add2(K, beta);
+    const double rbeta = sqrt(dot2(bK, bK));
+    const double arg = atan2(bK.y, bK.x);
+    const double complex phasefac = cexp(I * dot2(K, shift));
+    const double complex gamma_pq = clilgamma(rbeta / k);
+    const double complex x = gamma_pq * k / (2 * eta);
+    const double complex x2 = x * x;
+    kambe_delta(lMax, x2, (creal(x2) < 0 && !signbit(cimag(x2))) ? -1 : 0, I * k * gamma_pq * shift_z, D);
+    for (int n = 0; n <= lMax; ++n)
+      for (int m = -n; m <= n; ++m) {
+        const int y = n * (n + 1) + m, LM = n - abs(m);
+        double complex jsum = 0, jsum_c = 0;
+        for (int j = 0; j <= LM; ++j) {
+          double complex ssum = 0;
+          for (int s_ = j + (LM - j) % 2; s_ <= 2 * j && s_ <= LM; s_ += 2)
+            ssum += s1_shifted(n, m, j, s_, csphase) * cpow_0lim_zi(-k * shift_z, 2 * j - s_) *
+                    cpow_0lim_zi(rbeta / k, n - s_);
+          ckahanadd(&jsum, &jsum_c, ssum * cexp(I * m * arg) * D[j] * cpow(gamma_pq, 2 * j - 1));
+        }
+        jsum *= phasefac;
+        ckahanadd(target + y, tc + y, jsum);
+        kahanadd(&lsum, &lsum_c, cabs(jsum));
+      }
+    ++li;
+    double cursum_min = INFINITY;
+    for (int y = 0; y < nelem_sc; ++y) {
+      const double a = cabs(target[y]);
+      if (a && a < cursum_min) cursum_min = a;
+    }
+    if (li >= 12 * lw + 1) {
+      if (lsum < DBL_EPSILON * cursum_min) break;
+      lsum = lsum_c = 0;
+      li = 0;
+      ++lw;
+    }
+  }
+  for (int y = 0; y < nelem_sc; ++y) target[y] *= commonfac;
+  free(tc);
+}
+
+/* Direct lattice sum sum_R h_n(k |R - s|) leg_nm(cos theta) e^{i m phi} e^{i beta.(R - s)}
+ * over |i|, |j| <= nlayers (R = i b1 + j b2, R - s = 0 left out): the quantity
+ * the Ewald sums represent, convergent for Im k > 0. */
+void orc_sigma_direct(int lMax_e, int csphase, double complex k, orc_c2 b1, orc_c2 b2, orc_c2 beta, orc_c2 shift,
+                      double shift_z, int nlayers, double complex *out) {
+  const int ne = (lMax_e + 1) * (lMax_e + 1);
+  double complex *tc = calloc(ne, sizeof(double complex));
+  double *leg = malloc(sizeof(double) * (lMax_e + 1) * (lMax_e + 2) / 2);
+  double complex *h = malloc(sizeof(double complex) * (lMax_e + 1));
+  memset(out, 0, sizeof(double complex) * ne);
+  for (int i = -nlayers; i <= nlayers; ++i)
+    for (int j = -nlayers; j <= nlayers; ++j) {
+      orc_c2 Rb = add2(scale2(i, b1), scale2(j, b2));
+      orc_c2 Rs = sub2(Rb, shift);
+      const double dz = -shift_z;
+      const double r = sqrt(dot2(Rs, Rs) + dz * dz);
+      if (r == 0) continue;
+      orc_legendre_array(lMax_e, dz / r, csphase, leg);
+      orc_sph_bessel_fill(3, lMax_e, k * r, h);
+      const double arg = atan2(Rs.y, Rs.x);
+      const double complex e_beta = cexp(I * dot2(beta, Rs));
+      for (int n = 0; n <= lMax_e; ++n)
+        for (int m = -n; m <= n; ++m) {
+          const int y = n * (n + 1) + m;
+          ckahanadd(out + y, tc + y,
+                    h[n] * leg[leg_idx(n, abs(m))] * m1pow_m_neg(m) * cexp(I * m * arg) * e_beta);
+        }
+    }
+  free(h);
+  free(leg);
+  free(tc);
+}
+
+/* sigma = sigma_S + sigma_L (+ sigma0 when the shift vanishes), all nelem_sc;
+ * shift_z != 0: layers at different heights (terms of every parity) */
 void orc_ewald3_sigma_xy(int lMax_e, int csphase, double eta, double complex k, orc_c2 b1, orc_c2 b2, orc_c2 beta,
-                         orc_c2 shift, double maxR, double maxK, int parts, double complex *sigma_out,
+                         orc_c2 shift, double shift_z, double maxR, double maxK, int parts, double complex *sigma_out,
                          double complex *sigma_short_out, double complex *sigma_long_out) {
   e3c_t *c = e3c_init(lMax_e, csphase);
   const int ne = c->nelem_sc;
-  const int do_sigma0 = (shift.x == 0 && shift.y == 0);
+  const int do_sigma0 = (shift.x == 0 && shift.y == 0 && shift_z == 0);
   double complex *ss = calloc(ne, sizeof(double complex)), *sl = calloc(ne, sizeof(double complex));
   const double A = orc_l2d_unitcell_area(b1, b2);
   orc_c2 rb1, rb2;
   orc_l2d_reciprocalBasis2pi(b1, b2, &rb1, &rb2);
-  if (parts & 1) sigma_long(c, sl, eta, k, A, rb1, rb2, maxK, beta, shift);
-  if (parts & 2) sigma_short(c, ss, eta, k, b1, b2, maxR, !do_sigma0, beta, shift);
+  if (shift_z != 0) {
+    if (parts & 1) sigma_long_z(c, csphase, sl, eta, k, A, rb1, rb2, maxK, beta, shift, shift_z);
+    if (parts & 2) sigma_short_z(c, csphase, ss, eta, k, b1, b2, maxR, beta, shift, shift_z);
+  } else {
+    if (parts & 1) sigma_long(c, sl, eta, k, A, rb1, rb2, maxK, beta, shift);
+    if (parts & 2) sigma_short(c, ss, eta, k, b1, b2, maxR, !do_sigma0, beta, shift);
+  }
   for (int y = 0; y < ne; ++y) sigma_out[y] = ((parts & 2) ? ss[y] : 0) + ((parts & 1) ? sl[y] : 0);
   if (do_sigma0 && (parts & 4)) sigma_out[0] += sigma0(c, eta, k);
   if (sigma_short_out) memcpy(sigma_short_out, ss, sizeof(double complex) * ne);
@@ -559,11 +762,11 @@ void orc_ewald3_sigma_xy(int lMax_e, int csphase, double eta, double complex k, 
 int orc_trans_calculator_get_AB_arrays_e32(const orc_trans_calculator *c, double complex *Adest,
                                            double complex *Bdest, size_t deststride, size_t srcstride, double eta,
                                            double complex k, orc_c2 b1, orc_c2 b2, orc_c2 beta, orc_c2 shift,
-                                           double maxR, double maxK, int parts) {
+                                           double shift_z, double maxR, double maxK, int parts) {
   const int lMax_e = 2 * c->lMax + 1, ne_sc = lMax_e * (lMax_e + 2) + 1;
   const int csphase = (c->normalisation & 8) ? -1 : 1;
   double complex *sig = malloc(sizeof(double complex) * ne_sc);
-  orc_ewald3_sigma_xy(lMax_e, csphase, eta, k, b1, b2, beta, shift, maxR, maxK, parts, sig, NULL, NULL);
+  orc_ewald3_sigma_xy(lMax_e, csphase, eta, k, b1, b2, beta, shift, shift_z, maxR, maxK, parts, sig, NULL, NULL);
   size_t desti = 0, srci = 0;
   for (int n = 1; n <= c->lMax; ++n)
     for (int m = -n; m <= n; ++m) {
@@ -603,7 +806,7 @@ double orc_adjusted_eta(double unitcell_area, double complex wavenumber, const d
 }
 
 /* Periodic M = I - T W for np particles per cell with a common full bspec;
- * W(R <- C) from the e32 sums with particle_shift = pos_R - pos_C,
+ * W(R <- C) from the e32 sums with particle_shift = pos_R - pos_C (z included),
  * maxR = 64 sqrt(A), maxK = 2048 * 2 pi / maxR (scatsystem.c:1219-1237). */
 int orc_periodic_modeproblem(const orc_trans_calculator *c, int np, const double *pos, const double complex *T,
                              double complex k, orc_c2 b1, orc_c2 b2, const double kvec[2], double eta,
@@ -619,7 +822,9 @@ int orc_periodic_modeproblem(const orc_trans_calculator *c, int np, const double
   for (int R = 0; R < np; ++R)
     for (int Cc = 0; Cc < np; ++Cc) {
       orc_c2 shift = {pos[3 * R] - pos[3 * Cc], pos[3 * R + 1] - pos[3 * Cc + 1]};
-      orc_trans_calculator_get_AB_arrays_e32(c, Am, Bm, ne, 1, eta, k, b1, b2, beta, shift, maxR, maxK, 7);
+      const double shift_z = pos[3 * R + 2] - pos[3 * Cc + 2];
+      orc_trans_calculator_get_AB_arrays_e32(c, Am, Bm, ne, 1, eta, k, b1, b2, beta, shift, shift_z, maxR, maxK,
+                                             7);
       for (int ti = 0; ti < 2; ++ti)
         for (int yi = 0; yi < ne; ++yi)
           for (int tj = 0; tj < 2; ++tj)
@@ -645,14 +850,14 @@ void orc_ewald3_sigma_xy_ri(int lMax_e, int csphase, double eta, double kr, doub
                             const double *beta, const double *shift, double maxR, double maxK, int parts,
                             double complex *sig, double complex *ss, double complex *sl) {
   orc_c2 b1 = {b12[0], b12[1]}, b2 = {b12[2], b12[3]}, be = {beta[0], beta[1]}, sh = {shift[0], shift[1]};
-  orc_ewald3_sigma_xy(lMax_e, csphase, eta, kr + I * ki, b1, b2, be, sh, maxR, maxK, parts, sig, ss, sl);
+  orc_ewald3_sigma_xy(lMax_e, csphase, eta, kr + I * ki, b1, b2, be, sh, shift[2], maxR, maxK, parts, sig, ss, sl);
 }
 int orc_get_AB_arrays_e32_ri(const orc_trans_calculator *c, double complex *A, double complex *B, double eta,
                              double kr, double ki, const double *b12, const double *beta, const double *shift,
                              double maxR, double maxK, int parts) {
   orc_c2 b1 = {b12[0], b12[1]}, b2 = {b12[2], b12[3]}, be = {beta[0], beta[1]}, sh = {shift[0], shift[1]};
-  return orc_trans_calculator_get_AB_arrays_e32(c, A, B, c->nelem, 1, eta, kr + I * ki, b1, b2, be, sh, maxR, maxK,
-                                                parts);
+  return orc_trans_calculator_get_AB_arrays_e32(c, A, B, c->nelem, 1, eta, kr + I * ki, b1, b2, be, sh, shift[2],
+                                                maxR, maxK, parts);
 }
 int orc_periodic_modeproblem_ri(const orc_trans_calculator *c, int np, const double *pos, const double complex *T,
                                 double kr, double ki, const double *b12, const double *kvec, double eta,
@@ -665,4 +870,9 @@ void orc_complex_gamma_inc_ri(double a, double xr, double xi, int m, double comp
 }
 void orc_ewald_sr_integral_ri(double r, double kr, double ki, int n, double eta, double complex *out) {
   *out = orc_ewald_sr_integral(r, kr + I * ki, n, eta);
+}
+void orc_sigma_direct_ri(int lMax_e, int csphase, double kr, double ki, const double *b12, const double *beta,
+                         const double *shift, int nlayers, double complex *out) {
+  orc_c2 b1 = {b12[0], b12[1]}, b2 = {b12[2], b12[3]}, be = {beta[0], beta[1]}, sh = {shift[0], shift[1]};
+  orc_sigma_direct(lMax_e, csphase, kr + I * ki, b1, b2, be, sh, shift[2], nlayers, out);
 }

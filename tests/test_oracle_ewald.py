@@ -66,3 +66,48 @@ def test_adjusted_eta(orc):
         if abs(kap) ** 2 >= k2:
             exp = max(exp, np.sqrt(abs(abs(kap) ** 2 - k2) * (3 + 0.5) / 16))
         assert abs(orc.adjusted_eta(A, kap, kv, 3) - exp) <= 1e-14 * exp
+
+
+# ---- layers at different heights (particle_shift.z != 0) ----
+OBLIQUE = ((1.0, 0.0), (0.3, 1.1))
+
+
+@pytest.mark.parametrize("k,shift", [(2.3 + 0.9j, (0.31, -0.2, 0.37)), (4.1 + 1.1j, (0.0, 0.0, -0.5)),
+                                     (2.3 + 0.9j, (0.1, 0.2, 0.05)), (3.0 + 1.0j, (0.5, 0.55, -1.2))])
+def test_shifted_vs_direct_sum(orc, k, shift):
+    """The shifted Ewald sums against the lattice sum they represent, summed
+    directly (converges exponentially for Im k > 0), all (n, m) to lMax_e 5.
+    eta |z| <= 1.2 (the Delta series loses e^(2 eta^2 z^2) to cancellation)."""
+    d = orc.sigma_direct(5, k, *OBLIQUE, (0.7, -0.4), shift, 70)
+    eta = min(1.6, 1.2 / abs(shift[2]))
+    e = orc.ewald_sigma_xy(5, eta, k, *OBLIQUE, (0.7, -0.4), shift, 20, 160)[0]
+    assert np.abs(d - e).max() <= 1e-13 * np.abs(d).max()
+    assert np.abs(d[1::2]).max() > 1e-3 * np.abs(d).max()   # the odd-parity terms are present
+
+
+@pytest.mark.parametrize("k,shift", [(2.3, (0.31, -0.2, 0.37)), (5.3, (0.0, 0.0, 0.45)),
+                                     (5.3, (0.2, 0.5, -0.8)), (2.3 - 0.1j, (0.5, 0.1325, 0.2))])
+def test_shifted_eta_invariance(orc, k, shift):
+    """Real k (propagating diffraction orders: the branch of Gamma and of the
+    Kambe Delta series) and a lossy k with Im k < 0: sigma independent of eta."""
+    res = [orc.ewald_sigma_xy(5, eta, k, *OBLIQUE, (0.7, -0.4), shift, 20, 160)[0] for eta in (1.2, 1.6, 2.2)]
+    scale = np.abs(res[0]).max()
+    for r in res[1:]:
+        assert np.abs(r - res[0]).max() <= 1e-12 * scale
+
+
+def test_shifted_limit_and_parity(orc):
+    """shift.z -> 0 joins the xy sums; the even terms are even and the odd
+    terms odd in shift.z (reflection through the lattice plane)."""
+    args = (1.6, 2.3, (1, 0), (0, 1), (2.7, 1))
+    e0 = orc.ewald_sigma_xy(3, *args, (0.5, 0.1325), 20, 160)[0]
+    ez = orc.ewald_sigma_xy(3, *args, (0.5, 0.1325, 1e-12), 20, 160)[0]
+    assert np.abs(ez - e0).max() <= 1e-10 * np.abs(e0).max()
+    p = orc.ewald_sigma_xy(3, *args, (0.5, 0.1325, 0.3), 20, 160)[0]
+    q = orc.ewald_sigma_xy(3, *args, (0.5, 0.1325, -0.3), 20, 160)[0]
+    n = np.floor(np.sqrt(np.arange(16))).astype(int)
+    m = np.arange(16) - n * (n + 1)
+    odd = (n + m) % 2 == 1
+    sc = np.abs(p).max()
+    assert np.abs(p[~odd] - q[~odd]).max() <= 1e-13 * sc
+    assert np.abs(p[odd] + q[odd]).max() <= 1e-13 * sc and np.abs(p[odd]).max() > 1e-3 * sc
