@@ -477,8 +477,12 @@ qpms_ss_LU qpms_scatsyswk_build_modeproblem_matrix_full_LU(qpms_complex_t *targe
 
 /* Replace qpms_trans_calculator_get_AB_arrays_e32(_e) (translations.h:158-177,
  * translations.c:926-1078): lattice-summed A, B (2D xy lattice b1, b2, Bloch
- * vector beta, particle_shift in the plane, Ewald parameter eta) for the
- * calculator's normalisation, evaluated by the GPU Ewald kernel.  parts must be
+ * vector beta, particle_shift, Ewald parameter eta) for the calculator's
+ * normalisation, evaluated by the GPU Ewald kernel.  particle_shift.z != 0
+ * (layers at different heights) takes the shifted-layer sums (the reference's
+ * LAT_2D_IN_3D short-range branch and the shifted long-range branch,
+ * ewald.c:441-469, marked untested there; here derived anew and checked by
+ * eta invariance and direct summation).  parts must be
  * QPMS_EWALD_FULL (7); maxR / maxK are not used (the kernel truncates where the
  * terms fall below e^-56 of the leading ones); Aerr / Berr are zero-filled. */
 int qpms_trans_calculator_get_AB_arrays_e32(const qpms_trans_calculator *c,
@@ -544,10 +548,9 @@ ccart3_t qpms_scatsys_scattered_E__alt(const qpms_scatsys_t *ss, qpms_bessel_t b
 ccart3_t qpms_scatsysw_scattered_E__alt(const qpms_scatsys_at_omega_t *ssw,
     qpms_bessel_t btyp, const qpms_complex_t *cvf, cart3_t where);
 /* 2D-periodic system (scatsystem.c:2114-2188): the field of the lattice of
- * particles with Bloch vector sswk->k at points in the particles' plane,
- * btyp 3 only (as in the reference); sswk->eta = 0 selects
- * qpms_ss_adjusted_eta.  Points off that plane need the shifted-layer lattice
- * sums and are refused. */
+ * particles with Bloch vector sswk->k at any points (off the particles'
+ * plane through the shifted-layer lattice sums), btyp 3 only (as in the
+ * reference); sswk->eta = 0 selects qpms_ss_adjusted_eta. */
 ccart3_t qpms_scatsyswk_scattered_E(const qpms_scatsys_at_omega_k_t *sswk, qpms_bessel_t btyp,
     const qpms_complex_t *cvf, cart3_t where);
 int qpms_gpu_scatsyswk_scattered_E(const qpms_scatsys_at_omega_k_t *sswk, qpms_bessel_t btyp,

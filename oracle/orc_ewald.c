@@ -697,6 +697,57 @@ static void sigma_long_z(const e3c_t *c, int csphase, double complex *target, do
   free(tc);
 }
 
+/* Distant layers (|k z| large): the eta -> infinity limit of the shifted sums,
+ * a pure reciprocal-lattice (Weyl) sum.  The short-range part vanishes and
+ * Delta_j(0, z) = 2 (a/2)^(1/2-j) K_(j-1/2)(a), a = gamma k |z| (decaying or
+ * outgoing for the branch of gamma above), so
+ *   gamma^(2j-1) Delta_j = sqrt(pi) 2^j (k|z|)^-j e^-a gamma^(j-1) kappa_j(a),
+ * kappa_j = sqrt(2a/pi) e^a K_(j-1/2)(a) (kappa_0 = kappa_1 = 1,
+ * kappa_(j+1) = kappa_(j-1) + (2j - 1) kappa_j / a).  Converges like
+ * e^(-|beta + K| |z|). */
+static void sigma_spectral_z(const e3c_t *c, int csphase, double complex *target, double complex k, double A,
+                             orc_c2 rb1, orc_c2 rb2, orc_c2 beta, orc_c2 shift, double shift_z) {
+  const int nelem_sc = c->nelem_sc, lMax = c->lMax;
+  double complex *tc = calloc(nelem_sc, sizeof(double complex));
+  memset(target, 0, sizeof(double complex) * nelem_sc);
+  const double aw = fabs(shift_z);
+  const double maxK = 80.0 / aw + sqrt(dot2(beta, beta));
+  const double complex commonfac = 1 / (k * k * A);
+  const double complex kw = k * (-shift_z), kaw = k * aw;
+  xyweb g;
+  xyweb_init(&g, rb1, rb2, 1e-13, 0, 1, maxK, 0);
+  orc_c2 K;
+  double complex Kt[lMax + 2];
+  while (xyweb_next(&g, &K)) {
+    orc_c2 bK = add2(K, beta);
+    const double rbeta = sqrt(dot2(bK, bK));
+    const double arg = atan2(bK.y, bK.x);
+    const double complex phasefac = cexp(I * dot2(K, shift));
+    const double complex gamma_pq = clilgamma(rbeta / k);
+    const double complex a = gamma_pq * kaw;
+    /* Kt_j = gamma^(j-1) kappa_j: Kt_(j+1) = gamma^2 Kt_(j-1) + (2j - 1) Kt_j / (k |z|) */
+    Kt[0] = 1 / gamma_pq;
+    Kt[1] = 1;
+    for (int j = 1; j < lMax; ++j) Kt[j + 1] = gamma_pq * gamma_pq * Kt[j - 1] + (2 * j - 1) * Kt[j] / kaw;
+    const double complex ea = cexp(-a);
+    for (int n = 0; n <= lMax; ++n)
+      for (int m = -n; m <= n; ++m) {
+        const int y = n * (n + 1) + m, LM = n - abs(m);
+        double complex jsum = 0, jsum_c = 0;
+        for (int j = 0; j <= LM; ++j) {
+          double complex ssum = 0;
+          for (int s_ = j + (LM - j) % 2; s_ <= 2 * j && s_ <= LM; s_ += 2)
+            ssum += s1_shifted(n, m, j, s_, csphase) * cpow_0lim_zi(kw, 2 * j - s_) * cpow(kaw, -j) *
+                    cpow_0lim_zi(rbeta / k, n - s_);
+          ckahanadd(&jsum, &jsum_c, ssum * ORC_SQRTPI * ldexp(1.0, j) * Kt[j]);
+        }
+        ckahanadd(target + y, tc + y, jsum * cexp(I * m * arg) * ea * phasefac);
+      }
+  }
+  for (int y = 0; y < nelem_sc; ++y) target[y] *= commonfac;
+  free(tc);
+}
+
 /* Direct lattice sum sum_R h_n(k |R - s|) leg_nm(cos theta) e^{i m phi} e^{i beta.(R - s)}
  * over |i|, |j| <= nlayers (R = i b1 + j b2, R - s = 0 left out): the quantity
  * the Ewald sums represent, convergent for Im k > 0. */
@@ -731,7 +782,8 @@ void orc_sigma_direct(int lMax_e, int csphase, double complex k, orc_c2 b1, orc_
 }
 
 /* sigma = sigma_S + sigma_L (+ sigma0 when the shift vanishes), all nelem_sc;
- * shift_z != 0: layers at different heights (terms of every parity) */
+ * shift_z != 0: layers at different heights (terms of every parity);
+ * eta = INFINITY with shift_z != 0: the pure reciprocal-lattice sum */
 void orc_ewald3_sigma_xy(int lMax_e, int csphase, double eta, double complex k, orc_c2 b1, orc_c2 b2, orc_c2 beta,
                          orc_c2 shift, double shift_z, double maxR, double maxK, int parts, double complex *sigma_out,
                          double complex *sigma_short_out, double complex *sigma_long_out) {
@@ -742,7 +794,9 @@ void orc_ewald3_sigma_xy(int lMax_e, int csphase, double eta, double complex k, 
   const double A = orc_l2d_unitcell_area(b1, b2);
   orc_c2 rb1, rb2;
   orc_l2d_reciprocalBasis2pi(b1, b2, &rb1, &rb2);
-  if (shift_z != 0) {
+  if (shift_z != 0 && eta == INFINITY) {
+    if (parts & 1) sigma_spectral_z(c, csphase, sl, k, A, rb1, rb2, beta, shift, shift_z);
+  } else if (shift_z != 0) {
     if (parts & 1) sigma_long_z(c, csphase, sl, eta, k, A, rb1, rb2, maxK, beta, shift, shift_z);
     if (parts & 2) sigma_short_z(c, csphase, ss, eta, k, b1, b2, maxR, beta, shift, shift_z);
   } else {
@@ -766,6 +820,10 @@ int orc_trans_calculator_get_AB_arrays_e32(const orc_trans_calculator *c, double
   const int lMax_e = 2 * c->lMax + 1, ne_sc = lMax_e * (lMax_e + 2) + 1;
   const int csphase = (c->normalisation & 8) ? -1 : 1;
   double complex *sig = malloc(sizeof(double complex) * ne_sc);
+  /* layers at different heights: the same sums, evaluated where they are
+   * accurate -- the reciprocal-lattice sum for |k z| >= 2.5, else Ewald with
+   * eta |z| <= 1 (the Delta series cancels like e^(2 eta^2 z^2)) */
+  if (shift_z != 0) eta = (cabs(k) * fabs(shift_z) >= 2.5) ? INFINITY : fmin(eta, 1.0 / fabs(shift_z));
   orc_ewald3_sigma_xy(lMax_e, csphase, eta, k, b1, b2, beta, shift, shift_z, maxR, maxK, parts, sig, NULL, NULL);
   size_t desti = 0, srci = 0;
   for (int n = 1; n <= c->lMax; ++n)

@@ -32,6 +32,29 @@
 // subset of lattice points in registers; a shuffle + shared-memory reduction
 // gives sigma in shared memory, where the contraction reads it exactly as the
 // finite assembly reads its Bessel/Legendre factor table.
+//
+// Pairs of particles at different heights (shift.z = z_R - z_C != 0, layers of
+// the lattice; the reference's LAT_2D_IN_3D short-range branch and the
+// shifted long-range branch of ewald.c:441-469) have sums of every parity:
+//  * short range: Legendre P_n^|m|(cos theta) of R - shift by the upward
+//    recurrences, all (n, m);
+//  * long range: per reciprocal point the double sum over (j, s) of
+//      S1[y][j, s] (k w)^(2j - s) (|beta + K| / k)^(n - s) gamma^(2j - 1) Delta_j,
+//    w = -shift.z, with Kambe's Delta_j(X, z) = int_X^inf t^(-1/2-j) e^{-t + z^2/4t} dt,
+//    z^2 = -(gamma k w)^2, by the series sum_q (z^2/4)^q / q! Gamma(1/2 - j - q, X)
+//    (ewaldsf.c:344-402), written as X^-j sum_q r_q g_(j+q) with
+//    g_i = X^i Gamma(1/2 - i, X) (upward: g_i = (X g_(i-1) - sqrt(X) e^-X) / (1/2 - i))
+//    and r_q = (-w^2 eta^2)^q / q!;
+//  * eta is lowered to 1 / |w| where eta |w| > 1, which keeps the cancellation
+//    in the series below e^2 (the sums do not depend on eta);
+//  * distant layers, |k w| >= 2.5 (where eta <= 1 / |w| would let the short-
+//    and long-range parts cancel by e^(k^2 / 4 eta^2)): the eta -> infinity
+//    limit, a pure reciprocal-lattice sum (no short range) with
+//    Delta_j(0, z) = 2 (a/2)^(1/2-j) K_(j-1/2)(a), a = gamma k |w|, in closed
+//    form by the half-integer Bessel K recurrence; it converges like
+//    e^(-|beta + K| |w|);
+//  * the (n, m) accumulators are split into passes of at most 36 entries to
+//    stay in registers.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -107,6 +130,8 @@ struct EwShape {
   static constexpr int NE2 = NE * NE;
   static constexpr int NB = 2 * NE;
   static constexpr int NEVEN = (LE + 1) * (LE + 2) / 2;  // (n, m) with n + m even
+  static constexpr int ZP = S < 36 ? S : 36;               // accumulators per shifted pass
+  static constexpr int RED = NEVEN > ZP ? NEVEN : ZP;      // reduction buffer width
 };
 
 // (n, m) of the k-th even pair, in n-major order
@@ -117,17 +142,321 @@ __device__ __forceinline__ void even_nm(int k, int &n, int &m) {
   m = -n + 2 * (k - n * (n + 1) / 2);
 }
 
+
+// Unit data shared by the passes of one shifted pair.
+struct ZUnit {
+  qg_c k;
+  double eta, bx, by, sx, sy, w;
+  int KM;         // terms of the Delta series
+  int spectral;   // 1: pure reciprocal-lattice sum (distant layers, |k w| >= 2.5)
+};
+
+// One pass of the shifted sums: sigma_y for Y0 <= y < Y0 + NY into sig[].
+// s1u[e] = S1[e] (k w)^(2j - s) (2 eta / k)^(2j) (unit constants), rr[q] = r_q.
+template <int LMAX, int Y0, int NY>
+__device__ __forceinline__ void shifted_pass(const ZUnit &u, const qg_c *s1u, const double *rr, qg_c *sig,
+                                             qg_c (*red)[EwShape<LMAX>::RED], int *errflag) {
+  constexpr int LE = EwShape<LMAX>::LE;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const qg_c k = u.k;
+  const double eta = u.eta, w = u.w;
+  const bool kreal = (k.im == 0.0);
+  qg_c acc[NY];
+#pragma unroll
+  for (int i = 0; i < NY; ++i) acc[i] = cmk(0, 0);
+  const double sqpi = 1.7724538509055160273;
+
+  // ---------------- short range (none for the reciprocal-lattice sum) ----------------
+  if (!u.spectral) {
+    const double rc = 7.5 / eta;
+    const double smax = sqrt(u.sx * u.sx + u.sy * u.sy);
+    const int I1 = (int)ceil((rc + smax) * c_ew.rbn[0] / (2 * M_PI)) + 1;
+    const int I2 = (int)ceil((rc + smax) * c_ew.rbn[1] / (2 * M_PI)) + 1;
+    const int W1 = 2 * I1 + 1, W2 = 2 * I2 + 1;
+    const bool sr_ok = (long)W1 * W2 <= kEwMaxPoints && I1 >= 0 && I2 >= 0;
+    if (!sr_ok && tid == 0) atomicOr(errflag, 1);
+    const qg_c k2h = cscale(cmul(k, k), 0.5);
+    const qg_c ik2eta = cmk(-k.im / (2 * eta), k.re / (2 * eta));
+    const qg_c rk = crecip(k);
+    for (int t = tid; sr_ok && t < W1 * W2; t += kEThreads) {
+      const int i = t / W2 - I1, j = t % W2 - I2;
+      const double Rx = i * c_ew.b[0] + j * c_ew.b[2] - u.sx, Ry = i * c_ew.b[1] + j * c_ew.b[3] - u.sy;
+      const double rho2 = Rx * Rx + Ry * Ry, r2 = rho2 + w * w, r = sqrt(r2);
+      if (r * eta > 7.5) continue;
+      const qg_c zp = cmk(r * eta + ik2eta.re, ik2eta.im), zm = cmk(r * eta - ik2eta.re, -ik2eta.im);
+      const qg_c Ep = cmul(cexpi(cscale(k, r)), cerfc(zp, c_wd)), Em = cmul(cexpi(cscale(k, -r)), cerfc(zm, c_wd));
+      const qg_c d = csub(Em, Ep);
+      qg_c pm2 = cscale(cmul(cmk(d.im, -d.re), rk), sqpi / 2);  // I_{-1}
+      qg_c pm1 = cscale(cadd(Ep, Em), sqpi / (4 * r));           // I_0
+      const qg_c ex = cmk(-r2 * eta * eta + (k.re * k.re - k.im * k.im) / (4 * eta * eta),
+                          2 * k.re * k.im / (4 * eta * eta));
+      const qg_c E = cexpi(cmk(ex.im, -ex.re));
+      double sb, cb;
+      sincos(u.bx * Rx + u.by * Ry, &sb, &cb);
+      // base_n = -i (2/k)^(n+1) / sqrt(pi) r^n I_n e^{i beta.(R - s)}
+      qg_c base[LE + 1];
+      {
+        qg_c pf = cscale(cmul(cmk(0.0, -1.0), cscale(rk, 2.0)), 1.0 / sqpi);
+        const qg_c twok = cscale(rk, 2.0);
+        const qg_c eb = cmk(cb, sb);
+        double rn = 1.0, etap = eta;
+        const double inv2r2 = 1.0 / (2 * r2);
+#pragma unroll
+        for (int n = 0; n <= LE; ++n) {
+          qg_c In;
+          if (n == 0) {
+            In = pm1;
+          } else {
+            In = cscale(cadd(csub(cscale(pm1, 2 * n - 1), cmul(k2h, pm2)), cscale(E, etap)), inv2r2);
+            pm2 = pm1;
+            pm1 = In;
+            etap *= eta * eta;
+          }
+          base[n] = cmul(cmul(cscale(pf, rn), In), eb);
+          pf = cmul(pf, twok);
+          rn *= r;
+        }
+      }
+      const double rho = sqrt(rho2);
+      const double ct = w / r, st = rho / r;
+      const qg_c e1 = rho > 0 ? cmk(Rx / rho, Ry / rho) : cmk(1.0, 0.0);
+      double pmm = 1.0;  // P_mu^mu(ct) with the Condon-Shortley phase
+      qg_c em = cmk(1.0, 0.0);
+#pragma unroll
+      for (int mu = 0; mu <= LE; ++mu) {
+        if (mu > 0) {
+          pmm *= -(2 * mu - 1) * st;
+          em = cmul(em, e1);
+        }
+        double p0 = 0.0, p1 = pmm;
+#pragma unroll
+        for (int n = mu; n <= LE; ++n) {
+          double P;
+          if (n == mu) {
+            P = pmm;
+          } else {
+            P = ((2 * n - 1) * ct * p1 - (n + mu - 1) * p0) / (n - mu);
+            p0 = p1;
+            p1 = P;
+          }
+#pragma unroll
+          for (int sg = 0; sg < 2; ++sg) {
+            if (sg == 1 && mu == 0) continue;
+            const int m = sg ? -mu : mu, y = n * (n + 1) + m;
+            if (y < Y0 || y >= Y0 + NY) continue;
+            const qg_c e = sg ? cconj(em) : em;
+            acc[y - Y0] = cadd(acc[y - Y0], cscale(cmul(base[n], e), P * c_ew.legs[y]));
+          }
+        }
+      }
+    }
+  }
+  // ---------------- long range ----------------
+  {
+    const double kap2 = k.re * k.re + k.im * k.im;
+    const double aw = fabs(w);
+    // Ewald: terms below e^-56 past x^2 = 56; reciprocal-lattice sum: the terms
+    // fall like e^(-|beta + K| |w|) (|beta + K|/k)^(2 lMax + 1), below 1e-17 past |beta + K| |w| = 80
+    const double pmax = u.spectral ? 80.0 / aw : sqrt(kap2 + 56.0 * 4 * eta * eta);
+    const double Kc = pmax + sqrt(u.bx * u.bx + u.by * u.by);
+    const int I1 = (int)ceil(Kc * c_ew.bn[0] / (2 * M_PI)) + 1;
+    const int I2 = (int)ceil(Kc * c_ew.bn[1] / (2 * M_PI)) + 1;
+    const int W1 = 2 * I1 + 1, W2 = 2 * I2 + 1;
+    const bool lr_ok = (long)W1 * W2 <= kEwMaxPoints && I1 >= 0 && I2 >= 0;
+    if (!lr_ok && tid == 0) atomicOr(errflag, 1);
+    const qg_c rk = crecip(k);
+    const qg_c lrfac = crecip(cscale(cmul(k, k), c_ew.area));
+    const qg_c kaw = cscale(k, aw);
+    const qg_c rkaw = crecip(kaw);
+    const int KM = u.KM;
+    for (int t = tid; lr_ok && t < W1 * W2; t += kEThreads) {
+      const int i = t / W2 - I1, j = t % W2 - I2;
+      const double Kx = i * c_ew.rb[0] + j * c_ew.rb[2], Ky = i * c_ew.rb[1] + j * c_ew.rb[3];
+      const double qx = Kx + u.bx, qy = Ky + u.by;
+      const double rb = sqrt(qx * qx + qy * qy);
+      if (u.spectral && rb > pmax) continue;
+      qg_c gam, uu;
+      if (kreal) {
+        const double tt = rb / k.re;
+        if (tt >= 1.0) {
+          gam = cmk(sqrt(tt - 1.0) * sqrt(tt + 1.0), 0.0);
+          const double x = gam.re * k.re / (2 * eta);
+          if (!u.spectral && x * x > 56.0) continue;
+          uu = cmk(x, 0.0);
+        } else {
+          const double g = sqrt(1.0 - tt) * sqrt(1.0 + tt);
+          gam = cmk(0.0, -g);
+          uu = cmk(0.0, -g * k.re / (2 * eta));
+        }
+      } else {
+        const double kk2 = k.re * k.re + k.im * k.im;
+        const qg_c z = cmk((rb * k.re + 0.0 * k.im) / kk2, (0.0 * k.re - rb * k.im) / kk2);
+        qg_c a1 = cmk(z.re - 1, z.im), a2 = cmk(z.re + 1, z.im);
+        a2 = (a2.re < 0 && a2.im <= 0) ? cscale(csqrt_(a2), -1.0) : csqrt_(a2);
+        a1 = (a1.re < 0 && a1.im >= 0) ? cscale(csqrt_(a1), -1.0) : csqrt_(a1);
+        gam = cmul(a1, a2);
+        const qg_c x = cscale(cmul(gam, k), 1.0 / (2 * eta));
+        const qg_c x2 = cmul(x, x);
+        if (!u.spectral && x2.re > 56.0) continue;
+        uu = csqrt_(x2);
+        if (x2.re < 0 && !signbit(x2.im)) uu = cscale(uu, -1.0);
+      }
+      qg_c D[LE + 1];
+      if (u.spectral) {
+        // gamma^(2j-1) Delta_j(0, z) = sqrt(pi) 2^j (k|w|)^-j e^-a Kt_j, a = gamma k |w|,
+        // Kt_j = gamma^(j-1) kappa_j(a) (half-integer Bessel K); sqrt(pi) 2^j (k|w|)^-j is in s1u
+        const qg_c a = cmul(gam, kaw);
+        const qg_c ea = cexpi(cmk(-a.im, a.re));  // e^-a
+        const qg_c g2 = cmul(gam, gam);
+        qg_c km1 = crecip(gam), kc = cmk(1.0, 0.0);
+        D[0] = cmul(km1, ea);
+        if (LE >= 1) D[1] = ea;
+#pragma unroll
+        for (int jq = 1; jq < LE; ++jq) {
+          const qg_c kn = cadd(cmul(g2, km1), cscale(cmul(kc, rkaw), 2 * jq - 1));
+          km1 = kc;
+          kc = kn;
+          D[jq + 1] = cmul(kn, ea);
+        }
+      } else {
+        // D_a = sum_q r_q g_(a+q), g_i = X^i Gamma(1/2 - i, X)
+        const qg_c X = cmul(uu, uu);
+        const qg_c emX = cexpi(cmk(-X.im, X.re));
+        const qg_c uemX = cmul(uu, emX);
+#pragma unroll
+        for (int a2i = 0; a2i <= LE; ++a2i) D[a2i] = cmk(0, 0);
+        qg_c g = cscale(cerfc(uu, c_wd), sqpi);
+        for (int jj = 0; jj <= LE + KM; ++jj) {
+          if (jj > 0) g = cscale(csub(cmul(X, g), uemX), 1.0 / (0.5 - jj));
+#pragma unroll
+          for (int a2i = 0; a2i <= LE; ++a2i) {
+            const int q = jj - a2i;
+            if (q >= 0 && q <= KM) D[a2i] = cadd(D[a2i], cscale(g, rr[q]));
+          }
+        }
+        // gamma^(2j-1) Delta_j = (2 eta / k)^(2j) D_j / gamma; the (2 eta / k)^(2j) is in s1u
+        const qg_c rg = crecip(gam);
+#pragma unroll
+        for (int a2i = 0; a2i <= LE; ++a2i) D[a2i] = cmul(D[a2i], rg);
+      }
+      qg_c tpow[LE + 1];
+      tpow[0] = cmk(1, 0);
+      const qg_c tk = cscale(rk, rb);
+#pragma unroll
+      for (int p = 1; p <= LE; ++p) tpow[p] = cmul(tpow[p - 1], tk);
+      double sK, cK;
+      sincos(Kx * u.sx + Ky * u.sy, &sK, &cK);
+      const qg_c phasefac = cmul(cmk(cK, sK), lrfac);
+      const qg_c e1 = rb > 0 ? cmk(qx / rb, qy / rb) : cmk(1.0, 0.0);
+      qg_c em = cmk(1.0, 0.0);
+#pragma unroll
+      for (int mu = 0; mu <= LE; ++mu) {
+        if (mu > 0) em = cmul(em, e1);
+        const qg_c emp = cmul(em, phasefac), emn = cmul(cconj(em), phasefac);
+#pragma unroll
+        for (int n = mu; n <= LE; ++n) {
+#pragma unroll
+          for (int sg = 0; sg < 2; ++sg) {
+            if (sg == 1 && mu == 0) continue;
+            const int m = sg ? -mu : mu, y = n * (n + 1) + m;
+            if (y < Y0 || y >= Y0 + NY) continue;
+            const int LM = n - mu;
+            int e = c_ew.zoff[y];
+            qg_c js = cmk(0, 0);
+#pragma unroll
+            for (int jq = 0; jq <= LM; ++jq)
+#pragma unroll
+              for (int sv = jq + (LM - jq) % 2; sv <= 2 * jq && sv <= LM; sv += 2) {
+                js = cadd(js, cmul(cmul(s1u[e], tpow[n - sv]), D[jq]));
+                ++e;
+              }
+            acc[y - Y0] = cadd(acc[y - Y0], cmul(js, sg ? emn : emp));
+          }
+        }
+      }
+    }
+  }
+  // ---------------- reduction into sig[Y0 .. Y0 + NY) ----------------
+#pragma unroll
+  for (int i = 0; i < NY; ++i) {
+    double re = acc[i].re, im = acc[i].im;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) red[warp][i] = cmk(re, im);
+  }
+  __syncthreads();
+  if (tid < NY) {
+    qg_c v = cmk(0, 0);
+    for (int wq = 0; wq < kEThreads / 32; ++wq) v = cadd(v, red[wq][tid]);
+    sig[Y0 + tid] = v;
+  }
+  __syncthreads();
+}
+
+template <int LMAX, int Y0>
+__device__ __forceinline__ void shifted_passes(const ZUnit &u, const qg_c *s1u, const double *rr, qg_c *sig,
+                                               qg_c (*red)[EwShape<LMAX>::RED], int *errflag) {
+  constexpr int S = EwShape<LMAX>::S, ZP = EwShape<LMAX>::ZP;
+  constexpr int NY = (S - Y0 < ZP) ? S - Y0 : ZP;
+  shifted_pass<LMAX, Y0, NY>(u, s1u, rr, sig, red, errflag);
+  if constexpr (Y0 + NY < S) shifted_passes<LMAX, Y0 + NY>(u, s1u, rr, sig, red, errflag);
+}
+
+// M[R, C] = delta_RC I - T_R W(R <- C) from sigma in shared memory
+// (translations.c:926-1078 contraction; the B sum runs over q <= qmax_A).
+template <int LMAX>
+__device__ __forceinline__ void contract_block(const EwaldArgs &a, const TransDevTables &T, const qg_c *sig,
+                                               size_t wk, size_t per, int pr, int R, int C, int iw) {
+  using Sh = EwShape<LMAX>;
+  constexpr int NE = Sh::NE, NE2 = Sh::NE2, NB = Sh::NB;
+  const int tid = threadIdx.x;
+  const size_t N = (size_t)a.np * NB;
+  // full matrix: block (R, C) of the N x N matrix wk; pair list: block pr alone (ld NB)
+  qg_c *M = a.npairs ? a.M + (wk * per + pr) * NB * NB : a.M + wk * N * N;
+  const size_t ldm = a.npairs ? (size_t)NB : N;
+  const size_t row0 = a.npairs ? 0 : (size_t)R * NB, col0 = a.npairs ? 0 : (size_t)C * NB;
+  const qg_c *TR = a.T + ((size_t)iw * a.ntm + a.tmid[R]) * NB;
+#pragma unroll 1
+  for (int which = 0; which < 2; ++which) {
+    const uint8_t *cnt = which ? T.cntBe : T.cntA;
+    const double *coef = which ? T.coefB : T.coefA;
+    const uint16_t *slot = which ? T.slotB : T.slotA;
+    const int32_t *perm = which ? T.permB : T.perm;
+    for (int kx = tid; kx < NE2; kx += kEThreads) {
+      const int c = cnt[kx];
+      double sr = 0, si = 0;
+      for (int q = 0; q < c; ++q) {
+        const double cf = __ldg(coef + q * NE2 + kx);
+        const qg_c x = sig[__ldg(slot + q * NE2 + kx)];
+        sr = fma(cf, x.re, sr);
+        si = fma(cf, x.im, si);
+      }
+      const qg_c v = which ? cmk(-si, sr) : cmk(sr, si);
+      const int e = __ldg(perm + kx);
+      const int yi = e / NE, yj = e - yi * NE;
+      const int r1 = yi, c1 = which ? NE + yj : yj;
+      const int r2 = NE + yi, c2 = which ? yj : NE + yj;
+      const qg_c m1 = cscale(cmul(TR[r1], v), -1.0), m2 = cscale(cmul(TR[r2], v), -1.0);
+      M[(row0 + r1) * ldm + col0 + c1] = (R == C && r1 == c1) ? cadd(m1, cmk(1, 0)) : m1;
+      M[(row0 + r2) * ldm + col0 + c2] = (R == C && r2 == c2) ? cadd(m2, cmk(1, 0)) : m2;
+    }
+  }
+  __syncthreads();
+}
+
 template <int LMAX>
 __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, TransDevTables T) {
   using Sh = EwShape<LMAX>;
-  constexpr int LE = Sh::LE, S = Sh::S, NE = Sh::NE, NE2 = Sh::NE2, NB = Sh::NB, NEV = Sh::NEVEN;
+  constexpr int LE = Sh::LE, S = Sh::S, NEV = Sh::NEVEN;
   __shared__ qg_c sig[S];
-  __shared__ qg_c red[kEThreads / 32][NEV];
+  __shared__ qg_c red[kEThreads / 32][Sh::RED];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int np = a.np;
   const size_t per = a.npairs ? (size_t)a.npairs : (size_t)np * np;  // blocks per matrix
   const size_t units = (size_t)a.nw * a.nk * per;
-  const size_t N = (size_t)np * NB;
   for (size_t u = blockIdx.x; u < units; u += gridDim.x) {
     const int pr = (int)(u % per);
     const size_t wk = u / per;
@@ -138,6 +467,12 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
     const double eta = a.eta[wk];
     const double bx = a.beta[2 * ik], by = a.beta[2 * ik + 1];
     const double sx = a.pos[3 * R] - a.pos[3 * C], sy = a.pos[3 * R + 1] - a.pos[3 * C + 1];
+    const double sz = a.pos[3 * R + 2] - a.pos[3 * C + 2];
+    if (sz != 0.0) {
+      // a pair of layers: ewald_layers_kernel forms it (launched when a.layered)
+      if (!a.layered && tid == 0) atomicOr(a.err, 2);
+      continue;
+    }
     const bool self = (sx == 0.0 && sy == 0.0);
     const bool kreal = (k.im == 0.0);
     qg_c acc[NEV];
@@ -348,37 +683,85 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
       sig[0] = cadd(sig[0], cscale(G[1], 1.0 / (2 * 1.7724538509055160273)));
     }
     __syncthreads();
-    // ---------------- contraction into the M block ----------------
-    // full matrix: block (R, C) of the N x N matrix wk; pair list: block pr alone (ld NB)
-    qg_c *M = a.npairs ? a.M + (wk * per + pr) * NB * NB : a.M + wk * N * N;
-    const size_t ldm = a.npairs ? (size_t)NB : N;
-    const size_t row0 = a.npairs ? 0 : (size_t)R * NB, col0 = a.npairs ? 0 : (size_t)C * NB;
-    const qg_c *TR = a.T + ((size_t)iw * a.ntm + a.tmid[R]) * NB;
-#pragma unroll 1
-    for (int which = 0; which < 2; ++which) {
-      const uint8_t *cnt = which ? T.cntBe : T.cntA;
-      const double *coef = which ? T.coefB : T.coefA;
-      const uint16_t *slot = which ? T.slotB : T.slotA;
-      const int32_t *perm = which ? T.permB : T.perm;
-      for (int kx = tid; kx < NE2; kx += kEThreads) {
-        const int c = cnt[kx];
-        double sr = 0, si = 0;
-        for (int q = 0; q < c; ++q) {
-          const double cf = __ldg(coef + q * NE2 + kx);
-          const qg_c x = sig[__ldg(slot + q * NE2 + kx)];
-          sr = fma(cf, x.re, sr);
-          si = fma(cf, x.im, si);
-        }
-        const qg_c v = which ? cmk(-si, sr) : cmk(sr, si);
-        const int e = __ldg(perm + kx);
-        const int yi = e / NE, yj = e - yi * NE;
-        const int r1 = yi, c1 = which ? NE + yj : yj;
-        const int r2 = NE + yi, c2 = which ? yj : NE + yj;
-        const qg_c m1 = cscale(cmul(TR[r1], v), -1.0), m2 = cscale(cmul(TR[r2], v), -1.0);
-        M[(row0 + r1) * ldm + col0 + c1] = (R == C && r1 == c1) ? cadd(m1, cmk(1, 0)) : m1;
-        M[(row0 + r2) * ldm + col0 + c2] = (R == C && r2 == c2) ? cadd(m2, cmk(1, 0)) : m2;
+    contract_block<LMAX>(a, T, sig, wk, per, pr, R, C, iw);
+  }
+}
+
+template <int LMAX>
+__global__ void __launch_bounds__(kEThreads) ewald_layers_kernel(EwaldArgs a, TransDevTables T) {
+  using Sh = EwShape<LMAX>;
+  constexpr int S = Sh::S;
+  __shared__ qg_c sig[S];
+  __shared__ qg_c red[kEThreads / 32][Sh::RED];
+  __shared__ qg_c s1u[kEwZ];
+  __shared__ double rr[48];
+  const int tid = threadIdx.x;
+  const int np = a.np;
+  const size_t per = a.npairs ? (size_t)a.npairs : (size_t)np * np;  // blocks per matrix
+  const size_t units = (size_t)a.nw * a.nk * per;
+  for (size_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const int pr = (int)(u % per);
+    const size_t wk = u / per;
+    const int iw = (int)(wk / a.nk), ik = a.paired ? iw : (int)(wk % a.nk);
+    const int R = a.npairs ? a.pairs[2 * pr] : pr / np;
+    const int C = a.npairs ? a.pairs[2 * pr + 1] : pr - R * np;
+    const qg_c k = a.k[iw];
+    const double eta = a.eta[wk];
+    const double bx = a.beta[2 * ik], by = a.beta[2 * ik + 1];
+    const double sx = a.pos[3 * R] - a.pos[3 * C], sy = a.pos[3 * R + 1] - a.pos[3 * C + 1];
+    const double sz = a.pos[3 * R + 2] - a.pos[3 * C + 2];
+    if (sz == 0.0) continue;  // ewald_assemble_kernel
+    // ---------------- layers at different heights ----------------
+    ZUnit zu;
+    zu.k = k;
+    zu.w = -sz;
+    // distant layers (|k sz| >= 2.5): the pure reciprocal-lattice sum; else
+    // eta <= 1 / |sz| for the Delta series, which keeps k / (2 eta) <= 1.25
+    zu.spectral = hypot(k.re, k.im) * fabs(sz) >= 2.5;
+    zu.eta = fmin(eta, 1.0 / fabs(sz));
+    zu.bx = bx;
+    zu.by = by;
+    zu.sx = sx;
+    zu.sy = sy;
+    const double x2e = sz * sz * zu.eta * zu.eta;
+    {
+      int q = 0;
+      double tq = 1.0;
+      while (q < 46 && tq > 1e-18) {
+        ++q;
+        tq *= x2e / q;
+      }
+      zu.KM = q;
+    }
+    if (tid == 0) {
+      double tq = 1.0;
+      for (int q = 0; q <= zu.KM; ++q) {
+        rr[q] = tq;
+        tq *= -x2e / (q + 1);
       }
     }
+    {
+      // Ewald: S1 (k w)^(2j - s) (2 eta / k)^(2j);
+      // reciprocal-lattice sum: S1 sqrt(pi) 2^j sgn(w)^s (k |w|)^(j - s)
+      const qg_c kw = cscale(k, zu.w), te = cscale(crecip(k), 2 * zu.eta);
+      const qg_c te2 = cmul(te, te);
+      const qg_c rkaw = crecip(cscale(k, fabs(zu.w)));
+      for (int e = tid; e < c_ew.zoff[S]; e += kEThreads) {
+        const int jq = c_ew.zj[e], sv = c_ew.zsv[e];
+        qg_c f = c_ew.zs1[e];
+        if (zu.spectral) {
+          f = cscale(f, 1.7724538509055160273 * (double)(1 << jq) * ((zu.w < 0 && (sv & 1)) ? -1.0 : 1.0));
+          for (int q = 0; q < sv - jq; ++q) f = cmul(f, rkaw);
+        } else {
+          for (int q = 0; q < 2 * jq - sv; ++q) f = cmul(f, kw);
+          for (int q = 0; q < jq; ++q) f = cmul(f, te2);
+        }
+        s1u[e] = f;
+      }
+    }
+    __syncthreads();
+    shifted_passes<LMAX, 0>(zu, s1u, rr, sig, red, a.err);
+    contract_block<LMAX>(a, T, sig, wk, per, pr, R, C, iw);
     __syncthreads();
   }
 }
@@ -394,6 +777,11 @@ int launch_ew(const EwaldArgs &a, const TransDevTables &T, cudaStream_t st) {
   ewald_assemble_kernel<LMAX><<<(unsigned)grid, kEThreads, 0, st>>>(a, T);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(1);
+  if (a.layered) {
+    ewald_layers_kernel<LMAX><<<(unsigned)grid, kEThreads, 0, st>>>(a, T);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+  }
   return QPMS_SUCCESS;
 }
 

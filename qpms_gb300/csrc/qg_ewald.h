@@ -9,6 +9,8 @@ namespace qg {
 // Largest sigma order lMax_e = 2 lMax + 1 compiled (lMax <= 4).
 constexpr int kEwLE = 9;
 constexpr int kEwS = (kEwLE + 1) * (kEwLE + 1);
+// Number of (n, m, j, s) terms of the shifted long-range sum at lMax_e = kEwLE.
+constexpr int kEwZ = 420;
 
 // Lattice- and convention-dependent constants (one lattice at a time).
 struct EwaldConst {
@@ -22,6 +24,15 @@ struct EwaldConst {
   // long-range constants s1_constfacs[y][j] (ewald.c:142-146) times leg0m[y]
   int s1off[kEwS];
   qg_c s1[kEwS * (kEwLE / 2 + 1)];
+  // Pairs of layers at different heights (shift.z != 0):
+  // sign factors of leg_nm(x) = legs[y] P_n^|m|(x) with the Condon-Shortley
+  // phase in P (m1pow_m_neg(m), and (-1)^m for csphase +1)
+  double legs[kEwS];
+  // long-range constants S1[y][j, s] (derived for the shifted sum; entries
+  // zoff[y] .. zoff[y + 1] - 1 in (j, s) order) with their j and s
+  int zoff[kEwS + 1];
+  qg_c zs1[kEwZ];
+  unsigned char zj[kEwZ], zsv[kEwZ];
 };
 
 struct EwaldArgs {
@@ -33,13 +44,17 @@ struct EwaldArgs {
   const double *beta;  // [nk][2] Bloch vectors
   const double *eta;   // [nw * nk] Ewald parameters
   qg_c *M;             // [nw * nk][N][N]
-  int *err;            // set to 1 if a unit's lattice-point range exceeded the bound
+  int *err;            // bit 1: a unit's lattice-point range exceeded the bound
   int paired = 0;      // 1: nk == 1 and matrix w uses Bloch vector beta[w] (a list of (omega, k) pairs)
   // Optional list of particle pairs (R, C): only those blocks are formed,
   // block p of matrix wk at M + (wk * npairs + p) * NB * NB (row-major NB x NB)
   // instead of the full N x N matrices.
   int npairs = 0;
   const int *pairs = nullptr;  // [npairs][2]
+  // 1: some pair lies in different planes (z_R != z_C); those blocks are
+  // formed by a second kernel.  A pair with z_R != z_C and layered == 0 sets
+  // bit 2 of *err.
+  int layered = 0;
 };
 
 // Bound on the lattice points one unit may enumerate per sum.

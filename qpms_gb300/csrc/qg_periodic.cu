@@ -92,8 +92,67 @@ int build_ewald_const(const qpms_scatsys_t *ss, int lMax, EwaldConst *c, int csp
         off += (n - am) / 2 + 1;
       }
     }
+  // shifted layers: leg_nm sign factors and the S1[y][j, s] constants
+  //   S1 = -i (-1)^n 2 sqrt(pi) L_nm (-i)^mu c_t (-1)^(t+s) H_{s, s-j} 2^-s
+  // (mu = |m|, t = (n - mu - s) / 2, H_{s,l} = s! (-1)^l / (l! (s - 2l)!),
+  // r^n P_n^mu(cos theta) = rho^mu sum_t c_t rho^(2t) z^(n - mu - 2t) without
+  // the Condon-Shortley phase, L_nm = legs[y] (-1)^mu): the Gaussian-regularised
+  // h_n Y_nm summed over the lattice by 2D Poisson summation, z derivatives as
+  // Hermite polynomials.  At z = 0 only 2j = s remains and equals s1 above.
+  int zo = 0;
+  for (int n = 0; n <= LE; ++n)
+    for (int m = -n; m <= n; ++m) {
+      const int y = n * (n + 1) + m, mu = m < 0 ? -m : m, LM = n - mu;
+      const double msgn = (m < 0 && (m % 2)) ? -1.0 : 1.0;
+      c->legs[y] = msgn * ((csphase == -1 || (mu % 2) == 0) ? 1.0 : -1.0);
+      const double L = c->legs[y] * ((mu % 2) ? -1.0 : 1.0);
+      // -i (-1)^n (-i)^mu = (-i)^(mu + 1) (-1)^n
+      static const double mi[4][2] = {{1, 0}, {0, -1}, {-1, 0}, {0, 1}};  // (-i)^p
+      const double *ph = mi[(mu + 1) % 4];
+      const double pre = ((n % 2) ? -1.0 : 1.0) * 2 * 1.7724538509055160273 * L;
+      c->zoff[y] = zo;
+      for (int j = 0; j <= LM; ++j)
+        for (int sv = j + (LM - j) % 2; sv <= 2 * j && sv <= LM; sv += 2) {
+          const int t = (LM - sv) / 2, l = sv - j;
+          double ct = 0;
+          for (int kk = t; kk <= LM / 2; ++kk)
+            ct += ldexp(1.0, -n) * ((kk % 2) ? -1.0 : 1.0) * fact(n) / (fact(kk) * fact(n - kk)) *
+                  fact(2 * n - 2 * kk) / (fact(n) * fact(n - 2 * kk)) * fact(n - 2 * kk) / fact(n - 2 * kk - mu) *
+                  fact(kk) / (fact(t) * fact(kk - t));
+          const double h = fact(sv) * ((l % 2) ? -1.0 : 1.0) / (fact(l) * fact(sv - 2 * l));
+          const double v = pre * ct * (((t + sv) % 2) ? -1.0 : 1.0) * h * ldexp(1.0, -sv);
+          if (zo >= kEwZ) {
+            set_error("shifted Ewald constants: table overflow");
+            return QPMS_ERROR;
+          }
+          c->zs1[zo] = cmk(v * ph[0], v * ph[1]);
+          c->zj[zo] = (unsigned char)j;
+          c->zsv[zo] = (unsigned char)sv;
+          ++zo;
+        }
+    }
+  c->zoff[(LE + 1) * (LE + 1)] = zo;
   return QPMS_SUCCESS;
 }
+
+// 1 if the np positions (x, y, z) do not all lie in one plane z = const:
+// the Ewald assembly then also runs its kernel for pairs of layers.
+int layered_positions(const double *pos, size_t np) {
+  for (size_t i = 1; i < np; ++i)
+    if (pos[3 * i + 2] != pos[2]) return 1;
+  return 0;
+}
+
+}  // namespace
+
+// layered_positions for the particles of ss
+int layered_system(const qpms_scatsys_t *ss) {
+  for (qpms_ss_pi_t i = 1; i < ss->p_count; ++i)
+    if (ss->p[i].pos.z != ss->p[0].pos.z) return 1;
+  return 0;
+}
+
+namespace {
 
 // log|det| of nb row-major N x N LU factors (column-major getrf of M^T has
 // the same diagonal of U)
@@ -131,6 +190,10 @@ int ewald_assemble_locked(const qpms_scatsys_t *ss, const EwaldArgs &a, cudaStre
   int herr = 0;
   QG_CUDA_TRY(cudaMemcpyAsync(&herr, a.err, 4, cudaMemcpyDeviceToHost, st));
   QG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr & 2) {
+    set_error("Ewald sum: pair of layers at different heights without the layered flag");
+    return QPMS_ERROR;
+  }
   if (herr) {
     set_error("Ewald sum: lattice-point range above the bound (wavenumber or eta out of range)");
     return QPMS_ERROR;
@@ -241,10 +304,6 @@ int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_hos
     pos[3 * i + 1] = ss->p[i].pos.y;
     pos[3 * i + 2] = ss->p[i].pos.z;
     tm[i] = ss->p[i].tmatrix_id;
-    if (ss->p[i].pos.z != ss->p[0].pos.z) {
-      set_error("particles must share one z plane (xy lattice sums)");
-      return QPMS_EINVAL;
-    }
   }
   // the Ewald parameter sets how many lattice points each sum visits
   for (size_t i = 0; i < (size_t)nw * nk; ++i)
@@ -276,6 +335,7 @@ int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_hos
   a.eta = deta.as<double>();
   a.M = dM;
   a.err = derr.as<int>();
+  a.layered = layered_positions(pos.data(), np);
   const int n = (int)(ss->fecv_size / np);
   if (T_host.size() == (size_t)nw * ss->tm_count * n * n && n > 1) return ewald_assemble_dense(ss, a, n, st);
   return ewald_assemble_locked(ss, a, st);
@@ -287,7 +347,7 @@ using namespace qg;
 
 namespace qg {
 namespace {
-// Field of a 2D-periodic array at in-plane points from the lattice-summed
+// Field of a 2D-periodic array at points from the lattice-summed
 // blocks W(point <- particle) (pair-list Ewald assembly with T = -1, so a
 // block is W itself): a = sum_p W_qp f_p, of which only the electric l = 1
 // regular waves are non-zero at the point itself; E = sum_m a_(N,1,m) D_m with
@@ -342,20 +402,12 @@ void regular_dipoles_at_origin(qg_c *D) {
   }
 }
 
-// E at npts in-plane points (host where / E), lattice sums at (k, beta, eta).
+// E at npts points (host where / E), lattice sums at (k, beta, eta); points
+// off the particles' plane use the sums for layers at different heights.
 int periodic_field(const qpms_scatsys_t *ss, qg_c k, const double beta[2], double eta, const qg_c *cvf_host,
                    size_t npts, const double *where, qg_c *E_host) {
   const int np = ss->p_count;
   const int n = (int)(ss->fecv_size / np);
-  const double z0 = ss->p[0].pos.z;
-  for (int i = 0; i < np; ++i)
-    if (ss->p[i].pos.z != z0) { set_error("particles must share one z plane"); return QPMS_EINVAL; }
-  for (size_t q = 0; q < npts; ++q)
-    if (where[3 * q + 2] != z0) {
-      set_error("periodic field: points must lie in the particles' plane z = %g (off-plane points need the "
-                "shifted-layer lattice sums)", z0);
-      return QPMS_EINVAL;
-    }
   if (!(eta >= 0.05 * ss->per.eta && eta <= 50 * ss->per.eta)) {
     set_error("Ewald eta %g outside [0.05, 50] x the lattice default %g", eta, ss->per.eta);
     return QPMS_EINVAL;
@@ -413,6 +465,7 @@ int periodic_field(const qpms_scatsys_t *ss, qg_c k, const double beta[2], doubl
     a.err = derr.as<int>();
     a.npairs = (int)(m * np);
     a.pairs = dpairs.as<int>();
+    a.layered = layered_positions(pos.data(), np + m);
     if ((e = ewald_assemble_locked(ss, a, 0))) return e;
     periodic_field_kernel<<<(unsigned)m, 128>>>((int)m, np, n, dW.as<qg_c>(), df.as<qg_c>(), dD.as<qg_c>(),
                                                 dE.as<qg_c>());
@@ -621,9 +674,8 @@ int qpms_trans_calculator_get_AB_arrays_e32_e(const qpms_trans_calculator *c, qp
   clear_error();
   if (!c || !Adest || !Bdest) { set_error("NULL argument"); return QPMS_EINVAL; }
   if (parts != 7) { set_error("only the full Ewald sum (QPMS_EWALD_FULL) is implemented"); return QPMS_EINVAL; }
-  if (particle_shift.z != 0) { set_error("particle shift must lie in the lattice plane"); return QPMS_EINVAL; }
   if (c->lMax > 4) { set_error("lattice sums need lMax <= 4"); return QPMS_EINVAL; }
-  const double pos[6] = {particle_shift.x, particle_shift.y, 0, 0, 0, 0};
+  const double pos[6] = {particle_shift.x, particle_shift.y, particle_shift.z, 0, 0, 0};
   const int kind[2] = {0, 0};
   const double rad = 1.0;
   qpms_complex_t eps_in, eps_med;

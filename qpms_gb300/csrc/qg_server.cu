@@ -52,6 +52,7 @@ void planewave_direction_coeffs(int lMax, const double k_dir[3], const qpms_comp
 int blas_handle_get(cublasHandle_t *h);
 int ewald_assemble_locked(const qpms_scatsys_t *ss, const EwaldArgs &a, cudaStream_t st);
 int ewald_assemble_dense(const qpms_scatsys_t *ss, const EwaldArgs &a, int n, cudaStream_t st);
+int layered_system(const qpms_scatsys_t *ss);
 }  // namespace qg
 
 using namespace qg;
@@ -477,6 +478,7 @@ struct qpms_gpu_server {
     a.eta = deta;
     a.M = dM;
     a.err = derr;
+    a.layered = layered_system(ss);
     if (scatsys_dense(ss)) return ewald_assemble_dense(ss, a, (int)(ss->fecv_size / ss->p_count), st);
     return ewald_assemble_locked(ss, a, st);
   }

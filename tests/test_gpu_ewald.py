@@ -128,12 +128,20 @@ def test_dispersion_scan_vs_oracle(gpu, orc, lat, mode):
 
 
 @pytest.mark.parametrize("norm", [65536 | 8, 65536, 65536 * 3 | 8])
-@pytest.mark.parametrize("k,beta,shift", [(2.3, (2.7, 1.0), (0.5, 0.1325)), (2.3 + 0.1j, (2.7, 1.0), (0.0, 0.0)),
-                                          (2.3 - 0.1j, (0.3, -0.2), (0.25, 0.4))])
+@pytest.mark.parametrize("k,beta,shift", [(2.3, (2.7, 1.0), (0.5, 0.1325, 0.0)),
+                                          (2.3 + 0.1j, (2.7, 1.0), (0.0, 0.0, 0.0)),
+                                          (2.3 - 0.1j, (0.3, -0.2), (0.25, 0.4, 0.0)),
+                                          # layers at different heights
+                                          (2.3, (2.7, 1.0), (0.5, 0.1325, 0.3)),
+                                          (2.3 + 0.1j, (0.3, -0.2), (0.0, 0.0, -0.45)),
+                                          # |k z| >= 2.5: the reciprocal-lattice sum
+                                          (5.3, (0.7, -0.4), (0.2, 0.5, -0.8)),
+                                          (2.3 + 0.1j, (0.3, -0.2), (0.1, 0.3, 1.7))])
 def test_AB_arrays_e32_vs_oracle(gpu, orc, norm, k, beta, shift):
     """qpms_trans_calculator_get_AB_arrays_e32 (unit square lattice, lMax 3,
     eta 1.6: the reference's eta-invariance parameter sets) against the oracle,
-    for several normalisations (csphase on and off)."""
+    for several normalisations (csphase on and off); particle_shift.z != 0
+    takes the shifted-layer sums."""
     import ctypes as C
 
     class Cplx(C.Structure):
@@ -157,9 +165,40 @@ def test_AB_arrays_e32_vs_oracle(gpu, orc, norm, k, beta, shift):
     B = np.zeros((ne, ne), dtype=np.complex128)
     kc = complex(k)
     rc = f(calc.c, A.ctypes.data, None, B.ctypes.data, None, ne, 1, 1.6, Cplx(kc.real, kc.imag), Cart2(1, 0),
-           Cart2(0, 1), Cart2(*beta), Cart3(shift[0], shift[1], 0.0), 20.0, 160.0)
+           Cart2(0, 1), Cart2(*beta), Cart3(*shift), 20.0, 160.0)
     assert rc == 0, gpu.last_error()
     oc = orc.TransCalculator(lMax, norm)
     Ao, Bo = orc.get_AB_arrays_e32(oc, 1.6, kc, (1, 0), (0, 1), beta, shift, 20, 160)
     assert np.linalg.norm(A - Ao) <= 1e-11 * np.linalg.norm(Ao)
     assert np.linalg.norm(B - Bo) <= 1e-11 * np.linalg.norm(Bo)
+
+
+LAYERED = [  # positions in units of the square lattice constant 580 nm
+    ((0, 0, 0), (0.5, 0.3, 0.4)),
+    ((0, 0, 0), (0, 0, 0.35)),                     # second layer straight above (rho = 0 branch)
+    ((0, 0, 0), (0.5, 0.5, 0.25), (0.1, -0.2, -0.3)),
+]
+
+
+@pytest.mark.parametrize("cell", LAYERED)
+@pytest.mark.parametrize("E,kv", [(1.9, (0.0, 0.0)), (2.3, (4e6, -2e6)), (2.1 + 0.03j, (2e6, 1e6))])
+def test_layered_lattice_M_vs_oracle(gpu, orc, cell, E, kv):
+    """Particles of a square lattice at different heights (a bilayer and a
+    three-layer cell): the pairs of layers go through the shifted-layer Ewald
+    sums.  Same tolerances as the single-plane lattices."""
+    lMax = 2
+    a = 580e-9
+    b1, b2 = (a, 0.0), (0.0, a)
+    pos = np.array(cell, dtype=float) * a
+    ss = gpu.ScatteringSystem(pos, RAD, EPS_I, EPS_E, lMax, lattice=(b1, b2))
+    om = E * EV / HBAR
+    ke = np.sqrt(EPS_E) * om / C0
+    eta = ss.adjusted_eta(ke, kv)
+    M = ss(om).modeproblem_matrix_full(k=kv)
+    O = _oracle_M(orc, lMax, pos, b1, b2, om, kv, eta)
+    I = np.eye(len(M))
+    assert np.linalg.norm(M - O) <= 1e-10 * np.linalg.norm(O)
+    assert np.linalg.norm(M - O) <= 1e-9 * np.linalg.norm(O - I), np.linalg.norm(M - O) / np.linalg.norm(O - I)
+    # the sums do not depend on eta (the kernel lowers eta for distant layers)
+    M2 = ss(om).modeproblem_matrix_full(k=kv, eta=0.7 * eta)
+    assert np.linalg.norm(M2 - M) <= 1e-9 * np.linalg.norm(M - I)

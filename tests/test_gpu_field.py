@@ -163,7 +163,8 @@ def test_errors(gpu):
 
 
 def test_periodic_field_vs_oracle(gpu, orc):
-    """Field of a 2D lattice at in-plane points (qpms_scatsyswk_scattered_E):
+    """Field of a 2D lattice at points in and off the particles' plane
+    (qpms_scatsyswk_scattered_E; off-plane points use the shifted-layer sums):
     the lattice-summed translation W(point <- particle) applied to f, of which
     the regular electric dipole waves give the field at the point.  Oracle:
     the same blocks from its Ewald mode-problem builder with the point as an
@@ -179,8 +180,9 @@ def test_periodic_field_vs_oracle(gpu, orc):
     kv = np.array([kxy[0], kxy[1], 0.0])
     rng = np.random.default_rng(17)
     f = rng.normal(size=ss.fecv_size) + 1j * rng.normal(size=ss.fecv_size)
-    pts = np.zeros((12, 3))
-    pts[:, :2] = rng.uniform(-700e-9, 700e-9, size=(12, 2))
+    pts = np.zeros((16, 3))
+    pts[:, :2] = rng.uniform(-700e-9, 700e-9, size=(16, 2))
+    pts[12:, 2] = [150e-9, -90e-9, 400e-9, -1e-6]                 # off the particles' plane
     eta = orc.adjusted_eta(abs(b1[0] * b2[1] - b1[1] * b2[0]), k, kv, lMax)
     E = ss(om).scattered_E(f, pts, k=kxy, eta=eta)
     calc = orc.TransCalculator(lMax)
@@ -192,8 +194,6 @@ def test_periodic_field_vs_oracle(gpu, orc):
         a = sum(X[2 * n:3 * n, p * n:(p + 1) * n] @ f[p * n:(p + 1) * n] for p in range(2))
         ref = orc.scattered_E(lMax, r[None, :], 1, k, a, r[None, :])[0]
         assert np.linalg.norm(E[q] - ref) <= 1e-9 * np.linalg.norm(ref), (q, E[q], ref)
-    # the single-point reference form and the errors
-    with pytest.raises(QpmsGpuError):
-        ss(om).scattered_E(f, np.array([[0, 0, 1e-7]]), k=kxy)       # off the particles' plane
+    # the errors
     with pytest.raises(QpmsGpuError):
         ss(om).scattered_E(f, pts[:1], k=kxy, btyp=1)                 # Hankel waves only

@@ -111,3 +111,23 @@ def test_shifted_limit_and_parity(orc):
     sc = np.abs(p).max()
     assert np.abs(p[~odd] - q[~odd]).max() <= 1e-13 * sc
     assert np.abs(p[odd] + q[odd]).max() <= 1e-13 * sc and np.abs(p[odd]).max() > 1e-3 * sc
+
+
+@pytest.mark.parametrize("k,shift", [(3.0 + 1.0j, (0.5, 0.55, -1.2)), (4.1 + 0.5j, (0.1, 0.2, 0.9)),
+                                     (9.0 + 1.0j, (0.3, 0.1, -0.5))])
+def test_spectral_vs_direct_sum(orc, k, shift):
+    """Distant layers: the pure reciprocal-lattice (Weyl) sum, the eta -> inf
+    limit of the shifted sums with Delta_j(0, z) from half-integer Bessel K,
+    against the direct lattice sum."""
+    d = orc.sigma_direct(5, k, *OBLIQUE, (0.7, -0.4), shift, 90)
+    sp = orc.ewald_sigma_xy(5, np.inf, k, *OBLIQUE, (0.7, -0.4), shift, 20, 160)[0]
+    assert np.abs(d - sp).max() <= 1e-13 * np.abs(d).max()
+
+
+@pytest.mark.parametrize("k,shift", [(3.0, (0.5, 0.55, -1.2)), (5.3, (0.2, 0.5, -0.8)), (4.0 - 0.1j, (0.3, 0.1, 0.7))])
+def test_spectral_vs_ewald_real_k(orc, k, shift):
+    """Real k (propagating orders: the outgoing branch e^{i k_z |z|}): the
+    reciprocal-lattice sum against the Ewald sums at eta |z| = 1."""
+    ew = orc.ewald_sigma_xy(5, 1.0 / abs(shift[2]), k, *OBLIQUE, (0.7, -0.4), shift, 30, 160)[0]
+    sp = orc.ewald_sigma_xy(5, np.inf, k, *OBLIQUE, (0.7, -0.4), shift, 20, 160)[0]
+    assert np.abs(ew - sp).max() <= 1e-12 * np.abs(ew).max()
