@@ -316,6 +316,7 @@ void qpms_permittivity_interpolator_free(qpms_permittivity_interpolator_t *inter
 qpms_complex_t qpms_permittivity_interpolator_eps_at_omega(                               /* materials.h:128-131 */
     const qpms_permittivity_interpolator_t *interp, double omega_SI);
 qpms_epsmu_t qpms_permittivity_interpolator_epsmu_g(qpms_complex_t omega, const void *interp);  /* materials.h:133-139 */
+qpms_epsmu_t qpms_epsmu_const_g(qpms_complex_t omega, const void *epsmu);                     /* materials.h:36-38 */
 double qpms_permittivity_interpolator_omega_min(const qpms_permittivity_interpolator_t *ip);
 double qpms_permittivity_interpolator_omega_max(const qpms_permittivity_interpolator_t *ip);
 
@@ -345,6 +346,66 @@ int qpms_gpu_tmatrix_interpolator_eval_batch(const qpms_tmatrix_interpolator_t *
  * basis is missing for some frequency. */
 int qpms_load_scuff_tmatrix(const char *path, const qpms_vswf_set_spec_t *bs, size_t *n, double **freqs,
     double **freqs_su, qpms_tmatrix_t **tmatrices_array, qpms_complex_t **tmdata);
+
+/* ---- T-matrices of axially symmetric particles (tmatrices.h:415-523) ----
+ * Extended-boundary-condition method on the GPU: one CTA per (frequency, m)
+ * integrates the Q and R blocks over composite Gauss-Legendre panels (broken
+ * at the cylinder rims) and solves T = -R Q^-1 per m block; lMax_extend
+ * (the internal basis, >= bspec lMax) up to 12.  The reference integrates each
+ * entry by adaptive quadrature and warns that its results lose accuracy above
+ * l = 1 (tmatrices.h:455-460); these reproduce the Mie T-matrix of a sphere to
+ * double precision at every l. */
+typedef struct qpms_arc_function_retval_t {                          /* tmatrices.h:415-419 */
+  double r;     /* distance from the origin */
+  double beta;  /* angle between the surface normal and the radial direction */
+} qpms_arc_function_retval_t;
+typedef struct qpms_arc_function_t {                                 /* tmatrices.h:421-435 */
+  qpms_arc_function_retval_t (*function)(double theta, const void *params);
+  const void *params;
+} qpms_arc_function_t;
+typedef struct qpms_arc_cylinder_params_t { double R, h; } qpms_arc_cylinder_params_t;  /* tmatrices.h:437-441 */
+/* Spheroid with equatorial semi-axis a and polar (z) semi-axis c (no
+ * counterpart in the reference, which takes it as a user arc function). */
+typedef struct qpms_arc_spheroid_params_t { double a, c; } qpms_arc_spheroid_params_t;
+qpms_arc_function_retval_t qpms_arc_cylinder(double theta, const void *params);  /* tmatrices.h:443-446 */
+qpms_arc_function_retval_t qpms_arc_sphere(double theta, const void *R);          /* tmatrices.h:448-452 */
+qpms_arc_function_retval_t qpms_arc_spheroid(double theta, const void *params);
+/* Bridge for foreign-function callers that cannot return a struct from a
+ * callback (ctypes): params -> {fn, user}, fn(theta, &r, &beta, user).  The
+ * reference's Python layer wraps user arcs in Cython instead
+ * (cytmatrices.pyx:164-168). */
+typedef struct qpms_arc_callback_params_t {
+  void (*fn)(double theta, double *r, double *beta, void *user);
+  void *user;
+} qpms_arc_callback_params_t;
+qpms_arc_function_retval_t qpms_arc_callback(double theta, const void *params);
+typedef struct qpms_tmatrix_generator_axialsym_param_t {             /* tmatrices.h:493-499 */
+  qpms_epsmu_generator_t outside;
+  qpms_epsmu_generator_t inside;
+  qpms_arc_function_t shape;
+  qpms_l_t lMax_extend;
+} qpms_tmatrix_generator_axialsym_param_t;
+/* Replace qpms_tmatrix_axialsym_fill / qpms_tmatrix_axialsym
+ * (tmatrices.h:461-491, tmatrices.c:807-894). */
+int qpms_tmatrix_axialsym_fill(qpms_tmatrix_t *t, qpms_complex_t omega, qpms_epsmu_t outside,
+    qpms_epsmu_t inside, qpms_arc_function_t shape, qpms_l_t lMax_extend);
+qpms_tmatrix_t *qpms_tmatrix_axialsym(const qpms_vswf_set_spec_t *bspec, qpms_complex_t omega,
+    qpms_epsmu_t outside, qpms_epsmu_t inside, qpms_arc_function_t shape, qpms_l_t lMax_extend);
+/* Replaces qpms_tmatrix_generator_axialsym (tmatrices.h:502-506, tmatrices.c:970-976). */
+int qpms_tmatrix_generator_axialsym(qpms_tmatrix_t *t, qpms_complex_t omega, const void *params);
+/* Replace the Q / R debugging fills (tmatrices.h:509-521, tmatrices.c:896-968):
+ * target[i1 + i2 n] (n = 2 lMaxQR (lMaxQR + 2)) of the lMaxQR basis in
+ * normalisation norm, J = QPMS_HANKEL_PLUS for Q, QPMS_BESSEL_REGULAR for R. */
+int qpms_tmatrix_axialsym_RQ_transposed_fill(qpms_complex_t *target, qpms_complex_t omega,
+    qpms_epsmu_t outside, qpms_epsmu_t inside, qpms_arc_function_t shape, qpms_l_t lMaxQR,
+    qpms_normalisation_t norm, qpms_bessel_t J);
+int qpms_tmatrix_generator_axialsym_RQ_transposed_fill(qpms_complex_t *target, qpms_complex_t omega,
+    const qpms_tmatrix_generator_axialsym_param_t *param, qpms_normalisation_t norm, qpms_bessel_t J);
+/* Batch (no counterpart): T of one shape at nw frequencies, outside[w] /
+ * inside[w] the media there, into HOST T_out [nw][bspec->n][bspec->n]. */
+int qpms_gpu_tmatrix_axialsym_batch(const qpms_vswf_set_spec_t *bspec, qpms_l_t lMax_extend,
+    qpms_arc_function_t shape, size_t nw, const qpms_complex_t *omega, const qpms_epsmu_t *outside,
+    const qpms_epsmu_t *inside, qpms_complex_t *T_out);
 
 /* One particle kind of qpms_gpu_scatsys_create. */
 typedef struct qpms_gpu_particle_kind_t {

@@ -14,7 +14,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_ROOT = "/root/reference"
-SOURCES = ["orc_specfunc.c", "orc_trans.c", "orc_ewald.c", "orc_scatsys.c", "orc_interp.c", "orc_lu.c", "orc_beyn.c"]
+SOURCES = ["orc_specfunc.c", "orc_trans.c", "orc_ewald.c", "orc_scatsys.c", "orc_interp.c", "orc_axsym.c", "orc_lu.c", "orc_beyn.c"]
 
 
 def _newer(target, deps):

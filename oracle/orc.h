@@ -108,6 +108,13 @@ int orc_finite_sphere_scatter(const orc_trans_calculator *c, int np, const doubl
 void orc_scattered_E(int lMax, int np, const double *pos, int J, double complex k, const double complex *cvf,
                      int npts, const double *where, double complex *E);
 
+/* ---- axially symmetric particles (orc_axsym.c) ---- */
+/* shape 0 sphere {R}, 1 cylinder {R, h}, 2 spheroid {a, c} */
+void orc_arc(int shape, const double *par, double theta, double *r, double *beta);
+int orc_tmatrix_axialsym(int lMax, int lMaxQR, double complex k, double complex kin, double complex zr, int shape,
+                         const double *par, double rtol, double complex *T, double complex *Qout,
+                         double complex *Rout);
+
 /* ---- interpolation (orc_interp.c) ---- */
 /* kind 0 linear, 1 natural cubic spline; out[q] = S(xq[q]), NaN outside the knots */
 void orc_spline_eval(int kind, int n, const double *x, const double *y, int nq, const double *xq, double *out);

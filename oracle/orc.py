@@ -292,6 +292,10 @@ def _declare_ewald(L):
     L.orc_ewald3_sigma_xy_ri.argtypes = [ci, ci, cd, cd, cd, vp, vp, vp, cd, cd, ci, vp, vp, vp]
     L.orc_get_AB_arrays_e32_ri.restype = ci
     L.orc_get_AB_arrays_e32_ri.argtypes = [vp, vp, vp, cd, cd, cd, vp, vp, vp, cd, cd, ci]
+    L.orc_tmatrix_axialsym_ri.restype = None
+    L.orc_tmatrix_axialsym_ri.argtypes = [ci, ci, vp, ci, vp, cd, vp, vp, vp, vp]
+    L.orc_arc_ri.restype = None
+    L.orc_arc_ri.argtypes = [ci, vp, cd, vp]
     L.orc_sigma_direct_ri.restype = None
     L.orc_sigma_direct_ri.argtypes = [ci, ci, cd, cd, vp, vp, vp, ci, vp]
     L.orc_periodic_modeproblem_ri.restype = ci
@@ -380,3 +384,35 @@ def adjusted_eta(area, wavenumber, kvec, lMax):
     kv[:len(kvec)] = kvec
     w = complex(wavenumber)
     return lib().orc_adjusted_eta(float(area), w.real, w.imag, kv.ctypes.data, int(lMax))
+
+
+SHAPES = {"sphere": 0, "cylinder": 1, "spheroid": 2}
+
+
+def tmatrix_axialsym(lMax, k, kin, shape, par, lMaxQR=None, zr=None, rtol=1e-10, want_QR=False):
+    """T-matrix (default normalisation, bspec order) of an axially symmetric
+    particle by the extended-boundary-condition method; zr = z / z_in defaults
+    to kin / k (non-magnetic media).  Optionally Q, R at lMaxQR."""
+    L = lib()
+    lq = max(lMax, lMaxQR or lMax)
+    n, nq = 2 * lMax * (lMax + 2), 2 * lq * (lq + 2)
+    T = np.zeros((n, n), dtype=np.complex128)
+    Q = np.zeros((nq, nq), dtype=np.complex128)
+    R = np.zeros((nq, nq), dtype=np.complex128)
+    k, kin = complex(k), complex(kin)
+    zr = complex(kin / k if zr is None else zr)
+    kk = np.array([k.real, k.imag, kin.real, kin.imag, zr.real, zr.imag])
+    pr = np.ascontiguousarray(par, dtype=np.float64)
+    rc = np.zeros(1, dtype=np.int32)
+    L.orc_tmatrix_axialsym_ri(lMax, lq, kk.ctypes.data, SHAPES.get(shape, shape), pr.ctypes.data, float(rtol),
+                              T.ctypes.data, Q.ctypes.data, R.ctypes.data, rc.ctypes.data)
+    if rc[0]:
+        raise ArithmeticError("singular Q block")
+    return (T, Q, R) if want_QR else T
+
+
+def arc(shape, par, theta):
+    out = np.zeros(2)
+    lib().orc_arc_ri(SHAPES.get(shape, shape), np.ascontiguousarray(par, dtype=np.float64).ctypes.data,
+                     float(theta), out.ctypes.data)
+    return tuple(out)

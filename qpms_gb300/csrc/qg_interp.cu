@@ -141,6 +141,12 @@ __global__ void tmi_eval_kernel(int kind, const double *__restrict__ x, int nk, 
   out[idx] = cmk(re, im);
 }
 }  // namespace
+
+// the factor of the wave ui in normalisation norm (other translation units)
+qg_c uvswfi_norm_factor(int norm, qpms_uvswfi_t ui) {
+  const cd f = uvswfi_factor(norm, ui);
+  return cmk(f.real(), f.imag());
+}
 }  // namespace qg
 
 using namespace qg;
@@ -306,6 +312,12 @@ qpms_complex_t qpms_permittivity_interpolator_eps_at_omega(const qpms_permittivi
   r.re = e.real();
   r.im = e.imag();
   return r;
+}
+
+// materials.c:179-181: the constant medium *params as a qpms_epsmu_generator_t
+qpms_epsmu_t qpms_epsmu_const_g(qpms_complex_t omega, const void *epsmu) {
+  (void)omega;
+  return *(const qpms_epsmu_t *)epsmu;
 }
 
 // qpms_epsmu_generator_t form (materials.c:131-142): Im omega is discarded.

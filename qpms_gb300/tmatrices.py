@@ -16,6 +16,30 @@ class _TM(C.Structure):
     _fields_ = [("spec", C.c_void_p), ("m", C.c_void_p), ("owns_m", C.c_bool)]
 
 
+class _Cplx(C.Structure):
+    _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+
+class _EpsMu(C.Structure):
+    _fields_ = [("eps", _Cplx), ("mu", _Cplx)]
+
+
+class _ArcRet(C.Structure):
+    _fields_ = [("r", C.c_double), ("beta", C.c_double)]
+
+
+_ARCCB = C.CFUNCTYPE(None, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p)
+
+
+class _ArcCB(C.Structure):
+    """qpms_arc_callback_params_t"""
+    _fields_ = [("fn", C.c_void_p), ("user", C.c_void_p)]
+
+
+class _Arc(C.Structure):
+    _fields_ = [("function", C.c_void_p), ("params", C.c_void_p)]
+
+
 def declare(L):
     vp, sz, cd, ci = C.c_void_p, C.c_size_t, C.c_double, C.c_int
     L.qpms_vswf_set_spec_from_lMax.restype = vp
@@ -38,6 +62,10 @@ def declare(L):
     L.qpms_tmatrix_interpolator_bspec.argtypes = [vp]
     L.qpms_gpu_tmatrix_interpolator_eval_batch.restype = ci
     L.qpms_gpu_tmatrix_interpolator_eval_batch.argtypes = [vp, sz, vp, vp, vp]
+    L.qpms_gpu_tmatrix_axialsym_batch.restype = ci
+    L.qpms_gpu_tmatrix_axialsym_batch.argtypes = [vp, ci, _Arc, sz, vp, vp, vp, vp]
+    L.qpms_tmatrix_axialsym_RQ_transposed_fill.restype = ci
+    L.qpms_tmatrix_axialsym_RQ_transposed_fill.argtypes = [vp, _Cplx, _EpsMu, _EpsMu, _Arc, ci, ci, ci]
     L.qpms_load_scuff_tmatrix.restype = ci
     L.qpms_load_scuff_tmatrix.argtypes = [C.c_char_p, vp, C.POINTER(sz), C.POINTER(vp), C.POINTER(vp),
                                           C.POINTER(vp), C.POINTER(vp)]
@@ -168,3 +196,118 @@ class TMatrixInterpolator:
     @property
     def omega_table(self):
         return self.freqs.copy()
+
+
+# ---------------- axially symmetric particles ----------------
+
+class ArcFunction:
+    """qpms_arc_function_t (cytmatrices.pyx:149-191): the surface of a particle
+    with C_inf symmetry about z as r(theta) and the angle beta between the
+    surface normal and the radial direction.  The library's sphere and
+    cylinder (as the reference) and spheroid, or a Python callable
+    theta -> (r, beta) (slow: called at every quadrature node)."""
+
+    def __init__(self, function_name=None, params=(), callable_=None):
+        self._L = lib()
+        if callable_ is not None:
+            def _f(theta, r, b, _user):
+                rr, bb = callable_(theta)
+                r[0], b[0] = float(rr), float(bb)
+            self._cb = _ARCCB(_f)
+            self._par = _ArcCB(C.cast(self._cb, C.c_void_p).value, None)
+            self.arc = _Arc(C.cast(self._L.qpms_arc_callback, C.c_void_p).value, C.addressof(self._par))
+        else:
+            self._par = (C.c_double * len(params))(*[float(x) for x in params])
+            fn = getattr(self._L, function_name)
+            self.arc = _Arc(C.cast(fn, C.c_void_p).value, C.addressof(self._par))
+
+    @staticmethod
+    def sphere(r):
+        return ArcFunction("qpms_arc_sphere", (r,))
+
+    @staticmethod
+    def cylinder(r, h):
+        return ArcFunction("qpms_arc_cylinder", (r, h))
+
+    @staticmethod
+    def spheroid(a, c):
+        """Equatorial semi-axis a, polar (z) semi-axis c."""
+        return ArcFunction("qpms_arc_spheroid", (a, c))
+
+    @staticmethod
+    def custom(fn):
+        return ArcFunction(callable_=fn)
+
+
+def _epsmu(medium, omega):
+    """Constant permittivity, (eps, mu), or a callable omega -> eps (the
+    materials models)."""
+    if isinstance(medium, tuple):
+        e, mu = complex(medium[0]), complex(medium[1])
+    elif callable(medium):
+        e, mu = complex(medium(omega.real if isinstance(omega, complex) else omega)), 1.0
+    else:
+        e, mu = complex(medium), 1.0
+    return _EpsMu(_Cplx(e.real, e.imag), _Cplx(mu.real, mu.imag))
+
+
+class TMatrixGenerator:
+    """T-matrices of an axially symmetric particle by the extended-boundary-
+    condition method on the GPU (cytmatrices.pyx:193-384: the axialsym
+    __AxialSymParams generators; sphere_asarc, cylinder).  outside / inside:
+    constant permittivity, (eps, mu) or a materials model."""
+
+    def __init__(self, outside, inside, shape, lMax_extend=None):
+        self._L = lib()
+        self.outside, self.inside, self.shape = outside, inside, shape
+        self.lMax_extend = int(lMax_extend) if lMax_extend else 1
+
+    @staticmethod
+    def sphere_asarc(outside, inside, r, lMax_extend=None):
+        return TMatrixGenerator(outside, inside, ArcFunction.sphere(r), lMax_extend)
+
+    @staticmethod
+    def cylinder(outside, inside, r, h, lMax_extend=None):
+        return TMatrixGenerator(outside, inside, ArcFunction.cylinder(r, h), lMax_extend)
+
+    @staticmethod
+    def spheroid(outside, inside, a, c, lMax_extend=None):
+        return TMatrixGenerator(outside, inside, ArcFunction.spheroid(a, c), lMax_extend)
+
+    def batch(self, spec, omegas):
+        """T [len(omegas), n, n] in the basis spec (a BaseSpec or lMax)."""
+        if not isinstance(spec, BaseSpec):
+            spec = BaseSpec(spec)
+        om = np.ascontiguousarray(np.atleast_1d(omegas), dtype=np.complex128)
+        nw = om.shape[0]
+        outs = (_EpsMu * nw)(*[_epsmu(self.outside, complex(w)) for w in om])
+        ins = (_EpsMu * nw)(*[_epsmu(self.inside, complex(w)) for w in om])
+        T = np.empty((nw, spec.n, spec.n), dtype=np.complex128)
+        rc = self._L.qpms_gpu_tmatrix_axialsym_batch(spec.ptr, self.lMax_extend, self.shape.arc, nw, om.ctypes.data,
+                                                     C.addressof(outs), C.addressof(ins), T.ctypes.data)
+        if rc:
+            raise QpmsGpuError("qpms_gpu_tmatrix_axialsym_batch: " + last_error())
+        return T
+
+    def __call__(self, spec, omega):
+        return self.batch(spec, [omega])[0]
+
+    def _rq(self, omega, norm, J):
+        L = max(self.lMax_extend, 1)
+        n = 2 * L * (L + 2)
+        out = np.empty((n, n), dtype=np.complex128)
+        w = complex(omega)
+        rc = self._L.qpms_tmatrix_axialsym_RQ_transposed_fill(out.ctypes.data, _Cplx(w.real, w.imag),
+                                                              _epsmu(self.outside, w), _epsmu(self.inside, w),
+                                                              self.shape.arc, L, int(norm), J)
+        if rc:
+            raise QpmsGpuError("qpms_tmatrix_axialsym_RQ_transposed_fill: " + last_error())
+        return out
+
+    def Q_transposed(self, omega, norm=QPMS_NORMALISATION_DEFAULT):
+        """target[i1 + i2 n] as tmatrices.c:896-956 writes it (a C-ordered array
+        whose [i2, i1] element is Q(i1, i2))."""
+        return self._rq(omega, norm, 3)
+
+    def R_transposed(self, omega, norm=QPMS_NORMALISATION_DEFAULT):
+        return self._rq(omega, norm, 1)
