@@ -409,19 +409,23 @@ int qpms_gpu_tmatrix_axialsym_batch(const qpms_vswf_set_spec_t *bspec, qpms_l_t 
 
 /* One particle kind of qpms_gpu_scatsys_create. */
 typedef struct qpms_gpu_particle_kind_t {
-  int type;             /* 0: sphere (Mie T-matrix), 1: tabulated T-matrix */
+  int type;             /* 0: sphere (Mie T-matrix), 1: tabulated T-matrix,
+                           2: axially symmetric particle (T-matrix from its surface, GPU) */
   double radius;        /* sphere radius */
-  qpms_complex_t eps;   /* sphere: constant permittivity, used when neither ld nor eps_interp is set */
-  const qpms_ldparams_t *ld;                             /* sphere: Lorentz-Drude medium (copied) */
-  const qpms_permittivity_interpolator_t *eps_interp;    /* sphere: tabulated n, k (kept by reference) */
+  qpms_complex_t eps;   /* types 0, 2: constant permittivity, used when neither ld nor eps_interp is set */
+  const qpms_ldparams_t *ld;                             /* types 0, 2: Lorentz-Drude medium (copied) */
+  const qpms_permittivity_interpolator_t *eps_interp;    /* types 0, 2: tabulated n, k (kept by reference) */
   const qpms_tmatrix_interpolator_t *tmatrix;            /* type 1: T(omega) in the lMax basis of the system
                                                              (kept by reference) */
+  qpms_arc_function_t shape;   /* type 2: the surface (sampled once, at creation) */
+  qpms_l_t lMax_extend;        /* type 2: internal basis of the Q, R matrices (>= lMax, <= 12) */
 } qpms_gpu_particle_kind_t;
 
 /* General constructor: np particles at pos_xyz, kind[i] in [0, nkinds),
  * constant medium, lMax basis (vswf.c:76-92); b1 = b2 = NULL for a finite
- * system, else a 2D lattice.  With tabulated T-matrix kinds every T is dense
- * (spheres included).  Interpolated quantities
+ * system, else a 2D lattice.  With tabulated T-matrix or axially symmetric
+ * kinds every T is dense (spheres included); an axially symmetric kind's T
+ * is formed on the GPU at every frequency the system is evaluated at.  Interpolated quantities
  * use Re omega (materials.c:131-142, tmatrices.c:351-356). */
 qpms_scatsys_t *qpms_gpu_scatsys_create(int np, const double *pos_xyz, const int *kind, int nkinds,
     const qpms_gpu_particle_kind_t *kinds, qpms_complex_t eps_medium, qpms_l_t lMax,

@@ -8,6 +8,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <complex>
 #include <mutex>
 #include <new>
@@ -153,6 +154,8 @@ struct SphereKind {
   double ld_omega_p = 0;
   const qpms_permittivity_interpolator_t *pint = nullptr;  // tabulated n, k (set: used)
   const qpms_tmatrix_interpolator_t *tmi = nullptr;        // set: tabulated T(omega), not a sphere
+  std::vector<double> axnodes;  // non-empty: axially symmetric particle, surface quadrature nodes
+  int ax_lext = 0;              // its lMax_extend
 };
 
 // qpms_lorentzdrude_eps (materials.c:156-164): sum_j f_j wp^2 / (w_j^2 - w^2 - i w g_j).
@@ -307,6 +310,10 @@ void lattice_reduce(double *b1, double *b2) {
   }
 }
 
+int axsym_nodes(qpms_arc_function_t shape, std::vector<double> &nodes);  // qg_axsym.cu
+int axsym_tmatrix_device(const std::vector<double> &nodes, int L, const qpms_vswf_set_spec_t *bspec, int nw,
+                         const qg_c *k, const qg_c *kin, const qg_c *zr, qg_c *dT, qg_c *dQ, qg_c *dR,
+                         cudaStream_t st);
 void field_forget_system(const qpms_scatsys_t *ss);  // qg_field.cu
 void sym_forget_system(const qpms_scatsys_t *ss);    // qg_sym.cu
 
@@ -318,6 +325,20 @@ void kind_tmat(const ScatsysPriv *s, int t, cd om, std::vector<qg_c> &out) {
   if (K.tmi) {  // tabulated: tmatrices.c:351-356 uses Re omega
     out.assign(n * n, cmk(0, 0));
     tmatrix_interp_eval(K.tmi, om.real(), out.data());
+    return;
+  }
+  if (!K.axnodes.empty()) {  // axially symmetric: the EBCM kernel at om (NaN on failure)
+    out.assign(n * n, cmk(NAN, NAN));
+    const cd ei = kind_eps(K, om), em = s->eps_medium;
+    const cd kin = std::sqrt(ei) * om / kC0, kout = std::sqrt(em) * om / kC0;
+    const cd zr = std::sqrt(ei / em);  // z_out / z_in = sqrt(eps_in / eps_out) for mu = 1
+    const qg_c k1 = cmk(kout.real(), kout.imag()), k2 = cmk(kin.real(), kin.imag()), z = cmk(zr.real(), zr.imag());
+    qg_c *dT = nullptr;
+    if (cudaMalloc(&dT, n * n * 16) != cudaSuccess) return;
+    if (!axsym_tmatrix_device(K.axnodes, std::max<int>(K.ax_lext, s->lMax), &s->spec, 1, &k1, &k2, &z, dT,
+                              nullptr, nullptr, 0))
+      cudaMemcpy(out.data(), dT, n * n * 16, cudaMemcpyDeviceToHost);
+    cudaFree(dT);
     return;
   }
   std::vector<cd> d;
@@ -480,10 +501,18 @@ qpms_scatsys_t *qpms_gpu_scatsys_create(int np, const double *pos_xyz, const int
   bool dense = false;
   for (int t = 0; t < nkinds; ++t) {
     const qpms_gpu_particle_kind_t &K = kinds[t];
-    if (K.type != 0 && K.type != 1) { set_error("kind %d: type must be 0 (sphere) or 1 (T-matrix)", t); return nullptr; }
+    if (K.type < 0 || K.type > 2) {
+      set_error("kind %d: type must be 0 (sphere), 1 (T-matrix) or 2 (axially symmetric)", t);
+      return nullptr;
+    }
     radius[t] = K.type == 0 ? K.radius : 1.0;
     eps[t] = K.eps;
-    ld[t] = K.type == 0 ? K.ld : nullptr;
+    ld[t] = K.type != 1 ? K.ld : nullptr;
+    if (K.type == 2) {
+      if (K.lMax_extend > 12) { set_error("kind %d: lMax_extend above 12", t); return nullptr; }
+      dense = true;
+      continue;
+    }
     if (K.type == 1) {
       if (!K.tmatrix) { set_error("kind %d: NULL T-matrix interpolator", t); return nullptr; }
       const qpms_vswf_set_spec_t *sp = tmatrix_interp_spec(K.tmatrix);
@@ -509,8 +538,15 @@ qpms_scatsys_t *qpms_gpu_scatsys_create(int np, const double *pos_xyz, const int
   if (!ss) return nullptr;
   ScatsysPriv *s = sspriv(ss);
   for (int t = 0; t < nkinds; ++t) {
-    s->kinds[t].pint = kinds[t].type == 0 ? kinds[t].eps_interp : nullptr;
+    s->kinds[t].pint = kinds[t].type != 1 ? kinds[t].eps_interp : nullptr;
     s->kinds[t].tmi = kinds[t].type == 1 ? kinds[t].tmatrix : nullptr;
+    if (kinds[t].type == 2) {
+      if (axsym_nodes(kinds[t].shape, s->kinds[t].axnodes)) {
+        qpms_gpu_scatsys_free(ss);
+        return nullptr;
+      }
+      s->kinds[t].ax_lext = kinds[t].lMax_extend;
+    }
   }
   s->dense = dense;
   return ss;

@@ -27,10 +27,14 @@ class _Cplx2(C.Structure):
     _fields_ = [("re", C.c_double), ("im", C.c_double)]
 
 
+class _Arc(C.Structure):
+    _fields_ = [("function", C.c_void_p), ("params", C.c_void_p)]
+
+
 class _Kind(C.Structure):
     """qpms_gpu_particle_kind_t"""
     _fields_ = [("type", C.c_int), ("radius", C.c_double), ("eps", _Cplx2), ("ld", C.c_void_p),
-                ("eps_interp", C.c_void_p), ("tmatrix", C.c_void_p)]
+                ("eps_interp", C.c_void_p), ("tmatrix", C.c_void_p), ("shape", _Arc), ("lMax_extend", C.c_int)]
 
 
 class _LU(C.Structure):
@@ -150,10 +154,12 @@ class ScatteringSystem:
         permittivity, a ``materials.LorentzDrude`` model, a
         ``materials.MaterialInterpolator`` (tabulated n, k) or a
         ``tmatrices.TMatrixInterpolator`` (a tabulated T-matrix kind; its radius
-        entry is ignored).  kinds[i] selects the kind of particle i."""
+        entry is ignored) or a ``tmatrices.TMatrixGenerator`` (an axially
+        symmetric particle: its shape and inside medium; the outside medium is
+        eps_medium).  kinds[i] selects the kind of particle i."""
         self._L = _lib.lib()
         from .materials import LorentzDrude, MaterialInterpolator
-        from .tmatrices import TMatrixInterpolator
+        from .tmatrices import TMatrixGenerator, TMatrixInterpolator
         pos = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
         eps_list = list(eps_inside) if isinstance(eps_inside, (list, tuple)) else [eps_inside]
         nk = len(eps_list)
@@ -163,7 +169,20 @@ class ScatteringSystem:
         for t, e in enumerate(eps_list):
             K = karr[t]
             K.radius = float(radius[t])
-            if isinstance(e, TMatrixInterpolator):
+            if isinstance(e, TMatrixGenerator):
+                K.type = 2
+                K.shape = _Arc(e.shape.arc.function, e.shape.arc.params)
+                K.lMax_extend = max(int(e.lMax_extend), int(lMax))
+                inner = e.inside
+                if isinstance(inner, LorentzDrude):
+                    K.ld = inner.ptr
+                elif isinstance(inner, MaterialInterpolator):
+                    K.eps_interp = inner.ptr
+                else:
+                    c = complex(inner)
+                    K.eps = _Cplx2(c.real, c.imag)
+                self._keep.append(e)
+            elif isinstance(e, TMatrixInterpolator):
                 K.type = 1
                 K.tmatrix = e.ptr
                 self._keep.append(e)

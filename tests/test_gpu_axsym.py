@@ -160,3 +160,67 @@ def test_errors(gpu):
         _gen("cylinder", (50e-9, 100e-9), 2.25, 4.0, 13)(3, OM)       # lMax_extend above 12
     with pytest.raises(QpmsGpuError):
         _gen("cylinder", (-50e-9, 100e-9), 2.25, 4.0, 4)(3, OM)       # R <= 0
+
+
+# ---- axially symmetric particles in scattering systems ----
+
+def _cyl_system(gpu, lattice=None, lq=5):
+    from qpms_gb300.tmatrices import TMatrixGenerator
+    a = 580e-9
+    if lattice is None:
+        pos = np.array([[0, 0, 0], [a, 0, 0], [0, 1.1 * a, 0], [a, 1.1 * a, 0.2 * a]])
+    else:
+        pos = np.array([[0, 0, 0], [0.5 * a, 0.5 * a, 0.25 * a]])
+    gens = [TMatrixGenerator.cylinder(2.25, -12 + 1.2j, 50e-9, 100e-9, lq),
+            TMatrixGenerator.spheroid(2.25, 4.0, 40e-9, 80e-9, lq)]
+    kinds = np.arange(len(pos)) % 2
+    ss = gpu.ScatteringSystem(pos, 0.0, gens, 2.25, 3, kinds=kinds, lattice=lattice)
+    return ss, pos, kinds
+
+
+def _oracle_T(orc, om, lq=5):
+    k = np.sqrt(2.25) * om / C0
+    return [orc.tmatrix_axialsym(3, k, np.sqrt(-12 + 1.2j) * om / C0, "cylinder", (50e-9, 100e-9), lMaxQR=lq),
+            orc.tmatrix_axialsym(3, k, 2.0 * om / C0, "spheroid", (40e-9, 80e-9), lMaxQR=lq)]
+
+
+@pytest.mark.parametrize("om", [OM, OM * (1 + 0.01j)])
+def test_system_of_cylinders_vs_oracle(gpu, orc, om):
+    """Mode problem M = I - T S of cylinders and spheroids (dense T formed on
+    the GPU at omega) against the oracle's with the oracle's T."""
+    ss, pos, kinds = _cyl_system(gpu)
+    M = ss(om).modeproblem_matrix_full()
+    To = _oracle_T(orc, om)
+    T = np.stack([To[t] for t in kinds])
+    calc = orc.TransCalculator(3)
+    O = orc.finite_modeproblem(calc, pos, T, np.sqrt(2.25) * om / C0)
+    I = np.eye(len(M))
+    assert np.linalg.norm(M - O) <= 1e-10 * np.linalg.norm(O - I)
+
+
+def test_lattice_of_cylinders_vs_oracle(gpu, orc):
+    a = 580e-9
+    ss, pos, kinds = _cyl_system(gpu, lattice=((a, 0.0), (0.0, a)))
+    kv = (2e6, -1e6)
+    k = np.sqrt(2.25) * OM / C0
+    eta = ss.adjusted_eta(k, kv)
+    M = ss(OM).modeproblem_matrix_full(k=kv)
+    To = _oracle_T(orc, OM)
+    T = np.stack([To[t] for t in kinds])
+    O = orc.periodic_modeproblem(orc.TransCalculator(3), pos, T, k, (a, 0.0), (0.0, a), kv, eta)
+    I = np.eye(len(M))
+    assert np.linalg.norm(M - O) <= 1e-9 * np.linalg.norm(O - I)
+
+
+def test_sphere_as_arc_kind_equals_sphere_kind(gpu):
+    """The same spheres as Mie kinds and as arc kinds: extinction of a plane
+    wave agrees (the arc kind takes the dense-T path)."""
+    from qpms_gb300.tmatrices import TMatrixGenerator
+    a = 580e-9
+    pos = np.array([[0, 0, 0], [a, 0, 0], [0, a, 0], [a, a, 0]])
+    s1 = gpu.ScatteringSystem(pos, 50e-9, -12 + 1.2j, 2.25, 3)
+    s2 = gpu.ScatteringSystem(pos, 0.0, [TMatrixGenerator.sphere_asarc(2.25, -12 + 1.2j, 50e-9, 3)], 2.25, 3)
+    oms = OM * np.array([0.9, 1.0, 1.1])
+    r1 = s1.planewave_scatter_batch(oms, mode=0)
+    r2 = s2.planewave_scatter_batch(oms, mode=0)
+    np.testing.assert_allclose(r2["sigma_ext"], r1["sigma_ext"], rtol=1e-11)
