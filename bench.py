@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--nvec", type=int, default=N_VEC)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--sections", default="modeproblem,dispersion,beyn,serving,field",
+    ap.add_argument("--sections", default="modeproblem,dispersion,beyn,serving,field,axsym",
                     help="secondary workloads reported beside the headline (comma list, or 'none')")
     ap.add_argument("--case", default=None,
                     help="run one small case for a profiler and exit: dense:N:NRHS:MODE, "
@@ -570,6 +570,72 @@ def section_field(args):
     return res
 
 
+def _axsym_flops(L, nq, zsym=True):
+    """Algorithmic FP64 flops of the Q/R quadrature at lMax_extend L over nq
+    nodes: per m block 2 nb^2 dot products (n x y) . v of complex 3-vectors
+    (3 complex FMAs = 24 flops per node), half of them for a z-mirror
+    symmetric surface (the others vanish)."""
+    tot = 0
+    for m in range(-L, L + 1):
+        nb = 2 * (L - max(1, abs(m)) + 1)
+        tot += 2 * nb * nb // (2 if zsym else 1)
+    return tot * nq * 24
+
+
+def section_axsym(args):
+    """T-matrices of an axially symmetric particle (gold-like cylinder r 50 nm,
+    h 100 nm in eps 2.25, basis lMax 3, Q/R at lMax_extend 8) at 256
+    frequencies 1.6-2.6 eV: the batched EBCM kernel, device time and end to end."""
+    import torch
+    from qpms_gb300.tmatrices import TMatrixGenerator
+    from qpms_gb300.workloads import EV, HBAR
+    L, lMax, nw = 8, 3, 256
+    g = TMatrixGenerator.cylinder(2.25, -12 + 1.2j, 50e-9, 100e-9, L)
+    oms = np.linspace(1.6, 2.6, nw) * EV / HBAR
+    for _ in range(3):
+        g.batch(lMax, oms[:16])
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e0.record(st)
+    for _ in range(reps):
+        T = g.batch(lMax, oms)
+    e1.record(st)
+    torch.cuda.synchronize()
+    e2e = (time.perf_counter() - t0) / reps
+    dev_ms = e0.elapsed_time(e1) / reps
+    nq = (6 + 3) * 32  # cylinder, theta in [0, pi/2]: cap 6 panels, side 3 panels, 32 nodes each
+    flops = _axsym_flops(L, nq) * nw
+    import ctypes as C
+    import qpms_gb300
+    fp = C.c_double(0)
+    fp64 = fp.value if qpms_gb300.lib().qpms_gpu_measure_fp64_peak(C.byref(fp)) == 0 else None
+    ach = flops / (dev_ms * 1e-3) / 1e12
+    res = {"workload": "cylinder r 50 nm h 100 nm, eps -12+1.2i in 2.25, lMax 3, lMax_extend 8, %d frequencies" % nw,
+           "tmatrices_per_s": nw / (dev_ms * 1e-3), "ms_per_batch": dev_ms,
+           "fp64": {"achieved_tflops": ach, "peak_tflops": fp64, "frac": ach / fp64 if fp64 else None,
+                    "flops_per_batch": flops, "note": "device time includes the batch's H2D/D2H (host API)"},
+           "e2e": {"tmatrices_per_s": nw / e2e, "h2d_bytes": 0, "d2h_bytes": int(T.nbytes)}}
+    if not args.no_cpu:
+        from oracle import orc
+        C0 = 299792458.0
+        ns = 4
+        t0 = time.perf_counter()
+        worst = 0.0
+        for w in range(ns):
+            k, ki = np.sqrt(2.25) * oms[w] / C0, np.sqrt(-12 + 1.2j) * oms[w] / C0
+            O = orc.tmatrix_axialsym(lMax, k, ki, "cylinder", (50e-9, 100e-9), lMaxQR=L)
+            worst = max(worst, float(np.abs(T[w] - O).max() / np.abs(O).max()))
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"tmatrices_per_s": ns / dt, "cores": 1, "kind": "port",
+                               "sample": "first %d frequencies, adaptive quadrature (rtol 1e-10)" % ns,
+                               "max_rel_diff_vs_gpu": worst}
+        res["gpu_vs_cpu"] = res["tmatrices_per_s"] / res["cpu_baseline"]["tmatrices_per_s"]
+    return res
+
+
 def run_sections(args):
     out = {}
     names = [x for x in args.sections.split(",") if x and x != "none"]
@@ -623,6 +689,12 @@ def run_case(spec):
         pts = rng.uniform(-nx * 2e-7, nx * 2e-7, size=(npts, 3))
         E = ss.scattered_E(1.6e7, cv, pts)
         print("field", nx, npts, lMax, "sum |E|", float(np.abs(E).sum()))
+    elif f[0] == "axsym":
+        from qpms_gb300.tmatrices import TMatrixGenerator
+        L, nw = int(f[1]), int(f[2])
+        g = TMatrixGenerator.cylinder(2.25, -12 + 1.2j, 50e-9, 100e-9, L)
+        T = g.batch(3, np.linspace(1.6, 2.6, nw) * EV / HBAR)
+        print("axsym", L, nw, "sum |T|", float(np.abs(T).sum()))
     elif f[0] == "beyn":
         nx, nodes, mode = int(f[1]), int(f[2]), int(f[3])
         xs = (np.arange(nx) - (nx - 1) / 2) * 400e-9

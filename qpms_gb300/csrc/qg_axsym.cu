@@ -11,14 +11,18 @@
 // r^2 sin(theta) / cos(beta) (tmatrices.c:659-696), and T = -R Q^-1 per m
 // block (tmatrices.c:864-884), trimmed from lMax_extend to the bspec.
 //
-// GPU design: one CTA per (frequency, m).  Quadrature nodes (composite
+// GPU design: the radial factors (spherical Bessel/Hankel recurrences of
+// qg_specfunc.cuh) are formed once per (frequency, node) and the angular ones
+// (normalised Legendre recurrences) once per (|m|, node), by two small
+// kernels.  Then one CTA per (frequency, m): quadrature nodes (composite
 // Gauss-Legendre on panels that break at the kinks of the surface, e.g. the
-// cylinder's rims) are staged kAxChunk at a time: one thread per node forms
-// the three wave sets (spherical Bessel/Hankel recurrences of qg_specfunc.cuh,
-// normalised Legendre recurrences) into shared memory, then every thread
-// accumulates its Q / R entries over the staged nodes in FP64 registers.  The
-// m block (at most 24 x 24) is then solved in shared memory by Gauss-Jordan
-// elimination with partial pivoting (Q^T X = R^T, X = -T^T).  The reference
+// cylinder's rims) are staged kAxChunk at a time, all threads forming the
+// weighted n x y of the outside waves and the inside waves v in shared
+// memory; since n . (y x v) = (n x y) . v, every Q / R entry is then a
+// combination of dot products of those staged vectors (3 complex FMAs per
+// entry and node, accumulated in FP64 registers; GB300's FP64 pipe is the
+// bound).  The m block (at most 24 x 24) is solved in shared memory by
+// Gauss-Jordan elimination with partial pivoting (Q^T X = R^T, X = -T^T).  The reference
 // integrates each entry separately by adaptive quadrature (GSL qag, epsrel
 // 1e-5); the fixed rule here is the same integral to double precision on
 // smooth panels.
@@ -49,18 +53,112 @@ struct AxDev {
   int L, nw, nq;
   const double *nodes;       // [nq][5]: theta, weight * jac, r, cos beta, sin beta
   const qg_c *k, *kin, *zr;  // [nw]
+  const qg_c *rad;           // [nw][nq][3 sets][L][3]: z_l, z_l / x, z_(l-1) - l z_l / x (l = 1..L)
+  const double *ang;         // [L + 1 (mu)][nq][L][3]: leg, pi, tau at +mu (l = 1..L)
   qg_c *T;                   // [nw][nQ][nQ], default normalisation, m blocks only
   qg_c *Q, *R;               // optional, same layout (inside wave (t', l', -m) at the column of (t', l', m))
   int *err;                  // 1: a singular Q block
+  int zsym;                  // 1: surface symmetric under z -> -z; nodes cover theta in [0, pi/2] (weights x2)
 };
 
-__device__ __forceinline__ qg_c tprod(double nr, double nt, const qg_c *y, const qg_c *v) {
-  // n . (y x v) with n = (nr, nt, 0) in (r, theta, phi)
-  const qg_c a = csub(cmul(y[1], v[2]), cmul(y[2], v[1]));
-  const qg_c b = csub(cmul(y[2], v[0]), cmul(y[0], v[2]));
-  return cadd(cscale(a, nr), cscale(b, nt));
+// Radial factors per (frequency, node): set 0 h+(k r), set 1 j(k r), set 2 j(k_in r).
+template <int LQ>
+__global__ void axsym_radial_kernel(AxDev a, qg_c *rad) {
+  const int L = a.L;
+  const size_t tot = (size_t)a.nw * a.nq * 3;
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < tot; x += (size_t)gridDim.x * blockDim.x) {
+    const int set = (int)(x % 3);
+    const size_t wq = x / 3;
+    const int q = (int)(wq % a.nq), w = (int)(wq / a.nq);
+    const double r = a.nodes[5 * (size_t)q + 2];
+    const qg_c xx = cscale(set == 2 ? a.kin[w] : a.k[w], r);
+    qg_c z[LQ + 1];
+    sph_bessel<LQ>(set == 0 ? 3 : 1, xx, z);
+    const qg_c rx = crecip(xx);
+    qg_c *o = rad + (wq * 3 + set) * (size_t)L * 3;
+    for (int l = 1; l <= L; ++l) {
+      const qg_c bf = cmul(z[l], rx);
+      o[(l - 1) * 3] = z[l];
+      o[(l - 1) * 3 + 1] = bf;
+      o[(l - 1) * 3 + 2] = csub(z[l - 1], cscale(bf, (double)l));
+    }
+  }
 }
 
+// Angular factors per (mu, node): normalised Legendre (Condon-Shortley
+// phase) leg = P / sqrt(l(l+1)), pi = mu leg / sin, tau = dP/dtheta / sqrt(l(l+1)).
+__global__ void axsym_angular_kernel(int L, int nq, const double *__restrict__ nodes, double *__restrict__ ang) {
+  const size_t tot = (size_t)(L + 1) * nq;
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < tot; x += (size_t)gridDim.x * blockDim.x) {
+    const int q = (int)(x % nq), mu = (int)(x / nq);
+    double st, ct;
+    sincos(nodes[5 * (size_t)q], &st, &ct);
+    double *o = ang + x * (size_t)L * 3;
+    double pmm = 0.28209479177387814347;  // 1 / sqrt(4 pi)
+    for (int j = 1; j <= mu; ++j) pmm *= -sqrt((2.0 * j - 1) / (2.0 * j)) * st;
+    pmm *= sqrt(2.0 * mu + 1);
+    for (int l = 1; l < mu && l <= L; ++l) o[(l - 1) * 3] = o[(l - 1) * 3 + 1] = o[(l - 1) * 3 + 2] = 0.0;
+    double p2 = 0.0, p1 = 0.0;
+    for (int l = mu; l <= L; ++l) {
+      double P;
+      if (l == mu) {
+        P = pmm;
+      } else {
+        const double al = sqrt((4.0 * l * l - 1) / ((double)l * l - (double)mu * mu));
+        const double bl = sqrt(((l - 1.0) * (l - 1.0) - (double)mu * mu) / (4.0 * (l - 1.0) * (l - 1.0) - 1));
+        P = al * (ct * p1 - bl * p2);
+      }
+      if (l >= 1) {
+        const double rl = 1.0 / sqrt((double)l * (l + 1));
+        o[(l - 1) * 3] = P * rl;
+        o[(l - 1) * 3 + 1] = mu / st * P * rl;
+        o[(l - 1) * 3 + 2] =
+            (l * ct * P - sqrt((2.0 * l + 1) * ((double)l * l - (double)mu * mu) / (2.0 * l - 1)) * p1) / st * rl;
+      }
+      p2 = p1;
+      p1 = P;
+    }
+  }
+}
+
+// The e-th formed entry of D: set qr (0 Q, 1 R), row (t, l), column (t2, l2)
+// (l, l2 indices from l0).  With z-mirror symmetry only the entries with
+// l + l2 + [t == t2] even are formed (the others integrate to zero): each row
+// has nl of them, first t2 = t with l2 of the other parity, then t2 != t with
+// l2 of the same parity.
+__device__ __forceinline__ void d_entry(int e, int nb, int nl, int nb2, int zsym, int &qr, int &t, int &l, int &t2,
+                                        int &l2) {
+  if (!zsym) {
+    qr = e / nb2;
+    const int rem = e - qr * nb2, i = rem / nb, j = rem - i * nb;
+    t = i / nl;
+    l = i - t * nl;
+    t2 = j / nl;
+    l2 = j - t2 * nl;
+    return;
+  }
+  const int per = nb * nl;
+  qr = e / per;
+  const int rem = e - qr * per, i = rem / nl, kk = rem - i * nl;
+  t = i / nl;
+  l = i - t * nl;
+  const int p1 = (l + 1) & 1;               // parity of l2 when t2 == t
+  const int c1 = p1 ? nl / 2 : (nl + 1) / 2;  // number of l2 in [0, nl) with that parity
+  if (kk < c1) {
+    t2 = t;
+    l2 = 2 * kk + p1;
+  } else {
+    t2 = 1 - t;
+    l2 = 2 * (kk - c1) + (l & 1);
+  }
+}
+
+// One CTA per (frequency, m).  Staging: per node and l, the weighted
+// n x y of the outgoing (Q) and regular (R) outside waves of both types,
+// w = weight (n_theta y_phi, -n_r y_phi, n_r y_theta - n_theta y_r), and the
+// inside regular waves v, since n . (y x v) = (n x y) . v.  Accumulation: the
+// dot products D[(t,l),(s,l')] = sum_q w_(t,l) . v_(s,l') (3 complex FMAs per
+// entry and node); then Q[(t,l),(t',l')] = z/z_in D[(t,l),(t'bar,l')] + D[(tbar,l),(t',l')].
 template <int LQ>
 __global__ void __launch_bounds__(kAxThreads) axsym_kernel(AxDev a) {
   extern __shared__ qg_c sh[];
@@ -72,115 +170,114 @@ __global__ void __launch_bounds__(kAxThreads) axsym_kernel(AxDev a) {
   const int m = (int)blockIdx.x - L, iw = blockIdx.y;
   const int mu = m < 0 ? -m : m;
   const int l0 = mu > 1 ? mu : 1, nl = L - l0 + 1, nb = 2 * nl, nb2 = nb * nb, tot = 2 * nb2;
+  const int ntd = a.zsym ? tot / 2 : tot;  // D entries formed (z-mirror: nl of each row's nb)
   const int tid = threadIdx.x;
-  const qg_c k = a.k[iw], kin = a.kin[iw], zr = a.zr[iw];
+  const qg_c zr = a.zr[iw];
   const double sgn_mu = (mu & 1) ? -1.0 : 1.0;
+  // (leg, pi, tau) at -mu = (s leg, -s pi, s tau), s = (-1)^mu
+  const double fo_l = m >= 0 ? 1.0 : sgn_mu, fo_p = m >= 0 ? 1.0 : -sgn_mu;  // outside waves at m
+  const double fi_l = m >= 0 ? sgn_mu : 1.0, fi_p = m >= 0 ? -sgn_mu : 1.0;  // inside waves at -m
   qg_c acc[kAxPerThread];
 #pragma unroll
   for (int s = 0; s < kAxPerThread; ++s) acc[s] = cmk(0, 0);
+  const qg_c *radw = a.rad + (size_t)iw * a.nq * 3 * L * 3;
+  const double *angm = a.ang + (size_t)mu * a.nq * L * 3;
 
   for (int q0 = 0; q0 < a.nq; q0 += kAxChunk) {
     const int cnt = min(kAxChunk, a.nq - q0);
     __syncthreads();
     if (tid < cnt) {
-      // ---- the three wave sets at node q0 + tid ----
       const double *ndq = a.nodes + 5 * (size_t)(q0 + tid);
-      const double th = ndq[0], r = ndq[2];
       nd[tid][0] = ndq[1];
       nd[tid][1] = ndq[3];
       nd[tid][2] = ndq[4];
-      const qg_c x1 = cscale(k, r), x2 = cscale(kin, r);
-      qg_c zh[LQ + 1], zj[LQ + 1], zi[LQ + 1];
-      sph_bessel<LQ>(3, x1, zh);
-      sph_bessel<LQ>(1, x1, zj);
-      sph_bessel<LQ>(1, x2, zi);
-      const qg_c rx1 = crecip(x1), rx2 = crecip(x2);
-      double st, ct;
-      sincos(th, &st, &ct);
-      // normalised Legendre P^mu_l (Condon-Shortley phase) for l = mu..L
-      double pmm = 0.28209479177387814347;  // 1 / sqrt(4 pi)
-      for (int q = 1; q <= mu; ++q) pmm *= -sqrt((2.0 * q - 1) / (2.0 * q)) * st;
-      pmm *= sqrt(2.0 * mu + 1);
-      double p2 = 0.0, p1 = 0.0;
-      qg_c *W = sh + (size_t)tid * nl * 18;
-      for (int l = mu; l <= L; ++l) {
-        double P;
-        if (l == mu) {
-          P = pmm;
-        } else {
-          const double al = sqrt((4.0 * l * l - 1) / ((double)l * l - (double)mu * mu));
-          const double bl = sqrt(((l - 1.0) * (l - 1.0) - (double)mu * mu) / (4.0 * (l - 1.0) * (l - 1.0) - 1));
-          P = al * (ct * p1 - bl * p2);
-        }
-        if (l >= l0) {
-          const double rl = 1.0 / sqrt((double)l * (l + 1));
-          const double leg = P * rl;
-          const double pi_ = mu / st * leg;
-          const double tau = (l * ct * P - sqrt((2.0 * l + 1) * ((double)l * l - (double)mu * mu) / (2.0 * l - 1)) * p1) /
-                             st * rl;
-          // (leg, pi, tau) at +mu; at -mu: (s leg, -s pi, s tau), s = (-1)^mu
-          const double le = (m >= 0) ? leg : sgn_mu * leg, pe = (m >= 0) ? pi_ : -sgn_mu * pi_,
-                       te = (m >= 0) ? tau : sgn_mu * tau;
-          const double li = (m >= 0) ? sgn_mu * leg : leg, pI = (m >= 0) ? -sgn_mu * pi_ : pi_,
-                       ti = (m >= 0) ? sgn_mu * tau : tau;
-          qg_c *w = W + (size_t)(l - l0) * 18;
-#pragma unroll
-          for (int set = 0; set < 3; ++set) {
-            const qg_c *z = set == 0 ? zh : (set == 1 ? zj : zi);
-            const qg_c rx = set == 2 ? rx2 : rx1;
-            const double Lg = set == 2 ? li : le, Pi = set == 2 ? pI : pe, Ta = set == 2 ? ti : te;
-            const qg_c besfac = cmul(z[l], rx);
-            const qg_c besder = csub(z[l - 1], cscale(besfac, (double)l));
-            qg_c *o = w + set * 6;
-            o[0] = cscale(besfac, l * (l + 1.0) * Lg);  // N
-            o[1] = cscale(besder, Ta);
-            o[2] = cmk(-besder.im * Pi, besder.re * Pi);  // i pi besder
-            o[3] = cmk(0, 0);                              // M
-            o[4] = cmk(-z[l].im * Pi, z[l].re * Pi);      // i pi z
-            o[5] = cscale(z[l], -Ta);
-          }
-        }
-        p2 = p1;
-        p1 = P;
+    }
+    __syncthreads();
+    // ---- staging: items (node, l, set) ----
+    for (int it = tid; it < cnt * nl * 3; it += kAxThreads) {
+      const int set = it % 3, ql = it / 3, li = ql % nl, q = ql / nl;
+      const int l = l0 + li, qg = q0 + q;
+      const double *an = angm + ((size_t)qg * L + (l - 1)) * 3;
+      const qg_c *rd = radw + (((size_t)qg * 3 + set) * L + (l - 1)) * 3;
+      const double fl = set == 2 ? fi_l : fo_l, fp = set == 2 ? fi_p : fo_p;
+      const double Lg = an[0] * fl, Pi = an[1] * fp, Ta = an[2] * fl;
+      const qg_c z = rd[0], bf = rd[1], bd = rd[2];
+      // N = (l(l+1) leg z/x, tau besder, i pi besder), M = (0, i pi z, -tau z)
+      const qg_c N0 = cscale(bf, l * (l + 1.0) * Lg), N1 = cscale(bd, Ta), N2 = cmk(-bd.im * Pi, bd.re * Pi);
+      const qg_c M1 = cmk(-z.im * Pi, z.re * Pi), M2 = cscale(z, -Ta);
+      qg_c *o = sh + ((size_t)q * nl + li) * 18 + set * 6;
+      if (set == 2) {
+        o[0] = N0;
+        o[1] = N1;
+        o[2] = N2;
+        o[3] = cmk(0, 0);
+        o[4] = M1;
+        o[5] = M2;
+      } else {
+        const double wq = nd[q][0], nr = nd[q][1] * wq, nt = nd[q][2] * wq;
+        // weight (n x y): (nt y_phi, -nr y_phi, nr y_theta - nt y_r)
+        o[0] = cscale(N2, nt);
+        o[1] = cscale(N2, -nr);
+        o[2] = csub(cscale(N1, nr), cscale(N0, nt));
+        o[3] = cscale(M2, nt);
+        o[4] = cscale(M2, -nr);
+        o[5] = cscale(M1, nr);
       }
     }
     __syncthreads();
-    // ---- accumulate the entries of this thread over the staged nodes ----
+    // ---- D entries of this thread over the staged nodes ----
 #pragma unroll
     for (int s = 0; s < kAxPerThread; ++s) {
       const int e = tid + s * kAxThreads;
-      if (e >= tot) break;
-      const int qr = e / nb2, rem = e - qr * nb2;
-      const int i = rem / nb, j = rem - i * nb;
-      const int t = i / nl, l = i - t * nl, t2 = j / nl, l2 = j - t2 * nl;
-      qg_c sum = acc[s];
+      if (e >= ntd) break;
+      int qr, t, l, t2, l2;
+      d_entry(e, nb, nl, nb2, a.zsym, qr, t, l, t2, l2);
+      double sr = acc[s].re, si = acc[s].im;
       for (int q = 0; q < cnt; ++q) {
-        const qg_c *Y = sh + ((size_t)q * nl + l) * 18 + qr * 6;
-        const qg_c *V = sh + ((size_t)q * nl + l2) * 18 + 12;
-        const double nr = nd[q][1], nt = nd[q][2];
-        const qg_c v1 = tprod(nr, nt, Y + 3 * t, V + 3 * (1 - t2));
-        const qg_c v2 = tprod(nr, nt, Y + 3 * (1 - t), V + 3 * t2);
-        sum = cadd(sum, cscale(cadd(cmul(zr, v1), v2), nd[q][0]));
+        const qg_c *W = sh + ((size_t)q * nl + l) * 18 + qr * 6 + 3 * t;
+        const qg_c *V = sh + ((size_t)q * nl + l2) * 18 + 12 + 3 * t2;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const qg_c w = W[c], v = V[c];
+          sr = fma(w.re, v.re, sr);
+          sr = fma(-w.im, v.im, sr);
+          si = fma(w.re, v.im, si);
+          si = fma(w.im, v.re, si);
+        }
       }
-      acc[s] = sum;
+      acc[s] = cmk(sr, si);
     }
   }
   __syncthreads();
-  // ---- Q^T, R^T into shared memory (A, B), optional global copies ----
-  qg_c *A = sh, *B = sh + nb2;
-  const int neQ = L * (L + 2), nQ = 2 * neQ;
+  // ---- D into shared memory, then A = Q^T, B = R^T (optional global Q, R) ----
+  qg_c *D = sh, *A = sh + 2 * nb2, *B = A + nb2;
+  if (a.zsym)
+    for (int e = tid; e < tot; e += kAxThreads) D[e] = cmk(0, 0);
+  __syncthreads();
 #pragma unroll
   for (int s = 0; s < kAxPerThread; ++s) {
     const int e = tid + s * kAxThreads;
-    if (e >= tot) break;
+    if (e >= ntd) break;
+    int qr, t, l, t2, l2;
+    d_entry(e, nb, nl, nb2, a.zsym, qr, t, l, t2, l2);
+    D[qr * nb2 + (t * nl + l) * nb + t2 * nl + l2] = acc[s];
+  }
+  __syncthreads();
+  const int neQ = L * (L + 2), nQ = 2 * neQ;
+  for (int e = tid; e < tot; e += kAxThreads) {
     const int qr = e / nb2, rem = e - qr * nb2;
     const int i = rem / nb, j = rem - i * nb;
-    (qr ? B : A)[j * nb + i] = acc[s];
+    const int t = i / nl, li = i - t * nl, t2 = j / nl, lj = j - t2 * nl;
+    const qg_c *Dq = D + qr * nb2;
+    const qg_c v1 = Dq[(t * nl + li) * nb + (1 - t2) * nl + lj];
+    const qg_c v2 = Dq[((1 - t) * nl + li) * nb + t2 * nl + lj];
+    const qg_c val = cadd(cmul(zr, v1), v2);
+    (qr ? B : A)[j * nb + i] = val;
     qg_c *G = qr ? a.R : a.Q;
     if (G) {
-      const int t = i / nl, l = l0 + i % nl, t2 = j / nl, l2 = l0 + j % nl;
+      const int l = l0 + li, l2 = l0 + lj;
       const size_t gi = (size_t)t * neQ + l * (l + 1) + m - 1, gj = (size_t)t2 * neQ + l2 * (l2 + 1) + m - 1;
-      G[((size_t)iw * nQ + gi) * nQ + gj] = acc[s];
+      G[((size_t)iw * nQ + gi) * nQ + gj] = val;
     }
   }
   __syncthreads();
@@ -275,10 +372,20 @@ __global__ void axsym_gather_kernel(int nw, int nQ, int n, const qg_c *__restric
 }
 
 template <int LQ>
-int launch_axsym(const AxDev &a, cudaStream_t st) {
-  const int nlmax = LQ;  // largest nl = L - 1 + 1
-  const size_t wave_bytes = (size_t)kAxChunk * nlmax * 18 * sizeof(qg_c);
-  const size_t solve_bytes = (size_t)2 * (2 * LQ) * (2 * LQ) * sizeof(qg_c);
+int launch_axsym(AxDev a, qg_c *rad, double *ang, cudaStream_t st) {
+  {
+    const size_t tot = (size_t)a.nw * a.nq * 3;
+    axsym_radial_kernel<LQ><<<(unsigned)std::min<size_t>((tot + 127) / 128, 8192), 128, 0, st>>>(a, rad);
+    QG_CUDA_TRY(cudaGetLastError());
+    const size_t tot2 = (size_t)(a.L + 1) * a.nq;
+    axsym_angular_kernel<<<(unsigned)((tot2 + 127) / 128), 128, 0, st>>>(a.L, a.nq, a.nodes, ang);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(2);
+  }
+  a.rad = rad;
+  a.ang = ang;
+  const size_t wave_bytes = (size_t)kAxChunk * LQ * 18 * sizeof(qg_c);
+  const size_t solve_bytes = (size_t)4 * (2 * LQ) * (2 * LQ) * sizeof(qg_c);
   const size_t shmem = std::max(wave_bytes, solve_bytes);
   QG_CUDA_TRY(cudaFuncSetAttribute(axsym_kernel<LQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shmem));
   dim3 grid(2 * a.L + 1, a.nw);
@@ -386,14 +493,20 @@ namespace qg {
 
 // Quadrature nodes [nq][5] (theta, weight * jac, r, cos beta, sin beta) of
 // the surface: panels of kAxGauss Gauss-Legendre nodes, broken at the
-// cylinder rims; other shapes take 16 panels over [0, pi].
-int axsym_nodes(qpms_arc_function_t shape, std::vector<double> &nodes) {
+// cylinder rims.  The library's sphere, cylinder and spheroid are symmetric
+// under z -> -z (*zsym = 1): the integrands are then even or odd under
+// theta -> pi - theta, so the nodes cover [0, pi/2] with doubled weights and
+// the odd entries are not formed; other arcs take 16 panels over [0, pi].
+int axsym_nodes(qpms_arc_function_t shape, std::vector<double> &nodes, int *zsym) {
   if (!shape.function) {
     set_error("NULL arc function");
     return QPMS_EINVAL;
   }
+  // the library's shapes are symmetric under z -> -z: half the range, weights x 2
   std::vector<double> bp;
-  int per_piece = 16;
+  std::vector<int> panels;
+  double wfac = 1.0;
+  *zsym = 0;
   if (shape.function == qpms_arc_cylinder) {
     const qpms_arc_cylinder_params_t *p = (const qpms_arc_cylinder_params_t *)shape.params;
     if (!p || !(p->R > 0) || !(p->h > 0)) {
@@ -401,18 +514,23 @@ int axsym_nodes(qpms_arc_function_t shape, std::vector<double> &nodes) {
       return QPMS_EINVAL;
     }
     const double th = atan(2 * p->R / p->h);
-    bp = {0.0, th, M_PI - th, M_PI};
-    per_piece = 6;
-  } else if (shape.function == qpms_arc_sphere) {
-    bp = {0.0, M_PI};
-    per_piece = 4;
+    bp = {0.0, th, M_PI_2};
+    panels = {6, 3};
+    *zsym = 1;
+  } else if (shape.function == qpms_arc_sphere || shape.function == qpms_arc_spheroid) {
+    bp = {0.0, M_PI_2};
+    panels = {shape.function == qpms_arc_sphere ? 2 : 8};
+    *zsym = 1;
   } else {
     bp = {0.0, M_PI};
+    panels = {16};
   }
+  if (*zsym) wfac = 2.0;
   std::vector<double> gx, gw;
   gauss_legendre(kAxGauss, gx, gw);
   nodes.clear();
   for (size_t pc = 0; pc + 1 < bp.size(); ++pc) {
+    const int per_piece = panels[pc];
     const double a0 = bp[pc], a1 = bp[pc + 1], hw = (a1 - a0) / per_piece;
     for (int pn = 0; pn < per_piece; ++pn) {
       const double lo = a0 + pn * hw, c = lo + 0.5 * hw;
@@ -425,7 +543,7 @@ int axsym_nodes(qpms_arc_function_t shape, std::vector<double> &nodes) {
           return QPMS_EINVAL;
         }
         nodes.push_back(th);
-        nodes.push_back(0.5 * hw * gw[g] * rb.r * rb.r * sin(th) / cb);
+        nodes.push_back(wfac * 0.5 * hw * gw[g] * rb.r * rb.r * sin(th) / cb);
         nodes.push_back(rb.r);
         nodes.push_back(cb);
         nodes.push_back(sin(rb.beta));
@@ -438,8 +556,8 @@ int axsym_nodes(qpms_arc_function_t shape, std::vector<double> &nodes) {
 // T-matrices of one shape at nw frequencies (host k, k_in, z / z_in) into
 // dT [nw][bspec n][bspec n] on the device; optionally the full Q, R at L into
 // dQ, dR ([nw][nQ][nQ], default normalisation).
-int axsym_tmatrix_device(const std::vector<double> &nodes, int L, const qpms_vswf_set_spec_t *bspec, int nw,
-                         const qg_c *k, const qg_c *kin, const qg_c *zr, qg_c *dT, qg_c *dQ, qg_c *dR,
+int axsym_tmatrix_device(const std::vector<double> &nodes, int zsym, int L, const qpms_vswf_set_spec_t *bspec,
+                         int nw, const qg_c *k, const qg_c *kin, const qg_c *zr, qg_c *dT, qg_c *dQ, qg_c *dR,
                          cudaStream_t st) {
   if (L < 1 || L > kAxMaxL) {
     set_error("lMax_extend %d outside 1..%d", L, kAxMaxL);
@@ -499,10 +617,14 @@ int axsym_tmatrix_device(const std::vector<double> &nodes, int L, const qpms_vsw
   a.Q = dQ;
   a.R = dR;
   a.err = (int *)derr.p;
+  a.zsym = zsym;
+  DevMem drad, dang;
+  QG_CUDA_TRY(cudaMalloc(&drad.p, (size_t)nw * nq * 3 * L * 3 * 16));
+  QG_CUDA_TRY(cudaMalloc(&dang.p, (size_t)(L + 1) * nq * L * 3 * 8));
   int e;
-  if (L <= 4) e = launch_axsym<4>(a, st);
-  else if (L <= 8) e = launch_axsym<8>(a, st);
-  else e = launch_axsym<kAxMaxL>(a, st);
+  if (L <= 4) e = launch_axsym<4>(a, (qg_c *)drad.p, (double *)dang.p, st);
+  else if (L <= 8) e = launch_axsym<8>(a, (qg_c *)drad.p, (double *)dang.p, st);
+  else e = launch_axsym<kAxMaxL>(a, (qg_c *)drad.p, (double *)dang.p, st);
   if (e) return e;
   if (n && dT) {
     const size_t tot = (size_t)nw * n * n;
@@ -548,7 +670,8 @@ int axsym_tmatrix_batch_host(qpms_arc_function_t shape, int lMax_extend, const q
   }
   if (!nw) return QPMS_SUCCESS;
   std::vector<double> nodes;
-  int e = axsym_nodes(shape, nodes);
+  int zsym = 0;
+  int e = axsym_nodes(shape, nodes, &zsym);
   if (e) return e;
   const int L = std::max<int>(lMax_extend, bspec->lMax);
   std::vector<qg_c> k(nw), kin(nw), zr(nw);
@@ -560,7 +683,7 @@ int axsym_tmatrix_batch_host(qpms_arc_function_t shape, int lMax_extend, const q
   const size_t n = bspec->n;
   DevMem dT;
   QG_CUDA_TRY(cudaMalloc(&dT.p, (size_t)nw * n * n * 16 + 16));
-  if ((e = axsym_tmatrix_device(nodes, L, bspec, nw, k.data(), kin.data(), zr.data(), (qg_c *)dT.p, nullptr,
+  if ((e = axsym_tmatrix_device(nodes, zsym, L, bspec, nw, k.data(), kin.data(), zr.data(), (qg_c *)dT.p, nullptr,
                                 nullptr, 0)))
     return e;
   QG_CUDA_TRY(cudaMemcpy(T_out, dT.p, (size_t)nw * n * n * 16, cudaMemcpyDeviceToHost));
@@ -629,7 +752,8 @@ int qpms_tmatrix_axialsym_RQ_transposed_fill(qpms_complex_t *target, qpms_comple
     return QPMS_EINVAL;
   }
   std::vector<double> nodes;
-  int e = axsym_nodes(shape, nodes);
+  int zsym = 0;
+  int e = axsym_nodes(shape, nodes, &zsym);
   if (e) return e;
   const int L = lMaxQR;
   if (L < 1 || L > 12) {
@@ -640,7 +764,7 @@ int qpms_tmatrix_axialsym_RQ_transposed_fill(qpms_complex_t *target, qpms_comple
   const qg_c k = wavenumber_of(omega, outside), kin = wavenumber_of(omega, inside), zr = impedance_ratio(outside, inside);
   DevMem dG;
   QG_CUDA_TRY(cudaMalloc(&dG.p, (size_t)nQ * nQ * 16));
-  if ((e = axsym_tmatrix_device(nodes, L, nullptr, 1, &k, &kin, &zr, nullptr,
+  if ((e = axsym_tmatrix_device(nodes, zsym, L, nullptr, 1, &k, &kin, &zr, nullptr,
                                 J == QPMS_HANKEL_PLUS ? (qg_c *)dG.p : nullptr,
                                 J == QPMS_HANKEL_PLUS ? nullptr : (qg_c *)dG.p, 0)))
     return e;

@@ -156,6 +156,7 @@ struct SphereKind {
   const qpms_tmatrix_interpolator_t *tmi = nullptr;        // set: tabulated T(omega), not a sphere
   std::vector<double> axnodes;  // non-empty: axially symmetric particle, surface quadrature nodes
   int ax_lext = 0;              // its lMax_extend
+  int ax_zsym = 0;              // its surface is symmetric under z -> -z
 };
 
 // qpms_lorentzdrude_eps (materials.c:156-164): sum_j f_j wp^2 / (w_j^2 - w^2 - i w g_j).
@@ -310,9 +311,9 @@ void lattice_reduce(double *b1, double *b2) {
   }
 }
 
-int axsym_nodes(qpms_arc_function_t shape, std::vector<double> &nodes);  // qg_axsym.cu
-int axsym_tmatrix_device(const std::vector<double> &nodes, int L, const qpms_vswf_set_spec_t *bspec, int nw,
-                         const qg_c *k, const qg_c *kin, const qg_c *zr, qg_c *dT, qg_c *dQ, qg_c *dR,
+int axsym_nodes(qpms_arc_function_t shape, std::vector<double> &nodes, int *zsym);  // qg_axsym.cu
+int axsym_tmatrix_device(const std::vector<double> &nodes, int zsym, int L, const qpms_vswf_set_spec_t *bspec,
+                         int nw, const qg_c *k, const qg_c *kin, const qg_c *zr, qg_c *dT, qg_c *dQ, qg_c *dR,
                          cudaStream_t st);
 void field_forget_system(const qpms_scatsys_t *ss);  // qg_field.cu
 void sym_forget_system(const qpms_scatsys_t *ss);    // qg_sym.cu
@@ -335,8 +336,8 @@ void kind_tmat(const ScatsysPriv *s, int t, cd om, std::vector<qg_c> &out) {
     const qg_c k1 = cmk(kout.real(), kout.imag()), k2 = cmk(kin.real(), kin.imag()), z = cmk(zr.real(), zr.imag());
     qg_c *dT = nullptr;
     if (cudaMalloc(&dT, n * n * 16) != cudaSuccess) return;
-    if (!axsym_tmatrix_device(K.axnodes, std::max<int>(K.ax_lext, s->lMax), &s->spec, 1, &k1, &k2, &z, dT,
-                              nullptr, nullptr, 0))
+    if (!axsym_tmatrix_device(K.axnodes, K.ax_zsym, std::max<int>(K.ax_lext, s->lMax), &s->spec, 1, &k1, &k2,
+                              &z, dT, nullptr, nullptr, 0))
       cudaMemcpy(out.data(), dT, n * n * 16, cudaMemcpyDeviceToHost);
     cudaFree(dT);
     return;
@@ -541,7 +542,7 @@ qpms_scatsys_t *qpms_gpu_scatsys_create(int np, const double *pos_xyz, const int
     s->kinds[t].pint = kinds[t].type != 1 ? kinds[t].eps_interp : nullptr;
     s->kinds[t].tmi = kinds[t].type == 1 ? kinds[t].tmatrix : nullptr;
     if (kinds[t].type == 2) {
-      if (axsym_nodes(kinds[t].shape, s->kinds[t].axnodes)) {
+      if (axsym_nodes(kinds[t].shape, s->kinds[t].axnodes, &s->kinds[t].ax_zsym)) {
         qpms_gpu_scatsys_free(ss);
         return nullptr;
       }
