@@ -1,41 +1,49 @@
 // Point symmetry of finite systems and the irrep-packed (symmetry-adapted)
-// mode problem (scatsystem.c:751-1000 bases and packing, 1361-1471 packed
-// builder, 2202-2273 packed LU / solve).
+// mode problem (scatsystem.c:700-1000 projectors, bases and packing,
+// 1361-1471 packed builder, 2202-2273 packed LU / solve).
 //
-// Groups: those the reference's scripts use for rectangular arrays, generated
-// by the coordinate mirror operations (symmetries.py point_group_info:
-// trivial, C2 = rotation by pi about z, C2v = {x, y flips}, D2h = {x, y, z
-// flips}), with the reference's irrep names and its irrep order (the names
-// sorted, qpms_c.pyx:204).  Every element is a diagonal sign matrix S, and
-// all irreps are one-dimensional (characters +-1 fixed by the signs on the
-// generators).
+// Groups: the reference's point_group_info entries (symmetries.py:485-660)
+// generated by coordinate mirrors and rotations about z: trivial, C2, C2v,
+// D2h (x, y, z mirrors), C4 (rotation by pi/2), C4v (rotation by pi/2 and the
+// x mirror), D4h (those and the z mirror), with the reference's irrep names,
+// irrep matrices on the generators (E: ra = ((0,-1),(1,0)), -lam =
+// ((-1,0),(0,1)); E'' also -1 on the z mirror) and irrep order (the names
+// sorted, qpms_c.pyx:204).
 //
 // Action on VSWF coefficients (default normalisation, e^{i m phi},
 // Condon-Shortley phase), checked against the fields the oracle evaluates:
-//   z -> -z:  a_N(l,m) -> (-1)^(l+m) a_N(l,m),    a_M(l,m) -> -(-1)^(l+m) a_M(l,m)
-//   y -> -y:  a_N(l,m) -> (-1)^m a_N(l,-m),        a_M(l,m) -> -(-1)^m a_M(l,-m)
-//   x -> -x:  a_N(l,m) -> a_N(l,-m),               a_M(l,m) -> -a_M(l,-m)
-// and the particle at r goes to the particle at S r.  The representation on
-// the full coefficient vector is therefore monomial: each index goes to one
-// index with a sign.  The projector of irrep i, P_i = (1/|G|) sum_g chi_i(g) D(g),
-// maps a unit vector e_s to at most |G| entries; the normalised non-zero
-// P_i e_s of the smallest index s of every index orbit form an orthonormal
-// basis of the irrep subspace.  Packed index a is such a basis vector, stored
-// as (full index, coefficient) pairs: packed = U full with U[a][s] = c,
-// full = U^H packed.  The packed basis is this library's (particle-major
-// order); the reference orders by orbit type and uses its own orbit bases, so
-// packed vectors of the two libraries differ by a unitary change of basis
-// inside each irrep, while eigenvalues, determinants and unpacked solutions
-// agree.
+//   z -> -z:       a_N(l,m) -> (-1)^(l+m) a_N(l,m),  a_M(l,m) -> -(-1)^(l+m) a_M(l,m)
+//   y -> -y:       a_N(l,m) -> (-1)^m a_N(l,-m),      a_M(l,m) -> -(-1)^m a_M(l,-m)
+//   x -> -x:       a_N(l,m) -> a_N(l,-m),             a_M(l,m) -> -a_M(l,-m)
+//   rotation by +pi/2 about z: a(l,m) -> (-i)^m a(l,m) (both types)
+// and the particle at r goes to the particle at g r.  The representation on
+// the full coefficient vector is monomial: each index goes to one index with
+// a phase.  The projector of irrep i, P_i = (d_i/|G|) sum_g chi_i(g) D(g)
+// (the character summed from the diagonal irrep entries, as
+// qpms_orbit_irrep_projector_matrix does, scatsystem.c:716-731), maps the span
+// of an index orbit (at most |G| indices) into itself; Gram-Schmidt on the
+// images P_i e_s of the orbit's indices gives an orthonormal basis of the
+// irrep subspace there (the reference takes the SVD of the orbit projector,
+// scatsystem.c:758-800): one vector per orbit for a 1D irrep, d x
+// multiplicity for a d-dimensional one.  Packed index a is such a basis
+// vector b_a, stored as (full index, coefficient) pairs of U = [b_a^H]:
+// packed = U full, full = U^H packed.  The packed basis is this library's
+// (particle-major order); the reference orders by orbit type and uses its own
+// orbit bases, so packed vectors of the two libraries differ by a unitary
+// change of basis inside each irrep, while eigenvalues, determinants and
+// unpacked solutions agree.
 //
 // On the GPU: irrep_pack_kernel forms U M U^H from the full matrix (each
 // packed element gathers at most |G|^2 products); pack / unpack kernels move
-// right-hand sides and solutions between the full and the packed bases.
+// right-hand sides and solutions between the full and the packed bases
+// (unpacking through the transposed table, one thread per full index).
 #include <math.h>
 #include <string.h>
 
 #include <algorithm>
 #include <array>
+#include <complex>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -44,10 +52,12 @@
 
 namespace qg {
 
+typedef std::complex<double> cdx;
+
 struct SymDevCopy {
   int dev = -1;
-  int *off = nullptr, *idx = nullptr;
-  double *val = nullptr;
+  int *off = nullptr, *idx = nullptr, *toff = nullptr, *tidx = nullptr;
+  qg_c *val = nullptr, *tval = nullptr;
 };
 
 struct SymData {
@@ -55,9 +65,12 @@ struct SymData {
   std::string group;
   int order = 1;
   std::vector<std::string> names;
+  std::vector<int> dims;                     // irrep dimensions
   std::vector<size_t> sizes;                 // saecv_sizes
-  std::vector<std::vector<int>> off, idx;    // [irrep] CSR: packed a -> entries off[a]..off[a+1]
-  std::vector<std::vector<double>> val;
+  std::vector<std::vector<int>> off, idx;    // [irrep] CSR of U: packed a -> entries off[a]..off[a+1]
+  std::vector<std::vector<cdx>> val;         // U[a][idx]
+  std::vector<std::vector<int>> toff, tidx;  // [irrep] CSR of U^H: full s -> (packed a, conj U[a][s])
+  std::vector<std::vector<cdx>> tval;
   std::vector<std::vector<SymDevCopy>> dev;  // [irrep] device copies
   std::mutex mu;
   ~SymData() {
@@ -66,6 +79,9 @@ struct SymData {
         cudaFree(d.off);
         cudaFree(d.idx);
         cudaFree(d.val);
+        cudaFree(d.toff);
+        cudaFree(d.tidx);
+        cudaFree(d.tval);
       }
   }
 };
@@ -78,99 +94,154 @@ std::vector<SymData *> &sym_table() {
   return *t;
 }
 
+// generators: 'X', 'Y', 'Z' mirrors (x -> -x etc.), 'R' rotation by +pi/2
+// about z, 'C' rotation by pi about z
+struct IrrepDef {
+  const char *name;
+  int dim;
+  std::vector<std::vector<cdx>> gen;  // d x d row-major matrix per generator
+};
 struct GroupDef {
   const char *name;
-  std::vector<std::array<int, 3>> gens;
-  std::vector<std::pair<const char *, std::vector<int>>> irreps;  // name, signs on the generators
+  std::string gens;
+  std::vector<IrrepDef> irreps;
 };
 
+std::vector<cdx> sc(double v) { return {cdx(v, 0)}; }
+
 const std::vector<GroupDef> &group_defs() {
+  static const std::vector<cdx> ra = {0, -1, 1, 0}, mlam = {-1, 0, 0, 1}, eps = {1, 0, 0, 1}, meps = {-1, 0, 0, -1};
   static const std::vector<GroupDef> defs = {
-      {"trivial", {}, {{"A", {}}}},
-      {"C2", {{{-1, -1, 1}}}, {{"A", {1}}, {"B", {-1}}}},
-      {"C2v", {{{-1, 1, 1}}, {{1, -1, 1}}}, {{"A1", {1, 1}}, {"B2", {-1, 1}}, {"A2", {-1, -1}}, {"B1", {1, -1}}}},
-      {"D2h",
-       {{{-1, 1, 1}}, {{1, -1, 1}}, {{1, 1, -1}}},
-       {{"A1'", {1, 1, 1}},
-        {"B2'", {-1, 1, 1}},
-        {"A2'", {-1, -1, 1}},
-        {"B1'", {1, -1, 1}},
-        {"A1''", {-1, -1, -1}},
-        {"B2''", {1, -1, -1}},
-        {"A2''", {1, 1, -1}},
-        {"B1''", {-1, 1, -1}}}},
+      {"trivial", "", {{"A", 1, {}}}},
+      {"C2", "C", {{"A", 1, {sc(1)}}, {"B", 1, {sc(-1)}}}},
+      {"C2v", "XY",
+       {{"A1", 1, {sc(1), sc(1)}}, {"B2", 1, {sc(-1), sc(1)}}, {"A2", 1, {sc(-1), sc(-1)}},
+        {"B1", 1, {sc(1), sc(-1)}}}},
+      {"D2h", "XYZ",
+       {{"A1'", 1, {sc(1), sc(1), sc(1)}},
+        {"B2'", 1, {sc(-1), sc(1), sc(1)}},
+        {"A2'", 1, {sc(-1), sc(-1), sc(1)}},
+        {"B1'", 1, {sc(1), sc(-1), sc(1)}},
+        {"A1''", 1, {sc(-1), sc(-1), sc(-1)}},
+        {"B2''", 1, {sc(1), sc(-1), sc(-1)}},
+        {"A2''", 1, {sc(1), sc(1), sc(-1)}},
+        {"B1''", 1, {sc(-1), sc(1), sc(-1)}}}},
+      {"C4", "R",
+       {{"A", 1, {sc(1)}}, {"B", 1, {sc(-1)}}, {"1E", 1, {{cdx(0, -1)}}}, {"2E", 1, {{cdx(0, 1)}}}}},
+      {"C4v", "RX",
+       {{"E", 2, {ra, mlam}},
+        {"A1", 1, {sc(1), sc(1)}},
+        {"A2", 1, {sc(1), sc(-1)}},
+        {"B1", 1, {sc(-1), sc(1)}},
+        {"B2", 1, {sc(-1), sc(-1)}}}},
+      {"D4h", "RXZ",
+       {{"E'", 2, {ra, mlam, eps}},
+        {"E''", 2, {ra, mlam, meps}},
+        {"A1'", 1, {sc(1), sc(1), sc(1)}},
+        {"A2'", 1, {sc(1), sc(-1), sc(1)}},
+        {"A1''", 1, {sc(1), sc(-1), sc(-1)}},
+        {"A2''", 1, {sc(1), sc(1), sc(-1)}},
+        {"B1'", 1, {sc(-1), sc(1), sc(1)}},
+        {"B2'", 1, {sc(-1), sc(-1), sc(1)}},
+        {"B1''", 1, {sc(-1), sc(-1), sc(-1)}},
+        {"B2''", 1, {sc(-1), sc(1), sc(-1)}}}},
   };
   return defs;
 }
 
-// Wave index j' and sign of the image of wave j (bspec order: electric block
-// y = l(l+1)+m-1, then magnetic) under the diagonal sign matrix S.
-void wave_image(int lMax, const std::array<int, 3> &S, int j, int *jo, int *sg) {
+// Position matrix (3 x 3 integers, row-major) of a generator.
+std::array<int, 9> gen_matrix(char g) {
+  switch (g) {
+    case 'X': return {-1, 0, 0, 0, 1, 0, 0, 0, 1};
+    case 'Y': return {1, 0, 0, 0, -1, 0, 0, 0, 1};
+    case 'Z': return {1, 0, 0, 0, 1, 0, 0, 0, -1};
+    case 'C': return {-1, 0, 0, 0, -1, 0, 0, 0, 1};
+    default: return {0, -1, 0, 1, 0, 0, 0, 0, 1};  // 'R': (x, y) -> (-y, x)
+  }
+}
+
+// Image j' and phase of wave j (bspec order: electric block y = l(l+1)+m-1,
+// then magnetic) under one generator.
+void gen_wave(int lMax, char g, int j, int *jo, cdx *ph) {
   const int ne = lMax * (lMax + 2);
   const bool mag = j >= ne;
   const int y = mag ? j - ne : j;
   const int l = (int)floor(sqrt((double)y + 1) + 1e-9);
   int m = y - (l * (l + 1) - 1);
-  int s = 1;
   const int tsg = mag ? -1 : 1;
-  if (S[2] < 0) s *= (((l + m) & 1) ? -1 : 1) * tsg;
-  if (S[1] < 0) {
-    s *= ((m & 1) ? -1 : 1) * tsg;
-    m = -m;
-  }
-  if (S[0] < 0) {
-    s *= tsg;
-    m = -m;
+  cdx p = 1.0;
+  switch (g) {
+    case 'Z': p = (double)((((l + m) & 1) ? -1 : 1) * tsg); break;
+    case 'Y':
+      p = (double)(((m & 1) ? -1 : 1) * tsg);
+      m = -m;
+      break;
+    case 'X':
+      p = (double)tsg;
+      m = -m;
+      break;
+    case 'C': p = (double)((m & 1) ? -1 : 1); break;  // X then Y: (-1)^m
+    default: {                                        // 'R': (-i)^m
+      static const cdx mi[4] = {cdx(1, 0), cdx(0, -1), cdx(-1, 0), cdx(0, 1)};
+      p = mi[((m % 4) + 4) % 4];
+    }
   }
   *jo = (mag ? ne : 0) + l * (l + 1) + m - 1;
-  *sg = s;
+  *ph = p;
 }
 
+struct Element {
+  std::array<int, 9> M;
+  std::vector<int> wimg;  // wave image
+  std::vector<cdx> wph;   // phase
+  std::vector<std::vector<cdx>> rep;  // irrep matrices
+};
+
 __global__ void irrep_pack_kernel(const qg_c *__restrict__ M, size_t ldm, int na, const int *__restrict__ off,
-                                  const int *__restrict__ idx, const double *__restrict__ val, qg_c *__restrict__ out) {
+                                  const int *__restrict__ idx, const qg_c *__restrict__ val, qg_c *__restrict__ out) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (size_t)na * na) return;
   const int a = (int)(t / na), b = (int)(t % na);
   double re = 0, im = 0;
   for (int i = off[a]; i < off[a + 1]; ++i) {
     const qg_c *row = M + (size_t)idx[i] * ldm;
-    double rr = 0, ri = 0;
+    double rr = 0, ri = 0;  // sum_j M[i][j] conj(U[b][j])
     for (int j = off[b]; j < off[b + 1]; ++j) {
-      const qg_c v = row[idx[j]];
-      rr = fma(val[j], v.re, rr);
-      ri = fma(val[j], v.im, ri);
+      const qg_c v = row[idx[j]], u = val[j];
+      rr = fma(v.re, u.re, fma(v.im, u.im, rr));
+      ri = fma(v.im, u.re, fma(-v.re, u.im, ri));
     }
-    re = fma(val[i], rr, re);
-    im = fma(val[i], ri, im);
+    const qg_c u = val[i];
+    re = fma(u.re, rr, fma(-u.im, ri, re));
+    im = fma(u.re, ri, fma(u.im, rr, im));
   }
   out[t] = cmk(re, im);
 }
 
-// out[a] = sum over the entries of a of c * v[s]
+// out[a] = sum over the entries of a of U[a][s] v[s]
 __global__ void irrep_pack_vec_kernel(const qg_c *__restrict__ v, int na, int nrhs, size_t ldv, size_t ldo,
                                       const int *__restrict__ off, const int *__restrict__ idx,
-                                      const double *__restrict__ val, qg_c *__restrict__ out) {
+                                      const qg_c *__restrict__ val, qg_c *__restrict__ out) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (size_t)na * nrhs) return;
   const int a = (int)(t % na), r = (int)(t / na);
   qg_c acc = cmk(0, 0);
-  for (int i = off[a]; i < off[a + 1]; ++i) acc = cadd(acc, cscale(v[(size_t)r * ldv + idx[i]], val[i]));
+  for (int i = off[a]; i < off[a + 1]; ++i) acc = cadd(acc, cmul(val[i], v[(size_t)r * ldv + idx[i]]));
   out[(size_t)r * ldo + a] = acc;
 }
 
-// full[s] += c * packed[a] over the entries (each full index appears at most
-// once per irrep, so the threads of one irrep never write the same element)
-__global__ void irrep_unpack_vec_kernel(const qg_c *__restrict__ p, int na, int nrhs, size_t ldp, size_t ldf,
-                                        const int *__restrict__ off, const int *__restrict__ idx,
-                                        const double *__restrict__ val, qg_c *__restrict__ full) {
+// full[s] += sum over the packed a of conj(U[a][s]) packed[a] (transposed
+// table: one thread per full index, no write conflicts)
+__global__ void irrep_unpack_vec_kernel(const qg_c *__restrict__ p, int nfull, int nrhs, size_t ldp, size_t ldf,
+                                        const int *__restrict__ toff, const int *__restrict__ tidx,
+                                        const qg_c *__restrict__ tval, qg_c *__restrict__ full) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)na * nrhs) return;
-  const int a = (int)(t % na), r = (int)(t / na);
-  const qg_c x = p[(size_t)r * ldp + a];
-  for (int i = off[a]; i < off[a + 1]; ++i) {
-    qg_c &o = full[(size_t)r * ldf + idx[i]];
-    o = cadd(o, cscale(x, val[i]));
-  }
+  if (t >= (size_t)nfull * nrhs) return;
+  const int sidx = (int)(t % nfull), r = (int)(t / nfull);
+  if (toff[sidx] == toff[sidx + 1]) return;
+  qg_c acc = full[(size_t)r * ldf + sidx];
+  for (int i = toff[sidx]; i < toff[sidx + 1]; ++i) acc = cadd(acc, cmul(tval[i], p[(size_t)r * ldp + tidx[i]]));
+  full[(size_t)r * ldf + sidx] = acc;
 }
 
 }  // namespace
@@ -193,30 +264,35 @@ void sym_forget_system(const qpms_scatsys_t *ss) {
     }
 }
 
-// Device CSR of irrep iri (uploaded on first use on the current device).
-int sym_device(SymData *sd, int iri, const int **off, const int **idx, const double **val) {
+// Device tables of irrep iri (uploaded on first use on the current device).
+int sym_device(SymData *sd, int iri, SymDevCopy *out) {
   int dev = 0;
   QG_CUDA_TRY(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> g(sd->mu);
   for (auto &d : sd->dev[iri])
     if (d.dev == dev) {
-      *off = d.off;
-      *idx = d.idx;
-      *val = d.val;
+      *out = d;
       return QPMS_SUCCESS;
     }
   SymDevCopy d;
   d.dev = dev;
-  QG_CUDA_TRY(cudaMalloc(&d.off, sd->off[iri].size() * 4));
-  QG_CUDA_TRY(cudaMalloc(&d.idx, std::max<size_t>(1, sd->idx[iri].size()) * 4));
-  QG_CUDA_TRY(cudaMalloc(&d.val, std::max<size_t>(1, sd->val[iri].size()) * 8));
-  QG_CUDA_TRY(cudaMemcpy(d.off, sd->off[iri].data(), sd->off[iri].size() * 4, cudaMemcpyHostToDevice));
-  QG_CUDA_TRY(cudaMemcpy(d.idx, sd->idx[iri].data(), sd->idx[iri].size() * 4, cudaMemcpyHostToDevice));
-  QG_CUDA_TRY(cudaMemcpy(d.val, sd->val[iri].data(), sd->val[iri].size() * 8, cudaMemcpyHostToDevice));
+  const auto put_i = [](int **p, const std::vector<int> &v) -> int {
+    QG_CUDA_TRY(cudaMalloc(p, std::max<size_t>(1, v.size()) * 4));
+    QG_CUDA_TRY(cudaMemcpy(*p, v.data(), v.size() * 4, cudaMemcpyHostToDevice));
+    return QPMS_SUCCESS;
+  };
+  const auto put_c = [](qg_c **p, const std::vector<cdx> &v) -> int {
+    QG_CUDA_TRY(cudaMalloc(p, std::max<size_t>(1, v.size()) * 16));
+    QG_CUDA_TRY(cudaMemcpy(*p, v.data(), v.size() * 16, cudaMemcpyHostToDevice));
+    return QPMS_SUCCESS;
+  };
+  int e;
+  if ((e = put_i(&d.off, sd->off[iri])) || (e = put_i(&d.idx, sd->idx[iri])) || (e = put_c(&d.val, sd->val[iri])) ||
+      (e = put_i(&d.toff, sd->toff[iri])) || (e = put_i(&d.tidx, sd->tidx[iri])) ||
+      (e = put_c(&d.tval, sd->tval[iri])))
+    return e;
   sd->dev[iri].push_back(d);
-  *off = d.off;
-  *idx = d.idx;
-  *val = d.val;
+  *out = d;
   return QPMS_SUCCESS;
 }
 
@@ -225,13 +301,14 @@ int sym_pack_matrix_device(const qpms_scatsys_t *ss, int iri, const qg_c *dM, si
                            cudaStream_t st) {
   SymData *sd = sym_of(ss);
   if (!sd) { set_error("system has no symmetry"); return QPMS_EINVAL; }
-  const int *o, *ix;
-  const double *v;
+  SymDevCopy Dc;
+  const SymDevCopy *D = &Dc;
   int e;
-  if ((e = sym_device(sd, iri, &o, &ix, &v))) return e;
+  if ((e = sym_device(sd, iri, &Dc))) return e;
   const size_t na = sd->sizes[iri];
   if (!na) return QPMS_SUCCESS;
-  irrep_pack_kernel<<<(unsigned)((na * na + 255) / 256), 256, 0, st>>>(dM, ldm, (int)na, o, ix, v, dout);
+  irrep_pack_kernel<<<(unsigned)((na * na + 255) / 256), 256, 0, st>>>(dM, ldm, (int)na, D->off, D->idx, D->val,
+                                                                      dout);
   g_launches.fetch_add(1);
   QG_CUDA_TRY(cudaGetLastError());
   return QPMS_SUCCESS;
@@ -241,14 +318,14 @@ int sym_pack_vectors_device(const qpms_scatsys_t *ss, int iri, const qg_c *dv, i
                             size_t ldo, cudaStream_t st) {
   SymData *sd = sym_of(ss);
   if (!sd) { set_error("system has no symmetry"); return QPMS_EINVAL; }
-  const int *o, *ix;
-  const double *v;
+  SymDevCopy Dc;
+  const SymDevCopy *D = &Dc;
   int e;
-  if ((e = sym_device(sd, iri, &o, &ix, &v))) return e;
+  if ((e = sym_device(sd, iri, &Dc))) return e;
   const size_t na = sd->sizes[iri];
   if (!na) return QPMS_SUCCESS;
-  irrep_pack_vec_kernel<<<(unsigned)((na * nrhs + 255) / 256), 256, 0, st>>>(dv, (int)na, nrhs, ldv, ldo, o, ix,
-                                                                            v, dout);
+  irrep_pack_vec_kernel<<<(unsigned)((na * nrhs + 255) / 256), 256, 0, st>>>(dv, (int)na, nrhs, ldv, ldo, D->off,
+                                                                            D->idx, D->val, dout);
   g_launches.fetch_add(1);
   QG_CUDA_TRY(cudaGetLastError());
   return QPMS_SUCCESS;
@@ -258,14 +335,14 @@ int sym_unpack_add_vectors_device(const qpms_scatsys_t *ss, int iri, const qg_c 
                                   qg_c *dfull, size_t ldf, cudaStream_t st) {
   SymData *sd = sym_of(ss);
   if (!sd) { set_error("system has no symmetry"); return QPMS_EINVAL; }
-  const int *o, *ix;
-  const double *v;
+  SymDevCopy Dc;
+  const SymDevCopy *D = &Dc;
   int e;
-  if ((e = sym_device(sd, iri, &o, &ix, &v))) return e;
-  const size_t na = sd->sizes[iri];
+  if ((e = sym_device(sd, iri, &Dc))) return e;
+  const size_t na = sd->sizes[iri], N = ss->fecv_size;
   if (!na) return QPMS_SUCCESS;
-  irrep_unpack_vec_kernel<<<(unsigned)((na * nrhs + 255) / 256), 256, 0, st>>>(dp, (int)na, nrhs, ldp, ldf, o, ix,
-                                                                              v, dfull);
+  irrep_unpack_vec_kernel<<<(unsigned)((N * nrhs + 255) / 256), 256, 0, st>>>(dp, (int)N, nrhs, ldp, ldf, D->toff,
+                                                                             D->tidx, D->tval, dfull);
   g_launches.fetch_add(1);
   QG_CUDA_TRY(cudaGetLastError());
   return QPMS_SUCCESS;
@@ -340,9 +417,10 @@ using namespace qg;
 extern "C" {
 
 // Gives a finite system the point symmetry `group` ("trivial", "C2", "C2v",
-// "D2h"; the reference's point_group_info entries of these names).  Checks
-// that every operation maps each particle onto a particle of the same kind;
-// the particles' T-matrices must be invariant (Mie spheres are).
+// "D2h", "C4", "C4v", "D4h"; the reference's point_group_info entries of
+// these names).  Checks that every operation maps each particle onto a
+// particle of the same kind; the particles' T-matrices must be invariant
+// (Mie spheres are).
 int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group) {
   clear_error();
   if (!ss || !group) { set_error("NULL argument"); return QPMS_EINVAL; }
@@ -353,20 +431,59 @@ int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group) {
   const GroupDef *gd = nullptr;
   for (const auto &g : group_defs())
     if (!strcmp(g.name, group)) gd = &g;
-  if (!gd) { set_error("unknown point group %s (trivial, C2, C2v, D2h)", group); return QPMS_EINVAL; }
+  if (!gd) { set_error("unknown point group %s (trivial, C2, C2v, D2h, C4, C4v, D4h)", group); return QPMS_EINVAL; }
   const int np = ss->p_count, n = (int)(ss->fecv_size / np), N = (int)ss->fecv_size;
   const int lMax = (int)lround(sqrt(n / 2.0 + 1) - 1);
-  const int ng = (int)gd->gens.size(), order = 1 << ng;
-  // elements: products of generator subsets (bit b <-> generator b)
-  std::vector<std::array<int, 3>> el(order);
-  for (int e = 0; e < order; ++e) {
-    std::array<int, 3> S = {1, 1, 1};
-    for (int b = 0; b < ng; ++b)
-      if (e >> b & 1)
-        for (int c = 0; c < 3; ++c) S[c] *= gd->gens[b][c];
-    el[e] = S;
+  const int ng = (int)gd->gens.size(), nir = (int)gd->irreps.size();
+  // ---- the group: closure of the generators (element = g o previous) ----
+  std::vector<Element> el(1);
+  el[0].M = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  el[0].wimg.resize(n);
+  el[0].wph.assign(n, 1.0);
+  for (int j = 0; j < n; ++j) el[0].wimg[j] = j;
+  el[0].rep.resize(nir);
+  for (int i = 0; i < nir; ++i) {
+    const int d = gd->irreps[i].dim;
+    el[0].rep[i].assign(d * d, 0.0);
+    for (int a = 0; a < d; ++a) el[0].rep[i][a * d + a] = 1.0;
   }
-  // particle permutations
+  std::vector<std::vector<int>> gimg(ng, std::vector<int>(n));
+  std::vector<std::vector<cdx>> gph(ng, std::vector<cdx>(n));
+  for (int b = 0; b < ng; ++b)
+    for (int j = 0; j < n; ++j) gen_wave(lMax, gd->gens[b], j, &gimg[b][j], &gph[b][j]);
+  for (size_t q = 0; q < el.size() && el.size() <= 64; ++q)
+    for (int b = 0; b < ng; ++b) {
+      const std::array<int, 9> G = gen_matrix(gd->gens[b]);
+      Element e;
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+          int v = 0;
+          for (int k = 0; k < 3; ++k) v += G[r * 3 + k] * el[q].M[k * 3 + c];
+          e.M[r * 3 + c] = v;
+        }
+      bool seen = false;
+      for (const auto &x : el) seen = seen || x.M == e.M;
+      if (seen) continue;
+      e.wimg.resize(n);
+      e.wph.resize(n);
+      for (int j = 0; j < n; ++j) {
+        const int j1 = el[q].wimg[j];
+        e.wimg[j] = gimg[b][j1];
+        e.wph[j] = el[q].wph[j] * gph[b][j1];
+      }
+      e.rep.resize(nir);
+      for (int i = 0; i < nir; ++i) {
+        const int d = gd->irreps[i].dim;
+        const std::vector<cdx> &Gm = gd->irreps[i].gen[b];
+        e.rep[i].assign(d * d, 0.0);
+        for (int r = 0; r < d; ++r)
+          for (int c = 0; c < d; ++c)
+            for (int k = 0; k < d; ++k) e.rep[i][r * d + c] += Gm[r * d + k] * el[q].rep[i][k * d + c];
+      }
+      el.push_back(std::move(e));
+    }
+  const int order = (int)el.size();
+  // ---- particle permutations ----
   double scale = 0;
   for (int p = 0; p < np; ++p)
     scale = std::max(scale, fabs(ss->p[p].pos.x) + fabs(ss->p[p].pos.y) + fabs(ss->p[p].pos.z));
@@ -374,10 +491,12 @@ int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group) {
   std::vector<std::vector<int>> perm(order, std::vector<int>(np, -1));
   for (int e = 0; e < order; ++e)
     for (int p = 0; p < np; ++p) {
-      const double x = el[e][0] * ss->p[p].pos.x, y = el[e][1] * ss->p[p].pos.y, z = el[e][2] * ss->p[p].pos.z;
+      const double r0[3] = {ss->p[p].pos.x, ss->p[p].pos.y, ss->p[p].pos.z};
+      double x[3];
+      for (int r = 0; r < 3; ++r) x[r] = el[e].M[r * 3] * r0[0] + el[e].M[r * 3 + 1] * r0[1] + el[e].M[r * 3 + 2] * r0[2];
       for (int q = 0; q < np; ++q)
-        if (fabs(ss->p[q].pos.x - x) <= tol && fabs(ss->p[q].pos.y - y) <= tol && fabs(ss->p[q].pos.z - z) <= tol &&
-            ss->p[q].tmatrix_id == ss->p[p].tmatrix_id) {
+        if (fabs(ss->p[q].pos.x - x[0]) <= tol && fabs(ss->p[q].pos.y - x[1]) <= tol &&
+            fabs(ss->p[q].pos.z - x[2]) <= tol && ss->p[q].tmatrix_id == ss->p[p].tmatrix_id) {
           perm[e][p] = q;
           break;
         }
@@ -386,68 +505,83 @@ int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group) {
         return QPMS_EINVAL;
       }
     }
-  // wave images
-  std::vector<std::vector<int>> wimg(order, std::vector<int>(n)), wsg(order, std::vector<int>(n));
-  for (int e = 0; e < order; ++e)
-    for (int j = 0; j < n; ++j) wave_image(lMax, el[e], j, &wimg[e][j], &wsg[e][j]);
   auto *sd = new SymData();
   sd->ss = ss;
   sd->group = group;
   sd->order = order;
   // irreps in the reference's order: names sorted
-  std::vector<int> ord(gd->irreps.size());
-  for (size_t i = 0; i < ord.size(); ++i) ord[i] = (int)i;
-  std::sort(ord.begin(), ord.end(),
-            [&](int a, int b) { return std::string(gd->irreps[a].first) < std::string(gd->irreps[b].first); });
-  const int nir = (int)ord.size();
+  std::vector<int> ord(nir);
+  for (int i = 0; i < nir; ++i) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](int a, int b) {
+    return std::string(gd->irreps[a].name) < std::string(gd->irreps[b].name);
+  });
   sd->names.resize(nir);
+  sd->dims.resize(nir);
   sd->sizes.assign(nir, 0);
   sd->off.assign(nir, std::vector<int>(1, 0));
   sd->idx.resize(nir);
   sd->val.resize(nir);
   sd->dev.resize(nir);
-  // smallest index of each index orbit
-  std::vector<char> isrep(N, 1);
+  // ---- index orbits ----
+  std::vector<int> orbit_of(N, -1);
+  std::vector<std::vector<int>> orbits;
   for (int s = 0; s < N; ++s) {
+    if (orbit_of[s] >= 0) continue;
     const int p = s / n, j = s % n;
-    for (int e = 0; e < order; ++e)
-      if (perm[e][p] * n + wimg[e][j] < s) isrep[s] = 0;
-  }
-  std::vector<double> acc(N, 0.0);
-  std::vector<int> touched;
-  for (int ii = 0; ii < nir; ++ii) {
-    const auto &ir = gd->irreps[ord[ii]];
-    sd->names[ii] = ir.first;
-    std::vector<int> chi(order);
+    std::vector<int> o;
     for (int e = 0; e < order; ++e) {
-      int c = 1;
-      for (int b = 0; b < ng; ++b)
-        if (e >> b & 1) c *= ir.second[b];
-      chi[e] = c;
+      const int t = perm[e][p] * n + el[e].wimg[j];
+      if (std::find(o.begin(), o.end(), t) == o.end()) o.push_back(t);
     }
-    for (int s = 0; s < N; ++s) {
-      if (!isrep[s]) continue;
-      const int p = s / n, j = s % n;
-      touched.clear();
-      for (int e = 0; e < order; ++e) {
-        const int t = perm[e][p] * n + wimg[e][j];
-        if (std::find(touched.begin(), touched.end(), t) == touched.end()) touched.push_back(t);
-        acc[t] += (double)chi[e] * wsg[e][j];
-      }
-      double nrm = 0;
-      for (int t : touched) nrm += acc[t] * acc[t];
-      if (nrm > 0.5) {  // entries are integers: non-zero projection
-        std::sort(touched.begin(), touched.end());
+    std::sort(o.begin(), o.end());
+    for (int t : o) orbit_of[t] = (int)orbits.size();
+    orbits.push_back(o);
+  }
+  // ---- bases: Gram-Schmidt on P e_s over each orbit ----
+  for (int ii = 0; ii < nir; ++ii) {
+    const IrrepDef &ir = gd->irreps[ord[ii]];
+    sd->names[ii] = ir.name;
+    sd->dims[ii] = ir.dim;
+    const int d = ir.dim;
+    std::vector<cdx> chi(order);
+    for (int e = 0; e < order; ++e) {
+      cdx c = 0;
+      for (int a = 0; a < d; ++a) c += el[e].rep[ord[ii]][a * d + a];
+      chi[e] = c * (double)d / (double)order;
+    }
+    for (const auto &o : orbits) {
+      const int no = (int)o.size();
+      std::vector<std::vector<cdx>> basis;
+      for (int si = 0; si < no; ++si) {
+        const int s = o[si], p = s / n, j = s % n;
+        std::vector<cdx> v(no, 0.0);
+        for (int e = 0; e < order; ++e) {
+          const int t = perm[e][p] * n + el[e].wimg[j];
+          const int ti = (int)(std::lower_bound(o.begin(), o.end(), t) - o.begin());
+          v[ti] += chi[e] * el[e].wph[j];
+        }
+        for (int pass = 0; pass < 2; ++pass)  // re-orthogonalised once
+          for (const auto &b : basis) {
+            cdx dot = 0;
+            for (int k = 0; k < no; ++k) dot += std::conj(b[k]) * v[k];
+            for (int k = 0; k < no; ++k) v[k] -= dot * b[k];
+          }
+        double nrm = 0;
+        for (int k = 0; k < no; ++k) nrm += std::norm(v[k]);
+        if (nrm < 1e-16) continue;
         const double inv = 1.0 / sqrt(nrm);
-        for (int t : touched)
-          if (acc[t] != 0) {
-            sd->idx[ii].push_back(t);
-            sd->val[ii].push_back(acc[t] * inv);
+        for (int k = 0; k < no; ++k) v[k] *= inv;
+        basis.push_back(v);
+      }
+      for (const auto &b : basis) {
+        for (int k = 0; k < no; ++k)
+          if (std::abs(b[k]) > 1e-15) {
+            sd->idx[ii].push_back(o[k]);
+            sd->val[ii].push_back(std::conj(b[k]));  // U[a][s] = conj(b_a[s])
           }
         sd->off[ii].push_back((int)sd->idx[ii].size());
         ++sd->sizes[ii];
       }
-      for (int t : touched) acc[t] = 0;
     }
   }
   size_t tot = 0;
@@ -456,6 +590,24 @@ int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group) {
     set_error("internal: irrep bases span %zu of %d dimensions", tot, N);
     delete sd;
     return QPMS_ERROR;
+  }
+  // transposed tables (U^H: full s -> packed a, conj U[a][s])
+  sd->toff.resize(nir);
+  sd->tidx.resize(nir);
+  sd->tval.resize(nir);
+  for (int ii = 0; ii < nir; ++ii) {
+    std::vector<std::vector<std::pair<int, cdx>>> rows(N);
+    for (size_t a = 0; a < sd->sizes[ii]; ++a)
+      for (int i = sd->off[ii][a]; i < sd->off[ii][a + 1]; ++i)
+        rows[sd->idx[ii][i]].push_back({(int)a, std::conj(sd->val[ii][i])});
+    sd->toff[ii].assign(1, 0);
+    for (int t = 0; t < N; ++t) {
+      for (const auto &x : rows[t]) {
+        sd->tidx[ii].push_back(x.first);
+        sd->tval[ii].push_back(x.second);
+      }
+      sd->toff[ii].push_back((int)sd->tidx[ii].size());
+    }
   }
   sym_forget_system(ss);
   {
@@ -489,7 +641,10 @@ qpms_complex_t *qpms_scatsys_irrep_transform_matrix(qpms_complex_t *U, const qpm
   if (!U) { set_error("out of host memory"); return nullptr; }
   memset(U, 0, na * N * 16);
   for (size_t a = 0; a < na; ++a)
-    for (int i = sd->off[iri][a]; i < sd->off[iri][a + 1]; ++i) U[a * N + sd->idx[iri][i]].re = sd->val[iri][i];
+    for (int i = sd->off[iri][a]; i < sd->off[iri][a + 1]; ++i) {
+      U[a * N + sd->idx[iri][i]].re = sd->val[iri][i].real();
+      U[a * N + sd->idx[iri][i]].im = sd->val[iri][i].imag();
+    }
   return U;
 }
 
@@ -502,13 +657,13 @@ qpms_complex_t *qpms_scatsys_irrep_pack_vector(qpms_complex_t *target, const qpm
   if (!target) target = (qpms_complex_t *)malloc(std::max<size_t>(1, na) * 16);
   if (!target) { set_error("out of host memory"); return nullptr; }
   for (size_t a = 0; a < na; ++a) {
-    double re = 0, im = 0;
+    cdx acc = 0;
     for (int i = sd->off[iri][a]; i < sd->off[iri][a + 1]; ++i) {
-      re += sd->val[iri][i] * orig[sd->idx[iri][i]].re;
-      im += sd->val[iri][i] * orig[sd->idx[iri][i]].im;
+      const qpms_complex_t &o = orig[sd->idx[iri][i]];
+      acc += sd->val[iri][i] * cdx(o.re, o.im);
     }
-    target[a].re = re;
-    target[a].im = im;
+    target[a].re = acc.real();
+    target[a].im = acc.imag();
   }
   return target;
 }
@@ -524,8 +679,9 @@ qpms_complex_t *qpms_scatsys_irrep_unpack_vector(qpms_complex_t *target, const q
   if (!add) memset(target, 0, N * 16);
   for (size_t a = 0; a < na; ++a)
     for (int i = sd->off[iri][a]; i < sd->off[iri][a + 1]; ++i) {
-      target[sd->idx[iri][i]].re += sd->val[iri][i] * orig[a].re;
-      target[sd->idx[iri][i]].im += sd->val[iri][i] * orig[a].im;
+      const cdx v = std::conj(sd->val[iri][i]) * cdx(orig[a].re, orig[a].im);
+      target[sd->idx[iri][i]].re += v.real();
+      target[sd->idx[iri][i]].im += v.imag();
     }
   return target;
 }
@@ -561,12 +717,13 @@ qpms_complex_t *qpms_scatsys_irrep_unpack_matrix(qpms_complex_t *target, const q
   const auto &val = sd->val[iri];
   for (size_t a = 0; a < na; ++a)
     for (size_t b = 0; b < na; ++b) {
-      const qpms_complex_t x = orig[a * na + b];
+      const cdx x(orig[a * na + b].re, orig[a * na + b].im);
       for (int i = off[a]; i < off[a + 1]; ++i)
         for (int j = off[b]; j < off[b + 1]; ++j) {
+          const cdx v = std::conj(val[i]) * x * val[j];
           qpms_complex_t &o = target[(size_t)idx[i] * N + idx[j]];
-          o.re += val[i] * val[j] * x.re;
-          o.im += val[i] * val[j] * x.im;
+          o.re += v.real();
+          o.im += v.imag();
         }
     }
   return target;

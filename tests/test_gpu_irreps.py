@@ -36,13 +36,21 @@ def rect_array(nx, ny, px, py):
 
 
 REF_NAMES = {"D2h": ["A1'", "A1''", "A2'", "A2''", "B1'", "B1''", "B2'", "B2''"],
-             "C2v": ["A1", "A2", "B1", "B2"], "C2": ["A", "B"], "trivial": ["A"]}
+             "C2v": ["A1", "A2", "B1", "B2"], "C2": ["A", "B"], "trivial": ["A"],
+             "C4": ["1E", "2E", "A", "B"], "C4v": ["A1", "A2", "B1", "B2", "E"],
+             "D4h": ["A1'", "A1''", "A2'", "A2''", "B1'", "B1''", "B2'", "B2''", "E'", "E''"]}
 
 
 @pytest.mark.parametrize("group,nx,ny,lMax", [("D2h", 4, 3, 2), ("D2h", 3, 3, 3), ("C2v", 3, 2, 2),
-                                              ("C2", 4, 4, 1), ("trivial", 2, 2, 2)])
+                                              ("C2", 4, 4, 1), ("trivial", 2, 2, 2),
+                                              ("D4h", 4, 4, 2), ("D4h", 3, 3, 3), ("C4v", 3, 3, 2),
+                                              ("C4", 4, 4, 2)])
 def test_bases_and_block_diagonal_oracle_matrix(gpu, orc, group, nx, ny, lMax):
-    pos = rect_array(nx, ny, 400e-9, 330e-9)
+    """Square groups (C4, C4v, D4h: rotations by pi/2, two-dimensional E
+    irreps with d x multiplicity packed vectors, complex bases) on square
+    arrays; the mirror groups on rectangular ones."""
+    py = 400e-9 if group in ("C4", "C4v", "D4h") else 330e-9
+    pos = rect_array(nx, ny, 400e-9, py)
     ss = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax, sym=group)
     assert ss.irrep_names == REF_NAMES[group]
     assert sum(ss.saecv_sizes) == ss.fecv_size
@@ -74,10 +82,11 @@ def test_bases_and_block_diagonal_oracle_matrix(gpu, orc, group, nx, ny, lMax):
     assert np.linalg.norm(Sp - ref) <= 1e-10 * np.linalg.norm(ref)
 
 
-def test_vectors_and_packed_solves_vs_oracle(gpu, orc):
+@pytest.mark.parametrize("group", ["D2h", "D4h", "C4"])
+def test_vectors_and_packed_solves_vs_oracle(gpu, orc, group):
     lMax = 2
     pos = rect_array(4, 4, 400e-9, 400e-9)
-    ss = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax, sym="D2h")
+    ss = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax, sym=group)
     rng = np.random.default_rng(3)
     v = rng.normal(size=ss.fecv_size) + 1j * rng.normal(size=ss.fecv_size)
     back = sum(ss.unpack_vector(ss.pack_vector(v, i), i) for i in range(ss.nirreps))
@@ -108,7 +117,9 @@ def test_errors(gpu):
     with pytest.raises(QpmsGpuError):            # not symmetric
         gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, 2, sym="D2h")
     with pytest.raises(QpmsGpuError):            # unknown group
-        gpu.ScatteringSystem(rect_array(2, 2, 4e-7, 4e-7), 50e-9, EPS_I, EPS_E, 2, sym="D4h")
+        gpu.ScatteringSystem(rect_array(2, 2, 4e-7, 4e-7), 50e-9, EPS_I, EPS_E, 2, sym="D6h")
+    with pytest.raises(QpmsGpuError):            # a rectangle has no rotation by pi/2
+        gpu.ScatteringSystem(rect_array(2, 2, 4e-7, 3e-7), 50e-9, EPS_I, EPS_E, 2, sym="D4h")
     b1, b2, p1 = square_lattice()
     with pytest.raises(QpmsGpuError):            # lattices: full matrices only
         gpu.ScatteringSystem(p1, 80e-9, EPS_I, EPS_E, 2, lattice=(b1, b2), sym="D2h")
@@ -118,16 +129,17 @@ def test_errors(gpu):
         gpu.ScatteringSystem(pos, [50e-9, 60e-9], [EPS_I, EPS_I], EPS_E, 2, kinds=[0, 1], sym="C2v")
 
 
-def test_symmetric_large_scatter_vs_full(gpu, orc):
-    """720 unknowns (> 512) with D2h: each frequency is solved per irrep (8
-    systems of about 90 unknowns) and unpacked; the same as the system without
-    symmetry and as the oracle's full solve."""
-    lMax = 3
-    pos = rect_array(6, 4, 400e-9, 350e-9)
+@pytest.mark.parametrize("group,nx,ny,py,lMax,N", [("D2h", 6, 4, 350e-9, 3, 720), ("D4h", 6, 6, 400e-9, 2, 576)])
+def test_symmetric_large_scatter_vs_full(gpu, orc, group, nx, ny, py, lMax, N):
+    """Above 512 unknowns with D2h (8 systems of about N/8) or D4h (8 of
+    about N/16 and two two-dimensional irreps of about N/8): each frequency is
+    solved per irrep and unpacked; the same as the system without symmetry and
+    as the oracle's full solve."""
+    pos = rect_array(nx, ny, 400e-9, py)
     om = np.array([1.95, 2.35]) * EV / HBAR
-    sym = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax, sym="D2h")
+    sym = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax, sym=group)
     full = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax)
-    assert sym.fecv_size == 720
+    assert sym.fecv_size == N
     a = sym.planewave_scatter_batch(om, mode=1, want_f=True, want_scat=True)
     b = full.planewave_scatter_batch(om, mode=1, want_f=True, want_scat=True)
     calc = orc.TransCalculator(lMax)
@@ -140,12 +152,13 @@ def test_symmetric_large_scatter_vs_full(gpu, orc):
         assert abs(a["sigma_scat"][i] - b["sigma_scat"][i]) <= 1e-9 * abs(b["sigma_scat"][i])
 
 
-def test_beyn_per_irrep(gpu):
+@pytest.mark.parametrize("group", ["D2h", "D4h"])
+def test_beyn_per_irrep(gpu, group):
     """Eigenmodes of a symmetric 2 x 2 cluster searched irrep by irrep: every
     mode of the full search is found in one of the irreps (packed problems of
-    8 unknowns instead of 64)."""
+    8 unknowns or fewer instead of 64)."""
     pos = rect_array(2, 2, 400e-9, 400e-9)
-    ss = gpu.ScatteringSystem(pos, 60e-9, EPS_I, EPS_E, 2, sym="D2h")
+    ss = gpu.ScatteringSystem(pos, 60e-9, EPS_I, EPS_E, 2, sym=group)
     c, rr, ri = (2.52 - 0.3j) * EV / HBAR, 0.1 * EV / HBAR, 0.1 * EV / HBAR
     full0 = ss.find_modes(c, rr, ri, contour_points=64, rank_tol=1e300)
     full = ss.find_modes(c, rr, ri, contour_points=64, rank_tol=1e-10 * full0["ranktest_SV"][0])
