@@ -458,9 +458,10 @@ qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_ld(int np, const double *pos_xyz
 /* ---------------- point symmetry and irreps (scatsystem.h:300-430) ----------------
  * qpms_gpu_scatsys_set_symmetry gives a finite system one of the reference's
  * point groups generated by coordinate mirrors and rotations about z
- * ("trivial", "C2", "C2v", "D2h", "C4", "C4v", "D4h"; symmetries.py
- * point_group_info), with its irrep names, irrep matrices and order (names
- * sorted); the two-dimensional E irreps pack to d x multiplicity vectors.  The packed (symmetry-adapted) basis is this
+ * ("trivial", "trivial_g", "C2", "C2v", "D2h", "x_and_z_flip",
+ * "y_and_z_flip", "C4", "C4v", "D4h", "D3h"; symmetries.py point_group_info),
+ * with its irrep names, irrep matrices and order (names sorted); the
+ * two-dimensional E irreps pack to d x multiplicity vectors.  The packed (symmetry-adapted) basis is this
  * library's: packed vectors of the reference differ by a unitary change of
  * basis inside each irrep; eigenvalues, determinants and unpacked solutions
  * agree.  ss->saecv_sizes is set. */

@@ -2,20 +2,22 @@
 // mode problem (scatsystem.c:700-1000 projectors, bases and packing,
 // 1361-1471 packed builder, 2202-2273 packed LU / solve).
 //
-// Groups: the reference's point_group_info entries (symmetries.py:485-660)
-// generated by coordinate mirrors and rotations about z: trivial, C2, C2v,
-// D2h (x, y, z mirrors), C4 (rotation by pi/2), C4v (rotation by pi/2 and the
-// x mirror), D4h (those and the z mirror), with the reference's irrep names,
-// irrep matrices on the generators (E: ra = ((0,-1),(1,0)), -lam =
-// ((-1,0),(0,1)); E'' also -1 on the z mirror) and irrep order (the names
-// sorted, qpms_c.pyx:204).
+// Groups: the reference's point_group_info entries (symmetries.py:485-700)
+// generated by coordinate mirrors and rotations about z: trivial(_g), C2,
+// C2v, D2h (x, y, z mirrors), x_and_z_flip, y_and_z_flip, C4 (rotation by
+// pi/2), C4v (rotation by pi/2 and the x mirror), D4h (those and the z
+// mirror), D3h (rotation by 2pi/3, x and z mirrors), with the reference's
+// irrep names, irrep matrices on the generators (E of C4v / D4h: ra =
+// ((0,-1),(1,0)), -lam = ((-1,0),(0,1)); E of D3h: alif (rotation by 2pi/3),
+// lam = ((1,0),(0,-1)); E'' also -1 on the z mirror) and irrep order (the
+// names sorted, qpms_c.pyx:204).
 //
 // Action on VSWF coefficients (default normalisation, e^{i m phi},
 // Condon-Shortley phase), checked against the fields the oracle evaluates:
 //   z -> -z:       a_N(l,m) -> (-1)^(l+m) a_N(l,m),  a_M(l,m) -> -(-1)^(l+m) a_M(l,m)
 //   y -> -y:       a_N(l,m) -> (-1)^m a_N(l,-m),      a_M(l,m) -> -(-1)^m a_M(l,-m)
 //   x -> -x:       a_N(l,m) -> a_N(l,-m),             a_M(l,m) -> -a_M(l,-m)
-//   rotation by +pi/2 about z: a(l,m) -> (-i)^m a(l,m) (both types)
+//   rotation by alpha about z: a(l,m) -> e^{-i m alpha} a(l,m) (both types)
 // and the particle at r goes to the particle at g r.  The representation on
 // the full coefficient vector is monomial: each index goes to one index with
 // a phase.  The projector of irrep i, P_i = (d_i/|G|) sum_g chi_i(g) D(g)
@@ -95,7 +97,7 @@ std::vector<SymData *> &sym_table() {
 }
 
 // generators: 'X', 'Y', 'Z' mirrors (x -> -x etc.), 'R' rotation by +pi/2
-// about z, 'C' rotation by pi about z
+// about z, 'T' rotation by +2pi/3 about z, 'C' rotation by pi about z
 struct IrrepDef {
   const char *name;
   int dim;
@@ -110,9 +112,25 @@ struct GroupDef {
 std::vector<cdx> sc(double v) { return {cdx(v, 0)}; }
 
 const std::vector<GroupDef> &group_defs() {
-  static const std::vector<cdx> ra = {0, -1, 1, 0}, mlam = {-1, 0, 0, 1}, eps = {1, 0, 0, 1}, meps = {-1, 0, 0, -1};
+  static const double h3 = 0.86602540378443864676;  // sqrt(3) / 2
+  static const std::vector<cdx> ra = {0, -1, 1, 0}, mlam = {-1, 0, 0, 1}, eps = {1, 0, 0, 1}, meps = {-1, 0, 0, -1},
+                                lam = {1, 0, 0, -1}, alif = {-0.5, -h3, h3, -0.5};
   static const std::vector<GroupDef> defs = {
       {"trivial", "", {{"A", 1, {}}}},
+      {"trivial_g", "", {{"A", 1, {}}}},
+      {"x_and_z_flip", "XZ",
+       {{"P'", 1, {sc(1), sc(1)}}, {"R'", 1, {sc(-1), sc(1)}}, {"P''", 1, {sc(-1), sc(-1)}},
+        {"R''", 1, {sc(1), sc(-1)}}}},
+      {"y_and_z_flip", "YZ",
+       {{"P'", 1, {sc(1), sc(1)}}, {"R'", 1, {sc(-1), sc(1)}}, {"P''", 1, {sc(-1), sc(-1)}},
+        {"R''", 1, {sc(1), sc(-1)}}}},
+      {"D3h", "TXZ",
+       {{"E'", 2, {alif, lam, eps}},
+        {"E''", 2, {alif, lam, meps}},
+        {"A1'", 1, {sc(1), sc(1), sc(1)}},
+        {"A2'", 1, {sc(1), sc(-1), sc(1)}},
+        {"A1''", 1, {sc(1), sc(-1), sc(-1)}},
+        {"A2''", 1, {sc(1), sc(1), sc(-1)}}}},
       {"C2", "C", {{"A", 1, {sc(1)}}, {"B", 1, {sc(-1)}}}},
       {"C2v", "XY",
        {{"A1", 1, {sc(1), sc(1)}}, {"B2", 1, {sc(-1), sc(1)}}, {"A2", 1, {sc(-1), sc(-1)}},
@@ -149,14 +167,16 @@ const std::vector<GroupDef> &group_defs() {
   return defs;
 }
 
-// Position matrix (3 x 3 integers, row-major) of a generator.
-std::array<int, 9> gen_matrix(char g) {
+// Position matrix (3 x 3, row-major) of a generator.
+std::array<double, 9> gen_matrix(char g) {
+  const double h3 = 0.86602540378443864676;
   switch (g) {
     case 'X': return {-1, 0, 0, 0, 1, 0, 0, 0, 1};
     case 'Y': return {1, 0, 0, 0, -1, 0, 0, 0, 1};
     case 'Z': return {1, 0, 0, 0, 1, 0, 0, 0, -1};
     case 'C': return {-1, 0, 0, 0, -1, 0, 0, 0, 1};
-    default: return {0, -1, 0, 1, 0, 0, 0, 0, 1};  // 'R': (x, y) -> (-y, x)
+    case 'T': return {-0.5, -h3, 0, h3, -0.5, 0, 0, 0, 1};  // rotation by +2pi/3
+    default: return {0, -1, 0, 1, 0, 0, 0, 0, 1};            // 'R': (x, y) -> (-y, x)
   }
 }
 
@@ -181,6 +201,7 @@ void gen_wave(int lMax, char g, int j, int *jo, cdx *ph) {
       m = -m;
       break;
     case 'C': p = (double)((m & 1) ? -1 : 1); break;  // X then Y: (-1)^m
+    case 'T': p = std::polar(1.0, -m * 2.0943951023931954923); break;  // e^{-i m 2pi/3}
     default: {                                        // 'R': (-i)^m
       static const cdx mi[4] = {cdx(1, 0), cdx(0, -1), cdx(-1, 0), cdx(0, 1)};
       p = mi[((m % 4) + 4) % 4];
@@ -191,7 +212,7 @@ void gen_wave(int lMax, char g, int j, int *jo, cdx *ph) {
 }
 
 struct Element {
-  std::array<int, 9> M;
+  std::array<double, 9> M;
   std::vector<int> wimg;  // wave image
   std::vector<cdx> wph;   // phase
   std::vector<std::vector<cdx>> rep;  // irrep matrices
@@ -417,8 +438,8 @@ using namespace qg;
 extern "C" {
 
 // Gives a finite system the point symmetry `group` ("trivial", "C2", "C2v",
-// "D2h", "C4", "C4v", "D4h"; the reference's point_group_info entries of
-// these names).  Checks that every operation maps each particle onto a
+// "D2h", "x_and_z_flip", "y_and_z_flip", "C4", "C4v", "D4h", "D3h"; the
+// reference's point_group_info entries of these names).  Checks that every operation maps each particle onto a
 // particle of the same kind; the particles' T-matrices must be invariant
 // (Mie spheres are).
 int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group) {
@@ -431,7 +452,10 @@ int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group) {
   const GroupDef *gd = nullptr;
   for (const auto &g : group_defs())
     if (!strcmp(g.name, group)) gd = &g;
-  if (!gd) { set_error("unknown point group %s (trivial, C2, C2v, D2h, C4, C4v, D4h)", group); return QPMS_EINVAL; }
+  if (!gd) {
+    set_error("unknown point group %s (trivial, C2, C2v, D2h, x_and_z_flip, y_and_z_flip, C4, C4v, D4h, D3h)", group);
+    return QPMS_EINVAL;
+  }
   const int np = ss->p_count, n = (int)(ss->fecv_size / np), N = (int)ss->fecv_size;
   const int lMax = (int)lround(sqrt(n / 2.0 + 1) - 1);
   const int ng = (int)gd->gens.size(), nir = (int)gd->irreps.size();
@@ -453,16 +477,20 @@ int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group) {
     for (int j = 0; j < n; ++j) gen_wave(lMax, gd->gens[b], j, &gimg[b][j], &gph[b][j]);
   for (size_t q = 0; q < el.size() && el.size() <= 64; ++q)
     for (int b = 0; b < ng; ++b) {
-      const std::array<int, 9> G = gen_matrix(gd->gens[b]);
+      const std::array<double, 9> G = gen_matrix(gd->gens[b]);
       Element e;
       for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c) {
-          int v = 0;
+          double v = 0;
           for (int k = 0; k < 3; ++k) v += G[r * 3 + k] * el[q].M[k * 3 + c];
           e.M[r * 3 + c] = v;
         }
       bool seen = false;
-      for (const auto &x : el) seen = seen || x.M == e.M;
+      for (const auto &x : el) {
+        double d = 0;
+        for (int c = 0; c < 9; ++c) d = std::max(d, fabs(x.M[c] - e.M[c]));
+        seen = seen || d < 1e-9;
+      }
       if (seen) continue;
       e.wimg.resize(n);
       e.wph.resize(n);
@@ -493,7 +521,8 @@ int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group) {
     for (int p = 0; p < np; ++p) {
       const double r0[3] = {ss->p[p].pos.x, ss->p[p].pos.y, ss->p[p].pos.z};
       double x[3];
-      for (int r = 0; r < 3; ++r) x[r] = el[e].M[r * 3] * r0[0] + el[e].M[r * 3 + 1] * r0[1] + el[e].M[r * 3 + 2] * r0[2];
+      for (int r = 0; r < 3; ++r)
+        x[r] = el[e].M[r * 3] * r0[0] + el[e].M[r * 3 + 1] * r0[1] + el[e].M[r * 3 + 2] * r0[2];
       for (int q = 0; q < np; ++q)
         if (fabs(ss->p[q].pos.x - x[0]) <= tol && fabs(ss->p[q].pos.y - x[1]) <= tol &&
             fabs(ss->p[q].pos.z - x[2]) <= tol && ss->p[q].tmatrix_id == ss->p[p].tmatrix_id) {

@@ -214,7 +214,7 @@ class ScatteringSystem:
         if not self.s:
             raise _lib.QpmsGpuError("qpms_gpu_scatsys_create: " + _lib.last_error())
         self.sym = sym
-        if sym is not None:  # point group: "trivial", "C2", "C2v", "D2h", "C4", "C4v" or "D4h"
+        if sym is not None:  # a point_group_info name: "D2h", "D4h", "D3h", "C4v", ...
             _lib.check(self._L.qpms_gpu_scatsys_set_symmetry(self.s, str(sym).encode()),
                        "qpms_gpu_scatsys_set_symmetry")
         self.fecv_size = pos.shape[0] * 2 * self.lMax * (self.lMax + 2)

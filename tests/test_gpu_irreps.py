@@ -38,19 +38,31 @@ def rect_array(nx, ny, px, py):
 REF_NAMES = {"D2h": ["A1'", "A1''", "A2'", "A2''", "B1'", "B1''", "B2'", "B2''"],
              "C2v": ["A1", "A2", "B1", "B2"], "C2": ["A", "B"], "trivial": ["A"],
              "C4": ["1E", "2E", "A", "B"], "C4v": ["A1", "A2", "B1", "B2", "E"],
-             "D4h": ["A1'", "A1''", "A2'", "A2''", "B1'", "B1''", "B2'", "B2''", "E'", "E''"]}
+             "D4h": ["A1'", "A1''", "A2'", "A2''", "B1'", "B1''", "B2'", "B2''", "E'", "E''"],
+             "D3h": ["A1'", "A1''", "A2'", "A2''", "E'", "E''"], "trivial_g": ["A"],
+             "x_and_z_flip": ["P'", "P''", "R'", "R''"], "y_and_z_flip": ["P'", "P''", "R'", "R''"]}
+
+
+def hexagon_cluster(r):
+    """A centre particle and a hexagonal ring (D3h, D6h symmetric)."""
+    ang = np.arange(6) * np.pi / 3
+    ring = np.stack([r * np.cos(ang), r * np.sin(ang), np.zeros(6)], axis=1)
+    return np.vstack([np.zeros((1, 3)), ring])
 
 
 @pytest.mark.parametrize("group,nx,ny,lMax", [("D2h", 4, 3, 2), ("D2h", 3, 3, 3), ("C2v", 3, 2, 2),
                                               ("C2", 4, 4, 1), ("trivial", 2, 2, 2),
                                               ("D4h", 4, 4, 2), ("D4h", 3, 3, 3), ("C4v", 3, 3, 2),
-                                              ("C4", 4, 4, 2)])
+                                              ("C4", 4, 4, 2), ("D3h", 0, 0, 3), ("D3h", 0, 0, 2),
+                                              ("x_and_z_flip", 3, 2, 2), ("y_and_z_flip", 2, 3, 2),
+                                              ("trivial_g", 2, 1, 2)])
 def test_bases_and_block_diagonal_oracle_matrix(gpu, orc, group, nx, ny, lMax):
     """Square groups (C4, C4v, D4h: rotations by pi/2, two-dimensional E
     irreps with d x multiplicity packed vectors, complex bases) on square
-    arrays; the mirror groups on rectangular ones."""
+    arrays, D3h (rotation by 2 pi/3) on a hexagonal cluster; the mirror groups
+    on rectangular ones."""
     py = 400e-9 if group in ("C4", "C4v", "D4h") else 330e-9
-    pos = rect_array(nx, ny, 400e-9, py)
+    pos = hexagon_cluster(420e-9) if group == "D3h" else rect_array(nx, ny, 400e-9, py)
     ss = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax, sym=group)
     assert ss.irrep_names == REF_NAMES[group]
     assert sum(ss.saecv_sizes) == ss.fecv_size
@@ -82,10 +94,10 @@ def test_bases_and_block_diagonal_oracle_matrix(gpu, orc, group, nx, ny, lMax):
     assert np.linalg.norm(Sp - ref) <= 1e-10 * np.linalg.norm(ref)
 
 
-@pytest.mark.parametrize("group", ["D2h", "D4h", "C4"])
+@pytest.mark.parametrize("group", ["D2h", "D4h", "C4", "D3h"])
 def test_vectors_and_packed_solves_vs_oracle(gpu, orc, group):
     lMax = 2
-    pos = rect_array(4, 4, 400e-9, 400e-9)
+    pos = hexagon_cluster(420e-9) if group == "D3h" else rect_array(4, 4, 400e-9, 400e-9)
     ss = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, lMax, sym=group)
     rng = np.random.default_rng(3)
     v = rng.normal(size=ss.fecv_size) + 1j * rng.normal(size=ss.fecv_size)
