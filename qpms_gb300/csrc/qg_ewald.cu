@@ -497,59 +497,65 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
         const double Rx = i * c_ew.b[0] + j * c_ew.b[2] - sx, Ry = i * c_ew.b[1] + j * c_ew.b[3] - sy;
         const double r2 = Rx * Rx + Ry * Ry, r = sqrt(r2);
         if (r * eta > 7.5) continue;
-        const double phi = atan2(Ry, Rx);
-        // e^{i beta.R} e^{i m phi} handled below
-        const qg_c zp = cmk(r * eta + ik2eta.re, ik2eta.im), zm = cmk(r * eta - ik2eta.re, -ik2eta.im);
-        const qg_c ekr = cexpi(cscale(k, r)), emkr = cexpi(cscale(k, -r));
-        const qg_c Ep = cmul(ekr, cerfc(zp, c_wd)), Em = cmul(emkr, cerfc(zm, c_wd));
+        // e^{i beta.(R - s)} folded into E+-, E: the I_n recurrence is linear, so
+        // it yields I_n e^{i beta.(R - s)} directly
+        double sb, cb;
+        sincos(bx * Rx + by * Ry, &sb, &cb);
+        const qg_c ebeta = cmk(cb, sb);
+        const qg_c zp = cmk(r * eta + ik2eta.re, ik2eta.im);
+        const qg_c ekr = cexpi(cscale(k, r)), erp = cerfc(zp, c_wd);
+        qg_c emkr, erm;
+        if (kreal) {  // z- = conj(z+), e^{-ikr} = conj(e^{ikr}) for real k
+          emkr = cconj(ekr);
+          erm = cconj(erp);
+        } else {
+          emkr = cexpi(cscale(k, -r));
+          erm = cerfc(cmk(r * eta - ik2eta.re, -ik2eta.im), c_wd);
+        }
+        const qg_c Ep = cmul(cmul(ekr, erp), ebeta), Em = cmul(cmul(emkr, erm), ebeta);
         const double sqpi = 1.7724538509055160273;
-        qg_c In[LE + 1];
         const qg_c I0 = cscale(cadd(Ep, Em), sqpi / (4 * r));
         // I_{-1} = sqrt(pi)/(2 i k) (Em - Ep)
         const qg_c d = csub(Em, Ep);
         const qg_c Im1 = cscale(cmul(cmk(d.im, -d.re), rk), sqpi / 2);  // (Em-Ep)/(i) = -i (Em-Ep)
-        // E = exp(-r^2 eta^2 + k^2 / (4 eta^2))
+        // E = exp(-r^2 eta^2 + k^2 / (4 eta^2)) e^{i beta.(R - s)}
         const qg_c ex = cmk(-r2 * eta * eta + (k.re * k.re - k.im * k.im) / (4 * eta * eta),
                             2 * k.re * k.im / (4 * eta * eta));
-        const qg_c E = cexpi(cmk(ex.im, -ex.re));
-        In[0] = I0;
+        const qg_c E = cmul(cexpi(cmk(ex.im, -ex.re)), ebeta);
         qg_c pm2 = Im1, pm1 = I0;
         double etap = eta;  // eta^(2n-1)
         const double inv2r2 = 1.0 / (2 * r2);
-#pragma unroll
-        for (int n = 1; n <= LE; ++n) {
-          const qg_c v = cscale(cadd(csub(cscale(pm1, 2 * n - 1), cmul(k2h, pm2)), cscale(E, etap)), inv2r2);
-          In[n] = v;
-          pm2 = pm1;
-          pm1 = v;
-          etap *= eta * eta;
-        }
-        double sb, cb;
-        sincos(bx * Rx + by * Ry, &sb, &cb);
-        const qg_c ebeta = cmk(cb, sb);
-        double s1, c1;
-        sincos(phi, &s1, &c1);
-        const qg_c e1 = cmk(c1, s1);
-        // prefac_n r^n I_n e^{i beta R}: prefac_n = -i (2/k)^{n+1} / sqrt(pi)
-        qg_c pf = cscale(cmul(cmk(0.0, -1.0), cscale(rk, 2.0)), 1.0 / sqpi);  // -i (2/k) / sqrt(pi)
-        const qg_c twok = cscale(rk, 2.0);
-        double rn = 1.0;
+        const qg_c e1 = cmk(Rx / r, Ry / r), e2 = cmul(e1, e1), e1c = cconj(e1);  // e^{i phi}
+        // c_n = prefac_n r^n = -i (2/k)^{n+1} r^n / sqrt(pi)
+        qg_c cn = cscale(cmk(rk.im, -rk.re), 2.0 / sqpi);  // -i (2/k) / sqrt(pi)
+        const qg_c twor_k = cscale(rk, 2.0 * r);
+        qg_c emn = cmk(1, 0);  // e^{-i n phi}
 #pragma unroll
         for (int n = 0; n <= LE; ++n) {
-          const qg_c base = cmul(cmul(cscale(pf, rn), In[n]), ebeta);
-          // m = -n, -n+2, ..., n: e^{i m phi}
-          qg_c em = cmk(1, 0);
-          for (int q = 0; q < n; ++q) em = cmul(em, cconj(e1));  // e^{-i n phi}
-          const qg_c e2 = cmul(e1, e1);
+          qg_c In;
+          if (n == 0) {
+            In = I0;
+          } else {
+            In = cscale(cadd(csub(cscale(pm1, 2 * n - 1), cmul(k2h, pm2)), cscale(E, etap)), inv2r2);
+            pm2 = pm1;
+            pm1 = In;
+            etap *= eta * eta;
+          }
+          const qg_c base = cmul(cn, In);
+          // m = -n, -n+2, ..., n: acc += leg0m (base e^{i m phi})
+          qg_c em = emn;
 #pragma unroll
           for (int q = 0; q <= n; ++q) {
             const int m = -n + 2 * q;
             const int kk = n * (n + 1) / 2 + q;
-            acc[kk] = cadd(acc[kk], cscale(cmul(base, em), c_ew.leg0m[n * (n + 1) + m]));
+            const qg_c pr = cmul(base, em);
+            const double lg = c_ew.leg0m[n * (n + 1) + m];
+            acc[kk].re = fma(lg, pr.re, acc[kk].re);
+            acc[kk].im = fma(lg, pr.im, acc[kk].im);
             em = cmul(em, e2);
           }
-          pf = cmul(pf, twok);
-          rn *= r;
+          emn = cmul(emn, e1c);
+          cn = cmul(cn, twor_k);
         }
       }
     }
@@ -607,10 +613,8 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
         double sK, cK;
         sincos(Kx * sx + Ky * sy, &sK, &cK);
         const qg_c phasefac = cmul(cmk(cK, sK), lrfac);  // e^{i K.s} / (k^2 A)
-        const double alpha = atan2(qy, qx);
-        double s1, c1;
-        sincos(alpha, &s1, &c1);
-        const qg_c e1 = cmk(c1, s1), e2 = cmul(e1, e1);
+        // e^{i alpha}, alpha = arg(beta + K) (0 at the origin, as atan2(0, 0))
+        const qg_c e1 = rb > 0 ? cmk(qx / rb, qy / rb) : cmk(1.0, 0.0), e2 = cmul(e1, e1), e1c = cconj(e1);
         // powers: (rb/k)^(n - 2j) and gamma^(2j - 1)
         const qg_c tk = cscale(rk, rb);
         qg_c gp[LE / 2 + 1];  // gamma^(2j-1) G_j
@@ -625,22 +629,40 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
         qg_c tpow[LE + 1];
         tpow[0] = cmk(1, 0);
         for (int p = 1; p <= LE; ++p) tpow[p] = cmul(tpow[p - 1], tk);
+        // s1[y][j] = i^(n+1) s1r[y][j]: js = i^(n+1) sum_j s1r P_nj, P_nj = tpow[n-2j] gp[j]
+        qg_c emn = phasefac;  // e^{-i n alpha} e^{i K.s} / (k^2 A)
 #pragma unroll
         for (int n = 0; n <= LE; ++n) {
-          qg_c em = cmk(1, 0);
-          for (int q = 0; q < n; ++q) em = cmul(em, cconj(e1));
+          qg_c P[LE / 2 + 1];
+#pragma unroll
+          for (int j = 0; j <= n / 2; ++j) P[j] = cmul(tpow[n - 2 * j], gp[j]);
+          qg_c em = emn;
 #pragma unroll
           for (int q = 0; q <= n; ++q) {
             const int m = -n + 2 * q;
             const int y = n * (n + 1) + m;
             const int jmax = (n - (m < 0 ? -m : m)) / 2;
-            qg_c js = cmk(0, 0);
-            for (int j = 0; j <= jmax; ++j)
-              js = cadd(js, cmul(cmul(tpow[n - 2 * j], gp[j]), c_ew.s1[c_ew.s1off[y] + j]));
+            double jr = 0, ji = 0;
+#pragma unroll
+            for (int j = 0; j <= jmax; ++j) {
+              const double c = c_ew.s1r[c_ew.s1off[y] + j];
+              jr = fma(c, P[j].re, jr);
+              ji = fma(c, P[j].im, ji);
+            }
+            qg_c js;  // times i^(n+1)
+            switch ((n + 1) & 3) {
+              case 0: js = cmk(jr, ji); break;
+              case 1: js = cmk(-ji, jr); break;
+              case 2: js = cmk(-jr, -ji); break;
+              default: js = cmk(ji, -jr); break;
+            }
             const int kk = n * (n + 1) / 2 + q;
-            acc[kk] = cadd(acc[kk], cmul(cmul(js, em), phasefac));
+            const qg_c pr = cmul(js, em);
+            acc[kk].re += pr.re;
+            acc[kk].im += pr.im;
             em = cmul(em, e2);
           }
+          emn = cmul(emn, e1c);
         }
       }
     }

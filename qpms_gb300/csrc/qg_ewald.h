@@ -21,9 +21,11 @@ struct EwaldConst {
   double area;    // unit cell area
   // P_n^{|m|}(0) (-1)^{m<0 ? m : 0} per y = n(n+1) + m (ewald.c:425, 877, 886)
   double leg0m[kEwS];
-  // long-range constants s1_constfacs[y][j] (ewald.c:142-146) times leg0m[y]
+  // long-range constants s1_constfacs[y][j] (ewald.c:142-146) times leg0m[y],
+  // and the same as s1 = i^(n+1) s1r with s1r real
   int s1off[kEwS];
   qg_c s1[kEwS * (kEwLE / 2 + 1)];
+  double s1r[kEwS * (kEwLE / 2 + 1)];
   // Pairs of layers at different heights (shift.z != 0):
   // sign factors of leg_nm(x) = legs[y] P_n^|m|(x) with the Condon-Shortley
   // phase in P (m1pow_m_neg(m), and (-1)^m for csphase +1)

@@ -88,6 +88,7 @@ int build_ewald_const(const qpms_scatsys_t *ss, int lMax, EwaldConst *c, int csp
           const double f = -2 * 1.7724538509055160273 * fact((n - m) / 2) * fact((n + m) / 2) * ((j % 2) ? -1 : 1) /
                            (fact(j) * fact((n - m) / 2 - j) * fact((n + m) / 2 - j)) * c->leg0m[y];
           c->s1[off + j] = cmk(f * ip[0], f * ip[1]);
+          c->s1r[off + j] = f;
         }
         off += (n - am) / 2 + 1;
       }
