@@ -480,7 +480,22 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
     for (int i = 0; i < NEV; ++i) acc[i] = cmk(0, 0);
 
     // ---------------- short range (direct lattice) ----------------
-    {
+    if (a.srtab) {  // the tabulated terms of (frequency, pair) with the Bloch phase
+      const size_t ti = (size_t)iw * per + pr;
+      const int cnt = a.srcnt[ti];
+      const qg_c *tab = a.srtab + ti * NEV * (size_t)a.srmax;
+      const double *pts = a.srpts + ti * 2 * (size_t)a.srmax;
+      for (int p = tid; p < cnt; p += kEThreads) {
+        double sb, cb;
+        sincos(bx * pts[2 * p] + by * pts[2 * p + 1], &sb, &cb);
+#pragma unroll
+        for (int kk = 0; kk < NEV; ++kk) {
+          const qg_c c = tab[(size_t)kk * a.srmax + p];
+          acc[kk].re = fma(cb, c.re, fma(-sb, c.im, acc[kk].re));
+          acc[kk].im = fma(cb, c.im, fma(sb, c.re, acc[kk].im));
+        }
+      }
+    } else {
       const double rc = 7.5 / eta;  // |R - shift| eta <= 7.5
       const double smax = sqrt(sx * sx + sy * sy);
       const int I1 = (int)ceil((rc + smax) * c_ew.rbn[0] / (2 * M_PI)) + 1;
@@ -608,13 +623,70 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
           uu = csqrt_(x2);
           if (x2.re < 0 && !signbit(x2.im)) uu = cscale(uu, -1.0);  // branch m = -1 (ewald.c:390-393)
         }
-        qg_c G[LE / 2 + 1];
-        gamma_half_down(uu, LE / 2, G);
         double sK, cK;
         sincos(Kx * sx + Ky * sy, &sK, &cK);
         const qg_c phasefac = cmul(cmk(cK, sK), lrfac);  // e^{i K.s} / (k^2 A)
         // e^{i alpha}, alpha = arg(beta + K) (0 at the origin, as atan2(0, 0))
         const qg_c e1 = rb > 0 ? cmk(qx / rb, qy / rb) : cmk(1.0, 0.0), e2 = cmul(e1, e1), e1c = cconj(e1);
+        if (kreal && gam.im == 0.0) {
+          // evanescent order at real k: gamma, x = gamma k / 2 eta, Gamma(1/2 - j, x^2),
+          // rb / k are real, so is every P_nj; only e^{i m alpha} and the phase are complex
+          const double x = uu.re, X = x * x, emX = exp(-X);
+          double Gr[LE / 2 + 1];
+          Gr[0] = 1.7724538509055160273 * erfc(x);  // Gamma(1/2, x^2)
+          double zp = 1.0 / x;                      // x^(1-2j)
+          const double rX = 1.0 / X;
+#pragma unroll
+          for (int j = 1; j <= LE / 2; ++j) {
+            Gr[j] = (Gr[j - 1] - zp * emX) / (0.5 - j);
+            zp *= rX;
+          }
+          double gpr[LE / 2 + 1];
+          {
+            double g = 1.0 / gam.re;
+            const double gsq = gam.re * gam.re;
+#pragma unroll
+            for (int j = 0; j <= LE / 2; ++j) {
+              gpr[j] = g * Gr[j];
+              g *= gsq;
+            }
+          }
+          double tp[LE + 1];
+          tp[0] = 1.0;
+          const double tkr = rb / k.re;
+#pragma unroll
+          for (int p = 1; p <= LE; ++p) tp[p] = tp[p - 1] * tkr;
+          qg_c emn = phasefac;
+#pragma unroll
+          for (int n = 0; n <= LE; ++n) {
+            double P[LE / 2 + 1];
+#pragma unroll
+            for (int j = 0; j <= n / 2; ++j) P[j] = tp[n - 2 * j] * gpr[j];
+            qg_c em = emn;
+#pragma unroll
+            for (int q = 0; q <= n; ++q) {
+              const int m = -n + 2 * q;
+              const int y = n * (n + 1) + m;
+              const int jmax = (n - (m < 0 ? -m : m)) / 2;
+              double jr = 0;
+#pragma unroll
+              for (int j = 0; j <= jmax; ++j) jr = fma(c_ew.s1r[c_ew.s1off[y] + j], P[j], jr);
+              // acc += i^(n+1) jr em
+              const int kk = n * (n + 1) / 2 + q;
+              switch ((n + 1) & 3) {
+                case 0: acc[kk].re = fma(jr, em.re, acc[kk].re); acc[kk].im = fma(jr, em.im, acc[kk].im); break;
+                case 1: acc[kk].re = fma(-jr, em.im, acc[kk].re); acc[kk].im = fma(jr, em.re, acc[kk].im); break;
+                case 2: acc[kk].re = fma(-jr, em.re, acc[kk].re); acc[kk].im = fma(-jr, em.im, acc[kk].im); break;
+                default: acc[kk].re = fma(jr, em.im, acc[kk].re); acc[kk].im = fma(-jr, em.re, acc[kk].im); break;
+              }
+              em = cmul(em, e2);
+            }
+            emn = cmul(emn, e1c);
+          }
+          continue;
+        }
+        qg_c G[LE / 2 + 1];
+        gamma_half_down(uu, LE / 2, G);
         // powers: (rb/k)^(n - 2j) and gamma^(2j - 1)
         const qg_c tk = cscale(rk, rb);
         qg_c gp[LE / 2 + 1];  // gamma^(2j-1) G_j
@@ -709,6 +781,132 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
   }
 }
 
+// Short-range tables: one CTA per (frequency w, pair) at the common eta of w.
+// Lattice points are taken in grid order, compacted with a block prefix sum
+// (deterministic order); every valid point stores R - s and its terms
+// c_nm = prefac_n |R - s|^n I_n leg0m e^{i m phi} (n + m even).
+template <int LMAX>
+__global__ void __launch_bounds__(kEThreads) ewald_sr_table_kernel(EwaldArgs a) {
+  using Sh = EwShape<LMAX>;
+  constexpr int LE = Sh::LE, NEV = Sh::NEVEN;
+  __shared__ int wsum[kEThreads / 32];
+  __shared__ int base_s;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int np = a.np;
+  const size_t per = (size_t)np * np;
+  const size_t units = (size_t)a.nw * per;
+  for (size_t u = blockIdx.x; u < units; u += gridDim.x) {
+    const int pr = (int)(u % per), iw = (int)(u / per);
+    const int R = pr / np, C = pr - R * np;
+    const double sx = a.pos[3 * R] - a.pos[3 * C], sy = a.pos[3 * R + 1] - a.pos[3 * C + 1];
+    const double sz = a.pos[3 * R + 2] - a.pos[3 * C + 2];
+    const qg_c k = a.k[iw];
+    const double eta = a.eta[(size_t)iw * a.nk];
+    const bool self = (sx == 0.0 && sy == 0.0), kreal = (k.im == 0.0);
+    qg_c *tab = a.srtab + u * NEV * (size_t)a.srmax;
+    double *pts = a.srpts + u * 2 * (size_t)a.srmax;
+    if (tid == 0) base_s = 0;
+    __syncthreads();
+    if (sz == 0.0) {
+      const double rc = 7.5 / eta;
+      const double smax = sqrt(sx * sx + sy * sy);
+      const int I1 = (int)ceil((rc + smax) * c_ew.rbn[0] / (2 * M_PI)) + 1;
+      const int I2 = (int)ceil((rc + smax) * c_ew.rbn[1] / (2 * M_PI)) + 1;
+      const int W1 = 2 * I1 + 1, W2 = 2 * I2 + 1;
+      const bool sr_ok = (long)W1 * W2 <= kEwMaxPoints && I1 >= 0 && I2 >= 0;
+      if (!sr_ok && tid == 0) atomicOr(a.err, 1);
+      const qg_c k2h = cscale(cmul(k, k), 0.5);
+      const qg_c ik2eta = cmk(-k.im / (2 * eta), k.re / (2 * eta));
+      const qg_c rk = crecip(k);
+      const int tot = sr_ok ? W1 * W2 : 0;
+      for (int t0 = 0; t0 < tot; t0 += kEThreads) {
+        const int t = t0 + tid;
+        double Rx = 0, Ry = 0, r2 = 0, r = 0;
+        bool valid = false;
+        if (t < tot) {
+          const int i = t / W2 - I1, j = t % W2 - I2;
+          Rx = i * c_ew.b[0] + j * c_ew.b[2] - sx;
+          Ry = i * c_ew.b[1] + j * c_ew.b[3] - sy;
+          r2 = Rx * Rx + Ry * Ry;
+          r = sqrt(r2);
+          valid = !(self && i == 0 && j == 0) && r * eta <= 7.5;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, valid);
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        int off = base_s;
+        for (int w = 0; w < warp; ++w) off += wsum[w];
+        const int pos = off + __popc(bal & ((1u << lane) - 1u));
+        __syncthreads();
+        if (tid == 0) {
+          int s2 = base_s;
+          for (int w = 0; w < kEThreads / 32; ++w) s2 += wsum[w];
+          base_s = s2;
+        }
+        if (valid && pos < a.srmax) {
+          pts[2 * pos] = Rx;
+          pts[2 * pos + 1] = Ry;
+          const qg_c zp = cmk(r * eta + ik2eta.re, ik2eta.im);
+          const qg_c ekr = cexpi(cscale(k, r)), erp = cerfc(zp, c_wd);
+          qg_c emkr, erm;
+          if (kreal) {
+            emkr = cconj(ekr);
+            erm = cconj(erp);
+          } else {
+            emkr = cexpi(cscale(k, -r));
+            erm = cerfc(cmk(r * eta - ik2eta.re, -ik2eta.im), c_wd);
+          }
+          const qg_c Ep = cmul(ekr, erp), Em = cmul(emkr, erm);
+          const double sqpi = 1.7724538509055160273;
+          const qg_c I0 = cscale(cadd(Ep, Em), sqpi / (4 * r));
+          const qg_c d = csub(Em, Ep);
+          const qg_c Im1 = cscale(cmul(cmk(d.im, -d.re), rk), sqpi / 2);
+          const qg_c ex = cmk(-r2 * eta * eta + (k.re * k.re - k.im * k.im) / (4 * eta * eta),
+                              2 * k.re * k.im / (4 * eta * eta));
+          const qg_c E = cexpi(cmk(ex.im, -ex.re));
+          qg_c pm2 = Im1, pm1 = I0;
+          double etap = eta;
+          const double inv2r2 = 1.0 / (2 * r2);
+          const qg_c e1 = cmk(Rx / r, Ry / r), e2 = cmul(e1, e1), e1c = cconj(e1);
+          qg_c cn = cscale(cmk(rk.im, -rk.re), 2.0 / sqpi);
+          const qg_c twor_k = cscale(rk, 2.0 * r);
+          qg_c emn = cmk(1, 0);
+#pragma unroll
+          for (int n = 0; n <= LE; ++n) {
+            qg_c In;
+            if (n == 0) {
+              In = I0;
+            } else {
+              In = cscale(cadd(csub(cscale(pm1, 2 * n - 1), cmul(k2h, pm2)), cscale(E, etap)), inv2r2);
+              pm2 = pm1;
+              pm1 = In;
+              etap *= eta * eta;
+            }
+            const qg_c base = cmul(cn, In);
+            qg_c em = emn;
+#pragma unroll
+            for (int q = 0; q <= n; ++q) {
+              const int m = -n + 2 * q;
+              const int kk = n * (n + 1) / 2 + q;
+              tab[(size_t)kk * a.srmax + pos] = cscale(cmul(base, em), c_ew.leg0m[n * (n + 1) + m]);
+              em = cmul(em, e2);
+            }
+            emn = cmul(emn, e1c);
+            cn = cmul(cn, twor_k);
+          }
+        }
+        __syncthreads();
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      if (base_s > a.srmax) atomicOr(a.err, 1);
+      a.srcnt[u] = base_s < a.srmax ? base_s : a.srmax;
+    }
+    __syncthreads();
+  }
+}
+
 template <int LMAX>
 __global__ void __launch_bounds__(kEThreads) ewald_layers_kernel(EwaldArgs a, TransDevTables T) {
   using Sh = EwShape<LMAX>;
@@ -796,6 +994,12 @@ int launch_ew(const EwaldArgs &a, const TransDevTables &T, cudaStream_t st) {
   QG_CUDA_TRY(cudaGetDevice(&dev));
   QG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   size_t grid = std::min<size_t>(units, (size_t)nsm * 16);
+  if (a.srtab) {
+    const size_t tunits = (size_t)a.nw * a.np * a.np;
+    ewald_sr_table_kernel<LMAX><<<(unsigned)std::min<size_t>(tunits, (size_t)nsm * 16), kEThreads, 0, st>>>(a);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+  }
   ewald_assemble_kernel<LMAX><<<(unsigned)grid, kEThreads, 0, st>>>(a, T);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(1);

@@ -57,6 +57,16 @@ struct EwaldArgs {
   // formed by a second kernel.  A pair with z_R != z_C and layered == 0 sets
   // bit 2 of *err.
   int layered = 0;
+  // Short-range tables (dispersion scans, not with `paired`): when srtab is
+  // set, eta[w * nk + k] must be one value per frequency w, and the
+  // single-plane kernel takes the short-range terms c_nm(R) of (w, pair) from
+  // the tables (formed once per (w, pair) by the table kernel) and applies
+  // only the Bloch phase e^{i beta.(R - s)}: the radial integrals do not
+  // depend on beta.
+  qg_c *srtab = nullptr;   // [nw][pairs][NEVEN][srmax]
+  double *srpts = nullptr; // [nw][pairs][srmax][2]: R - s in the plane
+  int *srcnt = nullptr;    // [nw][pairs]
+  int srmax = 0;
 };
 
 // Bound on the lattice points one unit may enumerate per sum.

@@ -293,9 +293,22 @@ int ewald_assemble_dense(const qpms_scatsys_t *ss, const EwaldArgs &a, int n, cu
 }
 
 // Batched periodic assembly into device memory: nw frequencies x nk Bloch vectors.
+int periodic_assemble_device_ex(const qpms_scatsys_t *ss, int nw, const qg_c *k_host,
+                                const std::vector<qg_c> &T_host, int nk, const double *beta_host,
+                                const double *eta_host, qg_c *dM, cudaStream_t st, bool sr_tables);
+
 int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_host,
                                     const std::vector<qg_c> &T_host, int nk, const double *beta_host,
                                     const double *eta_host, qg_c *dM, cudaStream_t st) {
+  return periodic_assemble_device_ex(ss, nw, k_host, T_host, nk, beta_host, eta_host, dM, st, false);
+}
+
+// sr_tables: eta_host is one value per frequency (eta_host[w * nk + k] the
+// same for every k); the short-range terms are then formed once per
+// (frequency, particle pair) and shared by the nk Bloch vectors.
+int periodic_assemble_device_ex(const qpms_scatsys_t *ss, int nw, const qg_c *k_host,
+                                const std::vector<qg_c> &T_host, int nk, const double *beta_host,
+                                const double *eta_host, qg_c *dM, cudaStream_t st, bool sr_tables) {
   const int np = ss->p_count;
   int e;
   std::vector<double> pos(3 * np);
@@ -337,6 +350,37 @@ int periodic_assemble_device(const qpms_scatsys_t *ss, int nw, const qg_c *k_hos
   a.M = dM;
   a.err = derr.as<int>();
   a.layered = layered_positions(pos.data(), np);
+  Dev dtab, dpts, dcnt;
+  if (sr_tables) {
+    for (int w = 0; w < nw; ++w)
+      for (int k = 1; k < nk; ++k)
+        if (eta_host[(size_t)w * nk + k] != eta_host[(size_t)w * nk]) {
+          set_error("internal: short-range tables need one eta per frequency");
+          return QPMS_ERROR;
+        }
+    // table size: the lattice-index box of the short-range sum at the
+    // smallest eta (same bound as the kernels: |R - s| eta <= 7.5)
+    double emin = eta_host[0];
+    for (int w = 0; w < nw; ++w) emin = std::min(emin, eta_host[(size_t)w * nk]);
+    const double rbn0 = hypot(ss->per.reciprocal_basis[0].x, ss->per.reciprocal_basis[0].y);
+    const double rbn1 = hypot(ss->per.reciprocal_basis[1].x, ss->per.reciprocal_basis[1].y);
+    long srmax = 1;
+    for (int R = 0; R < np; ++R)
+      for (int C = 0; C < np; ++C) {
+        const double smax = hypot(pos[3 * R] - pos[3 * C], pos[3 * R + 1] - pos[3 * C + 1]);
+        const long I1 = (long)ceil((7.5 / emin + smax) * rbn0) + 1, I2 = (long)ceil((7.5 / emin + smax) * rbn1) + 1;
+        srmax = std::max(srmax, (2 * I1 + 1) * (2 * I2 + 1));
+      }
+    const int lMax = scatsys_lmax(ss), LE = 2 * lMax + 1, nev = (LE + 1) * (LE + 2) / 2;
+    const size_t units = (size_t)nw * np * np;
+    if ((e = dalloc(dtab, units * nev * srmax * 16)) || (e = dalloc(dpts, units * srmax * 16)) ||
+        (e = dalloc(dcnt, units * 4)))
+      return e;
+    a.srtab = dtab.as<qg_c>();
+    a.srpts = dpts.as<double>();
+    a.srcnt = dcnt.as<int>();
+    a.srmax = (int)srmax;
+  }
   const int n = (int)(ss->fecv_size / np);
   if (T_host.size() == (size_t)nw * ss->tm_count * n * n && n > 1) return ewald_assemble_dense(ss, a, n, st);
   return ewald_assemble_locked(ss, a, st);
@@ -600,10 +644,18 @@ int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *om
       }
       k[w] = scatsys_wavenumber(ss, omegas[w0 + w], 0.0);
       const double kap = k[w].re;
+      // one eta per frequency, the largest adjusted eta of its Bloch vectors
+      // (the sums do not depend on eta; a larger one only moves work to the
+      // long-range sum), so the short-range terms are shared by all of them
+      double eta_w = 0;
+      for (size_t ik = 0; ik < nk; ++ik) {
+        const double kv[3] = {kvecs[2 * ik], kvecs[2 * ik + 1], 0.0};
+        eta_w = std::max(eta_w, qpms_ss_adjusted_eta(ss, *(const qpms_complex_t *)&k[w], kv));
+      }
       for (size_t ik = 0; ik < nk; ++ik) {
         const size_t m = (size_t)w * nk + ik;
         const double kv[3] = {kvecs[2 * ik], kvecs[2 * ik + 1], 0.0};
-        eta[m] = qpms_ss_adjusted_eta(ss, *(const qpms_complex_t *)&k[w], kv);
+        eta[m] = eta_w;
         kk[m] = k[w];
         // incident plane wave with in-plane wavevector beta, E along x projected
         // perpendicular to k (x-polarised at normal incidence)
@@ -627,7 +679,8 @@ int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *om
                                                 T.begin() + ((size_t)w * ntm + t + 1) * tsz);
       }
     }
-    if ((e = periodic_assemble_device(ss, W, k.data(), T, (int)nk, kvecs, eta.data(), dM.as<qg_c>(), 0))) return e;
+    if ((e = periodic_assemble_device_ex(ss, W, k.data(), T, (int)nk, kvecs, eta.data(), dM.as<qg_c>(), 0, true)))
+      return e;
     // per-matrix incidence (coefficients and phases differ per (w, k)), b = T a
     QG_CUDA_TRY(cudaMemcpy(dcf.p, coefs.data(), coefs.size() * 16, cudaMemcpyHostToDevice));
     QG_CUDA_TRY(cudaMemcpy(dkv.p, kvec.data(), nm * 24, cudaMemcpyHostToDevice));
