@@ -405,6 +405,47 @@ __device__ __forceinline__ void shifted_passes(const ZUnit &u, const qg_c *s1u, 
   if constexpr (Y0 + NY < S) shifted_passes<LMAX, Y0 + NY>(u, s1u, rr, sig, red, errflag);
 }
 
+constexpr int kELChunks = 8;  // reciprocal-point chunks classified per batch
+
+// Class of a reciprocal point |beta + K| = rb: 0 past the cutoff (x^2 > 56),
+// 1 evanescent at real k (gamma and x real), 2 otherwise; gamma and the branch
+// of x = gamma k / 2 eta (clilgamma, ewald.h:157-170, and ewald.c:390-393).
+__device__ __forceinline__ int lr_class(qg_c k, bool kreal, double eta, double rb, qg_c &gam, qg_c &uu) {
+  if (kreal) {
+    // clilgamma(rb / k) for real k: sqrt(t - 1) sqrt(t + 1) with t - 1 exact;
+    // near a Rayleigh anomaly (t -> 1) the 1/gamma terms dominate, so gamma is
+    // formed from the exact differences as there
+    const double tt = rb / k.re;
+    if (tt >= 1.0) {
+      gam = cmk(sqrt(tt - 1.0) * sqrt(tt + 1.0), 0.0);
+      const double x = gam.re * k.re / (2 * eta);
+      if (x * x > 56.0) return 0;
+      uu = cmk(x, 0.0);
+      return 1;
+    }
+    const double g = sqrt(1.0 - tt) * sqrt(1.0 + tt);
+    gam = cmk(0.0, -g);  // -i sqrt(1 - t^2)
+    // x^2 = -(g k / 2 eta)^2, approached from below the negative axis: sqrt -> -i c
+    uu = cmk(0.0, -g * k.re / (2 * eta));
+    return 2;
+  }
+  // z = rb / k as C's real / complex division forms it: (rb + 0i)(conj k) / |k|^2.
+  // The sign of a zero imaginary part (rb = 0, i.e. beta on a reciprocal
+  // lattice point) picks the branch of a1 below, so it must be +0 as there.
+  const double kk2 = k.re * k.re + k.im * k.im;
+  const qg_c z = cmk((rb * k.re + 0.0 * k.im) / kk2, (0.0 * k.re - rb * k.im) / kk2);
+  qg_c a1 = cmk(z.re - 1, z.im), a2 = cmk(z.re + 1, z.im);
+  a2 = (a2.re < 0 && a2.im <= 0) ? cscale(csqrt_(a2), -1.0) : csqrt_(a2);
+  a1 = (a1.re < 0 && a1.im >= 0) ? cscale(csqrt_(a1), -1.0) : csqrt_(a1);
+  gam = cmul(a1, a2);
+  const qg_c x = cscale(cmul(gam, k), 1.0 / (2 * eta));
+  const qg_c x2 = cmul(x, x);
+  if (x2.re > 56.0) return 0;
+  uu = csqrt_(x2);
+  if (x2.re < 0 && !signbit(x2.im)) uu = cscale(uu, -1.0);  // branch m = -1 (ewald.c:390-393)
+  return 2;
+}
+
 // M[R, C] = delta_RC I - T_R W(R <- C) from sigma in shared memory
 // (translations.c:926-1078 contraction; the B sum runs over q <= qmax_A).
 template <int LMAX>
@@ -453,6 +494,8 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
   constexpr int LE = Sh::LE, S = Sh::S, NEV = Sh::NEVEN;
   __shared__ qg_c sig[S];
   __shared__ qg_c red[kEThreads / 32][Sh::RED];
+  __shared__ int lstA[kEThreads * kELChunks], lstB[kEThreads * kELChunks];
+  __shared__ int lw[2][kEThreads / 32], lcnt[2];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int np = a.np;
   const size_t per = a.npairs ? (size_t)a.npairs : (size_t)np * np;  // blocks per matrix
@@ -585,156 +628,171 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
       if (!lr_ok && tid == 0) atomicOr(a.err, 1);
       const qg_c rk = crecip(k);
       const qg_c lrfac = crecip(cscale(cmul(k, k), c_ew.area));  // commonfac 1 / (k^2 A), ewald.c:344
-      for (int t = tid; lr_ok && t < W1 * W2; t += kEThreads) {
-        const int i = t / W2 - I1, j = t % W2 - I2;
-        const double Kx = i * c_ew.rb[0] + j * c_ew.rb[2], Ky = i * c_ew.rb[1] + j * c_ew.rb[3];
-        const double qx = Kx + bx, qy = Ky + by;
-        const double rb = sqrt(qx * qx + qy * qy);
-        qg_c gam, uu;
-        if (kreal) {
-          // clilgamma(rb / k) (ewald.h:157-170) for real k: sqrt(t - 1) sqrt(t + 1)
-          // with t - 1 exact; near a Rayleigh anomaly (t -> 1) the 1/gamma terms
-          // dominate, so gamma is formed from the exact differences as there
-          const double tt = rb / k.re;
-          if (tt >= 1.0) {
-            gam = cmk(sqrt(tt - 1.0) * sqrt(tt + 1.0), 0.0);
-            const double x = gam.re * k.re / (2 * eta);
-            if (x * x > 56.0) continue;
-            uu = cmk(x, 0.0);
-          } else {
-            const double g = sqrt(1.0 - tt) * sqrt(1.0 + tt);
-            gam = cmk(0.0, -g);  // -i sqrt(1 - t^2)
-            // x^2 = -(g k / 2 eta)^2, approached from below the negative axis: sqrt -> -i c
-            uu = cmk(0.0, -g * k.re / (2 * eta));
-          }
-        } else {
-          // z = rb / k as C's real / complex division forms it: (rb + 0i)(conj k) / |k|^2.
-          // The sign of a zero imaginary part (rb = 0, i.e. beta on a reciprocal
-          // lattice point) picks the branch of a1 below, so it must be +0 as there.
-          const double kk2 = k.re * k.re + k.im * k.im;
-          const qg_c z = cmk((rb * k.re + 0.0 * k.im) / kk2, (0.0 * k.re - rb * k.im) / kk2);
-          qg_c a1 = cmk(z.re - 1, z.im), a2 = cmk(z.re + 1, z.im);
-          a2 = (a2.re < 0 && a2.im <= 0) ? cscale(csqrt_(a2), -1.0) : csqrt_(a2);
-          a1 = (a1.re < 0 && a1.im >= 0) ? cscale(csqrt_(a1), -1.0) : csqrt_(a1);
-          gam = cmul(a1, a2);
-          const qg_c x = cscale(cmul(gam, k), 1.0 / (2 * eta));
-          const qg_c x2 = cmul(x, x);
-          if (x2.re > 56.0) continue;
-          uu = csqrt_(x2);
-          if (x2.re < 0 && !signbit(x2.im)) uu = cscale(uu, -1.0);  // branch m = -1 (ewald.c:390-393)
+      // reciprocal points in batches: classified (outside the cutoff / evanescent
+      // at real k / other) and compacted in grid order with a block prefix sum,
+      // so the warps process dense lists (FP64 lanes masked off by divergence
+      // are lost time on the FP64 pipe)
+      const int WW = lr_ok ? W1 * W2 : 0;
+      for (int t0 = 0; t0 < WW; t0 += kEThreads * kELChunks) {
+        __syncthreads();
+        if (tid == 0) {
+          lcnt[0] = 0;
+          lcnt[1] = 0;
         }
-        double sK, cK;
-        sincos(Kx * sx + Ky * sy, &sK, &cK);
-        const qg_c phasefac = cmul(cmk(cK, sK), lrfac);  // e^{i K.s} / (k^2 A)
-        // e^{i alpha}, alpha = arg(beta + K) (0 at the origin, as atan2(0, 0))
-        const qg_c e1 = rb > 0 ? cmk(qx / rb, qy / rb) : cmk(1.0, 0.0), e2 = cmul(e1, e1), e1c = cconj(e1);
-        if (kreal && gam.im == 0.0) {
-          // evanescent order at real k: gamma, x = gamma k / 2 eta, Gamma(1/2 - j, x^2),
-          // rb / k are real, so is every P_nj; only e^{i m alpha} and the phase are complex
-          const double x = uu.re, X = x * x, emX = exp(-X);
-          double Gr[LE / 2 + 1];
-          Gr[0] = 1.7724538509055160273 * erfc(x);  // Gamma(1/2, x^2)
-          double zp = 1.0 / x;                      // x^(1-2j)
-          const double rX = 1.0 / X;
-#pragma unroll
-          for (int j = 1; j <= LE / 2; ++j) {
-            Gr[j] = (Gr[j - 1] - zp * emX) / (0.5 - j);
-            zp *= rX;
+        __syncthreads();
+        for (int c = 0; c < kELChunks; ++c) {
+          const int t = t0 + c * kEThreads + tid;
+          int cls = 0;
+          if (t < WW) {
+            const int i = t / W2 - I1, j = t % W2 - I2;
+            const double qx = i * c_ew.rb[0] + j * c_ew.rb[2] + bx, qy = i * c_ew.rb[1] + j * c_ew.rb[3] + by;
+            qg_c g_, u_;
+            cls = lr_class(k, kreal, eta, sqrt(qx * qx + qy * qy), g_, u_);
           }
-          double gpr[LE / 2 + 1];
-          {
-            double g = 1.0 / gam.re;
-            const double gsq = gam.re * gam.re;
-#pragma unroll
-            for (int j = 0; j <= LE / 2; ++j) {
-              gpr[j] = g * Gr[j];
-              g *= gsq;
+          const unsigned bA = __ballot_sync(0xffffffffu, cls == 1), bB = __ballot_sync(0xffffffffu, cls == 2);
+          if (lane == 0) {
+            lw[0][warp] = __popc(bA);
+            lw[1][warp] = __popc(bB);
+          }
+          __syncthreads();
+          int oA = lcnt[0], oB = lcnt[1];
+          for (int w = 0; w < warp; ++w) {
+            oA += lw[0][w];
+            oB += lw[1][w];
+          }
+          const unsigned lt = (1u << lane) - 1u;
+          if (cls == 1) lstA[oA + __popc(bA & lt)] = t;
+          if (cls == 2) lstB[oB + __popc(bB & lt)] = t;
+          __syncthreads();
+          if (tid == 0)
+            for (int w = 0; w < kEThreads / 32; ++w) {
+              lcnt[0] += lw[0][w];
+              lcnt[1] += lw[1][w];
             }
-          }
-          double tp[LE + 1];
-          tp[0] = 1.0;
-          const double tkr = rb / k.re;
-#pragma unroll
-          for (int p = 1; p <= LE; ++p) tp[p] = tp[p - 1] * tkr;
-          qg_c emn = phasefac;
-#pragma unroll
-          for (int n = 0; n <= LE; ++n) {
-            double P[LE / 2 + 1];
-#pragma unroll
-            for (int j = 0; j <= n / 2; ++j) P[j] = tp[n - 2 * j] * gpr[j];
-            qg_c em = emn;
-#pragma unroll
-            for (int q = 0; q <= n; ++q) {
-              const int m = -n + 2 * q;
-              const int y = n * (n + 1) + m;
-              const int jmax = (n - (m < 0 ? -m : m)) / 2;
-              double jr = 0;
-#pragma unroll
-              for (int j = 0; j <= jmax; ++j) jr = fma(c_ew.s1r[c_ew.s1off[y] + j], P[j], jr);
-              // acc += i^(n+1) jr em
-              const int kk = n * (n + 1) / 2 + q;
-              switch ((n + 1) & 3) {
-                case 0: acc[kk].re = fma(jr, em.re, acc[kk].re); acc[kk].im = fma(jr, em.im, acc[kk].im); break;
-                case 1: acc[kk].re = fma(-jr, em.im, acc[kk].re); acc[kk].im = fma(jr, em.re, acc[kk].im); break;
-                case 2: acc[kk].re = fma(-jr, em.re, acc[kk].re); acc[kk].im = fma(-jr, em.im, acc[kk].im); break;
-                default: acc[kk].re = fma(jr, em.im, acc[kk].re); acc[kk].im = fma(-jr, em.re, acc[kk].im); break;
+          __syncthreads();
+        }
+        const int nA = lcnt[0], nB = lcnt[1];
+        for (int pidx = tid; pidx < nA + nB; pidx += kEThreads) {
+          const int t = pidx < nA ? lstA[pidx] : lstB[pidx - nA];
+          const int i = t / W2 - I1, j = t % W2 - I2;
+          const double Kx = i * c_ew.rb[0] + j * c_ew.rb[2], Ky = i * c_ew.rb[1] + j * c_ew.rb[3];
+          const double qx = Kx + bx, qy = Ky + by;
+          const double rb = sqrt(qx * qx + qy * qy);
+          qg_c gam, uu;
+          lr_class(k, kreal, eta, rb, gam, uu);
+          double sK, cK;
+          sincos(Kx * sx + Ky * sy, &sK, &cK);
+          const qg_c phasefac = cmul(cmk(cK, sK), lrfac);  // e^{i K.s} / (k^2 A)
+          // e^{i alpha}, alpha = arg(beta + K) (0 at the origin, as atan2(0, 0))
+          const qg_c e1 = rb > 0 ? cmk(qx / rb, qy / rb) : cmk(1.0, 0.0), e2 = cmul(e1, e1), e1c = cconj(e1);
+          if (pidx < nA) {
+            // evanescent order at real k: gamma, x = gamma k / 2 eta, Gamma(1/2 - j, x^2),
+            // rb / k are real, so is every P_nj; only e^{i m alpha} and the phase are complex
+            const double x = uu.re, X = x * x, emX = exp(-X);
+            double Gr[LE / 2 + 1];
+            Gr[0] = 1.7724538509055160273 * erfc(x);  // Gamma(1/2, x^2)
+            double zp = 1.0 / x;                      // x^(1-2j)
+            const double rX = 1.0 / X;
+  #pragma unroll
+            for (int j = 1; j <= LE / 2; ++j) {
+              Gr[j] = (Gr[j - 1] - zp * emX) / (0.5 - j);
+              zp *= rX;
+            }
+            double gpr[LE / 2 + 1];
+            {
+              double g = 1.0 / gam.re;
+              const double gsq = gam.re * gam.re;
+  #pragma unroll
+              for (int j = 0; j <= LE / 2; ++j) {
+                gpr[j] = g * Gr[j];
+                g *= gsq;
               }
-              em = cmul(em, e2);
             }
-            emn = cmul(emn, e1c);
-          }
-          continue;
-        }
-        qg_c G[LE / 2 + 1];
-        gamma_half_down(uu, LE / 2, G);
-        // powers: (rb/k)^(n - 2j) and gamma^(2j - 1)
-        const qg_c tk = cscale(rk, rb);
-        qg_c gp[LE / 2 + 1];  // gamma^(2j-1) G_j
-        {
-          qg_c g = crecip(gam);  // gamma^-1
-          const qg_c gsq = cmul(gam, gam);
-          for (int j = 0; j <= LE / 2; ++j) {
-            gp[j] = cmul(g, G[j]);
-            g = cmul(g, gsq);
-          }
-        }
-        qg_c tpow[LE + 1];
-        tpow[0] = cmk(1, 0);
-        for (int p = 1; p <= LE; ++p) tpow[p] = cmul(tpow[p - 1], tk);
-        // s1[y][j] = i^(n+1) s1r[y][j]: js = i^(n+1) sum_j s1r P_nj, P_nj = tpow[n-2j] gp[j]
-        qg_c emn = phasefac;  // e^{-i n alpha} e^{i K.s} / (k^2 A)
-#pragma unroll
-        for (int n = 0; n <= LE; ++n) {
-          qg_c P[LE / 2 + 1];
-#pragma unroll
-          for (int j = 0; j <= n / 2; ++j) P[j] = cmul(tpow[n - 2 * j], gp[j]);
-          qg_c em = emn;
-#pragma unroll
-          for (int q = 0; q <= n; ++q) {
-            const int m = -n + 2 * q;
-            const int y = n * (n + 1) + m;
-            const int jmax = (n - (m < 0 ? -m : m)) / 2;
-            double jr = 0, ji = 0;
-#pragma unroll
-            for (int j = 0; j <= jmax; ++j) {
-              const double c = c_ew.s1r[c_ew.s1off[y] + j];
-              jr = fma(c, P[j].re, jr);
-              ji = fma(c, P[j].im, ji);
+            double tp[LE + 1];
+            tp[0] = 1.0;
+            const double tkr = rb / k.re;
+  #pragma unroll
+            for (int p = 1; p <= LE; ++p) tp[p] = tp[p - 1] * tkr;
+            qg_c emn = phasefac;
+  #pragma unroll
+            for (int n = 0; n <= LE; ++n) {
+              double P[LE / 2 + 1];
+  #pragma unroll
+              for (int j = 0; j <= n / 2; ++j) P[j] = tp[n - 2 * j] * gpr[j];
+              qg_c em = emn;
+  #pragma unroll
+              for (int q = 0; q <= n; ++q) {
+                const int m = -n + 2 * q;
+                const int y = n * (n + 1) + m;
+                const int jmax = (n - (m < 0 ? -m : m)) / 2;
+                double jr = 0;
+  #pragma unroll
+                for (int j = 0; j <= jmax; ++j) jr = fma(c_ew.s1r[c_ew.s1off[y] + j], P[j], jr);
+                // acc += i^(n+1) jr em
+                const int kk = n * (n + 1) / 2 + q;
+                switch ((n + 1) & 3) {
+                  case 0: acc[kk].re = fma(jr, em.re, acc[kk].re); acc[kk].im = fma(jr, em.im, acc[kk].im); break;
+                  case 1: acc[kk].re = fma(-jr, em.im, acc[kk].re); acc[kk].im = fma(jr, em.re, acc[kk].im); break;
+                  case 2: acc[kk].re = fma(-jr, em.re, acc[kk].re); acc[kk].im = fma(-jr, em.im, acc[kk].im); break;
+                  default: acc[kk].re = fma(jr, em.im, acc[kk].re); acc[kk].im = fma(-jr, em.re, acc[kk].im); break;
+                }
+                em = cmul(em, e2);
+              }
+              emn = cmul(emn, e1c);
             }
-            qg_c js;  // times i^(n+1)
-            switch ((n + 1) & 3) {
-              case 0: js = cmk(jr, ji); break;
-              case 1: js = cmk(-ji, jr); break;
-              case 2: js = cmk(-jr, -ji); break;
-              default: js = cmk(ji, -jr); break;
+          } else {
+            qg_c G[LE / 2 + 1];
+            gamma_half_down(uu, LE / 2, G);
+            // powers: (rb/k)^(n - 2j) and gamma^(2j - 1)
+            const qg_c tk = cscale(rk, rb);
+            qg_c gp[LE / 2 + 1];  // gamma^(2j-1) G_j
+            {
+              qg_c g = crecip(gam);  // gamma^-1
+              const qg_c gsq = cmul(gam, gam);
+              for (int j = 0; j <= LE / 2; ++j) {
+                gp[j] = cmul(g, G[j]);
+                g = cmul(g, gsq);
+              }
             }
-            const int kk = n * (n + 1) / 2 + q;
-            const qg_c pr = cmul(js, em);
-            acc[kk].re += pr.re;
-            acc[kk].im += pr.im;
-            em = cmul(em, e2);
+            qg_c tpow[LE + 1];
+            tpow[0] = cmk(1, 0);
+            for (int p = 1; p <= LE; ++p) tpow[p] = cmul(tpow[p - 1], tk);
+            // s1[y][j] = i^(n+1) s1r[y][j]: js = i^(n+1) sum_j s1r P_nj, P_nj = tpow[n-2j] gp[j]
+            qg_c emn = phasefac;  // e^{-i n alpha} e^{i K.s} / (k^2 A)
+    #pragma unroll
+            for (int n = 0; n <= LE; ++n) {
+              qg_c P[LE / 2 + 1];
+    #pragma unroll
+              for (int j = 0; j <= n / 2; ++j) P[j] = cmul(tpow[n - 2 * j], gp[j]);
+              qg_c em = emn;
+    #pragma unroll
+              for (int q = 0; q <= n; ++q) {
+                const int m = -n + 2 * q;
+                const int y = n * (n + 1) + m;
+                const int jmax = (n - (m < 0 ? -m : m)) / 2;
+                double jr = 0, ji = 0;
+    #pragma unroll
+                for (int j = 0; j <= jmax; ++j) {
+                  const double c = c_ew.s1r[c_ew.s1off[y] + j];
+                  jr = fma(c, P[j].re, jr);
+                  ji = fma(c, P[j].im, ji);
+                }
+                qg_c js;  // times i^(n+1)
+                switch ((n + 1) & 3) {
+                  case 0: js = cmk(jr, ji); break;
+                  case 1: js = cmk(-ji, jr); break;
+                  case 2: js = cmk(-jr, -ji); break;
+                  default: js = cmk(ji, -jr); break;
+                }
+                const int kk = n * (n + 1) / 2 + q;
+                const qg_c pr = cmul(js, em);
+                acc[kk].re += pr.re;
+                acc[kk].im += pr.im;
+                em = cmul(em, e2);
+              }
+              emn = cmul(emn, e1c);
+            }
           }
-          emn = cmul(emn, e1c);
         }
       }
     }
