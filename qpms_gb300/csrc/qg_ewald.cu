@@ -549,12 +549,37 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
       const qg_c k2h = cscale(cmul(k, k), 0.5);
       const qg_c ik2eta = cmk(-k.im / (2 * eta), k.re / (2 * eta));  // i k / (2 eta)
       const qg_c rk = crecip(k);
-      for (int t = tid; sr_ok && t < W1 * W2; t += kEThreads) {
+      // direct-lattice points in batches, compacted as the reciprocal ones below
+      const int WS = sr_ok ? W1 * W2 : 0;
+      for (int t0 = 0; t0 < WS; t0 += kEThreads * kELChunks) {
+        __syncthreads();
+        if (tid == 0) lcnt[0] = 0;
+        __syncthreads();
+        for (int c = 0; c < kELChunks; ++c) {
+          const int t = t0 + c * kEThreads + tid;
+          bool ok = false;
+          if (t < WS) {
+            const int i = t / W2 - I1, j = t % W2 - I2;
+            const double Rx = i * c_ew.b[0] + j * c_ew.b[2] - sx, Ry = i * c_ew.b[1] + j * c_ew.b[3] - sy;
+            ok = !(self && i == 0 && j == 0) && sqrt(Rx * Rx + Ry * Ry) * eta <= 7.5;
+          }
+          const unsigned bA = __ballot_sync(0xffffffffu, ok);
+          if (lane == 0) lw[0][warp] = __popc(bA);
+          __syncthreads();
+          int oA = lcnt[0];
+          for (int w = 0; w < warp; ++w) oA += lw[0][w];
+          if (ok) lstA[oA + __popc(bA & ((1u << lane) - 1u))] = t;
+          __syncthreads();
+          if (tid == 0)
+            for (int w = 0; w < kEThreads / 32; ++w) lcnt[0] += lw[0][w];
+          __syncthreads();
+        }
+        const int nS = lcnt[0];
+      for (int pidx = tid; pidx < nS; pidx += kEThreads) {
+        const int t = lstA[pidx];
         const int i = t / W2 - I1, j = t % W2 - I2;
-        if (self && i == 0 && j == 0) continue;
         const double Rx = i * c_ew.b[0] + j * c_ew.b[2] - sx, Ry = i * c_ew.b[1] + j * c_ew.b[3] - sy;
         const double r2 = Rx * Rx + Ry * Ry, r = sqrt(r2);
-        if (r * eta > 7.5) continue;
         // e^{i beta.(R - s)} folded into E+-, E: the I_n recurrence is linear, so
         // it yields I_n e^{i beta.(R - s)} directly
         double sb, cb;
@@ -615,6 +640,7 @@ __global__ void __launch_bounds__(kEThreads) ewald_assemble_kernel(EwaldArgs a, 
           emn = cmul(emn, e1c);
           cn = cmul(cn, twor_k);
         }
+      }
       }
     }
     // ---------------- long range (reciprocal lattice) ----------------
