@@ -466,6 +466,10 @@ qpms_scatsys_t *qpms_gpu_scatsys_create_spheres_ld(int np, const double *pos_xyz
  * basis inside each irrep; eigenvalues, determinants and unpacked solutions
  * agree.  ss->saecv_sizes is set. */
 int qpms_gpu_scatsys_set_symmetry(qpms_scatsys_t *ss, const char *group);
+/* The same from the reference's group object (a qpms_finite_group_t *, whose
+ * first member is the name, groups.h:53-54), e.g. the one
+ * FinitePointGroup(point_group_info['D2h']) builds. */
+int qpms_gpu_scatsys_set_symmetry_group(qpms_scatsys_t *ss, const void *finite_group);
 int qpms_gpu_scatsys_nirreps(const qpms_scatsys_t *ss);
 const char *qpms_gpu_scatsys_irrep_name(const qpms_scatsys_t *ss, int iri);
 const size_t *qpms_gpu_scatsys_saecv_sizes(const qpms_scatsys_t *ss);
@@ -481,11 +485,28 @@ qpms_complex_t *qpms_scatsys_irrep_unpack_vector(qpms_complex_t *target_full,   
     const qpms_complex_t *orig_packed, const qpms_scatsys_t *ss, int iri, bool add);
 qpms_complex_t *qpms_scatsys_build_translation_matrix_e_irrep_packed(               /* scatsystem.h:390-397 */
     qpms_complex_t *target, const qpms_scatsys_t *ss, int iri, qpms_complex_t k, qpms_bessel_t J);
+/* The reference's slow-implementation names and builder variants compute the
+ * same (scatsystem.h:318-326, 413-430). */
+qpms_complex_t *qpms_scatsys_irrep_pack_matrix_stupid(qpms_complex_t *target_packed,
+    const qpms_complex_t *orig_full, const qpms_scatsys_t *ss, int iri);
+qpms_complex_t *qpms_scatsys_irrep_unpack_matrix_stupid(qpms_complex_t *target_full,
+    const qpms_complex_t *orig_packed, const qpms_scatsys_t *ss, int iri, bool add);
+qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_irrep_packed_orbitorderR(qpms_complex_t *target,
+    const qpms_scatsys_at_omega_t *ssw, int iri);
+qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_irrep_packed_serial(qpms_complex_t *target,
+    const qpms_scatsys_at_omega_t *ssw, int iri);
 
 /* Evaluates the medium and the T-matrices at omega, like qpms_scatsys_at_omega
  * (scatsystem.c:606-630). */
 qpms_scatsys_at_omega_t *qpms_gpu_scatsys_at_omega(const qpms_scatsys_t *ss, qpms_complex_t omega);
 void qpms_gpu_scatsys_at_omega_free(qpms_scatsys_at_omega_t *ssw);
+/* The reference's names of the lifetime functions (scatsystem.h:297-306):
+ * qpms_scatsys_free, qpms_scatsys_at_omega, qpms_scatsys_at_omega_free. */
+void qpms_scatsys_free(qpms_scatsys_t *ss);
+qpms_scatsys_at_omega_t *qpms_scatsys_at_omega(const qpms_scatsys_t *ss, qpms_complex_t omega);
+void qpms_scatsys_at_omega_free(qpms_scatsys_at_omega_t *ssw);
+/* scatsystem.h:20: thread count of the reference's CPU builders; accepted and ignored. */
+void qpms_scatsystem_set_nthreads(long n);
 
 /* -- drop-in replacements of the reference's hot-path functions -- */
 
@@ -507,6 +528,17 @@ qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_full(qpms_complex_t *targ
  * scatsystem.c:1180-1217): S(R<-C) of kind J for R != C, zero diagonal blocks. */
 qpms_complex_t *qpms_scatsys_build_translation_matrix_e_full(qpms_complex_t *target,
     const qpms_scatsys_t *ss, qpms_complex_t k, qpms_bessel_t J);
+/* Replaces qpms_scatsys_build_translation_matrix_full (scatsystem.h:357-362): J = QPMS_HANKEL_PLUS. */
+qpms_complex_t *qpms_scatsys_build_translation_matrix_full(qpms_complex_t *target,
+    const qpms_scatsys_t *ss, qpms_complex_t k);
+/* Replace qpms_scatsys_periodic_build_translation_matrix_full and
+ * qpms_scatsyswk_build_translation_matrix_full (scatsystem.h:505-519,
+ * scatsystem.c:1252-1281): the lattice-summed W of the unit cell (2D xy
+ * lattice); eta 0 / NaN selects qpms_ss_adjusted_eta. */
+qpms_complex_t *qpms_scatsys_periodic_build_translation_matrix_full(qpms_complex_t *target,
+    const qpms_scatsys_t *ss, qpms_complex_t wavenumber, const cart3_t *wavevector, double eta);
+qpms_complex_t *qpms_scatsyswk_build_translation_matrix_full(qpms_complex_t *target,
+    const qpms_scatsys_at_omega_k_t *sswk);
 
 /* Replace qpms_scatsysw_modeproblem_matrix_full_factorise / _build_..._LU /
  * qpms_scatsys_scatter_solve / qpms_ss_LU_free (scatsystem.h:442-480,

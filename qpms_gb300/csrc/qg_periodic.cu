@@ -805,6 +805,52 @@ int qpms_gpu_scatsyswk_scattered_E(const qpms_scatsys_at_omega_k_t *sswk, qpms_b
   return periodic_field(ss, k, beta, eta, (const qg_c *)cvf, npoints, where_xyz, (qg_c *)E_xyz);
 }
 
+// W, the lattice-summed translation matrix of the unit cell (scatsystem.c:1252-1281):
+// the Ewald assembly with T = -1 gives I + W.
+qpms_complex_t *qpms_scatsys_periodic_build_translation_matrix_full(qpms_complex_t *target, const qpms_scatsys_t *ss,
+                                                                    qpms_complex_t wavenumber,
+                                                                    const cart3_t *wavevector, double eta) {
+  clear_error();
+  if (!ss || !wavevector) { set_error("NULL argument"); return nullptr; }
+  if (ss->lattice_dimension != 2) { set_error("Only 2D-periodic lattices implemented"); return nullptr; }
+  if (wavevector->z != 0) { set_error("Only 2D xy-lattices currently supported"); return nullptr; }
+  const double kv[3] = {wavevector->x, wavevector->y, 0.0};
+  if (eta == 0 || isnan(eta)) eta = qpms_ss_adjusted_eta(ss, wavenumber, kv);
+  const size_t N = ss->fecv_size;
+  const int np = ss->p_count, n = (int)(N / np);
+  std::vector<qg_c> T((size_t)ss->tm_count * n, cmk(-1.0, 0.0));
+  const qg_c k = cmk(wavenumber.re, wavenumber.im);
+  const double beta[2] = {kv[0], kv[1]};
+  Dev dM;
+  if (dalloc(dM, N * N * 16)) return nullptr;
+  if (periodic_assemble_device(ss, 1, &k, T, 1, beta, &eta, dM.as<qg_c>(), 0)) return nullptr;
+  bool own = false;
+  if (!target) {
+    target = (qpms_complex_t *)malloc(N * N * 16);
+    own = true;
+    if (!target) { set_error("out of host memory"); return nullptr; }
+  }
+  if (cudaMemcpy(target, dM.p, N * N * 16, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    set_error("device to host copy failed");
+    if (own) free(target);
+    return nullptr;
+  }
+  for (size_t i = 0; i < N; ++i) target[i * N + i].re -= 1.0;
+  return target;
+}
+
+qpms_complex_t *qpms_scatsyswk_build_translation_matrix_full(qpms_complex_t *target,
+                                                             const qpms_scatsys_at_omega_k_t *sswk) {
+  clear_error();
+  if (!sswk || !sswk->ssw) { set_error("NULL argument"); return nullptr; }
+  cart3_t kv;
+  kv.x = sswk->k[0];
+  kv.y = sswk->k[1];
+  kv.z = sswk->k[2];
+  return qpms_scatsys_periodic_build_translation_matrix_full(target, sswk->ssw->ss, sswk->ssw->wavenumber, &kv,
+                                                             sswk->eta);
+}
+
 ccart3_t qpms_scatsyswk_scattered_E(const qpms_scatsys_at_omega_k_t *sswk, qpms_bessel_t btyp,
                                     const qpms_complex_t *cvf, cart3_t where) {
   ccart3_t res;

@@ -729,6 +729,23 @@ qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_full(qpms_complex_t *targ
   return target;
 }
 
+// The reference's names of the system lifetime functions (scatsystem.h:297-306).
+void qpms_scatsys_free(qpms_scatsys_t *ss) { qpms_gpu_scatsys_free(ss); }
+qpms_scatsys_at_omega_t *qpms_scatsys_at_omega(const qpms_scatsys_t *ss, qpms_complex_t omega) {
+  return qpms_gpu_scatsys_at_omega(ss, omega);
+}
+void qpms_scatsys_at_omega_free(qpms_scatsys_at_omega_t *ssw) { qpms_gpu_scatsys_at_omega_free(ssw); }
+// scatsystem.h:20: the reference's thread count for its CPU builders; the
+// GPU paths have no such knob (accepted and ignored).
+void qpms_scatsystem_set_nthreads(long n) { (void)n; }
+
+// S with outgoing waves (scatsystem.h:357-362): qpms_scatsys_build_translation_matrix_e_full
+// with J = QPMS_HANKEL_PLUS.
+qpms_complex_t *qpms_scatsys_build_translation_matrix_full(qpms_complex_t *target, const qpms_scatsys_t *ss,
+                                                           qpms_complex_t k) {
+  return qpms_scatsys_build_translation_matrix_e_full(target, ss, k, QPMS_HANKEL_PLUS);
+}
+
 qpms_complex_t *qpms_scatsys_build_translation_matrix_e_full(qpms_complex_t *target, const qpms_scatsys_t *ss,
                                                              qpms_complex_t k, qpms_bessel_t J) {
   clear_error();

@@ -758,6 +758,28 @@ qpms_complex_t *qpms_scatsys_irrep_unpack_matrix(qpms_complex_t *target, const q
   return target;
 }
 
+// The reference's slow reference-implementation names (scatsystem.h:318-326)
+// and its orbit-ordered / serial builder variants (scatsystem.h:413-430)
+// compute the same matrices.
+qpms_complex_t *qpms_scatsys_irrep_pack_matrix_stupid(qpms_complex_t *target, const qpms_complex_t *orig,
+                                                      const qpms_scatsys_t *ss, int iri) {
+  return qpms_scatsys_irrep_pack_matrix(target, orig, ss, iri);
+}
+qpms_complex_t *qpms_scatsys_irrep_unpack_matrix_stupid(qpms_complex_t *target, const qpms_complex_t *orig,
+                                                        const qpms_scatsys_t *ss, int iri, bool add) {
+  return qpms_scatsys_irrep_unpack_matrix(target, orig, ss, iri, add);
+}
+
+// Symmetry from the reference's group object: its first member is the
+// group's name (groups.h:53-54), which selects the same group here.
+int qpms_gpu_scatsys_set_symmetry_group(qpms_scatsys_t *ss, const void *finite_group) {
+  clear_error();
+  if (!finite_group) { set_error("NULL group"); return QPMS_EINVAL; }
+  const char *name = *(const char *const *)finite_group;
+  if (!name) { set_error("group without a name"); return QPMS_EINVAL; }
+  return qpms_gpu_scatsys_set_symmetry(ss, name);
+}
+
 // (I - T S) directly in the irrep-packed form (scatsystem.c:1361-1471, 1602-1728):
 // the full matrix is assembled on the GPU and packed there.
 qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_irrep_packed(qpms_complex_t *target,
@@ -771,6 +793,15 @@ qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_irrep_packed(qpms_complex
   if (cudaMalloc(&dM.p, N * N * 16) != cudaSuccess) { set_error("out of device memory"); return nullptr; }
   if (ssw_modeproblem_device(ssw, (qg_c *)dM.p, 0)) return nullptr;
   return pack_device_to_host(ssw->ss, sd, iri, (const qg_c *)dM.p, target);
+}
+
+qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_irrep_packed_orbitorderR(
+    qpms_complex_t *target, const qpms_scatsys_at_omega_t *ssw, int iri) {
+  return qpms_scatsysw_build_modeproblem_matrix_irrep_packed(target, ssw, iri);
+}
+qpms_complex_t *qpms_scatsysw_build_modeproblem_matrix_irrep_packed_serial(qpms_complex_t *target,
+                                                                          const qpms_scatsys_at_omega_t *ssw, int iri) {
+  return qpms_scatsysw_build_modeproblem_matrix_irrep_packed(target, ssw, iri);
 }
 
 // The translation matrix S (Bessel kind J) projected on an irrep (scatsystem.c:1132-1178).

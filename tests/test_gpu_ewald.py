@@ -202,3 +202,69 @@ def test_layered_lattice_M_vs_oracle(gpu, orc, cell, E, kv):
     # the sums do not depend on eta (the kernel lowers eta for distant layers)
     M2 = ss(om).modeproblem_matrix_full(k=kv, eta=0.7 * eta)
     assert np.linalg.norm(M2 - M) <= 1e-9 * np.linalg.norm(M - I)
+
+
+def test_periodic_translation_matrix_dropins(gpu, orc):
+    """qpms_scatsys_periodic_build_translation_matrix_full and
+    qpms_scatsyswk_build_translation_matrix_full (scatsystem.c:1252-1281): W of
+    the unit cell (here a bilayer cell) against the oracle's I + W (T = -1)
+    minus I; the finite qpms_scatsys_build_translation_matrix_full equals the
+    _e_full form with outgoing waves."""
+    import ctypes as C
+
+    class Cplx(C.Structure):
+        _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+    class Cart3(C.Structure):
+        _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+    L = gpu.lib()
+    lMax, a = 2, 580e-9
+    pos = np.array([[0, 0, 0], [0.5, 0.3, 0.4]]) * a
+    ss = gpu.ScatteringSystem(pos, RAD, EPS_I, EPS_E, lMax, lattice=((a, 0.0), (0.0, a)))
+    om = 2.0 * EV / HBAR
+    k = np.sqrt(EPS_E) * om / C0
+    kv = (3e6, -1e6)
+    eta = ss.adjusted_eta(k, kv)
+    N = ss.fecv_size
+    f = L.qpms_scatsys_periodic_build_translation_matrix_full
+    f.restype = C.c_void_p
+    f.argtypes = [C.c_void_p, C.c_void_p, Cplx, C.POINTER(Cart3), C.c_double]
+    W = np.zeros((N, N), dtype=np.complex128)
+    assert f(W.ctypes.data, ss.s, Cplx(k, 0.0), C.byref(Cart3(kv[0], kv[1], 0.0)), 0.0), gpu.last_error()
+    n = 2 * lMax * (lMax + 2)
+    T = np.ascontiguousarray(np.broadcast_to(-np.eye(n), (2, n, n)), dtype=complex)
+    X = orc.periodic_modeproblem(orc.TransCalculator(lMax), pos, T, k, (a, 0.0), (0.0, a), kv, eta)
+    ref = X - np.eye(N)
+    assert np.linalg.norm(W - ref) <= 1e-10 * np.linalg.norm(ref)
+    # finite: the J = 3 shorthand
+    fin = gpu.ScatteringSystem(pos, RAD, EPS_I, EPS_E, lMax)
+    g = L.qpms_scatsys_build_translation_matrix_full
+    g.restype = C.c_void_p
+    g.argtypes = [C.c_void_p, C.c_void_p, Cplx]
+    h = L.qpms_scatsys_build_translation_matrix_e_full
+    h.restype = C.c_void_p
+    h.argtypes = [C.c_void_p, C.c_void_p, Cplx, C.c_int]
+    S1 = np.zeros((N, N), dtype=np.complex128)
+    S3 = np.zeros((N, N), dtype=np.complex128)
+    assert g(S1.ctypes.data, fin.s, Cplx(k, 0.0)) and h(S3.ctypes.data, fin.s, Cplx(k, 0.0), 3)
+    assert np.array_equal(S1, S3)
+
+
+def test_symmetry_from_reference_group_object(gpu):
+    """qpms_gpu_scatsys_set_symmetry_group reads the group's name, the first
+    member of the reference's qpms_finite_group_t."""
+    import ctypes as C
+
+    class FG(C.Structure):
+        _fields_ = [("name", C.c_char_p), ("order", C.c_int)]
+
+    a = 400e-9
+    pos = np.array([[x, y, 0.0] for x in (-a / 2, a / 2) for y in (-a / 2, a / 2)])
+    ss = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, 2)
+    L = gpu.lib()
+    L.qpms_gpu_scatsys_set_symmetry_group.restype = C.c_int
+    L.qpms_gpu_scatsys_set_symmetry_group.argtypes = [C.c_void_p, C.c_void_p]
+    grp = FG(b"D4h", 16)
+    assert L.qpms_gpu_scatsys_set_symmetry_group(ss.s, C.byref(grp)) == 0, gpu.last_error()
+    assert ss.nirreps == 10
