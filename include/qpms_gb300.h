@@ -855,6 +855,115 @@ int qpms_gpu_debug_cerfc(double re, double im, double *out);
 /* Number of kernels this library launched since load (for benchmarks). */
 unsigned long long qpms_gpu_kernel_launch_count(void);
 
+/* ---------------- reference-API convenience entry points ----------------
+ * Host set-up helpers beside the hot path (qg_dropins.cu): O(n) or O(n^2) per
+ * particle or contour.  The reference defines several of them as static
+ * inline functions (materials.h, tmatrices.h:380-412); exported here so that
+ * foreign-function callers can bind them. */
+typedef struct sph_t { double r, theta, phi; } sph_t;                        /* qpms_types.h:207-209 */
+typedef struct csphvec_t { qpms_complex_t rc, thetac, phic; } csphvec_t;     /* qpms_types.h:218-220 */
+
+/* materials.h:40-55, 28-34, 151-158; materials.c:166-177 */
+qpms_complex_t qpms_refindex(qpms_epsmu_t em);
+qpms_complex_t qpms_wavenumber(qpms_complex_t omega, qpms_epsmu_t em);
+qpms_complex_t qpms_waveimpedance(qpms_epsmu_t em);
+qpms_epsmu_t qpms_epsmu_generator_eval(qpms_epsmu_generator_t gen, qpms_complex_t omega);
+qpms_complex_t qpms_drude_epsilon(qpms_complex_t eps_inf, qpms_complex_t omega_p, qpms_complex_t gamma_p,
+    qpms_complex_t omega);
+qpms_epsmu_t qpms_lorentzdrude_epsmu(qpms_complex_t omega, const qpms_ldparams_t *p);
+qpms_epsmu_t qpms_lorentzdrude_epsmu_g(qpms_complex_t omega, const void *p);
+
+/* Sphere T-matrices (tmatrices.h:345-412, tmatrices.c:500-606).  Bessel
+ * orders are compiled up to lMax 10 here; a larger lMax, equal J_ext and
+ * J_scat, or a longitudinal basis element returns NULL / QPMS_EINVAL with a
+ * message (the reference aborts on the first two). */
+qpms_complex_t *qpms_mie_coefficients_reflection(qpms_complex_t *target, const qpms_vswf_set_spec_t *bspec,
+    double a, qpms_complex_t k_i, qpms_complex_t k_e, qpms_complex_t mu_i, qpms_complex_t mu_e,
+    qpms_bessel_t J_ext, qpms_bessel_t J_scat);
+int qpms_tmatrix_spherical_fill(qpms_tmatrix_t *t, double a, qpms_complex_t k_i, qpms_complex_t k_e,
+    qpms_complex_t mu_i, qpms_complex_t mu_e);
+qpms_tmatrix_t *qpms_tmatrix_spherical(const qpms_vswf_set_spec_t *bspec, double a, qpms_complex_t k_i,
+    qpms_complex_t k_e, qpms_complex_t mu_i, qpms_complex_t mu_e);
+int qpms_tmatrix_spherical_mu0_fill(qpms_tmatrix_t *t, double a, double omega, qpms_complex_t epsilon_fg,
+    qpms_complex_t epsilon_bg);
+qpms_tmatrix_t *qpms_tmatrix_spherical_mu0(const qpms_vswf_set_spec_t *bspec, double a, double omega,
+    qpms_complex_t epsilon_fg, qpms_complex_t epsilon_bg);
+typedef struct qpms_tmatrix_generator_sphere_param_t {               /* tmatrices.h:367-371 */
+  qpms_epsmu_generator_t outside;
+  qpms_epsmu_generator_t inside;
+  double radius;
+} qpms_tmatrix_generator_sphere_param_t;
+int qpms_tmatrix_generator_sphere(qpms_tmatrix_t *t, qpms_complex_t omega, const void *params);  /* tmatrices.h:374-377 */
+/* T-matrix generators and helpers (tmatrices.h:22-45, 245-281; tmatrices.c:49-75, 257-271, 608-619, 980-989) */
+typedef struct qpms_tmatrix_generator_t {                            /* tmatrices.h:258-264 */
+  int (*function)(qpms_tmatrix_t *t, qpms_complex_t omega, const void *params);
+  const void *params;
+} qpms_tmatrix_generator_t;
+qpms_tmatrix_t *qpms_tmatrix_init_from_generator(const qpms_vswf_set_spec_t *bspec, qpms_tmatrix_generator_t gen,
+    qpms_complex_t omega);
+int qpms_tmatrix_generator_constant(qpms_tmatrix_t *t, qpms_complex_t omega, const void *tmatrix_orig);
+qpms_tmatrix_t *qpms_tmatrix_copy(const qpms_tmatrix_t *T);
+qpms_tmatrix_t *qpms_tmatrix_mv(qpms_tmatrix_t *dest, const qpms_tmatrix_t *orig);
+bool qpms_tmatrix_isclose(const qpms_tmatrix_t *T1, const qpms_tmatrix_t *T2, double rtol, double atol);
+qpms_complex_t *qpms_apply_tmatrix(qpms_complex_t *f_target, const qpms_complex_t *a, const qpms_tmatrix_t *T);
+
+/* Plane waves (vswf.h:92-126, 229-234; vswf.c:445-530).  Longitudinal
+ * coefficients are zero for a transverse amplitude (rc == 0); a
+ * non-transverse amplitude with a longitudinal target returns QPMS_EINVAL.
+ * qpms_incfield_planewave takes the direction of Re k and multiplies the
+ * expansion by e^{i k . evalpoint} (complex k included). */
+int qpms_planewave2vswf_fill_cart(cart3_t wavedir, ccart3_t amplitude, qpms_complex_t *target_longcoeff,
+    qpms_complex_t *target_mgcoeff, qpms_complex_t *target_elcoeff, qpms_l_t lMax, qpms_normalisation_t norm);
+int qpms_planewave2vswf_fill_sph(sph_t wavedir, csphvec_t amplitude, qpms_complex_t *target_longcoeff,
+    qpms_complex_t *target_mgcoeff, qpms_complex_t *target_elcoeff, qpms_l_t lMax, qpms_normalisation_t norm);
+typedef int (*qpms_incfield_t)(qpms_complex_t *target, const qpms_vswf_set_spec_t *bspec,  /* vswf.h:17-24 */
+    const cart3_t evalpoint, const void *args, bool add);
+typedef struct qpms_incfield_planewave_params_t {                    /* vswf.h:93-103 */
+  bool use_cartesian;
+  union { ccart3_t cart; csph_t sph; } k;
+  union { ccart3_t cart; csphvec_t sph; } E;
+} qpms_incfield_planewave_params_t;
+int qpms_incfield_planewave(qpms_complex_t *target, const qpms_vswf_set_spec_t *bspec, const cart3_t evalpoint,
+    const void *args, bool add);
+/* scatsystem.h:621-629, scatsystem.c:1970-1983: field_at_point per particle
+ * into its slice of the full vector (allocated with calloc when NULL). */
+qpms_complex_t *qpms_scatsys_incident_field_vector_full(qpms_complex_t *target_full, const qpms_scatsys_t *ss,
+    qpms_incfield_t field_at_point, const void *args, bool add);
+
+/* Single translation coefficients (translations.h:40-44, 93-121): taken from
+ * one GPU evaluation of the A / B arrays; A(m n <- mu nu) is the
+ * [y(m, n)][y(mu, nu)] element of qpms_trans_calculator_get_AB_arrays.  An
+ * out-of-range index returns QPMS_EINVAL (NaN for the value-returning forms). */
+qpms_complex_t qpms_trans_single_A(qpms_normalisation_t norm, qpms_m_t m, qpms_l_t n, qpms_m_t mu, qpms_l_t nu,
+    csph_t kdlj, bool r_ge_d, qpms_bessel_t J);
+qpms_complex_t qpms_trans_single_B(qpms_normalisation_t norm, qpms_m_t m, qpms_l_t n, qpms_m_t mu, qpms_l_t nu,
+    csph_t kdlj, bool r_ge_d, qpms_bessel_t J);
+qpms_complex_t qpms_trans_calculator_get_A(const qpms_trans_calculator *c, qpms_m_t m, qpms_l_t n, qpms_m_t mu,
+    qpms_l_t nu, csph_t kdlj, bool r_ge_d, qpms_bessel_t J);
+qpms_complex_t qpms_trans_calculator_get_B(const qpms_trans_calculator *c, qpms_m_t m, qpms_l_t n, qpms_m_t mu,
+    qpms_l_t nu, csph_t kdlj, bool r_ge_d, qpms_bessel_t J);
+int qpms_trans_calculator_get_AB_p(const qpms_trans_calculator *c, qpms_complex_t *Adest, qpms_complex_t *Bdest,
+    qpms_m_t m, qpms_l_t n, qpms_m_t mu, qpms_l_t nu, csph_t kdlj, bool r_ge_d, qpms_bessel_t J);
+qpms_complex_t qpms_trans_calculator_get_A_ext(const qpms_trans_calculator *c, int m, int n, int mu, int nu,
+    qpms_complex_t kdlj_r, double kdlj_th, double kdlj_phi, int r_ge_d, int J);
+qpms_complex_t qpms_trans_calculator_get_B_ext(const qpms_trans_calculator *c, int m, int n, int mu, int nu,
+    qpms_complex_t kdlj_r, double kdlj_th, double kdlj_phi, int r_ge_d, int J);
+int qpms_trans_calculator_get_AB_p_ext(const qpms_trans_calculator *c, qpms_complex_t *Adest,
+    qpms_complex_t *Bdest, int m, int n, int mu, int nu, qpms_complex_t kdlj_r, double kdlj_th,
+    double kdlj_phi, int r_ge_d, int J);
+
+/* Half-ellipse and kidney contours (beyn.h:50-66, beyn.c:117-226): n nodes,
+ * the half-axes in entry n and the orientation after it; inside_test NULL. */
+typedef int beyn_contour_halfellipse_orientation;                   /* beyn.h:50-55 */
+#define BEYN_CONTOUR_HALFELLIPSE_RE_PLUS 3
+#define BEYN_CONTOUR_HALFELLIPSE_RE_MINUS 1
+#define BEYN_CONTOUR_HALFELLIPSE_IM_PLUS 0
+#define BEYN_CONTOUR_HALFELLIPSE_IM_MINUS 2
+beyn_contour_t *beyn_contour_halfellipse(qpms_complex_t centre, double halfax_re, double halfax_im,
+    size_t npoints, beyn_contour_halfellipse_orientation orientation);
+beyn_contour_t *beyn_contour_kidney(qpms_complex_t centre, double halfax_re, double halfax_im, double rounding,
+    size_t n, beyn_contour_halfellipse_orientation orientation);
+
 #ifdef __cplusplus
 }
 #endif

@@ -117,6 +117,61 @@ def ellipse(centre, rRe, rIm, n):
     return (z, dz, complex(centre))
 
 
+def _orientation(orient, rRe, rIm):
+    """(rotation, l, h) of a half-ellipse orientation (beyn.c:134-152)."""
+    return {3: (-1j, rIm, rRe), 1: (1j, rIm, rRe), 0: (1.0, rRe, rIm), 2: (-1.0, rRe, rIm)}[orient]
+
+
+def halfellipse(centre, rRe, rIm, n, orient):
+    """Contour tuple of beyn_contour_halfellipse (beyn.c:117-167): narc = n - n//2
+    midpoint nodes on the half-ellipse, n//2 equal steps along its straight side."""
+    fk, l, h = _orientation(orient, rRe, rIm)
+    nline = n // 2
+    narc = n - nline
+    t = (np.arange(narc) + 0.5) * np.pi / narc
+    za = centre + fk * (np.cos(t) * l + 1j * np.sin(t) * h)
+    dza = fk * (-l * np.sin(t) + 1j * h * np.cos(t)) * (np.pi / narc)
+    s = 0.5 * (1 - nline) + np.arange(nline)
+    zl = centre + fk * s * 2 * l / nline
+    dzl = np.full(nline, fk * 2 * l / nline, dtype=complex)
+    return (np.concatenate([za, zl]), np.concatenate([dza, dzl]), complex(centre))
+
+
+def kidney(centre, rRe, rIm, rounding, n, orient):
+    """Contour tuple of beyn_contour_kidney (beyn.c:169-226): the half-ellipse
+    with its two corners rounded by circles of radius rounding * h, nodes at
+    equal steps of the arc-length-like parameter."""
+    fk, l, h = _orientation(orient, rRe, rIm)
+    y = rounding * h
+    x = np.sqrt((h - y) ** 2 - y ** 2)
+    al = np.arcsin(y / (h - y))
+    ar = l / h
+    tmax = 2 * (x + (np.pi / 2 + al) * y + (np.pi / 2 - al) * h)
+    dt = tmax / n
+    b1 = x
+    b2 = b1 + (np.pi / 2 + al) * y
+    b3 = b2 + (np.pi - 2 * al) * h
+    b4 = b3 + (np.pi / 2 + al) * y
+    z, dz = np.empty(n, complex), np.empty(n, complex)
+    for i in range(n):
+        t = i * dt
+        if t <= b1:
+            z[i], dz[i] = centre + t * ar * fk, dt * ar * fk
+            continue
+        if t < b2:
+            ph, cx, cy, r = (t - b1) / y - np.pi / 2, x, y, y
+        elif t < b3:
+            ph, cx, cy, r = (t - b2) / h + al, 0.0, 0.0, h
+        elif t < b4:
+            ph, cx, cy, r = (t - b3) / y + np.pi - al, -x, y, y
+        else:
+            z[i], dz[i] = centre + (t - b4 - x) * ar * fk, dt * ar * fk
+            continue
+        z[i] = centre + (ar * (cx + r * np.cos(ph)) + 1j * (cy + r * np.sin(ph))) * fk
+        dz[i] = dt * (-ar * np.sin(ph) + 1j * np.cos(ph)) * fk
+    return (z, dz, complex(centre))
+
+
 def finite_sphere_M(orc, positions, radius, eps_inside, eps_medium, lMax):
     """M(omega) = I - T S of a finite cluster of identical spheres, as the
     reference's qpms_scatsys_finite_eval_Beyn_ImTS builds it

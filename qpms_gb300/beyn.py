@@ -29,6 +29,10 @@ def declare(L):
     R = C.POINTER(_BeynResult)
     L.beyn_contour_ellipse.restype = vp
     L.beyn_contour_ellipse.argtypes = [cd, cd, cd, cd, sz]
+    L.beyn_contour_halfellipse.restype = vp
+    L.beyn_contour_halfellipse.argtypes = [cd, cd, cd, cd, sz, ci]
+    L.beyn_contour_kidney.restype = vp
+    L.beyn_contour_kidney.argtypes = [cd, cd, cd, cd, cd, sz, ci]
     L.beyn_result_free.restype = None
     L.beyn_result_free.argtypes = [R]
     L.beyn_solve.restype = R
@@ -103,12 +107,45 @@ def probe_matrix(m, l, seed=DEFAULT_SEED):
     return out
 
 
+# orientations of the half-ellipse and kidney contours (beyn.h:50-55): the
+# side of the straight edge's normal that the curved part lies on
+HALFELLIPSE_RE_PLUS, HALFELLIPSE_RE_MINUS, HALFELLIPSE_IM_PLUS, HALFELLIPSE_IM_MINUS = 3, 1, 0, 2
+
+
+def make_contour(centre, rr, ri, n, shape=None):
+    """beyn_contour_t pointer (free with libc free): an ellipse (shape None),
+    ("halfellipse", orientation) or ("kidney", rounding, orientation)
+    (beyn.c:69-226)."""
+    L = lib()
+    c = complex(centre)
+    if shape is None:
+        p = L.beyn_contour_ellipse(c.real, c.imag, rr, ri, n)
+    elif shape[0] == "halfellipse":
+        p = L.beyn_contour_halfellipse(c.real, c.imag, rr, ri, n, shape[1])
+    elif shape[0] == "kidney":
+        p = L.beyn_contour_kidney(c.real, c.imag, rr, ri, shape[1], n, shape[2])
+    else:
+        raise ValueError("unknown contour shape %r" % (shape,))
+    if not p:
+        raise QpmsGpuError(last_error())
+    return p
+
+
+def contour_nodes(p):
+    """(z, dz) arrays of a beyn_contour_t pointer."""
+    n = C.c_size_t.from_address(p).value
+    # header: n (8 bytes), centre (16), inside_test (8)
+    zdz = np.frombuffer((C.c_char * (32 * n)).from_address(p + 32), dtype=np.complex128).reshape(n, 2)
+    return zdz[:, 0].copy(), zdz[:, 1].copy()
+
+
 def beyn_solve(M_function, m, l, omega_centre, omega_rr, omega_ri, contour_points, rank_tol=1e-4,
-               rank_sel_min=1, res_tol=0.0, Vhat=None, seed=DEFAULT_SEED, mode=1, refine_tol=0.0):
-    """Eigenvalues of M(z) inside an ellipse; M_function(z) -> m x m complex array.
+               rank_sel_min=1, res_tol=0.0, Vhat=None, seed=DEFAULT_SEED, mode=1, refine_tol=0.0, shape=None):
+    """Eigenvalues of M(z) inside a contour; M_function(z) -> m x m complex array.
 
     The quadrature solves run on the GPU; M is evaluated on the host by the
-    callback at every contour node (and at every candidate if res_tol > 0)."""
+    callback at every contour node (and at every candidate if res_tol > 0).
+    shape: None for the ellipse, else as in make_contour."""
     L = lib()
 
     @M_FUNCTION
@@ -122,9 +159,7 @@ def beyn_solve(M_function, m, l, omega_centre, omega_rr, omega_ri, contour_point
             return 1
 
     c = complex(omega_centre)
-    contour = L.beyn_contour_ellipse(c.real, c.imag, omega_rr, omega_ri, contour_points)
-    if not contour:
-        raise QpmsGpuError(last_error())
+    contour = make_contour(c, omega_rr, omega_ri, contour_points, shape)
     try:
         V = None
         if Vhat is not None:
@@ -137,6 +172,8 @@ def beyn_solve(M_function, m, l, omega_centre, omega_rr, omega_ri, contour_point
                                         V.ctypes.data if V is not None else None, seed, mode, refine_tol)
     finally:
         C.CDLL(None).free(C.c_void_p(contour))
+    if shape is not None:
+        return _collect(res, l)
     return _collect(res, l, c, omega_rr, omega_ri)
 
 

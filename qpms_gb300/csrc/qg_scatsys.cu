@@ -78,14 +78,15 @@ void bessel_fill(int J, int L, cd x, cd *out) {
   }
 }
 
-// Mie reflection coefficients RV (electric), RH (magnetic), l = 0..lMax.
-void mie_coefficients(int lMax, double a, cd k_i, cd k_e, cd mu_i, cd mu_e, cd *RV, cd *RH) {
+// Mie reflection coefficients RV (electric), RH (magnetic), l = 0..lMax;
+// Je / Js the Bessel kinds of the exciting and scattered waves.
+void mie_coefficients(int lMax, double a, cd k_i, cd k_e, cd mu_i, cd mu_e, cd *RV, cd *RH, int Je = 1, int Js = 3) {
   const cd x_i = k_i * a, x_e = k_e * a;
   const cd eta_inv_i = k_i / mu_i, eta_inv_e = k_e / mu_e;
   std::vector<cd> zi(lMax + 2), ze(lMax + 2), zs(lMax + 2);
   bessel_fill(1, lMax + 1, x_i, zi.data());
-  bessel_fill(1, lMax + 1, x_e, ze.data());
-  bessel_fill(3, lMax + 1, x_e, zs.data());
+  bessel_fill(Je, lMax + 1, x_e, ze.data());
+  bessel_fill(Js, lMax + 1, x_e, zs.data());
   for (int l = 0; l <= lMax; ++l) {
     const cd dzi = -zi[l + 1] + double(l) / x_i * zi[l];
     const cd dze = -ze[l + 1] + double(l) / x_e * ze[l];
@@ -412,6 +413,30 @@ void planewave_direction_coeffs(int lMax, const double k_dir[3], const qpms_comp
   }
 }
 int blas_handle_get(cublasHandle_t *h) { return blas_handle(h); }
+// Host-side helpers of the reference-API convenience entry points (qg_dropins.cu).
+const qpms_vswf_set_spec_t *scatsys_spec(const qpms_scatsys_t *ss) { return &sspriv(ss)->spec; }
+void mie_reflection(int lMax, double a, qpms_complex_t k_i, qpms_complex_t k_e, qpms_complex_t mu_i,
+                    qpms_complex_t mu_e, int Je, int Js, qpms_complex_t *RV, qpms_complex_t *RH) {
+  std::vector<cd> v(lMax + 1), h(lMax + 1);
+  mie_coefficients(lMax, a, to_cd(k_i), to_cd(k_e), to_cd(mu_i), to_cd(mu_e), v.data(), h.data(), Je, Js);
+  for (int l = 0; l <= lMax; ++l) {
+    RV[l] = from_cd(v[l]);
+    RH[l] = from_cd(h[l]);
+  }
+}
+// Plane-wave coefficients for direction (theta, phi) and local amplitude Es,
+// default normalisation, el / mg of length lMax (lMax + 2).
+void planewave_sph_coeffs(int lMax, double theta, double phi, const qpms_complex_t Es[3], qpms_complex_t *el,
+                          qpms_complex_t *mg) {
+  const int ne = lMax * (lMax + 2);
+  const cd E[3] = {to_cd(Es[0]), to_cd(Es[1]), to_cd(Es[2])};
+  std::vector<cd> e(ne), m(ne);
+  planewave_coeffs(lMax, theta, phi, E, e.data(), m.data());
+  for (int y = 0; y < ne; ++y) {
+    el[y] = from_cd(e[y]);
+    mg[y] = from_cd(m[y]);
+  }
+}
 
 // Assemble M for nw frequencies of one system into device memory dM
 // (the T-matrices per frequency are given host-side, dense or diagonal).
