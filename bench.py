@@ -658,7 +658,13 @@ def run_case(spec):
     import qpms_gb300
     from qpms_gb300.workloads import EV, HBAR
     f = spec.split(":")
-    if f[0] == "dense":
+    if f[0] == "finite":  # finite:nx:lMax:nw:mode -- nx x nx spheres, pitch 400 nm, plane-wave scatter
+        nx, lMax, nw, mode = int(f[1]), int(f[2]), int(f[3]), int(f[4])
+        ss = qpms_gb300.ScatteringSystem(_sq(nx, 400e-9), 50e-9, -12 + 1.2j, 2.25, lMax)
+        r = ss.planewave_scatter_batch(np.linspace(1.6, 2.6, nw) * EV / HBAR, mode=mode)
+        torch.cuda.synchronize()
+        print("finite", nx, lMax, nw, "max resid", float(r["residual"].max()))
+    elif f[0] == "dense":
         N, nrhs, mode = int(f[1]), int(f[2]), int(f[3])
         dev = torch.device("cuda:0")
         g = torch.Generator(device=dev)

@@ -55,8 +55,8 @@ cd coeff_to_norm(int norm, int t, int l, int m, cd a) {
 }
 
 // Plane-wave coefficients (vswf.c:445-476) in normalisation norm; long
-// coefficients are zero for a transverse amplitude (amplitude.rc == 0) and
-// not available otherwise.
+// coefficients are zero for a transverse amplitude (amplitude.rc == 0 up to
+// rounding) and not available otherwise.
 int planewave_fill(double theta, double phi, const qpms_complex_t Es[3], qpms_complex_t *lc, qpms_complex_t *mc,
                    qpms_complex_t *ec, int lMax, int norm) {
   if (lMax < 1 || lMax > 16) {
@@ -65,7 +65,9 @@ int planewave_fill(double theta, double phi, const qpms_complex_t Es[3], qpms_co
   }
   const int ne = lMax * (lMax + 2);
   if (lc) {
-    if (Es[0].re != 0 || Es[0].im != 0) {
+    // transverse up to rounding: |E_r| <= 1e-12 |E|
+    const double amp = std::abs(to_cd(Es[0])) + std::abs(to_cd(Es[1])) + std::abs(to_cd(Es[2]));
+    if (std::abs(to_cd(Es[0])) > 1e-12 * amp) {
       set_error("plane wave: longitudinal coefficients of a non-transverse amplitude are not supported");
       return QPMS_EINVAL;
     }

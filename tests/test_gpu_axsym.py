@@ -117,7 +117,7 @@ def test_user_arc_and_generator(gpu, orc):
     from qpms_gb300.tmatrices import ArcFunction, TMatrixGenerator, _EpsMu, _Cplx, _TM, BaseSpec
     a, c = 40e-9, 80e-9
     ref = _gen("spheroid", (a, c), 2.25, 4.0, 4)(3, OM)
-    L = gpu.lib()
+    L = C.CDLL(gpu.lib()._name)  # private handle: argtypes set here stay out of the package's
     arc_lib = ArcFunction.spheroid(a, c)
 
     def f(theta):

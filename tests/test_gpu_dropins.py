@@ -21,6 +21,7 @@ from qpms_gb300.workloads import EV, HBAR, C0
 
 pytestmark = pytest.mark.gpu
 OM = 2.1 * EV / HBAR
+NDEF = 65536 | 8  # QPMS_NORMALISATION_DEFAULT
 
 
 class Cplx(C.Structure):
@@ -105,7 +106,7 @@ def L():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     from qpms_gb300._lib import lib
-    L = lib()
+    L = C.CDLL(lib()._name)  # private handle: argtypes set here stay out of the package's
     vp, cd, ci, sz = C.c_void_p, C.c_double, C.c_int, C.c_size_t
     PT, PS = C.POINTER(TM), C.POINTER(Spec)
     L.qpms_vswf_set_spec_from_lMax.restype = PS
@@ -169,7 +170,7 @@ def _mat(t):
 def test_sphere_tmatrix_vs_oracle(L, orc, lMax, eps_i):
     a, eps_e = 50e-9, 2.25
     Td = orc.tmatrix_sphere_diag(lMax, a, OM, eps_i, eps_e)
-    sp = L.qpms_vswf_set_spec_from_lMax(lMax, 0x3)  # QPMS_NORMALISATION_DEFAULT
+    sp = L.qpms_vswf_set_spec_from_lMax(lMax, NDEF)
     k_i, k_e = np.sqrt(complex(eps_i)) * OM / C0, np.sqrt(eps_e) * OM / C0
     d = np.empty(sp.contents.n, dtype=np.complex128)
     assert L.qpms_mie_coefficients_reflection(d.ctypes.data, sp, a, cx(k_i), cx(k_e), cx(1), cx(1), 1, 3)
@@ -208,7 +209,7 @@ def test_sphere_tmatrix_vs_oracle(L, orc, lMax, eps_i):
             L.qpms_tmatrix_free(t)
         L.qpms_vswf_set_spec_free(sp)
     # J_ext == J_scat is refused
-    assert not L.qpms_mie_coefficients_reflection(None, L.qpms_vswf_set_spec_from_lMax(2, 3), a, cx(k_i),
+    assert not L.qpms_mie_coefficients_reflection(None, L.qpms_vswf_set_spec_from_lMax(2, NDEF), a, cx(k_i),
                                                   cx(k_e), cx(1), cx(1), 1, 1)
 
 
@@ -238,7 +239,7 @@ def test_planewave_coefficients(L, orc, lMax):
     # one particle at the origin: fill_cart gives the per-particle block
     el, mg, lc = (np.empty(ne, dtype=np.complex128) for _ in range(3))
     assert L.qpms_planewave2vswf_fill_cart(Cart3(*kdir), CCart3(*map(cx, Ec)), lc.ctypes.data, mg.ctypes.data,
-                                           el.ctypes.data, lMax, 3) == 0
+                                           el.ctypes.data, lMax, NDEF) == 0
     ref0 = orc.planewave_full(lMax, np.zeros((1, 3)), kv, Ec)
     assert np.abs(np.concatenate([el, mg]) - ref0).max() <= 1e-9 * np.abs(ref0).max()
     assert np.abs(lc).max() <= 1e-12 * np.abs(Ec).max()   # transverse amplitude
@@ -248,7 +249,7 @@ def test_planewave_coefficients(L, orc, lMax):
     Es = [0.0, Ec[0] * ct * cf + Ec[1] * ct * sf - Ec[2] * st, -Ec[0] * sf + Ec[1] * cf]
     el2, mg2 = np.empty(ne, dtype=np.complex128), np.empty(ne, dtype=np.complex128)
     assert L.qpms_planewave2vswf_fill_sph(Sph(1.0, th, ph), CSphVec(*map(cx, Es)), None, mg2.ctypes.data,
-                                          el2.ctypes.data, lMax, 3) == 0
+                                          el2.ctypes.data, lMax, NDEF) == 0
     assert np.abs(el2 - el).max() <= 1e-12 * np.abs(el).max() and np.abs(mg2 - mg).max() <= 1e-12 * np.abs(mg).max()
     # the incident vector of a system through the reference's callback interface
     ss = ScatteringSystem(pos, 50e-9, 4.0, 2.25, lMax)
@@ -264,14 +265,14 @@ def test_planewave_coefficients(L, orc, lMax):
 
 
 def test_single_translation_coefficients(L, orc):
-    lMax, norm = 4, 3
+    lMax, norm = 4, NDEF
     c = L.qpms_trans_calculator_init(lMax, norm)
     try:
         rng = np.random.default_rng(3)
         for J in (1, 3):
             for _ in range(12):
-                n, nu = rng.integers(1, lMax + 1, size=2)
-                m, mu = rng.integers(-n, n + 1), rng.integers(-nu, nu + 1)
+                n, nu = (int(v) for v in rng.integers(1, lMax + 1, size=2))
+                m, mu = int(rng.integers(-n, n + 1)), int(rng.integers(-nu, nu + 1))
                 kr = complex(rng.uniform(0.5, 6), 0.0 if J == 3 else rng.uniform(-0.2, 0.2))
                 th, ph = rng.uniform(0, np.pi), rng.uniform(-np.pi, np.pi)
                 for which, get in (("A", L.qpms_trans_calculator_get_A_ext), ("B", L.qpms_trans_calculator_get_B_ext)):
@@ -291,24 +292,47 @@ def test_single_translation_coefficients(L, orc):
         L.qpms_trans_calculator_free(c)
 
 
-@pytest.mark.parametrize("shape", [("halfellipse", 0), ("halfellipse", 3), ("kidney", 0.3, 0)])
+def _pencil(n=40, seed=11):
+    """complex quadratic pencil T0 + z T1 + z^2 T2 and its eigenvalues (linearised)"""
+    import scipy.linalg as sl
+    rng = np.random.default_rng(seed)
+    T = [rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)) for _ in range(3)]
+    I, Z = np.eye(n), np.zeros((n, n))
+    lam = sl.eigvals(np.block([[Z, I], [-T[0], -T[1]]]), np.block([[I, Z], [Z, T[2]]]))
+    return T, lam[np.isfinite(lam)]
+
+
+def _radius(lam, curved_side):
+    """a radius between two eigenvalue moduli (a 15 % gap) enclosing at least
+    two eigenvalues on the curved side of the straight edge, none near it"""
+    c = np.sort(np.abs(lam[curved_side(lam)]))
+    for k in range(2, c.size):
+        if c[k] > 1.15 * c[k - 1]:
+            return 0.5 * (c[k - 1] + c[k])
+    raise AssertionError("no gap")
+
+
+@pytest.mark.parametrize("shape", [("halfellipse", 0), ("halfellipse", 3), ("kidney", 0.2, 0)])
 def test_beyn_on_halfplane_contours(shape):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     from oracle import beyn as ob
     from qpms_gb300 import beyn as qb
-    rng = np.random.default_rng(11)
-    T0, T1, T2 = (rng.normal(size=(40, 40)) for _ in range(3))
+    (T0, T1, T2), lam = _pencil()
     Mf = lambda z: T0 + z * T1 + z * z * T2
-    V = rng.normal(size=(40, 20)) + 1j * rng.normal(size=(40, 20))
-    centre, rr, ri, n = 0.0, 0.6, 0.6, 240
+    orient = shape[-1]
+    side = (lambda z: z.imag > 0) if orient == 0 else (lambda z: z.real > 0)
+    R = _radius(lam, side)
+    n = 320
     if shape[0] == "halfellipse":
-        contour = ob.halfellipse(centre, rr, ri, n, shape[1])
+        contour = ob.halfellipse(0.0, R, R, n, orient)
     else:
-        contour = ob.kidney(centre, rr, ri, shape[1], n, shape[2])
+        contour = ob.kidney(0.0, R, R, shape[1], n, orient)
+    V = np.random.default_rng(5).normal(size=(40, 20)) + 1j * np.random.default_rng(6).normal(size=(40, 20))
     ref = ob.beyn_solve(Mf, 40, 20, contour, V, 1e-4, 1, 1e-4)
-    got = qb.beyn_solve(Mf, 40, 20, centre, rr, ri, n, 1e-4, 1, 1e-4, Vhat=V, mode=0, shape=shape)
-    assert got["eigval"].size == ref["neig"] >= 1
+    got = qb.beyn_solve(Mf, 40, 20, 0.0, R, R, n, 1e-4, 1, 1e-4, Vhat=V, mode=0, shape=shape)
+    assert got["eigval"].size == ref["neig"] >= 2
     for e in ref["eigval"]:
         assert np.min(np.abs(got["eigval"] - e)) <= 1e-8 * max(abs(e), 1e-3)
+        assert np.min(np.abs(lam - e)) <= 1e-3 * abs(e)   # a true eigenvalue (to the quadrature error)

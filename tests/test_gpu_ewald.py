@@ -153,7 +153,7 @@ def test_AB_arrays_e32_vs_oracle(gpu, orc, norm, k, beta, shift):
     class Cart3(C.Structure):
         _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
 
-    L = gpu.lib()
+    L = C.CDLL(gpu.lib()._name)  # private handle: argtypes set here stay out of the package's
     f = L.qpms_trans_calculator_get_AB_arrays_e32
     f.restype = C.c_int
     f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_ssize_t, C.c_ssize_t, C.c_double,
@@ -218,7 +218,7 @@ def test_periodic_translation_matrix_dropins(gpu, orc):
     class Cart3(C.Structure):
         _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
 
-    L = gpu.lib()
+    L = C.CDLL(gpu.lib()._name)  # private handle: argtypes set here stay out of the package's
     lMax, a = 2, 580e-9
     pos = np.array([[0, 0, 0], [0.5, 0.3, 0.4]]) * a
     ss = gpu.ScatteringSystem(pos, RAD, EPS_I, EPS_E, lMax, lattice=((a, 0.0), (0.0, a)))
@@ -262,7 +262,7 @@ def test_symmetry_from_reference_group_object(gpu):
     a = 400e-9
     pos = np.array([[x, y, 0.0] for x in (-a / 2, a / 2) for y in (-a / 2, a / 2)])
     ss = gpu.ScatteringSystem(pos, 50e-9, EPS_I, EPS_E, 2)
-    L = gpu.lib()
+    L = C.CDLL(gpu.lib()._name)  # private handle: argtypes set here stay out of the package's
     L.qpms_gpu_scatsys_set_symmetry_group.restype = C.c_int
     L.qpms_gpu_scatsys_set_symmetry_group.argtypes = [C.c_void_p, C.c_void_p]
     grp = FG(b"D4h", 16)

@@ -162,7 +162,7 @@ def test_trans_array_lc3p_vs_oracle(torch_cuda, orc):
                     ("lMax_N", C.c_int), ("lMax_L", C.c_int), ("capacity", C.c_size_t), ("norm", C.c_int)]
 
     lMax = 3
-    L = qpms_gb300.lib()
+    L = C.CDLL(qpms_gb300.lib()._name)  # private handle: argtypes set here stay out of the package's
     L.qpms_trans_calculator_get_trans_array_lc3p.restype = C.c_int
     L.qpms_trans_calculator_get_trans_array_lc3p.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(Spec), C.c_size_t,
                                                               C.POINTER(Spec), C.c_size_t, Cplx, Cart3, Cart3, C.c_int]
