@@ -60,7 +60,8 @@ def parse():
                     help="secondary workloads reported beside the headline (comma list, or 'none')")
     ap.add_argument("--case", default=None,
                     help="run one small case for a profiler and exit: dense:N:NRHS:MODE, "
-                         "scan:LATTICE:NW:NK:MODE, beyn:NX:NODES:MODE")
+                         "scan:{square,honeycomb,bilayer}:NW:NK:MODE, finite:NX:LMAX:NW:MODE, "
+                         "field:NX:NPTS:LMAX, axsym:L:NW, beyn:NX:NODES:MODE")
     return ap.parse_args()
 
 
@@ -681,9 +682,13 @@ def run_case(spec):
     elif f[0] == "scan":
         from qpms_gb300.workloads import honeycomb_lattice, honeycomb_path, square_lattice, square_path
         lat, nw, nk, mode = f[1], int(f[2]), int(f[3]), int(f[4])
-        b1, b2, pos = square_lattice() if lat == "square" else honeycomb_lattice()
+        if lat == "bilayer":  # square lattice, second particle shifted (a/2, a/2, 150 nm): layered Ewald sums
+            b1, b2, pos = square_lattice()
+            pos = np.array([[0.0, 0.0, 0.0], [290e-9, 290e-9, 150e-9]])
+        else:
+            b1, b2, pos = square_lattice() if lat == "square" else honeycomb_lattice()
         ss = qpms_gb300.ScatteringSystem(pos, 80e-9, -12 + 1.2j, 2.25, 3, lattice=(b1, b2))
-        kp = (square_path if lat == "square" else honeycomb_path)(n=nk)
+        kp = (honeycomb_path if lat == "honeycomb" else square_path)(n=nk)
         r = ss.dispersion_scan(np.linspace(1.6, 2.6, nw) * EV / HBAR, kp, mode=mode)
         print("scan", lat, nw, nk, "logdet sum", float(np.sum(r["logdet"])), "max resid", float(r["residual"].max()))
     elif f[0] == "field":
