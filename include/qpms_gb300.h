@@ -140,6 +140,13 @@ int qpms_gpu_trans_AB_arrays_batch_host_noalloc(const qpms_trans_calculator *c, 
     const unsigned char *r_ge_d, qpms_bessel_t J,
     qpms_complex_t *A, qpms_complex_t *B);
 
+/* Every entry point that takes a calculator checks that the current device is
+ * the one current at qpms_trans_calculator_init (its device tables live
+ * there) and returns QPMS_EINVAL otherwise.  Test hook: overwrites the device
+ * recorded in the calculator, so that tests on a one-GPU machine can provoke
+ * that mismatch; no counterpart in the reference, not for production use. */
+int qpms_gpu_testing_set_calculator_device(qpms_trans_calculator *c, int device);
+
 /* Number of A / B multipliers (ragged table sizes), for tests. */
 size_t qpms_gpu_trans_calculator_n_multipliers(const qpms_trans_calculator *c, int which_B);
 

@@ -13,8 +13,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
-SOURCES = ["orc_specfunc.c", "orc_trans.c", "orc_ewald.c", "orc_scatsys.c", "orc_interp.c", "orc_axsym.c", "orc_lu.c", "orc_beyn.c"]
+# root of the reference checkout (read only); QPMS_REFERENCE_ROOT overrides it
+REF_ROOT = os.environ.get("QPMS_REFERENCE_ROOT", "/root/reference")
+SOURCES = ["orc_specfunc.c", "orc_trans.c", "orc_ewald.c", "orc_scatsys.c", "orc_interp.c", "orc_axsym.c"]
 
 
 def _newer(target, deps):
@@ -28,7 +29,7 @@ def build_oracle(force=False):
     out_dir = os.path.join(HERE, "_build")
     os.makedirs(out_dir, exist_ok=True)
     out = os.path.join(out_dir, "liborc.so")
-    srcs = [os.path.join(HERE, s) for s in SOURCES if os.path.exists(os.path.join(HERE, s))]
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
     deps = srcs + [os.path.join(HERE, "orc.h")]
     if force or _newer(out, deps):
         cmd = ["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", "-o", out] + srcs + ["-lm"]

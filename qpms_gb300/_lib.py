@@ -51,6 +51,8 @@ def _declare(L):
     L.qpms_gpu_trans_AB_arrays_batch.argtypes = [vp, sz, vp, vp, vp, vp, ci, vp, vp, vp]
     L.qpms_gpu_trans_AB_arrays_batch_host_noalloc.restype = ci
     L.qpms_gpu_trans_AB_arrays_batch_host_noalloc.argtypes = [vp, sz, vp, vp, vp, vp, ci, vp, vp]
+    L.qpms_gpu_testing_set_calculator_device.restype = ci
+    L.qpms_gpu_testing_set_calculator_device.argtypes = [vp, ci]
     L.qpms_gpu_trans_AB_arrays_batch_host.restype = ci
     L.qpms_gpu_trans_AB_arrays_batch_host.argtypes = [vp, sz, vp, vp, vp, vp, ci, vp, vp]
     L.qpms_gpu_trans_multipliers_export.restype = ci

@@ -87,6 +87,10 @@ inline TransCalcPriv *priv(const qpms_trans_calculator *c) {
   return reinterpret_cast<TransCalcPriv *>(const_cast<qpms_trans_calculator *>(c));
 }
 
+// QPMS_EINVAL (with a message) unless the current device is the one that holds
+// the calculator's device tables (qg_trans_api.cu).
+int check_calc_device(const qpms_trans_calculator *c);
+
 // Kernel launcher (qg_trans_kernel.cu).  variant 0 = sorted + TMA-staged
 // stores (default), 1 = natural order with direct stores.
 int launch_trans_ab(const TransDevTables &T, size_t n, const qg_c *kr, const double *theta,

@@ -70,19 +70,28 @@ extern "C" int qpms_gpu_trans_AB_arrays_batch_host_noalloc(const qpms_trans_calc
   if (J < 1 || J > 4) { set_error("invalid Bessel kind J=%d", J); return QPMS_EINVAL; }
   if (n == 0) return QPMS_SUCCESS;
   if (!kr || !theta || !phi || !A || !B) { set_error("NULL buffer"); return QPMS_EINVAL; }
+  int e = check_calc_device(c);
+  if (e) return e;
   const TransDevTables &T = priv(c)->dev;
   const size_t ne2 = (size_t)T.ne2;
+  // per-translation bytes, padding included, bound n before any product with it can wrap
+  const size_t per = 16 + 8 + 8 + (r_ge_d ? 1 : 0) + 2 * ne2 * 16;
+  if (n > kNoAllocScratchBytes / per) {
+    set_error("batch of %zu translations does not fit the allocation-free entry point's %zu bytes of scratch "
+              "(at most about %zu translations at lMax %d)",
+              n, kNoAllocScratchBytes, (kNoAllocScratchBytes - 64) / per, T.lMax);
+    return QPMS_EINVAL;
+  }
   const size_t in_bytes = align16(n * 16) + align16(n * 8) + align16(n * 8) + (r_ge_d ? align16(n) : 0);
   const size_t out_bytes = 2 * n * ne2 * 16;
   if (in_bytes + out_bytes > kNoAllocScratchBytes) {
-    const size_t per = 16 + 8 + 8 + (r_ge_d ? 1 : 0) + 2 * ne2 * 16;
     set_error("batch of %zu translations needs %zu bytes of scratch; the allocation-free entry point holds "
               "%zu bytes (at most about %zu translations at lMax %d)",
               n, in_bytes + out_bytes, kNoAllocScratchBytes, (kNoAllocScratchBytes - 64) / per, T.lMax);
     return QPMS_EINVAL;
   }
   void *base = nullptr;
-  int e = scratch_address(&base);
+  e = scratch_address(&base);
   if (e) return e;
   char *p = (char *)base;
   qg_c *dkr = (qg_c *)p;

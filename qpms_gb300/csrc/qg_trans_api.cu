@@ -87,7 +87,7 @@ int check_batch_args(const qpms_trans_calculator *c, const void *kr, const void 
     set_error("complex buffers must be 16-byte aligned");
     return QPMS_EINVAL;
   }
-  return QPMS_SUCCESS;
+  return check_calc_device(c);
 }
 
 // Host-API staging: chunk of vectors processed per pipeline stage.
@@ -143,6 +143,18 @@ void par_memcpy(void *dst, const void *src, size_t bytes) {
 }
 
 }  // namespace
+
+int check_calc_device(const qpms_trans_calculator *c) {
+  int dev = -1;
+  QG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev != priv(c)->device) {
+    set_error("the calculator's tables live on device %d but device %d is current; make device %d current "
+              "before calling", priv(c)->device, dev, priv(c)->device);
+    return QPMS_EINVAL;
+  }
+  return QPMS_SUCCESS;
+}
+
 }  // namespace qg
 
 using namespace qg;
@@ -198,6 +210,12 @@ void qpms_trans_calculator_free(qpms_trans_calculator *c) {
     if (p->ev[s]) cudaEventDestroy(p->ev[s]);
   }
   delete p;
+}
+
+int qpms_gpu_testing_set_calculator_device(qpms_trans_calculator *c, int device) {
+  if (!c) return QPMS_EINVAL;
+  priv(c)->device = device;
+  return QPMS_SUCCESS;
 }
 
 size_t qpms_gpu_trans_calculator_n_multipliers(const qpms_trans_calculator *c, int which_B) {
