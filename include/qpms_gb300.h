@@ -693,6 +693,43 @@ int qpms_gpu_bf16_gemm(int m, int n, int k, const void *A, const void *B, float 
 int qpms_gpu_dense_solve(int N, int nrhs, const qpms_complex_t *M, const qpms_complex_t *B,
     qpms_complex_t *X, int mode, double *resid, int *iters);
 
+/* Complex64 GEMM on the tensor cores (tcgen05, TMA-staged operands):
+ * D = beta C + alpha A B with A (m x k), B (k x n), C, D (m x n) complex64
+ * (interleaved float pairs), column-major, leading dimensions in complex
+ * elements, device pointers, asynchronous on `stream` (C == D allowed; C is
+ * not read when beta == 0).  Operands are cut into nsplit bf16 digits
+ * (1, 2 or 3) and the digit products with s + t < nsplit are accumulated in
+ * FP32: relative error about 4e-3, 2e-5 and 2e-7.  The building block of the
+ * mixed-precision LU that replaces the reference's LAPACKE_zgetrf / zgetrs
+ * (scatsystem.c:2202-2273, beyn.c:552-564).  Allocates its digit planes with
+ * cudaMallocAsync on the stream. */
+int qpms_gpu_tc_cgemm(int m, int n, int k, const void *A, size_t lda, const void *B, size_t ldb,
+    float alpha, float beta, const void *C, size_t ldc, void *D, size_t ldd, int nsplit, void *stream);
+
+/* Real bf16 GEMM on the tensor cores with FP32 output: D = beta C + alpha A B^T,
+ * A [m][k] and B [n][k] row-major bf16 (row strides lda, ldb: multiples of 8),
+ * D (and C) m x n column-major float.  The digit products of the FP64
+ * refinement residual use it (exact for integer operands whose products sum
+ * below 2^24). */
+int qpms_gpu_tc_gemm_bf16(int m, int n, int k, const void *A, size_t lda, const void *B, size_t ldb,
+    float alpha, float beta, const float *C, size_t ldc, float *D, size_t ldd, void *stream);
+
+/* Live kernel timing for measurements (off by default): enable != 0 starts
+ * recording a CUDA event pair around every launch of the library's main
+ * kernels, on the stream each is launched on, with the launch's work; 0 stops.
+ * Either call clears the sums.  Kinds: 0 tensor-core GEMM (work: executed
+ * bf16 flops), 1 finite assembly (matrix bytes), 2 lattice-sum assembly
+ * (matrix bytes), 3 batched small LU (complex flops 8 N^3 / 3), 4 dense
+ * diagonal-block LU (8 nb^3 / 3), 5 translation coefficients (output bytes),
+ * 6 digit splitting (bytes written).  _get synchronises the recorded events
+ * and returns the summed device milliseconds, work and launch count. */
+int qpms_gpu_kernel_timing(int enable);
+int qpms_gpu_kernel_timing_get(int kind, double *ms, double *work, unsigned long long *launches);
+
+/* QPMS_ERROR (with a message) if a tensor-core kernel's pipeline wait ran out
+ * of time since the last check; synchronises the stream and clears the flag. */
+int qpms_gpu_tc_check_error(void *stream);
+
 /* ---------------- Beyn contour-integral eigensolver (beyn.h) ---------------- */
 #define QPMS_NO_IRREP ((qpms_iri_t) -1)   /* qpms_types.h:325 */
 
@@ -759,7 +796,13 @@ beyn_result_t *qpms_scatsys_periodic_find_eigenmodes(const qpms_scatsys_t *ss, c
 /* Extended form of the two above (k = NULL: finite system): l probe columns
  * (l <= fecv_size), Vhat (row-major fecv_size x l, or NULL for the seeded
  * generator), mode 0 = plain FP64 LU per node, 1 = complex64 LU with FP64
- * refinement to refine_tol (relative residual; <= 0 selects 1e-12). */
+ * refinement to refine_tol (relative residual; <= 0 selects 1e-12).
+ * rank_tol < 0 selects a relative rank test (extended entry points only):
+ * singular values above |rank_tol| * sum_i |dz_i| * ||Vhat||_F / sqrt(l), the
+ * size of the quadrature sums without cancellation -- with no eigenvalue
+ * inside the contour they are cancellation noise near 1e-16 of it, which the
+ * reference's absolute threshold cannot tell from a mode when omega ~ 1e15.
+ * The drop-ins above keep the absolute test (negative values act as 0). */
 beyn_result_t *qpms_gpu_scatsys_find_eigenmodes(const qpms_scatsys_t *ss, const double *k,
     qpms_complex_t omega_centre, double omega_rr, double omega_ri, size_t contour_npoints,
     double rank_tol, size_t rank_sel_min, double res_tol, size_t l, const qpms_complex_t *Vhat,

@@ -81,6 +81,8 @@ def beyn_solve(M_function, m, l, contour, Vhat, rank_tol=1e-4, rank_sel_min=1, r
     z, dz, z0 = contour
     Vhat = np.asarray(Vhat, dtype=np.complex128)
     assert Vhat.shape == (m, l) and l <= m
+    if rank_tol < 0:  # the library's relative rank test (the reference's is absolute)
+        rank_tol = -rank_tol * rank_scale(dz, Vhat)
     A0, A1, A0c, A1c = quadrature(M_function, contour, Vhat, 0, len(z))
     _, err, _, _, _ = _process_matrices(A0c, A1c, z0, rank_tol, rank_sel_min, res_tol, M_function, False)
     K, ev, vec, res, sigma = _process_matrices(A0, A1, z0, rank_tol, rank_sel_min, res_tol, M_function, True)
@@ -109,6 +111,37 @@ def quadrature(M_function, contour, Vhat, node_begin, node_end):
             A1c += X
             A1c += X
     return A0, A1, A0c, A1c
+
+
+def probe_matrix(m, l, seed):
+    """The library's seeded complex-Gaussian probe matrix (m x l, row-major):
+    splitmix64 draws u in (0, 1], Box-Muller sqrt(-2 log u1) cos(2 pi u2), the
+    real then the imaginary part of each entry.  The reference seeds random()
+    with the time instead (beyn.c:306-316), so its probe is not reproducible;
+    this restatement lets fixtures be regenerated from the seed alone."""
+    n = 4 * m * l
+    with np.errstate(over="ignore"):
+        st = np.uint64(seed) + np.arange(1, n + 1, dtype=np.uint64) * np.uint64(0x9e3779b97f4a7c15)
+        z = st
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xbf58476d1ce4e5b9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94d049bb133111eb)
+        z = z ^ (z >> np.uint64(31))
+    u = ((z >> np.uint64(11)) + np.uint64(1)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    u = u.reshape(-1, 4)
+    re = np.sqrt(-2 * np.log(u[:, 0])) * np.cos(2 * np.pi * u[:, 1])
+    im = np.sqrt(-2 * np.log(u[:, 2])) * np.cos(2 * np.pi * u[:, 3])
+    return (re + 1j * im).reshape(m, l)
+
+
+def rank_scale(dz, Vhat):
+    """Scale of the quadrature sums against which the library's relative rank
+    tolerance (rank_tol < 0) is taken: sum_i |dz_i| times the RMS column norm
+    ||Vhat||_F / sqrt(l), the size of A0 without cancellation when M^-1 is of
+    order one along the contour.  With no eigenvalue inside, A0 is
+    cancellation noise of about 1e-16 of it; each enclosed eigenvalue adds a
+    singular value of the order of its residue."""
+    Vhat = np.asarray(Vhat)
+    return float(np.sum(np.abs(dz)) * np.linalg.norm(Vhat) / np.sqrt(Vhat.shape[1]))
 
 
 def ellipse(centre, rRe, rIm, n):

@@ -63,6 +63,10 @@ def _declare(L):
     L.qpms_gpu_ozaki_residual.argtypes = [ci, ci, vp, sz, ci, vp, vp, vp]
     L.qpms_gpu_bf16_gemm.restype = ci
     L.qpms_gpu_bf16_gemm.argtypes = [ci, ci, ci, vp, vp, vp]
+    L.qpms_gpu_kernel_timing.restype = ci
+    L.qpms_gpu_kernel_timing.argtypes = [ci]
+    L.qpms_gpu_kernel_timing_get.restype = ci
+    L.qpms_gpu_kernel_timing_get.argtypes = [ci, vp, vp, vp]
     L.qpms_gpu_measure_fp64_peak.restype = ci
     L.qpms_gpu_measure_fp64_peak.argtypes = [vp]
     # complex by value is passed as two doubles (same registers on x86-64 and aarch64)
@@ -74,3 +78,22 @@ def _declare(L):
     beyn.declare(L)
     serving.declare(L)
     materials.declare(L)
+
+
+KERNEL_KINDS = ("tc_gemm", "assemble", "ewald", "batch_lu", "diag_lu", "trans", "split")
+
+
+def kernel_timing(enable):
+    """Start (True) or stop (False) live per-kind kernel timing; clears the sums."""
+    lib().qpms_gpu_kernel_timing(1 if enable else 0)
+
+
+def kernel_timing_get():
+    """{kind: (device ms, work, launches)} of the launches recorded since the last kernel_timing()."""
+    out = {}
+    for i, name in enumerate(KERNEL_KINDS):
+        ms, work, n = C.c_double(0), C.c_double(0), C.c_ulonglong(0)
+        lib().qpms_gpu_kernel_timing_get(i, C.byref(ms), C.byref(work), C.byref(n))
+        if n.value:
+            out[name] = (ms.value, work.value, n.value)
+    return out

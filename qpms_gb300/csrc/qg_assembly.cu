@@ -14,6 +14,7 @@
 #include <stdint.h>
 
 #include "qg_internal.h"
+#include "qg_ktimer.h"
 #include "qg_specfunc.cuh"
 #include "qg_assembly.h"
 
@@ -203,6 +204,8 @@ int launch_asm(const AsmArgs &a, const TransDevTables &T, cudaStream_t st) {
   const size_t units = (size_t)a.nw * a.np * a.np;
   const size_t nchunks = (units + Sh::V - 1) / Sh::V;
   if (nchunks == 0) return QPMS_SUCCESS;
+  const double nrow = (double)a.np * 2 * LMAX * (LMAX + 2);
+  KtScope kt(KT_ASSEMBLE, st, 16.0 * a.nw * nrow * nrow);
   if (a.dense) {
     auto k = assemble_kernel<LMAX, true>;
     const size_t smem = asm_smem_bytes<LMAX>(true);

@@ -1,6 +1,7 @@
 // Batched solve of many small mode-problem systems (the (omega, k) points of a
-// dispersion scan, serving batches of lattice solves): one cuBLAS batched LU
-// for all systems, then the right-hand sides.  The mixed mode factorises in
+// dispersion scan, serving batches of lattice solves): one batched LU launch
+// for all systems (qg_batchlu.cu, partial pivoting on the row-major matrices),
+// then the right-hand sides.  The mixed mode factorises in
 // complex64 and recovers FP64 accuracy by iterative refinement with an FP64
 // residual (residual_kernel, one warp per row), as qg_solve.cu does for the
 // finite plane-wave scatter.  The reference factorises each matrix with
@@ -11,6 +12,7 @@
 
 #include "qg_assembly.h"
 #include "qg_batched.h"
+#include "qg_batchlu.h"
 
 namespace qg {
 
@@ -32,8 +34,8 @@ __global__ void logabsdet_kernel(int nm, size_t N, const T *LU, double *out) {
 
 size_t batched_solve_bytes(int nm, size_t N, int mode) {
   const size_t m = (size_t)nm;
-  return al(m * N * N * (mode ? 8 : 16)) + al(m * N * 4) + al(m * 4) + 2 * al(m * 8) + al(m * N * 8) +
-         al(m * N * 16) + al(2 * m * 8);
+  return al(m * N * N * (mode ? 8 : 16)) + al(m * N * 4) + al(m * 4) + al(m * N * 8) + al(m * N * 16) +
+         al(2 * m * 8);
 }
 
 int batched_solve(cublasHandle_t h, cudaStream_t st, int nm, size_t N, const qg_c *dM, const qg_c *db, qg_c *dx,
@@ -48,52 +50,36 @@ int batched_solve(cublasHandle_t h, cudaStream_t st, int nm, size_t N, const qg_
   p += al(m * N * 4);
   int *info = (int *)p;
   p += al(m * 4);
-  void **arrA = (void **)p;
-  p += al(m * 8);
-  void **arrB = (void **)p;
-  p += al(m * 8);
   void *cb = p;
   p += al(m * N * 8);
   qg_c *r = (qg_c *)p;
   p += al(m * N * 16);
   double *rn2 = (double *)p, *bn2 = rn2 + m;
-  QG_BLAS_TRY(cublasSetStream(h, st));
-  {
-    std::vector<void *> pa(m), pb(m);
-    for (size_t i = 0; i < m; ++i) {
-      pa[i] = (char *)LU + i * N2 * (mode ? 8 : 16);
-      pb[i] = mode ? (void *)((char *)cb + i * N * 8) : (void *)(dx + i * N);
-    }
-    QG_CUDA_TRY(cudaMemcpyAsync(arrA, pa.data(), m * 8, cudaMemcpyHostToDevice, st));
-    QG_CUDA_TRY(cudaMemcpyAsync(arrB, pb.data(), m * 8, cudaMemcpyHostToDevice, st));
-    QG_CUDA_TRY(cudaStreamSynchronize(st));  // pa, pb are local
-  }
+  (void)h;
   std::vector<double> hr(m), hb(m);
   std::vector<int> its(m, 0);
-  int e, hinfo = 0;
-  // the row-major buffers read column-major are M^T: factorise M^T and solve with OP_T
+  int e;
+  if (N > (size_t)kBatchLuMaxN) {
+    set_error("batched solve: N = %zu above %d", N, kBatchLuMaxN);
+    return QPMS_EINVAL;
+  }
   if (mode == 0) {
     QG_CUDA_TRY(cudaMemcpyAsync(LU, dM, m * N2 * 16, cudaMemcpyDeviceToDevice, st));
     QG_CUDA_TRY(cudaMemcpyAsync(dx, db, m * N * 16, cudaMemcpyDeviceToDevice, st));
-    QG_BLAS_TRY(cublasZgetrfBatched(h, (int)N, (cuDoubleComplex **)arrA, (int)N, piv, info, nm));
-    QG_BLAS_TRY(cublasZgetrsBatched(h, CUBLAS_OP_T, (int)N, 1, (const cuDoubleComplex *const *)arrA, (int)N, piv,
-                                    (cuDoubleComplex **)arrB, (int)N, &hinfo, nm));
-    g_launches.fetch_add(2);
+    if ((e = batch_getrf_c128(nm, (int)N, LU, piv, info, st))) return e;
+    if ((e = batch_getrs_c128(nm, (int)N, LU, piv, dx, st))) return e;
     if ((e = launch_residual(nm, N, dM, dx, db, r, rn2, bn2, st))) return e;
     QG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, m * 8, cudaMemcpyDeviceToHost, st));
     QG_CUDA_TRY(cudaMemcpyAsync(hb.data(), bn2, m * 8, cudaMemcpyDeviceToHost, st));
     QG_CUDA_TRY(cudaStreamSynchronize(st));
   } else {
     if ((e = launch_c128_to_c64(m * N2, dM, LU, st))) return e;
-    QG_BLAS_TRY(cublasCgetrfBatched(h, (int)N, (cuComplex **)arrA, (int)N, piv, info, nm));
-    g_launches.fetch_add(1);
+    if ((e = batch_getrf_c64(nm, (int)N, LU, piv, info, st))) return e;
     QG_CUDA_TRY(cudaMemcpyAsync(r, db, m * N * 16, cudaMemcpyDeviceToDevice, st));
     double prev = 1e300;
     for (int it = 0; it <= max_iter; ++it) {
       if ((e = launch_c128_to_c64(m * N, r, cb, st))) return e;
-      QG_BLAS_TRY(cublasCgetrsBatched(h, CUBLAS_OP_T, (int)N, 1, (const cuComplex *const *)arrA, (int)N, piv,
-                                      (cuComplex **)arrB, (int)N, &hinfo, nm));
-      g_launches.fetch_add(1);
+      if ((e = batch_getrs_c64(nm, (int)N, LU, piv, cb, st))) return e;
       if ((e = launch_add_c64(m * N, cb, dx, it == 0, st))) return e;
       if ((e = launch_residual(nm, N, dM, dx, db, r, rn2, bn2, st))) return e;
       QG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, m * 8, cudaMemcpyDeviceToHost, st));

@@ -418,6 +418,18 @@ BeynResultPriv *beyn_postprocess(Residual *resid, size_t m, size_t l, cd z0, con
   return r;
 }
 
+// Scale of the quadrature sums for a relative rank tolerance: sum |dz_i| times
+// the RMS column norm of Vhat, the size A0 would have without cancellation
+// when M^-1 is of order one on the contour.  With no eigenvalue inside, A0 is
+// cancellation noise of about 1e-16 of it (the reference's absolute rank_tol
+// cannot tell this from a mode when the frequencies are of order 1e15).
+double rank_scale(const beyn_contour_t *contour, const std::vector<cd> &Vh, size_t l) {
+  double s = 0, f = 0;
+  for (size_t i = 0; i < contour->n; ++i) s += std::abs(to_cd(contour->z_dz[i][1]));
+  for (const cd &v : Vh) f += std::norm(v);
+  return s * sqrt(f / (double)l);
+}
+
 std::vector<cd> probe_or_given(size_t m, size_t l, const qpms_complex_t *Vhat, unsigned long long seed) {
   std::vector<cd> Vh(m * l);
   if (Vhat)
@@ -437,6 +449,7 @@ BeynResultPriv *beyn_core(MSource &src, beyn_function_M_inv_Vhat_t minv, void *m
   }
   if (refine_tol <= 0) refine_tol = kDefaultRefineTol;
   const std::vector<cd> Vh = probe_or_given(m, l, Vhat, seed);
+  if (rank_tol < 0) rank_tol = -rank_tol * rank_scale(contour, Vh, l);
   std::vector<cd> A0, A1, A0c, A1c;
   double max_res = 0;
   int max_it = 0;
@@ -587,6 +600,9 @@ beyn_result_t *beyn_solve(size_t m, size_t l, beyn_function_M_t M, beyn_function
                           void *params, const beyn_contour_t *contour, double rank_tol, size_t rank_sel_min,
                           double res_tol) {
   clear_error();
+  // the reference's rank test is absolute; negative values (the extended
+  // entry points' relative test) keep every singular value there
+  if (rank_tol < 0) rank_tol = 0;
   if (!M_inv_Vhat)
     return qpms_gpu_beyn_solve(m, l, M, params, contour, rank_tol, rank_sel_min, res_tol, nullptr, kDefaultSeed, 1,
                                kDefaultRefineTol);
@@ -624,7 +640,8 @@ beyn_result_t *qpms_scatsys_finite_find_eigenmodes(const qpms_scatsys_t *ss, qpm
                                                    double res_tol) {
   clear_error();
   // iri: QPMS_NO_IRREP for the full system, else M projected on the irrep
-  // (eigenvectors in the packed basis)
+  // (eigenvectors in the packed basis); absolute rank test as the reference's
+  if (rank_tol < 0) rank_tol = 0;
   BeynResultPriv *r = scatsys_beyn(ss, nullptr, omega_centre, omega_rr, omega_ri, contour_npoints, rank_tol,
                                    rank_sel_min, res_tol, 0, nullptr, kDefaultSeed, 1, kDefaultRefineTol,
                                    iri == QPMS_NO_IRREP ? -1 : iri);
@@ -657,6 +674,7 @@ beyn_result_t *qpms_scatsys_periodic_find_eigenmodes(const qpms_scatsys_t *ss, c
     set_error("NULL Bloch vector");
     return nullptr;
   }
+  if (rank_tol < 0) rank_tol = 0;  // absolute rank test as the reference's
   BeynResultPriv *r = scatsys_beyn(ss, k, omega_centre, omega_rr, omega_ri, contour_npoints, rank_tol, rank_sel_min,
                                    res_tol, 0, nullptr, kDefaultSeed, 1, kDefaultRefineTol);
   return r ? &r->pub : nullptr;

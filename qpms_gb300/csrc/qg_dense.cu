@@ -34,6 +34,8 @@
 
 #include "qg_dense.h"
 #include "qg_internal.h"
+#include "qg_ktimer.h"
+#include "qg_tcgemm.h"
 
 namespace qg {
 int blas_handle_get(cublasHandle_t *h);
@@ -397,6 +399,167 @@ int lu_solve(cublasHandle_t h, int N, int nb, const T *A, size_t lda, const T *D
   return QPMS_SUCCESS;
 }
 
+// ---------------- complex64 LU and substitutions on the tensor cores ----------------
+// The same blocked algorithm as lu_nopiv / lu_solve with every product a
+// tcgen05 GEMM of split-bf16 digits (qg_tcgemm.cu): operands are cut into
+// digit planes first, so each GEMM may write its result over an operand it
+// read (the panels L21 = A21 U^-1, U12 = L^-1 A12 and the right-hand-side
+// blocks are formed in place).
+int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, int nsplit, __nv_bfloat16 *pa,
+                __nv_bfloat16 *pb, cudaStream_t st) {
+  const size_t smem = diag_smem<float2>(nb);
+  QG_CUDA_TRY(
+      cudaFuncSetAttribute(diag_lu_inv_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  TcPlanes P;
+  P.a = pa;
+  P.b = pb;
+  P.nsplit = nsplit;
+  int e;
+  for (int k = 0, blk = 0; k < N; k += nb, ++blk) {
+    const int kb = (N - k < nb) ? N - k : nb;
+    float2 *Lk = Dinv + (size_t)blk * 2 * nb * nb, *Uk = Lk + (size_t)nb * nb;
+    {
+      KtScope kt(KT_DIAGLU, st, 8.0 * kb * (double)kb * kb / 3.0);
+      diag_lu_inv_kernel<float2><<<1, 1024, diag_smem<float2>(kb), st>>>(A + (size_t)k * lda + k, lda, kb, Lk,
+                                                                         Uk, dinfo);
+    }
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+    const int m2 = N - k - kb;
+    if (m2 <= 0) break;
+    float2 *A21 = A + (size_t)k * lda + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = A21 + (size_t)kb * lda;
+    // L21 = A21 U^-1
+    if ((e = tc_split_a(A21, lda, m2, kb, nsplit, pa, st)) || (e = tc_split_b(Uk, kb, kb, kb, nsplit, pb, st)))
+      return e;
+    P.m = m2, P.n = kb, P.k = kb;
+    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, A21, lda, st))) return e;
+    // U12 = L^-1 A12
+    if ((e = tc_split_a(Lk, kb, kb, kb, nsplit, pa, st)) || (e = tc_split_b(A12, lda, kb, m2, nsplit, pb, st)))
+      return e;
+    P.m = kb, P.n = m2, P.k = kb;
+    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, A12, lda, st))) return e;
+    // A22 -= L21 U12
+    if ((e = tc_split_a(A21, lda, m2, kb, nsplit, pa, st)) || (e = tc_split_b(A12, lda, kb, m2, nsplit, pb, st)))
+      return e;
+    P.m = m2, P.n = m2, P.k = kb;
+    if ((e = tc_cgemm_planes(P, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
+  }
+  return QPMS_SUCCESS;
+}
+
+// (L U) X = B in place, B: N x nrhs (ldb), products on the tensor cores.
+int lu_solve_tc(int N, int nb, const float2 *A, size_t lda, const float2 *Dinv, float2 *B, size_t ldb, int nrhs,
+                int nsplit, __nv_bfloat16 *pa, __nv_bfloat16 *pb, cudaStream_t st) {
+  TcPlanes P;
+  P.a = pa;
+  P.b = pb;
+  P.nsplit = nsplit;
+  int e;
+  const int nblk = (N + nb - 1) / nb;
+  for (int blk = 0; blk < nblk; ++blk) {  // forward: L y = b
+    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
+    const float2 *Lk = Dinv + (size_t)blk * 2 * nb * nb;
+    if ((e = tc_split_a(Lk, kb, kb, kb, nsplit, pa, st)) || (e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st)))
+      return e;
+    P.m = kb, P.n = nrhs, P.k = kb;
+    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, B + k, ldb, st))) return e;
+    const int m2 = N - k - kb;
+    if (m2 <= 0) continue;
+    if ((e = tc_split_a(A + (size_t)k * lda + k + kb, lda, m2, kb, nsplit, pa, st)) ||
+        (e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st)))
+      return e;
+    P.m = m2, P.n = nrhs, P.k = kb;
+    if ((e = tc_cgemm_planes(P, -1.f, 1.f, B + k + kb, ldb, B + k + kb, ldb, st))) return e;
+  }
+  for (int blk = nblk - 1; blk >= 0; --blk) {  // backward: U x = y
+    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
+    const float2 *Uk = Dinv + (size_t)blk * 2 * nb * nb + (size_t)nb * nb;
+    if ((e = tc_split_a(Uk, kb, kb, kb, nsplit, pa, st)) || (e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st)))
+      return e;
+    P.m = kb, P.n = nrhs, P.k = kb;
+    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, B + k, ldb, st))) return e;
+    if (k == 0) continue;
+    if ((e = tc_split_a(A + (size_t)k * lda, lda, k, kb, nsplit, pa, st)) ||
+        (e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st)))
+      return e;
+    P.m = k, P.n = nrhs, P.k = kb;
+    if ((e = tc_cgemm_planes(P, -1.f, 1.f, B, ldb, B, ldb, st))) return e;
+  }
+  return QPMS_SUCCESS;
+}
+
+// ---------------- substitutions for a few right-hand sides (bandwidth-bound) ----------------
+constexpr int kSmallRhs = 8;
+
+// Bk (kb x nrhs, ldb) <- Tri (kb x kb, leading dimension kb) Bk; one CTA.
+template <typename T>
+__global__ void __launch_bounds__(256) blk_apply_kernel(const T *__restrict__ Tri, int kb, T *Bk, size_t ldb,
+                                                        int nrhs) {
+  __shared__ T sB[128 * kSmallRhs];
+  for (int t = threadIdx.x; t < kb * nrhs; t += blockDim.x) {
+    const int c = t / kb, r = t - c * kb;
+    sB[c * kb + r] = Bk[(size_t)c * ldb + r];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kb * nrhs; t += blockDim.x) {
+    const int c = t / kb, r = t - c * kb;
+    T acc = mk<T>(0, 0);
+    for (int l = 0; l < kb; ++l) acc = fma_c(acc, Tri[(size_t)l * kb + r], sB[c * kb + l]);
+    Bk[(size_t)c * ldb + r] = acc;
+  }
+}
+
+// Bdst (m2 x nrhs) -= Pn (m2 x kb, leading dimension lda) Bk (kb x nrhs); a
+// thread per row, the panel read once and coalesced.
+template <typename T>
+__global__ void __launch_bounds__(256) panel_sub_kernel(const T *__restrict__ Pn, size_t lda, int m2, int kb,
+                                                        const T *Bk, size_t ldb, T *Bdst, int nrhs) {
+  __shared__ T sB[128 * kSmallRhs];
+  for (int t = threadIdx.x; t < kb * nrhs; t += blockDim.x) {
+    const int c = t / kb, r = t - c * kb;
+    sB[c * kb + r] = Bk[(size_t)c * ldb + r];
+  }
+  __syncthreads();
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m2) return;
+  T acc[kSmallRhs];
+#pragma unroll
+  for (int c = 0; c < kSmallRhs; ++c) acc[c] = mk<T>(0, 0);
+  for (int l = 0; l < kb; ++l) {
+    const T p = Pn[(size_t)l * lda + r];
+#pragma unroll
+    for (int c = 0; c < kSmallRhs; ++c)
+      if (c < nrhs) acc[c] = fma_c(acc[c], p, sB[c * kb + l]);
+  }
+#pragma unroll
+  for (int c = 0; c < kSmallRhs; ++c)
+    if (c < nrhs) Bdst[(size_t)c * ldb + r] = sub(Bdst[(size_t)c * ldb + r], acc[c]);
+}
+
+template <typename T>
+int lu_solve_small(int N, int nb, const T *A, size_t lda, const T *Dinv, T *B, size_t ldb, int nrhs, cudaStream_t st) {
+  const int nblk = (N + nb - 1) / nb;
+  for (int blk = 0; blk < nblk; ++blk) {
+    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
+    blk_apply_kernel<T><<<1, 256, 0, st>>>(Dinv + (size_t)blk * 2 * nb * nb, kb, B + k, ldb, nrhs);
+    const int m2 = N - k - kb;
+    if (m2 > 0)
+      panel_sub_kernel<T><<<(m2 + 255) / 256, 256, 0, st>>>(A + (size_t)k * lda + k + kb, lda, m2, kb, B + k, ldb,
+                                                            B + k + kb, nrhs);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(m2 > 0 ? 2 : 1);
+  }
+  for (int blk = nblk - 1; blk >= 0; --blk) {
+    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
+    blk_apply_kernel<T><<<1, 256, 0, st>>>(Dinv + (size_t)blk * 2 * nb * nb + (size_t)nb * nb, kb, B + k, ldb, nrhs);
+    if (k > 0)
+      panel_sub_kernel<T><<<(k + 255) / 256, 256, 0, st>>>(A + (size_t)k * lda, lda, k, kb, B + k, ldb, B, nrhs);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(k > 0 ? 2 : 1);
+  }
+  return QPMS_SUCCESS;
+}
+
 }  // namespace
 
 // ---------------- solver object ----------------
@@ -438,6 +601,21 @@ cublasComputeType_t trailing_compute(int nrhs_max) {
   if (ev && !strcmp(ev, "BF16X9")) return CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
   return nrhs_max <= 4 ? CUBLAS_COMPUTE_32F_FAST_TF32 : CUBLAS_COMPUTE_32F;
 }
+// bf16 digits per operand of the tensor-core LU (0: the cuBLAS path chosen by
+// QPMS_GB300_LU_COMPUTE).  Two digits (three digit products, ~1e-5 relative
+// product error) by default; a refinement that stalls refactors with three
+// digits (six products, FP32-like), then in complex128.
+int tc_digits(int nrhs_max) {
+  (void)nrhs_max;
+  const char *ev = getenv("QPMS_GB300_LU_COMPUTE");
+  if (ev && !strcmp(ev, "TC3")) return 3;
+  if (ev && !strcmp(ev, "TC2")) return 2;
+  if (ev && (!strcmp(ev, "32F") || !strcmp(ev, "TF32") || !strcmp(ev, "BF16X9"))) return 0;
+  return 2;
+}
+size_t tc_plane_bytes(int Np, int nrhs_max, int nb) {
+  return tc_planes_bytes_a(Np, nb, 3) + tc_planes_bytes_b(std::max(Np, nrhs_max), nb, 3) + 512;
+}
 }  // namespace
 
 int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed, cudaMemPool_t pool_,
@@ -454,9 +632,11 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   nrhs_max = nrhs_max_;
   mode = mode_;
   trail_ct = (int)trailing_compute(nrhs_max);
+  tc_split = mode ? tc_digits(nrhs_max) : 0;
   refactors = 0;
   base_mode = mode;
   base_trail = trail_ct;
+  base_tc = tc_split;
   nb = mode ? 128 : 64;
   const size_t esz = mode ? 8 : 16;
   const size_t NN = (size_t)Np * Np;
@@ -472,6 +652,10 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   QG_CUDA_TRY(dev_alloc(&y64, (size_t)N * nrhs_max * 16));
   QG_CUDA_TRY(dev_alloc(&dinfo, 16));
   QG_CUDA_TRY(dev_alloc(&rs, (size_t)4 * Np * sizeof(double)));
+  if (tc_split) {
+    QG_CUDA_TRY(dev_alloc(&tc_pa, tc_planes_bytes_a(Np, nb, 3)));
+    QG_CUDA_TRY(dev_alloc(&tc_pb, tc_planes_bytes_b(std::max(Np, nrhs_max), nb, 3)));
+  }
   use_ozaki = ozaki_wanted(nrhs_max);
   if (use_ozaki && (dev_alloc(&oz_mat, ozaki_matrix_bytes(N)) != cudaSuccess ||
                     dev_alloc(&oz_work, ozaki_work_bytes(N, nrhs_max)) != cudaSuccess)) {
@@ -503,6 +687,7 @@ size_t DenseSolver::footprint(int N, int nrhs, int mode) {
   b += std::max<size_t>(Np * nb, nb * std::max<size_t>(Np, nrhs)) * esz;
   b += Np * nrhs * (8 + 16) + (size_t)N * nrhs * 32 + 16 + 4 * Np * 8;
   if (ozaki_wanted(nrhs)) b += ozaki_matrix_bytes(N) + ozaki_work_bytes(N, nrhs);
+  if (mode && tc_digits(nrhs)) b += tc_plane_bytes((int)Np, nrhs, (int)nb);
   return b + 12 * 512;  // allocation rounding
 }
 
@@ -519,7 +704,7 @@ cudaError_t DenseSolver::dev_alloc(void *ptr, size_t bytes) {
 
 void DenseSolver::release() {
   for (void *p : {(void *)A, (void *)T64, (void *)Dinv, (void *)work, (void *)rhs_lo, (void *)rp, (void *)r64,
-                  (void *)y64, (void *)dinfo, (void *)rs, oz_mat, oz_work})
+                  (void *)y64, (void *)dinfo, (void *)rs, oz_mat, oz_work, tc_pa, tc_pb})
     if (p) {
       if (pool)
         cudaFreeAsync(p, ast);
@@ -531,6 +716,7 @@ void DenseSolver::release() {
   dinfo = nullptr;
   rs = nullptr;
   oz_mat = oz_work = nullptr;
+  tc_pa = tc_pb = nullptr;
   use_ozaki = false;
 }
 
@@ -558,6 +744,7 @@ int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st, bool ro
   row_major = rowmaj;
   mode = base_mode;
   trail_ct = base_trail;
+  tc_split = base_tc;
   nb = mode ? 128 : 64;
   if (use_ozaki) {
     int e;
@@ -598,8 +785,12 @@ int DenseSolver::factorize_current(const void *M64, size_t ldm, cudaStream_t st)
     d2f_kernel<<<grid1(NN), 256, 0, st>>>(NN, (const double2 *)T64, (float2 *)A);
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
-    e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
-                         (cublasComputeType_t)trail_ct, st);
+    if (tc_split)
+      e = lu_nopiv_tc(Np, nb, (float2 *)A, Np, (float2 *)Dinv, dinfo, tc_split, (__nv_bfloat16 *)tc_pa,
+                      (__nv_bfloat16 *)tc_pb, st);
+    else
+      e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
+                           (cublasComputeType_t)trail_ct, st);
   } else {
     e = lu_nopiv<double2>(h, Np, nb, (double2 *)T64, Np, (double2 *)Dinv, (double2 *)work, dinfo,
                           CUBLAS_COMPUTE_64F, st);
@@ -630,16 +821,26 @@ int DenseSolver::apply_inverse(const void *R, size_t ldr, void *Y, size_t ldy, i
     d2f_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)rp, (float2 *)rhs_lo);
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
-    if ((e = lu_solve<float2>(h, Np, nb, (const float2 *)A, Np, (const float2 *)Dinv, (float2 *)rhs_lo, Np, nrhs,
-                              (float2 *)work, CUBLAS_COMPUTE_32F, st)))
-      return e;
+    if (nrhs <= kSmallRhs)
+      e = lu_solve_small<float2>(Np, nb, (const float2 *)A, Np, (const float2 *)Dinv, (float2 *)rhs_lo, Np, nrhs, st);
+    else if (tc_split)
+      e = lu_solve_tc(Np, nb, (const float2 *)A, Np, (const float2 *)Dinv, (float2 *)rhs_lo, Np, nrhs, 3,
+                      (__nv_bfloat16 *)tc_pa, (__nv_bfloat16 *)tc_pb, st);
+    else
+      e = lu_solve<float2>(h, Np, nb, (const float2 *)A, Np, (const float2 *)Dinv, (float2 *)rhs_lo, Np, nrhs,
+                           (float2 *)work, CUBLAS_COMPUTE_32F, st);
+    if (e) return e;
     f2d_add_kernel<<<grid1(n), 256, 0, st>>>(n, (const float2 *)rhs_lo, (double2 *)rp, 1);
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
   } else {
-    if ((e = lu_solve<double2>(h, Np, nb, (const double2 *)T64, Np, (const double2 *)Dinv, (double2 *)rp, Np, nrhs,
-                               (double2 *)work, CUBLAS_COMPUTE_64F, st)))
-      return e;
+    if (nrhs <= kSmallRhs)
+      e = lu_solve_small<double2>(Np, nb, (const double2 *)T64, Np, (const double2 *)Dinv, (double2 *)rp, Np, nrhs,
+                                  st);
+    else
+      e = lu_solve<double2>(h, Np, nb, (const double2 *)T64, Np, (const double2 *)Dinv, (double2 *)rp, Np, nrhs,
+                            (double2 *)work, CUBLAS_COMPUTE_64F, st);
+    if (e) return e;
   }
   if ((e = rbt_right_solution(*this, (double2 *)rp, Np, nrhs, st))) return e;
   QG_CUDA_TRY(cudaMemcpy2DAsync(Y, ldy * 16, rp, (size_t)Np * 16, (size_t)N * 16, nrhs, cudaMemcpyDeviceToDevice,
@@ -701,7 +902,9 @@ int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int 
         // cond x the factors' error): TF32 -> FP32 -> FP64 factors, continue from x.
         // mode 0 reuses the same buffers: T64 is factored in place, Dinv and
         // work hold 2 x (64 x 64 x 16 B) per 64 rows as 2 x (128 x 128 x 8 B) per 128
-        if (trail_ct != (int)CUBLAS_COMPUTE_32F) {
+        if (tc_split == 2) {
+          tc_split = 3;
+        } else if (!tc_split && trail_ct != (int)CUBLAS_COMPUTE_32F) {
           trail_ct = (int)CUBLAS_COMPUTE_32F;
         } else {
           mode = 0;

@@ -34,7 +34,10 @@ struct DenseSolver {
   cudaMemPool_t pool = nullptr;
   cudaStream_t ast = nullptr;
   bool row_major = false;  // set by factorize(): M64 is row-major (the reference's layout)
-  int trail_ct = 0;        // cublasComputeType_t of the complex64 trailing updates (mode 1)
+  int trail_ct = 0;        // cublasComputeType_t of the complex64 trailing updates (mode 1, tc_split 0)
+  int tc_split = 0;        // mode 1 on the tensor cores: bf16 digits per operand (2 or 3); 0: cuBLAS
+  int base_tc = 0;
+  void *tc_pa = nullptr, *tc_pb = nullptr;  // digit planes of the GEMM operands
   int refactors = 0;       // refinement stalls answered by more precise factors
   int base_mode = 0, base_trail = 0;  // what factorize() starts from (the fallbacks change mode / trail_ct)
   // digit slices of M for the tensor-core residual (nrhs_max >= kOzakiMinRhs)

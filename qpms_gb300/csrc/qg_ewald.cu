@@ -65,6 +65,7 @@
 #include "qg_ewald.h"
 #include "qg_faddeeva.cuh"
 #include "qg_internal.h"
+#include "qg_ktimer.h"
 
 namespace qg {
 
@@ -1078,6 +1079,8 @@ int launch_ew(const EwaldArgs &a, const TransDevTables &T, cudaStream_t st) {
   QG_CUDA_TRY(cudaGetDevice(&dev));
   QG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   size_t grid = std::min<size_t>(units, (size_t)nsm * 16);
+  const double nblk = 2.0 * LMAX * (LMAX + 2);
+  KtScope kt(KT_EWALD, st, 16.0 * nblk * nblk * (double)units);
   if (a.srtab) {
     const size_t tunits = (size_t)a.nw * a.np * a.np;
     ewald_sr_table_kernel<LMAX><<<(unsigned)std::min<size_t>(tunits, (size_t)nsm * 16), kEThreads, 0, st>>>(a);

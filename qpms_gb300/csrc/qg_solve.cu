@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "qg_assembly.h"
+#include "qg_batchlu.h"
 #include "qg_dense.h"
 #include "qg_internal.h"
 
@@ -260,7 +261,23 @@ static qpms_ss_LU factorise_any(qpms_complex_t *mpmatrix_full, int *target_piv, 
       dalloc(dI, 4))
     return fail();
   if (cudaMemcpy(dA.p, mpmatrix_full, N * N * 16, cudaMemcpyHostToDevice) != cudaSuccess) return fail();
-  // row-major M -> column-major M, factorise (zgetrf), back to row-major storage
+  if (N <= (size_t)kBatchLuMaxN) {
+    // the library's batched LU on the row-major matrix; LAPACK's 1-based pivots
+    std::vector<int> p0(N);
+    if (batch_getrf_c128(1, (int)N, dA.p, dP.as<int>(), dI.as<int>(), 0) ||
+        cudaMemcpy(mpmatrix_full, dA.p, N * N * 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(p0.data(), dP.p, N * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(&info, dI.p, 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      if (!qpms_gpu_last_error()[0]) set_error("batched LU or device to host copy failed");
+      return fail();
+    }
+    for (size_t i = 0; i < N; ++i) target_piv[i] = p0[i] + 1;
+    if (info != 0) set_error("LU: U(%d,%d) is exactly zero", info, info);
+    lu.a = mpmatrix_full;
+    lu.ipiv = target_piv;
+    return lu;
+  }
+  // larger orders: row-major M -> column-major M, cuBLAS zgetrf, back to row-major storage
   if (launch_transpose(N, 1, dA.as<qg_c>(), dT.as<qg_c>(), 0)) return fail();
   if (ptr_array(arr, dT.p, 0, 1)) return fail();
   if (cublasZgetrfBatched(h, (int)N, arr.as<cuDoubleComplex *>(), (int)N, dP.as<int>(), dI.as<int>(), 1) !=
@@ -309,10 +326,23 @@ qpms_complex_t *qpms_scatsys_scatter_solve(qpms_complex_t *f, const qpms_complex
     set_error("host to device copy failed");
     return nullptr;
   }
-  if (launch_transpose(N, 1, dA.as<qg_c>(), dT.as<qg_c>(), 0)) return nullptr;
-  if (ptr_array(arrA, dT.p, 0, 1) || ptr_array(arrB, dB.p, 0, 1)) return nullptr;
   int info = 0;
-  if (cublasZgetrsBatched(h, CUBLAS_OP_N, (int)N, 1, arrA.as<const cuDoubleComplex *>(), (int)N, dP.as<int>(),
+  if (N <= (size_t)kBatchLuMaxN) {  // LAPACK's 1-based pivots -> the batched kernel's 0-based
+    std::vector<int> p0(N);
+    for (size_t i = 0; i < N; ++i) {
+      p0[i] = lu.ipiv[i] - 1;
+      if (p0[i] < 0 || p0[i] >= (int)N) {
+        set_error("LU: pivot %d of row %zu outside 1..%zu", lu.ipiv[i], i + 1, N);
+        return nullptr;
+      }
+    }
+    if (cudaMemcpy(dP.p, p0.data(), N * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        batch_getrs_c128(1, (int)N, dA.p, dP.as<int>(), dB.p, 0))
+      return nullptr;
+  } else if (launch_transpose(N, 1, dA.as<qg_c>(), dT.as<qg_c>(), 0) || ptr_array(arrA, dT.p, 0, 1) ||
+             ptr_array(arrB, dB.p, 0, 1)) {
+    return nullptr;
+  } else if (cublasZgetrsBatched(h, CUBLAS_OP_N, (int)N, 1, arrA.as<const cuDoubleComplex *>(), (int)N, dP.as<int>(),
                           arrB.as<cuDoubleComplex *>(), (int)N, &info, 1) != CUBLAS_STATUS_SUCCESS ||
       info != 0) {
     set_error("cublasZgetrsBatched failed (info %d)", info);
@@ -443,7 +473,7 @@ int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw, c
   int e;
   if ((e = blas_handle_get(&h))) return e;
   QG_BLAS_TRY(cublasSetStream(h, st));
-  Dev dM, dLU, dpiv, dinfo, dT, dtm, dpos, dk, dkv, dcoef, da, db, dx, dr, dn, dsig, dcb, arrA, arrB;
+  Dev dM, dLU, dpiv, dinfo, dT, dtm, dpos, dk, dkv, dcoef, da, db, dx, dr, dn, dsig, dcb;
   if ((e = dalloc(dM, N2 * W * 16)) || (e = dalloc(dLU, N2 * W * (mode ? 8 : 16))) ||
       (e = dalloc(dpiv, N * W * 4)) || (e = dalloc(dinfo, W * 4)) || (e = dalloc(dT, T.size() * 16)) ||
       (e = dalloc(dtm, np * 4)) || (e = dalloc(dpos, np * 24)) || (e = dalloc(dk, W * 16)) ||
@@ -492,31 +522,22 @@ int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw, c
   if (mode == 0) {
     QG_CUDA_TRY(cudaMemcpyAsync(dLU.p, dM.p, N2 * W * 16, cudaMemcpyDeviceToDevice, st));
     QG_CUDA_TRY(cudaMemcpyAsync(dx.p, db.p, N * W * 16, cudaMemcpyDeviceToDevice, st));
-    if ((e = ptr_array(arrA, dLU.p, N2 * 16, W)) || (e = ptr_array(arrB, dx.p, N * 16, W))) return e;
-    // the row-major buffer is M^T in column-major order: factorise M^T, solve with OP_T
-    QG_BLAS_TRY(cublasZgetrfBatched(h, (int)N, arrA.as<cuDoubleComplex *>(), (int)N, dpiv.as<int>(),
-                                    dinfo.as<int>(), W));
-    QG_BLAS_TRY(cublasZgetrsBatched(h, CUBLAS_OP_T, (int)N, 1, arrA.as<const cuDoubleComplex *>(), (int)N,
-                                    dpiv.as<int>(), arrB.as<cuDoubleComplex *>(), (int)N, &info, W));
-    g_launches.fetch_add(2);
+    if ((e = batch_getrf_c128(W, (int)N, dLU.p, dpiv.as<int>(), dinfo.as<int>(), st))) return e;
+    if ((e = batch_getrs_c128(W, (int)N, dLU.p, dpiv.as<int>(), dx.p, st))) return e;
     if ((e = launch_residual(W, N, dM.as<qg_c>(), dx.as<qg_c>(), db.as<qg_c>(), dr.as<qg_c>(), rn2, bn2, st)))
       return e;
     QG_CUDA_TRY(cudaMemcpy(hr.data(), rn2, W * 8, cudaMemcpyDeviceToHost));
     QG_CUDA_TRY(cudaMemcpy(hb.data(), bn2, W * 8, cudaMemcpyDeviceToHost));
   } else {
     if ((e = launch_c128_to_c64(N2 * W, dM.as<qg_c>(), dLU.p, st))) return e;
-    if ((e = ptr_array(arrA, dLU.p, N2 * 8, W)) || (e = ptr_array(arrB, dcb.p, N * 8, W))) return e;
-    QG_BLAS_TRY(cublasCgetrfBatched(h, (int)N, arrA.as<cuComplex *>(), (int)N, dpiv.as<int>(), dinfo.as<int>(), W));
-    g_launches.fetch_add(1);
+    if ((e = batch_getrf_c64(W, (int)N, dLU.p, dpiv.as<int>(), dinfo.as<int>(), st))) return e;
     // x0 = LU32^{-1} b, then refine: r = b - M x (FP64), x += LU32^{-1} r
     QG_CUDA_TRY(cudaMemcpyAsync(dr.p, db.p, N * W * 16, cudaMemcpyDeviceToDevice, st));
     const int kMaxIter = 12;
     double prev = 1e300;
     for (int it = 0; it <= kMaxIter; ++it) {
       if ((e = launch_c128_to_c64(N * W, dr.as<qg_c>(), dcb.p, st))) return e;
-      QG_BLAS_TRY(cublasCgetrsBatched(h, CUBLAS_OP_T, (int)N, 1, arrA.as<const cuComplex *>(), (int)N,
-                                      dpiv.as<int>(), arrB.as<cuComplex *>(), (int)N, &info, W));
-      g_launches.fetch_add(1);
+      if ((e = batch_getrs_c64(W, (int)N, dLU.p, dpiv.as<int>(), dcb.p, st))) return e;
       if ((e = launch_add_c64(N * W, dcb.p, dx.as<qg_c>(), it == 0, st))) return e;
       if ((e = launch_residual(W, N, dM.as<qg_c>(), dx.as<qg_c>(), db.as<qg_c>(), dr.as<qg_c>(), rn2, bn2, st)))
         return e;

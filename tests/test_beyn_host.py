@@ -43,6 +43,15 @@ def test_probe_matrix_seeded_gaussian():
     assert abs(x.mean()) < 0.01 and abs(x.std() - 1) < 0.01
 
 
+def test_probe_matrix_matches_oracle_restatement():
+    from oracle import beyn as ob
+    from qpms_gb300 import beyn
+    for m, l, seed in ((37, 5, 12345), (300, 64, beyn.DEFAULT_SEED)):
+        a = beyn.probe_matrix(m, l, seed)
+        o = ob.probe_matrix(m, l, seed)
+        assert np.abs(a - o).max() <= 1e-14 * np.abs(o).max()
+
+
 @pytest.mark.parametrize("m,n,deficient", [(40, 10, False), (300, 64, True), (64, 64, False), (1000, 30, True)])
 def test_host_svd(m, n, deficient):
     from qpms_gb300 import beyn
