@@ -37,6 +37,7 @@ typedef int qpms_bessel_t;            /* enum, qpms_types.h:176-182: 1 j, 2 y, 3
 #define QPMS_ERROR 1
 #define QPMS_ENOMEM 12
 #define QPMS_EINVAL 22
+#define QPMS_ECANCELED 125
 #define QPMS_NAN_ENCOUNTERED 1024  /* qpms_types.h:91 */
 #define QPMS_NORMALISATION_INVERSE 1
 #define QPMS_NORMALISATION_REVERSE_AZIMUTHAL_PHASE 2
@@ -865,9 +866,11 @@ typedef struct qpms_gpu_request_t {
 } qpms_gpu_request_t;
 
 typedef struct qpms_gpu_result_t {
-  int status;                    /* 0 = solved */
+  int status;                    /* 0 = solved; QPMS_ECANCELED if cancelled before it started */
   int iters;                     /* refinement steps (mixed mode) */
   int batch_size;                /* requests solved together with this one */
+  int fallback;                  /* 1: the mixed-precision refinement stalled and the system was solved
+                                    again with more precise factors (complex128 at the end) */
   double sigma_ext;              /* extinction cross-section (per unit cell if periodic) */
   double residual;               /* FP64 relative residual |b - M x| / |b| */
   double t_submit, t_start, t_done;   /* seconds on the server clock */
@@ -886,8 +889,20 @@ int qpms_gpu_server_submit(qpms_gpu_server_t *s, const qpms_gpu_request_t *req, 
     uint64_t *ticket);
 /* Block until the request is solved; returns its status. */
 int qpms_gpu_server_wait(qpms_gpu_server_t *s, uint64_t ticket, qpms_gpu_result_t *out);
+/* Withdraw a request that has not started: it completes with status
+ * QPMS_ECANCELED (its ticket must still be waited for).  Returns 0, or
+ * QPMS_EINVAL if the ticket is unknown or the request has already started. */
+int qpms_gpu_server_cancel(qpms_gpu_server_t *s, uint64_t ticket);
 /* Block until nothing is queued or running. */
 int qpms_gpu_server_drain(qpms_gpu_server_t *s);
+/* Test hook: the next `count` device-pool allocations of the server's
+ * workers fail as if the pool were exhausted (the affected request completes
+ * with QPMS_ENOMEM; the server keeps serving).  No counterpart in the reference. */
+int qpms_gpu_server_testing_fail_allocations(qpms_gpu_server_t *s, int count);
+/* Test hook: caps the FP64 refinement steps of the mixed-precision solves
+ * (batched and dense) at max_steps (-1 restores the default), so that tests
+ * can force the precision fallback.  No counterpart in the reference. */
+int qpms_gpu_testing_set_max_refine(int max_steps);
 double qpms_gpu_server_clock(qpms_gpu_server_t *s);
 int qpms_gpu_server_stats(qpms_gpu_server_t *s, size_t *completed, size_t *batches, size_t *peak_bytes,
     int *max_concurrent, size_t *budget_bytes);

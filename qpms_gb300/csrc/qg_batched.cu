@@ -8,6 +8,7 @@
 // LAPACKE_zgetrf and solves with zgetrs (scatsystem.c:2202-2273).
 #include <math.h>
 
+#include <atomic>
 #include <vector>
 
 #include "qg_assembly.h"
@@ -38,10 +39,47 @@ size_t batched_solve_bytes(int nm, size_t N, int mode) {
          al(2 * m * 8);
 }
 
+namespace {
+std::atomic<int> g_max_refine{-1};
+}  // namespace
+
+int max_refine_steps(int dflt) {
+  const int v = g_max_refine.load();
+  return v >= 0 ? v : dflt;
+}
+
+// Re-solve the systems listed in idx (of a contiguous batch) with complex128
+// LU and partial pivoting: the fallback of a stalled complex64 refinement.
+int resolve_fp64(cudaStream_t st, const std::vector<int> &idx, size_t N, const qg_c *dM, const qg_c *db, qg_c *dx) {
+  if (idx.empty()) return QPMS_SUCCESS;
+  const size_t nb = idx.size(), N2 = N * N;
+  void *LU = nullptr, *piv = nullptr;
+  QG_CUDA_TRY(cudaMallocAsync(&LU, nb * N2 * 16, st));
+  QG_CUDA_TRY(cudaMallocAsync(&piv, nb * N * 4, st));
+  int e = QPMS_SUCCESS;
+  for (size_t i = 0; i < nb && !e; ++i) {
+    if (cudaMemcpyAsync((char *)LU + i * N2 * 16, dM + (size_t)idx[i] * N2, N2 * 16, cudaMemcpyDeviceToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(dx + (size_t)idx[i] * N, db + (size_t)idx[i] * N, N * 16, cudaMemcpyDeviceToDevice, st) !=
+            cudaSuccess) {
+      set_error("batched solve: fallback copy failed");
+      e = QPMS_ERROR;
+    }
+  }
+  if (!e) e = batch_getrf_c128((int)nb, (int)N, LU, (int *)piv, nullptr, st);
+  // the right-hand sides were copied into dx in place; solve them where they lie
+  for (size_t i = 0; i < nb && !e; ++i)
+    e = batch_getrs_c128(1, (int)N, (char *)LU + i * N2 * 16, (int *)piv + i * N, dx + (size_t)idx[i] * N, st);
+  cudaFreeAsync(LU, st);
+  cudaFreeAsync(piv, st);
+  return e;
+}
+
 int batched_solve(cublasHandle_t h, cudaStream_t st, int nm, size_t N, const qg_c *dM, const qg_c *db, qg_c *dx,
                   int mode, double tol, int max_iter, void *scratch, double *resid_host, int *iters_host,
-                  int *info_host, double *logabsdet) {
+                  int *info_host, double *logabsdet, int *fallback_host) {
   if (nm <= 0) return QPMS_SUCCESS;
+  max_iter = max_refine_steps(max_iter);
   const size_t m = (size_t)nm, N2 = N * N;
   char *p = (char *)scratch;
   void *LU = p;
@@ -94,14 +132,49 @@ int batched_solve(cublasHandle_t h, cudaStream_t st, int nm, size_t N, const qg_
       if (worst <= tol || worst >= 0.5 * prev) break;  // converged or stagnated
       prev = worst;
     }
+    // systems whose refinement stalled above tol: solved again in complex128
+    std::vector<int> bad;
+    for (size_t i = 0; i < m; ++i)
+      if (sqrt(hr[i] / (hb[i] > 0 ? hb[i] : 1)) > tol) bad.push_back((int)i);
+    if (!bad.empty()) {
+      if ((e = resolve_fp64(st, bad, N, dM, db, dx))) return e;
+      if ((e = launch_residual(nm, N, dM, dx, db, r, rn2, bn2, st))) return e;
+      QG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, m * 8, cudaMemcpyDeviceToHost, st));
+      QG_CUDA_TRY(cudaMemcpyAsync(hb.data(), bn2, m * 8, cudaMemcpyDeviceToHost, st));
+      QG_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    if (fallback_host) {
+      for (size_t i = 0; i < m; ++i) fallback_host[i] = 0;
+      for (int i : bad) fallback_host[i] = 1;
+    }
   }
+  if (mode == 0 && fallback_host)
+    for (size_t i = 0; i < m; ++i) fallback_host[i] = 0;
   if (logabsdet) {
-    if (mode)
-      logabsdet_kernel<float2><<<(nm + 127) / 128, 128, 0, st>>>(nm, N, (const float2 *)LU, logabsdet);
-    else
+    if (mode) {
+      // log|det M| from complex128 factors of the FP64 matrices (complex64
+      // factors hold it to ~1e-5 only; these small LUs are not the cost)
+      void *LU64 = nullptr, *piv64 = nullptr;
+      QG_CUDA_TRY(cudaMallocAsync(&LU64, m * N2 * 16, st));
+      QG_CUDA_TRY(cudaMallocAsync(&piv64, m * N * 4, st));
+      QG_CUDA_TRY(cudaMemcpyAsync(LU64, dM, m * N2 * 16, cudaMemcpyDeviceToDevice, st));
+      e = batch_getrf_c128(nm, (int)N, LU64, (int *)piv64, nullptr, st);
+      if (!e) {
+        logabsdet_kernel<double2><<<(nm + 127) / 128, 128, 0, st>>>(nm, N, (const double2 *)LU64, logabsdet);
+        if (cudaGetLastError() != cudaSuccess) {
+          set_error("logabsdet kernel launch failed");
+          e = QPMS_ERROR;
+        }
+        g_launches.fetch_add(1);
+      }
+      cudaFreeAsync(LU64, st);
+      cudaFreeAsync(piv64, st);
+      if (e) return e;
+    } else {
       logabsdet_kernel<double2><<<(nm + 127) / 128, 128, 0, st>>>(nm, N, (const double2 *)LU, logabsdet);
-    QG_CUDA_TRY(cudaGetLastError());
-    g_launches.fetch_add(1);
+      QG_CUDA_TRY(cudaGetLastError());
+      g_launches.fetch_add(1);
+    }
   }
   if (info_host) {
     QG_CUDA_TRY(cudaMemcpyAsync(info_host, info, m * 4, cudaMemcpyDeviceToHost, st));
@@ -115,3 +188,8 @@ int batched_solve(cublasHandle_t h, cudaStream_t st, int nm, size_t N, const qg_
 }
 
 }  // namespace qg
+
+extern "C" int qpms_gpu_testing_set_max_refine(int max_steps) {
+  qg::g_max_refine.store(max_steps < 0 ? -1 : max_steps);
+  return QPMS_SUCCESS;
+}

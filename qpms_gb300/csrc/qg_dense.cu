@@ -32,6 +32,7 @@
 #include <random>
 #include <vector>
 
+#include "qg_batched.h"
 #include "qg_dense.h"
 #include "qg_internal.h"
 #include "qg_ktimer.h"
@@ -858,6 +859,7 @@ int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int 
     set_error("dense solver: nrhs %d outside 1..%d", nrhs, nrhs_max);
     return QPMS_EINVAL;
   }
+  max_iter = max_refine_steps(max_iter);
   cublasHandle_t h;
   int e;
   if ((e = blas_handle_get(&h))) return e;

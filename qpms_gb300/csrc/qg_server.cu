@@ -84,6 +84,16 @@ struct SysDev {
   int *tmid = nullptr;
 };
 
+// allocations still to fail on purpose (qpms_gpu_server_testing_fail_allocations)
+std::atomic<int> g_fail_allocs{0};
+
+bool injected_failure() {
+  int n = g_fail_allocs.load();
+  while (n > 0)
+    if (g_fail_allocs.compare_exchange_weak(n, n - 1)) return true;
+  return false;
+}
+
 // device buffers of one job or batch, returned to the pool on destruction
 struct PoolBufs {
   cudaStream_t st;
@@ -95,6 +105,10 @@ struct PoolBufs {
   template <typename T>
   int get(T **out, size_t bytes, cudaMemPool_t pool) {
     void *p = nullptr;
+    if (injected_failure()) {
+      set_error("server: device pool allocation of %zu bytes failed (injected)", bytes);
+      return QPMS_ENOMEM;
+    }
     if (cudaMallocFromPoolAsync(&p, bytes ? bytes : 16, pool, st) != cudaSuccess) {
       set_error("server: device pool allocation of %zu bytes failed", bytes);
       return QPMS_ENOMEM;
@@ -310,6 +324,7 @@ struct qpms_gpu_server {
     if ((e = ds.init((int)N, 1, mode, 0x5eed ^ j->id, pool, st))) return e;
     if ((e = ds.factorize(dM, N, st, true))) return e;
     if ((e = ds.solve(dM, N, db, dx, 1, kRefineTol, kMaxRefine, &res, &it, st))) return e;
+    j->res.fallback = ds.refactors > 0 ? 1 : 0;
     if ((e = launch_sigma_ext(1, N, da, dx, dk, dsig, st))) return e;
     double sig = 0;
     QG_CUDA_TRY(cudaMemcpyAsync(&sig, dsig, 8, cudaMemcpyDeviceToHost, st));
@@ -376,9 +391,9 @@ struct qpms_gpu_server {
     if ((e = launch_incident(nb, np, n, dcoef, dkv, sd.pos, da, st, (size_t)n))) return e;
     if ((e = launch_apply_t(nb, np, n, ntm, scatsys_dense(ss) ? 1 : 0, sd.tmid, dT, da, db, st))) return e;
     std::vector<double> res(nb), sig(nb);
-    std::vector<int> its(nb), info(nb);
+    std::vector<int> its(nb), info(nb), fb(nb);
     if ((e = batched_solve(h, st, nb, N, dM, db, dx, mode, kRefineTol, kMaxRefine, scratch, res.data(), its.data(),
-                           info.data(), nullptr)))
+                           info.data(), nullptr, fb.data())))
       return e;
     if ((e = launch_sigma_ext(nb, N, da, dx, dk, dsig, st))) return e;
     QG_CUDA_TRY(cudaMemcpyAsync(sig.data(), dsig, nb * 8, cudaMemcpyDeviceToHost, st));
@@ -390,6 +405,7 @@ struct qpms_gpu_server {
       work[b]->res.sigma_ext = sig[b];
       work[b]->res.residual = res[b];
       work[b]->res.iters = its[b];
+      work[b]->res.fallback = fb[b];
       if (info[b]) {
         work[b]->res.status = QPMS_ERROR;
         work[b]->err = "singular matrix";
@@ -590,6 +606,39 @@ int qpms_gpu_server_wait(qpms_gpu_server_t *s, uint64_t ticket, qpms_gpu_result_
   s->jobs.erase(it);
   delete j;
   return st;
+}
+
+int qpms_gpu_server_cancel(qpms_gpu_server_t *s, uint64_t ticket) {
+  clear_error();
+  if (!s) return QPMS_EINVAL;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(ticket);
+    if (it == s->jobs.end()) {
+      set_error("unknown ticket %llu", (unsigned long long)ticket);
+      return QPMS_EINVAL;
+    }
+    Job *j = it->second;
+    auto q = std::find(s->pending.begin(), s->pending.end(), j);
+    if (q == s->pending.end()) {
+      set_error("request %llu has already started", (unsigned long long)ticket);
+      return QPMS_EINVAL;
+    }
+    s->pending.erase(q);
+    j->res.status = QPMS_ECANCELED;
+    j->res.t_start = j->res.t_done = s->now();
+    j->err = "cancelled before it started";
+    j->done = true;
+  }
+  s->cv_done.notify_all();
+  s->cv_work.notify_all();
+  return QPMS_SUCCESS;
+}
+
+int qpms_gpu_server_testing_fail_allocations(qpms_gpu_server_t *s, int count) {
+  if (!s || count < 0) return QPMS_EINVAL;
+  g_fail_allocs.store(count);
+  return QPMS_SUCCESS;
 }
 
 int qpms_gpu_server_drain(qpms_gpu_server_t *s) {

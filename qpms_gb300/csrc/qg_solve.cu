@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "qg_assembly.h"
+#include "qg_batched.h"
 #include "qg_batchlu.h"
 #include "qg_dense.h"
 #include "qg_internal.h"
@@ -533,7 +534,7 @@ int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw, c
     if ((e = batch_getrf_c64(W, (int)N, dLU.p, dpiv.as<int>(), dinfo.as<int>(), st))) return e;
     // x0 = LU32^{-1} b, then refine: r = b - M x (FP64), x += LU32^{-1} r
     QG_CUDA_TRY(cudaMemcpyAsync(dr.p, db.p, N * W * 16, cudaMemcpyDeviceToDevice, st));
-    const int kMaxIter = 12;
+    const int kMaxIter = max_refine_steps(12);
     double prev = 1e300;
     for (int it = 0; it <= kMaxIter; ++it) {
       if ((e = launch_c128_to_c64(N * W, dr.as<qg_c>(), dcb.p, st))) return e;
@@ -551,6 +552,17 @@ int qpms_gpu_finite_planewave_scatter_ext(const qpms_scatsys_t *ss, size_t nw, c
       }
       if (worst <= 1e-13 || worst >= 0.5 * prev) break;  // converged or stagnated
       prev = worst;
+    }
+    // frequencies whose refinement stalled: solved again in complex128
+    std::vector<int> bad;
+    for (int w = 0; w < W; ++w)
+      if (sqrt(hr[w] / (hb[w] > 0 ? hb[w] : 1)) > 1e-13) bad.push_back(w);
+    if (!bad.empty()) {
+      if ((e = resolve_fp64(st, bad, N, dM.as<qg_c>(), db.as<qg_c>(), dx.as<qg_c>()))) return e;
+      if ((e = launch_residual(W, N, dM.as<qg_c>(), dx.as<qg_c>(), db.as<qg_c>(), dr.as<qg_c>(), rn2, bn2, st)))
+        return e;
+      QG_CUDA_TRY(cudaMemcpy(hr.data(), rn2, W * 8, cudaMemcpyDeviceToHost));
+      QG_CUDA_TRY(cudaMemcpy(hb.data(), bn2, W * 8, cudaMemcpyDeviceToHost));
     }
   }
   if ((e = launch_sigma_ext(W, N, da.as<qg_c>(), dx.as<qg_c>(), dk.as<qg_c>(), dsig.as<double>(), st))) return e;

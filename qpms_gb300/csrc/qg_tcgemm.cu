@@ -48,6 +48,7 @@ namespace {
 constexpr int BM = 128;  // accumulator rows = tensor-memory lanes
 constexpr int BK = 64;   // bf16 per 128-byte swizzled row
 constexpr unsigned long long kTimeoutNs = 4000000000ull;  // 4 s per wait
+constexpr int kReservedSms = 8;
 
 __device__ int g_tc_error;
 
@@ -258,28 +259,31 @@ __global__ void __launch_bounds__(192, 1)
     }
   } else if (warp >= 2) {
     // ---- epilogue ----
+    // Each thread owns one accumulator row (its tensor-memory lane) of the
+    // tile.  Its BN values of C are loaded into registers before the wait for
+    // the accumulator, so the HBM reads of this tile overlap its MMAs; D is
+    // then stored column by column (a warp writes 32 consecutive floats).
     const int quad = warp & 3;  // tensor-memory lane quarter this warp may read
+    const bool has_c = g.beta != 0.f;
     uint32_t t = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++t) {
       const uint32_t b = t & 1, tph = (t >> 1) & 1;
-      if (!(ok = mbar_wait(tfull + b, tph, 4))) break;
-      tc_fence_after();
       const int m0 = (tile % mt) * BM, n0 = (tile / mt) * BN;
       const int r = m0 + quad * 32 + lane;
       const bool rok = r < g.Md;
-      const bool has_c = g.beta != 0.f;
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        // the C values of 32 columns are loaded first, all in flight at once
-        // (C may be D: each element is read and then written by this thread)
-        float cv[32];
-        if (has_c && rok) {
+      float cv[BN];
+      if (has_c && rok) {
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const int j = n0 + c0 + c;
-            cv[c] = (j < g.Nd) ? g.C[(size_t)j * g.ldc + r] : 0.f;
-          }
+        for (int c = 0; c < BN; ++c) {
+          const int j = n0 + c;
+          cv[c] = (j < g.Nd) ? g.C[(size_t)j * g.ldc + r] : 0.f;
         }
+      }
+      if (!(ok = mbar_wait(tfull + b, tph, 4))) break;
+      tc_fence_after();
+#pragma unroll
+      for (int c0 = 0; c0 < BN; c0 += 32) {
         uint32_t v[16], w[16];
         tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0, v);
         tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0 + 16, w);
@@ -289,7 +293,7 @@ __global__ void __launch_bounds__(192, 1)
             const int j = n0 + c0 + c;
             if (j < g.Nd) {
               float x = g.alpha * __uint_as_float(c < 16 ? v[c] : w[c - 16]);
-              if (has_c) x += g.beta * cv[c];
+              if (has_c) x += g.beta * cv[c0 + c];
               g.D[(size_t)j * g.ldd + r] = x;
             }
           }
@@ -431,8 +435,12 @@ int launch_gemm(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g,
                                     S::kBytes);
   });
   QG_CUDA_TRY(attr_err);
+  // Persistent CTAs on all but kReservedSms SMs: the single-CTA kernels of the
+  // dense LU (diagonal blocks) and the small launches of concurrent solves on
+  // other streams always find an SM instead of waiting for a whole GEMM.
   const int ntiles = ((g.Md + BM - 1) / BM) * ((g.Nd + BN - 1) / BN);
-  const int grid = ntiles < g_num_sms ? ntiles : g_num_sms;
+  const int slots = g_num_sms > 2 * kReservedSms ? g_num_sms - kReservedSms : g_num_sms;
+  const int grid = ntiles < slots ? ntiles : slots;
   if (grid <= 0) return QPMS_SUCCESS;
   KtScope kt(KT_TCGEMM, st, 2.0 * g.Md * (double)g.Nd * (double)g.kblocks * BK * g.npairs);
   tc_gemm_kernel<BN, STAGES><<<grid, 192, S::kBytes, st>>>(ma, mb, g);

@@ -20,9 +20,9 @@ class _Request(C.Structure):
 
 
 class _Result(C.Structure):
-    _fields_ = [("status", C.c_int), ("iters", C.c_int), ("batch_size", C.c_int), ("sigma_ext", C.c_double),
-                ("residual", C.c_double), ("t_submit", C.c_double), ("t_start", C.c_double),
-                ("t_done", C.c_double)]
+    _fields_ = [("status", C.c_int), ("iters", C.c_int), ("batch_size", C.c_int), ("fallback", C.c_int),
+                ("sigma_ext", C.c_double), ("residual", C.c_double), ("t_submit", C.c_double),
+                ("t_start", C.c_double), ("t_done", C.c_double)]
 
 
 def declare(L):
@@ -35,6 +35,12 @@ def declare(L):
     L.qpms_gpu_server_wait.argtypes = [vp, C.c_uint64, C.POINTER(_Result)]
     L.qpms_gpu_server_drain.restype = ci
     L.qpms_gpu_server_drain.argtypes = [vp]
+    L.qpms_gpu_server_cancel.restype = ci
+    L.qpms_gpu_server_cancel.argtypes = [vp, C.c_uint64]
+    L.qpms_gpu_server_testing_fail_allocations.restype = ci
+    L.qpms_gpu_server_testing_fail_allocations.argtypes = [vp, ci]
+    L.qpms_gpu_testing_set_max_refine.restype = ci
+    L.qpms_gpu_testing_set_max_refine.argtypes = [ci]
     L.qpms_gpu_server_clock.restype = cd
     L.qpms_gpu_server_clock.argtypes = [vp]
     L.qpms_gpu_server_stats.restype = ci
@@ -78,11 +84,17 @@ class Server:
         rc = self._L.qpms_gpu_server_wait(self.s, ticket, C.byref(res))
         f, _ = self._live.pop(ticket)
         out = {"status": rc, "sigma_ext": res.sigma_ext, "residual": res.residual, "iters": res.iters,
-               "batch_size": res.batch_size, "t_submit": res.t_submit, "t_start": res.t_start,
-               "t_done": res.t_done, "f": f}
+               "batch_size": res.batch_size, "fallback": res.fallback, "t_submit": res.t_submit,
+               "t_start": res.t_start, "t_done": res.t_done, "f": f}
         if rc:
             out["error"] = last_error()
         return out
+
+    def cancel(self, ticket):
+        """Withdraw a request that has not started (True), or False if it already
+        started; a cancelled request still has to be waited for (status
+        QPMS_ECANCELED)."""
+        return self._L.qpms_gpu_server_cancel(self.s, ticket) == 0
 
     def drain(self):
         self._L.qpms_gpu_server_drain(self.s)

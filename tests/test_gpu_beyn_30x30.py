@@ -35,6 +35,8 @@ def sys30():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     import qpms_gb300
+    if not os.path.exists(GOLDEN):
+        pytest.skip("fixture tests/golden/beyn_30x30.json not generated")
     g = json.load(open(GOLDEN))
     xs = (np.arange(g["nx"]) - (g["nx"] - 1) / 2) * g["pitch"]
     X, Y = np.meshgrid(xs, xs, indexing="ij")

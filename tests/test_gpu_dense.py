@@ -39,7 +39,7 @@ def _solve(torch, M, B, mode):
 
 
 @pytest.mark.parametrize("mode", [0, 1])
-@pytest.mark.parametrize("N", [256, 1000])
+@pytest.mark.parametrize("N", [37, 256, 300, 1000])
 def test_random_system(torch_cuda, mode, N):
     rng = np.random.default_rng(N)
     M = (rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))) / np.sqrt(N) + 2 * np.eye(N)
