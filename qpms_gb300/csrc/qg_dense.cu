@@ -32,6 +32,7 @@
 #include <random>
 #include <vector>
 
+#include "qg_assembly.h"
 #include "qg_batched.h"
 #include "qg_dense.h"
 #include "qg_internal.h"
@@ -430,18 +431,15 @@ int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, 
     if (m2 <= 0) break;
     float2 *A21 = A + (size_t)k * lda + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = A21 + (size_t)kb * lda;
     // L21 = A21 U^-1
-    if ((e = tc_split_a(A21, lda, m2, kb, nsplit, pa, st)) || (e = tc_split_b(Uk, kb, kb, kb, nsplit, pb, st)))
-      return e;
+    if ((e = tc_split_ab(A21, lda, m2, kb, Uk, kb, kb, nsplit, pa, pb, st))) return e;
     P.m = m2, P.n = kb, P.k = kb;
     if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, A21, lda, st))) return e;
     // U12 = L^-1 A12
-    if ((e = tc_split_a(Lk, kb, kb, kb, nsplit, pa, st)) || (e = tc_split_b(A12, lda, kb, m2, nsplit, pb, st)))
-      return e;
+    if ((e = tc_split_ab(Lk, kb, kb, kb, A12, lda, m2, nsplit, pa, pb, st))) return e;
     P.m = kb, P.n = m2, P.k = kb;
     if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, A12, lda, st))) return e;
     // A22 -= L21 U12
-    if ((e = tc_split_a(A21, lda, m2, kb, nsplit, pa, st)) || (e = tc_split_b(A12, lda, kb, m2, nsplit, pb, st)))
-      return e;
+    if ((e = tc_split_ab(A21, lda, m2, kb, A12, lda, m2, nsplit, pa, pb, st))) return e;
     P.m = m2, P.n = m2, P.k = kb;
     if ((e = tc_cgemm_planes(P, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
   }
@@ -460,29 +458,23 @@ int lu_solve_tc(int N, int nb, const float2 *A, size_t lda, const float2 *Dinv, 
   for (int blk = 0; blk < nblk; ++blk) {  // forward: L y = b
     const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
     const float2 *Lk = Dinv + (size_t)blk * 2 * nb * nb;
-    if ((e = tc_split_a(Lk, kb, kb, kb, nsplit, pa, st)) || (e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st)))
-      return e;
+    if ((e = tc_split_ab(Lk, kb, kb, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
     P.m = kb, P.n = nrhs, P.k = kb;
     if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, B + k, ldb, st))) return e;
     const int m2 = N - k - kb;
     if (m2 <= 0) continue;
-    if ((e = tc_split_a(A + (size_t)k * lda + k + kb, lda, m2, kb, nsplit, pa, st)) ||
-        (e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st)))
-      return e;
+    if ((e = tc_split_ab(A + (size_t)k * lda + k + kb, lda, m2, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
     P.m = m2, P.n = nrhs, P.k = kb;
     if ((e = tc_cgemm_planes(P, -1.f, 1.f, B + k + kb, ldb, B + k + kb, ldb, st))) return e;
   }
   for (int blk = nblk - 1; blk >= 0; --blk) {  // backward: U x = y
     const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
     const float2 *Uk = Dinv + (size_t)blk * 2 * nb * nb + (size_t)nb * nb;
-    if ((e = tc_split_a(Uk, kb, kb, kb, nsplit, pa, st)) || (e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st)))
-      return e;
+    if ((e = tc_split_ab(Uk, kb, kb, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
     P.m = kb, P.n = nrhs, P.k = kb;
     if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, B + k, ldb, st))) return e;
     if (k == 0) continue;
-    if ((e = tc_split_a(A + (size_t)k * lda, lda, k, kb, nsplit, pa, st)) ||
-        (e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st)))
-      return e;
+    if ((e = tc_split_ab(A + (size_t)k * lda, lda, k, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
     P.m = k, P.n = nrhs, P.k = kb;
     if ((e = tc_cgemm_planes(P, -1.f, 1.f, B, ldb, B, ldb, st))) return e;
   }
@@ -653,6 +645,7 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   QG_CUDA_TRY(dev_alloc(&y64, (size_t)N * nrhs_max * 16));
   QG_CUDA_TRY(dev_alloc(&dinfo, 16));
   QG_CUDA_TRY(dev_alloc(&rs, (size_t)4 * Np * sizeof(double)));
+  QG_CUDA_TRY(dev_alloc(&res_nrm, (size_t)2 * kOzakiMinRhs * sizeof(double)));
   if (tc_split) {
     QG_CUDA_TRY(dev_alloc(&tc_pa, tc_planes_bytes_a(Np, nb, 3)));
     QG_CUDA_TRY(dev_alloc(&tc_pb, tc_planes_bytes_b(std::max(Np, nrhs_max), nb, 3)));
@@ -686,7 +679,7 @@ size_t DenseSolver::footprint(int N, int nrhs, int mode) {
   const size_t nblk = (Np + nb - 1) / nb;
   size_t b = (mode ? Np * Np * esz : 0) + Np * Np * 16 + nblk * 2 * nb * nb * esz;
   b += std::max<size_t>(Np * nb, nb * std::max<size_t>(Np, nrhs)) * esz;
-  b += Np * nrhs * (8 + 16) + (size_t)N * nrhs * 32 + 16 + 4 * Np * 8;
+  b += Np * nrhs * (8 + 16) + (size_t)N * nrhs * 32 + 16 + 4 * Np * 8 + 2 * kOzakiMinRhs * 8;
   if (ozaki_wanted(nrhs)) b += ozaki_matrix_bytes(N) + ozaki_work_bytes(N, nrhs);
   if (mode && tc_digits(nrhs)) b += tc_plane_bytes((int)Np, nrhs, (int)nb);
   return b + 12 * 512;  // allocation rounding
@@ -705,7 +698,7 @@ cudaError_t DenseSolver::dev_alloc(void *ptr, size_t bytes) {
 
 void DenseSolver::release() {
   for (void *p : {(void *)A, (void *)T64, (void *)Dinv, (void *)work, (void *)rhs_lo, (void *)rp, (void *)r64,
-                  (void *)y64, (void *)dinfo, (void *)rs, oz_mat, oz_work, tc_pa, tc_pb})
+                  (void *)y64, (void *)dinfo, (void *)rs, (void *)res_nrm, oz_mat, oz_work, tc_pa, tc_pb})
     if (p) {
       if (pool)
         cudaFreeAsync(p, ast);
@@ -716,6 +709,7 @@ void DenseSolver::release() {
   r64 = y64 = nullptr;
   dinfo = nullptr;
   rs = nullptr;
+  res_nrm = nullptr;
   oz_mat = oz_work = nullptr;
   tc_pa = tc_pb = nullptr;
   use_ozaki = false;
@@ -786,12 +780,13 @@ int DenseSolver::factorize_current(const void *M64, size_t ldm, cudaStream_t st)
     d2f_kernel<<<grid1(NN), 256, 0, st>>>(NN, (const double2 *)T64, (float2 *)A);
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
-    if (tc_split)
+    if (tc_split) {
       e = lu_nopiv_tc(Np, nb, (float2 *)A, Np, (float2 *)Dinv, dinfo, tc_split, (__nv_bfloat16 *)tc_pa,
                       (__nv_bfloat16 *)tc_pb, st);
-    else
+    } else {
       e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
                            (cublasComputeType_t)trail_ct, st);
+    }
   } else {
     e = lu_nopiv<double2>(h, Np, nb, (double2 *)T64, Np, (double2 *)Dinv, (double2 *)work, dinfo,
                           CUBLAS_COMPUTE_64F, st);
@@ -882,7 +877,14 @@ int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int 
     first = false;
     // r = B - M X (FP64 accuracy)
     if (use_ozaki && nrhs >= kOzakiMinRhs) {
-      if ((e = ozaki_residual(h, oz, X, B, r64, nrhs, oz_work, st))) return e;
+      if ((e = ozaki_residual(oz, X, B, r64, nrhs, oz_work, st))) return e;
+    } else if (row_major && ldm == (size_t)N && nrhs <= kOzakiMinRhs) {
+      // few right-hand sides: one warp per row of the row-major M, FP64 (a pass over M per column)
+      for (int c = 0; c < nrhs; ++c)
+        if ((e = launch_residual(1, N, (const qg_c *)M64, (const qg_c *)X + (size_t)c * N,
+                                 (const qg_c *)B + (size_t)c * N, (qg_c *)r64 + (size_t)c * N, res_nrm + 2 * c,
+                                 res_nrm + 2 * c + 1, st)))
+          return e;
     } else {
       QG_CUDA_TRY(cudaMemcpyAsync(r64, B, n * 16, cudaMemcpyDeviceToDevice, st));
       // a row-major M read column-major is M^T: multiply with OP_T

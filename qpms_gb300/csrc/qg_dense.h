@@ -27,6 +27,7 @@ struct DenseSolver {
   void *r64 = nullptr, *y64 = nullptr;  // complex128 N x nrhs_max: residual and correction
   int *dinfo = nullptr;    // zero-pivot flag, then two doubles of norm scratch
   double *rs = nullptr;    // butterfly diagonals [u L1][u L2][v L1][v L2], Np each
+  double *res_nrm = nullptr;  // norms scratch of the few-right-hand-side residual kernel
 
   // Stream-ordered allocation: with a memory pool, every buffer comes from
   // cudaMallocFromPoolAsync on stream `ast` and returns to it in release(),

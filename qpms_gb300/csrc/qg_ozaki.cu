@@ -18,15 +18,18 @@
 //
 // One GEMM per row digit i multiplies D_i with the concatenation
 // [E_0 | ... | E_{p-1-i}] (the column digits are stored contiguously, so
-// that concatenation is a prefix): p GEMMs of 2N x 2 nrhs (p - i) x N.
+// that concatenation is a prefix): p GEMMs of 2N x 2 nrhs (p - i) x N, on the
+// library's tcgen05 GEMM (qg_tcgemm.cu).  Both digit sets are stored K-major
+// (rows of M, columns of X contiguous) with the row length padded to a
+// multiple of 8 (N8), the alignment the tensor-memory-access loads need.
 #include <cuda_bf16.h>
 #include <math.h>
 
 #include "qg_internal.h"
 #include "qg_ozaki.h"
+#include "qg_tcgemm.h"
 
 namespace qg {
-int blas_handle_get(cublasHandle_t *h);
 
 namespace {
 
@@ -95,10 +98,9 @@ __device__ __forceinline__ void digits(double v, int s, int p, Store st) {
   }
 }
 
-// Slices of [Re M; Im M]; element (R, k) of digit i at
-//   row-major layout: sl[i 2N N + R N + k]   (rows contiguous, GEMM op T)
-//   column-major:     sl[i 2N N + k 2N + R]  (GEMM op N)
-__global__ void split_matrix_kernel(const double2 *__restrict__ M, size_t ldm, int N, bool row_major,
+// Slices of [Re M; Im M]; element (R, k) of digit i at sl[i 2N N8 + R N8 + k]
+// (rows of M contiguous, K-major for the GEMM), from M row-major or column-major.
+__global__ void split_matrix_kernel(const double2 *__restrict__ M, size_t ldm, int N, size_t N8, bool row_major,
                                     const double *__restrict__ scale, int s, int p, __nv_bfloat16 *sl) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const size_t NN = (size_t)N * N;
@@ -112,9 +114,9 @@ __global__ void split_matrix_kernel(const double2 *__restrict__ M, size_t ldm, i
     r = (int)(idx % N);
   }
   const double2 v = row_major ? M[(size_t)r * ldm + k] : M[(size_t)k * ldm + r];
-  const size_t slab = 2 * NN;
-  const size_t oR = row_major ? (size_t)r * N + k : (size_t)k * 2 * N + r;
-  const size_t oI = row_major ? (size_t)(N + r) * N + k : (size_t)k * 2 * N + N + r;
+  const size_t slab = 2 * (size_t)N * N8;
+  const size_t oR = (size_t)r * N8 + k;
+  const size_t oI = (size_t)(N + r) * N8 + k;
   digits(v.x / scale[r], s, p, [&](int i, __nv_bfloat16 d) { sl[i * slab + oR] = d; });
   digits(v.y / scale[N + r], s, p, [&](int i, __nv_bfloat16 d) { sl[i * slab + oI] = d; });
 }
@@ -141,17 +143,17 @@ __global__ void colmax_kernel(const double2 *__restrict__ X, int N, int nrhs, do
   }
 }
 
-// Column digits: element (k, C) of digit j at bsl[(j 2nrhs + C) N + k].
-__global__ void split_rhs_kernel(const double2 *__restrict__ X, int N, int nrhs, const double *__restrict__ tau,
-                                 int s, int p, __nv_bfloat16 *bsl) {
+// Column digits: element (k, C) of digit j at bsl[(j 2nrhs + C) N8 + k].
+__global__ void split_rhs_kernel(const double2 *__restrict__ X, int N, size_t N8, int nrhs,
+                                 const double *__restrict__ tau, int s, int p, __nv_bfloat16 *bsl) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)N * nrhs) return;
   const int c = (int)(idx / N), k = (int)(idx % N);
   const double2 v = X[idx];
-  const size_t w = (size_t)2 * nrhs * N;
-  digits(v.x / tau[c], s, p, [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)c * N + k] = d; });
+  const size_t w = (size_t)2 * nrhs * N8;
+  digits(v.x / tau[c], s, p, [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)c * N8 + k] = d; });
   digits(v.y / tau[nrhs + c], s, p,
-         [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)(nrhs + c) * N + k] = d; });
+         [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)(nrhs + c) * N8 + k] = d; });
 }
 
 // P[R, C] (+)= sum_{j <= p-1-i} 2^{-s (i+j+2)} G[R, j 2nrhs + C], j descending
@@ -196,17 +198,19 @@ void ozaki_digits(int K, int *s, int *p) {
   *p = (55 + ss - 1) / ss;
 }
 
+size_t n8(int N) { return ((size_t)N + 7) / 8 * 8; }
+
 size_t ozaki_matrix_bytes(int N) {
   int s, p;
   ozaki_digits(N, &s, &p);
-  return al256((size_t)p * 2 * N * N * 2) + 2 * al256((size_t)2 * N * 8);
+  return al256((size_t)p * 2 * N * n8(N) * 2) + 2 * al256((size_t)2 * N * 8);
 }
 
 size_t ozaki_work_bytes(int N, int nrhs) {
   int s, p;
   ozaki_digits(N, &s, &p);
   const size_t tn = 2 * (size_t)nrhs;
-  return al256((size_t)p * N * tn * 2) + al256(tn * 8) + al256((size_t)2 * N * tn * p * 4) +
+  return al256((size_t)p * n8(N) * tn * 2) + al256(tn * 8) + al256((size_t)2 * N * tn * p * 4) +
          al256((size_t)2 * N * tn * 8);
 }
 
@@ -220,7 +224,8 @@ int ozaki_split_matrix(const void *M, size_t ldm, bool row_major, int N, void *b
   om->p = p;
   om->row_major = row_major;
   om->slices = b;
-  b += al256((size_t)p * 2 * N * N * 2);
+  om->ld = n8(N);
+  b += al256((size_t)p * 2 * N * om->ld * 2);
   om->scale = (double *)b;
   b += al256((size_t)2 * N * 8);
   om->rowmax = (unsigned long long *)b;
@@ -236,19 +241,20 @@ int ozaki_split_matrix(const void *M, size_t ldm, bool row_major, int N, void *b
   QG_CUDA_TRY(cudaGetLastError());
   scale_kernel<<<grid1(2 * (size_t)N), 256, 0, st>>>(om->rowmax, 2 * N, om->scale);
   QG_CUDA_TRY(cudaGetLastError());
-  split_matrix_kernel<<<grid1((size_t)N * N), 256, 0, st>>>(Md, ldm, N, row_major, om->scale, s, p,
+  split_matrix_kernel<<<grid1((size_t)N * N), 256, 0, st>>>(Md, ldm, N, om->ld, row_major, om->scale, s, p,
                                                             (__nv_bfloat16 *)om->slices);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(3);
   return QPMS_SUCCESS;
 }
 
-int ozaki_residual(cublasHandle_t h, const OzakiMatrix &om, const void *X, const void *B, void *R, int nrhs,
-                   void *work, cudaStream_t st) {
+int ozaki_residual(const OzakiMatrix &om, const void *X, const void *B, void *R, int nrhs, void *work,
+                   cudaStream_t st) {
   const int N = om.N, s = om.s, p = om.p, tn = 2 * nrhs, twoN = 2 * N;
+  const size_t ld = om.ld;
   char *w = (char *)work;
   __nv_bfloat16 *bsl = (__nv_bfloat16 *)w;
-  w += al256((size_t)p * N * tn * 2);
+  w += al256((size_t)p * ld * tn * 2);
   double *tau = (double *)w;
   w += al256((size_t)tn * 8);
   float *G = (float *)w;
@@ -256,20 +262,17 @@ int ozaki_residual(cublasHandle_t h, const OzakiMatrix &om, const void *X, const
   double *P = (double *)w;
   colmax_kernel<<<tn, 256, 0, st>>>((const double2 *)X, N, nrhs, tau);
   QG_CUDA_TRY(cudaGetLastError());
-  split_rhs_kernel<<<grid1((size_t)N * nrhs), 256, 0, st>>>((const double2 *)X, N, nrhs, tau, s, p, bsl);
+  split_rhs_kernel<<<grid1((size_t)N * nrhs), 256, 0, st>>>((const double2 *)X, N, ld, nrhs, tau, s, p, bsl);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(2);
-  const float one = 1.0f, zero = 0.0f;
-  const cublasOperation_t opA = om.row_major ? CUBLAS_OP_T : CUBLAS_OP_N;
-  const int lda = om.row_major ? N : twoN;
+  int e;
   for (int i = p - 1; i >= 0; --i) {  // smallest contributions first
     const int n = tn * (p - i);
-    const __nv_bfloat16 *Ai = (const __nv_bfloat16 *)om.slices + (size_t)i * twoN * N;
-    QG_BLAS_TRY(cublasGemmEx(h, opA, CUBLAS_OP_N, twoN, n, N, &one, Ai, CUDA_R_16BF, lda, bsl, CUDA_R_16BF, N,
-                             &zero, G, CUDA_R_32F, twoN, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT));
+    const __nv_bfloat16 *Ai = (const __nv_bfloat16 *)om.slices + (size_t)i * twoN * ld;
+    if ((e = tc_gemm_bf16(Ai, ld, bsl, ld, twoN, n, N, 1.f, 0.f, nullptr, 0, G, twoN, st))) return e;
     accumulate_kernel<<<grid1((size_t)twoN * tn), 256, 0, st>>>(G, twoN, tn, i, s, p, i == p - 1, P);
     QG_CUDA_TRY(cudaGetLastError());
-    g_launches.fetch_add(2);
+    g_launches.fetch_add(1);
   }
   combine_kernel<<<grid1((size_t)N * nrhs), 256, 0, st>>>(P, om.scale, tau, N, nrhs, (const double2 *)B,
                                                           (double2 *)R);
@@ -292,10 +295,7 @@ extern "C" int qpms_gpu_ozaki_residual(int N, int nrhs, const qpms_complex_t *M,
     set_error("invalid arguments");
     return QPMS_EINVAL;
   }
-  cublasHandle_t h;
   int e;
-  if ((e = blas_handle_get(&h))) return e;
-  QG_BLAS_TRY(cublasSetStream(h, 0));
   void *mb = nullptr, *wb = nullptr;
   QG_CUDA_TRY(cudaMalloc(&mb, ozaki_matrix_bytes(N)));
   if (cudaMalloc(&wb, ozaki_work_bytes(N, nrhs)) != cudaSuccess) {
@@ -305,7 +305,7 @@ extern "C" int qpms_gpu_ozaki_residual(int N, int nrhs, const qpms_complex_t *M,
   }
   OzakiMatrix om;
   e = ozaki_split_matrix(M, ldm, row_major != 0, N, mb, &om, 0);
-  if (!e) e = ozaki_residual(h, om, X, B, R, nrhs, wb, 0);
+  if (!e) e = ozaki_residual(om, X, B, R, nrhs, wb, 0);
   cudaError_t se = cudaDeviceSynchronize();
   cudaFree(mb);
   cudaFree(wb);
@@ -314,18 +314,46 @@ extern "C" int qpms_gpu_ozaki_residual(int N, int nrhs, const qpms_complex_t *M,
   return QPMS_SUCCESS;
 }
 
+namespace qg {
+namespace {
+// dst [m][k] (row stride ld) = src (m x k column-major)
+__global__ void bf16_to_kmajor_kernel(int m, int k, const __nv_bfloat16 *__restrict__ src, size_t ld,
+                                      __nv_bfloat16 *__restrict__ dst) {
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)m * k) return;
+  const int c = (int)(idx / m), r = (int)(idx % m);
+  dst[(size_t)r * ld + c] = src[idx];
+}
+}  // namespace
+}  // namespace qg
+
 // Test entry: C = A B for bf16 A (m x k), B (k x n) column-major, FP32 C,
-// through the same cuBLAS call as the digit products (checks that integer
-// products with partial sums below 2^24 come out exact).
+// through the tensor-core GEMM of the digit products (checks that integer
+// products with partial sums below 2^24 come out exact).  A is first copied
+// K-major (the GEMM's operand layout).
 extern "C" int qpms_gpu_bf16_gemm(int m, int n, int k, const void *A, const void *B, float *C) {
   clear_error();
-  cublasHandle_t h;
-  int e;
-  if ((e = blas_handle_get(&h))) return e;
-  QG_BLAS_TRY(cublasSetStream(h, 0));
-  const float one = 1.0f, zero = 0.0f;
-  QG_BLAS_TRY(cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A, CUDA_R_16BF, m, B, CUDA_R_16BF, k, &zero,
-                           C, CUDA_R_32F, m, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT));
-  QG_CUDA_TRY(cudaDeviceSynchronize());
-  return QPMS_SUCCESS;
+  if (m <= 0 || n <= 0 || k <= 0 || !A || !B || !C) {
+    set_error("invalid arguments");
+    return QPMS_EINVAL;
+  }
+  const size_t ld = n8(k);
+  __nv_bfloat16 *Ak = nullptr, *Bk = nullptr;
+  QG_CUDA_TRY(cudaMalloc(&Ak, (size_t)m * ld * 2));
+  if (cudaMalloc(&Bk, (size_t)n * ld * 2) != cudaSuccess) {
+    cudaFree(Ak);
+    set_error("out of device memory");
+    return QPMS_ENOMEM;
+  }
+  bf16_to_kmajor_kernel<<<grid1((size_t)m * k), 256>>>(m, k, (const __nv_bfloat16 *)A, ld, Ak);
+  // B (k x n column-major) is K-major already: row stride k, copied to stride ld
+  cudaError_t ce = cudaMemcpy2D(Bk, ld * 2, B, (size_t)k * 2, (size_t)k * 2, n, cudaMemcpyDeviceToDevice);
+  int e = ce == cudaSuccess ? tc_gemm_bf16(Ak, ld, Bk, ld, m, n, k, 1.f, 0.f, nullptr, 0, C, m, 0) : QPMS_ERROR;
+  if (ce != cudaSuccess) set_error("copy failed: %s", cudaGetErrorString(ce));
+  cudaError_t se = cudaDeviceSynchronize();
+  cudaFree(Ak);
+  cudaFree(Bk);
+  if (e) return e;
+  QG_CUDA_TRY(se);
+  return tc_check_error(0);
 }

@@ -1,7 +1,6 @@
 // FP64-accurate complex matrix products on the bf16 tensor cores (Ozaki
 // splitting), for the refinement residual R = B - M X of the dense solver.
 #pragma once
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
 
@@ -13,8 +12,9 @@ namespace qg {
 // d_i integers with |d_0| <= 2^s, |d_i| <= 2^{s-1}, stored exactly in bf16.
 struct OzakiMatrix {
   int N = 0, s = 0, p = 0;
-  bool row_major = false;  // slice layout: (N x 2N) column-major (rows of M contiguous) if true
-  void *slices = nullptr;  // p x 2N x N bf16
+  bool row_major = false;  // layout of the source M
+  size_t ld = 0;           // slice row length: N rounded up to a multiple of 8
+  void *slices = nullptr;  // p x 2N x ld bf16, rows of [Re M; Im M] contiguous
   double *scale = nullptr; // 2N row scales sigma_R
   unsigned long long *rowmax = nullptr;  // 2N, bits of max |entry|
 };
@@ -38,7 +38,7 @@ int ozaki_split_matrix(const void *M, size_t ldm, bool row_major, int N, void *b
 // R = B - M X for complex128 X, B, R (N x nrhs, leading dimension N) with the
 // slices of M; work: ozaki_work_bytes(N, nrhs).  The products of digits run as
 // bf16 GEMMs with FP32 accumulation (exact), their sums in FP64.
-int ozaki_residual(cublasHandle_t h, const OzakiMatrix &om, const void *X, const void *B, void *R, int nrhs,
-                   void *work, cudaStream_t st);
+int ozaki_residual(const OzakiMatrix &om, const void *X, const void *B, void *R, int nrhs, void *work,
+                   cudaStream_t st);
 
 }  // namespace qg

@@ -320,49 +320,58 @@ __device__ __forceinline__ void digits(float x, int ns, __nv_bfloat16 *d) {
 }
 
 // A planes [s][2m][rs]: rows 2i, 2i+1 of E(A) at columns 2l, 2l+1.
-// 32 x 32 complex tiles through shared memory; blockDim (32, 8).
-__global__ void split_a_kernel(const float2 *__restrict__ A, size_t lda, int m, int k, int ns, size_t rs,
-                               size_t plane, int trans, __nv_bfloat16 *__restrict__ P) {
-  __shared__ float2 tile[32][33];  // [l][i]
-  const int i0 = blockIdx.x * 32, l0 = blockIdx.y * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;
+// 32 x 32 complex tiles through shared memory, 256 threads (tx 0..31, ty 0..7).
+struct SplitA {
+  const float2 *A;
+  size_t lda, rs, plane;
+  int m, k, trans;
+  __nv_bfloat16 *P;
+};
+__device__ __forceinline__ void split_a_tile(const SplitA &a, int ns, int bx, int by, int tx, int ty,
+                                             float2 (*tile)[33]) {
+  const int i0 = bx * 32, l0 = by * 32;
   for (int q = ty; q < 32; q += 8) {
-    if (!trans) {  // A(i, l) at A[l lda + i]: threads along i
+    if (!a.trans) {  // A(i, l) at A[l lda + i]: threads along i
       const int i = i0 + tx, l = l0 + q;
-      tile[q][tx] = (i < m && l < k) ? A[(size_t)l * lda + i] : make_float2(0.f, 0.f);
+      tile[q][tx] = (i < a.m && l < a.k) ? a.A[(size_t)l * a.lda + i] : make_float2(0.f, 0.f);
     } else {  // A(i, l) = Asrc(l, i) at A[i lda + l]: threads along l
       const int i = i0 + q, l = l0 + tx;
-      tile[tx][q] = (i < m && l < k) ? A[(size_t)i * lda + l] : make_float2(0.f, 0.f);
+      tile[tx][q] = (i < a.m && l < a.k) ? a.A[(size_t)i * a.lda + l] : make_float2(0.f, 0.f);
     }
   }
   __syncthreads();
   for (int q = ty; q < 32; q += 8) {  // write: threads along l
     const int i = i0 + q, l = l0 + tx;
-    if (i >= m || l >= k) continue;
+    if (i >= a.m || l >= a.k) continue;
     const float2 v = tile[tx][q];
     __nv_bfloat16 dr[3], di[3];
     digits(v.x, ns, dr);
     digits(v.y, ns, di);
     for (int s = 0; s < ns; ++s) {
-      __nv_bfloat16 *p = P + s * plane;
+      __nv_bfloat16 *p = a.P + s * a.plane;
       __nv_bfloat162 top, bot;  // row 2i: (Re, -Im); row 2i+1: (Im, Re)
       top.x = dr[s];
       top.y = __hneg(di[s]);
       bot.x = di[s];
       bot.y = dr[s];
-      *reinterpret_cast<__nv_bfloat162 *>(p + (size_t)(2 * i) * rs + 2 * l) = top;
-      *reinterpret_cast<__nv_bfloat162 *>(p + (size_t)(2 * i + 1) * rs + 2 * l) = bot;
+      *reinterpret_cast<__nv_bfloat162 *>(p + (size_t)(2 * i) * a.rs + 2 * l) = top;
+      *reinterpret_cast<__nv_bfloat162 *>(p + (size_t)(2 * i + 1) * a.rs + 2 * l) = bot;
     }
   }
 }
 
 // B planes [s][n][rs]: column j, entries 2l (Re) and 2l+1 (Im).
-__global__ void split_b_kernel(const float2 *__restrict__ B, size_t ldb, int k, int n, int ns, size_t rs,
-                               size_t plane, __nv_bfloat16 *__restrict__ P) {
-  const size_t total = (size_t)k * n;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-    const int j = (int)(t / k), l = (int)(t - (size_t)j * k);
-    const float2 v = B[(size_t)j * ldb + l];
+struct SplitB {
+  const float2 *B;
+  size_t ldb, rs, plane;
+  int k, n;
+  __nv_bfloat16 *P;
+};
+__device__ __forceinline__ void split_b_range(const SplitB &b, int ns, size_t start, size_t stride) {
+  const size_t total = (size_t)b.k * b.n;
+  for (size_t t = start; t < total; t += stride) {
+    const int j = (int)(t / b.k), l = (int)(t - (size_t)j * b.k);
+    const float2 v = b.B[(size_t)j * b.ldb + l];
     __nv_bfloat16 dr[3], di[3];
     digits(v.x, ns, dr);
     digits(v.y, ns, di);
@@ -370,8 +379,31 @@ __global__ void split_b_kernel(const float2 *__restrict__ B, size_t ldb, int k, 
       __nv_bfloat162 w;
       w.x = dr[s];
       w.y = di[s];
-      *reinterpret_cast<__nv_bfloat162 *>(P + s * plane + (size_t)j * rs + 2 * l) = w;
+      *reinterpret_cast<__nv_bfloat162 *>(b.P + s * b.plane + (size_t)j * b.rs + 2 * l) = w;
     }
+  }
+}
+
+__global__ void __launch_bounds__(256) split_a_kernel(SplitA a, int ns) {
+  __shared__ float2 tile[32][33];  // [l][i]
+  split_a_tile(a, ns, blockIdx.x, blockIdx.y, threadIdx.x & 31, threadIdx.x >> 5, tile);
+}
+
+__global__ void __launch_bounds__(256) split_b_kernel(SplitB b, int ns) {
+  split_b_range(b, ns, blockIdx.x * (size_t)blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+}
+
+// Both operands of one GEMM in one launch: blocks [0, na_x * na_y) make the A
+// planes (tile by tile), the rest the B planes.
+__global__ void __launch_bounds__(256) split_ab_kernel(SplitA a, int na_x, int na_y, SplitB b, int nb_blocks,
+                                                      int ns) {
+  __shared__ float2 tile[32][33];
+  const int na = na_x * na_y;
+  if ((int)blockIdx.x < na) {
+    split_a_tile(a, ns, blockIdx.x % na_x, blockIdx.x / na_x, threadIdx.x & 31, threadIdx.x >> 5, tile);
+  } else {
+    const size_t bb = blockIdx.x - na;
+    split_b_range(b, ns, bb * blockDim.x + threadIdx.x, (size_t)nb_blocks * blockDim.x);
   }
 }
 
@@ -472,17 +504,52 @@ size_t rs_of(int k) { return ((size_t)2 * k + 7) / 8 * 8; }
 size_t tc_planes_bytes_a(int m, int k, int nsplit) { return (size_t)nsplit * 2 * m * rs_of(k) * 2; }
 size_t tc_planes_bytes_b(int n, int k, int nsplit) { return (size_t)nsplit * n * rs_of(k) * 2; }
 
-int tc_split_a(const float2 *A, size_t lda, int m, int k, int nsplit, __nv_bfloat16 *planes, cudaStream_t st,
-               bool trans_a) {
-  if (m <= 0 || k <= 0) return QPMS_SUCCESS;
+namespace {
+SplitA split_a_args(const float2 *A, size_t lda, int m, int k, __nv_bfloat16 *planes, bool trans_a) {
+  SplitA a;
+  a.A = A;
+  a.lda = lda;
+  a.m = m;
+  a.k = k;
+  a.trans = trans_a ? 1 : 0;
+  a.rs = rs_of(k);
+  a.plane = (size_t)2 * m * a.rs;
+  a.P = planes;
+  return a;
+}
+SplitB split_b_args(const float2 *B, size_t ldb, int k, int n, __nv_bfloat16 *planes) {
+  SplitB b;
+  b.B = B;
+  b.ldb = ldb;
+  b.k = k;
+  b.n = n;
+  b.rs = rs_of(k);
+  b.plane = (size_t)n * b.rs;
+  b.P = planes;
+  return b;
+}
+int split_b_blocks(int k, int n) {
+  size_t blocks = ((size_t)k * n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  return (int)(blocks ? blocks : 1);
+}
+int check_ns(int nsplit) {
   if (nsplit < 1 || nsplit > 3) {
     set_error("nsplit %d not in 1..3", nsplit);
     return QPMS_EINVAL;
   }
-  const size_t rs = rs_of(k);
-  dim3 grid((m + 31) / 32, (k + 31) / 32), block(32, 8);
+  return QPMS_SUCCESS;
+}
+}  // namespace
+
+int tc_split_a(const float2 *A, size_t lda, int m, int k, int nsplit, __nv_bfloat16 *planes, cudaStream_t st,
+               bool trans_a) {
+  if (m <= 0 || k <= 0) return QPMS_SUCCESS;
+  int e;
+  if ((e = check_ns(nsplit))) return e;
+  dim3 grid((m + 31) / 32, (k + 31) / 32);
   KtScope kt(KT_SPLIT, st, 8.0 * nsplit * m * (double)k);
-  split_a_kernel<<<grid, block, 0, st>>>(A, lda, m, k, nsplit, rs, (size_t)2 * m * rs, trans_a ? 1 : 0, planes);
+  split_a_kernel<<<grid, 256, 0, st>>>(split_a_args(A, lda, m, k, planes, trans_a), nsplit);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(1);
   return QPMS_SUCCESS;
@@ -490,15 +557,24 @@ int tc_split_a(const float2 *A, size_t lda, int m, int k, int nsplit, __nv_bfloa
 
 int tc_split_b(const float2 *B, size_t ldb, int k, int n, int nsplit, __nv_bfloat16 *planes, cudaStream_t st) {
   if (n <= 0 || k <= 0) return QPMS_SUCCESS;
-  if (nsplit < 1 || nsplit > 3) {
-    set_error("nsplit %d not in 1..3", nsplit);
-    return QPMS_EINVAL;
-  }
-  const size_t rs = rs_of(k), total = (size_t)k * n;
-  size_t blocks = (total + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  int e;
+  if ((e = check_ns(nsplit))) return e;
   KtScope kt(KT_SPLIT, st, 4.0 * nsplit * n * (double)k);
-  split_b_kernel<<<(unsigned)blocks, 256, 0, st>>>(B, ldb, k, n, nsplit, rs, (size_t)n * rs, planes);
+  split_b_kernel<<<split_b_blocks(k, n), 256, 0, st>>>(split_b_args(B, ldb, k, n, planes), nsplit);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(1);
+  return QPMS_SUCCESS;
+}
+
+int tc_split_ab(const float2 *A, size_t lda, int m, int k, const float2 *B, size_t ldb, int n, int nsplit,
+                __nv_bfloat16 *a_planes, __nv_bfloat16 *b_planes, cudaStream_t st) {
+  if (m <= 0 || n <= 0 || k <= 0) return QPMS_SUCCESS;
+  int e;
+  if ((e = check_ns(nsplit))) return e;
+  const int na_x = (m + 31) / 32, na_y = (k + 31) / 32, nb = split_b_blocks(k, n);
+  KtScope kt(KT_SPLIT, st, 8.0 * nsplit * m * (double)k + 4.0 * nsplit * n * (double)k);
+  split_ab_kernel<<<na_x * na_y + nb, 256, 0, st>>>(split_a_args(A, lda, m, k, a_planes, false), na_x, na_y,
+                                                    split_b_args(B, ldb, k, n, b_planes), nb, nsplit);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(1);
   return QPMS_SUCCESS;

@@ -28,6 +28,9 @@ int tc_split_a(const float2 *A, size_t lda, int m, int k, int nsplit, __nv_bfloa
                bool trans_a = false);
 // Fill the B planes from complex64 B (k x n, column-major, ldb).
 int tc_split_b(const float2 *B, size_t ldb, int k, int n, int nsplit, __nv_bfloat16 *planes, cudaStream_t st);
+// Both operands of one product A (m x k) B (k x n) in one launch.
+int tc_split_ab(const float2 *A, size_t lda, int m, int k, const float2 *B, size_t ldb, int n, int nsplit,
+                __nv_bfloat16 *a_planes, __nv_bfloat16 *b_planes, cudaStream_t st);
 
 // D = beta C + alpha A B on complex64 column-major C, D (leading dimensions in
 // complex elements; C == D allowed, C unused when beta == 0) from the planes.
