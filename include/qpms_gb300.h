@@ -590,8 +590,13 @@ qpms_ss_LU qpms_scatsyswk_build_modeproblem_matrix_full_LU(qpms_complex_t *targe
  * LAT_2D_IN_3D short-range branch and the shifted long-range branch,
  * ewald.c:441-469, marked untested there; here derived anew and checked by
  * eta invariance and direct summation).  parts must be
- * QPMS_EWALD_FULL (7); maxR / maxK are not used (the kernel truncates where the
- * terms fall below e^-56 of the leading ones); Aerr / Berr are zero-filled. */
+ * QPMS_EWALD_FULL (7).  maxR / maxK bound the lattice-point layers as in the
+ * reference (PGen_xyWeb, latticegens.c:449-568): when those layers hold every
+ * point whose term is above ~1e-16 of the leading one the result is the full
+ * sum; a maxR / maxK that cuts into that region (a truncated sum) returns
+ * QPMS_EINVAL with a message.  Aerr / Berr (optional) receive
+ * |A(eta) - A(1.25 eta)| elementwise (B likewise): the eta-invariance of the
+ * full sum as an estimate of its evaluation error. */
 int qpms_trans_calculator_get_AB_arrays_e32(const qpms_trans_calculator *c,
     qpms_complex_t *Adest, double *Aerr, qpms_complex_t *Bdest, double *Berr,
     ptrdiff_t deststride, ptrdiff_t srcstride, double eta, qpms_complex_t wavenumber,

@@ -710,25 +710,136 @@ int qpms_gpu_periodic_scan(const qpms_scatsys_t *ss, size_t nw, const double *om
 }
 
 
+namespace {
+// ---- Lattice-point "web" of PGen_xyWeb (latticegens.c:449-568) ----
+// The reference enumerates the points of a 2D lattice in layers: in the
+// reduced basis (r1, r2) (lattices2d.c, l2d_reduceBasis), layer L holds the
+// points i r1 + j r2 with |i| + |j| = L for a rectangular basis and
+// max(|i|, |j|, |i + j|) = L otherwise; the layers 0 .. last are generated,
+// last = floor(maxR / h) (one less when last h == maxR), h the in-circle
+// radius of the unit hexagon (l2d_hexWebInCircleRadius).
+struct LatticeWeb {
+  double r1[2], r2[2];
+  bool rect;
+  long last;
+};
+
+double dot2(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1]; }
+
+void reduce_basis(const double *b1in, const double *b2in, double *o1, double *o2) {
+  double b1[2] = {b1in[0], b1in[1]}, b2[2] = {b2in[0], b2in[1]};
+  double B1 = dot2(b1, b1);
+  double mu = round(dot2(b1, b2) / B1);
+  b2[0] -= mu * b1[0];
+  b2[1] -= mu * b1[1];
+  double B2 = dot2(b2, b2);
+  for (int guard = 0; B2 < B1 && guard < 64; ++guard) {
+    std::swap(b1[0], b2[0]);
+    std::swap(b1[1], b2[1]);
+    B1 = B2;
+    mu = round(dot2(b1, b2) / B1);
+    b2[0] -= mu * b1[0];
+    b2[1] -= mu * b1[1];
+    B2 = dot2(b2, b2);
+  }
+  o1[0] = b1[0]; o1[1] = b1[1];
+  o2[0] = b2[0]; o2[1] = b2[1];
+}
+
+LatticeWeb lattice_web(const double *b1, const double *b2, double maxR) {
+  LatticeWeb w;
+  reduce_basis(b1, b2, w.r1, w.r2);
+  const double B1 = dot2(w.r1, w.r1), B2 = dot2(w.r2, w.r2);
+  const double d[2] = {w.r2[0] - w.r1[0], w.r2[1] - w.r1[1]};
+  w.rect = dot2(d, d) - B1 - B2 <= 1e-13 * (B1 + B2);  // l2d_detectRightAngles, BASIS_RTOL
+  // in-circle radius: the triangle (r1, r2, third side) with the third side
+  // r2 - r1, or r2 + r1 when the basis is obtuse; height onto the third side
+  double s3[2] = {d[0], d[1]}, s2[2] = {w.r2[0], w.r2[1]};
+  if (dot2(d, d) - B1 - B2 > 0) {
+    s3[0] = w.r2[0]; s3[1] = w.r2[1];
+    s2[0] = w.r2[0] + w.r1[0]; s2[1] = w.r2[1] + w.r1[1];
+  }
+  const double e1 = sqrt(B1), e2 = sqrt(dot2(s2, s2)), e3 = sqrt(dot2(s3, s3)), p = 0.5 * (e1 + e2 + e3);
+  const double h = 2 * sqrt(p * (p - e1) * (p - e2) * (p - e3)) / e3;
+  w.last = (maxR > 0 && h > 0) ? (long)floor(maxR / h) : -1;
+  if (w.last >= 0 && w.last * h >= maxR) --w.last;
+  return w;
+}
+
+// 1 if every lattice point p with |p - c| <= rad lies in the generated layers.
+bool web_covers(const LatticeWeb &w, double cx, double cy, double rad) {
+  const double det = w.r1[0] * w.r2[1] - w.r1[1] * w.r2[0];
+  if (det == 0 || !(rad >= 0)) return false;
+  // |i| <= (|c| + rad) |r2| / |det| (distance between the lines i = const)
+  const double reach = hypot(cx, cy) + rad;
+  const long I = (long)ceil(reach * sqrt(dot2(w.r2, w.r2)) / fabs(det)) + 1;
+  const long J = (long)ceil(reach * sqrt(dot2(w.r1, w.r1)) / fabs(det)) + 1;
+  if (I > 4096 || J > 4096) return false;
+  for (long i = -I; i <= I; ++i)
+    for (long j = -J; j <= J; ++j) {
+      const double px = i * w.r1[0] + j * w.r2[0] - cx, py = i * w.r1[1] + j * w.r2[1] - cy;
+      if (px * px + py * py > rad * rad) continue;
+      const long L = w.rect ? labs(i) + labs(j) : std::max(std::max(labs(i), labs(j)), labs(i + j));
+      if (L > w.last) return false;
+    }
+  return true;
+}
+}  // namespace
+
 // qpms_trans_calculator_get_AB_arrays_e32_e (translations.h:167-177,
 // translations.c:926-1078): the lattice-summed A, B for one Bloch vector and
 // particle shift.  Evaluated by the Ewald assembly kernel on a two-particle
 // cell (positions shift and 0) with T = -1, whose off-diagonal block is then
 // exactly W(shift) = [A B; B A].  Only the full sum is available (parts must
-// be QPMS_EWALD_FULL); the kernel's cutoffs are set by the exponential decay
-// of the terms (|R| eta <= 7.5, x^2 <= 56), so maxR / maxK are not used;
-// Aerr / Berr, if given, are zero-filled (no error estimate is formed).
+// be QPMS_EWALD_FULL).
+//
+// maxR / maxK: the reference sums the direct-lattice points R of the layers
+// below maxR and the reciprocal points K of the layers below maxK
+// (PGen_xyWeb, translations.c:960-1000).  The kernel's own cutoffs are set by
+// the decay of the terms (|R - s| eta <= 7.5, x^2 <= 56).  When the caller's
+// layers hold every point whose term is above ~1e-16 of the leading one
+// (|R - s| eta <= 6, (|K + beta|^2 - |k|^2) / (4 eta^2) <= 36) the two sums
+// agree to rounding; a maxR / maxK that cuts into that region asks for a
+// truncated sum, which is not available: QPMS_EINVAL with a message.
+//
+// Aerr / Berr (if given): |A(eta) - A(1.25 eta)| elementwise (and the same
+// for B), from a second evaluation in the same launch.  The full sum does not
+// depend on eta, so the difference measures the truncation and rounding error
+// of the evaluation (the reference propagates per-term quadrature and
+// incomplete-gamma error estimates instead, ewald.c:420-468, 880-882).
 int qpms_trans_calculator_get_AB_arrays_e32_e(const qpms_trans_calculator *c, qpms_complex_t *Adest, double *Aerr,
                                               qpms_complex_t *Bdest, double *Berr, ptrdiff_t deststride,
                                               ptrdiff_t srcstride, double eta, qpms_complex_t wavenumber,
                                               cart2_t b1, cart2_t b2, cart2_t beta, cart3_t particle_shift,
                                               double maxR, double maxK, int parts) {
-  (void)maxR;
-  (void)maxK;
   clear_error();
   if (!c || !Adest || !Bdest) { set_error("NULL argument"); return QPMS_EINVAL; }
   if (parts != 7) { set_error("only the full Ewald sum (QPMS_EWALD_FULL) is implemented"); return QPMS_EINVAL; }
   if (c->lMax > 4) { set_error("lattice sums need lMax <= 4"); return QPMS_EINVAL; }
+  if (!(eta > 0)) { set_error("eta must be positive"); return QPMS_EINVAL; }
+  const double bb1[2] = {b1.x, b1.y}, bb2[2] = {b2.x, b2.y};
+  {
+    if (fabs(bb1[0] * bb2[1] - bb1[1] * bb2[0]) <= 1e-13 * (dot2(bb1, bb1) + dot2(bb2, bb2))) {
+      set_error("degenerate lattice basis");
+      return QPMS_EINVAL;
+    }
+    const double z2 = particle_shift.z * particle_shift.z, rs = 6.0 / eta;
+    const double rad_R = rs * rs > z2 ? sqrt(rs * rs - z2) : -1.0;
+    const double det = bb1[0] * bb2[1] - bb1[1] * bb2[0];
+    const double rk1[2] = {2 * M_PI * bb2[1] / det, -2 * M_PI * bb2[0] / det};
+    const double rk2[2] = {-2 * M_PI * bb1[1] / det, 2 * M_PI * bb1[0] / det};
+    const double k2 = wavenumber.re * wavenumber.re + wavenumber.im * wavenumber.im;
+    const double rad_K = sqrt(k2 + 36.0 * 4 * eta * eta);
+    const bool r_ok = rad_R < 0 || web_covers(lattice_web(bb1, bb2, maxR), particle_shift.x, particle_shift.y, rad_R);
+    const bool k_ok = web_covers(lattice_web(rk1, rk2, maxK), -beta.x, -beta.y, rad_K);
+    if (!r_ok || !k_ok) {
+      set_error("%s truncates the lattice sum where its terms are above 1e-16 of the leading ones "
+                "(needs %s >= about %.6g); truncated sums are not available",
+                r_ok ? "maxK" : "maxR", r_ok ? "maxK" : "maxR",
+                r_ok ? rad_K + hypot(beta.x, beta.y) : rad_R + hypot(particle_shift.x, particle_shift.y));
+      return QPMS_EINVAL;
+    }
+  }
   const double pos[6] = {particle_shift.x, particle_shift.y, particle_shift.z, 0, 0, 0};
   const int kind[2] = {0, 0};
   const double rad = 1.0;
@@ -737,22 +848,24 @@ int qpms_trans_calculator_get_AB_arrays_e32_e(const qpms_trans_calculator *c, qp
   eps_in.im = 0;
   eps_med.re = 1.0;
   eps_med.im = 0;
-  const double bb1[2] = {b1.x, b1.y}, bb2[2] = {b2.x, b2.y};
   qpms_scatsys_t *ss = qpms_gpu_scatsys_create_spheres_2d(2, pos, kind, 1, &rad, &eps_in, eps_med, c->lMax, bb1, bb2);
   if (!ss) return QPMS_ERROR;
   qpms_trans_calculator *own = ss->c;
   ss->c = const_cast<qpms_trans_calculator *>(c);  // the caller's normalisation and tables
   const int ne = c->nelem, n = 2 * ne, N = 2 * n;
+  const bool doerr = Aerr || Berr;
+  const int nk = doerr ? 2 : 1;  // (beta, eta) and, for the error estimate, (beta, 1.25 eta)
   std::vector<qg_c> T(n, cmk(-1.0, 0.0));
   const qg_c k = cmk(wavenumber.re, wavenumber.im);
-  const double bt[2] = {beta.x, beta.y};
+  const double bt[4] = {beta.x, beta.y, beta.x, beta.y};
+  const double etas[2] = {eta, 1.25 * eta};
   int e = QPMS_SUCCESS;
-  std::vector<qg_c> M((size_t)N * N);
+  std::vector<qg_c> M((size_t)nk * N * N);
   {
     Dev dM;
-    if (!(e = dalloc(dM, (size_t)N * N * 16)))
-      if (!(e = periodic_assemble_device(ss, 1, &k, T, 1, bt, &eta, dM.as<qg_c>(), 0)))
-        if (cudaMemcpy(M.data(), dM.p, (size_t)N * N * 16, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    if (!(e = dalloc(dM, M.size() * 16)))
+      if (!(e = periodic_assemble_device(ss, 1, &k, T, nk, bt, etas, dM.as<qg_c>(), 0)))
+        if (cudaMemcpy(M.data(), dM.p, M.size() * 16, cudaMemcpyDeviceToHost) != cudaSuccess) {
           set_error("device to host copy failed");
           e = QPMS_ERROR;
         }
@@ -761,15 +874,17 @@ int qpms_trans_calculator_get_AB_arrays_e32_e(const qpms_trans_calculator *c, qp
   qpms_gpu_scatsys_free(ss);
   if (e) return e;
   // block (particle 0 <- particle 1): rows 0..n-1, columns n..2n-1
+  const qg_c *M2 = M.data() + (size_t)(nk - 1) * N * N;
   for (int y = 0; y < ne; ++y)
     for (int yu = 0; yu < ne; ++yu) {
-      const qg_c a = M[(size_t)y * N + n + yu], b = M[(size_t)y * N + n + ne + yu];
+      const size_t ia = (size_t)y * N + n + yu, ib = ia + ne;
+      const qg_c a = M[ia], b = M[ib];
       Adest[deststride * y + srcstride * yu].re = a.re;
       Adest[deststride * y + srcstride * yu].im = a.im;
       Bdest[deststride * y + srcstride * yu].re = b.re;
       Bdest[deststride * y + srcstride * yu].im = b.im;
-      if (Aerr) Aerr[deststride * y + srcstride * yu] = 0;
-      if (Berr) Berr[deststride * y + srcstride * yu] = 0;
+      if (Aerr) Aerr[deststride * y + srcstride * yu] = hypot(a.re - M2[ia].re, a.im - M2[ia].im);
+      if (Berr) Berr[deststride * y + srcstride * yu] = hypot(b.re - M2[ib].re, b.im - M2[ib].im);
     }
   return QPMS_SUCCESS;
 }

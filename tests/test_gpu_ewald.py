@@ -268,3 +268,57 @@ def test_symmetry_from_reference_group_object(gpu):
     grp = FG(b"D4h", 16)
     assert L.qpms_gpu_scatsys_set_symmetry_group(ss.s, C.byref(grp)) == 0, gpu.last_error()
     assert ss.nirreps == 10
+
+
+def test_AB_arrays_e32_cutoffs_and_error_estimate(gpu, orc):
+    """The caller's maxR / maxK (translations.c:960-1000: PGen_xyWeb layers,
+    latticegens.c:449-568).  Unit square lattice, eta 1.6, shift (0.5,
+    0.1325): the points with |R - s| eta <= 6 reach the diamond layer
+    |i| + |j| = 5, of height 5 / sqrt(2) = 3.536, so maxR 3.6 keeps the full
+    sum (matching the oracle's sum over those layers) and maxR 3.5 asks for a
+    truncated one (QPMS_EINVAL).  Aerr / Berr hold |A(eta) - A(1.25 eta)|."""
+    import ctypes as C
+
+    class Cplx(C.Structure):
+        _fields_ = [("re", C.c_double), ("im", C.c_double)]
+
+    class Cart2(C.Structure):
+        _fields_ = [("x", C.c_double), ("y", C.c_double)]
+
+    class Cart3(C.Structure):
+        _fields_ = [("x", C.c_double), ("y", C.c_double), ("z", C.c_double)]
+
+    L = C.CDLL(gpu.lib()._name)  # private handle: argtypes set here stay out of the package's
+    f = L.qpms_trans_calculator_get_AB_arrays_e32
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_ssize_t, C.c_ssize_t, C.c_double,
+                  Cplx, Cart2, Cart2, Cart2, Cart3, C.c_double, C.c_double]
+    lMax, ne = 3, 15
+    calc = gpu.trans_calculator(lMax)
+    oc = orc.TransCalculator(lMax)
+    beta, shift = (2.7, 1.0), (0.5, 0.1325, 0.0)
+
+    def run(maxR, maxK, err=False):
+        A = np.zeros((ne, ne), dtype=np.complex128)
+        B = np.zeros_like(A)
+        Ae = np.full((ne, ne), np.nan) if err else None
+        Be = np.full((ne, ne), np.nan) if err else None
+        rc = f(calc.c, A.ctypes.data, None if Ae is None else Ae.ctypes.data, B.ctypes.data,
+               None if Be is None else Be.ctypes.data, ne, 1, 1.6, Cplx(2.3, 0.0), Cart2(1, 0), Cart2(0, 1),
+               Cart2(*beta), Cart3(*shift), maxR, maxK)
+        return rc, A, B, Ae, Be
+
+    rc, A, B, Ae, Be = run(3.6, 160.0, err=True)
+    assert rc == 0, gpu.last_error()
+    Ao, Bo = orc.get_AB_arrays_e32(oc, 1.6, 2.3, (1, 0), (0, 1), beta, shift, 3.6, 160)
+    assert np.linalg.norm(A - Ao) <= 1e-11 * np.linalg.norm(Ao)
+    assert np.linalg.norm(B - Bo) <= 1e-11 * np.linalg.norm(Bo)
+    for G, E in ((A, Ae), (B, Be)):
+        assert np.all(np.isfinite(E)) and np.all(E >= 0)
+        assert E.max() <= 1e-10 * np.abs(G).max()
+    assert Ae.max() > 0  # a second evaluation, not a zero fill
+    rc, *_ = run(3.5, 160.0)
+    assert rc == 22 and "maxR" in gpu.last_error()
+    # |K + beta|^2 - |k|^2 <= 36 (2 eta)^2 reaches |K| ~ 22.8: maxK 10 truncates
+    rc, *_ = run(20.0, 10.0)
+    assert rc == 22 and "maxK" in gpu.last_error()
