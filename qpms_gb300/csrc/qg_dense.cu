@@ -10,16 +10,20 @@
 //      Herrmann, Tomov, "Accelerating linear system solutions using
 //      randomization techniques", ACM TOMS 39 (2013)), after which Gaussian
 //      elimination without pivoting is stable with high probability;
-//   2. factorises A' = L U without pivoting by blocks: an nb x nb diagonal
-//      block is factored and its triangular factors inverted in shared memory
-//      by one CTA; the panels below and to the right and the trailing update are
-//      then GEMMs (cuBLAS, tensor cores);
-//   3. solves by blocked forward/back substitution (GEMMs with the inverted
-//      diagonal blocks);
+//   2. factorises A' without pivoting by blocks in Schur-complement form: at
+//      step k the nb x nb diagonal block D is inverted by one CTA
+//      (Gauss-Jordan in registers), the whole column block k is multiplied
+//      by D^-1 (below the block this is P = A21 D^-1, above it
+//      Q = A_0:k,k D^-1, the block itself becomes I - D^-1) and the trailing
+//      matrix is updated, A22 -= P A12, with the row panel A12 kept as it is;
+//      A' = L U with L = [I 0; P I] (per level) and U = [D A12; 0 S];
+//   3. solves with two sweeps of one product per block: forward
+//      b_below -= P_k b_k, backward b_0:k+kb -= [Q_k; I - D_k^-1] b_k (which
+//      leaves D_k^-1 b_k, the block's solution, in b_k);
 //   4. in the mixed mode, the factorisation and substitutions run in complex64
-//      (GEMMs with FP32-accurate BF16x9 emulation on the tensor cores) and the
-//      FP64 solution is recovered by iterative refinement against the FP64
-//      matrix: x += W_v (LU)^-1 W_u^T (b - M x), residual in FP64.
+//      (products on the tensor cores, qg_tcgemm.cu) and the FP64 solution is
+//      recovered by iterative refinement against the FP64 matrix:
+//      x += W_v (LU)^-1 W_u^T (b - M x), residual in FP64.
 // The plain mode runs steps 1-3 in complex128 (FP64 GEMMs).
 // All matrices are column-major (LAPACK order).  The butterflies halve the
 // system twice, so it is padded internally to a multiple of 4 with identity.
@@ -29,6 +33,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <mutex>
 #include <random>
 #include <vector>
 
@@ -79,155 +84,138 @@ __device__ __forceinline__ T rcp(T b) {
   return mk<T>(b.x / d, -b.y / d);
 }
 
-// ---------------- diagonal block: LU without pivoting + triangular inverses ----------------
-// D (kb x kb, kb <= 128 and a multiple of 32 except for the last block,
-// column-major in global, leading dimension lda) is factored in place
-// (unit-lower L below the diagonal, U on and above); L^-1 and U^-1 are written
-// to Linv and Uinv (column-major kb x kb each).  info is set to 1 on an
-// exactly zero pivot.  One CTA of 1024 threads with the block in shared
-// memory:
-//   1. right-looking elimination, a 32 x 32 thread tile sweeping the trailing
-//      matrix of each step (no index division);
-//   2. the inverses by recursive doubling: each 32 x 32 diagonal block is
-//      inverted by one warp (substitution with warp barriers only), then
-//      adjacent blocks are combined level by level,
-//        [L11 0; L21 L22]^-1 = [X11 0; -X22 L21 X11  X22],
-//        [U11 U12; 0 U22]^-1 = [Y11 -Y11 U12 Y22; 0 Y22],
-//      as two small products per level through a shared-memory temporary.
-// The unit diagonal of L^-1 is implicit in shared memory (the slot holds U^-1).
-// Capacity of each doubling temporary: npair * h^2 <= 4096 for every block size
-// kb <= 128 the solver uses (h = 32: at most 2 pairs; h = 64: one pair).
-constexpr int kDiagTmp = 4096;
+// ---------------- diagonal block: inverse by Gauss-Jordan ----------------
+// D (kb x kb, kb <= 32 NA, column-major in global, leading dimension lda):
+// Ainv (column-major kb x kb, leading dimension kb) receives D^-1, and D is
+// overwritten with D - I (the column-block product that follows turns it into
+// I - D^-1, the slot the back substitution reads).  info is set to 1 on an
+// exactly zero pivot.  Gauss-Jordan elimination without pivoting (the random
+// butterflies make it safe with high probability, as for the whole LU).  One
+// CTA of kDiagWarps warps with the block in registers: thread (lane, warp)
+// holds the NA x NB elements (lane + 32 i, warp + kDiagWarps j), so column c
+// lives in warp c % kDiagWarps and row r in lane r % 32 of every warp.  At
+// step j the lanes of row j publish the row and the warp of column j the
+// column (two alternating shared-memory slots, so one barrier per step);
+// every thread then forms the pivot's reciprocal itself and updates its
+// elements:
+//   a_jj <- 1/p,  a_jc <- a_jc / p,  a_rj <- -a_rj / p,
+//   a_rc <- a_rc - a_rj a_jc / p  (r, c != j).
+constexpr int kDiagMaxNb = 128, kDiagWarps = 16;
 
 template <typename T>
 __device__ __forceinline__ T fma_c(T acc, T a, T b) {  // acc + a b
   return mk<T>(acc.x + a.x * b.x - a.y * b.y, acc.y + a.x * b.y + a.y * b.x);
 }
-
 template <typename T>
-__global__ void __launch_bounds__(1024) diag_lu_inv_kernel(T *D, size_t lda, int kb, T *Linv, T *Uinv, int *info) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  T *S = reinterpret_cast<T *>(sm);  // [kb][kb] column-major: S[c * kb + r]
-  T *TL = S + kb * kb;               // temporaries of the doubling products (kDiagTmp entries each)
-  T *TU = TL + kDiagTmp;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int lane = tid & 31, warp = tid >> 5;
-  for (int t = tid; t < kb * kb; t += nt) {
-    const int c = t / kb, r = t - c * kb;
-    S[t] = D[(size_t)c * lda + r];
-  }
-  __syncthreads();
-  // ---- 1. elimination ----
-  for (int j = 0; j < kb; ++j) {
-    const T d = S[j * kb + j];
-    const bool zero = (d.x == 0 && d.y == 0);
-    if (zero && tid == 0) atomicOr(info, 1);
-    const T inv = zero ? mk<T>(0, 0) : rcp(d);
-    if (tid > j && tid < kb) S[j * kb + tid] = mul(S[j * kb + tid], inv);
-    __syncthreads();
-    for (int c = j + 1 + warp; c < kb; c += 32) {
-      const T u = S[c * kb + j];
-      for (int r = j + 1 + lane; r < kb; r += 32) S[c * kb + r] = sub(S[c * kb + r], mul(S[j * kb + r], u));
-    }
-    __syncthreads();
-  }
-  for (int t = tid; t < kb * kb; t += nt) {
-    const int c = t / kb, r = t - c * kb;
-    D[(size_t)c * lda + r] = S[t];
-  }
-  // ---- 2a. 32 x 32 diagonal blocks, one warp each: warps [0, nblk) L, [16, 16 + nblk) U ----
-  const int nb32 = (kb + 31) / 32;
-  if (warp < nb32 || (warp >= 16 && warp < 16 + nb32)) {
-    const bool isL = warp < 16;
-    const int o = (isL ? warp : warp - 16) * 32;
-    const int s = min(32, kb - o);  // block size (the last block may be short)
-    const int i = lane;
-    if (isL) {
-      // X(i, j) = -(L(i, j) + sum_{j<k<i} X(i, k) L(k, j)), columns from the right
-      for (int j = s - 2; j >= 0; --j) {
-        T acc = mk<T>(0, 0);
-        if (i > j && i < s) {
-          acc = S[(o + j) * kb + o + i];
-          for (int k = j + 1; k < i; ++k) acc = fma_c(acc, S[(o + k) * kb + o + i], S[(o + j) * kb + o + k]);
-        }
-        __syncwarp();
-        if (i > j && i < s) S[(o + j) * kb + o + i] = mk<T>(-acc.x, -acc.y);
-        __syncwarp();
-      }
-    } else {
-      // Y(j, j) = 1 / U(j, j); Y(i, j) = -(sum_{i<=k<j} Y(i, k) U(k, j)) Y(j, j), columns from the left
-      for (int j = 0; j < s; ++j) {
-        const T u = S[(o + j) * kb + o + j];
-        const T dj = (u.x == 0 && u.y == 0) ? mk<T>(0, 0) : rcp(u);
-        T acc = mk<T>(0, 0);
-        if (i < j) {
-          for (int k = i; k < j; ++k) {
-            const T yik = (k == i) ? S[(o + i) * kb + o + i] : S[(o + k) * kb + o + i];
-            acc = fma_c(acc, yik, S[(o + j) * kb + o + k]);
-          }
-        }
-        __syncwarp();
-        if (i < j) S[(o + j) * kb + o + i] = mk<T>(-(acc.x * dj.x - acc.y * dj.y), -(acc.x * dj.y + acc.y * dj.x));
-        if (i == j) S[(o + j) * kb + o + j] = dj;
-        __syncwarp();
-      }
-    }
-  }
-  __syncthreads();
-  // ---- 2b. doubling: blocks of size h are combined into blocks of size 2h ----
-  for (int h = 32; h < kb; h *= 2) {
-    const int npair = kb / (2 * h) + ((kb % (2 * h)) > h ? 1 : 0);
-    // products 1: TL = L21 X11, TU = U12 Y22 (h2 = rows / cols of the second block)
-    for (int t = tid; t < 2 * npair * h * h; t += nt) {
-      const bool isL = t < npair * h * h;
-      const int tt = isL ? t : t - npair * h * h;
-      const int p = tt / (h * h), e = tt - p * h * h, r = e % h, c = e / h;
-      const int o = p * 2 * h, h2 = min(h, kb - o - h);
-      if (r >= h2 && isL) continue;   // rows of L21 beyond the short block
-      if (c >= h2 && !isL) continue;  // columns of U12 beyond the short block
-      T acc = mk<T>(0, 0);
-      if (isL) {  // T(r, c) = sum_{k >= c} L21(r, k) X11(k, c), X11(c, c) = 1
-        acc = S[(o + c) * kb + o + h + r];
-        for (int k = c + 1; k < h; ++k) acc = fma_c(acc, S[(o + k) * kb + o + h + r], S[(o + c) * kb + o + k]);
-        TL[p * h * h + c * h + r] = acc;
-      } else {    // T(r, c) = sum_{k <= c} U12(r, k) Y22(k, c)
-        for (int k = 0; k <= c; ++k) acc = fma_c(acc, S[(o + h + k) * kb + o + r], S[(o + h + c) * kb + o + h + k]);
-        TU[p * h * h + c * h + r] = acc;
-      }
-    }
-    __syncthreads();
-    // products 2: X21 = -X22 TL, Y12 = -Y11 TU, written over L21 / U12
-    for (int t = tid; t < 2 * npair * h * h; t += nt) {
-      const bool isL = t < npair * h * h;
-      const int tt = isL ? t : t - npair * h * h;
-      const int p = tt / (h * h), e = tt - p * h * h, r = e % h, c = e / h;
-      const int o = p * 2 * h, h2 = min(h, kb - o - h);
-      T acc = mk<T>(0, 0);
-      if (isL) {  // X21(r, c) = -(T(r, c) + sum_{k < r} X22(r, k) T(k, c)), X22 unit lower
-        if (r >= h2) continue;
-        acc = TL[p * h * h + c * h + r];
-        for (int k = 0; k < r; ++k) acc = fma_c(acc, S[(o + h + k) * kb + o + h + r], TL[p * h * h + c * h + k]);
-        S[(o + c) * kb + o + h + r] = mk<T>(-acc.x, -acc.y);
-      } else {    // Y12(r, c) = -sum_{k >= r} Y11(r, k) T(k, c)
-        if (c >= h2) continue;
-        for (int k = r; k < h; ++k) acc = fma_c(acc, S[(o + k) * kb + o + r], TU[p * h * h + c * h + k]);
-        S[(o + h + c) * kb + o + r] = mk<T>(-acc.x, -acc.y);
-      }
-    }
-    __syncthreads();
-  }
-  for (int t = tid; t < kb * kb; t += nt) {
-    const int c = t / kb, r = t - c * kb;
-    const T v = S[t];
-    Linv[t] = r > c ? v : (r == c ? mk<T>(1, 0) : mk<T>(0, 0));
-    Uinv[t] = r <= c ? v : mk<T>(0, 0);
-  }
+__device__ __forceinline__ T fms_c(T acc, T a, T b) {  // acc - a b
+  return mk<T>(acc.x - (a.x * b.x - a.y * b.y), acc.y - (a.x * b.y + a.y * b.x));
 }
 
-// shared memory of diag_lu_inv_kernel for block size kb
+template <typename T, int NA>
+__global__ void __launch_bounds__(32 * kDiagWarps, 1) diag_inv_kernel(T *D, size_t lda, int kb, T *Ainv, int *info) {
+  constexpr int NB = 32 * NA / kDiagWarps;  // = 2 NA: column tiles per thread
+  static_assert(kDiagWarps == 16, "the step loop splits 32 rows into two halves of 16 columns");
+  __shared__ T sc[2 * kDiagMaxNb];  // column j, alternating slots
+  __shared__ T sr[2 * kDiagMaxNb];  // row j
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T a[NA][NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j)
+#pragma unroll
+    for (int i = 0; i < NA; ++i) {
+      const int r = lane + 32 * i, c = w + kDiagWarps * j;
+      a[i][j] = mk<T>(0, 0);
+      if (r < kb && c < kb) {
+        T v = D[(size_t)c * lda + r];
+        a[i][j] = v;
+        if (r == c) v.x -= 1;
+        D[(size_t)c * lda + r] = v;
+      }
+    }
+  bool zero = false;
+  // Step j = 32 jt + 16 h + q: row j is tile row jt of lane 16 h + q, column j
+  // tile column 2 jt + h of warp q; jt and h are unrolled, so every register
+  // index is static.
+#pragma unroll
+  for (int jt = 0; jt < NA; ++jt) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int ct = 2 * jt + h;
+      for (int q = 0; q < 16; ++q) {
+        const int j = 32 * jt + 16 * h + q;
+        if (j >= kb) break;  // uniform
+        const int rl = 16 * h + q, buf = (j & 1) * kDiagMaxNb;
+        if (lane == rl) {
+#pragma unroll
+          for (int jj = 0; jj < NB; ++jj) {
+            const int c = w + kDiagWarps * jj;
+            if (c < kb) sr[buf + c] = a[jt][jj];
+          }
+        }
+        if (w == q) {
+#pragma unroll
+          for (int i = 0; i < NA; ++i) {
+            const int r = lane + 32 * i;
+            if (r < kb) sc[buf + r] = a[i][ct];
+          }
+        }
+        __syncthreads();
+        const T p = sc[buf + j];
+        const bool z = (p.x == 0 && p.y == 0);
+        zero |= z;
+        const T pinv = z ? mk<T>(0, 0) : rcp(p);
+        T f[NA];
+#pragma unroll
+        for (int i = 0; i < NA; ++i) f[i] = (32 * i < kb) ? sc[buf + min(lane + 32 * i, kb - 1)] : mk<T>(0, 0);
+        // every element: a_rc -= a_rj a_jc / p (row j and column j become 0
+        // here and are set right after)
+#pragma unroll
+        for (int jj = 0; jj < NB; ++jj) {
+          const int c = w + kDiagWarps * jj;
+          if (c >= kb) continue;  // warp-uniform
+          const T u = mul(sr[buf + c], pinv);  // a_jc / p
+#pragma unroll
+          for (int i = 0; i < NA; ++i) {
+            if (32 * i >= kb) continue;  // uniform
+            a[i][jj] = fms_c(a[i][jj], f[i], u);
+          }
+          if (lane == rl) a[jt][jj] = u;  // row j: a_jc / p
+        }
+        if (w == q) {  // column j: -a_rj / p, the pivot 1 / p
+#pragma unroll
+          for (int i = 0; i < NA; ++i) a[i][ct] = mk<T>(-(f[i].x * pinv.x - f[i].y * pinv.y),
+                                                        -(f[i].x * pinv.y + f[i].y * pinv.x));
+          if (lane == rl) a[jt][ct] = pinv;
+        }
+      }
+    }
+  }
+  if (zero && threadIdx.x == 0) atomicOr(info, 1);
+#pragma unroll
+  for (int j = 0; j < NB; ++j)
+#pragma unroll
+    for (int i = 0; i < NA; ++i) {
+      const int r = lane + 32 * i, c = w + kDiagWarps * j;
+      if (r < kb && c < kb) Ainv[c * kb + r] = a[i][j];
+    }
+}
+
+// Invert one diagonal block (kb <= 128; complex128 blocks up to 64).
 template <typename T>
-size_t diag_smem(int kb) {
-  return ((size_t)kb * kb + 2 * (size_t)kDiagTmp) * sizeof(T);
+int launch_diag(T *D, size_t lda, int kb, T *Ainv, int *info, cudaStream_t st) {
+  constexpr int kMaxNa = sizeof(T) == 16 ? 2 : 4;  // complex128 blocks: nb <= 64
+  if (kb <= 0 || kb > 32 * kMaxNa) {
+    set_error("diagonal block of size %d not supported", kb);
+    return QPMS_EINVAL;
+  }
+  KtScope kt(KT_DIAGLU, st, 8.0 * kb * (double)kb * kb);
+  if (kb <= 64)
+    diag_inv_kernel<T, 2><<<1, 32 * kDiagWarps, 0, st>>>(D, lda, kb, Ainv, info);
+  else
+    diag_inv_kernel<T, kMaxNa><<<1, 32 * kDiagWarps, 0, st>>>(D, lda, kb, Ainv, info);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(1);
+  return QPMS_SUCCESS;
 }
 
 // ---------------- random butterfly transforms (FP64) ----------------
@@ -339,64 +327,56 @@ T cval(double r) {
   return z;
 }
 
-// LU without pivoting, blocked (see the header comment).
+// Blocked LU without pivoting in Schur-complement form (see the header
+// comment).  Step k with the diagonal block D = A_kk, kb columns:
+//   Ainv = D^-1 (diag_inv_kernel, which also leaves D - I in the slot);
+//   column block k (all N rows) <- column block k x Ainv: the rows below the
+//     block become P_k = A21 D^-1, the block itself I - D^-1, the rows above
+//     Q_k = A_0:k,k D^-1;
+//   A22 -= P_k A12 (A12: the row panel right of the block, kept as it is).
 template <typename T>
 int lu_nopiv(cublasHandle_t h, int N, int nb, T *A, size_t lda, T *Dinv, T *work, int *dinfo,
              cublasComputeType_t ct, cudaStream_t st) {
-  const size_t smem = diag_smem<T>(nb);
-  QG_CUDA_TRY(cudaFuncSetAttribute(diag_lu_inv_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int e;
+  const cublasComputeType_t cp = (sizeof(T) == 8) ? CUBLAS_COMPUTE_32F : CUBLAS_COMPUTE_64F;  // column blocks
   for (int k = 0, blk = 0; k < N; k += nb, ++blk) {
     const int kb = (N - k < nb) ? N - k : nb;
-    T *Lk = Dinv + (size_t)blk * 2 * nb * nb, *Uk = Lk + (size_t)nb * nb;
-    diag_lu_inv_kernel<T><<<1, 1024, diag_smem<T>(kb), st>>>(A + (size_t)k * lda + k, lda, kb, Lk, Uk, dinfo);
-    QG_CUDA_TRY(cudaGetLastError());
-    g_launches.fetch_add(1);
+    T *Ainv = Dinv + (size_t)blk * nb * nb, *Ck = A + (size_t)k * lda;
+    if ((e = launch_diag<T>(Ck + k, lda, kb, Ainv, dinfo, st))) return e;
+    if ((e = gemm<T>(h, N, kb, kb, cone<T>(), Ck, lda, Ainv, kb, cval<T>(0), work, N, cp))) return e;
+    QG_CUDA_TRY(cudaMemcpy2DAsync(Ck, lda * sizeof(T), work, (size_t)N * sizeof(T), (size_t)N * sizeof(T), kb,
+                                  cudaMemcpyDeviceToDevice, st));
     const int m2 = N - k - kb;
     if (m2 <= 0) break;
-    T *A21 = A + (size_t)k * lda + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = A21 + (size_t)kb * lda;
-    int e;
-    // L21 = A21 Uinv   (m2 x kb)
-    const cublasComputeType_t cp = (sizeof(T) == 8) ? CUBLAS_COMPUTE_32F : CUBLAS_COMPUTE_64F;  // panels
-    if ((e = gemm<T>(h, m2, kb, kb, cone<T>(), A21, lda, Uk, kb, cval<T>(0), work, m2, cp))) return e;
-    QG_CUDA_TRY(cudaMemcpy2DAsync(A21, lda * sizeof(T), work, (size_t)m2 * sizeof(T), (size_t)m2 * sizeof(T), kb,
-                                  cudaMemcpyDeviceToDevice, st));
-    // U12 = Linv A12   (kb x m2)
-    if ((e = gemm<T>(h, kb, m2, kb, cone<T>(), Lk, kb, A12, lda, cval<T>(0), work, kb, cp))) return e;
-    QG_CUDA_TRY(cudaMemcpy2DAsync(A12, lda * sizeof(T), work, (size_t)kb * sizeof(T), (size_t)kb * sizeof(T), m2,
-                                  cudaMemcpyDeviceToDevice, st));
-    // A22 -= L21 U12
-    if ((e = gemm<T>(h, m2, m2, kb, cval<T>(-1), A21, lda, A12, lda, cone<T>(), A22, lda, ct))) return e;
+    T *P = Ck + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = P + (size_t)kb * lda;
+    if ((e = gemm<T>(h, m2, m2, kb, cval<T>(-1), P, lda, A12, lda, cone<T>(), A22, lda, ct))) return e;
   }
   return QPMS_SUCCESS;
 }
 
-// Solve (L U) X = B in place (B: N x nrhs, column-major, ldb).
+// Solve with the factors of lu_nopiv (B: N x nrhs, column-major, ldb, in place):
+//   forward, k ascending:   B_k+kb:N -= P_k B_k
+//   backward, k descending: B_0:k+kb -= [Q_k; I - D_k^-1] B_k
+// (the block rows of the second product leave D_k^-1 B_k in B_k).  B_k is
+// copied to `work` first where the product writes over it.
 template <typename T>
-int lu_solve(cublasHandle_t h, int N, int nb, const T *A, size_t lda, const T *Dinv, T *B, size_t ldb, int nrhs,
-             T *work, cublasComputeType_t ct, cudaStream_t st) {
+int lu_solve(cublasHandle_t h, int N, int nb, const T *A, size_t lda, T *B, size_t ldb, int nrhs, T *work,
+             cublasComputeType_t ct, cudaStream_t st) {
   int e;
   const int nblk = (N + nb - 1) / nb;
-  for (int blk = 0; blk < nblk; ++blk) {  // forward: L y = b
-    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
-    const T *Lk = Dinv + (size_t)blk * 2 * nb * nb;
-    if ((e = gemm<T>(h, kb, nrhs, kb, cone<T>(), Lk, kb, B + k, ldb, cval<T>(0), work, kb, ct))) return e;
-    QG_CUDA_TRY(cudaMemcpy2DAsync(B + k, ldb * sizeof(T), work, (size_t)kb * sizeof(T), (size_t)kb * sizeof(T), nrhs,
-                                  cudaMemcpyDeviceToDevice, st));
-    const int m2 = N - k - kb;
+  for (int blk = 0; blk < nblk; ++blk) {
+    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb, m2 = N - k - kb;
     if (m2 > 0)
       if ((e = gemm<T>(h, m2, nrhs, kb, cval<T>(-1), A + (size_t)k * lda + k + kb, lda, B + k, ldb, cone<T>(),
                        B + k + kb, ldb, ct)))
         return e;
   }
-  for (int blk = nblk - 1; blk >= 0; --blk) {  // backward: U x = y
+  for (int blk = nblk - 1; blk >= 0; --blk) {
     const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
-    const T *Uk = Dinv + (size_t)blk * 2 * nb * nb + (size_t)nb * nb;
-    if ((e = gemm<T>(h, kb, nrhs, kb, cone<T>(), Uk, kb, B + k, ldb, cval<T>(0), work, kb, ct))) return e;
-    QG_CUDA_TRY(cudaMemcpy2DAsync(B + k, ldb * sizeof(T), work, (size_t)kb * sizeof(T), (size_t)kb * sizeof(T), nrhs,
+    QG_CUDA_TRY(cudaMemcpy2DAsync(work, (size_t)kb * sizeof(T), B + k, ldb * sizeof(T), (size_t)kb * sizeof(T), nrhs,
                                   cudaMemcpyDeviceToDevice, st));
-    if (k > 0)
-      if ((e = gemm<T>(h, k, nrhs, kb, cval<T>(-1), A + (size_t)k * lda, lda, B + k, ldb, cone<T>(), B, ldb, ct)))
-        return e;
+    if ((e = gemm<T>(h, k + kb, nrhs, kb, cval<T>(-1), A + (size_t)k * lda, lda, work, kb, cone<T>(), B, ldb, ct)))
+      return e;
   }
   return QPMS_SUCCESS;
 }
@@ -405,13 +385,9 @@ int lu_solve(cublasHandle_t h, int N, int nb, const T *A, size_t lda, const T *D
 // The same blocked algorithm as lu_nopiv / lu_solve with every product a
 // tcgen05 GEMM of split-bf16 digits (qg_tcgemm.cu): operands are cut into
 // digit planes first, so each GEMM may write its result over an operand it
-// read (the panels L21 = A21 U^-1, U12 = L^-1 A12 and the right-hand-side
-// blocks are formed in place).
+// read (the column blocks and the right-hand-side blocks are formed in place).
 int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, int nsplit, __nv_bfloat16 *pa,
                 __nv_bfloat16 *pb, cudaStream_t st) {
-  const size_t smem = diag_smem<float2>(nb);
-  QG_CUDA_TRY(
-      cudaFuncSetAttribute(diag_lu_inv_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   TcPlanes P;
   P.a = pa;
   P.b = pb;
@@ -419,63 +395,43 @@ int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, 
   int e;
   for (int k = 0, blk = 0; k < N; k += nb, ++blk) {
     const int kb = (N - k < nb) ? N - k : nb;
-    float2 *Lk = Dinv + (size_t)blk * 2 * nb * nb, *Uk = Lk + (size_t)nb * nb;
-    {
-      KtScope kt(KT_DIAGLU, st, 8.0 * kb * (double)kb * kb / 3.0);
-      diag_lu_inv_kernel<float2><<<1, 1024, diag_smem<float2>(kb), st>>>(A + (size_t)k * lda + k, lda, kb, Lk,
-                                                                         Uk, dinfo);
-    }
-    QG_CUDA_TRY(cudaGetLastError());
-    g_launches.fetch_add(1);
+    float2 *Ainv = Dinv + (size_t)blk * nb * nb, *Ck = A + (size_t)k * lda;
+    if ((e = launch_diag<float2>(Ck + k, lda, kb, Ainv, dinfo, st))) return e;
+    // column block k <- column block k x D^-1 (all N rows)
+    if ((e = tc_split_ab(Ck, lda, N, kb, Ainv, kb, kb, nsplit, pa, pb, st))) return e;
+    P.m = N, P.n = kb, P.k = kb;
+    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, Ck, lda, st))) return e;
     const int m2 = N - k - kb;
     if (m2 <= 0) break;
-    float2 *A21 = A + (size_t)k * lda + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = A21 + (size_t)kb * lda;
-    // L21 = A21 U^-1
-    if ((e = tc_split_ab(A21, lda, m2, kb, Uk, kb, kb, nsplit, pa, pb, st))) return e;
-    P.m = m2, P.n = kb, P.k = kb;
-    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, A21, lda, st))) return e;
-    // U12 = L^-1 A12
-    if ((e = tc_split_ab(Lk, kb, kb, kb, A12, lda, m2, nsplit, pa, pb, st))) return e;
-    P.m = kb, P.n = m2, P.k = kb;
-    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, A12, lda, st))) return e;
-    // A22 -= L21 U12
-    if ((e = tc_split_ab(A21, lda, m2, kb, A12, lda, m2, nsplit, pa, pb, st))) return e;
+    float2 *Pk = Ck + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = Pk + (size_t)kb * lda;
+    // A22 -= P_k A12
+    if ((e = tc_split_ab(Pk, lda, m2, kb, A12, lda, m2, nsplit, pa, pb, st))) return e;
     P.m = m2, P.n = m2, P.k = kb;
     if ((e = tc_cgemm_planes(P, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
   }
   return QPMS_SUCCESS;
 }
 
-// (L U) X = B in place, B: N x nrhs (ldb), products on the tensor cores.
-int lu_solve_tc(int N, int nb, const float2 *A, size_t lda, const float2 *Dinv, float2 *B, size_t ldb, int nrhs,
-                int nsplit, __nv_bfloat16 *pa, __nv_bfloat16 *pb, cudaStream_t st) {
+// lu_solve's substitutions with the products on the tensor cores (in place).
+int lu_solve_tc(int N, int nb, const float2 *A, size_t lda, float2 *B, size_t ldb, int nrhs, int nsplit,
+                __nv_bfloat16 *pa, __nv_bfloat16 *pb, cudaStream_t st) {
   TcPlanes P;
   P.a = pa;
   P.b = pb;
   P.nsplit = nsplit;
   int e;
   const int nblk = (N + nb - 1) / nb;
-  for (int blk = 0; blk < nblk; ++blk) {  // forward: L y = b
-    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
-    const float2 *Lk = Dinv + (size_t)blk * 2 * nb * nb;
-    if ((e = tc_split_ab(Lk, kb, kb, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
-    P.m = kb, P.n = nrhs, P.k = kb;
-    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, B + k, ldb, st))) return e;
-    const int m2 = N - k - kb;
+  for (int blk = 0; blk < nblk; ++blk) {
+    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb, m2 = N - k - kb;
     if (m2 <= 0) continue;
     if ((e = tc_split_ab(A + (size_t)k * lda + k + kb, lda, m2, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
     P.m = m2, P.n = nrhs, P.k = kb;
     if ((e = tc_cgemm_planes(P, -1.f, 1.f, B + k + kb, ldb, B + k + kb, ldb, st))) return e;
   }
-  for (int blk = nblk - 1; blk >= 0; --blk) {  // backward: U x = y
+  for (int blk = nblk - 1; blk >= 0; --blk) {
     const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
-    const float2 *Uk = Dinv + (size_t)blk * 2 * nb * nb + (size_t)nb * nb;
-    if ((e = tc_split_ab(Uk, kb, kb, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
-    P.m = kb, P.n = nrhs, P.k = kb;
-    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, B + k, ldb, st))) return e;
-    if (k == 0) continue;
-    if ((e = tc_split_ab(A + (size_t)k * lda, lda, k, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
-    P.m = k, P.n = nrhs, P.k = kb;
+    if ((e = tc_split_ab(A + (size_t)k * lda, lda, k + kb, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
+    P.m = k + kb, P.n = nrhs, P.k = kb;
     if ((e = tc_cgemm_planes(P, -1.f, 1.f, B, ldb, B, ldb, st))) return e;
   }
   return QPMS_SUCCESS;
@@ -484,71 +440,89 @@ int lu_solve_tc(int N, int nb, const float2 *A, size_t lda, const float2 *Dinv, 
 // ---------------- substitutions for a few right-hand sides (bandwidth-bound) ----------------
 constexpr int kSmallRhs = 8;
 
-// Bk (kb x nrhs, ldb) <- Tri (kb x kb, leading dimension kb) Bk; one CTA.
-template <typename T>
-__global__ void __launch_bounds__(256) blk_apply_kernel(const T *__restrict__ Tri, int kb, T *Bk, size_t ldb,
-                                                        int nrhs) {
-  __shared__ T sB[128 * kSmallRhs];
-  for (int t = threadIdx.x; t < kb * nrhs; t += blockDim.x) {
-    const int c = t / kb, r = t - c * kb;
-    sB[c * kb + r] = Bk[(size_t)c * ldb + r];
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < kb * nrhs; t += blockDim.x) {
-    const int c = t / kb, r = t - c * kb;
-    T acc = mk<T>(0, 0);
-    for (int l = 0; l < kb; ++l) acc = fma_c(acc, Tri[(size_t)l * kb + r], sB[c * kb + l]);
-    Bk[(size_t)c * ldb + r] = acc;
-  }
-}
+// One block step of lu_solve's substitutions for nrhs <= kSmallRhs:
+//   rows r < msub:              Bsub_r -= Pn_r V
+//   rows msub <= r < msub+mout: Xout_(r-msub) = V_(r-msub) - Pn_r V
+// with Pn (msub + mout) x kb (leading dimension lda) and V kb x nrhs (ldv).
+// V is staged in shared memory by every CTA; it is only read in this launch
+// (Bsub and Xout never overlap it), so the CTAs need no ordering.  Each CTA
+// takes kSubRows rows: thread (r, s) sums the columns l = s, s + kSubSlices,
+// ... of row r (coalesced loads down the columns); the kSubSlices partial sums
+// meet in shared memory.
+constexpr int kSubRows = 64, kSubSlices = 4;
 
-// Bdst (m2 x nrhs) -= Pn (m2 x kb, leading dimension lda) Bk (kb x nrhs); a
-// thread per row, the panel read once and coalesced.
 template <typename T>
-__global__ void __launch_bounds__(256) panel_sub_kernel(const T *__restrict__ Pn, size_t lda, int m2, int kb,
-                                                        const T *Bk, size_t ldb, T *Bdst, int nrhs) {
-  __shared__ T sB[128 * kSmallRhs];
-  for (int t = threadIdx.x; t < kb * nrhs; t += blockDim.x) {
-    const int c = t / kb, r = t - c * kb;
-    sB[c * kb + r] = Bk[(size_t)c * ldb + r];
+__global__ void __launch_bounds__(256) panel_apply_kernel(const T *__restrict__ Pn, size_t lda, int msub, int mout,
+                                                          int kb, const T *V, size_t ldv, T *Bsub, size_t ldb,
+                                                          T *Xout, size_t ldx, int nrhs) {
+  __shared__ T sV[128 * kSmallRhs];                  // [c][l]
+  __shared__ T sP[kSubSlices * kSmallRhs * kSubRows];  // [slice][c][r]
+  const int tid = threadIdx.x;
+  for (int t = tid; t < kb * nrhs; t += blockDim.x) {
+    const int c = t / kb, l = t - c * kb;
+    sV[c * kb + l] = V[(size_t)c * ldv + l];
   }
   __syncthreads();
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= m2) return;
+  const int m = msub + mout;
+  const int r = tid % kSubRows, sl = tid / kSubRows;
+  const int row = blockIdx.x * kSubRows + r;
   T acc[kSmallRhs];
 #pragma unroll
   for (int c = 0; c < kSmallRhs; ++c) acc[c] = mk<T>(0, 0);
-  for (int l = 0; l < kb; ++l) {
-    const T p = Pn[(size_t)l * lda + r];
+  if (row < m) {
+#pragma unroll 8
+    for (int l = sl; l < kb; l += kSubSlices) {
+      const T p = Pn[(size_t)l * lda + row];
 #pragma unroll
-    for (int c = 0; c < kSmallRhs; ++c)
-      if (c < nrhs) acc[c] = fma_c(acc[c], p, sB[c * kb + l]);
+      for (int c = 0; c < kSmallRhs; ++c)
+        if (c < nrhs) acc[c] = fma_c(acc[c], p, sV[c * kb + l]);
+    }
   }
 #pragma unroll
   for (int c = 0; c < kSmallRhs; ++c)
-    if (c < nrhs) Bdst[(size_t)c * ldb + r] = sub(Bdst[(size_t)c * ldb + r], acc[c]);
+    if (c < nrhs) sP[(sl * kSmallRhs + c) * kSubRows + r] = acc[c];
+  __syncthreads();
+  for (int t = tid; t < kSubRows * nrhs; t += blockDim.x) {
+    const int c = t / kSubRows, rr = t - c * kSubRows, rw = blockIdx.x * kSubRows + rr;
+    if (rw >= m) continue;
+    T s = sP[c * kSubRows + rr];
+#pragma unroll
+    for (int q = 1; q < kSubSlices; ++q) {
+      const T v = sP[(q * kSmallRhs + c) * kSubRows + rr];
+      s = mk<T>(s.x + v.x, s.y + v.y);
+    }
+    if (rw < msub) {
+      T *d = Bsub + (size_t)c * ldb + rw;
+      *d = sub(*d, s);
+    } else {
+      const int i = rw - msub;
+      Xout[(size_t)c * ldx + i] = sub(sV[c * kb + i], s);
+    }
+  }
 }
 
+// lu_solve for nrhs <= kSmallRhs: one launch per block and sweep.  The
+// forward sweep works in place in B; the backward sweep updates the rows
+// above each block in B and writes the block's solution to X (N x nrhs, ld
+// ldb; X must not overlap B).
 template <typename T>
-int lu_solve_small(int N, int nb, const T *A, size_t lda, const T *Dinv, T *B, size_t ldb, int nrhs, cudaStream_t st) {
+int lu_solve_small(int N, int nb, const T *A, size_t lda, T *B, size_t ldb, int nrhs, T *X, cudaStream_t st) {
   const int nblk = (N + nb - 1) / nb;
   for (int blk = 0; blk < nblk; ++blk) {
-    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
-    blk_apply_kernel<T><<<1, 256, 0, st>>>(Dinv + (size_t)blk * 2 * nb * nb, kb, B + k, ldb, nrhs);
-    const int m2 = N - k - kb;
-    if (m2 > 0)
-      panel_sub_kernel<T><<<(m2 + 255) / 256, 256, 0, st>>>(A + (size_t)k * lda + k + kb, lda, m2, kb, B + k, ldb,
-                                                            B + k + kb, nrhs);
+    const int k = blk * nb, kb = (N - k < nb) ? N - k : nb, m2 = N - k - kb;
+    if (m2 <= 0) continue;
+    panel_apply_kernel<T><<<(m2 + kSubRows - 1) / kSubRows, 256, 0, st>>>(A + (size_t)k * lda + k + kb, lda, m2, 0,
+                                                                          kb, B + k, ldb, B + k + kb, ldb, nullptr,
+                                                                          0, nrhs);
     QG_CUDA_TRY(cudaGetLastError());
-    g_launches.fetch_add(m2 > 0 ? 2 : 1);
+    g_launches.fetch_add(1);
   }
   for (int blk = nblk - 1; blk >= 0; --blk) {
     const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
-    blk_apply_kernel<T><<<1, 256, 0, st>>>(Dinv + (size_t)blk * 2 * nb * nb + (size_t)nb * nb, kb, B + k, ldb, nrhs);
-    if (k > 0)
-      panel_sub_kernel<T><<<(k + 255) / 256, 256, 0, st>>>(A + (size_t)k * lda, lda, k, kb, B + k, ldb, B, nrhs);
+    panel_apply_kernel<T><<<(k + kb + kSubRows - 1) / kSubRows, 256, 0, st>>>(A + (size_t)k * lda, lda, k, kb, kb,
+                                                                               B + k, ldb, B, ldb, X + k, ldb, nrhs);
     QG_CUDA_TRY(cudaGetLastError());
-    g_launches.fetch_add(k > 0 ? 2 : 1);
+    g_launches.fetch_add(1);
   }
   return QPMS_SUCCESS;
 }
@@ -817,25 +791,30 @@ int DenseSolver::apply_inverse(const void *R, size_t ldr, void *Y, size_t ldy, i
     d2f_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)rp, (float2 *)rhs_lo);
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
-    if (nrhs <= kSmallRhs)
-      e = lu_solve_small<float2>(Np, nb, (const float2 *)A, Np, (const float2 *)Dinv, (float2 *)rhs_lo, Np, nrhs, st);
-    else if (tc_split)
-      e = lu_solve_tc(Np, nb, (const float2 *)A, Np, (const float2 *)Dinv, (float2 *)rhs_lo, Np, nrhs, 3,
-                      (__nv_bfloat16 *)tc_pa, (__nv_bfloat16 *)tc_pb, st);
-    else
-      e = lu_solve<float2>(h, Np, nb, (const float2 *)A, Np, (const float2 *)Dinv, (float2 *)rhs_lo, Np, nrhs,
-                           (float2 *)work, CUBLAS_COMPUTE_32F, st);
+    const float2 *sol = (const float2 *)rhs_lo;
+    if (nrhs <= kSmallRhs) {
+      e = lu_solve_small<float2>(Np, nb, (const float2 *)A, Np, (float2 *)rhs_lo, Np, nrhs, (float2 *)work, st);
+      sol = (const float2 *)work;
+    } else if (tc_split) {
+      e = lu_solve_tc(Np, nb, (const float2 *)A, Np, (float2 *)rhs_lo, Np, nrhs, 3, (__nv_bfloat16 *)tc_pa,
+                      (__nv_bfloat16 *)tc_pb, st);
+    } else {
+      e = lu_solve<float2>(h, Np, nb, (const float2 *)A, Np, (float2 *)rhs_lo, Np, nrhs, (float2 *)work,
+                           CUBLAS_COMPUTE_32F, st);
+    }
     if (e) return e;
-    f2d_add_kernel<<<grid1(n), 256, 0, st>>>(n, (const float2 *)rhs_lo, (double2 *)rp, 1);
+    f2d_add_kernel<<<grid1(n), 256, 0, st>>>(n, sol, (double2 *)rp, 1);
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
   } else {
-    if (nrhs <= kSmallRhs)
-      e = lu_solve_small<double2>(Np, nb, (const double2 *)T64, Np, (const double2 *)Dinv, (double2 *)rp, Np, nrhs,
-                                  st);
-    else
-      e = lu_solve<double2>(h, Np, nb, (const double2 *)T64, Np, (const double2 *)Dinv, (double2 *)rp, Np, nrhs,
-                            (double2 *)work, CUBLAS_COMPUTE_64F, st);
+    if (nrhs <= kSmallRhs) {
+      e = lu_solve_small<double2>(Np, nb, (const double2 *)T64, Np, (double2 *)rp, Np, nrhs, (double2 *)work, st);
+      if (!e)
+        QG_CUDA_TRY(cudaMemcpyAsync(rp, work, n * 16, cudaMemcpyDeviceToDevice, st));
+    } else {
+      e = lu_solve<double2>(h, Np, nb, (const double2 *)T64, Np, (double2 *)rp, Np, nrhs, (double2 *)work,
+                            CUBLAS_COMPUTE_64F, st);
+    }
     if (e) return e;
   }
   if ((e = rbt_right_solution(*this, (double2 *)rp, Np, nrhs, st))) return e;
