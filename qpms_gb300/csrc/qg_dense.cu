@@ -85,21 +85,22 @@ __device__ __forceinline__ T rcp(T b) {
 }
 
 // ---------------- diagonal block: inverse by Gauss-Jordan ----------------
-// D (kb x kb, kb <= 32 NA, column-major in global, leading dimension lda):
-// Ainv (column-major kb x kb, leading dimension kb) receives D^-1, and D is
-// overwritten with D - I (the column-block product that follows turns it into
-// I - D^-1, the slot the back substitution reads).  info is set to 1 on an
-// exactly zero pivot.  Gauss-Jordan elimination without pivoting (the random
-// butterflies make it safe with high probability, as for the whole LU).  One
-// CTA of kDiagWarps warps with the block in registers: thread (lane, warp)
-// holds the NA x NB elements (lane + 32 i, warp + kDiagWarps j), so column c
-// lives in warp c % kDiagWarps and row r in lane r % 32 of every warp.  At
-// step j the lanes of row j publish the row and the warp of column j the
-// column (two alternating shared-memory slots, so one barrier per step);
-// every thread then forms the pivot's reciprocal itself and updates its
-// elements:
-//   a_jj <- 1/p,  a_jc <- a_jc / p,  a_rj <- -a_rj / p,
-//   a_rc <- a_rc - a_rj a_jc / p  (r, c != j).
+// D (kb x kb, kb even and <= 32 NA, column-major in global, leading dimension
+// lda): Ainv (column-major kb x kb, leading dimension kb) receives D^-1, and D
+// is overwritten with D - I (the column-block product that follows turns it
+// into I - D^-1, the slot the back substitution reads).  info is set to 1 on
+// a singular pivot block.  Gauss-Jordan elimination without pivoting (the
+// random butterflies make it safe with high probability, as for the whole
+// LU), two columns per step: with J = {j, j + 1} and the 2 x 2 pivot block P,
+//   A_JJ <- P^-1,  A_Jc <- P^-1 A_Jc,  A_rJ <- -A_rJ P^-1,
+//   A_rc <- A_rc - A_rJ P^-1 A_Jc        (r, c not in J).
+// One CTA of kDiagWarps warps with the block in registers: thread (lane,
+// warp) holds the NA x NB elements (lane + 32 i, warp + kDiagWarps j), so
+// column c lives in warp c % kDiagWarps and row r in lane r % 32 of every
+// warp.  At each step the two pivot rows and columns are published through
+// two alternating shared-memory slots (one barrier per step); every thread
+// then forms P^-1 itself, updates all its elements and overwrites the pivot
+// rows and columns.
 constexpr int kDiagMaxNb = 128, kDiagWarps = 16;
 
 template <typename T>
@@ -115,8 +116,8 @@ template <typename T, int NA>
 __global__ void __launch_bounds__(32 * kDiagWarps, 1) diag_inv_kernel(T *D, size_t lda, int kb, T *Ainv, int *info) {
   constexpr int NB = 32 * NA / kDiagWarps;  // = 2 NA: column tiles per thread
   static_assert(kDiagWarps == 16, "the step loop splits 32 rows into two halves of 16 columns");
-  __shared__ T sc[2 * kDiagMaxNb];  // column j, alternating slots
-  __shared__ T sr[2 * kDiagMaxNb];  // row j
+  __shared__ T sc[2][2][kDiagMaxNb];  // [slot][e][r] = a_(r, j+e)
+  __shared__ T sr[2][2][kDiagMaxNb];  // [slot][e][c] = a_(j+e, c)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   T a[NA][NB];
 #pragma unroll
@@ -133,59 +134,77 @@ __global__ void __launch_bounds__(32 * kDiagWarps, 1) diag_inv_kernel(T *D, size
       }
     }
   bool zero = false;
-  // Step j = 32 jt + 16 h + q: row j is tile row jt of lane 16 h + q, column j
-  // tile column 2 jt + h of warp q; jt and h are unrolled, so every register
+  // Step (j, j + 1), j = 32 jt + 16 h + q, q even: rows j, j + 1 are tile row
+  // jt of lanes 16 h + q, 16 h + q + 1; columns j, j + 1 are tile column
+  // 2 jt + h of warps q, q + 1.  jt and h are unrolled, so every register
   // index is static.
 #pragma unroll
   for (int jt = 0; jt < NA; ++jt) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int ct = 2 * jt + h;
-      for (int q = 0; q < 16; ++q) {
+      for (int q = 0; q < 16; q += 2) {
         const int j = 32 * jt + 16 * h + q;
         if (j >= kb) break;  // uniform
-        const int rl = 16 * h + q, buf = (j & 1) * kDiagMaxNb;
-        if (lane == rl) {
+        const int rl = 16 * h + q, slot = (j >> 1) & 1;
+        if (lane == rl || lane == rl + 1) {
+          const int e = lane - rl;
 #pragma unroll
           for (int jj = 0; jj < NB; ++jj) {
             const int c = w + kDiagWarps * jj;
-            if (c < kb) sr[buf + c] = a[jt][jj];
+            if (c < kb) sr[slot][e][c] = a[jt][jj];
           }
         }
-        if (w == q) {
+        if (w == q || w == q + 1) {
+          const int e = w - q;
 #pragma unroll
           for (int i = 0; i < NA; ++i) {
             const int r = lane + 32 * i;
-            if (r < kb) sc[buf + r] = a[i][ct];
+            if (r < kb) sc[slot][e][r] = a[i][ct];
           }
         }
         __syncthreads();
-        const T p = sc[buf + j];
-        const bool z = (p.x == 0 && p.y == 0);
+        // P = [p00 p01; p10 p11], P^-1 = [q00 q01; q10 q11]
+        const T p00 = sc[slot][0][j], p10 = sc[slot][0][j + 1], p01 = sc[slot][1][j], p11 = sc[slot][1][j + 1];
+        const T det = sub(mul(p00, p11), mul(p01, p10));
+        const bool z = (det.x == 0 && det.y == 0);
         zero |= z;
-        const T pinv = z ? mk<T>(0, 0) : rcp(p);
-        T f[NA];
+        const T dinv = z ? mk<T>(0, 0) : rcp(det);
+        const T q00 = mul(p11, dinv), q11 = mul(p00, dinv);
+        const T q01 = mk<T>(-(p01.x * dinv.x - p01.y * dinv.y), -(p01.x * dinv.y + p01.y * dinv.x));
+        const T q10 = mk<T>(-(p10.x * dinv.x - p10.y * dinv.y), -(p10.x * dinv.y + p10.y * dinv.x));
+        T f0[NA], f1[NA];
 #pragma unroll
-        for (int i = 0; i < NA; ++i) f[i] = (32 * i < kb) ? sc[buf + min(lane + 32 * i, kb - 1)] : mk<T>(0, 0);
-        // every element: a_rc -= a_rj a_jc / p (row j and column j become 0
-        // here and are set right after)
+        for (int i = 0; i < NA; ++i) {
+          const int r = min(lane + 32 * i, kb - 1);  // rows >= kb are padding, never stored
+          f0[i] = sc[slot][0][r];
+          f1[i] = sc[slot][1][r];
+        }
+        // every element: a_rc -= a_rj u0_c + a_r,j+1 u1_c with u = P^-1 A_Jc;
+        // the pivot rows and columns are overwritten right after
 #pragma unroll
         for (int jj = 0; jj < NB; ++jj) {
           const int c = w + kDiagWarps * jj;
           if (c >= kb) continue;  // warp-uniform
-          const T u = mul(sr[buf + c], pinv);  // a_jc / p
+          const T x0 = sr[slot][0][c], x1 = sr[slot][1][c];
+          const T u0 = fma_c(mul(q00, x0), q01, x1), u1 = fma_c(mul(q10, x0), q11, x1);
 #pragma unroll
           for (int i = 0; i < NA; ++i) {
             if (32 * i >= kb) continue;  // uniform
-            a[i][jj] = fms_c(a[i][jj], f[i], u);
+            a[i][jj] = fms_c(fms_c(a[i][jj], f0[i], u0), f1[i], u1);
           }
-          if (lane == rl) a[jt][jj] = u;  // row j: a_jc / p
+          if (lane == rl) a[jt][jj] = u0;
+          if (lane == rl + 1) a[jt][jj] = u1;
         }
-        if (w == q) {  // column j: -a_rj / p, the pivot 1 / p
+        if (w == q || w == q + 1) {  // columns j + e: -A_rJ P^-1, the pivot block P^-1
+          const T qa = (w == q) ? q00 : q01, qb = (w == q) ? q10 : q11;
 #pragma unroll
-          for (int i = 0; i < NA; ++i) a[i][ct] = mk<T>(-(f[i].x * pinv.x - f[i].y * pinv.y),
-                                                        -(f[i].x * pinv.y + f[i].y * pinv.x));
-          if (lane == rl) a[jt][ct] = pinv;
+          for (int i = 0; i < NA; ++i) {
+            const T g = fma_c(mul(f0[i], qa), f1[i], qb);
+            a[i][ct] = mk<T>(-g.x, -g.y);
+          }
+          if (lane == rl) a[jt][ct] = qa;
+          if (lane == rl + 1) a[jt][ct] = qb;
         }
       }
     }
@@ -204,7 +223,7 @@ __global__ void __launch_bounds__(32 * kDiagWarps, 1) diag_inv_kernel(T *D, size
 template <typename T>
 int launch_diag(T *D, size_t lda, int kb, T *Ainv, int *info, cudaStream_t st) {
   constexpr int kMaxNa = sizeof(T) == 16 ? 2 : 4;  // complex128 blocks: nb <= 64
-  if (kb <= 0 || kb > 32 * kMaxNa) {
+  if (kb <= 0 || kb > 32 * kMaxNa || (kb & 1)) {
     set_error("diagonal block of size %d not supported", kb);
     return QPMS_EINVAL;
   }

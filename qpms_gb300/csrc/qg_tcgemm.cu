@@ -142,14 +142,16 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+// 64 consecutive accumulator columns of this thread's lane: two loads and one
+// wait in a single statement, so no use of r can be scheduled before the wait.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%64];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%65];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      : "r"(taddr), "r"(taddr + 32u)
+      : "memory");
 }
 
 // ---------------- the GEMM kernel ----------------
@@ -159,7 +161,7 @@ struct GemmArgs {
   int Md, Nd;         // output rows (real) and columns
   int kblocks;        // ceil(K / 64) per digit product
   int npairs;
-  int8_t pa[kMaxPairs], pb[kMaxPairs];  // digit planes of each product
+  uint32_t pa, pb;  // digit planes of product i in bits [4i, 4i + 4)
   float alpha, beta;
   const float *C;
   float *D;
@@ -229,8 +231,8 @@ __global__ void __launch_bounds__(192, 1)
         const int pr = kb / g.kblocks, kk = kb - pr * g.kblocks;
         unsigned char *sa = base + s * S::kStage, *sb = sa + S::kA;
         mbar_expect_tx(full + s, S::kStage);
-        tma_load_3d(sa, &mapA, full + s, kk * BK, m0, g.pa[pr]);
-        tma_load_3d(sb, &mapB, full + s, kk * BK, n0, g.pb[pr]);
+        tma_load_3d(sa, &mapA, full + s, kk * BK, m0, (int)((g.pa >> (4 * pr)) & 15u));
+        tma_load_3d(sb, &mapB, full + s, kk * BK, n0, (int)((g.pb >> (4 * pr)) & 15u));
       }
     }
   } else if (warp == 1 && lane == 0) {
@@ -282,19 +284,28 @@ __global__ void __launch_bounds__(192, 1)
       }
       if (!(ok = mbar_wait(tfull + b, tph, 4))) break;
       tc_fence_after();
+      const bool full_cols = n0 + BN <= g.Nd;
 #pragma unroll
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        uint32_t v[16], w[16];
-        tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0, v);
-        tmem_ld16(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0 + 16, w);
+      for (int c0 = 0; c0 < BN; c0 += 64) {
+        uint32_t v[64];
+        tmem_ld64(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0, v);
         if (rok) {
+          float *drow = g.D + (size_t)(n0 + c0) * g.ldd + r;
+          if (full_cols) {
 #pragma unroll
-          for (int c = 0; c < 32; ++c) {
-            const int j = n0 + c0 + c;
-            if (j < g.Nd) {
-              float x = g.alpha * __uint_as_float(c < 16 ? v[c] : w[c - 16]);
+            for (int c = 0; c < 64; ++c) {
+              float x = g.alpha * __uint_as_float(v[c]);
               if (has_c) x += g.beta * cv[c0 + c];
-              g.D[(size_t)j * g.ldd + r] = x;
+              drow[(size_t)c * g.ldd] = x;
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < 64; ++c) {
+              if (n0 + c0 + c < g.Nd) {
+                float x = g.alpha * __uint_as_float(v[c]);
+                if (has_c) x += g.beta * cv[c0 + c];
+                drow[(size_t)c * g.ldd] = x;
+              }
             }
           }
         }
@@ -596,8 +607,8 @@ int tc_cgemm_planes(const TcPlanes &P, float alpha, float beta, const float2 *C,
   int np = 0;
   for (int sum = P.nsplit - 1; sum >= 0; --sum)
     for (int s = 0; s <= sum && np < kMaxPairs; ++s) {
-      g.pa[np] = (int8_t)s;
-      g.pb[np] = (int8_t)(sum - s);
+      g.pa |= (uint32_t)s << (4 * np);
+      g.pb |= (uint32_t)(sum - s) << (4 * np);
       ++np;
     }
   g.npairs = np;
