@@ -687,9 +687,21 @@ def section_beyn(args):
     ss = qpms_gb300.ScatteringSystem(_sq(30, 400e-9), 60e-9, EPS_I, EPS_E, 2)
     N, L = ss.fecv_size, 64
     c, rr, ri = 2.1 * EV / HBAR, 0.05 * EV / HBAR, 0.005 * EV / HBAR
+    Lb = qpms_gb300.lib()
     ss.find_modes(c, rr, ri, contour_points=1, rank_tol=-1e-10, rank_min_sel=0, l=L, seed=12345, mode=1)
-    _lib.kernel_timing(True)
+    l0, g0 = Lb.qpms_gpu_kernel_launch_count(), Lb.qpms_gpu_graph_replay_count()
     r = ss.find_modes(c, rr, ri, contour_points=64, rank_tol=-1e-10, rank_min_sel=0, l=L, seed=12345, mode=1)
+    launches = (Lb.qpms_gpu_kernel_launch_count() - l0) / 64
+    replays = (Lb.qpms_gpu_graph_replay_count() - g0) / 64
+    # the same nodes with every launch issued eagerly (no CUDA graphs)
+    os.environ["QPMS_GB300_GRAPHS"] = "0"
+    try:
+        re_ = ss.find_modes(c, rr, ri, contour_points=16, rank_tol=-1e-10, rank_min_sel=0, l=L, seed=12345, mode=1)
+    finally:
+        del os.environ["QPMS_GB300_GRAPHS"]
+    # per-kind kernel times on a shorter contour (per-launch timing runs eagerly)
+    _lib.kernel_timing(True)
+    ss.find_modes(c, rr, ri, contour_points=8, rank_tol=-1e-10, rank_min_sel=0, l=L, seed=12345, mode=1)
     kt = _lib.kernel_timing_get()
     _lib.kernel_timing(False)
     from oracle import beyn as ob
@@ -707,14 +719,18 @@ def section_beyn(args):
                                   "refine_iters_max": r["node_refine_iters_max"],
                                   "note": "no eigenfrequency of this array lies inside (its modes have "
                                           "Im(hbar omega) <= -0.0159 eV); K = 0 is the valid result"},
-           "lu_tflops_per_node": lu_flops / node_s / 1e12}
+           "lu_tflops_per_node": lu_flops / node_s / 1e12,
+           "graphs": {"launches_per_node": launches, "graph_replays_per_node": replays, "node_s": node_s,
+                      "node_s_eager": re_["quadrature_s"] / 16,
+                      "note": "the dense solver's factorisation and solve launch sequences are captured at the "
+                              "second node and replayed after; eager = QPMS_GB300_GRAPHS=0, 16 nodes"}}
     if "tc_gemm" in kt:
         ms, work, n = kt["tc_gemm"]
-        out["tc_gemm"] = {"ms_per_node": ms / 64, "launches_per_node": n / 64,
+        out["tc_gemm"] = {"ms_per_node": ms / 8, "launches_per_node": n / 8,
                           "tflops_bf16_executed": work / (ms * 1e-3) / 1e12,
                           "frac_of_sustained": work / (ms * 1e-3) / 1e12 /
                           (measured_peaks().get("bf16_tflops_sustained") or 1700.0)}
-    out["kernels_ms_per_node"] = {k: v[0] / 64 for k, v in kt.items()}
+    out["kernels_ms_per_node"] = {k: v[0] / 8 for k, v in kt.items()}
     # the modes below the Rayleigh anomaly, against the FP64 oracle's eigenvalues
     cr = complex(*BEYN_RA["centre_eV"]) * EV / HBAR
     q = ss.find_modes(cr, BEYN_RA["rRe_eV"] * EV / HBAR, BEYN_RA["rIm_eV"] * EV / HBAR, contour_points=64,

@@ -922,8 +922,13 @@ const char *qpms_gpu_last_error(void);
 int qpms_gpu_measure_fp64_peak(double *tflops);
 /* Host evaluation of the library's complex erfc (Weideman Faddeeva), for tests. */
 int qpms_gpu_debug_cerfc(double re, double im, double *out);
-/* Number of kernels this library launched since load (for benchmarks). */
+/* Number of kernels this library launched since load (for benchmarks); the
+ * launches inside a replayed CUDA graph count as well. */
 unsigned long long qpms_gpu_kernel_launch_count(void);
+/* Number of CUDA-graph replays since load: the dense solver of the Beyn node
+ * loop captures its factorisation and solve launch sequences once and replays
+ * them at the following nodes (QPMS_GB300_GRAPHS=0 turns this off). */
+unsigned long long qpms_gpu_graph_replay_count(void);
 
 /* ---------------- reference-API convenience entry points ----------------
  * Host set-up helpers beside the hot path (qg_dropins.cu): O(n) or O(n^2) per

@@ -41,6 +41,8 @@ def _declare(L):
     L.qpms_gpu_last_error.argtypes = []
     L.qpms_gpu_kernel_launch_count.restype = C.c_ulonglong
     L.qpms_gpu_kernel_launch_count.argtypes = []
+    L.qpms_gpu_graph_replay_count.restype = C.c_ulonglong
+    L.qpms_gpu_graph_replay_count.argtypes = []
     L.qpms_trans_calculator_init.restype = vp
     L.qpms_trans_calculator_init.argtypes = [ci, ci]
     L.qpms_trans_calculator_free.restype = None

@@ -309,9 +309,24 @@ int beyn_quadrature(MSource &src, beyn_function_M_inv_Vhat_t minv, void *minv_pa
     set_error("Beyn: host to device copy failed");
     return QPMS_ERROR;
   }
+  // the nodes run on a stream of their own (ordered with the legacy default
+  // stream), so that the solver's repeated launch sequences can be captured
+  // as CUDA graphs and replayed node after node
+  struct Stream {
+    cudaStream_t s = nullptr;
+    ~Stream() {
+      if (s) cudaStreamDestroy(s);
+    }
+  } ns;
+  if (cudaStreamCreate(&ns.s) != cudaSuccess) {
+    set_error("Beyn: stream creation failed");
+    return QPMS_ERROR;
+  }
+  const cudaStream_t st = ns.s;
   DenseSolver ds;
   int e;
   if (!minv && (e = ds.init((int)m, (int)l, mode, seed ^ 0x9e3779b97f4a7c15ULL))) return e;
+  ds.graphs = true;
   std::vector<qpms_complex_t> hx;
   double max_res = 0;
   int max_it = 0;
@@ -334,14 +349,14 @@ int beyn_quadrature(MSource &src, beyn_function_M_inv_Vhat_t minv, void *minv_pa
     } else {
       double res = 0;
       int it = 0;
-      if ((e = src.build_rowmajor(z, 0))) return e;
+      if ((e = src.build_rowmajor(z, st))) return e;
       // the staged row-major M(z) goes straight to the solver (transposed on the fly)
-      if ((e = ds.factorize(src.stage, m, 0, true))) return e;
-      if ((e = ds.solve(src.stage, m, dV.p, dX.p, (int)l, refine_tol, kMaxRefine, &res, &it, 0))) return e;
+      if ((e = ds.factorize(src.stage, m, st, true))) return e;
+      if ((e = ds.solve(src.stage, m, dV.p, dX.p, (int)l, refine_tol, kMaxRefine, &res, &it, st))) return e;
       if (!(res <= max_res)) max_res = res;  // NaN-propagating max
       if (it > max_it) max_it = it;
     }
-    beyn_accumulate_kernel<<<grid1(nml), 256>>>(nml, (const double2 *)dX.p, make_double2(dz.real(), dz.imag()),
+    beyn_accumulate_kernel<<<grid1(nml), 256, 0, st>>>(nml, (const double2 *)dX.p, make_double2(dz.real(), dz.imag()),
                                                 make_double2((z - z0).real(), (z - z0).imag()), (i % 2) == 0,
                                                 (double2 *)dA[0].p, (double2 *)dA[1].p, (double2 *)dA[2].p,
                                                 (double2 *)dA[3].p);

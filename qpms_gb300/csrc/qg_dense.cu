@@ -30,6 +30,7 @@
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -282,6 +283,106 @@ __global__ void rbt_cols_kernel(size_t N, size_t ld, double2 *A, int h, const do
   }
 }
 
+// A = W_u^T diag(M, I) W_v in complex64 (Np x Np, column-major): the depth-2
+// butterflies of rbt_rows_kernel / rbt_cols_kernel fused with the FP64 ->
+// complex64 conversion, one pass over M.  Entry (r, c) of the result depends
+// only on the 4 x 4 entries of diag(M, I) in the rows r mod Np/4 + q Np/4 and
+// the columns c mod Np/4 + p Np/4 (q, p = 0..3).  A CTA takes kRbtT x kRbtT
+// such row / column orbits: it stages their 4 kRbtT x 4 kRbtT entries in
+// shared memory (reads coalesced in M's own layout, row- or column-major),
+// each thread transforms one orbit pair in registers (rows level 2 then 1,
+// columns level 2 then 1, in the order of the separate passes), and the
+// results leave coalesced down A's columns.  The entries are rounded to
+// complex64 as they are read and the butterflies run in FP32: the factors are
+// complex64 anyway, and GB300's FP64 rate (1/64 of FP32) would make this pass
+// arithmetic-bound; the FP64 refinement works against the exact transform.
+constexpr int kRbtT = 16, kRbtS = 4 * kRbtT;  // orbits per CTA side, staged entries per side
+
+__device__ __forceinline__ void rbt_pair(float2 &top, float2 &bot, float R, float S) {
+  const float is2 = 0.70710678118654752440f;
+  const float2 t = top, b = bot;
+  top = make_float2(R * is2 * (t.x + b.x), R * is2 * (t.y + b.y));
+  bot = make_float2(S * is2 * (t.x - b.x), S * is2 * (t.y - b.y));
+}
+
+__global__ void __launch_bounds__(256) rbt_convert_kernel(const double2 *__restrict__ M, size_t ldm, int rowmaj,
+                                                          int N, int Np, const double *__restrict__ rs,
+                                                          float2 *__restrict__ A) {
+  constexpr int LD = kRbtS + 1;
+  __shared__ float2 S[kRbtS * LD];  // S[lc * LD + lr]
+  const int Q = Np / 4;
+  const int I0 = blockIdx.x * kRbtT, J0 = blockIdx.y * kRbtT;
+  const int tid = threadIdx.x;
+  // global index of local row / column l: (l / kRbtT) Q + base + l % kRbtT
+  for (int t = tid; t < kRbtS * kRbtS; t += blockDim.x) {
+    const int la = t % kRbtS, lb = t / kRbtS;  // la walks the source's contiguous dimension
+    const int lr = rowmaj ? lb : la, lc = rowmaj ? la : lb;
+    const int ir = I0 + lr % kRbtT, jc = J0 + lc % kRbtT;
+    if (ir >= Q || jc >= Q) continue;
+    const int R = (lr / kRbtT) * Q + ir, C = (lc / kRbtT) * Q + jc;
+    float2 v;
+    if (R < N && C < N) {
+      const double2 d = rowmaj ? M[(size_t)R * ldm + C] : M[(size_t)C * ldm + R];
+      v = make_float2((float)d.x, (float)d.y);
+    } else {
+      v = make_float2(R == C ? 1.f : 0.f, 0.f);
+    }
+    S[lc * LD + lr] = v;
+  }
+  __syncthreads();
+  {
+    const int i = tid % kRbtT, j = tid / kRbtT;
+    const int i0 = I0 + i, j0 = J0 + j;
+    if (i0 < Q && j0 < Q) {
+      float2 x[4][4];  // x[q][p]: row q Q + i0, column p Q + j0
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int p = 0; p < 4; ++p) x[q][p] = S[(p * kRbtT + j) * LD + q * kRbtT + i];
+      const double *r2 = rs + Np, *r1 = rs, *c2 = rs + 3 * (size_t)Np, *c1 = rs + 2 * (size_t)Np;
+      // rows, level 2 (halves Q within blocks of 2Q): pairs (0, 1), (2, 3)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        const float R = (float)r2[b * 2 * Q + i0], Sv = (float)r2[b * 2 * Q + Q + i0];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) rbt_pair(x[2 * b][p], x[2 * b + 1][p], R, Sv);
+      }
+      // rows, level 1 (halves 2Q): pairs (0, 2), (1, 3)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const float R = (float)r1[q * Q + i0], Sv = (float)r1[2 * Q + q * Q + i0];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) rbt_pair(x[q][p], x[q + 2][p], R, Sv);
+      }
+      // columns, level 2 then level 1
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        const float R = (float)c2[b * 2 * Q + j0], Sv = (float)c2[b * 2 * Q + Q + j0];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) rbt_pair(x[q][2 * b], x[q][2 * b + 1], R, Sv);
+      }
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        const float R = (float)c1[p * Q + j0], Sv = (float)c1[2 * Q + p * Q + j0];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) rbt_pair(x[q][p], x[q][p + 2], R, Sv);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int p = 0; p < 4; ++p) S[(p * kRbtT + j) * LD + q * kRbtT + i] = x[q][p];
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < kRbtS * kRbtS; t += blockDim.x) {
+    const int lr = t % kRbtS, lc = t / kRbtS;
+    const int ir = I0 + lr % kRbtT, jc = J0 + lc % kRbtT;
+    if (ir >= Q || jc >= Q) continue;
+    const int R = (lr / kRbtT) * Q + ir, C = (lc / kRbtT) * Q + jc;
+    A[(size_t)C * Np + R] = S[lc * LD + lr];
+  }
+}
+
 __global__ void d2f_kernel(size_t n, const double2 *src, float2 *dst) {
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
     dst[t] = make_float2((float)src[t].x, (float)src[t].y);
@@ -468,7 +569,7 @@ constexpr int kSmallRhs = 8;
 // takes kSubRows rows: thread (r, s) sums the columns l = s, s + kSubSlices,
 // ... of row r (coalesced loads down the columns); the kSubSlices partial sums
 // meet in shared memory.
-constexpr int kSubRows = 64, kSubSlices = 4;
+constexpr int kSubRows = 32, kSubSlices = 8;
 
 template <typename T>
 __global__ void __launch_bounds__(256) panel_apply_kernel(const T *__restrict__ Pn, size_t lda, int msub, int mout,
@@ -489,7 +590,7 @@ __global__ void __launch_bounds__(256) panel_apply_kernel(const T *__restrict__ 
 #pragma unroll
   for (int c = 0; c < kSmallRhs; ++c) acc[c] = mk<T>(0, 0);
   if (row < m) {
-#pragma unroll 8
+#pragma unroll 16
     for (int l = sl; l < kb; l += kSubSlices) {
       const T p = Pn[(size_t)l * lda + row];
 #pragma unroll
@@ -628,8 +729,10 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   const size_t NN = (size_t)Np * Np;
   const int nblk = (Np + nb - 1) / nb;
   size_t wsz = std::max<size_t>((size_t)Np * nb, (size_t)nb * std::max(Np, nrhs_max)) * esz;
-  if (mode) QG_CUDA_TRY(dev_alloc(&A, NN * esz));
-  QG_CUDA_TRY(dev_alloc(&T64, NN * 16));
+  if (mode)
+    QG_CUDA_TRY(dev_alloc(&A, NN * esz));  // complex64 factors; the FP64 transform is fused into their fill
+  else
+    QG_CUDA_TRY(dev_alloc(&T64, NN * 16));
   QG_CUDA_TRY(dev_alloc(&Dinv, (size_t)nblk * 2 * nb * nb * esz));
   QG_CUDA_TRY(dev_alloc(&work, wsz));
   QG_CUDA_TRY(dev_alloc(&rhs_lo, (size_t)Np * nrhs_max * 8));
@@ -670,7 +773,7 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
 size_t DenseSolver::footprint(int N, int nrhs, int mode) {
   const size_t Np = (size_t)(N + 3) / 4 * 4, nb = mode ? 128 : 64, esz = mode ? 8 : 16;
   const size_t nblk = (Np + nb - 1) / nb;
-  size_t b = (mode ? Np * Np * esz : 0) + Np * Np * 16 + nblk * 2 * nb * nb * esz;
+  size_t b = (mode ? Np * Np * esz : Np * Np * 16) + nblk * 2 * nb * nb * esz;
   b += std::max<size_t>(Np * nb, nb * std::max<size_t>(Np, nrhs)) * esz;
   b += Np * nrhs * (8 + 16) + (size_t)N * nrhs * 32 + 16 + 4 * Np * 8 + 2 * kOzakiMinRhs * 8;
   if (ozaki_wanted(nrhs)) b += ozaki_matrix_bytes(N) + ozaki_work_bytes(N, nrhs);
@@ -698,6 +801,10 @@ void DenseSolver::release() {
       else
         cudaFree(p);
     }
+  for (Graph *g : {&gf, &gs}) {
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    *g = Graph();
+  }
   A = T64 = Dinv = work = rhs_lo = rp = nullptr;
   r64 = y64 = nullptr;
   dinfo = nullptr;
@@ -728,20 +835,79 @@ static int rbt_right_solution(const DenseSolver &s, double2 *X, size_t ld, size_
   return QPMS_SUCCESS;
 }
 
+template <class F>
+int DenseSolver::run_graph(Graph &g, const unsigned long long (&key)[6], bool capturable, cudaStream_t st, F body) {
+  const char *ev = getenv("QPMS_GB300_GRAPHS");
+  const bool env_off = ev && !strcmp(ev, "0");
+  if (!graphs || env_off || !capturable || st == 0 || kt_on()) return body();
+  bool same = g.keyed;
+  for (int i = 0; i < 6 && same; ++i) same = g.key[i] == key[i];
+  if (same && g.exec) {
+    QG_CUDA_TRY(cudaGraphLaunch(g.exec, st));
+    g_launches.fetch_add(g.launches);
+    g_graph_replays.fetch_add(1);
+    ++graph_replays;
+    return QPMS_SUCCESS;
+  }
+  if (!same) {  // first call with these buffers: eager
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g.exec = nullptr;
+    for (int i = 0; i < 6; ++i) g.key[i] = key[i];
+    g.keyed = true;
+    return body();
+  }
+  // second call with the same buffers: capture, then launch the graph
+  cudaGraph_t graph = nullptr;
+  const unsigned long long l0 = g_launches.load();
+  QG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  const int e = body();
+  const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  if (e || ce != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    g.keyed = false;
+    if (e) return e;
+    set_error("stream capture failed: %s", cudaGetErrorString(ce));
+    return QPMS_ERROR;
+  }
+  g.launches = g_launches.load() - l0;
+  const cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) {
+    g.exec = nullptr;
+    g.keyed = false;
+    set_error("graph instantiation failed: %s", cudaGetErrorString(ie));
+    return QPMS_ERROR;
+  }
+  QG_CUDA_TRY(cudaGraphLaunch(g.exec, st));
+  return QPMS_SUCCESS;
+}
+
 int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st, bool rowmaj) {
   row_major = rowmaj;
   mode = base_mode;
   trail_ct = base_trail;
   tc_split = base_tc;
   nb = mode ? 128 : 64;
-  if (use_ozaki) {
-    int e;
-    if ((e = ozaki_split_matrix(M64, ldm, rowmaj, N, oz_mat, &oz, st))) return e;
-  }
-  return factorize_current(M64, ldm, st);
+  const unsigned long long key[6] = {(unsigned long long)(uintptr_t)M64, ldm, rowmaj ? 1ull : 0ull,
+                                     (unsigned long long)mode, (unsigned long long)tc_split,
+                                     use_ozaki ? 1ull : 0ull};
+  int e = run_graph(gf, key, mode == 1 && tc_split != 0, st, [&]() -> int {
+    int e2;
+    if (use_ozaki && (e2 = ozaki_split_matrix(M64, ldm, row_major, N, oz_mat, &oz, st))) return e2;
+    return factor_launch(M64, ldm, st);
+  });
+  if (e) return e;
+  return check_info(st);
 }
 
 int DenseSolver::factorize_current(const void *M64, size_t ldm, cudaStream_t st) {
+  int e;
+  if ((e = factor_launch(M64, ldm, st))) return e;
+  return check_info(st);
+}
+
+int DenseSolver::factor_launch(const void *M64, size_t ldm, cudaStream_t st) {
   const bool rowmaj = row_major;
   const size_t NN = (size_t)Np * Np;
   cublasHandle_t h;
@@ -749,7 +915,27 @@ int DenseSolver::factorize_current(const void *M64, size_t ldm, cudaStream_t st)
   if ((e = blas_handle_get(&h))) return e;
   QG_BLAS_TRY(cublasSetStream(h, st));
   QG_CUDA_TRY(cudaMemsetAsync(dinfo, 0, 4, st));
-  // T64 = W_u^T diag(M, I) W_v   (M W = column pass with level 2 first: M L2 L1)
+  if (mode) {
+    // complex64 A = W_u^T diag(M, I) W_v in one pass over M
+    const unsigned g = (unsigned)((Np / 4 + kRbtT - 1) / kRbtT);
+    rbt_convert_kernel<<<dim3(g, g), 256, 0, st>>>((const double2 *)M64, ldm, rowmaj ? 1 : 0, N, Np, rs,
+                                                   (float2 *)A);
+    QG_CUDA_TRY(cudaGetLastError());
+    g_launches.fetch_add(1);
+    if (tc_split) {
+      e = lu_nopiv_tc(Np, nb, (float2 *)A, Np, (float2 *)Dinv, dinfo, tc_split, (__nv_bfloat16 *)tc_pa,
+                      (__nv_bfloat16 *)tc_pb, st);
+    } else {
+      e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
+                           (cublasComputeType_t)trail_ct, st);
+    }
+    return e;
+  }
+  // complex128: T64 = W_u^T diag(M, I) W_v   (M W = column pass with level 2 first: M L2 L1)
+  if (!T64) {  // mixed-mode solvers allocate it at their first fallback to complex128
+    QG_CUDA_TRY(dev_alloc(&T64, NN * 16));
+    if (pool) QG_CUDA_TRY(cudaStreamSynchronize(ast));  // allocated in ast's order, used in st's
+  }
   if (Np != N) QG_CUDA_TRY(cudaMemsetAsync(T64, 0, NN * 16, st));
   if (rowmaj) {
     const dim3 g((unsigned)((N + 31) / 32), (unsigned)((N + 31) / 32)), b(32, 8);
@@ -769,22 +955,11 @@ int DenseSolver::factorize_current(const void *M64, size_t ldm, cudaStream_t st)
   rbt_cols_kernel<<<grid1(NN / 2), 256, 0, st>>>(Np, Np, (double2 *)T64, Np / 2, rs + 2 * Np);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(2);
-  if (mode) {
-    d2f_kernel<<<grid1(NN), 256, 0, st>>>(NN, (const double2 *)T64, (float2 *)A);
-    QG_CUDA_TRY(cudaGetLastError());
-    g_launches.fetch_add(1);
-    if (tc_split) {
-      e = lu_nopiv_tc(Np, nb, (float2 *)A, Np, (float2 *)Dinv, dinfo, tc_split, (__nv_bfloat16 *)tc_pa,
-                      (__nv_bfloat16 *)tc_pb, st);
-    } else {
-      e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
-                           (cublasComputeType_t)trail_ct, st);
-    }
-  } else {
-    e = lu_nopiv<double2>(h, Np, nb, (double2 *)T64, Np, (double2 *)Dinv, (double2 *)work, dinfo,
-                          CUBLAS_COMPUTE_64F, st);
-  }
-  if (e) return e;
+  return lu_nopiv<double2>(h, Np, nb, (double2 *)T64, Np, (double2 *)Dinv, (double2 *)work, dinfo,
+                           CUBLAS_COMPUTE_64F, st);
+}
+
+int DenseSolver::check_info(cudaStream_t st) {
   int info = 0;
   QG_CUDA_TRY(cudaMemcpyAsync(&info, dinfo, 4, cudaMemcpyDeviceToHost, st));
   QG_CUDA_TRY(cudaStreamSynchronize(st));
@@ -797,6 +972,14 @@ int DenseSolver::factorize_current(const void *M64, size_t ldm, cudaStream_t st)
 
 // One application of the factorised inverse: Y = W_v (LU)^-1 W_u^T R  (FP64 in and out)
 int DenseSolver::apply_inverse(const void *R, size_t ldr, void *Y, size_t ldy, int nrhs, cudaStream_t st) {
+  const unsigned long long key[6] = {(unsigned long long)(uintptr_t)R, ldr, (unsigned long long)(uintptr_t)Y, ldy,
+                                     (unsigned long long)nrhs,
+                                     (unsigned long long)mode | ((unsigned long long)tc_split << 8)};
+  const bool capturable = mode == 1 && (nrhs <= kSmallRhs || tc_split != 0);
+  return run_graph(gs, key, capturable, st, [&]() { return apply_launch(R, ldr, Y, ldy, nrhs, st); });
+}
+
+int DenseSolver::apply_launch(const void *R, size_t ldr, void *Y, size_t ldy, int nrhs, cudaStream_t st) {
   cublasHandle_t h;
   int e;
   if ((e = blas_handle_get(&h))) return e;

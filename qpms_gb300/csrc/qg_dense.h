@@ -19,7 +19,7 @@ bool ozaki_wanted(int nrhs_max);
 struct DenseSolver {
   int N = 0, Np = 0, nrhs_max = 0, mode = 0, nb = 64;
   void *A = nullptr;       // mode 1: complex64 LU factors, Np x Np (mode 0 factors T64 in place)
-  void *T64 = nullptr;     // complex128 Np x Np: W_u^T diag(M, I) W_v
+  void *T64 = nullptr;     // complex128 Np x Np: W_u^T diag(M, I) W_v (mode 0; mode 1 at its first fallback)
   void *Dinv = nullptr;    // per diagonal block: L^-1 and U^-1 (nb x nb each)
   void *work = nullptr;    // panel / RHS work buffer
   void *rhs_lo = nullptr;  // complex64 Np x nrhs_max
@@ -46,6 +46,23 @@ struct DenseSolver {
   void *oz_mat = nullptr, *oz_work = nullptr;
   OzakiMatrix oz;
 
+  // CUDA graphs for solvers that repeat the same launch sequence on the same
+  // buffers (the Beyn contour nodes): with `graphs` set (and the environment
+  // variable QPMS_GB300_GRAPHS not 0), factorize() and apply_inverse() run
+  // eagerly at the first call with a given set of buffers, are captured on
+  // the second and replayed from then on.  Only the mixed tensor-core and
+  // few-right-hand-side paths are captured, on streams other than the legacy
+  // default stream, and not while per-launch timing is on.
+  struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long key[6] = {0, 0, 0, 0, 0, 0};
+    bool keyed = false;
+    unsigned long long launches = 0;  // kernel launches of one replay
+  };
+  bool graphs = false;
+  Graph gf, gs;
+  unsigned long long graph_replays = 0;
+
   int init(int N, int nrhs_max, int mode, unsigned long long seed, cudaMemPool_t pool = nullptr,
            cudaStream_t alloc_stream = nullptr);
   void release();
@@ -68,6 +85,11 @@ struct DenseSolver {
 
  private:
   cudaError_t dev_alloc(void *ptr, size_t bytes);
+  int check_info(cudaStream_t st);  // zero-pivot flag of the last factorisation
+  int factor_launch(const void *M64, size_t ldm, cudaStream_t st);  // factorize_current's launches
+  int apply_launch(const void *R, size_t ldr, void *Y, size_t ldy, int nrhs, cudaStream_t st);
+  template <class F>
+  int run_graph(Graph &g, const unsigned long long (&key)[6], bool capturable, cudaStream_t st, F body);
 };
 
 }  // namespace qg

@@ -16,6 +16,7 @@ namespace qg {
 void set_error(const char *fmt, ...);
 void clear_error();
 extern std::atomic<unsigned long long> g_launches;
+extern std::atomic<unsigned long long> g_graph_replays;
 
 #define QG_CUDA_TRY(expr)                                                            \
   do {                                                                               \

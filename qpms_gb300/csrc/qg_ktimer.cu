@@ -42,6 +42,8 @@ void drain_locked() {
 
 }  // namespace
 
+bool kt_on() { return g_on.load(std::memory_order_relaxed); }
+
 KtScope::KtScope(int kind, cudaStream_t st, double work) : kind_(kind), st_(st), work_(work) {
   if (!g_on.load(std::memory_order_relaxed) || kind < 0 || kind >= KT_KINDS) return;
   if (cudaEventCreate(&a_) != cudaSuccess) return;

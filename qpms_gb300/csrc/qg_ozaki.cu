@@ -86,16 +86,50 @@ __global__ void scale_kernel(const unsigned long long *rowmax, int n, double *sc
   scale[i] = ldexp(1.0, e);
 }
 
-// p digits of v in (-1, 1): t = v 2^s, d = rint(t), v = t - d (all exact).
-template <typename Store>
-__device__ __forceinline__ void digits(double v, int s, int p, Store st) {
-  const double two_s = ldexp(1.0, s);
-  for (int i = 0; i < p; ++i) {
-    const double t = v * two_s;
-    const double d = rint(t);
-    v = t - d;
-    st(i, __double2bfloat16(d));
+// p digits of x = v / 2^e, |x| < 1, in integer arithmetic (GB300's FP64 rate
+// is 1/64 of its FP32 rate, and this runs over every entry of M): the 64-bit
+// fixed-point integer X = round(x 2^(s p)) (round half to even, exact from the
+// double's mantissa and exponent) is cut into base-2^s digits from the least
+// significant one, each balanced into [-2^(s-1), 2^(s-1)); the carry left over
+// goes to the leading digit, |d_0| <= 2^s.  x = sum_i d_i 2^(-s (i+1)) up to
+// the rounding of X, 2^(-s p - 1) <= 2^-56.  Every digit is an integer of at
+// most 9 bits (s <= 8), exact in bf16.
+__device__ __forceinline__ long long fixed_point(double v, int shift) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)((bits >> 52) & 0x7ff);
+  if (ex == 0) return 0;  // zero or subnormal: below 2^-1022, nothing at these shifts
+  const unsigned long long mant = (bits & ((1ull << 52) - 1)) | (1ull << 52);  // v = mant 2^(ex - 1075)
+  const int e = ex - 1075 + shift;
+  unsigned long long q;
+  if (e >= 0) {
+    q = e < 10 ? mant << e : 0;  // |x| < 1 keeps |X| < 2^(s p) <= 2^62: e <= 9
+  } else if (e < -53) {
+    q = 0;  // below 1/2
+  } else {
+    const int sh = -e;
+    q = mant >> sh;
+    const unsigned long long rem = mant & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (q & 1))) ++q;
   }
+  return (bits >> 63) ? -(long long)q : (long long)q;
+}
+
+template <typename Store>
+__device__ __forceinline__ void digits(double v, int e, int s, int p, Store st) {
+  long long X = fixed_point(v, s * p - e);
+  const long long mask = (1ll << s) - 1, halfd = 1ll << (s - 1);
+  for (int i = p - 1; i >= 1; --i) {
+    long long d = X & mask;
+    if (d >= halfd) d -= (1ll << s);
+    X = (X - d) >> s;
+    st(i, __int2bfloat16_rn((int)d));
+  }
+  st(0, __int2bfloat16_rn((int)X));
+}
+
+// exponent e of a power of two 2^e (the row and column scales)
+__device__ __forceinline__ int pow2_exp(double x) {
+  return (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
 }
 
 // Slices of [Re M; Im M]; element (R, k) of digit i at sl[i 2N N8 + R N8 + k]
@@ -117,8 +151,8 @@ __global__ void split_matrix_kernel(const double2 *__restrict__ M, size_t ldm, i
   const size_t slab = 2 * (size_t)N * N8;
   const size_t oR = (size_t)r * N8 + k;
   const size_t oI = (size_t)(N + r) * N8 + k;
-  digits(v.x / scale[r], s, p, [&](int i, __nv_bfloat16 d) { sl[i * slab + oR] = d; });
-  digits(v.y / scale[N + r], s, p, [&](int i, __nv_bfloat16 d) { sl[i * slab + oI] = d; });
+  digits(v.x, pow2_exp(scale[r]), s, p, [&](int i, __nv_bfloat16 d) { sl[i * slab + oR] = d; });
+  digits(v.y, pow2_exp(scale[N + r]), s, p, [&](int i, __nv_bfloat16 d) { sl[i * slab + oI] = d; });
 }
 
 // max |entry| per column of [Re X, Im X] (N x 2 nrhs): one block per column.
@@ -151,8 +185,8 @@ __global__ void split_rhs_kernel(const double2 *__restrict__ X, int N, size_t N8
   const int c = (int)(idx / N), k = (int)(idx % N);
   const double2 v = X[idx];
   const size_t w = (size_t)2 * nrhs * N8;
-  digits(v.x / tau[c], s, p, [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)c * N8 + k] = d; });
-  digits(v.y / tau[nrhs + c], s, p,
+  digits(v.x, pow2_exp(tau[c]), s, p, [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)c * N8 + k] = d; });
+  digits(v.y, pow2_exp(tau[nrhs + c]), s, p,
          [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)(nrhs + c) * N8 + k] = d; });
 }
 

@@ -64,7 +64,7 @@ namespace {
 constexpr size_t kSmallN = 256;     // systems up to this size go through the batched path
 constexpr int kMaxBatch = 256;      // requests per batch
 constexpr int kMaxSkips = 8;        // times a waiting request may be overtaken
-constexpr double kRefineTol = 1e-13;
+constexpr double kRefineTol = 1e-11;  // results are promised at a 1e-10 relative residual: a tenfold margin
 constexpr int kMaxRefine = 12;
 
 struct Job {

@@ -14,6 +14,7 @@ namespace qg {
 
 static thread_local char t_err[512] = "";
 std::atomic<unsigned long long> g_launches{0};
+std::atomic<unsigned long long> g_graph_replays{0};
 
 void set_error(const char *fmt, ...) {
   va_list ap;
@@ -163,6 +164,7 @@ extern "C" {
 
 const char *qpms_gpu_last_error(void) { return qg::t_err; }
 unsigned long long qpms_gpu_kernel_launch_count(void) { return qg::g_launches.load(); }
+unsigned long long qpms_gpu_graph_replay_count(void) { return qg::g_graph_replays.load(); }
 
 qpms_trans_calculator *qpms_trans_calculator_init(qpms_l_t lMax, qpms_normalisation_t nt) {
   clear_error();

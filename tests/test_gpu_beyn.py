@@ -167,3 +167,25 @@ def test_split_quadrature_matches_whole(qb):
     r_split = qb.process(*[a + b for a, b in zip(p1, p2)], c, tol, 1)
     assert r_split["eigval"].size == r_whole["eigval"].size >= 1
     _match(r_whole["eigval"], r_split["eigval"], rtol=1e-10)
+
+
+def test_graph_replay_matches_eager(qb, monkeypatch):
+    """The Beyn node loop captures the dense solver's factorisation and solve
+    launch sequences as CUDA graphs at the second node and replays them from
+    the third: the four quadrature sums equal those of eager execution (the
+    same kernels in the same order) to 1e-13, with replays counted."""
+    import qpms_gb300
+    L = qpms_gb300.lib()
+    pos = _square(6, 400e-9)
+    ss = qpms_gb300.ScatteringSystem(pos, 60e-9, -12 + 1.2j, 2.25, 2)
+    c, rr, ri = (2.1 - 0.05j) * EV / HBAR, 0.1 * EV / HBAR, 0.06 * EV / HBAR
+    args = (ss.s, ss.fecv_size, c, rr, ri, 16, 0, 16, 40)
+    monkeypatch.setenv("QPMS_GB300_GRAPHS", "0")
+    r0 = L.qpms_gpu_graph_replay_count()
+    eager = qb.scatsys_quadrature(*args, seed=77, mode=1)
+    assert L.qpms_gpu_graph_replay_count() == r0
+    monkeypatch.delenv("QPMS_GB300_GRAPHS")
+    graph = qb.scatsys_quadrature(*args, seed=77, mode=1)
+    assert L.qpms_gpu_graph_replay_count() - r0 >= 14  # factorisations of nodes 3..16 at least
+    for a, b in zip(eager, graph):
+        assert np.linalg.norm(a - b) <= 1e-13 * np.linalg.norm(a)

@@ -80,7 +80,7 @@ def test_cancel_before_start(q):
             if cancelled.get(t):
                 assert r["status"] == QPMS_ECANCELED and "cancel" in r["error"]
             else:
-                assert r["status"] == 0 and r["residual"] <= 1e-12
+                assert r["status"] == 0 and r["residual"] <= 1e-11  # the server refines to 1e-11
         # the server still serves afterwards
         assert srv.wait(srv.submit(sysm, oms[0]))["status"] == 0
     finally:
