@@ -507,7 +507,13 @@ int lu_solve(cublasHandle_t h, int N, int nb, const T *A, size_t lda, T *B, size
 // digit planes first, so each GEMM may write its result over an operand it
 // read (the column blocks and the right-hand-side blocks are formed in place).
 int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, int nsplit, __nv_bfloat16 *pa,
-                __nv_bfloat16 *pb, cudaStream_t st) {
+                __nv_bfloat16 *pb, cudaStream_t st, cudaStream_t side, cudaEvent_t ev_a, cudaEvent_t ev_d) {
+  // Lookahead (side != nullptr): the trailing update of step k first updates
+  // the next block column, then the diagonal block of step k + 1 is inverted
+  // on the side stream while the rest of the update runs; step k + 1 waits for
+  // it before its column-block product.  The update GEMMs leave SMs free for
+  // the single-CTA inversion.
+  const bool la = side != nullptr;
   TcPlanes P;
   P.a = pa;
   P.b = pb;
@@ -516,18 +522,44 @@ int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, 
   for (int k = 0, blk = 0; k < N; k += nb, ++blk) {
     const int kb = (N - k < nb) ? N - k : nb;
     float2 *Ainv = Dinv + (size_t)blk * nb * nb, *Ck = A + (size_t)k * lda;
-    if ((e = launch_diag<float2>(Ck + k, lda, kb, Ainv, dinfo, st))) return e;
+    if (!la || blk == 0) {
+      if ((e = launch_diag<float2>(Ck + k, lda, kb, Ainv, dinfo, st))) return e;
+    } else {
+      QG_CUDA_TRY(cudaStreamWaitEvent(st, ev_d, 0));
+    }
     // column block k <- column block k x D^-1 (all N rows)
     if ((e = tc_split_ab(Ck, lda, N, kb, Ainv, kb, kb, nsplit, pa, pb, st))) return e;
     P.m = N, P.n = kb, P.k = kb;
+    P.a_plane = P.b_plane = 0;
     if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, Ck, lda, st))) return e;
     const int m2 = N - k - kb;
     if (m2 <= 0) break;
     float2 *Pk = Ck + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = Pk + (size_t)kb * lda;
     // A22 -= P_k A12
     if ((e = tc_split_ab(Pk, lda, m2, kb, A12, lda, m2, nsplit, pa, pb, st))) return e;
-    P.m = m2, P.n = m2, P.k = kb;
-    if ((e = tc_cgemm_planes(P, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
+    if (!la) {
+      P.m = m2, P.n = m2, P.k = kb;
+      if ((e = tc_cgemm_planes(P, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
+      continue;
+    }
+    const int kb1 = m2 < nb ? m2 : nb;  // the next block column
+    const size_t rs = tc_planes_row(kb);
+    TcPlanes Pn = P;
+    Pn.m = m2, Pn.n = kb1, Pn.k = kb;
+    Pn.b_plane = (size_t)m2 * rs;
+    if ((e = tc_cgemm_planes(Pn, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
+    QG_CUDA_TRY(cudaEventRecord(ev_a, st));
+    QG_CUDA_TRY(cudaStreamWaitEvent(side, ev_a, 0));
+    if ((e = launch_diag<float2>(A22, lda, kb1, Dinv + (size_t)(blk + 1) * nb * nb, dinfo, side))) return e;
+    QG_CUDA_TRY(cudaEventRecord(ev_d, side));
+    if (m2 > kb1) {
+      TcPlanes Pr = P;
+      Pr.b = pb + (size_t)kb1 * rs;
+      Pr.m = m2, Pr.n = m2 - kb1, Pr.k = kb;
+      Pr.b_plane = (size_t)m2 * rs;
+      if ((e = tc_cgemm_planes(Pr, -1.f, 1.f, A22 + (size_t)kb1 * lda, lda, A22 + (size_t)kb1 * lda, lda, st)))
+        return e;
+    }
   }
   return QPMS_SUCCESS;
 }
@@ -745,6 +777,14 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   if (tc_split) {
     QG_CUDA_TRY(dev_alloc(&tc_pa, tc_planes_bytes_a(Np, nb, 3)));
     QG_CUDA_TRY(dev_alloc(&tc_pb, tc_planes_bytes_b(std::max(Np, nrhs_max), nb, 3)));
+    const char *la = getenv("QPMS_GB300_LOOKAHEAD");
+    if (!(la && !strcmp(la, "0")) && Np > nb) {
+      int lo = 0, hi = 0;
+      QG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      QG_CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi));
+      QG_CUDA_TRY(cudaEventCreateWithFlags(&ev_a, cudaEventDisableTiming));
+      QG_CUDA_TRY(cudaEventCreateWithFlags(&ev_d, cudaEventDisableTiming));
+    }
   }
   use_ozaki = ozaki_wanted(nrhs_max);
   if (use_ozaki && (dev_alloc(&oz_mat, ozaki_matrix_bytes(N)) != cudaSuccess ||
@@ -793,6 +833,7 @@ cudaError_t DenseSolver::dev_alloc(void *ptr, size_t bytes) {
 }
 
 void DenseSolver::release() {
+  if (side) cudaStreamSynchronize(side);  // its last inversion reads buffers freed below
   for (void *p : {(void *)A, (void *)T64, (void *)Dinv, (void *)work, (void *)rhs_lo, (void *)rp, (void *)r64,
                   (void *)y64, (void *)dinfo, (void *)rs, (void *)res_nrm, oz_mat, oz_work, tc_pa, tc_pb})
     if (p) {
@@ -805,6 +846,11 @@ void DenseSolver::release() {
     if (g->exec) cudaGraphExecDestroy(g->exec);
     *g = Graph();
   }
+  if (side) cudaStreamDestroy(side);
+  if (ev_a) cudaEventDestroy(ev_a);
+  if (ev_d) cudaEventDestroy(ev_d);
+  side = nullptr;
+  ev_a = ev_d = nullptr;
   A = T64 = Dinv = work = rhs_lo = rp = nullptr;
   r64 = y64 = nullptr;
   dinfo = nullptr;
@@ -924,7 +970,7 @@ int DenseSolver::factor_launch(const void *M64, size_t ldm, cudaStream_t st) {
     g_launches.fetch_add(1);
     if (tc_split) {
       e = lu_nopiv_tc(Np, nb, (float2 *)A, Np, (float2 *)Dinv, dinfo, tc_split, (__nv_bfloat16 *)tc_pa,
-                      (__nv_bfloat16 *)tc_pb, st);
+                      (__nv_bfloat16 *)tc_pb, st, side, ev_a, ev_d);
     } else {
       e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
                            (cublasComputeType_t)trail_ct, st);

@@ -61,6 +61,11 @@ struct DenseSolver {
   };
   bool graphs = false;
   Graph gf, gs;
+  // lookahead of the tensor-core LU: the next diagonal block is inverted on
+  // `side` (high priority) while the trailing update runs (QPMS_GB300_LOOKAHEAD=0
+  // turns it off)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_a = nullptr, ev_d = nullptr;
   unsigned long long graph_replays = 0;
 
   int init(int N, int nrhs_max, int mode, unsigned long long seed, cudaMemPool_t pool = nullptr,

@@ -512,6 +512,7 @@ size_t rs_of(int k) { return ((size_t)2 * k + 7) / 8 * 8; }
 
 }  // namespace
 
+size_t tc_planes_row(int k) { return rs_of(k); }
 size_t tc_planes_bytes_a(int m, int k, int nsplit) { return (size_t)nsplit * 2 * m * rs_of(k) * 2; }
 size_t tc_planes_bytes_b(int n, int k, int nsplit) { return (size_t)nsplit * n * rs_of(k) * 2; }
 
@@ -622,8 +623,8 @@ int tc_cgemm_planes(const TcPlanes &P, float alpha, float beta, const float2 *C,
     g.alpha = 0.f;
   }
   const size_t rs = rs_of(P.k);
-  return dispatch(P.a, 2 * P.k, 2 * P.m, P.nsplit, rs, (size_t)2 * P.m * rs, P.b, P.n, P.nsplit, rs,
-                  (size_t)P.n * rs, g, st);
+  return dispatch(P.a, 2 * P.k, 2 * P.m, P.nsplit, rs, P.a_plane ? P.a_plane : (size_t)2 * P.m * rs, P.b, P.n,
+                  P.nsplit, rs, P.b_plane ? P.b_plane : (size_t)P.n * rs, g, st);
 }
 
 int tc_gemm_bf16(const __nv_bfloat16 *A, size_t lda, const __nv_bfloat16 *B, size_t ldb, int m, int n, int k,

@@ -16,7 +16,14 @@ namespace qg {
 struct TcPlanes {
   __nv_bfloat16 *a = nullptr, *b = nullptr;
   int m = 0, n = 0, k = 0, nsplit = 0;
+  // Distance between digit planes in elements; 0: that of planes filled for
+  // exactly (m, n, k) (2m rows of A, n rows of B).  Set to use a block of
+  // rows of larger planes (a / b then point at the first row of the block).
+  size_t a_plane = 0, b_plane = 0;
 };
+
+// Row length (elements) of the digit planes for inner dimension k.
+size_t tc_planes_row(int k);
 
 // Bytes of the A and B planes for (m, n, k, nsplit).
 size_t tc_planes_bytes_a(int m, int k, int nsplit);

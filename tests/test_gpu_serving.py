@@ -136,3 +136,35 @@ def test_admission_by_memory(mix):
     with pytest.raises(QpmsGpuError):
         srv.submit(huge, 3e15)
     srv.close()
+
+
+def test_serving_size_request_vs_oracle(orc):
+    """One request of the serving trace's largest size class (400 spheres of
+    the jittered 400 nm grid, lMax 4: 19,200 unknowns) through the server's
+    mixed path: its FP64 residual is <= 1e-10, and its f solves the oracle's
+    own M = I - T S (assembled by the oracle, 5.9 GB) to a 1e-10 normwise
+    backward error (no LAPACK solve at this size: the backward error needs only
+    M f)."""
+    import qpms_gb300
+    from qpms_gb300.serving import Server
+    rng = np.random.default_rng(400)
+    pos = jittered_square_cluster(400, rng)
+    lMax, om = 4, 2.05 * EV / HBAR
+    ss = qpms_gb300.ScatteringSystem(pos, 50e-9, -12 + 1.2j, 2.25, lMax)
+    assert ss.fecv_size == 19200
+    srv = Server(mode=1, workers=1)
+    try:
+        r = srv.wait(srv.submit(ss, om))
+    finally:
+        srv.close()
+    assert r["status"] == 0 and r["residual"] <= 1e-10, (r["status"], r["residual"])
+    calc = orc.TransCalculator(lMax)
+    Td = orc.tmatrix_sphere_diag(lMax, 50e-9, om, -12 + 1.2j, 2.25)
+    T = np.ascontiguousarray(np.broadcast_to(np.diag(Td), (pos.shape[0], Td.size, Td.size)))
+    k = 1.5 * om / C0
+    M = orc.finite_modeproblem(calc, pos, T, k)
+    a_inc = orc.planewave_full(lMax, pos, np.array([0, 0, k.real]), np.array([1.0, 0, 0]))
+    rhs = (T @ a_inc.reshape(pos.shape[0], -1, 1)).reshape(-1)
+    f = r["f"]
+    be = np.linalg.norm(M @ f - rhs) / (np.linalg.norm(M) * np.linalg.norm(f) + np.linalg.norm(rhs))
+    assert be <= 1e-10, be
