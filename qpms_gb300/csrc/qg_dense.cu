@@ -778,7 +778,7 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
     QG_CUDA_TRY(dev_alloc(&tc_pa, tc_planes_bytes_a(Np, nb, 3)));
     QG_CUDA_TRY(dev_alloc(&tc_pb, tc_planes_bytes_b(std::max(Np, nrhs_max), nb, 3)));
     const char *la = getenv("QPMS_GB300_LOOKAHEAD");
-    if (!(la && !strcmp(la, "0")) && Np > nb) {
+    if (lookahead && !(la && !strcmp(la, "0")) && Np > nb) {
       int lo = 0, hi = 0;
       QG_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
       QG_CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, hi));

@@ -63,7 +63,9 @@ struct DenseSolver {
   Graph gf, gs;
   // lookahead of the tensor-core LU: the next diagonal block is inverted on
   // `side` (high priority) while the trailing update runs (QPMS_GB300_LOOKAHEAD=0
-  // turns it off)
+  // turns it off; so does lookahead = false before init(): a serving loop with
+  // several workers already overlaps the inversions with other requests' work)
+  bool lookahead = true;
   cudaStream_t side = nullptr;
   cudaEvent_t ev_a = nullptr, ev_d = nullptr;
   unsigned long long graph_replays = 0;

@@ -321,6 +321,10 @@ struct qpms_gpu_server {
     DenseSolver ds;
     double res = 0;
     int it = 0;
+    // with several workers the diagonal-block inversions already overlap other
+    // requests' work; the LU's own lookahead then only costs launches
+    // (measured on the serving trace: 94.5 solves/s with it, 100.7 without)
+    ds.lookahead = nworkers == 1;
     if ((e = ds.init((int)N, 1, mode, 0x5eed ^ j->id, pool, st))) return e;
     if ((e = ds.factorize(dM, N, st, true))) return e;
     if ((e = ds.solve(dM, N, db, dx, 1, kRefineTol, kMaxRefine, &res, &it, st))) return e;

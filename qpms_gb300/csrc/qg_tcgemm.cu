@@ -17,15 +17,16 @@
 // the digit products x_s y_t with s + t < nsplit in the same FP32 accumulator
 // (3 products give about 2^-16 relative error, 6 products about FP32's 2^-24).
 //
-// Kernel layout (one CTA per SM, 192 threads):
+// Kernel layout (one CTA per SM, 320 threads):
 //   warp 0  TMA producer: A tile 128 x 64 and B tile BN x 64 (bf16, K-major,
 //           128-byte swizzle) per pipeline stage, STAGES stages;
 //   warp 1  allocates 2 x BN tensor-memory columns (two accumulators), and its
 //           lane 0 issues tcgen05.mma (M 128, N BN, K 16; four per stage),
 //           committing each stage back to the producer and each finished tile
 //           to the epilogue;
-//   warps 2-5  epilogue: tcgen05.ld of the accumulator (each warp its 32-lane
-//           quarter), D = beta C + alpha acc, stores coalesced along the rows,
+//   warps 2-9  epilogue: tcgen05.ld of the accumulator (a warp reads its
+//           32-lane quarter, two warps per quarter with half the columns
+//           each), D = beta C + alpha acc, stores coalesced along the rows,
 //           while the MMA warp fills the other accumulator.
 // Every wait on an mbarrier is bounded (kTimeoutNs); a wait that runs out
 // sets a device error flag (tc_check_error) and the kernel winds down.
@@ -49,6 +50,7 @@ constexpr int BM = 128;  // accumulator rows = tensor-memory lanes
 constexpr int BK = 64;   // bf16 per 128-byte swizzled row
 constexpr unsigned long long kTimeoutNs = 4000000000ull;  // 4 s per wait
 constexpr int kReservedSms = 8;
+constexpr int kEpiWarps = 8;  // warps 2..9: two per tensor-memory lane quarter, half the columns each
 
 __device__ int g_tc_error;
 
@@ -142,6 +144,16 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
                : "memory");
 }
 
+// 32 consecutive accumulator columns of this thread's lane, load and wait in
+// one statement.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+}
 // 64 consecutive accumulator columns of this thread's lane: two loads and one
 // wait in a single statement, so no use of r can be scheduled before the wait.
 __device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&r)[64]) {
@@ -175,7 +187,7 @@ struct Smem {
 };
 
 template <int BN, int STAGES>
-__global__ void __launch_bounds__(192, 1)
+__global__ void __launch_bounds__(64 + 32 * kEpiWarps, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    const GemmArgs g) {
   using S = Smem<BN, STAGES>;
@@ -200,7 +212,7 @@ __global__ void __launch_bounds__(192, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(tfull + b, 1);
-      mbar_init(tempty + b, 128);
+      mbar_init(tempty + b, 32 * kEpiWarps);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -266,46 +278,47 @@ __global__ void __launch_bounds__(192, 1)
     // the accumulator, so the HBM reads of this tile overlap its MMAs; D is
     // then stored column by column (a warp writes 32 consecutive floats).
     const int quad = warp & 3;  // tensor-memory lane quarter this warp may read
+    constexpr int CW = BN / 2;  // columns per epilogue warp: two warps share each lane quarter
+    const int c0 = ((warp - 2) >> 2) * CW;
     const bool has_c = g.beta != 0.f;
     uint32_t t = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++t) {
       const uint32_t b = t & 1, tph = (t >> 1) & 1;
-      const int m0 = (tile % mt) * BM, n0 = (tile / mt) * BN;
+      const int m0 = (tile % mt) * BM, n0 = (tile / mt) * BN + c0;
       const int r = m0 + quad * 32 + lane;
       const bool rok = r < g.Md;
-      float cv[BN];
+      float cv[CW];
       if (has_c && rok) {
 #pragma unroll
-        for (int c = 0; c < BN; ++c) {
+        for (int c = 0; c < CW; ++c) {
           const int j = n0 + c;
           cv[c] = (j < g.Nd) ? g.C[(size_t)j * g.ldc + r] : 0.f;
         }
       }
       if (!(ok = mbar_wait(tfull + b, tph, 4))) break;
       tc_fence_after();
-      const bool full_cols = n0 + BN <= g.Nd;
-#pragma unroll
-      for (int c0 = 0; c0 < BN; c0 += 64) {
-        uint32_t v[64];
+      uint32_t v[CW];
+      if constexpr (CW == 64)
         tmem_ld64(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0, v);
-        if (rok) {
-          float *drow = g.D + (size_t)(n0 + c0) * g.ldd + r;
-          if (full_cols) {
+      else
+        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0, v);
+      if (rok) {
+        float *drow = g.D + (size_t)n0 * g.ldd + r;
+        if (n0 + CW <= g.Nd) {
 #pragma unroll
-            for (int c = 0; c < 64; ++c) {
+          for (int c = 0; c < CW; ++c) {
+            float x = g.alpha * __uint_as_float(v[c]);
+            if (has_c) x += g.beta * cv[c];
+            drow[(size_t)c * g.ldd] = x;
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < CW; ++c) {
+            if (n0 + c < g.Nd) {
               float x = g.alpha * __uint_as_float(v[c]);
-              if (has_c) x += g.beta * cv[c0 + c];
+              if (has_c) x += g.beta * cv[c];
               drow[(size_t)c * g.ldd] = x;
-            }
-          } else {
-#pragma unroll
-            for (int c = 0; c < 64; ++c) {
-              if (n0 + c0 + c < g.Nd) {
-                float x = g.alpha * __uint_as_float(v[c]);
-                if (has_c) x += g.beta * cv[c0 + c];
-                drow[(size_t)c * g.ldd] = x;
-              }
             }
           }
         }
@@ -486,7 +499,7 @@ int launch_gemm(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g,
   const int grid = ntiles < slots ? ntiles : slots;
   if (grid <= 0) return QPMS_SUCCESS;
   KtScope kt(KT_TCGEMM, st, 2.0 * g.Md * (double)g.Nd * (double)g.kblocks * BK * g.npairs);
-  tc_gemm_kernel<BN, STAGES><<<grid, 192, S::kBytes, st>>>(ma, mb, g);
+  tc_gemm_kernel<BN, STAGES><<<grid, 64 + 32 * kEpiWarps, S::kBytes, st>>>(ma, mb, g);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(1);
   return QPMS_SUCCESS;
