@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--requests", type=int, default=N_REQ)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workers", type=int, default=WORKERS, help="worker streams of the serving loop")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 pass of the trace")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="budget of the CPU baseline sample")
@@ -294,9 +295,9 @@ def config_dict(args, ws, specs):
     return {"workload": "serving trace: %d seeded plane-wave scattering requests, 70%% finite clusters of 16-400 "
                         "spheres (jittered 400 nm grid, r 50 nm, lMax 2-4), 30%% single (omega, k) solves of the "
                         "square / honeycomb lattices (a 580 nm, r 80 nm, lMax 3); all submitted at once to %d "
-                        "worker streams" % (len(specs), WORKERS),
+                        "worker streams" % (len(specs), args.workers),
             "requests": len(specs), "mean_unknowns": float(np.mean(unk)), "max_unknowns": int(max(unk)),
-            "workers": WORKERS, "parallelism": "replicas (one trace per rank)" if ws > 1 else "single GPU",
+            "workers": args.workers, "parallelism": "replicas (one trace per rank)" if ws > 1 else "single GPU",
             "l2": "no flush needed: each step assembles and factors %.1f GB of FP64 mode-problem matrices, "
                   ">> 129 MB L2" % (16.0 * sum(u * u for u in unk) / 1e9)}
 
@@ -323,7 +324,7 @@ def run_ours(args, ws, rank, local):
     L = qpms_gb300.lib()
     specs = trace_specs(args.requests)
     reqs, _lat_systems = build_trace(specs)
-    srv = Server(mode=1, workers=WORKERS)
+    srv = Server(mode=1, workers=args.workers)
 
     def barrier():
         if ws > 1:
@@ -405,7 +406,7 @@ def run_ours(args, ws, rank, local):
     # the plain FP64 GPU path on the same full trace
     plain = None
     if rank == 0 and not args.no_plain:
-        psrv = Server(mode=0, workers=WORKERS)
+        psrv = Server(mode=0, workers=args.workers)
         _serve_pass(psrv, reqs[:2], False)
         torch.cuda.synchronize()
         _, psumm, plat = _serve_pass(psrv, reqs, False)

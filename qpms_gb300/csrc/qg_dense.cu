@@ -44,6 +44,7 @@
 #include "qg_internal.h"
 #include "qg_ktimer.h"
 #include "qg_tcgemm.h"
+#include "qg_tuned.h"
 
 namespace qg {
 int blas_handle_get(cublasHandle_t *h);
@@ -104,13 +105,17 @@ __device__ __forceinline__ T rcp(T b) {
 // rows and columns.
 constexpr int kDiagMaxNb = 128, kDiagWarps = 16;
 
+// Complex multiply-add as four fused multiply-adds (no separate product and
+// sum: fewer instructions in the update loops, one rounding per term).
+__device__ __forceinline__ float fmar(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmar(double a, double b, double c) { return fma(a, b, c); }
 template <typename T>
 __device__ __forceinline__ T fma_c(T acc, T a, T b) {  // acc + a b
-  return mk<T>(acc.x + a.x * b.x - a.y * b.y, acc.y + a.x * b.y + a.y * b.x);
+  return mk<T>(fmar(-a.y, b.y, fmar(a.x, b.x, acc.x)), fmar(a.y, b.x, fmar(a.x, b.y, acc.y)));
 }
 template <typename T>
 __device__ __forceinline__ T fms_c(T acc, T a, T b) {  // acc - a b
-  return mk<T>(acc.x - (a.x * b.x - a.y * b.y), acc.y - (a.x * b.y + a.y * b.x));
+  return mk<T>(fmar(a.y, b.y, fmar(-a.x, b.x, acc.x)), fmar(-a.y, b.x, fmar(-a.x, b.y, acc.y)));
 }
 
 template <typename T, int NA>
@@ -298,6 +303,26 @@ __global__ void rbt_cols_kernel(size_t N, size_t ld, double2 *A, int h, const do
 // arithmetic-bound; the FP64 refinement works against the exact transform.
 constexpr int kRbtT = 16, kRbtS = 4 * kRbtT;  // orbits per CTA side, staged entries per side
 
+// FP64 -> FP32, round to nearest even, in integer arithmetic: GB300 runs the
+// conversion instruction on its FP64 pipe (1/64 of the FP32 rate), which made
+// it the bound of this pass.  Below 2^-126 the result is 0 (no FP32
+// subnormals), above the FP32 range infinity; NaN stays NaN.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(bits >> 32), lo = (unsigned)bits;
+  const unsigned sign = hi & 0x80000000u;
+  const unsigned ed = (hi >> 20) & 0x7ffu;
+  if (ed == 0x7ffu) return __int_as_float((int)(sign | 0x7f800000u | (((hi & 0xfffffu) | lo) ? 0x400000u : 0u)));
+  const int e = (int)ed - 1023 + 127;
+  if (e <= 0) return __int_as_float((int)sign);
+  if (e >= 255) return __int_as_float((int)(sign | 0x7f800000u));
+  unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 of the 52 mantissa bits
+  const unsigned rest = lo & 0x1fffffffu;             // the 29 dropped ones
+  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ++m;
+  // a carry out of the mantissa steps the exponent, which is the right result
+  return __int_as_float((int)((sign | ((unsigned)e << 23)) + m));
+}
+
 __device__ __forceinline__ void rbt_pair(float2 &top, float2 &bot, float R, float S) {
   const float is2 = 0.70710678118654752440f;
   const float2 t = top, b = bot;
@@ -323,7 +348,7 @@ __global__ void __launch_bounds__(256) rbt_convert_kernel(const double2 *__restr
     float2 v;
     if (R < N && C < N) {
       const double2 d = rowmaj ? M[(size_t)R * ldm + C] : M[(size_t)C * ldm + R];
-      v = make_float2((float)d.x, (float)d.y);
+      v = make_float2(d2f_rn(d.x), d2f_rn(d.y));
     } else {
       v = make_float2(R == C ? 1.f : 0.f, 0.f);
     }
@@ -343,27 +368,27 @@ __global__ void __launch_bounds__(256) rbt_convert_kernel(const double2 *__restr
       // rows, level 2 (halves Q within blocks of 2Q): pairs (0, 1), (2, 3)
 #pragma unroll
       for (int b = 0; b < 2; ++b) {
-        const float R = (float)r2[b * 2 * Q + i0], Sv = (float)r2[b * 2 * Q + Q + i0];
+        const float R = d2f_rn(r2[b * 2 * Q + i0]), Sv = d2f_rn(r2[b * 2 * Q + Q + i0]);
 #pragma unroll
         for (int p = 0; p < 4; ++p) rbt_pair(x[2 * b][p], x[2 * b + 1][p], R, Sv);
       }
       // rows, level 1 (halves 2Q): pairs (0, 2), (1, 3)
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
-        const float R = (float)r1[q * Q + i0], Sv = (float)r1[2 * Q + q * Q + i0];
+        const float R = d2f_rn(r1[q * Q + i0]), Sv = d2f_rn(r1[2 * Q + q * Q + i0]);
 #pragma unroll
         for (int p = 0; p < 4; ++p) rbt_pair(x[q][p], x[q + 2][p], R, Sv);
       }
       // columns, level 2 then level 1
 #pragma unroll
       for (int b = 0; b < 2; ++b) {
-        const float R = (float)c2[b * 2 * Q + j0], Sv = (float)c2[b * 2 * Q + Q + j0];
+        const float R = d2f_rn(c2[b * 2 * Q + j0]), Sv = d2f_rn(c2[b * 2 * Q + Q + j0]);
 #pragma unroll
         for (int q = 0; q < 4; ++q) rbt_pair(x[q][2 * b], x[q][2 * b + 1], R, Sv);
       }
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
-        const float R = (float)c1[p * Q + j0], Sv = (float)c1[2 * Q + p * Q + j0];
+        const float R = d2f_rn(c1[p * Q + j0]), Sv = d2f_rn(c1[2 * Q + p * Q + j0]);
 #pragma unroll
         for (int q = 0; q < 4; ++q) rbt_pair(x[q][p], x[q][p + 2], R, Sv);
       }
@@ -385,7 +410,7 @@ __global__ void __launch_bounds__(256) rbt_convert_kernel(const double2 *__restr
 
 __global__ void d2f_kernel(size_t n, const double2 *src, float2 *dst) {
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
-    dst[t] = make_float2((float)src[t].x, (float)src[t].y);
+    dst[t] = make_float2(d2f_rn(src[t].x), d2f_rn(src[t].y));
 }
 __global__ void f2d_add_kernel(size_t n, const float2 *src, double2 *dst, int init) {
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
@@ -737,6 +762,17 @@ size_t tc_plane_bytes(int Np, int nrhs_max, int nb) {
 }
 }  // namespace
 
+// Block size of the LU: complex128 factors use 64; complex64 factors use 128
+// for large systems (the trailing updates carry the time) and 64 below the
+// tuned size kTunedNb64Below (the chain of diagonal-block inversions carries
+// it there: an inversion costs nb^3).  QPMS_GB300_LU_NB = 64 / 128 overrides.
+int lu_block_size(int N, int mode) {
+  if (!mode) return 64;
+  const char *ev = getenv("QPMS_GB300_LU_NB");
+  if (ev && (!strcmp(ev, "64") || !strcmp(ev, "128"))) return atoi(ev);
+  return N < kTunedNb64Below ? 64 : 128;
+}
+
 int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed, cudaMemPool_t pool_,
                       cudaStream_t alloc_stream) {
   release();
@@ -756,11 +792,14 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   base_mode = mode;
   base_trail = trail_ct;
   base_tc = tc_split;
-  nb = mode ? 128 : 64;
+  nb = (mode && (nb_pref == 64 || nb_pref == 128)) ? nb_pref : lu_block_size(N, mode);
   const size_t esz = mode ? 8 : 16;
   const size_t NN = (size_t)Np * Np;
   const int nblk = (Np + nb - 1) / nb;
   size_t wsz = std::max<size_t>((size_t)Np * nb, (size_t)nb * std::max(Np, nrhs_max)) * esz;
+  // a mixed solver that falls back to complex128 factors uses the same work
+  // buffer for nb = 64 complex128 column blocks (N x 64 x 16 bytes)
+  if (mode) wsz = std::max<size_t>(wsz, (size_t)std::max(Np, nrhs_max) * 64 * 16);
   if (mode)
     QG_CUDA_TRY(dev_alloc(&A, NN * esz));  // complex64 factors; the FP64 transform is fused into their fill
   else
@@ -811,10 +850,12 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
 }
 
 size_t DenseSolver::footprint(int N, int nrhs, int mode) {
+  // mode 1: sized for 128-wide blocks, the larger of the two block sizes
   const size_t Np = (size_t)(N + 3) / 4 * 4, nb = mode ? 128 : 64, esz = mode ? 8 : 16;
   const size_t nblk = (Np + nb - 1) / nb;
   size_t b = (mode ? Np * Np * esz : Np * Np * 16) + nblk * 2 * nb * nb * esz;
-  b += std::max<size_t>(Np * nb, nb * std::max<size_t>(Np, nrhs)) * esz;
+  b += std::max<size_t>(std::max<size_t>(Np * nb, nb * std::max<size_t>(Np, nrhs)) * esz,
+                        mode ? std::max<size_t>(Np, nrhs) * 64 * 16 : 0);
   b += Np * nrhs * (8 + 16) + (size_t)N * nrhs * 32 + 16 + 4 * Np * 8 + 2 * kOzakiMinRhs * 8;
   if (ozaki_wanted(nrhs)) b += ozaki_matrix_bytes(N) + ozaki_work_bytes(N, nrhs);
   if (mode && tc_digits(nrhs)) b += tc_plane_bytes((int)Np, nrhs, (int)nb);
@@ -934,7 +975,7 @@ int DenseSolver::factorize(const void *M64, size_t ldm, cudaStream_t st, bool ro
   mode = base_mode;
   trail_ct = base_trail;
   tc_split = base_tc;
-  nb = mode ? 128 : 64;
+  nb = (mode && (nb_pref == 64 || nb_pref == 128)) ? nb_pref : lu_block_size(N, mode);
   const unsigned long long key[6] = {(unsigned long long)(uintptr_t)M64, ldm, rowmaj ? 1ull : 0ull,
                                      (unsigned long long)mode, (unsigned long long)tc_split,
                                      use_ozaki ? 1ull : 0ull};

@@ -66,6 +66,9 @@ struct DenseSolver {
   // turns it off; so does lookahead = false before init(): a serving loop with
   // several workers already overlaps the inversions with other requests' work)
   bool lookahead = true;
+  // block size of the complex64 LU: 0 = the tuned choice (lu_block_size), else
+  // 64 or 128; set before init()
+  int nb_pref = 0;
   cudaStream_t side = nullptr;
   cudaEvent_t ev_a = nullptr, ev_d = nullptr;
   unsigned long long graph_replays = 0;

@@ -155,6 +155,53 @@ __global__ void split_matrix_kernel(const double2 *__restrict__ M, size_t ldm, i
   digits(v.y, pow2_exp(scale[N + r]), s, p, [&](int i, __nv_bfloat16 d) { sl[i * slab + oI] = d; });
 }
 
+// The same for a row-major M, four consecutive columns k per thread: each
+// digit plane then takes one 8-byte store per thread for Re and one for Im
+// instead of four 2-byte ones (the narrow stores throttled the load/store
+// unit).  Columns N..N8-1 of the planes receive zeros.
+__device__ __forceinline__ unsigned short next_digit(long long &X, int s, bool last) {
+  long long d;
+  if (last) {
+    d = X;
+  } else {
+    d = X & ((1ll << s) - 1);
+    if (d >= (1ll << (s - 1))) d -= (1ll << s);
+    X = (X - d) >> s;
+  }
+  return __bfloat16_as_ushort(__int2bfloat16_rn((int)d));
+}
+
+__global__ void split_matrix_rows4_kernel(const double2 *__restrict__ M, size_t ldm, int N, size_t N8,
+                                          const double *__restrict__ scale, int s, int p, __nv_bfloat16 *sl) {
+  const size_t q = N8 / 4;
+  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (size_t)N * q) return;
+  const int r = (int)(idx / q), k0 = 4 * (int)(idx % q);
+  const int er = pow2_exp(scale[r]), ei = pow2_exp(scale[N + r]);
+  long long XR[4], XI[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int k = k0 + j;
+    const double2 v = k < N ? M[(size_t)r * ldm + k] : make_double2(0.0, 0.0);
+    XR[j] = fixed_point(v.x, s * p - er);
+    XI[j] = fixed_point(v.y, s * p - ei);
+  }
+  const size_t slab = 2 * (size_t)N * N8;
+  uint2 *oR = reinterpret_cast<uint2 *>(sl + (size_t)r * N8 + k0);
+  uint2 *oI = reinterpret_cast<uint2 *>(sl + (size_t)(N + r) * N8 + k0);
+  for (int i = p - 1; i >= 0; --i) {
+    unsigned short hr[4], hi[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      hr[j] = next_digit(XR[j], s, i == 0);
+      hi[j] = next_digit(XI[j], s, i == 0);
+    }
+    const size_t o = (size_t)i * slab / 4;  // in uint2 (4 bf16) units
+    oR[o] = make_uint2((unsigned)hr[0] | ((unsigned)hr[1] << 16), (unsigned)hr[2] | ((unsigned)hr[3] << 16));
+    oI[o] = make_uint2((unsigned)hi[0] | ((unsigned)hi[1] << 16), (unsigned)hi[2] | ((unsigned)hi[3] << 16));
+  }
+}
+
 // max |entry| per column of [Re X, Im X] (N x 2 nrhs): one block per column.
 __global__ void colmax_kernel(const double2 *__restrict__ X, int N, int nrhs, double *tau) {
   const int C = blockIdx.x;
@@ -275,8 +322,12 @@ int ozaki_split_matrix(const void *M, size_t ldm, bool row_major, int N, void *b
   QG_CUDA_TRY(cudaGetLastError());
   scale_kernel<<<grid1(2 * (size_t)N), 256, 0, st>>>(om->rowmax, 2 * N, om->scale);
   QG_CUDA_TRY(cudaGetLastError());
-  split_matrix_kernel<<<grid1((size_t)N * N), 256, 0, st>>>(Md, ldm, N, om->ld, row_major, om->scale, s, p,
-                                                            (__nv_bfloat16 *)om->slices);
+  if (row_major)
+    split_matrix_rows4_kernel<<<grid1((size_t)N * (om->ld / 4)), 256, 0, st>>>(Md, ldm, N, om->ld, om->scale, s, p,
+                                                                              (__nv_bfloat16 *)om->slices);
+  else
+    split_matrix_kernel<<<grid1((size_t)N * N), 256, 0, st>>>(Md, ldm, N, om->ld, row_major, om->scale, s, p,
+                                                              (__nv_bfloat16 *)om->slices);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(3);
   return QPMS_SUCCESS;

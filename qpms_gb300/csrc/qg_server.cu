@@ -325,6 +325,10 @@ struct qpms_gpu_server {
     // requests' work; the LU's own lookahead then only costs launches
     // (measured on the serving trace: 94.5 solves/s with it, 100.7 without)
     ds.lookahead = nworkers == 1;
+    // and 128-wide blocks at every size: the trailing updates, not the
+    // inversion chain, bound a loaded server (107.5 solves/s against 104.4
+    // with the single-solve tuning's 64-wide blocks below 6144 unknowns)
+    ds.nb_pref = 128;
     if ((e = ds.init((int)N, 1, mode, 0x5eed ^ j->id, pool, st))) return e;
     if ((e = ds.factorize(dM, N, st, true))) return e;
     if ((e = ds.solve(dM, N, db, dx, 1, kRefineTol, kMaxRefine, &res, &it, st))) return e;
