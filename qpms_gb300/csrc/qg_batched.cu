@@ -101,11 +101,34 @@ int batched_solve(cublasHandle_t h, cudaStream_t st, int nm, size_t N, const qg_
     set_error("batched solve: N = %zu above %d", N, kBatchLuMaxN);
     return QPMS_EINVAL;
   }
-  if (mode == 0) {
-    QG_CUDA_TRY(cudaMemcpyAsync(LU, dM, m * N2 * 16, cudaMemcpyDeviceToDevice, st));
+  // log|det| wanted: the complex128 factors it needs also solve the systems
+  // (these small LUs are not the cost of a scan), so the mixed mode takes the
+  // complex128 path outright, with factors in buffers of their own (the
+  // scratch holds complex64 factors in mixed mode)
+  void *LU64 = nullptr, *piv64 = nullptr;
+  if (mode == 1 && logabsdet) {
+    QG_CUDA_TRY(cudaMallocAsync(&LU64, m * N2 * 16, st));
+    if (cudaMallocAsync(&piv64, m * N * 4, st) != cudaSuccess) {
+      cudaFreeAsync(LU64, st);
+      set_error("batched solve: out of device memory");
+      return QPMS_ENOMEM;
+    }
+  }
+  struct Free64 {
+    void *a, *b;
+    cudaStream_t s;
+    ~Free64() {
+      if (a) cudaFreeAsync(a, s);
+      if (b) cudaFreeAsync(b, s);
+    }
+  } free64{LU64, piv64, st};
+  if (mode == 0 || LU64) {
+    void *LUd = LU64 ? LU64 : LU;
+    int *pivd = LU64 ? (int *)piv64 : piv;
+    QG_CUDA_TRY(cudaMemcpyAsync(LUd, dM, m * N2 * 16, cudaMemcpyDeviceToDevice, st));
     QG_CUDA_TRY(cudaMemcpyAsync(dx, db, m * N * 16, cudaMemcpyDeviceToDevice, st));
-    if ((e = batch_getrf_c128(nm, (int)N, LU, piv, info, st))) return e;
-    if ((e = batch_getrs_c128(nm, (int)N, LU, piv, dx, st))) return e;
+    if ((e = batch_getrf_c128(nm, (int)N, LUd, pivd, info, st))) return e;
+    if ((e = batch_getrs_c128(nm, (int)N, LUd, pivd, dx, st))) return e;
     if ((e = launch_residual(nm, N, dM, dx, db, r, rn2, bn2, st))) return e;
     QG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rn2, m * 8, cudaMemcpyDeviceToHost, st));
     QG_CUDA_TRY(cudaMemcpyAsync(hb.data(), bn2, m * 8, cudaMemcpyDeviceToHost, st));
@@ -148,28 +171,13 @@ int batched_solve(cublasHandle_t h, cudaStream_t st, int nm, size_t N, const qg_
       for (int i : bad) fallback_host[i] = 1;
     }
   }
-  if (mode == 0 && fallback_host)
+  if ((mode == 0 || LU64) && fallback_host)
     for (size_t i = 0; i < m; ++i) fallback_host[i] = 0;
   if (logabsdet) {
-    if (mode) {
-      // log|det M| from complex128 factors of the FP64 matrices (complex64
-      // factors hold it to ~1e-5 only; these small LUs are not the cost)
-      void *LU64 = nullptr, *piv64 = nullptr;
-      QG_CUDA_TRY(cudaMallocAsync(&LU64, m * N2 * 16, st));
-      QG_CUDA_TRY(cudaMallocAsync(&piv64, m * N * 4, st));
-      QG_CUDA_TRY(cudaMemcpyAsync(LU64, dM, m * N2 * 16, cudaMemcpyDeviceToDevice, st));
-      e = batch_getrf_c128(nm, (int)N, LU64, (int *)piv64, nullptr, st);
-      if (!e) {
-        logabsdet_kernel<double2><<<(nm + 127) / 128, 128, 0, st>>>(nm, N, (const double2 *)LU64, logabsdet);
-        if (cudaGetLastError() != cudaSuccess) {
-          set_error("logabsdet kernel launch failed");
-          e = QPMS_ERROR;
-        }
-        g_launches.fetch_add(1);
-      }
-      cudaFreeAsync(LU64, st);
-      cudaFreeAsync(piv64, st);
-      if (e) return e;
+    if (LU64) {
+      logabsdet_kernel<double2><<<(nm + 127) / 128, 128, 0, st>>>(nm, N, (const double2 *)LU64, logabsdet);
+      QG_CUDA_TRY(cudaGetLastError());
+      g_launches.fetch_add(1);
     } else {
       logabsdet_kernel<double2><<<(nm + 127) / 128, 128, 0, st>>>(nm, N, (const double2 *)LU, logabsdet);
       QG_CUDA_TRY(cudaGetLastError());

@@ -23,7 +23,8 @@ size_t batched_solve_bytes(int nm, size_t N, int mode);
 // scratch: batched_solve_bytes(nm, N, mode) device bytes.  Host outputs per
 // system (each may be NULL): relative FP64 residual, refinement steps, LU info.
 // logabsdet (device, may be NULL): log|det M_i| from the diagonal of complex128
-// factors (mode 1 factors the FP64 matrices once more for it).
+// factors; with it, mode 1 solves through those complex128 factors as mode 0
+// does (the factors it needs solve the systems too).
 int batched_solve(cublasHandle_t h, cudaStream_t st, int nm, size_t N, const qg_c *dM, const qg_c *db, qg_c *dx,
                   int mode, double tol, int max_iter, void *scratch, double *resid_host, int *iters_host,
                   int *info_host, double *logabsdet, int *fallback_host = nullptr);
