@@ -35,6 +35,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <mutex>
@@ -42,6 +43,7 @@
 #include "qg_internal.h"
 #include "qg_ktimer.h"
 #include "qg_tcgemm.h"
+#include "qg_tuned.h"
 
 namespace qg {
 namespace {
@@ -186,7 +188,7 @@ struct Smem {
   static constexpr int kBytes = STAGES * kStage + 1024 /* align */ + 256 /* barriers */;
 };
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, int NACC>
 __global__ void __launch_bounds__(64 + 32 * kEpiWarps, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    const GemmArgs g) {
@@ -196,9 +198,13 @@ __global__ void __launch_bounds__(64 + 32 * kEpiWarps, 1)
   unsigned char *base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
   uint64_t *full = reinterpret_cast<uint64_t *>(base + STAGES * S::kStage);
   uint64_t *empty = full + STAGES;
-  uint64_t *tfull = empty + STAGES;  // [2]
-  uint64_t *tempty = tfull + 2;      // [2]
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + 2);
+  uint64_t *tfull = empty + STAGES;  // [NACC]
+  uint64_t *tempty = tfull + NACC;   // [NACC]
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(tempty + NACC);
+  // tensor-memory columns: NACC accumulators of BN, allocated as a power of two
+  constexpr uint32_t kTmemCols = (NACC * BN <= 32) ? 32 : (NACC * BN <= 64) ? 64 : (NACC * BN <= 128) ? 128
+                                 : (NACC * BN <= 256) ? 256 : 512;
+  static_assert(NACC * BN <= 512, "accumulators exceed tensor memory");
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mt = (g.Md + BM - 1) / BM, nt = (g.Nd + BN - 1) / BN;
@@ -210,7 +216,7 @@ __global__ void __launch_bounds__(64 + 32 * kEpiWarps, 1)
       mbar_init(full + s, 1);
       mbar_init(empty + s, 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < NACC; ++b) {
       mbar_init(tfull + b, 1);
       mbar_init(tempty + b, 32 * kEpiWarps);
     }
@@ -219,7 +225,7 @@ __global__ void __launch_bounds__(64 + 32 * kEpiWarps, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(2 * BN)
+                 "r"(kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -253,7 +259,7 @@ __global__ void __launch_bounds__(64 + 32 * kEpiWarps, 1)
     uint32_t it = 0, t = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++t) {
-      const uint32_t b = t & 1, tph = (t >> 1) & 1;
+      const uint32_t b = t % NACC, tph = (t / NACC) & 1;
       if (!(ok = mbar_wait(tempty + b, tph ^ 1, 2))) break;
       tc_fence_after();
       const uint32_t dt = tmem + b * BN;
@@ -279,58 +285,67 @@ __global__ void __launch_bounds__(64 + 32 * kEpiWarps, 1)
     // then stored column by column (a warp writes 32 consecutive floats).
     const int quad = warp & 3;  // tensor-memory lane quarter this warp may read
     constexpr int CW = BN / 2;  // columns per epilogue warp: two warps share each lane quarter
+    constexpr int CH = CW < 64 ? CW : 64;  // columns per chunk (registers: C and accumulator of one chunk)
+    constexpr int NCH = CW / CH;
     const int c0 = ((warp - 2) >> 2) * CW;
     const bool has_c = g.beta != 0.f;
     uint32_t t = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++t) {
-      const uint32_t b = t & 1, tph = (t >> 1) & 1;
+      const uint32_t b = t % NACC, tph = (t / NACC) & 1;
       const int m0 = (tile % mt) * BM, n0 = (tile / mt) * BN + c0;
       const int r = m0 + quad * 32 + lane;
       const bool rok = r < g.Md;
-      float cv[CW];
-      if (has_c && rok) {
+      float cv[CH];
+      auto load_c = [&](int nc) {
+        if (has_c && rok) {
 #pragma unroll
-        for (int c = 0; c < CW; ++c) {
-          const int j = n0 + c;
-          cv[c] = (j < g.Nd) ? g.C[(size_t)j * g.ldc + r] : 0.f;
+          for (int c = 0; c < CH; ++c) {
+            const int j = nc + c;
+            cv[c] = (j < g.Nd) ? g.C[(size_t)j * g.ldc + r] : 0.f;
+          }
         }
-      }
+      };
+      load_c(n0);  // the first chunk's C before the wait: its reads overlap the tile's MMAs
       if (!(ok = mbar_wait(tfull + b, tph, 4))) break;
       tc_fence_after();
-      uint32_t v[CW];
-      if constexpr (CW == 64)
-        tmem_ld64(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0, v);
-      else
-        tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0, v);
-      if (rok) {
-        float *drow = g.D + (size_t)n0 * g.ldd + r;
-        if (n0 + CW <= g.Nd) {
 #pragma unroll
-          for (int c = 0; c < CW; ++c) {
-            float x = g.alpha * __uint_as_float(v[c]);
-            if (has_c) x += g.beta * cv[c];
-            drow[(size_t)c * g.ldd] = x;
-          }
-        } else {
+      for (int h = 0; h < NCH; ++h) {
+        const int nc = n0 + h * CH;
+        uint32_t v[CH];
+        if constexpr (CH == 64)
+          tmem_ld64(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0 + h * CH, v);
+        else
+          tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + b * BN + c0 + h * CH, v);
 #pragma unroll
-          for (int c = 0; c < CW; ++c) {
-            if (n0 + c < g.Nd) {
-              float x = g.alpha * __uint_as_float(v[c]);
-              if (has_c) x += g.beta * cv[c];
-              drow[(size_t)c * g.ldd] = x;
-            }
+        for (int c = 0; c < CH; ++c) {
+          float x = g.alpha * __uint_as_float(v[c]);
+          if (has_c) x += g.beta * cv[c];
+          v[c] = __float_as_uint(x);
+        }
+        if (h + 1 < NCH) load_c(nc + CH);  // the next chunk's C, in flight during these stores
+        if (h + 1 == NCH) {                 // the accumulator is read out: free it for the MMAs
+          tc_fence_before();
+          mbar_arrive(tempty + b);
+        }
+        if (rok) {
+          float *drow = g.D + (size_t)nc * g.ldd + r;
+          if (nc + CH <= g.Nd) {
+#pragma unroll
+            for (int c = 0; c < CH; ++c) drow[(size_t)c * g.ldd] = __uint_as_float(v[c]);
+          } else {
+#pragma unroll
+            for (int c = 0; c < CH; ++c)
+              if (nc + c < g.Nd) drow[(size_t)c * g.ldd] = __uint_as_float(v[c]);
           }
         }
       }
-      tc_fence_before();
-      mbar_arrive(tempty + b);
     }
   }
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
   }
 }
 
@@ -481,13 +496,13 @@ int make_map(CUtensorMap *map, const __nv_bfloat16 *p, int kdim, int rows, int p
   return QPMS_SUCCESS;
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, int NACC>
 int launch_gemm(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, cudaStream_t st) {
   using S = Smem<BN, STAGES>;
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(tc_gemm_kernel<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    attr_err = cudaFuncSetAttribute(tc_gemm_kernel<BN, STAGES, NACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     S::kBytes);
   });
   QG_CUDA_TRY(attr_err);
@@ -499,10 +514,34 @@ int launch_gemm(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g,
   const int grid = ntiles < slots ? ntiles : slots;
   if (grid <= 0) return QPMS_SUCCESS;
   KtScope kt(KT_TCGEMM, st, 2.0 * g.Md * (double)g.Nd * (double)g.kblocks * BK * g.npairs);
-  tc_gemm_kernel<BN, STAGES><<<grid, 64 + 32 * kEpiWarps, S::kBytes, st>>>(ma, mb, g);
+  tc_gemm_kernel<BN, STAGES, NACC><<<grid, 64 + 32 * kEpiWarps, S::kBytes, st>>>(ma, mb, g);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(1);
   return QPMS_SUCCESS;
+}
+
+// Pipeline depth and accumulator count of the wide-tile kernel (tuning knob
+// QPMS_GB300_GEMM_PIPE = "SxA": S operand stages, A tensor-memory
+// accumulators; 6x2, 6x3, 7x2 or 7x3).
+int gemm_pipe() {
+  static int v = [] {
+    const char *e = getenv("QPMS_GB300_GEMM_PIPE");
+    if (e && !strcmp(e, "6x2")) return 62;
+    if (e && !strcmp(e, "6x3")) return 63;
+    if (e && !strcmp(e, "7x2")) return 72;
+    if (e && !strcmp(e, "7x3")) return 73;
+    return kTunedGemmPipe;
+  }();
+  return v;
+}
+
+// 256-wide tiles for wide outputs (QPMS_GB300_GEMM_WIDE=0 turns them off).
+bool gemm_wide() {
+  static bool v = [] {
+    const char *e = getenv("QPMS_GB300_GEMM_WIDE");
+    return !(e && !strcmp(e, "0")) && kTunedGemmWide;
+  }();
+  return v;
 }
 
 // N tile by the output width: narrow outputs (right-hand-side blocks) waste
@@ -515,10 +554,22 @@ int dispatch(const __nv_bfloat16 *a, int kdim, int arows, int aplanes, size_t ar
   if ((e = make_map(&ma, a, kdim, arows, aplanes, ars, aplane, BM))) return e;
   if (g.Nd <= 64) {
     if ((e = make_map(&mb, b, kdim, brows, bplanes, brs, bplane, 64))) return e;
-    return launch_gemm<64, 6>(ma, mb, g, st);
+    return launch_gemm<64, 6, 2>(ma, mb, g, st);
+  }
+  // wide outputs: 256-wide tiles (A tiles reloaded half as often, twice the
+  // MMA work per staged byte), when they still fill the SMs twice over
+  const long tiles256 = (long)((g.Md + BM - 1) / BM) * ((g.Nd + 255) / 256);
+  if (g.Nd >= 256 && tiles256 >= 2L * g_num_sms && gemm_wide()) {
+    if ((e = make_map(&mb, b, kdim, brows, bplanes, brs, bplane, 256))) return e;
+    return launch_gemm<256, 4, 2>(ma, mb, g, st);
   }
   if ((e = make_map(&mb, b, kdim, brows, bplanes, brs, bplane, 128))) return e;
-  return launch_gemm<128, 6>(ma, mb, g, st);
+  switch (gemm_pipe()) {
+    case 63: return launch_gemm<128, 6, 3>(ma, mb, g, st);
+    case 72: return launch_gemm<128, 7, 2>(ma, mb, g, st);
+    case 73: return launch_gemm<128, 7, 3>(ma, mb, g, st);
+    default: return launch_gemm<128, 6, 2>(ma, mb, g, st);
+  }
 }
 
 size_t rs_of(int k) { return ((size_t)2 * k + 7) / 8 * 8; }

@@ -10,4 +10,11 @@ namespace qg {
 // and 128-wide ones from it on.
 constexpr int kTunedNb64Below = 6144;
 
+// Operand stages and tensor-memory accumulators of the 128-wide GEMM tile,
+// as 10 x stages + accumulators.
+constexpr int kTunedGemmPipe = 62;
+
+// 256-wide GEMM tiles for outputs wide enough to fill the GPU twice.
+constexpr bool kTunedGemmWide = true;
+
 }  // namespace qg
