@@ -303,26 +303,6 @@ __global__ void rbt_cols_kernel(size_t N, size_t ld, double2 *A, int h, const do
 // arithmetic-bound; the FP64 refinement works against the exact transform.
 constexpr int kRbtT = 16, kRbtS = 4 * kRbtT;  // orbits per CTA side, staged entries per side
 
-// FP64 -> FP32, round to nearest even, in integer arithmetic: GB300 runs the
-// conversion instruction on its FP64 pipe (1/64 of the FP32 rate), which made
-// it the bound of this pass.  Below 2^-126 the result is 0 (no FP32
-// subnormals), above the FP32 range infinity; NaN stays NaN.
-__device__ __forceinline__ float d2f_rn(double x) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-  const unsigned hi = (unsigned)(bits >> 32), lo = (unsigned)bits;
-  const unsigned sign = hi & 0x80000000u;
-  const unsigned ed = (hi >> 20) & 0x7ffu;
-  if (ed == 0x7ffu) return __int_as_float((int)(sign | 0x7f800000u | (((hi & 0xfffffu) | lo) ? 0x400000u : 0u)));
-  const int e = (int)ed - 1023 + 127;
-  if (e <= 0) return __int_as_float((int)sign);
-  if (e >= 255) return __int_as_float((int)(sign | 0x7f800000u));
-  unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 of the 52 mantissa bits
-  const unsigned rest = lo & 0x1fffffffu;             // the 29 dropped ones
-  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ++m;
-  // a carry out of the mantissa steps the exponent, which is the right result
-  return __int_as_float((int)((sign | ((unsigned)e << 23)) + m));
-}
-
 __device__ __forceinline__ void rbt_pair(float2 &top, float2 &bot, float R, float S) {
   const float is2 = 0.70710678118654752440f;
   const float2 t = top, b = bot;
@@ -348,7 +328,7 @@ __global__ void __launch_bounds__(256) rbt_convert_kernel(const double2 *__restr
     float2 v;
     if (R < N && C < N) {
       const double2 d = rowmaj ? M[(size_t)R * ldm + C] : M[(size_t)C * ldm + R];
-      v = make_float2(d2f_rn(d.x), d2f_rn(d.y));
+      v = make_float2((float)d.x, (float)d.y);
     } else {
       v = make_float2(R == C ? 1.f : 0.f, 0.f);
     }
@@ -368,27 +348,27 @@ __global__ void __launch_bounds__(256) rbt_convert_kernel(const double2 *__restr
       // rows, level 2 (halves Q within blocks of 2Q): pairs (0, 1), (2, 3)
 #pragma unroll
       for (int b = 0; b < 2; ++b) {
-        const float R = d2f_rn(r2[b * 2 * Q + i0]), Sv = d2f_rn(r2[b * 2 * Q + Q + i0]);
+        const float R = (float)r2[b * 2 * Q + i0], Sv = (float)r2[b * 2 * Q + Q + i0];
 #pragma unroll
         for (int p = 0; p < 4; ++p) rbt_pair(x[2 * b][p], x[2 * b + 1][p], R, Sv);
       }
       // rows, level 1 (halves 2Q): pairs (0, 2), (1, 3)
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
-        const float R = d2f_rn(r1[q * Q + i0]), Sv = d2f_rn(r1[2 * Q + q * Q + i0]);
+        const float R = (float)r1[q * Q + i0], Sv = (float)r1[2 * Q + q * Q + i0];
 #pragma unroll
         for (int p = 0; p < 4; ++p) rbt_pair(x[q][p], x[q + 2][p], R, Sv);
       }
       // columns, level 2 then level 1
 #pragma unroll
       for (int b = 0; b < 2; ++b) {
-        const float R = d2f_rn(c2[b * 2 * Q + j0]), Sv = d2f_rn(c2[b * 2 * Q + Q + j0]);
+        const float R = (float)c2[b * 2 * Q + j0], Sv = (float)c2[b * 2 * Q + Q + j0];
 #pragma unroll
         for (int q = 0; q < 4; ++q) rbt_pair(x[q][2 * b], x[q][2 * b + 1], R, Sv);
       }
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
-        const float R = d2f_rn(c1[p * Q + j0]), Sv = d2f_rn(c1[2 * Q + p * Q + j0]);
+        const float R = (float)c1[p * Q + j0], Sv = (float)c1[2 * Q + p * Q + j0];
 #pragma unroll
         for (int q = 0; q < 4; ++q) rbt_pair(x[q][p], x[q][p + 2], R, Sv);
       }
@@ -408,9 +388,22 @@ __global__ void __launch_bounds__(256) rbt_convert_kernel(const double2 *__restr
   }
 }
 
+// exp(r / 10) with r uniform in [-1/2, 1/2) from a counter-based generator
+// (splitmix64 of seed + i): the random butterfly diagonals.
+__global__ void rbt_diag_kernel(double *rs, size_t n, unsigned long long seed) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    unsigned long long z = seed + (i + 1) * 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    const double r = (double)(z >> 11) * 0x1.0p-53 - 0.5;
+    rs[i] = exp(r / 10);
+  }
+}
+
 __global__ void d2f_kernel(size_t n, const double2 *src, float2 *dst) {
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
-    dst[t] = make_float2(d2f_rn(src[t].x), d2f_rn(src[t].y));
+    dst[t] = make_float2((float)src[t].x, (float)src[t].y);
 }
 __global__ void f2d_add_kernel(size_t n, const float2 *src, double2 *dst, int init) {
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
@@ -839,13 +832,11 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
       }
     use_ozaki = false;
   }
-  // random butterfly diagonals exp(r/10), r ~ U(-1/2, 1/2): [u level1][u level2][v level1][v level2]
-  std::mt19937_64 gen(seed);
-  std::uniform_real_distribution<double> U(-0.5, 0.5);
-  std::vector<double> h(4 * (size_t)Np);
-  for (auto &v : h) v = exp(U(gen) / 10);
-  QG_CUDA_TRY(cudaMemcpyAsync(rs, h.data(), h.size() * 8, cudaMemcpyHostToDevice, ast));
-  QG_CUDA_TRY(cudaStreamSynchronize(ast));  // h is a local buffer
+  // random butterfly diagonals exp(r/10), r ~ U(-1/2, 1/2): [u level1][u level2][v level1][v level2],
+  // drawn on the device in allocation order (no host work, no synchronisation)
+  rbt_diag_kernel<<<grid1(4 * (size_t)Np), 256, 0, ast>>>(rs, 4 * (size_t)Np, seed);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(1);
   return QPMS_SUCCESS;
 }
 
