@@ -5,7 +5,7 @@ of 60 plane-wave scattering solves (70 % finite clusters of 16-400 spheres on
 a jittered 400 nm grid, r 50 nm, eps -12+1.2i in eps 2.25, lMax 2-4, i.e.
 736-18,912 unknowns; 30 % single (omega, k) solves of the square and
 honeycomb lattices of the dispersion configuration), all submitted at once to
-the continuous-batching server (qpms_gpu_server_*, 4 worker streams).  One
+the continuous-batching server (qpms_gpu_server_*, 8 worker streams).  One
 solve = assembly of M = I - T S (or I - T W), LU, solve for the scattered
 coefficients f at <= 1e-10 relative FP64 residual, sigma_ext.
 
@@ -48,7 +48,7 @@ METRIC = "solves/s + p50/p99 latency vs plain FP64 GPU path at ≤1e-10 rel. res
 UNIT = "solves/s"
 N_REQ = 60
 TRACE_SEED = 5
-WORKERS = 4
+WORKERS = 8
 EPS_I, EPS_E = -12 + 1.2j, 2.25
 C0 = 299792458.0
 

@@ -2,7 +2,7 @@
 contour-integral eigensolver, qpms/beyn.c, and of its two scattering-system
 callers, qpms/scatsystem.c:2280-2372.
 
-Only tests and the CPU leg of the benchmark use this module, as the checker;
+Only tests and the CPU leg of the benchmark use this module, to check results;
 the library never calls it.
 
 The linear algebra is the reference's own LAPACK drivers through numpy:

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library (qpms_gb300/) links,
  * loads or calls this code; only the tests, the smoke check and the CPU
- * baseline leg of bench.py do, and there only as the checker.
+ * baseline leg of bench.py do, and there only to check results.
  *
  * Every function restates one function of the reference (kostyfisik/qpms) and
  * cites the reference file:line it follows.  The reference's third-party

@@ -1,7 +1,7 @@
 """ctypes binding of the oracle library (test infrastructure only).
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
-this module, and only as the checker.
+this module, and only to check results.
 """
 import ctypes as C
 import os

@@ -87,23 +87,25 @@ __device__ __forceinline__ T rcp(T b) {
 }
 
 // ---------------- diagonal block: inverse by Gauss-Jordan ----------------
-// D (kb x kb, kb even and <= 32 NA, column-major in global, leading dimension
-// lda): Ainv (column-major kb x kb, leading dimension kb) receives D^-1, and D
-// is overwritten with D - I (the column-block product that follows turns it
-// into I - D^-1, the slot the back substitution reads).  info is set to 1 on
-// a singular pivot block.  Gauss-Jordan elimination without pivoting (the
-// random butterflies make it safe with high probability, as for the whole
-// LU), two columns per step: with J = {j, j + 1} and the 2 x 2 pivot block P,
+// D (kb x kb, kb even and <= 32 NB, column-major in global, leading
+// dimension lda): Ainv (column-major kb x kb, leading dimension kb) receives
+// D^-1, and D is overwritten with D - I (the column-block product that follows
+// turns it into I - D^-1, the slot the back substitution reads).  info is set
+// to 1 on a singular pivot block.  Gauss-Jordan elimination without pivoting
+// (the random butterflies make it safe with high probability, as for the
+// whole LU), two columns per step: with J = {j, j + 1} and the 2 x 2 pivot
+// block P,
 //   A_JJ <- P^-1,  A_Jc <- P^-1 A_Jc,  A_rJ <- -A_rJ P^-1,
 //   A_rc <- A_rc - A_rJ P^-1 A_Jc        (r, c not in J).
-// One CTA of kDiagWarps warps with the block in registers: thread (lane,
-// warp) holds the NA x NB elements (lane + 32 i, warp + kDiagWarps j), so
-// column c lives in warp c % kDiagWarps and row r in lane r % 32 of every
-// warp.  At each step the two pivot rows and columns are published through
-// two alternating shared-memory slots (one barrier per step); every thread
-// then forms P^-1 itself, updates all its elements and overwrites the pivot
-// rows and columns.
-constexpr int kDiagMaxNb = 128, kDiagWarps = 16;
+// One CTA of 512 threads with the block in registers: thread t holds the
+// NA x NB elements (t % 16 + 16 i, t / 16 + 32 j), rows-heavy so that the
+// per-column factors u = P^-1 A_Jc (the costly part of a step besides the
+// update) are formed for NB = 4 columns only.  Row r lives in the threads with
+// t % 16 == r % 16, column c in those with t / 16 == c % 32.  At each step the
+// two pivot rows and columns are published through two alternating
+// shared-memory slots (one barrier per step); every thread then forms P^-1
+// itself, updates all its elements and overwrites the pivot rows and columns.
+constexpr int kDiagMaxNb = 128, kDiagThreads = 512;
 
 // Complex multiply-add as four fused multiply-adds (no separate product and
 // sum: fewer instructions in the update loops, one rounding per term).
@@ -118,19 +120,18 @@ __device__ __forceinline__ T fms_c(T acc, T a, T b) {  // acc - a b
   return mk<T>(fmar(a.y, b.y, fmar(-a.x, b.x, acc.x)), fmar(-a.y, b.x, fmar(-a.x, b.y, acc.y)));
 }
 
-template <typename T, int NA>
-__global__ void __launch_bounds__(32 * kDiagWarps, 1) diag_inv_kernel(T *D, size_t lda, int kb, T *Ainv, int *info) {
-  constexpr int NB = 32 * NA / kDiagWarps;  // = 2 NA: column tiles per thread
-  static_assert(kDiagWarps == 16, "the step loop splits 32 rows into two halves of 16 columns");
+template <typename T, int NB>
+__global__ void __launch_bounds__(kDiagThreads, 1) diag_inv_kernel(T *D, size_t lda, int kb, T *Ainv, int *info) {
+  constexpr int NA = 2 * NB;  // row tiles per thread: 16 rows x NA, 32 columns x NB
   __shared__ T sc[2][2][kDiagMaxNb];  // [slot][e][r] = a_(r, j+e)
   __shared__ T sr[2][2][kDiagMaxNb];  // [slot][e][c] = a_(j+e, c)
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lr = threadIdx.x & 15, lc = threadIdx.x >> 4;
   T a[NA][NB];
 #pragma unroll
   for (int j = 0; j < NB; ++j)
 #pragma unroll
     for (int i = 0; i < NA; ++i) {
-      const int r = lane + 32 * i, c = w + kDiagWarps * j;
+      const int r = lr + 16 * i, c = lc + 32 * j;
       a[i][j] = mk<T>(0, 0);
       if (r < kb && c < kb) {
         T v = D[(size_t)c * lda + r];
@@ -140,32 +141,32 @@ __global__ void __launch_bounds__(32 * kDiagWarps, 1) diag_inv_kernel(T *D, size
       }
     }
   bool zero = false;
-  // Step (j, j + 1), j = 32 jt + 16 h + q, q even: rows j, j + 1 are tile row
-  // jt of lanes 16 h + q, 16 h + q + 1; columns j, j + 1 are tile column
-  // 2 jt + h of warps q, q + 1.  jt and h are unrolled, so every register
-  // index is static.
+  // Step (j, j + 1), j = 32 ct + 16 h + q, q even: rows j, j + 1 are tile row
+  // 2 ct + h of the threads with lr = q, q + 1; columns j, j + 1 are tile
+  // column ct of the threads with lc = 16 h + q, 16 h + q + 1.  ct and h are
+  // unrolled, so every register index is static.
 #pragma unroll
-  for (int jt = 0; jt < NA; ++jt) {
+  for (int ct = 0; ct < NB; ++ct) {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int ct = 2 * jt + h;
+      const int rt = 2 * ct + h;
       for (int q = 0; q < 16; q += 2) {
-        const int j = 32 * jt + 16 * h + q;
+        const int j = 32 * ct + 16 * h + q;
         if (j >= kb) break;  // uniform
-        const int rl = 16 * h + q, slot = (j >> 1) & 1;
-        if (lane == rl || lane == rl + 1) {
-          const int e = lane - rl;
+        const int slot = (j >> 1) & 1, cl = 16 * h + q;
+        if (lr == q || lr == q + 1) {
+          const int e = lr - q;
 #pragma unroll
           for (int jj = 0; jj < NB; ++jj) {
-            const int c = w + kDiagWarps * jj;
-            if (c < kb) sr[slot][e][c] = a[jt][jj];
+            const int c = lc + 32 * jj;
+            if (c < kb) sr[slot][e][c] = a[rt][jj];
           }
         }
-        if (w == q || w == q + 1) {
-          const int e = w - q;
+        if (lc == cl || lc == cl + 1) {
+          const int e = lc - cl;
 #pragma unroll
           for (int i = 0; i < NA; ++i) {
-            const int r = lane + 32 * i;
+            const int r = lr + 16 * i;
             if (r < kb) sc[slot][e][r] = a[i][ct];
           }
         }
@@ -179,38 +180,44 @@ __global__ void __launch_bounds__(32 * kDiagWarps, 1) diag_inv_kernel(T *D, size
         const T q00 = mul(p11, dinv), q11 = mul(p00, dinv);
         const T q01 = mk<T>(-(p01.x * dinv.x - p01.y * dinv.y), -(p01.x * dinv.y + p01.y * dinv.x));
         const T q10 = mk<T>(-(p10.x * dinv.x - p10.y * dinv.y), -(p10.x * dinv.y + p10.y * dinv.x));
-        T f0[NA], f1[NA];
-#pragma unroll
-        for (int i = 0; i < NA; ++i) {
-          const int r = min(lane + 32 * i, kb - 1);  // rows >= kb are padding, never stored
-          f0[i] = sc[slot][0][r];
-          f1[i] = sc[slot][1][r];
-        }
-        // every element: a_rc -= a_rj u0_c + a_r,j+1 u1_c with u = P^-1 A_Jc;
-        // the pivot rows and columns are overwritten right after
+        // u = P^-1 A_Jc for this thread's NB columns
+        T u0[NB], u1[NB];
 #pragma unroll
         for (int jj = 0; jj < NB; ++jj) {
-          const int c = w + kDiagWarps * jj;
-          if (c >= kb) continue;  // warp-uniform
+          const int c = min(lc + 32 * jj, kb - 1);  // columns >= kb are padding, never stored
           const T x0 = sr[slot][0][c], x1 = sr[slot][1][c];
-          const T u0 = fma_c(mul(q00, x0), q01, x1), u1 = fma_c(mul(q10, x0), q11, x1);
-#pragma unroll
-          for (int i = 0; i < NA; ++i) {
-            if (32 * i >= kb) continue;  // uniform
-            a[i][jj] = fms_c(fms_c(a[i][jj], f0[i], u0), f1[i], u1);
-          }
-          if (lane == rl) a[jt][jj] = u0;
-          if (lane == rl + 1) a[jt][jj] = u1;
+          u0[jj] = fma_c(mul(q00, x0), q01, x1);
+          u1[jj] = fma_c(mul(q10, x0), q11, x1);
         }
-        if (w == q || w == q + 1) {  // columns j + e: -A_rJ P^-1, the pivot block P^-1
-          const T qa = (w == q) ? q00 : q01, qb = (w == q) ? q10 : q11;
+        // every element: a_rc -= a_rj u0_c + a_r,j+1 u1_c; the pivot rows and
+        // columns are overwritten right after
+#pragma unroll
+        for (int i = 0; i < NA; ++i) {
+          if (16 * i >= kb) continue;  // uniform
+          const int r = min(lr + 16 * i, kb - 1);  // rows >= kb are padding, never stored
+          const T f0 = sc[slot][0][r], f1 = sc[slot][1][r];
+#pragma unroll
+          for (int jj = 0; jj < NB; ++jj) a[i][jj] = fms_c(fms_c(a[i][jj], f0, u0[jj]), f1, u1[jj]);
+          if (i == rt) {  // static: the pivot rows' tile row
+            if (lr == q)
+#pragma unroll
+              for (int jj = 0; jj < NB; ++jj) a[i][jj] = u0[jj];
+            if (lr == q + 1)
+#pragma unroll
+              for (int jj = 0; jj < NB; ++jj) a[i][jj] = u1[jj];
+          }
+        }
+        if (lc == cl || lc == cl + 1) {  // columns j + e: -A_rJ P^-1, the pivot block P^-1
+          const bool e0 = lc == cl;
+          const T qa = e0 ? q00 : q01, qb = e0 ? q10 : q11;
 #pragma unroll
           for (int i = 0; i < NA; ++i) {
-            const T g = fma_c(mul(f0[i], qa), f1[i], qb);
+            const int r = min(lr + 16 * i, kb - 1);
+            const T g = fma_c(mul(sc[slot][0][r], qa), sc[slot][1][r], qb);
             a[i][ct] = mk<T>(-g.x, -g.y);
           }
-          if (lane == rl) a[jt][ct] = qa;
-          if (lane == rl + 1) a[jt][ct] = qb;
+          if (lr == q) a[rt][ct] = qa;
+          if (lr == q + 1) a[rt][ct] = qb;
         }
       }
     }
@@ -220,7 +227,7 @@ __global__ void __launch_bounds__(32 * kDiagWarps, 1) diag_inv_kernel(T *D, size
   for (int j = 0; j < NB; ++j)
 #pragma unroll
     for (int i = 0; i < NA; ++i) {
-      const int r = lane + 32 * i, c = w + kDiagWarps * j;
+      const int r = lr + 16 * i, c = lc + 32 * j;
       if (r < kb && c < kb) Ainv[c * kb + r] = a[i][j];
     }
 }
@@ -228,16 +235,16 @@ __global__ void __launch_bounds__(32 * kDiagWarps, 1) diag_inv_kernel(T *D, size
 // Invert one diagonal block (kb <= 128; complex128 blocks up to 64).
 template <typename T>
 int launch_diag(T *D, size_t lda, int kb, T *Ainv, int *info, cudaStream_t st) {
-  constexpr int kMaxNa = sizeof(T) == 16 ? 2 : 4;  // complex128 blocks: nb <= 64
-  if (kb <= 0 || kb > 32 * kMaxNa || (kb & 1)) {
+  constexpr int kMaxNb = sizeof(T) == 16 ? 2 : 4;  // complex128 blocks: nb <= 64
+  if (kb <= 0 || kb > 32 * kMaxNb || (kb & 1)) {
     set_error("diagonal block of size %d not supported", kb);
     return QPMS_EINVAL;
   }
   KtScope kt(KT_DIAGLU, st, 8.0 * kb * (double)kb * kb);
   if (kb <= 64)
-    diag_inv_kernel<T, 2><<<1, 32 * kDiagWarps, 0, st>>>(D, lda, kb, Ainv, info);
+    diag_inv_kernel<T, 2><<<1, kDiagThreads, 0, st>>>(D, lda, kb, Ainv, info);
   else
-    diag_inv_kernel<T, kMaxNa><<<1, 32 * kDiagWarps, 0, st>>>(D, lda, kb, Ainv, info);
+    diag_inv_kernel<T, kMaxNb><<<1, kDiagThreads, 0, st>>>(D, lda, kb, Ainv, info);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(1);
   return QPMS_SUCCESS;
@@ -625,27 +632,36 @@ template <typename T>
 __global__ void __launch_bounds__(256) panel_apply_kernel(const T *__restrict__ Pn, size_t lda, int msub, int mout,
                                                           int kb, const T *V, size_t ldv, T *Bsub, size_t ldb,
                                                           T *Xout, size_t ldx, int nrhs) {
+  constexpr int kPer = 128 / kSubSlices;               // panel entries per thread (kb <= 128)
   __shared__ T sV[128 * kSmallRhs];                  // [c][l]
   __shared__ T sP[kSubSlices * kSmallRhs * kSubRows];  // [slice][c][r]
   const int tid = threadIdx.x;
+  const int m = msub + mout;
+  const int r = tid % kSubRows, sl = tid / kSubRows;
+  const int row = blockIdx.x * kSubRows + r;
+  // the panel entries are requested first, so their latency overlaps the
+  // staging of V (one round trip to memory per step, not two)
+  T pv[kPer];
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    const int l = sl + q * kSubSlices;
+    pv[q] = (row < m && l < kb) ? Pn[(size_t)l * lda + row] : mk<T>(0, 0);
+  }
   for (int t = tid; t < kb * nrhs; t += blockDim.x) {
     const int c = t / kb, l = t - c * kb;
     sV[c * kb + l] = V[(size_t)c * ldv + l];
   }
   __syncthreads();
-  const int m = msub + mout;
-  const int r = tid % kSubRows, sl = tid / kSubRows;
-  const int row = blockIdx.x * kSubRows + r;
   T acc[kSmallRhs];
 #pragma unroll
   for (int c = 0; c < kSmallRhs; ++c) acc[c] = mk<T>(0, 0);
-  if (row < m) {
-#pragma unroll 16
-    for (int l = sl; l < kb; l += kSubSlices) {
-      const T p = Pn[(size_t)l * lda + row];
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    const int l = sl + q * kSubSlices;
+    if (l < kb) {
 #pragma unroll
       for (int c = 0; c < kSmallRhs; ++c)
-        if (c < nrhs) acc[c] = fma_c(acc[c], p, sV[c * kb + l]);
+        if (c < nrhs) acc[c] = fma_c(acc[c], pv[q], sV[c * kb + l]);
     }
   }
 #pragma unroll

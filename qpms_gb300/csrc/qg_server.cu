@@ -324,6 +324,8 @@ struct qpms_gpu_server {
     // with several workers the diagonal-block inversions already overlap other
     // requests' work; the LU's own lookahead then only costs launches
     // (measured on the serving trace: 94.5 solves/s with it, 100.7 without)
+    // (also measured: lookahead only for requests above 4,096 / 8,192 / 12,000
+    // unknowns, 106-109 solves/s against 116 without)
     ds.lookahead = nworkers == 1;
     // and 128-wide blocks at every size: the trailing updates, not the
     // inversion chain, bound a loaded server (107.5 solves/s against 104.4

@@ -1,5 +1,5 @@
 """Pins the oracle's axially symmetric T-matrices (extended-boundary-condition
-method, tmatrices.c:615-894) before they serve as the checker:
+method, tmatrices.c:615-894) before the GPU results are checked against them:
 
 * a sphere given as an arc reproduces the Mie T-matrix (Bohren-Huffman-pinned
   oracle) at every l, for a metal and a dielectric: 1e-12;

@@ -1,4 +1,4 @@
-"""Pins the oracle's Beyn eigensolver (oracle/beyn.py) before it serves as the checker.
+"""Pins the oracle's Beyn eigensolver (oracle/beyn.py) before the GPU eigenvalues are checked against it.
 
 * The reference's own Beyn test problems, with eigenvalues known independently:
   tests/tbeyn2.c (Beyn's example 4.9, a random quadratic eigenproblem

@@ -1,4 +1,4 @@
-"""Pins the oracle's 2D Ewald sums before they serve as the checker.
+"""Pins the oracle's 2D Ewald sums before the GPU sums are checked against them.
 
 * The reference's own eta-invariance test (tests/test_scalar_ewald32.c with the
   seven parameter sets of tests/CMakeLists.txt:87-120): sigma_total = sigma_S +

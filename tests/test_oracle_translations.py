@@ -1,4 +1,4 @@
-"""Pins the oracle's translation path before it is trusted as the checker.
+"""Pins the oracle's translation path before the GPU coefficients are checked against it.
 
 * Gaunt coefficients against the reference's own gaunt.c (compiled from its
   sources into oracle/_ref by oracle/build_oracle.py) and against sympy's exact
