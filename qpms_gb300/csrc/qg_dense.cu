@@ -34,6 +34,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <random>
 #include <vector>
@@ -532,59 +533,108 @@ int lu_solve(cublasHandle_t h, int N, int nb, const T *A, size_t lda, T *B, size
 // digit planes first, so each GEMM may write its result over an operand it
 // read (the column blocks and the right-hand-side blocks are formed in place).
 int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, int nsplit, __nv_bfloat16 *pa,
-                __nv_bfloat16 *pb, cudaStream_t st, cudaStream_t side, cudaEvent_t ev_a, cudaEvent_t ev_d) {
-  // Lookahead (side != nullptr): the trailing update of step k first updates
-  // the next block column, then the diagonal block of step k + 1 is inverted
-  // on the side stream while the rest of the update runs; step k + 1 waits for
-  // it before its column-block product.  The update GEMMs leave SMs free for
-  // the single-CTA inversion.
+                __nv_bfloat16 *pb, cudaStream_t st, cudaStream_t side, cudaEvent_t ev_a, cudaEvent_t ev_d,
+                bool pairs) {
+  // Lookahead (side != nullptr): the trailing update first updates the next
+  // block column, then the next diagonal block is inverted on the side stream
+  // while the rest of the update runs; the next step waits for it before its
+  // column-block product.  The update GEMMs leave SMs free for the single-CTA
+  // inversion.
+  // Pairs: blocks are taken two at a time.  Step k's update is applied first
+  // to block column k + 1 and block row k + 1 only (two narrow products), block
+  // k + 1 is inverted and its column block multiplied, and the rest of both
+  // updates runs as one product with K = 2 nb:
+  //   A33 -= [P_k P_k+1] [A12_k; A12_k+1]   (rows and columns past block k + 1).
+  // The same sums as two updates in sequence, with half the passes over the
+  // trailing matrix (its read and write bound a K = nb update on HBM).
   const bool la = side != nullptr;
   TcPlanes P;
   P.a = pa;
   P.b = pb;
   P.nsplit = nsplit;
   int e;
-  for (int k = 0, blk = 0; k < N; k += nb, ++blk) {
+  // column block k <- column block k x D^-1 (all N rows)
+  auto colprod = [&](int k, int kb, const float2 *Ainv) -> int {
+    float2 *Ck = A + (size_t)k * lda;
+    int e2;
+    if ((e2 = tc_split_ab(Ck, lda, N, kb, Ainv, kb, kb, nsplit, pa, pb, st))) return e2;
+    TcPlanes Q = P;
+    Q.m = N, Q.n = kb, Q.k = kb;
+    return tc_cgemm_planes(Q, 1.f, 0.f, nullptr, 0, Ck, lda, st);
+  };
+  // rows and columns r0.. (m of each) -= A(r0.., c0..c0+kk) A(c0..c0+kk, r0..);
+  // with lookahead the first block column first, then the inversion of that
+  // diagonal block (slot next_blk of Dinv) on the side stream
+  auto trailing = [&](int r0, int c0, int kk, int m, int next_blk) -> int {
+    float2 *C = A + (size_t)r0 * lda + r0;
+    int e2;
+    if ((e2 = tc_split_ab(A + (size_t)c0 * lda + r0, lda, m, kk, A + (size_t)r0 * lda + c0, lda, m, nsplit, pa, pb,
+                          st)))
+      return e2;
+    TcPlanes Q = P;
+    Q.m = m, Q.k = kk;
+    if (!la) {
+      Q.n = m;
+      return tc_cgemm_planes(Q, -1.f, 1.f, C, lda, C, lda, st);
+    }
+    const int kb1 = m < nb ? m : nb;
+    const size_t rs = tc_planes_row(kk);
+    Q.n = kb1;
+    Q.b_plane = (size_t)m * rs;
+    if ((e2 = tc_cgemm_planes(Q, -1.f, 1.f, C, lda, C, lda, st))) return e2;
+    QG_CUDA_TRY(cudaEventRecord(ev_a, st));
+    QG_CUDA_TRY(cudaStreamWaitEvent(side, ev_a, 0));
+    if ((e2 = launch_diag<float2>(C, lda, kb1, Dinv + (size_t)next_blk * nb * nb, dinfo, side))) return e2;
+    QG_CUDA_TRY(cudaEventRecord(ev_d, side));
+    if (m > kb1) {
+      Q.b = pb + (size_t)kb1 * rs;
+      Q.n = m - kb1;
+      if ((e2 = tc_cgemm_planes(Q, -1.f, 1.f, C + (size_t)kb1 * lda, lda, C + (size_t)kb1 * lda, lda, st)))
+        return e2;
+    }
+    return QPMS_SUCCESS;
+  };
+  for (int k = 0, blk = 0; k < N;) {
     const int kb = (N - k < nb) ? N - k : nb;
-    float2 *Ainv = Dinv + (size_t)blk * nb * nb, *Ck = A + (size_t)k * lda;
+    float2 *Ainv = Dinv + (size_t)blk * nb * nb;
     if (!la || blk == 0) {
-      if ((e = launch_diag<float2>(Ck + k, lda, kb, Ainv, dinfo, st))) return e;
+      if ((e = launch_diag<float2>(A + (size_t)k * lda + k, lda, kb, Ainv, dinfo, st))) return e;
     } else {
       QG_CUDA_TRY(cudaStreamWaitEvent(st, ev_d, 0));
     }
-    // column block k <- column block k x D^-1 (all N rows)
-    if ((e = tc_split_ab(Ck, lda, N, kb, Ainv, kb, kb, nsplit, pa, pb, st))) return e;
-    P.m = N, P.n = kb, P.k = kb;
-    P.a_plane = P.b_plane = 0;
-    if ((e = tc_cgemm_planes(P, 1.f, 0.f, nullptr, 0, Ck, lda, st))) return e;
+    if ((e = colprod(k, kb, Ainv))) return e;
     const int m2 = N - k - kb;
     if (m2 <= 0) break;
-    float2 *Pk = Ck + k + kb, *A12 = A + (size_t)(k + kb) * lda + k, *A22 = Pk + (size_t)kb * lda;
-    // A22 -= P_k A12
-    if ((e = tc_split_ab(Pk, lda, m2, kb, A12, lda, m2, nsplit, pa, pb, st))) return e;
-    if (!la) {
-      P.m = m2, P.n = m2, P.k = kb;
-      if ((e = tc_cgemm_planes(P, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
+    if (!pairs) {
+      if ((e = trailing(k + kb, k, kb, m2, blk + 1))) return e;
+      k += kb;
+      ++blk;
       continue;
     }
-    const int kb1 = m2 < nb ? m2 : nb;  // the next block column
+    const int k2 = k + kb, kb2 = m2 < nb ? m2 : nb, m3 = m2 - kb2;
+    float2 *A22 = A + (size_t)k2 * lda + k2;
+    if ((e = tc_split_ab(A + (size_t)k * lda + k2, lda, m2, kb, A + (size_t)k2 * lda + k, lda, m2, nsplit, pa, pb,
+                         st)))
+      return e;
     const size_t rs = tc_planes_row(kb);
-    TcPlanes Pn = P;
-    Pn.m = m2, Pn.n = kb1, Pn.k = kb;
-    Pn.b_plane = (size_t)m2 * rs;
-    if ((e = tc_cgemm_planes(Pn, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
-    QG_CUDA_TRY(cudaEventRecord(ev_a, st));
-    QG_CUDA_TRY(cudaStreamWaitEvent(side, ev_a, 0));
-    if ((e = launch_diag<float2>(A22, lda, kb1, Dinv + (size_t)(blk + 1) * nb * nb, dinfo, side))) return e;
-    QG_CUDA_TRY(cudaEventRecord(ev_d, side));
-    if (m2 > kb1) {
-      TcPlanes Pr = P;
-      Pr.b = pb + (size_t)kb1 * rs;
-      Pr.m = m2, Pr.n = m2 - kb1, Pr.k = kb;
-      Pr.b_plane = (size_t)m2 * rs;
-      if ((e = tc_cgemm_planes(Pr, -1.f, 1.f, A22 + (size_t)kb1 * lda, lda, A22 + (size_t)kb1 * lda, lda, st)))
+    TcPlanes Q = P;
+    Q.k = kb;
+    Q.m = m2, Q.n = kb2;  // block column k2, every row below block k
+    Q.b_plane = (size_t)m2 * rs;
+    if ((e = tc_cgemm_planes(Q, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
+    if (m3 > 0) {  // block row k2, right of block k2: the first kb2 rows of the A planes
+      Q.m = kb2, Q.a_plane = (size_t)2 * m2 * rs;
+      Q.b = pb + (size_t)kb2 * rs, Q.n = m3;
+      if ((e = tc_cgemm_planes(Q, -1.f, 1.f, A22 + (size_t)kb2 * lda, lda, A22 + (size_t)kb2 * lda, lda, st)))
         return e;
     }
+    float2 *Ainv2 = Dinv + (size_t)(blk + 1) * nb * nb;
+    if ((e = launch_diag<float2>(A22, lda, kb2, Ainv2, dinfo, st))) return e;
+    if ((e = colprod(k2, kb2, Ainv2))) return e;
+    if (m3 <= 0) break;
+    if ((e = trailing(k2 + kb2, k, kb + kb2, m3, blk + 2))) return e;
+    k += kb + kb2;
+    blk += 2;
   }
   return QPMS_SUCCESS;
 }
@@ -713,6 +763,244 @@ int lu_solve_small(int N, int nb, const T *A, size_t lda, T *B, size_t ldb, int 
   return QPMS_SUCCESS;
 }
 
+// ---------------- the same sweeps in one launch each ----------------
+// The two substitutions of lu_solve_small as one launch per sweep, over tiles
+// of kSweepRows rows (nb a multiple of kSweepRows, at most 128).
+//   forward, tile rows r of block j:  b_r <- b_r - sum_{k<j} P_k(r, :) b_k
+//   backward:                          b_r <- b_r - sum_{k>j} Q_k(r, :) b_k,
+// after which the last tile of block j to finish writes the block's solution
+// x_j = b_j - (I - D_j^-1) b_j.  b_k is final once every tile of block k has
+// written its rows (per-block completion counters).  A tile keeps its sums
+// over all k in registers and writes its rows once.
+// Tiles are handed out in dependency order by an atomic ticket (ascending
+// rows forward, descending backward): a tile only waits for tiles with earlier
+// tickets, which CTAs already running hold, so the waits end whatever number
+// of CTAs is resident (the argument of single-pass decoupled look-back scans).
+// Every wait is bounded (kSweepWaitNs); a wait that runs out sets the error
+// word, which makes the other CTAs leave too.
+// Sync words of one pair of sweeps (sweep_words): [0] error, [1] forward
+// ticket, [2] backward ticket, [3, 3 + nblk) forward block counters,
+// [3 + nblk, 3 + 2 nblk) backward block counters.
+// Thread t of a CTA handles row (t / 32) * 4 + (t % 32) / 8 of the tile and
+// the columns l = t % 8 + 8 q of each block: the eight partial sums of a row
+// sit in eight adjacent lanes and meet by shuffles.
+constexpr int kSweepRows = 32;
+constexpr unsigned long long kSweepWaitNs = 2000000000ull;  // 2 s
+size_t sweep_words(int nblk) { return 3 + 2 * (size_t)nblk; }
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long sweep_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait until *cnt >= need; false if the error word is set or the wait ran out
+// (which sets it).
+__device__ bool sweep_wait(const unsigned *cnt, unsigned need, unsigned *err) {
+  if (ld_acquire(cnt) >= need) return true;
+  const unsigned long long t0 = sweep_clock();
+  for (;;) {
+    __nanosleep(64);
+    if (ld_acquire(cnt) >= need) return true;
+    if (ld_acquire(err)) return false;
+    if (sweep_clock() - t0 > kSweepWaitNs) {
+      atomicExch(err, 1u);
+      return false;
+    }
+  }
+}
+
+// the 16 entries l = sl + 8 q < kb of one row of a block column (col0: its
+// first column at that row)
+template <typename T>
+__device__ __forceinline__ void sweep_load(const T *col0, size_t lda, int kb, bool rowok, int sl, T (&pv)[16]) {
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int l = sl + 8 * q;
+    pv[q] = (rowok && l < kb) ? col0[(size_t)l * lda] : mk<T>(0, 0);
+  }
+}
+// b_k (kb x nrhs from row k0 of B) into shared memory as v[c * 128 + l],
+// through L2 (other CTAs wrote it)
+template <typename T>
+__device__ __forceinline__ void sweep_stage(T *v, const T *B, size_t ldb, int k0, int kb, int nrhs) {
+  for (int i = threadIdx.x; i < kb * nrhs; i += blockDim.x) {
+    const int c = i / kb, l = i - c * kb;
+    v[c * 128 + l] = __ldcg(B + (size_t)c * ldb + k0 + l);
+  }
+}
+template <typename T>
+__device__ __forceinline__ void sweep_fma(const T (&pv)[16], const T *v, int kb, int nrhs, int sl,
+                                          T (&acc)[kSmallRhs]) {
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const int l = sl + 8 * q;
+    if (l < kb) {
+#pragma unroll
+      for (int c = 0; c < kSmallRhs; ++c)
+        if (c < nrhs) acc[c] = fma_c(acc[c], pv[q], v[c * 128 + l]);
+    }
+  }
+}
+// sums over the eight lanes of a row (every lane gets the total)
+template <typename T>
+__device__ __forceinline__ void sweep_reduce(T (&acc)[kSmallRhs], int nrhs) {
+#pragma unroll
+  for (int c = 0; c < kSmallRhs; ++c)
+    if (c < nrhs) {
+#pragma unroll
+      for (int o = 1; o < 8; o <<= 1) {
+        acc[c].x += __shfl_xor_sync(0xffffffffu, acc[c].x, o);
+        acc[c].y += __shfl_xor_sync(0xffffffffu, acc[c].y, o);
+      }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 2) sweep_fwd_kernel(const T *__restrict__ A, size_t lda, int N, int nb, T *B,
+                                                           size_t ldb, int nrhs, unsigned *sync) {
+  __shared__ T sV[128 * kSmallRhs];
+  __shared__ int s_tile, s_abort;
+  const int tid = threadIdx.x, lane = tid & 31, sl = lane & 7, rr = (tid >> 5) * 4 + (lane >> 3);
+  const int ntiles = (N + kSweepRows - 1) / kSweepRows;
+  unsigned *err = sync, *ticket = sync + 1, *cnt = sync + 3;
+  if (tid == 0) s_abort = 0;
+  for (;;) {
+    if (tid == 0) s_tile = (int)atomicAdd(ticket, 1u);
+    __syncthreads();
+    const int t = s_tile;
+    if (t >= ntiles) return;
+    const int row0 = t * kSweepRows, j = row0 / nb, row = row0 + rr;
+    const bool rowok = row < N;
+    T acc[kSmallRhs];
+#pragma unroll
+    for (int c = 0; c < kSmallRhs; ++c) acc[c] = mk<T>(0, 0);
+    for (int k = 0; k < j; ++k) {  // the blocks above are full: kb = nb
+      T pv[16];
+      sweep_load(A + (size_t)k * nb * lda + row, lda, nb, rowok, sl, pv);
+      if (tid == 0 && !sweep_wait(cnt + k, (unsigned)(nb / kSweepRows), err)) s_abort = 1;
+      __syncthreads();  // also: every thread is done with sV of step k - 1
+      if (s_abort) return;
+      sweep_stage(sV, B, ldb, k * nb, nb, nrhs);
+      __syncthreads();
+      sweep_fma(pv, sV, nb, nrhs, sl, acc);
+    }
+    sweep_reduce(acc, nrhs);
+    if (sl == 0 && rowok) {
+#pragma unroll
+      for (int c = 0; c < kSmallRhs; ++c)
+        if (c < nrhs) {
+          T *d = B + (size_t)c * ldb + row;
+          *d = sub(__ldcg(d), acc[c]);
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicAdd(cnt + j, 1u);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256, 2) sweep_bwd_kernel(const T *__restrict__ A, size_t lda, int N, int nb, T *B,
+                                                           size_t ldb, T *X, size_t ldx, int nrhs, unsigned *sync) {
+  __shared__ T sV[128 * kSmallRhs];
+  __shared__ int s_tile, s_abort, s_last;
+  const int tid = threadIdx.x, lane = tid & 31, sl = lane & 7, rr = (tid >> 5) * 4 + (lane >> 3);
+  const int ntiles = (N + kSweepRows - 1) / kSweepRows, nblk = (N + nb - 1) / nb;
+  unsigned *err = sync, *ticket = sync + 2, *cnt = sync + 3 + nblk;
+  if (tid == 0) s_abort = 0;
+  for (;;) {
+    if (tid == 0) s_tile = (int)atomicAdd(ticket, 1u);
+    __syncthreads();
+    const int tk = s_tile;
+    if (tk >= ntiles) return;
+    const int t = ntiles - 1 - tk, row0 = t * kSweepRows, j = row0 / nb, row = row0 + rr;
+    const bool rowok = row < N;
+    T acc[kSmallRhs];
+#pragma unroll
+    for (int c = 0; c < kSmallRhs; ++c) acc[c] = mk<T>(0, 0);
+    for (int k = nblk - 1; k > j; --k) {
+      const int k0 = k * nb, kb = min(nb, N - k0);
+      T pv[16];
+      sweep_load(A + (size_t)k0 * lda + row, lda, kb, rowok, sl, pv);
+      if (tid == 0 && !sweep_wait(cnt + k, (unsigned)((kb + kSweepRows - 1) / kSweepRows), err)) s_abort = 1;
+      __syncthreads();
+      if (s_abort) return;
+      sweep_stage(sV, B, ldb, k0, kb, nrhs);
+      __syncthreads();
+      sweep_fma(pv, sV, kb, nrhs, sl, acc);
+    }
+    sweep_reduce(acc, nrhs);
+    if (sl == 0 && rowok) {
+#pragma unroll
+      for (int c = 0; c < kSmallRhs; ++c)
+        if (c < nrhs) {
+          T *d = B + (size_t)c * ldb + row;
+          *d = sub(__ldcg(d), acc[c]);
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    const int j0 = j * nb, kbj = min(nb, N - j0);
+    if (tid == 0) {
+      s_last = atomicAdd(cnt + j, 1u) == (unsigned)((kbj + kSweepRows - 1) / kSweepRows) - 1;
+      if (s_last) __threadfence();
+    }
+    __syncthreads();
+    if (s_last) {  // every tile of block j is done: x_j = b_j - (I - D_j^-1) b_j
+      sweep_stage(sV, B, ldb, j0, kbj, nrhs);
+      __syncthreads();
+      for (int rs = 0; rs < kbj; rs += kSweepRows) {
+        const int ri = rs + rr;
+        const bool ok = ri < kbj;
+        T pv[16], a2[kSmallRhs];
+#pragma unroll
+        for (int c = 0; c < kSmallRhs; ++c) a2[c] = mk<T>(0, 0);
+        sweep_load(A + (size_t)j0 * lda + j0 + ri, lda, kbj, ok, sl, pv);
+        sweep_fma(pv, sV, kbj, nrhs, sl, a2);
+        sweep_reduce(a2, nrhs);
+        if (sl == 0 && ok) {
+#pragma unroll
+          for (int c = 0; c < kSmallRhs; ++c)
+            if (c < nrhs) X[(size_t)c * ldx + j0 + ri] = sub(sV[c * 128 + ri], a2[c]);
+        }
+      }
+    }
+  }
+}
+
+// lu_solve_small's result in two launches.  sync: sweep_words(nblk) words
+// whose error word is zero; the others are cleared here.
+template <typename T>
+int lu_solve_sweep(int N, int nb, const T *A, size_t lda, T *B, size_t ldb, int nrhs, T *X, unsigned *sync,
+                   cudaStream_t st) {
+  const int nblk = (N + nb - 1) / nb, ntiles = (N + kSweepRows - 1) / kSweepRows;
+  int dev = 0, sms = 0;
+  QG_CUDA_TRY(cudaGetDevice(&dev));
+  QG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = std::min(ntiles, 2 * std::max(sms, 1));
+  QG_CUDA_TRY(cudaMemsetAsync(sync + 1, 0, (sweep_words(nblk) - 1) * sizeof(unsigned), st));
+  sweep_fwd_kernel<T><<<grid, 256, 0, st>>>(A, lda, N, nb, B, ldb, nrhs, sync);
+  QG_CUDA_TRY(cudaGetLastError());
+  sweep_bwd_kernel<T><<<grid, 256, 0, st>>>(A, lda, N, nb, B, ldb, X, ldb, nrhs, sync);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(2);
+  return QPMS_SUCCESS;
+}
+
+// Environment override of a solver's boolean choice: 1 / 0 when the variable
+// holds one of the two words, else -1 (the solver's own setting).
+int env_choice(const char *name, const char *yes, const char *no) {
+  const char *e = getenv(name);
+  if (e && !strcmp(e, yes)) return 1;
+  if (e && !strcmp(e, no)) return 0;
+  return -1;
+}
+
 }  // namespace
 
 // ---------------- solver object ----------------
@@ -822,9 +1110,14 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   QG_CUDA_TRY(dev_alloc(&dinfo, 16));
   QG_CUDA_TRY(dev_alloc(&rs, (size_t)4 * Np * sizeof(double)));
   QG_CUDA_TRY(dev_alloc(&res_nrm, (size_t)2 * kOzakiMinRhs * sizeof(double)));
+  // sized for 64-wide blocks (the complex128 fallback's), the larger count
+  const size_t sweep_bytes = sweep_words((Np + 63) / 64) * sizeof(unsigned);
+  QG_CUDA_TRY(dev_alloc(&sweep, sweep_bytes));
+  QG_CUDA_TRY(cudaMemsetAsync(sweep, 0, sweep_bytes, ast));
   if (tc_split) {
-    QG_CUDA_TRY(dev_alloc(&tc_pa, tc_planes_bytes_a(Np, nb, 3)));
-    QG_CUDA_TRY(dev_alloc(&tc_pb, tc_planes_bytes_b(std::max(Np, nrhs_max), nb, 3)));
+    // K up to 2 nb: the combined update of a pair of blocks
+    QG_CUDA_TRY(dev_alloc(&tc_pa, tc_planes_bytes_a(Np, 2 * nb, 3)));
+    QG_CUDA_TRY(dev_alloc(&tc_pb, tc_planes_bytes_b(std::max(Np, nrhs_max), 2 * nb, 3)));
     const char *la = getenv("QPMS_GB300_LOOKAHEAD");
     if (lookahead && !(la && !strcmp(la, "0")) && Np > nb) {
       int lo = 0, hi = 0;
@@ -864,9 +1157,10 @@ size_t DenseSolver::footprint(int N, int nrhs, int mode) {
   b += std::max<size_t>(std::max<size_t>(Np * nb, nb * std::max<size_t>(Np, nrhs)) * esz,
                         mode ? std::max<size_t>(Np, nrhs) * 64 * 16 : 0);
   b += Np * nrhs * (8 + 16) + (size_t)N * nrhs * 32 + 16 + 4 * Np * 8 + 2 * kOzakiMinRhs * 8;
+  b += sweep_words((int)((Np + 63) / 64)) * sizeof(unsigned);
   if (ozaki_wanted(nrhs)) b += ozaki_matrix_bytes(N) + ozaki_work_bytes(N, nrhs);
-  if (mode && tc_digits(nrhs)) b += tc_plane_bytes((int)Np, nrhs, (int)nb);
-  return b + 12 * 512;  // allocation rounding
+  if (mode && tc_digits(nrhs)) b += tc_plane_bytes((int)Np, nrhs, 2 * (int)nb);
+  return b + 13 * 512;  // allocation rounding
 }
 
 bool ozaki_wanted(int nrhs_max) {
@@ -883,7 +1177,8 @@ cudaError_t DenseSolver::dev_alloc(void *ptr, size_t bytes) {
 void DenseSolver::release() {
   if (side) cudaStreamSynchronize(side);  // its last inversion reads buffers freed below
   for (void *p : {(void *)A, (void *)T64, (void *)Dinv, (void *)work, (void *)rhs_lo, (void *)rp, (void *)r64,
-                  (void *)y64, (void *)dinfo, (void *)rs, (void *)res_nrm, oz_mat, oz_work, tc_pa, tc_pb})
+                  (void *)y64, (void *)dinfo, (void *)rs, (void *)res_nrm, (void *)sweep, oz_mat, oz_work, tc_pa,
+                  tc_pb})
     if (p) {
       if (pool)
         cudaFreeAsync(p, ast);
@@ -904,6 +1199,7 @@ void DenseSolver::release() {
   dinfo = nullptr;
   rs = nullptr;
   res_nrm = nullptr;
+  sweep = nullptr;
   oz_mat = oz_work = nullptr;
   tc_pa = tc_pb = nullptr;
   use_ozaki = false;
@@ -1018,7 +1314,7 @@ int DenseSolver::factor_launch(const void *M64, size_t ldm, cudaStream_t st) {
     g_launches.fetch_add(1);
     if (tc_split) {
       e = lu_nopiv_tc(Np, nb, (float2 *)A, Np, (float2 *)Dinv, dinfo, tc_split, (__nv_bfloat16 *)tc_pa,
-                      (__nv_bfloat16 *)tc_pb, st, side, ev_a, ev_d);
+                      (__nv_bfloat16 *)tc_pb, st, side, ev_a, ev_d, use_pairs());
     } else {
       e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
                            (cublasComputeType_t)trail_ct, st);
@@ -1051,6 +1347,15 @@ int DenseSolver::factor_launch(const void *M64, size_t ldm, cudaStream_t st) {
   g_launches.fetch_add(2);
   return lu_nopiv<double2>(h, Np, nb, (double2 *)T64, Np, (double2 *)Dinv, (double2 *)work, dinfo,
                            CUBLAS_COMPUTE_64F, st);
+}
+
+bool DenseSolver::use_sweeps() const {
+  static const int v = env_choice("QPMS_GB300_SUBST", "sweep", "steps");
+  return v < 0 ? sweeps : v == 1;
+}
+bool DenseSolver::use_pairs() const {
+  static const int v = env_choice("QPMS_GB300_LU_PAIRS", "1", "0");
+  return v < 0 ? pairs : v == 1;
 }
 
 int DenseSolver::check_info(cudaStream_t st) {
@@ -1089,7 +1394,10 @@ int DenseSolver::apply_launch(const void *R, size_t ldr, void *Y, size_t ldy, in
     g_launches.fetch_add(1);
     const float2 *sol = (const float2 *)rhs_lo;
     if (nrhs <= kSmallRhs) {
-      e = lu_solve_small<float2>(Np, nb, (const float2 *)A, Np, (float2 *)rhs_lo, Np, nrhs, (float2 *)work, st);
+      e = !use_sweeps() ? lu_solve_small<float2>(Np, nb, (const float2 *)A, Np, (float2 *)rhs_lo, Np, nrhs,
+                                                 (float2 *)work, st)
+                        : lu_solve_sweep<float2>(Np, nb, (const float2 *)A, Np, (float2 *)rhs_lo, Np, nrhs,
+                                                 (float2 *)work, sweep, st);
       sol = (const float2 *)work;
     } else if (tc_split) {
       e = lu_solve_tc(Np, nb, (const float2 *)A, Np, (float2 *)rhs_lo, Np, nrhs, 3, (__nv_bfloat16 *)tc_pa,
@@ -1104,7 +1412,10 @@ int DenseSolver::apply_launch(const void *R, size_t ldr, void *Y, size_t ldy, in
     g_launches.fetch_add(1);
   } else {
     if (nrhs <= kSmallRhs) {
-      e = lu_solve_small<double2>(Np, nb, (const double2 *)T64, Np, (double2 *)rp, Np, nrhs, (double2 *)work, st);
+      e = !use_sweeps() ? lu_solve_small<double2>(Np, nb, (const double2 *)T64, Np, (double2 *)rp, Np, nrhs,
+                                                  (double2 *)work, st)
+                        : lu_solve_sweep<double2>(Np, nb, (const double2 *)T64, Np, (double2 *)rp, Np, nrhs,
+                                                  (double2 *)work, sweep, st);
       if (!e)
         QG_CUDA_TRY(cudaMemcpyAsync(rp, work, n * 16, cudaMemcpyDeviceToDevice, st));
     } else {
@@ -1171,8 +1482,15 @@ int DenseSolver::solve(const void *M64, size_t ldm, const void *B, void *X, int 
     QG_CUDA_TRY(cudaMemsetAsync(nrm, 0, 8, st));
     norm2_kernel<<<grid1(n), 256, 0, st>>>(n, (const double2 *)r64, nrm);
     QG_CUDA_TRY(cudaMemcpyAsync(&hr, nrm, 8, cudaMemcpyDeviceToHost, st));
+    unsigned sweep_err = 0;
+    if (nrhs <= kSmallRhs) QG_CUDA_TRY(cudaMemcpyAsync(&sweep_err, sweep, 4, cudaMemcpyDeviceToHost, st));
     QG_CUDA_TRY(cudaStreamSynchronize(st));
     g_launches.fetch_add(1);
+    if (sweep_err) {
+      QG_CUDA_TRY(cudaMemsetAsync(sweep, 0, 4, st));
+      set_error("dense solver: a substitution sweep waited more than 2 s for a block");
+      return QPMS_ERROR;
+    }
     rel = sqrt(hr / (hb > 0 ? hb : 1));
     if (rel <= tol) break;
     if (rel >= 0.5 * prev || it == max_iter + extra) {  // stagnated

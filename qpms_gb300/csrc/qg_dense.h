@@ -28,6 +28,7 @@ struct DenseSolver {
   int *dinfo = nullptr;    // zero-pivot flag, then two doubles of norm scratch
   double *rs = nullptr;    // butterfly diagonals [u L1][u L2][v L1][v L2], Np each
   double *res_nrm = nullptr;  // norms scratch of the few-right-hand-side residual kernel
+  unsigned *sweep = nullptr;  // sync words of the one-launch substitution sweeps (error word first)
 
   // Stream-ordered allocation: with a memory pool, every buffer comes from
   // cudaMallocFromPoolAsync on stream `ast` and returns to it in release(),
@@ -66,6 +67,15 @@ struct DenseSolver {
   // turns it off; so does lookahead = false before init(): a serving loop with
   // several workers already overlaps the inversions with other requests' work)
   bool lookahead = true;
+  // few-right-hand-side substitutions as one launch per sweep (tiles that wait
+  // on per-block counters) rather than one launch per block and sweep; a
+  // serving loop with several workers turns it off: the waiting CTAs would hold
+  // SMs that other requests' GEMMs need (QPMS_GB300_SUBST=sweep / steps
+  // overrides either way)
+  bool sweeps = true;
+  // tensor-core LU by pairs of blocks: one trailing update with K = 2 nb per
+  // pair (QPMS_GB300_LU_PAIRS=1 / 0 overrides either way)
+  bool pairs = true;
   // block size of the complex64 LU: 0 = the tuned choice (lu_block_size), else
   // 64 or 128; set before init()
   int nb_pref = 0;
@@ -96,6 +106,8 @@ struct DenseSolver {
  private:
   cudaError_t dev_alloc(void *ptr, size_t bytes);
   int check_info(cudaStream_t st);  // zero-pivot flag of the last factorisation
+  bool use_sweeps() const;
+  bool use_pairs() const;
   int factor_launch(const void *M64, size_t ldm, cudaStream_t st);  // factorize_current's launches
   int apply_launch(const void *R, size_t ldr, void *Y, size_t ldy, int nrhs, cudaStream_t st);
   template <class F>

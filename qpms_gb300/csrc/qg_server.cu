@@ -331,6 +331,10 @@ struct qpms_gpu_server {
     // inversion chain, bound a loaded server (107.5 solves/s against 104.4
     // with the single-solve tuning's 64-wide blocks below 6144 unknowns)
     ds.nb_pref = 128;
+    // and the substitutions as one launch per block and sweep: the one-launch
+    // sweeps' waiting CTAs hold SMs the other requests' GEMMs need (121.0 /
+    // 121.3 solves/s with them, 123.4 without, 8 workers)
+    ds.sweeps = nworkers == 1;
     if ((e = ds.init((int)N, 1, mode, 0x5eed ^ j->id, pool, st))) return e;
     if ((e = ds.factorize(dM, N, st, true))) return e;
     if ((e = ds.solve(dM, N, db, dx, 1, kRefineTol, kMaxRefine, &res, &it, st))) return e;

@@ -86,3 +86,30 @@ def test_single_rhs_refinement(torch_cuda, cond):
     # FP64 attains a relative residual of about eps * cond at best
     assert res <= max(1e-12, 1e-16 * cond * 100), (res, it)
     assert np.linalg.norm(X - ref) <= cond * 1e-13 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("nrhs", [1, 3, 8])
+def test_one_application_of_the_sweeps(torch_cuda, nrhs):
+    """Refinement capped at zero steps, complex128 factors: one application of
+    the factors through the one-launch substitution sweeps must already give
+    the solution to FP64 accuracy.  A tile that read a block of the right-hand
+    side before the tiles writing it had finished would show here (refinement
+    would hide it).  4,100 unknowns: 65 blocks of 64, the last one 4 rows wide;
+    three right-hand-side sets against one matrix."""
+    import scipy.linalg as sla
+    import qpms_gb300
+    N = 4100
+    rng = np.random.default_rng(41 + nrhs)
+    M = (rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))) / np.sqrt(N) + 2 * np.eye(N)
+    lu = sla.lu_factor(M)
+    L = qpms_gb300.lib()
+    L.qpms_gpu_testing_set_max_refine(0)
+    try:
+        for rep in range(3):
+            B = rng.normal(size=(N, nrhs)) + 1j * rng.normal(size=(N, nrhs))
+            X, res, it = _solve(torch_cuda, M, B, 0)
+            ref = sla.lu_solve(lu, B)
+            assert it == 1
+            assert np.linalg.norm(X - ref) <= 1e-11 * np.linalg.norm(ref), rep
+    finally:
+        L.qpms_gpu_testing_set_max_refine(-1)
