@@ -141,6 +141,44 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "fallback": True}
 
 
+def isolated_tc_rate(peaks):
+    """The dominant kernel with the GPU to itself: one mixed dense solve of
+    14,400 unknowns (random well-conditioned matrix, one right-hand side), every
+    tc_gemm launch timed with CUDA events on its stream (second of two solves)."""
+    import torch
+    import qpms_gb300
+    from qpms_gb300 import _lib
+    L = qpms_gb300.lib()
+    dev = torch.device("cuda:0")
+    N = 14400
+    g = torch.Generator(device=dev)
+    g.manual_seed(N)
+    M = torch.randn(N, N, dtype=torch.complex128, device=dev, generator=g) / N ** 0.5
+    M += 2 * torch.eye(N, dtype=torch.complex128, device=dev)
+    B = torch.randn(1, N, dtype=torch.complex128, device=dev, generator=g)
+    X = torch.empty_like(B)
+    res, it = np.zeros(1), np.zeros(1, dtype=np.int32)
+    for rep in range(2):
+        if rep == 1:
+            _lib.kernel_timing(True)
+        rc = L.qpms_gpu_dense_solve(N, 1, M.data_ptr(), B.data_ptr(), X.data_ptr(), 1, res.ctypes.data,
+                                    it.ctypes.data)
+        if rc:
+            return {"error": qpms_gb300.last_error()}
+    torch.cuda.synchronize()
+    kt = _lib.kernel_timing_get()
+    _lib.kernel_timing(False)
+    del M, B, X
+    if "tc_gemm" not in kt:
+        return None
+    ms, work, n = kt["tc_gemm"]
+    ach = work / (ms * 1e-3) / 1e12
+    pk = peaks.get("bf16_tflops") or 1900.0
+    return {"achieved": ach, "peak": pk, "frac": ach / pk, "unit": "TFLOP/s", "launches": n,
+            "ms": ms, "peak_source": "measured burst (MEASURED_PEAKS.json bf16_tflops)",
+            "of": "one 14,400-unknown mixed dense solve alone on the GPU (%d tc_gemm launches)" % n}
+
+
 def profile_json(name):
     """A figure from a committed ncu summary under profiles/ (json), if present."""
     try:
@@ -421,6 +459,8 @@ def run_ours(args, ws, rank, local):
     if rank == 0:
         peaks = measured_peaks()
         roof, kernels = roofline(kt, peaks)
+        if roof and roof.get("bound") == "tensor":
+            roof["isolated"] = isolated_tc_rate(peaks)
         cb = None if args.no_cpu else cpu_baseline(specs, args.cpu_seconds, sig)
         smry = clk.summary(local)
         sections = run_sections(args)
@@ -465,7 +505,10 @@ def roofline(kt, peaks):
                 else "fallback 1.7 PFLOP/s sustained",
                 "kernel": "tc_gemm_kernel (tcgen05 bf16 digit products, FP32 accumulate)",
                 "launches": n, "ms_per_launch": ms / n,
-                "work": "executed bf16 flops (2 x rows x cols x K per digit product)"}
+                "work": "executed bf16 flops (2 x rows x cols x K per digit product)",
+                "concurrency": "the worker streams run concurrently: a launch's CUDA-event duration includes the "
+                               "time it shares the SMs with other requests' kernels, so this is the per-launch "
+                               "rate under that sharing (the same kernel alone: 'isolated')"}
     else:
         fp64 = fp64_probe()
         ach = work / (ms * 1e-3) / 1e9

@@ -534,20 +534,22 @@ int lu_solve(cublasHandle_t h, int N, int nb, const T *A, size_t lda, T *B, size
 // read (the column blocks and the right-hand-side blocks are formed in place).
 int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, int nsplit, __nv_bfloat16 *pa,
                 __nv_bfloat16 *pb, cudaStream_t st, cudaStream_t side, cudaEvent_t ev_a, cudaEvent_t ev_d,
-                bool pairs) {
+                int group) {
   // Lookahead (side != nullptr): the trailing update first updates the next
   // block column, then the next diagonal block is inverted on the side stream
   // while the rest of the update runs; the next step waits for it before its
   // column-block product.  The update GEMMs leave SMs free for the single-CTA
   // inversion.
-  // Pairs: blocks are taken two at a time.  Step k's update is applied first
-  // to block column k + 1 and block row k + 1 only (two narrow products), block
-  // k + 1 is inverted and its column block multiplied, and the rest of both
-  // updates runs as one product with K = 2 nb:
-  //   A33 -= [P_k P_k+1] [A12_k; A12_k+1]   (rows and columns past block k + 1).
-  // The same sums as two updates in sequence, with half the passes over the
-  // trailing matrix (its read and write bound a K = nb update on HBM).
+  // Groups: blocks are taken `group` at a time.  Within a group, block i's
+  // update is applied at once only to the group's later block columns (every
+  // row below block i) and to the group's later block rows (the columns past
+  // the group): two narrow products.  The rest of the group's updates runs as
+  // one product with K = the group's width past its last block:
+  //   A33 -= [P_0 ... P_g-1] [A12_0; ...; A12_g-1].
+  // The same sums as g updates in sequence, with 1/g of the passes over the
+  // trailing matrix (its complex64 read and write bound a K = nb update on HBM).
   const bool la = side != nullptr;
+  if (group < 1) group = 1;
   TcPlanes P;
   P.a = pa;
   P.b = pb;
@@ -594,47 +596,42 @@ int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, 
     }
     return QPMS_SUCCESS;
   };
-  for (int k = 0, blk = 0; k < N;) {
-    const int kb = (N - k < nb) ? N - k : nb;
-    float2 *Ainv = Dinv + (size_t)blk * nb * nb;
-    if (!la || blk == 0) {
-      if ((e = launch_diag<float2>(A + (size_t)k * lda + k, lda, kb, Ainv, dinfo, st))) return e;
-    } else {
-      QG_CUDA_TRY(cudaStreamWaitEvent(st, ev_d, 0));
-    }
-    if ((e = colprod(k, kb, Ainv))) return e;
-    const int m2 = N - k - kb;
-    if (m2 <= 0) break;
-    if (!pairs) {
-      if ((e = trailing(k + kb, k, kb, m2, blk + 1))) return e;
-      k += kb;
-      ++blk;
-      continue;
-    }
-    const int k2 = k + kb, kb2 = m2 < nb ? m2 : nb, m3 = m2 - kb2;
-    float2 *A22 = A + (size_t)k2 * lda + k2;
-    if ((e = tc_split_ab(A + (size_t)k * lda + k2, lda, m2, kb, A + (size_t)k2 * lda + k, lda, m2, nsplit, pa, pb,
-                         st)))
-      return e;
-    const size_t rs = tc_planes_row(kb);
-    TcPlanes Q = P;
-    Q.k = kb;
-    Q.m = m2, Q.n = kb2;  // block column k2, every row below block k
-    Q.b_plane = (size_t)m2 * rs;
-    if ((e = tc_cgemm_planes(Q, -1.f, 1.f, A22, lda, A22, lda, st))) return e;
-    if (m3 > 0) {  // block row k2, right of block k2: the first kb2 rows of the A planes
-      Q.m = kb2, Q.a_plane = (size_t)2 * m2 * rs;
-      Q.b = pb + (size_t)kb2 * rs, Q.n = m3;
-      if ((e = tc_cgemm_planes(Q, -1.f, 1.f, A22 + (size_t)kb2 * lda, lda, A22 + (size_t)kb2 * lda, lda, st)))
+  for (int k = 0, blk = 0; k < N;) {  // one group per pass: blocks blk.., columns k..ge
+    const int ge = std::min<long>((long)k + (long)group * nb, (long)N);
+    for (int ki = k, b = blk; ki < ge; ki += nb, ++b) {
+      const int kbi = (N - ki < nb) ? N - ki : nb, ke = ki + kbi, mi = N - ke;
+      float2 *Ainv = Dinv + (size_t)b * nb * nb;
+      if (ki > k || !la || blk == 0) {
+        if ((e = launch_diag<float2>(A + (size_t)ki * lda + ki, lda, kbi, Ainv, dinfo, st))) return e;
+      } else {
+        QG_CUDA_TRY(cudaStreamWaitEvent(st, ev_d, 0));
+      }
+      if ((e = colprod(ki, kbi, Ainv))) return e;
+      if (mi <= 0) return QPMS_SUCCESS;
+      if (ke == ge) {  // the group's last block: everything past the group at once
+        if ((e = trailing(ge, k, ge - k, mi, b + 1))) return e;
+        break;
+      }
+      // block i's update of the group's later block columns and rows
+      const int wi = ge - ke;
+      if ((e = tc_split_ab(A + (size_t)ki * lda + ke, lda, mi, kbi, A + (size_t)ke * lda + ki, lda, mi, nsplit, pa,
+                           pb, st)))
         return e;
+      const size_t rs = tc_planes_row(kbi);
+      float2 *C = A + (size_t)ke * lda + ke;
+      TcPlanes Q = P;
+      Q.k = kbi;
+      Q.m = mi, Q.n = wi;  // the later block columns of the group, every row below block i
+      Q.b_plane = (size_t)mi * rs;
+      if ((e = tc_cgemm_planes(Q, -1.f, 1.f, C, lda, C, lda, st))) return e;
+      if (mi > wi) {  // the later block rows of the group, past the group: the first wi rows of the A planes
+        Q.m = wi, Q.a_plane = (size_t)2 * mi * rs;
+        Q.b = pb + (size_t)wi * rs, Q.n = mi - wi;
+        if ((e = tc_cgemm_planes(Q, -1.f, 1.f, C + (size_t)wi * lda, lda, C + (size_t)wi * lda, lda, st))) return e;
+      }
     }
-    float2 *Ainv2 = Dinv + (size_t)(blk + 1) * nb * nb;
-    if ((e = launch_diag<float2>(A22, lda, kb2, Ainv2, dinfo, st))) return e;
-    if ((e = colprod(k2, kb2, Ainv2))) return e;
-    if (m3 <= 0) break;
-    if ((e = trailing(k2 + kb2, k, kb + kb2, m3, blk + 2))) return e;
-    k += kb + kb2;
-    blk += 2;
+    blk += (ge - k + nb - 1) / nb;
+    k = ge;
   }
   return QPMS_SUCCESS;
 }
@@ -765,26 +762,40 @@ int lu_solve_small(int N, int nb, const T *A, size_t lda, T *B, size_t ldb, int 
 
 // ---------------- the same sweeps in one launch each ----------------
 // The two substitutions of lu_solve_small as one launch per sweep, over tiles
-// of kSweepRows rows (nb a multiple of kSweepRows, at most 128).
+// of kSweepRows rows, one warp per tile (nb a multiple of kSweepRows, at most
+// 128):
 //   forward, tile rows r of block j:  b_r <- b_r - sum_{k<j} P_k(r, :) b_k
 //   backward:                          b_r <- b_r - sum_{k>j} Q_k(r, :) b_k,
-// after which the last tile of block j to finish writes the block's solution
-// x_j = b_j - (I - D_j^-1) b_j.  b_k is final once every tile of block k has
-// written its rows (per-block completion counters).  A tile keeps its sums
-// over all k in registers and writes its rows once.
+// then a third launch writes every block's solution x_j = b_j - (I - D_j^-1)
+// b_j (no dependencies left).  b_k is final once every tile of block k has
+// written its rows (per-block completion counters, released after a fence,
+// read with acquire loads; b_k itself is read through L2).  A tile keeps its
+// sums over all k in registers and writes its rows once; the panel entries of
+// step k + 1 are requested before step k's wait.
 // Tiles are handed out in dependency order by an atomic ticket (ascending
 // rows forward, descending backward): a tile only waits for tiles with earlier
-// tickets, which CTAs already running hold, so the waits end whatever number
+// tickets, which warps already running hold, so the waits end whatever number
 // of CTAs is resident (the argument of single-pass decoupled look-back scans).
-// Every wait is bounded (kSweepWaitNs); a wait that runs out sets the error
-// word, which makes the other CTAs leave too.
+// Blocks also finish in sweep order (block k's tiles wait for block k - 1
+// forward, k + 1 backward), so a warp that has seen block k final knows the
+// earlier ones are.  Every wait is bounded (kSweepWaitNs); a wait that runs
+// out sets the error word, which makes the other warps leave too.  Warps are
+// independent (no CTA barrier), and a CTA of 4 warps at about 100 registers
+// fits on an SM beside a tensor-core GEMM CTA.
 // Sync words of one pair of sweeps (sweep_words): [0] error, [1] forward
 // ticket, [2] backward ticket, [3, 3 + nblk) forward block counters,
 // [3 + nblk, 3 + 2 nblk) backward block counters.
-// Thread t of a CTA handles row (t / 32) * 4 + (t % 32) / 8 of the tile and
-// the columns l = t % 8 + 8 q of each block: the eight partial sums of a row
-// sit in eight adjacent lanes and meet by shuffles.
-constexpr int kSweepRows = 32;
+// Lane 8 r + s of a warp handles row r of the tile and the columns
+// l = s + 8 q of each block: the eight partial sums of a row sit in eight
+// adjacent lanes and meet by shuffles; a column's four rows are one 32-byte
+// sector (complex64).
+constexpr int kSweepRows = 4, kSweepThreads = 128;
+// complex64: at most 102 registers, so that a sweep CTA fits on an SM beside a
+// tensor-core GEMM CTA (320 threads x 160 registers)
+template <typename T>
+struct SweepMinCtas {
+  static constexpr int v = sizeof(T) == 8 ? 5 : 2;
+};
 constexpr unsigned long long kSweepWaitNs = 2000000000ull;  // 2 s
 size_t sweep_words(int nblk) { return 3 + 2 * (size_t)nblk; }
 
@@ -804,7 +815,7 @@ __device__ bool sweep_wait(const unsigned *cnt, unsigned need, unsigned *err) {
   if (ld_acquire(cnt) >= need) return true;
   const unsigned long long t0 = sweep_clock();
   for (;;) {
-    __nanosleep(64);
+    __nanosleep(32);
     if (ld_acquire(cnt) >= need) return true;
     if (ld_acquire(err)) return false;
     if (sweep_clock() - t0 > kSweepWaitNs) {
@@ -812,6 +823,28 @@ __device__ bool sweep_wait(const unsigned *cnt, unsigned need, unsigned *err) {
       return false;
     }
   }
+}
+// lane 0 waits, the warp follows (the barrier orders the other lanes' loads
+// after lane 0's acquire)
+__device__ __forceinline__ bool warp_wait(const unsigned *cnt, unsigned need, unsigned *err, int lane) {
+  int ok = 1;
+  if (lane == 0) ok = sweep_wait(cnt, need, err) ? 1 : 0;
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+// lane 0 looks once (no wait): is *cnt >= need?
+__device__ __forceinline__ bool warp_peek(const unsigned *cnt, unsigned need, int lane) {
+  int ok = 0;
+  if (lane == 0) ok = ld_acquire(cnt) >= need ? 1 : 0;
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  __syncwarp();
+  return ok != 0;
+}
+__device__ __forceinline__ int warp_ticket(unsigned *ticket, int lane) {
+  int t = 0;
+  if (lane == 0) t = (int)atomicAdd(ticket, 1u);
+  return __shfl_sync(0xffffffffu, t, 0);
 }
 
 // the 16 entries l = sl + 8 q < kb of one row of a block column (col0: its
@@ -824,27 +857,19 @@ __device__ __forceinline__ void sweep_load(const T *col0, size_t lda, int kb, bo
     pv[q] = (rowok && l < kb) ? col0[(size_t)l * lda] : mk<T>(0, 0);
   }
 }
-// b_k (kb x nrhs from row k0 of B) into shared memory as v[c * 128 + l],
-// through L2 (other CTAs wrote it)
+// acc[c] += sum_l pv[l] b_k(l, c), b_k (kb x nrhs from Bk) read through L2
 template <typename T>
-__device__ __forceinline__ void sweep_stage(T *v, const T *B, size_t ldb, int k0, int kb, int nrhs) {
-  for (int i = threadIdx.x; i < kb * nrhs; i += blockDim.x) {
-    const int c = i / kb, l = i - c * kb;
-    v[c * 128 + l] = __ldcg(B + (size_t)c * ldb + k0 + l);
-  }
-}
-template <typename T>
-__device__ __forceinline__ void sweep_fma(const T (&pv)[16], const T *v, int kb, int nrhs, int sl,
+__device__ __forceinline__ void sweep_fma(const T (&pv)[16], const T *Bk, size_t ldb, int kb, int nrhs, int sl,
                                           T (&acc)[kSmallRhs]) {
 #pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const int l = sl + 8 * q;
-    if (l < kb) {
+  for (int c = 0; c < kSmallRhs; ++c)
+    if (c < nrhs) {
 #pragma unroll
-      for (int c = 0; c < kSmallRhs; ++c)
-        if (c < nrhs) acc[c] = fma_c(acc[c], pv[q], v[c * 128 + l]);
+      for (int q = 0; q < 16; ++q) {
+        const int l = sl + 8 * q;
+        if (l < kb) acc[c] = fma_c(acc[c], pv[q], __ldcg(Bk + (size_t)c * ldb + l));
+      }
     }
-  }
 }
 // sums over the eight lanes of a row (every lane gets the total)
 template <typename T>
@@ -859,136 +884,147 @@ __device__ __forceinline__ void sweep_reduce(T (&acc)[kSmallRhs], int nrhs) {
       }
     }
 }
+// the tile's rows: b_r <- b_r - acc, then the tile is counted in its block
+template <typename T>
+__device__ __forceinline__ void sweep_finish(T *B, size_t ldb, int row, bool rowok, int sl, int nrhs,
+                                             const T (&acc)[kSmallRhs], unsigned *cnt, int lane) {
+  if (sl == 0 && rowok) {
+#pragma unroll
+    for (int c = 0; c < kSmallRhs; ++c)
+      if (c < nrhs) {
+        T *d = B + (size_t)c * ldb + row;
+        *d = sub(__ldcg(d), acc[c]);
+      }
+    __threadfence();
+  }
+  __syncwarp();
+  if (lane == 0) atomicAdd(cnt, 1u);
+}
 
 template <typename T>
-__global__ void __launch_bounds__(256, 2) sweep_fwd_kernel(const T *__restrict__ A, size_t lda, int N, int nb, T *B,
-                                                           size_t ldb, int nrhs, unsigned *sync) {
-  __shared__ T sV[128 * kSmallRhs];
-  __shared__ int s_tile, s_abort;
-  const int tid = threadIdx.x, lane = tid & 31, sl = lane & 7, rr = (tid >> 5) * 4 + (lane >> 3);
+__global__ void __launch_bounds__(kSweepThreads, SweepMinCtas<T>::v) sweep_fwd_kernel(const T *__restrict__ A, size_t lda, int N, int nb,
+                                                                  T *B, size_t ldb, int nrhs, unsigned *sync) {
+  const int lane = threadIdx.x & 31, sl = lane & 7, rr = lane >> 3;
   const int ntiles = (N + kSweepRows - 1) / kSweepRows;
+  const unsigned need = (unsigned)(nb / kSweepRows);  // tiles of a full block
   unsigned *err = sync, *ticket = sync + 1, *cnt = sync + 3;
-  if (tid == 0) s_abort = 0;
+  int known = -1;  // blocks 0..known are final
   for (;;) {
-    if (tid == 0) s_tile = (int)atomicAdd(ticket, 1u);
-    __syncthreads();
-    const int t = s_tile;
+    const int t = warp_ticket(ticket, lane);
     if (t >= ntiles) return;
     const int row0 = t * kSweepRows, j = row0 / nb, row = row0 + rr;
     const bool rowok = row < N;
     T acc[kSmallRhs];
 #pragma unroll
     for (int c = 0; c < kSmallRhs; ++c) acc[c] = mk<T>(0, 0);
+    if (j - 1 > known && warp_peek(cnt + j - 1, need, lane)) known = j - 1;
+    T pv[16];
+    if (j > 0) sweep_load(A + row, lda, nb, rowok, sl, pv);
     for (int k = 0; k < j; ++k) {  // the blocks above are full: kb = nb
-      T pv[16];
-      sweep_load(A + (size_t)k * nb * lda + row, lda, nb, rowok, sl, pv);
-      if (tid == 0 && !sweep_wait(cnt + k, (unsigned)(nb / kSweepRows), err)) s_abort = 1;
-      __syncthreads();  // also: every thread is done with sV of step k - 1
-      if (s_abort) return;
-      sweep_stage(sV, B, ldb, k * nb, nb, nrhs);
-      __syncthreads();
-      sweep_fma(pv, sV, nb, nrhs, sl, acc);
+      T pn[16];
+      if (k + 1 < j) sweep_load(A + (size_t)(k + 1) * nb * lda + row, lda, nb, rowok, sl, pn);
+      if (k > known) {
+        if (!warp_wait(cnt + k, need, err, lane)) return;
+        known = k;
+      }
+      sweep_fma(pv, B + (size_t)k * nb, ldb, nb, nrhs, sl, acc);
+      if (k + 1 < j) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) pv[q] = pn[q];
+      }
     }
     sweep_reduce(acc, nrhs);
-    if (sl == 0 && rowok) {
-#pragma unroll
-      for (int c = 0; c < kSmallRhs; ++c)
-        if (c < nrhs) {
-          T *d = B + (size_t)c * ldb + row;
-          *d = sub(__ldcg(d), acc[c]);
-        }
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) atomicAdd(cnt + j, 1u);
+    sweep_finish(B, ldb, row, rowok, sl, nrhs, acc, cnt + j, lane);
   }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256, 2) sweep_bwd_kernel(const T *__restrict__ A, size_t lda, int N, int nb, T *B,
-                                                           size_t ldb, T *X, size_t ldx, int nrhs, unsigned *sync) {
-  __shared__ T sV[128 * kSmallRhs];
-  __shared__ int s_tile, s_abort, s_last;
-  const int tid = threadIdx.x, lane = tid & 31, sl = lane & 7, rr = (tid >> 5) * 4 + (lane >> 3);
+__global__ void __launch_bounds__(kSweepThreads, SweepMinCtas<T>::v) sweep_bwd_kernel(const T *__restrict__ A, size_t lda, int N, int nb,
+                                                                  T *B, size_t ldb, int nrhs, unsigned *sync) {
+  const int lane = threadIdx.x & 31, sl = lane & 7, rr = lane >> 3;
   const int ntiles = (N + kSweepRows - 1) / kSweepRows, nblk = (N + nb - 1) / nb;
   unsigned *err = sync, *ticket = sync + 2, *cnt = sync + 3 + nblk;
-  if (tid == 0) s_abort = 0;
+  auto need = [&](int k) { return (unsigned)((min(nb, N - k * nb) + kSweepRows - 1) / kSweepRows); };
+  int known = nblk;  // blocks known..nblk-1 are final
   for (;;) {
-    if (tid == 0) s_tile = (int)atomicAdd(ticket, 1u);
-    __syncthreads();
-    const int tk = s_tile;
+    const int tk = warp_ticket(ticket, lane);
     if (tk >= ntiles) return;
     const int t = ntiles - 1 - tk, row0 = t * kSweepRows, j = row0 / nb, row = row0 + rr;
     const bool rowok = row < N;
     T acc[kSmallRhs];
 #pragma unroll
     for (int c = 0; c < kSmallRhs; ++c) acc[c] = mk<T>(0, 0);
+    if (j + 1 < known && j + 1 < nblk && warp_peek(cnt + j + 1, need(j + 1), lane)) known = j + 1;
+    T pv[16];
+    if (j < nblk - 1) sweep_load(A + (size_t)(nblk - 1) * nb * lda + row, lda, N - (nblk - 1) * nb, rowok, sl, pv);
     for (int k = nblk - 1; k > j; --k) {
       const int k0 = k * nb, kb = min(nb, N - k0);
-      T pv[16];
-      sweep_load(A + (size_t)k0 * lda + row, lda, kb, rowok, sl, pv);
-      if (tid == 0 && !sweep_wait(cnt + k, (unsigned)((kb + kSweepRows - 1) / kSweepRows), err)) s_abort = 1;
-      __syncthreads();
-      if (s_abort) return;
-      sweep_stage(sV, B, ldb, k0, kb, nrhs);
-      __syncthreads();
-      sweep_fma(pv, sV, kb, nrhs, sl, acc);
+      T pn[16];
+      if (k - 1 > j) sweep_load(A + (size_t)(k0 - nb) * lda + row, lda, nb, rowok, sl, pn);  // block k - 1 is full
+      if (k < known) {
+        if (!warp_wait(cnt + k, need(k), err, lane)) return;
+        known = k;
+      }
+      sweep_fma(pv, B + k0, ldb, kb, nrhs, sl, acc);
+      if (k - 1 > j) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) pv[q] = pn[q];
+      }
     }
+    sweep_reduce(acc, nrhs);
+    sweep_finish(B, ldb, row, rowok, sl, nrhs, acc, cnt + j, lane);
+  }
+}
+
+// x_j = b_j - (I - D_j^-1) b_j for every block, one warp per tile of rows
+template <typename T>
+__global__ void __launch_bounds__(kSweepThreads) sweep_diag_kernel(const T *__restrict__ A, size_t lda, int N, int nb,
+                                                                   const T *B, size_t ldb, T *X, size_t ldx,
+                                                                   int nrhs) {
+  const int lane = threadIdx.x & 31, sl = lane & 7, rr = lane >> 3;
+  const int ntiles = (N + kSweepRows - 1) / kSweepRows;
+  const int nwarps = (int)(gridDim.x * blockDim.x) >> 5;
+  for (int t = (int)(blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < ntiles; t += nwarps) {
+    const int row0 = t * kSweepRows, j0 = row0 / nb * nb, kbj = min(nb, N - j0), row = row0 + rr;
+    const bool rowok = row < N;
+    T pv[16], acc[kSmallRhs];
+#pragma unroll
+    for (int c = 0; c < kSmallRhs; ++c) acc[c] = mk<T>(0, 0);
+    sweep_load(A + (size_t)j0 * lda + row, lda, kbj, rowok, sl, pv);
+    sweep_fma(pv, B + j0, ldb, kbj, nrhs, sl, acc);
     sweep_reduce(acc, nrhs);
     if (sl == 0 && rowok) {
 #pragma unroll
       for (int c = 0; c < kSmallRhs; ++c)
-        if (c < nrhs) {
-          T *d = B + (size_t)c * ldb + row;
-          *d = sub(__ldcg(d), acc[c]);
-        }
-    }
-    __threadfence();
-    __syncthreads();
-    const int j0 = j * nb, kbj = min(nb, N - j0);
-    if (tid == 0) {
-      s_last = atomicAdd(cnt + j, 1u) == (unsigned)((kbj + kSweepRows - 1) / kSweepRows) - 1;
-      if (s_last) __threadfence();
-    }
-    __syncthreads();
-    if (s_last) {  // every tile of block j is done: x_j = b_j - (I - D_j^-1) b_j
-      sweep_stage(sV, B, ldb, j0, kbj, nrhs);
-      __syncthreads();
-      for (int rs = 0; rs < kbj; rs += kSweepRows) {
-        const int ri = rs + rr;
-        const bool ok = ri < kbj;
-        T pv[16], a2[kSmallRhs];
-#pragma unroll
-        for (int c = 0; c < kSmallRhs; ++c) a2[c] = mk<T>(0, 0);
-        sweep_load(A + (size_t)j0 * lda + j0 + ri, lda, kbj, ok, sl, pv);
-        sweep_fma(pv, sV, kbj, nrhs, sl, a2);
-        sweep_reduce(a2, nrhs);
-        if (sl == 0 && ok) {
-#pragma unroll
-          for (int c = 0; c < kSmallRhs; ++c)
-            if (c < nrhs) X[(size_t)c * ldx + j0 + ri] = sub(sV[c * 128 + ri], a2[c]);
-        }
-      }
+        if (c < nrhs) X[(size_t)c * ldx + row] = sub(B[(size_t)c * ldb + row], acc[c]);
     }
   }
 }
 
-// lu_solve_small's result in two launches.  sync: sweep_words(nblk) words
+// lu_solve_small's result in three launches.  sync: sweep_words(nblk) words
 // whose error word is zero; the others are cleared here.
 template <typename T>
 int lu_solve_sweep(int N, int nb, const T *A, size_t lda, T *B, size_t ldb, int nrhs, T *X, unsigned *sync,
                    cudaStream_t st) {
+  if (nb % kSweepRows || nb > 128) return lu_solve_small<T>(N, nb, A, lda, B, ldb, nrhs, X, st);
   const int nblk = (N + nb - 1) / nb, ntiles = (N + kSweepRows - 1) / kSweepRows;
+  const int wpc = kSweepThreads / 32, ctas = (ntiles + wpc - 1) / wpc;
   int dev = 0, sms = 0;
   QG_CUDA_TRY(cudaGetDevice(&dev));
   QG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int grid = std::min(ntiles, 2 * std::max(sms, 1));
+  sms = std::max(sms, 1);
   QG_CUDA_TRY(cudaMemsetAsync(sync + 1, 0, (sweep_words(nblk) - 1) * sizeof(unsigned), st));
-  sweep_fwd_kernel<T><<<grid, 256, 0, st>>>(A, lda, N, nb, B, ldb, nrhs, sync);
+  // enough warps for a tile each up to the register-limited residency: a
+  // tile's steps are a chain of dependent loads, so the sweep needs warps in
+  // flight, not CTAs that loop
+  const int grid = std::min(ctas, SweepMinCtas<T>::v * sms);
+  sweep_fwd_kernel<T><<<grid, kSweepThreads, 0, st>>>(A, lda, N, nb, B, ldb, nrhs, sync);
   QG_CUDA_TRY(cudaGetLastError());
-  sweep_bwd_kernel<T><<<grid, 256, 0, st>>>(A, lda, N, nb, B, ldb, X, ldb, nrhs, sync);
+  sweep_bwd_kernel<T><<<grid, kSweepThreads, 0, st>>>(A, lda, N, nb, B, ldb, nrhs, sync);
   QG_CUDA_TRY(cudaGetLastError());
-  g_launches.fetch_add(2);
+  sweep_diag_kernel<T><<<std::min(ctas, 8 * sms), kSweepThreads, 0, st>>>(A, lda, N, nb, B, ldb, X, ldb, nrhs);
+  QG_CUDA_TRY(cudaGetLastError());
+  g_launches.fetch_add(3);
   return QPMS_SUCCESS;
 }
 
@@ -1115,9 +1151,10 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
   QG_CUDA_TRY(dev_alloc(&sweep, sweep_bytes));
   QG_CUDA_TRY(cudaMemsetAsync(sweep, 0, sweep_bytes, ast));
   if (tc_split) {
-    // K up to 2 nb: the combined update of a pair of blocks
-    QG_CUDA_TRY(dev_alloc(&tc_pa, tc_planes_bytes_a(Np, 2 * nb, 3)));
-    QG_CUDA_TRY(dev_alloc(&tc_pb, tc_planes_bytes_b(std::max(Np, nrhs_max), 2 * nb, 3)));
+    // K up to group x nb: the combined update of a group of blocks
+    const int kmax = lu_group() * nb;
+    QG_CUDA_TRY(dev_alloc(&tc_pa, tc_planes_bytes_a(Np, kmax, 3)));
+    QG_CUDA_TRY(dev_alloc(&tc_pb, tc_planes_bytes_b(std::max(Np, nrhs_max), kmax, 3)));
     const char *la = getenv("QPMS_GB300_LOOKAHEAD");
     if (lookahead && !(la && !strcmp(la, "0")) && Np > nb) {
       int lo = 0, hi = 0;
@@ -1159,7 +1196,7 @@ size_t DenseSolver::footprint(int N, int nrhs, int mode) {
   b += Np * nrhs * (8 + 16) + (size_t)N * nrhs * 32 + 16 + 4 * Np * 8 + 2 * kOzakiMinRhs * 8;
   b += sweep_words((int)((Np + 63) / 64)) * sizeof(unsigned);
   if (ozaki_wanted(nrhs)) b += ozaki_matrix_bytes(N) + ozaki_work_bytes(N, nrhs);
-  if (mode && tc_digits(nrhs)) b += tc_plane_bytes((int)Np, nrhs, 2 * (int)nb);
+  if (mode && tc_digits(nrhs)) b += tc_plane_bytes((int)Np, nrhs, kMaxLuGroup * (int)nb);
   return b + 13 * 512;  // allocation rounding
 }
 
@@ -1314,7 +1351,7 @@ int DenseSolver::factor_launch(const void *M64, size_t ldm, cudaStream_t st) {
     g_launches.fetch_add(1);
     if (tc_split) {
       e = lu_nopiv_tc(Np, nb, (float2 *)A, Np, (float2 *)Dinv, dinfo, tc_split, (__nv_bfloat16 *)tc_pa,
-                      (__nv_bfloat16 *)tc_pb, st, side, ev_a, ev_d, use_pairs());
+                      (__nv_bfloat16 *)tc_pb, st, side, ev_a, ev_d, lu_group());
     } else {
       e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
                            (cublasComputeType_t)trail_ct, st);
@@ -1353,9 +1390,13 @@ bool DenseSolver::use_sweeps() const {
   static const int v = env_choice("QPMS_GB300_SUBST", "sweep", "steps");
   return v < 0 ? sweeps : v == 1;
 }
-bool DenseSolver::use_pairs() const {
-  static const int v = env_choice("QPMS_GB300_LU_PAIRS", "1", "0");
-  return v < 0 ? pairs : v == 1;
+int DenseSolver::lu_group() const {
+  static const int v = [] {
+    const char *e = getenv("QPMS_GB300_LU_GROUP");
+    const int g = e ? atoi(e) : 0;
+    return g >= 1 && g <= kMaxLuGroup ? g : 0;
+  }();
+  return v ? v : std::max(1, std::min(group, kMaxLuGroup));
 }
 
 int DenseSolver::check_info(cudaStream_t st) {

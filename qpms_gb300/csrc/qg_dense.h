@@ -12,6 +12,8 @@ namespace qg {
 // GEMM; below it the residual is bandwidth-bound on M and the FP64 GEMM is
 // cheaper.  QPMS_GB300_RESIDUAL=ZGEMM turns the digit path off.
 constexpr int kOzakiMinRhs = 8;
+// Largest group of blocks of the tensor-core LU (DenseSolver::group).
+constexpr int kMaxLuGroup = 4;
 bool ozaki_wanted(int nrhs_max);
 
 // The system is padded to Np = N rounded up to a multiple of 4 (identity on the
@@ -73,9 +75,10 @@ struct DenseSolver {
   // SMs that other requests' GEMMs need (QPMS_GB300_SUBST=sweep / steps
   // overrides either way)
   bool sweeps = true;
-  // tensor-core LU by pairs of blocks: one trailing update with K = 2 nb per
-  // pair (QPMS_GB300_LU_PAIRS=1 / 0 overrides either way)
-  bool pairs = true;
+  // tensor-core LU by groups of `group` blocks (1 .. kMaxLuGroup): one
+  // trailing update with K = group x nb per group (QPMS_GB300_LU_GROUP
+  // overrides); set before init(), which sizes the operand planes for it
+  int group = 2;
   // block size of the complex64 LU: 0 = the tuned choice (lu_block_size), else
   // 64 or 128; set before init()
   int nb_pref = 0;
@@ -107,7 +110,7 @@ struct DenseSolver {
   cudaError_t dev_alloc(void *ptr, size_t bytes);
   int check_info(cudaStream_t st);  // zero-pivot flag of the last factorisation
   bool use_sweeps() const;
-  bool use_pairs() const;
+  int lu_group() const;
   int factor_launch(const void *M64, size_t ldm, cudaStream_t st);  // factorize_current's launches
   int apply_launch(const void *R, size_t ldr, void *Y, size_t ldy, int nrhs, cudaStream_t st);
   template <class F>

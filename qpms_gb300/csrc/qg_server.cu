@@ -332,9 +332,13 @@ struct qpms_gpu_server {
     // with the single-solve tuning's 64-wide blocks below 6144 unknowns)
     ds.nb_pref = 128;
     // and the substitutions as one launch per block and sweep: the one-launch
-    // sweeps' waiting CTAs hold SMs the other requests' GEMMs need (121.0 /
-    // 121.3 solves/s with them, 123.4 without, 8 workers)
+    // sweeps' waiting warps hold SM slots the other requests' kernels could
+    // use (135.4 / 135.6 solves/s with them, 138.2 / 137.7 without, 8 workers)
     ds.sweeps = nworkers == 1;
+    // and groups of 3 blocks in the LU: without the lookahead the in-group
+    // inversions cost nothing extra here (136.0 / 137.0 solves/s with pairs,
+    // 138.1 with groups of 3, 138.2 / 137.0 with groups of 4)
+    ds.group = nworkers == 1 ? 2 : 3;
     if ((e = ds.init((int)N, 1, mode, 0x5eed ^ j->id, pool, st))) return e;
     if ((e = ds.factorize(dM, N, st, true))) return e;
     if ((e = ds.solve(dM, N, db, dx, 1, kRefineTol, kMaxRefine, &res, &it, st))) return e;
