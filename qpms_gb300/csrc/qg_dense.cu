@@ -637,24 +637,43 @@ int lu_nopiv_tc(int N, int nb, float2 *A, size_t lda, float2 *Dinv, int *dinfo, 
 }
 
 // lu_solve's substitutions with the products on the tensor cores (in place).
+// fp: nsplit digit planes of the whole factored matrix (tc_split_a of the
+// N x N factors), or null.  With them each step cuts only its right-hand-side
+// block into digits and reads its panel's planes in place (row length
+// tc_planes_row(N)); without them each step cuts its panel too.
 int lu_solve_tc(int N, int nb, const float2 *A, size_t lda, float2 *B, size_t ldb, int nrhs, int nsplit,
-                __nv_bfloat16 *pa, __nv_bfloat16 *pb, cudaStream_t st) {
+                __nv_bfloat16 *pa, __nv_bfloat16 *pb, const __nv_bfloat16 *fp, cudaStream_t st) {
   TcPlanes P;
   P.a = pa;
   P.b = pb;
   P.nsplit = nsplit;
+  const size_t frs = tc_planes_row(N);
+  if (fp) {
+    P.a_rs = frs;
+    P.a_plane = (size_t)2 * N * frs;
+  }
   int e;
   const int nblk = (N + nb - 1) / nb;
   for (int blk = 0; blk < nblk; ++blk) {
     const int k = blk * nb, kb = (N - k < nb) ? N - k : nb, m2 = N - k - kb;
     if (m2 <= 0) continue;
-    if ((e = tc_split_ab(A + (size_t)k * lda + k + kb, lda, m2, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
+    if (fp) {
+      if ((e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st))) return e;
+      P.a = const_cast<__nv_bfloat16 *>(fp) + (size_t)2 * (k + kb) * frs + 2 * (size_t)k;
+    } else if ((e = tc_split_ab(A + (size_t)k * lda + k + kb, lda, m2, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) {
+      return e;
+    }
     P.m = m2, P.n = nrhs, P.k = kb;
     if ((e = tc_cgemm_planes(P, -1.f, 1.f, B + k + kb, ldb, B + k + kb, ldb, st))) return e;
   }
   for (int blk = nblk - 1; blk >= 0; --blk) {
     const int k = blk * nb, kb = (N - k < nb) ? N - k : nb;
-    if ((e = tc_split_ab(A + (size_t)k * lda, lda, k + kb, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) return e;
+    if (fp) {
+      if ((e = tc_split_b(B + k, ldb, kb, nrhs, nsplit, pb, st))) return e;
+      P.a = const_cast<__nv_bfloat16 *>(fp) + 2 * (size_t)k;
+    } else if ((e = tc_split_ab(A + (size_t)k * lda, lda, k + kb, kb, B + k, ldb, nrhs, nsplit, pa, pb, st))) {
+      return e;
+    }
     P.m = k + kb, P.n = nrhs, P.k = kb;
     if ((e = tc_cgemm_planes(P, -1.f, 1.f, B, ldb, B, ldb, st))) return e;
   }
@@ -1164,6 +1183,15 @@ int DenseSolver::init(int N_, int nrhs_max_, int mode_, unsigned long long seed,
       QG_CUDA_TRY(cudaEventCreateWithFlags(&ev_d, cudaEventDisableTiming));
     }
   }
+  // many right-hand sides on the tensor cores: the factors' digit planes, cut
+  // once per factorisation instead of per substitution step (skipped when
+  // they do not fit: the steps then cut their panels themselves)
+  if (tc_split && nrhs_max > kSmallRhs && fac_planes_wanted()) {
+    if (dev_alloc(&fac_planes, tc_planes_bytes_a(Np, Np, 3)) != cudaSuccess) {
+      cudaGetLastError();
+      fac_planes = nullptr;
+    }
+  }
   use_ozaki = ozaki_wanted(nrhs_max);
   if (use_ozaki && (dev_alloc(&oz_mat, ozaki_matrix_bytes(N)) != cudaSuccess ||
                     dev_alloc(&oz_work, ozaki_work_bytes(N, nrhs_max)) != cudaSuccess)) {
@@ -1197,7 +1225,13 @@ size_t DenseSolver::footprint(int N, int nrhs, int mode) {
   b += sweep_words((int)((Np + 63) / 64)) * sizeof(unsigned);
   if (ozaki_wanted(nrhs)) b += ozaki_matrix_bytes(N) + ozaki_work_bytes(N, nrhs);
   if (mode && tc_digits(nrhs)) b += tc_plane_bytes((int)Np, nrhs, kMaxLuGroup * (int)nb);
+  if (mode && tc_digits(nrhs) && nrhs > kSmallRhs && fac_planes_wanted()) b += tc_planes_bytes_a((int)Np, (int)Np, 3);
   return b + 13 * 512;  // allocation rounding
+}
+
+bool fac_planes_wanted() {
+  static const int v = env_choice("QPMS_GB300_FACTOR_PLANES", "1", "0");
+  return v != 0;
 }
 
 bool ozaki_wanted(int nrhs_max) {
@@ -1215,7 +1249,7 @@ void DenseSolver::release() {
   if (side) cudaStreamSynchronize(side);  // its last inversion reads buffers freed below
   for (void *p : {(void *)A, (void *)T64, (void *)Dinv, (void *)work, (void *)rhs_lo, (void *)rp, (void *)r64,
                   (void *)y64, (void *)dinfo, (void *)rs, (void *)res_nrm, (void *)sweep, oz_mat, oz_work, tc_pa,
-                  tc_pb})
+                  tc_pb, fac_planes})
     if (p) {
       if (pool)
         cudaFreeAsync(p, ast);
@@ -1239,6 +1273,7 @@ void DenseSolver::release() {
   sweep = nullptr;
   oz_mat = oz_work = nullptr;
   tc_pa = tc_pb = nullptr;
+  fac_planes = nullptr;
   use_ozaki = false;
 }
 
@@ -1352,6 +1387,8 @@ int DenseSolver::factor_launch(const void *M64, size_t ldm, cudaStream_t st) {
     if (tc_split) {
       e = lu_nopiv_tc(Np, nb, (float2 *)A, Np, (float2 *)Dinv, dinfo, tc_split, (__nv_bfloat16 *)tc_pa,
                       (__nv_bfloat16 *)tc_pb, st, side, ev_a, ev_d, lu_group());
+      // the substitutions' panels as 3-digit planes, cut once per factorisation
+      if (!e && fac_planes) e = tc_split_a((const float2 *)A, Np, Np, Np, 3, (__nv_bfloat16 *)fac_planes, st);
     } else {
       e = lu_nopiv<float2>(h, Np, nb, (float2 *)A, Np, (float2 *)Dinv, (float2 *)work, dinfo,
                            (cublasComputeType_t)trail_ct, st);
@@ -1442,7 +1479,7 @@ int DenseSolver::apply_launch(const void *R, size_t ldr, void *Y, size_t ldy, in
       sol = (const float2 *)work;
     } else if (tc_split) {
       e = lu_solve_tc(Np, nb, (const float2 *)A, Np, (float2 *)rhs_lo, Np, nrhs, 3, (__nv_bfloat16 *)tc_pa,
-                      (__nv_bfloat16 *)tc_pb, st);
+                      (__nv_bfloat16 *)tc_pb, (const __nv_bfloat16 *)fac_planes, st);
     } else {
       e = lu_solve<float2>(h, Np, nb, (const float2 *)A, Np, (float2 *)rhs_lo, Np, nrhs, (float2 *)work,
                            CUBLAS_COMPUTE_32F, st);

@@ -15,6 +15,9 @@ constexpr int kOzakiMinRhs = 8;
 // Largest group of blocks of the tensor-core LU (DenseSolver::group).
 constexpr int kMaxLuGroup = 4;
 bool ozaki_wanted(int nrhs_max);
+// Whether a solver for many right-hand sides keeps the digit planes of its
+// factors (QPMS_GB300_FACTOR_PLANES=0 turns it off).
+bool fac_planes_wanted();
 
 // The system is padded to Np = N rounded up to a multiple of 4 (identity on the
 // padding), the size the two butterfly levels halve.
@@ -42,6 +45,7 @@ struct DenseSolver {
   int tc_split = 0;        // mode 1 on the tensor cores: bf16 digits per operand (2 or 3); 0: cuBLAS
   int base_tc = 0;
   void *tc_pa = nullptr, *tc_pb = nullptr;  // digit planes of the GEMM operands
+  void *fac_planes = nullptr;  // 3-digit planes of the whole factored matrix (many right-hand sides)
   int refactors = 0;       // refinement stalls answered by more precise factors
   int base_mode = 0, base_trail = 0;  // what factorize() starts from (the fallbacks change mode / trail_ct)
   // digit slices of M for the tensor-core residual (nrhs_max >= kOzakiMinRhs)

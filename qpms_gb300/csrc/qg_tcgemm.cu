@@ -686,8 +686,8 @@ int tc_cgemm_planes(const TcPlanes &P, float alpha, float beta, const float2 *C,
   if (P.k <= 0) {  // empty product: D = beta C
     g.alpha = 0.f;
   }
-  const size_t rs = rs_of(P.k);
-  return dispatch(P.a, 2 * P.k, 2 * P.m, P.nsplit, rs, P.a_plane ? P.a_plane : (size_t)2 * P.m * rs, P.b, P.n,
+  const size_t rs = rs_of(P.k), ars = P.a_rs ? P.a_rs : rs;
+  return dispatch(P.a, 2 * P.k, 2 * P.m, P.nsplit, ars, P.a_plane ? P.a_plane : (size_t)2 * P.m * ars, P.b, P.n,
                   P.nsplit, rs, P.b_plane ? P.b_plane : (size_t)P.n * rs, g, st);
 }
 

@@ -20,6 +20,10 @@ struct TcPlanes {
   // exactly (m, n, k) (2m rows of A, n rows of B).  Set to use a block of
   // rows of larger planes (a / b then point at the first row of the block).
   size_t a_plane = 0, b_plane = 0;
+  // Row length of the A planes in elements; 0: tc_planes_row(k).  Set to use
+  // a block of columns of planes cut for a larger k (a then points at the
+  // block's first element; its column offset a multiple of 8 elements).
+  size_t a_rs = 0;
 };
 
 // Row length (elements) of the digit planes for inner dimension k.

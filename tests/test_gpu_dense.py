@@ -113,3 +113,41 @@ def test_one_application_of_the_sweeps(torch_cuda, nrhs):
             assert np.linalg.norm(X - ref) <= 1e-11 * np.linalg.norm(ref), rep
     finally:
         L.qpms_gpu_testing_set_max_refine(-1)
+
+
+_PLANES_CHILD = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+import qpms_gb300
+N, nrhs = 1500, 24
+rng = np.random.default_rng(7)
+M = (rng.normal(size=(N, N)) + 1j * rng.normal(size=(N, N))) / np.sqrt(N) + 2 * np.eye(N)
+B = rng.normal(size=(N, nrhs)) + 1j * rng.normal(size=(N, nrhs))
+dev = torch.device("cuda:0")
+tM = torch.from_numpy(np.asfortranarray(M).reshape(-1, order="F")).to(dev)
+tB = torch.from_numpy(np.asfortranarray(B).reshape(-1, order="F")).to(dev)
+tX = torch.empty_like(tB)
+res, it = np.zeros(1), np.zeros(1, dtype=np.int32)
+rc = qpms_gb300.lib().qpms_gpu_dense_solve(N, nrhs, tM.data_ptr(), tB.data_ptr(), tX.data_ptr(), 1,
+                                           res.ctypes.data, it.ctypes.data)
+assert rc == 0, qpms_gb300.last_error()
+np.save(sys.argv[2], tX.cpu().numpy())
+"""
+
+
+def test_factor_planes_match_per_step_splits(torch_cuda, tmp_path):
+    """Many right-hand sides: the substitutions reading the factors' digit
+    planes cut once per factorisation give bit-for-bit the result of cutting
+    each step's panel (the same elementwise digits, the same products), in a
+    child process with the cached planes off (QPMS_GB300_FACTOR_PLANES=0)."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = {}
+    for flag in ("1", "0"):
+        env = dict(os.environ, QPMS_GB300_FACTOR_PLANES=flag)
+        f = str(tmp_path / ("x%s.npy" % flag))
+        subprocess.run([sys.executable, "-c", _PLANES_CHILD, root, f], env=env, check=True, timeout=600)
+        out[flag] = np.load(f)
+    assert np.array_equal(out["1"], out["0"])
