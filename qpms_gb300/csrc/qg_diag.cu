@@ -1,5 +1,5 @@
 // Diagnostics: an FP64 FMA throughput probe used as the FP64-pipe roofline
-// denominator (the measured peaks cover HBM copy and bf16 GEMM only).
+// denominator (the measured-peaks file covers HBM copy and bf16 GEMM only).
 #include "qg_internal.h"
 
 namespace qg {

@@ -464,7 +464,7 @@ int encode_fn(PFN_cuTensorMapEncodeTiled_v12000 *out) {
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
   });
   if (!g_encode) {
-    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    set_error("cuTensorMapEncodeTiled is not available from the CUDA driver API");
     return QPMS_ERROR;
   }
   *out = g_encode;
