@@ -237,32 +237,41 @@ __global__ void split_rhs_kernel(const double2 *__restrict__ X, int N, size_t N8
          [&](int j, __nv_bfloat16 d) { bsl[j * w + (size_t)(nrhs + c) * N8 + k] = d; });
 }
 
-// P[R, C] (+)= sum_{j <= p-1-i} 2^{-s (i+j+2)} G[R, j 2nrhs + C], j descending
-// (smallest terms first); G = D_i [E_0 | ... ] exact in FP32.
-__global__ void accumulate_kernel(const float *__restrict__ G, int twoN, int twonrhs, int i, int s, int p,
-                                  bool first, double *P) {
-  const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= (size_t)twoN * twonrhs) return;
-  const int C = (int)(idx / twoN), R = (int)(idx % twoN);
-  double acc = 0;
-  for (int j = p - 1 - i; j >= 0; --j)
-    acc += ldexp((double)G[(size_t)(j * twonrhs + C) * twoN + R], -s * (i + j + 2));
-  P[idx] = first ? acc : P[idx] + acc;
+// Digit products of equal total weight summed exactly: for the products of
+// digit i of M with digits j = 0..p-1-i of X (G = D_i [E_0 | ... ], exact
+// integers in FP32, |G| < 2^24), H[t][e] (+)= G[j][e] with t = i + j.  A
+// weight t gets at most p terms, so |H| < p 2^24 fits int32 exactly.  The
+// calls run i = p-1 .. 0, so weight t is first reached at i = t (j = 0),
+// which writes instead of adding (no clearing pass).  cnt = 2N x 2nrhs.
+__global__ void accumulate_kernel(const float *__restrict__ G, size_t cnt, int i, int p, int *__restrict__ H) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= cnt) return;
+  H[(size_t)i * cnt + e] = __float2int_rn(G[e]);
+  for (int j = 1; j <= p - 1 - i; ++j) H[(size_t)(i + j) * cnt + e] += __float2int_rn(G[(size_t)j * cnt + e]);
 }
 
-// R = B - M X from P = [Re M; Im M] [Re X, Im X] (unscaled digits sums).
-__global__ void combine_kernel(const double *__restrict__ P, const double *__restrict__ sigma,
+// sum_t H[t][e] 2^{-s (t + 2)}, smallest weights first (exact powers of two
+// built from their exponent bits)
+__device__ __forceinline__ double digit_sum(const int *__restrict__ H, size_t cnt, size_t e, int s, int p) {
+  double acc = 0;
+  for (int t = p - 1; t >= 0; --t)
+    acc = fma((double)H[(size_t)t * cnt + e], __hiloint2double((1023 - s * (t + 2)) << 20, 0), acc);
+  return acc;
+}
+
+// R = B - M X from H, the digit sums of [Re M; Im M] [Re X, Im X] (unscaled).
+__global__ void combine_kernel(const int *__restrict__ H, int s, int p, const double *__restrict__ sigma,
                                const double *__restrict__ tau, int N, int nrhs, const double2 *__restrict__ B,
                                double2 *__restrict__ Rout) {
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (size_t)N * nrhs) return;
   const int c = (int)(idx / N), r = (int)(idx % N);
-  const size_t twoN = 2 * (size_t)N;
+  const size_t twoN = 2 * (size_t)N, cnt = twoN * 2 * nrhs;
   const double sr = sigma[r], si = sigma[N + r], tr = tau[c], ti = tau[nrhs + c];
-  const double pRR = P[(size_t)c * twoN + r] * sr * tr;
-  const double pII = P[(size_t)(nrhs + c) * twoN + N + r] * si * ti;
-  const double pRI = P[(size_t)(nrhs + c) * twoN + r] * sr * ti;
-  const double pIR = P[(size_t)c * twoN + N + r] * si * tr;
+  const double pRR = digit_sum(H, cnt, (size_t)c * twoN + r, s, p) * sr * tr;
+  const double pII = digit_sum(H, cnt, (size_t)(nrhs + c) * twoN + N + r, s, p) * si * ti;
+  const double pRI = digit_sum(H, cnt, (size_t)(nrhs + c) * twoN + r, s, p) * sr * ti;
+  const double pIR = digit_sum(H, cnt, (size_t)c * twoN + N + r, s, p) * si * tr;
   const double2 b = B[idx];
   Rout[idx] = make_double2(b.x - (pRR - pII), b.y - (pRI + pIR));
 }
@@ -291,8 +300,7 @@ size_t ozaki_work_bytes(int N, int nrhs) {
   int s, p;
   ozaki_digits(N, &s, &p);
   const size_t tn = 2 * (size_t)nrhs;
-  return al256((size_t)p * n8(N) * tn * 2) + al256(tn * 8) + al256((size_t)2 * N * tn * p * 4) +
-         al256((size_t)2 * N * tn * 8);
+  return al256((size_t)p * n8(N) * tn * 2) + al256(tn * 8) + 2 * al256((size_t)2 * N * tn * p * 4);
 }
 
 int ozaki_split_matrix(const void *M, size_t ldm, bool row_major, int N, void *buf, OzakiMatrix *om,
@@ -344,7 +352,7 @@ int ozaki_residual(const OzakiMatrix &om, const void *X, const void *B, void *R,
   w += al256((size_t)tn * 8);
   float *G = (float *)w;
   w += al256((size_t)twoN * tn * p * 4);
-  double *P = (double *)w;
+  int *H = (int *)w;  // [p][2N x 2nrhs]
   colmax_kernel<<<tn, 256, 0, st>>>((const double2 *)X, N, nrhs, tau);
   QG_CUDA_TRY(cudaGetLastError());
   split_rhs_kernel<<<grid1((size_t)N * nrhs), 256, 0, st>>>((const double2 *)X, N, ld, nrhs, tau, s, p, bsl);
@@ -355,11 +363,11 @@ int ozaki_residual(const OzakiMatrix &om, const void *X, const void *B, void *R,
     const int n = tn * (p - i);
     const __nv_bfloat16 *Ai = (const __nv_bfloat16 *)om.slices + (size_t)i * twoN * ld;
     if ((e = tc_gemm_bf16(Ai, ld, bsl, ld, twoN, n, N, 1.f, 0.f, nullptr, 0, G, twoN, st))) return e;
-    accumulate_kernel<<<grid1((size_t)twoN * tn), 256, 0, st>>>(G, twoN, tn, i, s, p, i == p - 1, P);
+    accumulate_kernel<<<grid1((size_t)twoN * tn), 256, 0, st>>>(G, (size_t)twoN * tn, i, p, H);
     QG_CUDA_TRY(cudaGetLastError());
     g_launches.fetch_add(1);
   }
-  combine_kernel<<<grid1((size_t)N * nrhs), 256, 0, st>>>(P, om.scale, tau, N, nrhs, (const double2 *)B,
+  combine_kernel<<<grid1((size_t)N * nrhs), 256, 0, st>>>(H, s, p, om.scale, tau, N, nrhs, (const double2 *)B,
                                                           (double2 *)R);
   QG_CUDA_TRY(cudaGetLastError());
   g_launches.fetch_add(1);
